@@ -1,0 +1,138 @@
+"""ctypes binding of the C ABI in include/gx_eval.h (libgxeval.so).
+
+The library is built in-tree by ``blazingsql_gb300.build_ext.build()``.  There
+is no CPU fallback: if the library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgxeval.so")
+
+GX_OK = 0
+GX_ERR_PARSE = 1
+GX_ERR_UNSUPPORTED = 2
+GX_ERR_TYPE = 3
+GX_ERR_OOM = 4
+GX_ERR_CUDA = 5
+GX_ERR_TIMEOUT = 6
+GX_ERR_INVALID = 7
+GX_ERR_CAPACITY = 8
+
+GX_FILTER_AUTO = 0
+GX_FILTER_TWO_PASS = 1
+GX_FILTER_SINGLE_PASS = 2
+
+
+class GxError(RuntimeError):
+    """A non-OK status from the evaluator; ``code`` is the gx_status value."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[gx status {code}] {message}")
+        self.code = code
+        self.message = message
+
+    @property
+    def retryable(self) -> bool:
+        return self.code == GX_ERR_OOM
+
+
+class ColumnView(C.Structure):
+    _fields_ = [("type_id", C.c_int32), ("reserved", C.c_int32), ("data", C.c_void_p),
+                ("null_mask", C.c_void_p), ("offset", C.c_int64), ("size", C.c_int64)]
+
+
+class Column(C.Structure):
+    _fields_ = [("type_id", C.c_int32), ("reserved", C.c_int32), ("data", C.c_void_p),
+                ("null_mask", C.c_void_p), ("size", C.c_int64), ("capacity", C.c_int64)]
+
+
+class StatusInfo(C.Structure):
+    _fields_ = [("code", C.c_int32), ("message", C.c_char * 500)]
+
+
+class PlanOptions(C.Structure):
+    _fields_ = [("filter_mode", C.c_int32), ("block_threads", C.c_int32), ("words_per_warp", C.c_int32),
+                ("use_tma", C.c_int32), ("short_circuit", C.c_int32), ("num_conjuncts", C.c_int32),
+                ("conjunct_order", C.c_int32 * 16), ("rand_seed", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libgxeval.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"native evaluator library missing ({LIB_PATH}); build it with "
+                           "blazingsql_gb300.build_ext.build() -- there is no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    L.gx_version.restype = C.c_char_p
+    L.gx_evaluate_expressions.argtypes = [P(ColumnView), C.c_int, P(C.c_char_p), C.c_int, P(Column), C.c_void_p,
+                                          P(StatusInfo)]
+    L.gx_process_project.argtypes = [P(ColumnView), C.c_int, C.c_char_p, P(Column), C.c_int, P(C.c_int),
+                                     C.c_char_p, C.c_int, C.c_void_p, P(StatusInfo)]
+    L.gx_process_filter.argtypes = [P(ColumnView), C.c_int, C.c_char_p, P(Column), P(C.c_int64), C.c_void_p,
+                                    P(StatusInfo)]
+    L.gx_filter_project.argtypes = [P(ColumnView), C.c_int, C.c_char_p, P(C.c_char_p), C.c_int, P(Column),
+                                    P(C.c_int64), C.c_void_p, P(StatusInfo)]
+    L.gx_free_columns.argtypes = [P(Column), C.c_int, C.c_void_p]
+    L.gx_free_columns.restype = None
+    L.gx_column_to_host.argtypes = [P(Column), C.c_void_p, C.c_void_p, C.c_void_p, P(StatusInfo)]
+    L.gx_plan_options_init.argtypes = [P(PlanOptions)]
+    L.gx_plan_options_init.restype = None
+    L.gx_plan_compile.argtypes = [P(C.c_int32), P(C.c_uint8), C.c_int, C.c_char_p, P(C.c_char_p), C.c_int,
+                                  P(PlanOptions), P(StatusInfo)]
+    L.gx_plan_compile.restype = C.c_void_p
+    L.gx_plan_num_outputs.argtypes = [C.c_void_p]
+    L.gx_plan_output_type.argtypes = [C.c_void_p, C.c_int]
+    L.gx_plan_output_type.restype = C.c_int32
+    L.gx_plan_num_conjuncts.argtypes = [C.c_void_p]
+    L.gx_plan_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
+                                  P(StatusInfo)]
+    L.gx_plan_destroy.argtypes = [C.c_void_p]
+    L.gx_plan_destroy.restype = None
+    L.gx_debug_kernel_source.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), C.c_char_p, C.c_int64, P(StatusInfo)]
+    L.gx_debug_kernel_source.restype = C.c_int64
+    L.gx_debug_compile_check.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(StatusInfo)]
+    L.gx_debug_fail_allocation.argtypes = [C.c_int]
+    L.gx_debug_fail_allocation.restype = None
+    L.gx_debug_jit_stats.argtypes = [P(C.c_int64), P(C.c_double)]
+    L.gx_debug_jit_stats.restype = None
+    L.gx_debug_rebuild_expression.argtypes = [C.c_char_p, C.c_char_p, C.c_int, P(StatusInfo)]
+    L.gx_debug_set_kernel_timing.argtypes = [C.c_int]
+    L.gx_debug_set_kernel_timing.restype = None
+    L.gx_debug_kernel_ms.argtypes = [C.c_int]
+    L.gx_debug_kernel_ms.restype = C.c_double
+    L.gx_debug_launch_count.argtypes = []
+    L.gx_debug_launch_count.restype = C.c_int64
+    _lib = L
+    return L
+
+
+def check(rc: int, st: StatusInfo) -> None:
+    if rc != GX_OK:
+        raise GxError(rc, st.message.decode(errors="replace"))
+
+
+# every symbol declared in include/gx_eval.h
+EXPORTED_SYMBOLS = [
+    "gx_evaluate_expressions", "gx_process_project", "gx_process_filter", "gx_filter_project", "gx_free_columns",
+    "gx_column_to_host", "gx_plan_options_init", "gx_plan_compile", "gx_plan_num_outputs", "gx_plan_output_type",
+    "gx_plan_num_conjuncts", "gx_plan_execute", "gx_plan_destroy", "gx_version", "gx_debug_kernel_source",
+    "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
+    "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
+]
+
+
+def rebuild_expression(expr: str) -> str:
+    """The product parser's lowered form of one expression, as text."""
+    buf = C.create_string_buffer(8192)
+    st = StatusInfo()
+    check(lib().gx_debug_rebuild_expression(expr.encode(), buf, 8192, C.byref(st)), st)
+    return buf.value.decode()

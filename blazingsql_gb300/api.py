@@ -1,0 +1,301 @@
+"""Host-side mirror of BlazingSQL's evaluator interface over the C ABI.
+
+Names and argument meaning follow the reference:
+``evaluate_expressions(table, expressions)`` (LogicalProject.cpp:796),
+``process_project(table, query_part)`` (LogicalProject.cpp:943) and
+``process_filter(table, query_part)`` (LogicalFilter.cpp:31).  Errors surface
+as :class:`GxError` with the C status code (``retryable`` for OOM, as the
+reference maps ``rmm::bad_alloc`` to a retry).
+
+Device memory for inputs is held by torch tensors (plain device buffers);
+outputs are owned by the native library and released when the returned
+:class:`NativeColumn` objects are garbage collected.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _native as N
+from .types import HostColumn, TypeId, np_dtype
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required (the evaluator has no CPU path)")
+    return torch
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        torch = _torch()
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+@dataclass
+class DeviceColumn:
+    """A borrowed device column: raw byte tensors for data and validity words."""
+    type_id: int
+    data: object                  # torch.uint8 tensor on the device
+    mask: Optional[object]        # torch.uint8 tensor (uint32 words) or None
+    offset: int
+    size: int
+
+    @staticmethod
+    def from_host(col: HostColumn, device: str = "cuda") -> "DeviceColumn":
+        torch = _torch()
+        raw = np.ascontiguousarray(col.data).view(np.uint8)
+        data = torch.from_numpy(raw.copy()).to(device) if raw.size else torch.zeros(64, dtype=torch.uint8,
+                                                                                      device=device)
+        mask = None
+        if col.mask is not None:
+            mask = torch.from_numpy(np.ascontiguousarray(col.mask).view(np.uint8).copy()).to(device)
+        return DeviceColumn(col.type_id, data, mask, col.offset, col.size)
+
+    def view(self) -> N.ColumnView:
+        v = N.ColumnView()
+        v.type_id = self.type_id
+        v.data = self.data.data_ptr()
+        v.null_mask = self.mask.data_ptr() if self.mask is not None else None
+        v.offset = self.offset
+        v.size = self.size
+        return v
+
+
+class NativeColumn:
+    """An output column owned by the native library."""
+
+    def __init__(self, col: N.Column, stream: int = 0):
+        self._c = col
+        self._stream = stream
+
+    @property
+    def type_id(self) -> int:
+        return self._c.type_id
+
+    @property
+    def size(self) -> int:
+        return self._c.size
+
+    @property
+    def data_ptr(self) -> int:
+        return self._c.data or 0
+
+    @property
+    def mask_ptr(self) -> int:
+        return self._c.null_mask or 0
+
+    def view(self) -> N.ColumnView:
+        v = N.ColumnView()
+        v.type_id, v.data, v.null_mask, v.offset, v.size = self._c.type_id, self._c.data, self._c.null_mask, 0, \
+            self._c.size
+        return v
+
+    def to_host(self) -> HostColumn:
+        dt = np_dtype(self.type_id)
+        data = np.empty(max(self.size, 1), dtype=dt)
+        nwords = max(16, ((self.size + 31) // 32 + 15) // 16 * 16)
+        mask = np.zeros(nwords, dtype=np.uint32)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_column_to_host(C.byref(self._c), data.ctypes.data, mask.ctypes.data, self._stream,
+                                          C.byref(st)), st)
+        return HostColumn(self.type_id, data[:self.size], mask)
+
+    def free(self):
+        if self._c.data:
+            N.lib().gx_free_columns(C.byref(self._c), 1, self._stream)
+            self._c.data = None
+            self._c.null_mask = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+Table = Sequence[Union[DeviceColumn, HostColumn, NativeColumn]]
+
+
+def _views(table: Table, keep: list):
+    cols = []
+    for c in table:
+        if isinstance(c, HostColumn):
+            c = DeviceColumn.from_host(c)
+        keep.append(c)
+        cols.append(c.view())
+    arr = (N.ColumnView * max(1, len(cols)))(*cols)
+    return arr, len(cols)
+
+
+def _wrap(outs, n: int, stream: int) -> List[NativeColumn]:
+    return [NativeColumn(N.Column(outs[i].type_id, 0, outs[i].data, outs[i].null_mask, outs[i].size,
+                                  outs[i].capacity), stream) for i in range(n)]
+
+
+def evaluate_expressions(table: Table, expressions: Sequence[str], stream=None) -> List[NativeColumn]:
+    """ral::processor::evaluate_expressions: one output column per expression."""
+    keep: list = []
+    views, nc = _views(table, keep)
+    s = _stream_handle(stream)
+    ex = (C.c_char_p * max(1, len(expressions)))(*[e.encode() for e in expressions])
+    outs = (N.Column * max(1, len(expressions)))()
+    st = N.StatusInfo()
+    N.check(N.lib().gx_evaluate_expressions(views, nc, ex, len(expressions), outs, s, C.byref(st)), st)
+    return _wrap(outs, len(expressions), s)
+
+
+def process_project(table: Table, query_part: str, stream=None) -> Tuple[List[NativeColumn], List[str]]:
+    """ral::processor::process_project on a LogicalProject(...) text."""
+    keep: list = []
+    views, nc = _views(table, keep)
+    s = _stream_handle(stream)
+    max_out = 256
+    outs = (N.Column * max_out)()
+    names = C.create_string_buffer(max_out * 128)
+    nout = C.c_int(0)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_process_project(views, nc, query_part.encode(), outs, max_out, C.byref(nout), names, 128, s,
+                                       C.byref(st)), st)
+    raw = names.raw
+    out_names = [raw[i * 128:(i + 1) * 128].split(b"\0", 1)[0].decode() for i in range(nout.value)]
+    return _wrap(outs, nout.value, s), out_names
+
+
+def process_filter(table: Table, query_part: str, stream=None) -> List[NativeColumn]:
+    """ral::processor::process_filter on a LogicalFilter(condition=[...]) text."""
+    keep: list = []
+    views, nc = _views(table, keep)
+    s = _stream_handle(stream)
+    outs = (N.Column * max(1, nc))()
+    rows = C.c_int64(0)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_process_filter(views, nc, query_part.encode(), outs, C.byref(rows), s, C.byref(st)), st)
+    return _wrap(outs, nc, s)
+
+
+def filter_project(table: Table, condition: Optional[str], expressions: Sequence[str],
+                   stream=None) -> List[NativeColumn]:
+    """process_project(process_filter(table, condition), expressions) in one device pass."""
+    keep: list = []
+    views, nc = _views(table, keep)
+    s = _stream_handle(stream)
+    ex = (C.c_char_p * len(expressions))(*[e.encode() for e in expressions])
+    outs = (N.Column * len(expressions))()
+    rows = C.c_int64(0)
+    st = N.StatusInfo()
+    cond = condition.encode() if condition else None
+    N.check(N.lib().gx_filter_project(views, nc, cond, ex, len(expressions), outs, C.byref(rows), s, C.byref(st)),
+            st)
+    return _wrap(outs, len(expressions), s)
+
+
+class Plan:
+    """A compiled filter+project plan (gx_plan_compile / gx_plan_execute)."""
+
+    def __init__(self, schema: Sequence[int], condition: Optional[str], expressions: Sequence[str],
+                 nullable: Optional[Sequence[bool]] = None, filter_mode: int = N.GX_FILTER_AUTO,
+                 block_threads: int = 0, words_per_warp: int = 0, short_circuit: bool = False,
+                 conjunct_order: Optional[Sequence[int]] = None, rand_seed: int = 0):
+        L = N.lib()
+        o = N.PlanOptions()
+        L.gx_plan_options_init(C.byref(o))
+        o.filter_mode = filter_mode
+        o.block_threads = block_threads
+        o.words_per_warp = words_per_warp
+        o.short_circuit = 1 if short_circuit else 0
+        o.rand_seed = rand_seed
+        if conjunct_order:
+            o.num_conjuncts = len(conjunct_order)
+            for i, c in enumerate(conjunct_order):
+                o.conjunct_order[i] = c
+        types = (C.c_int32 * max(1, len(schema)))(*[int(t) for t in schema])
+        nb = None
+        if nullable is not None:
+            nb = (C.c_uint8 * max(1, len(schema)))(*[1 if x else 0 for x in nullable])
+        ex = (C.c_char_p * max(1, len(expressions)))(*[e.encode() for e in expressions])
+        st = N.StatusInfo()
+        h = L.gx_plan_compile(types, nb, len(schema), condition.encode() if condition else None, ex,
+                              len(expressions), C.byref(o), C.byref(st))
+        if not h:
+            raise N.GxError(st.code, st.message.decode(errors="replace"))
+        self._h = h
+        self.schema = list(schema)
+
+    @property
+    def num_outputs(self) -> int:
+        return N.lib().gx_plan_num_outputs(self._h)
+
+    @property
+    def num_conjuncts(self) -> int:
+        return N.lib().gx_plan_num_conjuncts(self._h)
+
+    def output_types(self) -> List[int]:
+        return [N.lib().gx_plan_output_type(self._h, i) for i in range(self.num_outputs)]
+
+    def execute(self, table: Table, out: Optional[Sequence[N.Column]] = None, stream=None):
+        """Runs the plan; returns (columns, rows).  ``out`` may hold caller buffers."""
+        keep: list = []
+        views, nc = _views(table, keep)
+        s = _stream_handle(stream)
+        n = self.num_outputs
+        outs = (N.Column * max(1, n))()
+        if out is not None:
+            for i, c in enumerate(out):
+                outs[i] = c
+        rows = C.c_int64(0)
+        st = N.StatusInfo()
+        rc = N.lib().gx_plan_execute(self._h, views, nc, outs, C.byref(rows), s, C.byref(st))
+        if rc == N.GX_ERR_CAPACITY:
+            raise N.GxError(rc, f"{st.message.decode(errors='replace')} (needed rows={rows.value})")
+        N.check(rc, st)
+        if out is not None:
+            return [outs[i] for i in range(n)], rows.value
+        return _wrap(outs, n, s), rows.value
+
+    def kernel_source(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None) -> str:
+        L = N.lib()
+        st = N.StatusInfo()
+        hm = None if has_mask is None else (C.c_uint8 * len(has_mask))(*[1 if x else 0 for x in has_mask])
+        n = L.gx_debug_kernel_source(self._h, kind, hm, None, 0, C.byref(st))
+        if n < 0:
+            raise N.GxError(st.code, st.message.decode(errors="replace"))
+        buf = C.create_string_buffer(n + 1)
+        L.gx_debug_kernel_source(self._h, kind, hm, buf, n + 1, C.byref(st))
+        return buf.value.decode()
+
+    def compile_check(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None) -> None:
+        st = N.StatusInfo()
+        hm = None if has_mask is None else (C.c_uint8 * len(has_mask))(*[1 if x else 0 for x in has_mask])
+        N.check(N.lib().gx_debug_compile_check(self._h, kind, hm, C.byref(st)), st)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.lib().gx_plan_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def version() -> str:
+    return N.lib().gx_version().decode()
+
+
+def jit_stats():
+    c = C.c_int64(0)
+    ms = C.c_double(0)
+    N.lib().gx_debug_jit_stats(C.byref(c), C.byref(ms))
+    return c.value, ms.value
+
+
+def fail_next_allocation(n: int = 1) -> None:
+    """Host-side fault injection: the n-th next device allocation fails (GX_ERR_OOM)."""
+    N.lib().gx_debug_fail_allocation(n)

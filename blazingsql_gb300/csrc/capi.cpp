@@ -1,0 +1,434 @@
+// capi.cpp -- extern "C" entry points of include/gx_eval.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <list>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <unordered_map>
+
+#include "frontend.h"
+#include "plan.h"
+#include "runtime.h"
+
+namespace gx {
+namespace {
+
+void set_status(gx_status_info* st, int code, const char* msg) {
+  if (!st) return;
+  st->code = code;
+  std::snprintf(st->message, sizeof st->message, "%s", msg ? msg : "");
+}
+
+template <class F>
+int guarded(gx_status_info* st, F&& f) {
+  try {
+    f();
+    set_status(st, GX_OK, "");
+    return GX_OK;
+  } catch (const Error& e) {
+    set_status(st, e.code, e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_status(st, GX_ERR_OOM, "host allocation failed");
+    return GX_ERR_OOM;
+  } catch (const std::exception& e) {
+    set_status(st, GX_ERR_INVALID, e.what());
+    return GX_ERR_INVALID;
+  }
+}
+
+int env_int(const char* name, int dflt) {
+  const char* v = std::getenv(name);
+  return (v && *v) ? std::atoi(v) : dflt;
+}
+
+KernelConfig default_config() {
+  KernelConfig c;
+  c.warps = env_int("GX_WARPS", 8);
+  c.words = env_int("GX_WORDS", 4);
+  return c;
+}
+
+// One call's plans: expression lists longer than GX_OUTPUTS_PER_KERNEL run as
+// several kernels (chunks), each writing its slice of the outputs.
+struct PlanSet {
+  std::vector<std::shared_ptr<CompiledPlan>> chunks;
+  std::vector<int> first_output;
+  int num_outputs = 0;
+  int num_conjuncts = 0;
+  std::vector<int> output_types;
+
+  void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const {
+    const bool caller_bufs = num_outputs > 0 && out[0].data != nullptr;
+    int64_t rows = -1;
+    size_t done = 0;
+    try {
+      for (size_t c = 0; c < chunks.size(); c++) {
+        int64_t r = 0;
+        chunks[c]->execute(cols, out + first_output[c], &r, s);
+        done = c + 1;
+        if (rows >= 0 && r != rows) fail(GX_ERR_CUDA, "chunks of one plan disagree on the row count");
+        rows = r;
+      }
+    } catch (...) {
+      if (!caller_bufs)  // release the outputs of the chunks that completed
+        for (size_t c = 0; c < done; c++)
+          for (size_t j = 0; j < chunks[c]->plan().outputs.size(); j++) free_column(out[first_output[c] + j], s);
+      throw;
+    }
+    if (out_rows) *out_rows = rows < 0 ? 0 : rows;
+  }
+};
+
+std::shared_ptr<PlanSet> make_plan_set(const std::vector<int>& schema, const std::vector<bool>& nullable,
+                                       const std::string& cond, const std::vector<std::string>& exprs,
+                                       bool rand_by_out, const KernelConfig& cfg, int mode, uint64_t seed) {
+  auto ps = std::make_shared<PlanSet>();
+  int rand_base = 0;
+  for (size_t i = 0; i < exprs.size() || (i == 0 && exprs.empty()); i += GX_OUTPUTS_PER_KERNEL) {
+    std::vector<std::string> part(exprs.begin() + i,
+                                  exprs.begin() + std::min(exprs.size(), i + (size_t)GX_OUTPUTS_PER_KERNEL));
+    int used = 0;
+    Plan p = build_plan(schema, nullable, cond, part, false, rand_by_out, rand_base, &used);
+    rand_base += used;
+    p.rand_seed = seed;
+    if (ps->chunks.empty()) ps->num_conjuncts = (int)p.conjuncts.size();
+    for (const auto& o : p.outputs) ps->output_types.push_back(o.type);
+    ps->first_output.push_back(ps->num_outputs);
+    ps->num_outputs += (int)p.outputs.size();
+    KernelConfig c = cfg;
+    if (!c.conjunct_order.empty() && c.conjunct_order.size() != p.conjuncts.size())
+      fail(GX_ERR_INVALID, "conjunct order must list every conjunct");
+    ps->chunks.push_back(std::make_shared<CompiledPlan>(std::move(p), c, mode));
+    if (exprs.empty()) break;
+  }
+  return ps;
+}
+
+// Host-side cache of compiled plans keyed by the call's text + schema, so the
+// per-batch host work of the execution graph's many small batches is a lookup
+// (the reference re-parses with std::regex on every batch).
+class PlanCache {
+ public:
+  std::shared_ptr<PlanSet> get(const std::string& key) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = map_.find(key);
+    if (it == map_.end()) return nullptr;
+    lru_.splice(lru_.begin(), lru_, it->second.second);
+    return it->second.first;
+  }
+  void put(const std::string& key, std::shared_ptr<PlanSet> p) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (map_.count(key)) return;
+    lru_.push_front(key);
+    map_[key] = {std::move(p), lru_.begin()};
+    while (map_.size() > 256) {
+      map_.erase(lru_.back());
+      lru_.pop_back();
+    }
+  }
+
+ private:
+  std::mutex mu_;
+  std::list<std::string> lru_;
+  std::unordered_map<std::string, std::pair<std::shared_ptr<PlanSet>, std::list<std::string>::iterator>> map_;
+};
+
+PlanCache& cache() {
+  static PlanCache c;
+  return c;
+}
+
+std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, const std::string& cond,
+                      const std::vector<std::string>& exprs, const KernelConfig& cfg, int mode) {
+  std::string k = kind;
+  k += '|';
+  for (const auto& c : cols) {
+    k += std::to_string(c.type);
+    k += c.mask ? 'n' : '-';
+    k += ',';
+  }
+  k += '|' + cond + '|';
+  for (const auto& e : exprs) {
+    k += e;
+    k += '\x1f';
+  }
+  k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode);
+  return k;
+}
+
+std::shared_ptr<PlanSet> plan_for(const char* kind, const std::vector<ColumnView>& cols, const std::string& cond,
+                                  const std::vector<std::string>& exprs, bool rand_by_out) {
+  const KernelConfig cfg = default_config();
+  const int mode = env_int("GX_FILTER_MODE", GX_FILTER_AUTO);
+  const std::string key = cache_key(kind, cols, cond, exprs, cfg, mode);
+  if (auto p = cache().get(key)) return p;
+  std::vector<int> schema;
+  std::vector<bool> nullable;
+  for (const auto& c : cols) {
+    schema.push_back(c.type);
+    nullable.push_back(c.mask != nullptr);
+  }
+  auto ps = make_plan_set(schema, nullable, cond, exprs, rand_by_out, cfg, mode, 0);
+  cache().put(key, ps);
+  return ps;
+}
+
+std::vector<int> schema_of(const std::vector<ColumnView>& cols) {
+  std::vector<int> s;
+  for (const auto& c : cols) s.push_back(c.type);
+  return s;
+}
+
+}  // namespace
+}  // namespace gx
+
+struct gx_plan {
+  std::shared_ptr<gx::PlanSet> ps;
+};
+
+using namespace gx;
+
+extern "C" {
+
+const char* gx_version(void) {
+  static const char* v = "gx-eval 0.1 (sm_103a; NVRTC plan kernels; abi " "1" ")";
+  return v;
+}
+
+void gx_plan_options_init(gx_plan_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->filter_mode = GX_FILTER_AUTO;
+  o->use_tma = -1;
+}
+
+int gx_evaluate_expressions(const gx_column_view* columns, int num_columns, const char* const* expressions,
+                            int num_expressions, gx_column* out, void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (num_expressions < 0 || (num_expressions > 0 && (!expressions || !out))) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(columns, num_columns);
+    std::vector<std::string> ex;
+    for (int i = 0; i < num_expressions; i++) {
+      if (!expressions[i]) fail(GX_ERR_INVALID, "null expression");
+      ex.emplace_back(expressions[i]);
+    }
+    if (ex.empty()) return;
+    for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
+    auto ps = plan_for("eval", cols, "", ex, false);
+    int64_t rows = 0;
+    ps->execute(cols, out, &rows, (cudaStream_t)stream);
+  });
+}
+
+int gx_process_project(const gx_column_view* columns, int num_columns, const char* query_part, gx_column* out,
+                       int max_out, int* num_out, char* out_names, int name_len, void* stream,
+                       gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!query_part || !out || !num_out) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(columns, num_columns);
+    std::vector<std::string> names, exprs;
+    split_projections(query_part, names, exprs);
+    if ((int)exprs.size() > max_out) fail(GX_ERR_INVALID, "output array too small for the projections");
+    const std::vector<int> schema = schema_of(cols);
+    for (auto& e : exprs) {
+      if (e.find(" OVER ") != std::string::npos) fail(GX_ERR_UNSUPPORTED, "window functions are out of scope");
+      e = preprocess_expression(e, schema);
+    }
+    for (size_t i = 0; i < exprs.size(); i++) out[i] = gx_column{};
+    auto ps = plan_for("eval", cols, "", exprs, false);
+    int64_t rows = 0;
+    ps->execute(cols, out, &rows, (cudaStream_t)stream);
+    *num_out = (int)exprs.size();
+    if (out_names && name_len > 0)
+      for (size_t i = 0; i < names.size(); i++)
+        std::snprintf(out_names + i * name_len, (size_t)name_len, "%s", names[i].c_str());
+  });
+}
+
+int gx_process_filter(const gx_column_view* columns, int num_columns, const char* query_part, gx_column* out,
+                      int64_t* out_rows, void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!query_part || (num_columns > 0 && !out)) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(columns, num_columns);
+    const int64_t n = cols.empty() ? 0 : cols[0].size;
+    if (n == 0) {  // LogicalFilter.cpp:36-38: empty input -> empty_like, no parsing
+      for (int i = 0; i < num_columns; i++) {
+        out[i] = alloc_column(cols[i].type, 0, (cudaStream_t)stream);
+        launch_fill_mask(out[i].null_mask, 0, false, 16, (cudaStream_t)stream);
+      }
+      if (out_rows) *out_rows = 0;
+      return;
+    }
+    const std::string qp(query_part);
+    std::string cond = named_expression(qp, "condition");
+    if (cond.empty()) cond = named_expression(qp, "filters");
+    if (cond.empty()) fail(GX_ERR_PARSE, "no condition=[...] or filters=[...] in: " + qp);
+    cond = preprocess_expression(cond, schema_of(cols));
+    // every input column compacted = the projections $0..$k-1 of the filtered rows
+    std::vector<std::string> all;
+    for (int i = 0; i < num_columns; i++) {
+      out[i] = gx_column{};
+      all.push_back("$" + std::to_string(i));
+    }
+    auto ps = plan_for("filter", cols, cond, all, false);
+    ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+  });
+}
+
+int gx_filter_project(const gx_column_view* columns, int num_columns, const char* condition,
+                      const char* const* expressions, int num_expressions, gx_column* out, int64_t* out_rows,
+                      void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (num_expressions <= 0 || !expressions || !out) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(columns, num_columns);
+    const std::vector<int> schema = schema_of(cols);
+    std::string cond = condition ? std::string(condition) : std::string();
+    if (!cond.empty()) cond = preprocess_expression(cond, schema);
+    std::vector<std::string> ex;
+    for (int i = 0; i < num_expressions; i++) {
+      if (!expressions[i]) fail(GX_ERR_INVALID, "null expression");
+      ex.push_back(preprocess_expression(expressions[i], schema));
+    }
+    for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
+    auto ps = plan_for("fused", cols, cond, ex, true);
+    ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+  });
+}
+
+void gx_free_columns(gx_column* columns, int num_columns, void* stream) {
+  if (!columns) return;
+  for (int i = 0; i < num_columns; i++) free_column(columns[i], (cudaStream_t)stream);
+}
+
+int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_mask, void* stream,
+                      gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!column) fail(GX_ERR_INVALID, "null column");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t bytes = (size_t)column->size * type_size(column->type_id);
+    if (bytes && host_data)
+      check_cuda(cudaMemcpyAsync(host_data, column->data, bytes, cudaMemcpyDeviceToHost, s), "column to host");
+    if (host_mask) {
+      const size_t words = (size_t)((column->size + 31) / 32);
+      if (words)
+        check_cuda(cudaMemcpyAsync(host_mask, column->null_mask, words * 4, cudaMemcpyDeviceToHost, s), "mask to host");
+    }
+    check_cuda(cudaStreamSynchronize(s), "column to host sync");
+  });
+}
+
+gx_plan* gx_plan_compile(const int32_t* column_types, const uint8_t* column_nullable, int num_columns,
+                         const char* condition, const char* const* expressions, int num_expressions,
+                         const gx_plan_options* options, gx_status_info* status) {
+  gx_plan* out = nullptr;
+  guarded(status, [&] {
+    if (num_columns < 0 || (num_columns > 0 && !column_types)) fail(GX_ERR_INVALID, "bad schema");
+    std::vector<int> schema(column_types, column_types + num_columns);
+    std::vector<bool> nullable(num_columns, true);
+    if (column_nullable)
+      for (int i = 0; i < num_columns; i++) nullable[i] = column_nullable[i] != 0;
+    gx_plan_options o;
+    gx_plan_options_init(&o);
+    if (options) o = *options;
+    std::string cond = condition ? std::string(condition) : std::string();
+    if (!cond.empty()) cond = preprocess_expression(cond, schema);
+    std::vector<std::string> ex;
+    for (int i = 0; i < num_expressions; i++) ex.push_back(preprocess_expression(expressions[i], schema));
+    KernelConfig cfg = default_config();
+    if (o.block_threads > 0) cfg.warps = o.block_threads / 32;
+    if (o.words_per_warp > 0) cfg.words = o.words_per_warp;
+    cfg.short_circuit = o.short_circuit != 0;
+    for (int i = 0; i < o.num_conjuncts && i < 16; i++) {
+      if (o.conjunct_order[i] < 0 || o.conjunct_order[i] >= 16) fail(GX_ERR_INVALID, "conjunct order index out of range");
+      cfg.conjunct_order.push_back(o.conjunct_order[i]);
+    }
+    if (!cfg.conjunct_order.empty()) {
+      std::vector<int> sorted = cfg.conjunct_order;
+      std::sort(sorted.begin(), sorted.end());
+      for (size_t i = 0; i < sorted.size(); i++)
+        if (sorted[i] != (int)i) fail(GX_ERR_INVALID, "conjunct order must be a permutation");
+    }
+    out = new gx_plan{make_plan_set(schema, nullable, cond, ex, true, cfg, o.filter_mode, o.rand_seed)};
+  });
+  return out;
+}
+
+int gx_plan_num_outputs(const gx_plan* plan) { return plan ? plan->ps->num_outputs : -1; }
+
+int32_t gx_plan_output_type(const gx_plan* plan, int index) {
+  if (!plan || index < 0 || index >= plan->ps->num_outputs) return -1;
+  return plan->ps->output_types[index];
+}
+
+int gx_plan_num_conjuncts(const gx_plan* plan) { return plan ? plan->ps->num_conjuncts : -1; }
+
+int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_columns, gx_column* out,
+                    int64_t* out_rows, void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!plan || !out) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(columns, num_columns);
+    plan->ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+  });
+}
+
+void gx_plan_destroy(gx_plan* plan) { delete plan; }
+
+static KernelKind kind_of(int k) {
+  switch (k) {
+    case 0: return KernelKind::PROJECT;
+    case 1: return KernelKind::FUSED_FILTER;
+    case 2: return KernelKind::COUNT_FILTER;
+    case 3: return KernelKind::WRITE_FILTER;
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..3");
+  }
+}
+
+static std::string debug_source(const gx_plan* plan, int kind, const uint8_t* has_mask) {
+  if (!plan) fail(GX_ERR_INVALID, "null plan");
+  Plan p = plan->ps->chunks.at(0)->plan();
+  for (size_t i = 0; i < p.nullable.size(); i++) p.nullable[i] = has_mask ? has_mask[i] != 0 : true;
+  return generate_kernel(p, kind_of(kind), plan->ps->chunks.at(0)->config(), "gx_kernel");
+}
+
+int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,
+                               int64_t buf_len, gx_status_info* status) {
+  int64_t n = -1;
+  guarded(status, [&] {
+    const std::string s = std::string(jit_prelude()) + "\n" + debug_source(plan, kind, column_has_mask);
+    n = (int64_t)s.size();
+    if (buf && buf_len > 0) std::snprintf(buf, (size_t)buf_len, "%s", s.c_str());
+  });
+  return n;
+}
+
+int gx_debug_compile_check(const gx_plan* plan, int kind, const uint8_t* column_has_mask, gx_status_info* status) {
+  return guarded(status, [&] { jit_compile_check(debug_source(plan, kind, column_has_mask), "gx_kernel"); });
+}
+
+void gx_debug_fail_allocation(int n) { debug_fail_allocation(n); }
+
+void gx_debug_set_kernel_timing(int enable) { set_kernel_timing(enable != 0); }
+
+double gx_debug_kernel_ms(int reset) { return kernel_ms(reset != 0); }
+
+int64_t gx_debug_launch_count(void) { return launch_count(); }
+
+int gx_debug_rebuild_expression(const char* expression, char* buf, int buf_len, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!expression || !buf || buf_len <= 0) fail(GX_ERR_INVALID, "bad arguments");
+    std::snprintf(buf, (size_t)buf_len, "%s", rebuild(parse_and_lower(expression)).c_str());
+  });
+}
+
+void gx_debug_jit_stats(int64_t* compiles, double* total_ms) {
+  if (compiles) *compiles = jit_compile_count();
+  if (total_ms) *total_ms = jit_compile_ms_total();
+}
+
+}  // extern "C"

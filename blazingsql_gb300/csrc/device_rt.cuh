@@ -1,0 +1,216 @@
+// device_rt.cuh -- device-side runtime included (as text) ahead of every
+// plan kernel the library JIT-compiles with NVRTC for sm_103a.
+//
+// Value model: every intermediate is 64 bits that an op reads as int64 or as
+// double depending on its operand's kernel type, plus a validity bit -- the
+// slot model of engine/src/Interpreter/interpreter_ops.cuh:248-262, kept in
+// registers instead of a shared-memory slot file.  Plans are compiled with
+// --fmad=false so every FP64 op rounds once, in the reference's op order.
+
+typedef unsigned long long u64;
+typedef long long i64;
+typedef unsigned int u32;
+
+#define GX_MAGIC_I 9223372036854775794LL   /* INT64_MAX - 13, interpreter_ops.cuh:41 */
+#define GX_MAGIC_D 1.7976931348623123e+308 /* interpreter_ops.cuh:47 */
+#define GX_FULL 0xffffffffu
+
+// ---- bit views -------------------------------------------------------------
+__device__ __forceinline__ double gx_D(u64 b) { return __longlong_as_double((i64)b); }
+__device__ __forceinline__ u64 gx_B(double d) { return (u64)__double_as_longlong(d); }
+__device__ __forceinline__ double gx_I2D(u64 b) { return (double)(i64)b; }
+// static_cast<int64_t>(double) on the GPU: truncate, saturate, NaN -> 0
+__device__ __forceinline__ i64 gx_D2LL(double d) { return __double2ll_rz(d); }
+
+// ---- integer division guards (the reference's DIV marks /0 NULL) -----------
+__device__ __forceinline__ u64 gx_div_ii(u64 a, u64 b) {
+  const i64 x = (i64)a, y = (i64)b;
+  return y == 0 ? 0ull : (y == -1 ? 0ull - a : (u64)(x / y));
+}
+__device__ __forceinline__ u64 gx_mod_ii(u64 a, u64 b) {
+  const i64 x = (i64)a, y = (i64)b;
+  return (y == 0 || y == -1) ? 0ull : (u64)(x % y);
+}
+
+// ---- ROUND scale: correctly rounded 10^d for integral |d| <= 22 -------------
+__constant__ double gx_p10[23] = {1e0, 1e1, 1e2, 1e3, 1e4, 1e5, 1e6, 1e7, 1e8, 1e9, 1e10, 1e11,
+                                  1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+__constant__ double gx_n10[23] = {1e-0, 1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9, 1e-10, 1e-11,
+                                  1e-12, 1e-13, 1e-14, 1e-15, 1e-16, 1e-17, 1e-18, 1e-19, 1e-20, 1e-21, 1e-22};
+__device__ __forceinline__ double gx_pow10(double d) {
+  if (d == floor(d) && d >= -22.0 && d <= 22.0) {
+    const int k = (int)d;
+    return k >= 0 ? gx_p10[k] : gx_n10[-k];
+  }
+  return pow(10.0, d);
+}
+__device__ __forceinline__ double gx_round_to(double x, double digits) {
+  const double f = gx_pow10(digits);
+  const double p = x * f;
+  return round(p) / f;
+}
+
+// ---- timestamps ------------------------------------------------------------
+// count of a timestamp/duration value: int32 representation for *_DAYS
+__device__ __forceinline__ i64 gx_days32(i64 v) { return (i64)(int)v; }
+__device__ __forceinline__ i64 gx_floordiv(i64 a, i64 b) {
+  i64 q = a / b;
+  if ((a % b != 0) && ((a < 0) != (b < 0))) q--;
+  return q;
+}
+// civil_from_days (H. Hinnant's published algorithm); part: 0 year, 1 month, 2 day
+__device__ __forceinline__ i64 gx_civil(i64 days, int part) {
+  const i64 z = days + 719468;
+  const i64 era = (z >= 0 ? z : z - 146096) / 146097;
+  const i64 doe = z - era * 146097;
+  const i64 yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+  const i64 doy = doe - (365 * yoe + yoe / 4 - yoe / 100);
+  const i64 mp = (5 * doy + 2) / 153;
+  const i64 d = doy - (153 * mp + 2) / 5 + 1;
+  const i64 m = mp < 10 ? mp + 3 : mp - 9;
+  const i64 y = yoe + era * 400 + (m <= 2);
+  return part == 0 ? y : (part == 1 ? m : d);
+}
+// EXTRACT on a timestamp count with `per_day` units per day (1 for DAYS).
+// which: 0 year, 1 month, 2 day, 3 iso day-of-week, 4 hour, 5 minute, 6 second
+__device__ __forceinline__ i64 gx_extract(i64 cnt, i64 per_day, int which) {
+  const i64 days = per_day == 1 ? cnt : gx_floordiv(cnt, per_day);
+  if (which <= 2) return gx_civil(days, which);
+  if (which == 3) {
+    const i64 wd = ((days % 7) + 7 + 4) % 7;
+    return wd == 0 ? 7 : wd;
+  }
+  if (per_day == 1) return 0;
+  const i64 tsm = cnt - days * per_day;
+  const i64 ph = per_day / 24, pm = ph / 60, ps = pm / 60;
+  if (which == 4) return tsm / ph;
+  if (which == 5) return (tsm % ph) / pm;
+  return (tsm % pm) / ps;
+}
+
+// ---- RAND: Philox4x32-10 (Salmon et al., SC'11) -> uniform double in (0, 1] -
+__device__ __forceinline__ double gx_philox_uniform(u64 seed, u32 rand_id, u64 row) {
+  u32 c0 = (u32)row, c1 = (u32)(row >> 32), c2 = rand_id, c3 = 0x5EEDu;
+  u32 k0 = (u32)seed, k1 = (u32)(seed >> 32);
+#pragma unroll
+  for (int i = 0; i < 10; i++) {
+    const u32 h0 = __umulhi(0xD2511F53u, c0), l0 = 0xD2511F53u * c0;
+    const u32 h1 = __umulhi(0xCD9E8D57u, c2), l1 = 0xCD9E8D57u * c2;
+    const u32 n0 = h1 ^ c1 ^ k0, n1 = l1, n2 = h0 ^ c3 ^ k1, n3 = l0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  const u64 m = ((u64)c0 << 21) | (c1 >> 11);
+  return (double)(m + 1ull) * (1.0 / 9007199254740992.0);
+}
+
+// ---- validity --------------------------------------------------------------
+__device__ __forceinline__ bool gx_valid(const u32* __restrict__ m, i64 bit) {
+  return m == nullptr ? true : ((__ldg(m + (bit >> 5)) >> (bit & 31)) & 1u);
+}
+
+// ---- streaming loads / stores ------------------------------------------------
+__device__ __forceinline__ i64 gx_ld_i8(const void* p, i64 i) { return (i64)__ldcs((const signed char*)p + i); }
+__device__ __forceinline__ i64 gx_ld_u8(const void* p, i64 i) { return (i64)__ldcs((const unsigned char*)p + i); }
+__device__ __forceinline__ i64 gx_ld_i16(const void* p, i64 i) { return (i64)__ldcs((const short*)p + i); }
+__device__ __forceinline__ i64 gx_ld_u16(const void* p, i64 i) { return (i64)__ldcs((const unsigned short*)p + i); }
+__device__ __forceinline__ i64 gx_ld_i32(const void* p, i64 i) { return (i64)__ldcs((const int*)p + i); }
+__device__ __forceinline__ i64 gx_ld_u32(const void* p, i64 i) { return (i64)__ldcs((const unsigned int*)p + i); }
+__device__ __forceinline__ u64 gx_ld_64(const void* p, i64 i) { return (u64)__ldcs((const long long*)p + i); }
+__device__ __forceinline__ u64 gx_ld_f32(const void* p, i64 i) { return gx_B((double)__ldcs((const float*)p + i)); }
+
+__device__ __forceinline__ void gx_st_8(void* p, i64 i, u64 v) { __stcs((signed char*)p + i, (signed char)v); }
+__device__ __forceinline__ void gx_st_16(void* p, i64 i, u64 v) { __stcs((short*)p + i, (short)v); }
+__device__ __forceinline__ void gx_st_32(void* p, i64 i, u64 v) { __stcs((int*)p + i, (int)v); }
+__device__ __forceinline__ void gx_st_64(void* p, i64 i, u64 v) { __stcs((long long*)p + i, (long long)v); }
+__device__ __forceinline__ void gx_st_f32(void* p, i64 i, u64 v) { __stcs((float*)p + i, (float)gx_D(v)); }
+
+// ---- decoupled look-back (single-pass stable compaction) --------------------
+// tile status word: bits 62..63 flag (0 none, 1 aggregate, 2 inclusive prefix),
+// bits 0..61 value.
+#define GX_ST_AGG (1ull << 62)
+#define GX_ST_PFX (2ull << 62)
+#define GX_ST_VAL ((1ull << 62) - 1ull)
+
+__device__ __forceinline__ void gx_st_release(u64* p, u64 v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ u64 gx_ld_acquire(const u64* p) {
+  u64 v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Exclusive prefix of tile `tile` given its aggregate; called by one full warp.
+// Waits are bounded: after `max_spins` polls without progress it records an
+// error in *err and returns ~0ull (callers then skip their writes).
+__device__ __forceinline__ u64 gx_lookback(u64* status, i64 tile, u64 agg, int* err, u32 max_spins) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {
+    if (lane == 0) gx_st_release(status, GX_ST_PFX | agg);
+    return 0ull;
+  }
+  if (lane == 0) gx_st_release(status + tile, GX_ST_AGG | agg);
+  u64 excl = 0;
+  i64 pred = tile - 1;
+  u32 spins = 0;
+  while (true) {
+    const i64 idx = pred - lane;
+    u64 s = idx >= 0 ? gx_ld_acquire(status + idx) : GX_ST_PFX;  // before tile 0: prefix 0
+    const u32 flag = (u32)(s >> 62);
+    const u32 not_ready = __ballot_sync(GX_FULL, flag == 0);
+    const u32 is_pfx = __ballot_sync(GX_FULL, flag == 2);
+    // lanes up to (and including) the first prefix must all be ready
+    const u32 upto = is_pfx ? ((is_pfx & (0u - is_pfx)) << 1) - 1u : GX_FULL;
+    if (not_ready & upto) {
+      if (++spins > max_spins) {
+        if (lane == 0) atomicExch(err, 1);
+        return ~0ull;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    u64 v = ((1u << lane) & upto) ? (s & GX_ST_VAL) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(GX_FULL, v, o);
+    excl += v;
+    if (is_pfx) break;
+    pred -= 32;
+  }
+  if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (excl + agg));
+  return excl;
+}
+
+// Appends `nbits` compressed validity bits to a warp's output bit stream.
+// acc/fill are warp-uniform; full words inside the warp's own range are stored,
+// words shared with a neighbouring range are OR-ed atomically (the mask was
+// zeroed before the launch).
+struct GxBitWriter {
+  u64 acc;
+  int fill;
+  i64 word;     // output word index of acc's low 32 bits
+  bool first;   // the first word may be shared with the previous range
+  __device__ __forceinline__ void init(i64 start_bit) {
+    acc = 0;
+    fill = (int)(start_bit & 31);
+    word = start_bit >> 5;
+    first = fill != 0;
+  }
+  __device__ __forceinline__ void append(u32* mask, u32 bits, int nbits) {
+    acc |= (u64)bits << fill;
+    fill += nbits;
+    if (fill >= 32) {
+      if ((threadIdx.x & 31) == 0) {
+        if (first) atomicOr(mask + word, (u32)acc);
+        else mask[word] = (u32)acc;
+      }
+      first = false;
+      acc >>= 32;
+      fill -= 32;
+      word++;
+    }
+  }
+  __device__ __forceinline__ void flush(u32* mask) {
+    if (fill > 0 && (threadIdx.x & 31) == 0) atomicOr(mask + word, (u32)acc);
+  }
+};

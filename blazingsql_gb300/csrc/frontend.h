@@ -1,0 +1,63 @@
+// frontend.h -- RexNode text -> typed expression tree.
+//
+// Accepts the Calcite RexNode grammar BlazingSQL's parser accepts
+// (engine/src/parser/expression_tree.cpp:183-279) and applies the same
+// normalisation (expression_utils.cpp:1068-1113, 1624-1632), n-ary AND/OR
+// nesting (CalciteExpressionParsing.cpp:330-398), CASE / ROUND / CAST-literal
+// lowering (expression_tree.hpp:181-258) and result-type rules
+// (expression_utils.cpp:115-266).  No std::regex: the lexer is a hand-written
+// scanner (the reference runs ~14 regex searches per token).
+#pragma once
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gx_common.h"
+
+namespace gx {
+
+struct Expr;
+using ExprPtr = std::shared_ptr<Expr>;
+
+struct Expr {
+  enum Kind { COL, LIT, OP } kind = OP;
+  Op op = OP_NONE;
+  std::string token;          // operator token / literal text (diagnostics, rebuild)
+  int col = -1;               // COL
+  int lit_type = EMPTY;       // LIT: declared / inferred type
+  bool lit_valid = false;     // LIT: false for a null literal
+  uint64_t lit_bits = 0;      // LIT: value as the kernel reads it (int64 or double bits)
+  int vtype = EMPTY;          // result type as expr_output_type_visitor computes it
+  int ktype = EMPTY;          // result type as perform_interpreter_operation computes it
+  std::vector<ExprPtr> ch;
+};
+
+// Whole-expression pipeline of evaluate_expressions for one expression:
+// normalise, nest n-ary AND/OR, parse, lower CASE/ROUND/CAST-literal, type.
+ExprPtr compile_expression(const std::string& text, const std::vector<int>& schema);
+
+// preprocess_expression (expression_utils.cpp:1624-1632)
+std::string preprocess_expression(const std::string& text, const std::vector<int>& schema);
+
+// get_named_expression (expression_utils.cpp:537-547)
+std::string named_expression(const std::string& query_part, const std::string& name);
+
+// get_query_part (expression_utils.cpp:764-769)
+std::string query_part_of(const std::string& plan_text);
+
+// get_expressions_from_expression_list (expression_utils.cpp:1012-1066); applies
+// the Calcite normalisation to the text first, as the reference does.
+std::vector<std::string> split_expression_list(std::string text, bool trim_items);
+
+// Splits a LogicalProject(...) query part into (names, expressions).
+void split_projections(const std::string& plan_text, std::vector<std::string>& names,
+                       std::vector<std::string>& exprs);
+
+// Rebuilds a (lowered) expression tree as text: "OP(a, b)".
+std::string rebuild(const ExprPtr& e);
+
+// Parse + lower without typing (used by tests of the lowering rules).
+ExprPtr parse_and_lower(const std::string& text);
+
+}  // namespace gx

@@ -1,0 +1,647 @@
+// plan.cpp -- expression DAG + CUDA code generation (see plan.h).
+#include "plan.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <set>
+#include <sstream>
+
+namespace gx {
+namespace {
+
+std::string hex64(uint64_t v) {
+  char buf[32];
+  std::snprintf(buf, sizeof buf, "0x%016llxull", (unsigned long long)v);
+  return buf;
+}
+
+struct Builder {
+  Plan& p;
+  std::map<std::string, int> memo;
+  int rand_counter = 0;
+  bool rand_out_row = false;
+
+  int push(Node n, const std::string& key) {
+    if (!key.empty()) {
+      auto it = memo.find(key);
+      if (it != memo.end()) return it->second;
+    }
+    p.nodes.push_back(n);
+    int id = (int)p.nodes.size() - 1;
+    if (!key.empty()) memo[key] = id;
+    return id;
+  }
+
+  int add(const ExprPtr& e) {
+    if (e->kind == Expr::COL) {
+      Node n;
+      n.kind = Node::COL;
+      n.col = e->col;
+      n.vtype = e->vtype;
+      n.ktype = e->ktype;
+      return push(n, "c" + std::to_string(e->col));
+    }
+    if (e->kind == Expr::LIT) {
+      Node n;
+      n.kind = Node::LIT;
+      n.lit_type = e->lit_type;
+      n.lit_valid = e->lit_valid;
+      n.lit_bits = e->lit_bits;
+      n.vtype = e->vtype;
+      n.ktype = e->ktype;
+      return push(n, "l" + std::to_string(e->vtype) + ":" + std::to_string(e->ktype) + ":" +
+                         std::to_string(e->lit_valid) + ":" + std::to_string(e->lit_bits));
+    }
+    // every operand is visited (RAND ordinals follow the reference's post-order
+    // visit, which also walks the extra operands of an un-nested OR)
+    std::vector<int> kids;
+    for (const auto& c : e->ch) kids.push_back(add(c));
+    Node n;
+    n.kind = Node::OP;
+    n.op = e->op;
+    n.vtype = e->vtype;
+    n.ktype = e->ktype;
+    if (!kids.empty()) n.a = kids[0];
+    if (op_is_binary(e->op) && kids.size() > 1) n.b = kids[1];
+    if (e->op == OP_RAND) {
+      n.rand_id = rand_counter++;
+      n.rand_out_row = rand_out_row;
+      return push(n, "");  // never shared
+    }
+    return push(n, "o" + std::to_string(n.op) + ":" + std::to_string(n.a) + ":" + std::to_string(n.b) + ":" +
+                       std::to_string(n.vtype) + ":" + std::to_string(n.ktype));
+  }
+};
+
+void flatten_and(const Plan& p, int id, std::vector<int>& out) {
+  const Node& n = p.nodes[id];
+  if (n.kind == Node::OP && n.op == OP_AND) {
+    flatten_and(p, n.a, out);
+    flatten_and(p, n.b, out);
+  } else {
+    out.push_back(id);
+  }
+}
+
+}  // namespace
+
+uint64_t OutSpec::lit_bits_as_element() const {
+  if (type == FLOAT32) {
+    double d;
+    std::memcpy(&d, &lit_bits, 8);
+    const float f = (float)d;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+  }
+  if (type == BOOL8) return lit_bits != 0;
+  return lit_bits;
+}
+
+bool Plan::needs_kernel() const {
+  if (has_filter()) return true;
+  for (const auto& o : outputs)
+    if (o.kind == OutSpec::NODE) return true;
+  return false;
+}
+
+Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullable, const std::string& condition,
+                const std::vector<std::string>& expressions, bool filter_all, bool rand_by_output_row,
+                int first_rand_id, int* rand_count) {
+  Plan p;
+  p.schema = schema;
+  p.nullable = nullable;
+  Builder b{p};
+  if (!condition.empty()) {
+    ExprPtr c = compile_expression(condition, schema);
+    if (c->vtype != BOOL8) fail(GX_ERR_TYPE, "Expression does not evaluate to a boolean mask");
+    p.predicate = b.add(c);
+    flatten_and(p, p.predicate, p.conjuncts);
+  }
+  b.rand_counter = first_rand_id;
+  b.rand_out_row = rand_by_output_row && !condition.empty();
+  if (filter_all) {
+    p.filter_copies_all = true;
+    for (size_t i = 0; i < schema.size(); i++) {
+      OutSpec o;
+      o.kind = OutSpec::COPY;
+      o.col = (int)i;
+      o.type = schema[i];
+      p.outputs.push_back(o);
+    }
+  } else {
+    for (const auto& text : expressions) {
+      ExprPtr e = compile_expression(text, schema);
+      OutSpec o;
+      if (e->kind == Expr::LIT) {
+        o.kind = OutSpec::BROADCAST;
+        o.type = e->lit_type;
+        o.lit_bits = e->lit_bits;
+        o.lit_valid = e->lit_valid;
+        if (o.type == EMPTY || type_size(o.type) == 0) fail(GX_ERR_TYPE, "a bare null literal has no column type");
+      } else if (e->kind == Expr::COL) {
+        o.kind = OutSpec::COPY;
+        o.col = e->col;
+        o.type = schema[e->col];
+      } else {
+        o.kind = OutSpec::NODE;
+        o.node = b.add(e);
+        o.type = e->vtype;
+        if (type_size(o.type) == 0) fail(GX_ERR_TYPE, "expression has no fixed-width output type");
+      }
+      p.outputs.push_back(o);
+    }
+  }
+  if (rand_count) *rand_count = b.rand_counter - first_rand_id;
+  if (p.outputs.size() > (size_t)GX_MAX_OUTS) fail(GX_ERR_UNSUPPORTED, "too many output columns in one plan");
+  if (schema.size() > (size_t)GX_MAX_COLS) fail(GX_ERR_UNSUPPORTED, "too many input columns in one plan");
+  // data under NULL is observable where it reaches CASE's magic-number test
+  for (int i = (int)p.nodes.size() - 1; i >= 0; i--) {
+    Node& n = p.nodes[i];
+    if (n.kind != Node::OP) continue;
+    if (n.op == OP_MAGIC_IF_NOT && n.b >= 0) p.nodes[n.b].exact_null = true;
+    if (n.op == OP_FIRST_NON_MAGIC) {
+      p.nodes[n.a].exact_null = true;
+      if (n.exact_null) p.nodes[n.b].exact_null = true;
+    }
+  }
+  return p;
+}
+
+// =============================================================== code generation
+namespace {
+
+const char* load_fn(int t) {
+  switch (t) {
+    case INT8: return "gx_ld_i8";
+    case UINT8: case BOOL8: return "gx_ld_u8";
+    case INT16: return "gx_ld_i16";
+    case UINT16: return "gx_ld_u16";
+    case INT32: case TIMESTAMP_DAYS: case DURATION_DAYS: return "gx_ld_i32";
+    case UINT32: return "gx_ld_u32";
+    case FLOAT32: return "gx_ld_f32";
+    default: return "gx_ld_64";
+  }
+}
+
+// store of 64-bit value bits into an output column of type t
+// (device_ptr_write_from_buffer, interpreter_ops.cuh:329-395)
+std::string store_stmt(int t, const std::string& ptr, const std::string& idx, const std::string& bits) {
+  switch (t) {
+    case BOOL8: return "gx_st_8(" + ptr + ", " + idx + ", (u64)((" + bits + ") != 0ull));";
+    case INT8: case UINT8: return "gx_st_8(" + ptr + ", " + idx + ", " + bits + ");";
+    case INT16: case UINT16: return "gx_st_16(" + ptr + ", " + idx + ", " + bits + ");";
+    case INT32: case UINT32: case TIMESTAMP_DAYS: case DURATION_DAYS:
+      return "gx_st_32(" + ptr + ", " + idx + ", " + bits + ");";
+    case FLOAT32: return "gx_st_f32(" + ptr + ", " + idx + ", " + bits + ");";
+    default: return "gx_st_64(" + ptr + ", " + idx + ", " + bits + ");";
+  }
+}
+
+// raw element copy for COPY outputs of filter kernels
+std::string raw_type(int t) {
+  switch (type_size(t)) {
+    case 1: return "unsigned char";
+    case 2: return "unsigned short";
+    case 4: return "unsigned int";
+    default: return "unsigned long long";
+  }
+}
+
+int64_t ns_per_unit(int t) {
+  switch (t) {
+    case TIMESTAMP_DAYS: case DURATION_DAYS: return 86400000000000LL;
+    case TIMESTAMP_SECONDS: case DURATION_SECONDS: return 1000000000LL;
+    case TIMESTAMP_MILLISECONDS: case DURATION_MILLISECONDS: return 1000000LL;
+    case TIMESTAMP_MICROSECONDS: case DURATION_MICROSECONDS: return 1000LL;
+    default: return 1;
+  }
+}
+
+class Gen {
+ public:
+  Gen(const Plan& p, const KernelConfig& c) : p_(p), cfg_(c) {}
+
+  // operand views for node id in word-slot k
+  std::string B(int id) const { return value_bits(id); }
+  std::string V(int id) const { return value_valid(id); }
+
+  std::string value_bits(int id) const {
+    const Node& n = p_.nodes[id];
+    if (n.kind == Node::LIT) return n.lit_valid ? hex64(n.lit_bits) : std::string("0ull");
+    return "b" + std::to_string(id) + "[k]";
+  }
+  std::string value_valid(int id) const {
+    const Node& n = p_.nodes[id];
+    if (n.kind == Node::LIT) return n.lit_valid ? "true" : "false";
+    return "v" + std::to_string(id) + "[k]";
+  }
+  bool kind_f(int id) const { return is_float(p_.nodes[id].ktype); }
+  std::string asD(int id) const { return kind_f(id) ? "gx_D(" + B(id) + ")" : "gx_I2D(" + B(id) + ")"; }
+  std::string asI(int id) const { return kind_f(id) ? "gx_D2LL(gx_D(" + B(id) + "))" : "(i64)(" + B(id) + ")"; }
+  std::string nz(int id) const { return kind_f(id) ? "(gx_D(" + B(id) + ") != 0.0)" : "(" + B(id) + " != 0ull)"; }
+
+  // statements computing node id for slot k; row / out-row expressions given
+  void emit_node(std::ostringstream& o, int id, const std::string& ind) const {
+    const Node& n = p_.nodes[id];
+    const std::string b = "b" + std::to_string(id) + "[k]", v = "v" + std::to_string(id) + "[k]";
+    if (n.kind == Node::LIT) return;
+    if (n.kind == Node::COL) {
+      const int c = n.col;
+      o << ind << b << " = inr ? (u64)" << load_fn(p_.schema[c]) << "(a.in_data[" << c << "], a.in_off[" << c
+        << "] + row) : 0ull;\n";
+      if (p_.nullable[c]) o << ind << v << " = inr && gx_valid(a.in_mask[" << c << "], a.in_off[" << c << "] + row);\n";
+      else o << ind << v << " = inr;\n";
+      return;
+    }
+    std::string r, vv;
+    const Op op = n.op;
+    if (op == OP_RAND) {
+      o << ind << b << " = gx_B(gx_philox_uniform(a.seed, " << n.rand_id << "u, (u64)("
+        << (n.rand_out_row ? "orow" : "row") << ")));\n";
+      o << ind << v << " = true;\n";
+      return;
+    }
+    if (op_is_unary(op)) {
+      const int x = n.a;
+      const int lt = p_.nodes[x].ktype;
+      const bool lf = kind_f(x);
+      const std::string X = B(x), XV = V(x);
+      bool always_valid = false;
+      switch (op) {
+        case OP_IS_NOT_TRUE:
+          r = "(u64)(!(" + XV + " && " + (lf ? "gx_D(" + X + ") == 1.0" : "(i64)(" + X + ") == 1LL") + "))";
+          always_valid = true;
+          break;
+        case OP_IS_NOT_FALSE:
+          r = "(u64)(!(" + XV + " && " + (lf ? "gx_D(" + X + ") == 0.0" : "(i64)(" + X + ") == 0LL") + "))";
+          always_valid = true;
+          break;
+        case OP_IS_NULL: r = "(u64)(!" + XV + ")"; always_valid = true; break;
+        case OP_IS_NOT_NULL: r = "(u64)(" + XV + ")"; always_valid = true; break;
+        case OP_FLOOR: r = "gx_B(floor(" + asD(x) + "))"; break;
+        case OP_CEIL: r = "gx_B(ceil(" + asD(x) + "))"; break;
+        case OP_SIN: r = "gx_B(sin(" + asD(x) + "))"; break;
+        case OP_COS: r = "gx_B(cos(" + asD(x) + "))"; break;
+        case OP_ASIN: r = "gx_B(asin(" + asD(x) + "))"; break;
+        case OP_ACOS: r = "gx_B(acos(" + asD(x) + "))"; break;
+        case OP_TAN: r = "gx_B(tan(" + asD(x) + "))"; break;
+        case OP_COTAN: r = "gx_B(cos(" + asD(x) + ") / sin(" + asD(x) + "))"; break;
+        case OP_ATAN: r = "gx_B(atan(" + asD(x) + "))"; break;
+        case OP_LN: r = "gx_B(log(" + asD(x) + "))"; break;
+        case OP_LOG10: r = "gx_B(log10(" + asD(x) + "))"; break;
+        case OP_EXP: r = "gx_B(exp(" + asD(x) + "))"; break;
+        case OP_ABS:
+          r = lf ? "gx_B(fabs(gx_D(" + X + ")))" : "((i64)(" + X + ") < 0LL ? 0ull - (" + X + ") : (" + X + "))";
+          break;
+        case OP_NOT: r = "(u64)(!" + nz(x) + ")"; break;
+        case OP_IS_TRUE: r = "(u64)" + asI(x); break;
+        case OP_YEAR: case OP_MONTH: case OP_DAY: case OP_DAYOFWEEK: case OP_HOUR: case OP_MINUTE: case OP_SECOND: {
+          if (!is_timestamp(lt)) { r = "0ull"; break; }
+          const int which = op == OP_YEAR ? 0 : op == OP_MONTH ? 1 : op == OP_DAY ? 2 : op == OP_DAYOFWEEK ? 3
+                          : op == OP_HOUR ? 4 : op == OP_MINUTE ? 5 : 6;
+          const long long per_day = lt == TIMESTAMP_DAYS ? 1LL : 86400000000000LL / ns_per_unit(lt);
+          const std::string cnt = lt == TIMESTAMP_DAYS ? "gx_days32((i64)(" + X + "))" : "(i64)(" + X + ")";
+          r = "(u64)gx_extract(" + cnt + ", " + std::to_string(per_day) + "LL, " + std::to_string(which) + ")";
+          break;
+        }
+        case OP_CAST_TINYINT: case OP_CAST_SMALLINT: case OP_CAST_INTEGER: case OP_CAST_BIGINT:
+          r = "(u64)" + asI(x);
+          break;
+        case OP_CAST_FLOAT: case OP_CAST_DOUBLE: r = "gx_B(" + asD(x) + ")"; break;
+        case OP_CAST_DATE: {
+          long long div = lt == TIMESTAMP_SECONDS ? 86400LL : lt == TIMESTAMP_MILLISECONDS ? 86400000LL
+                        : lt == TIMESTAMP_MICROSECONDS ? 86400000000LL : lt == TIMESTAMP_NANOSECONDS ? 86400000000000LL : 1;
+          r = div == 1 ? "(u64)(i64)(int)" + asI(x) : "(u64)(i64)(int)(" + asI(x) + " / " + std::to_string(div) + "LL)";
+          break;
+        }
+        case OP_CAST_TIMESTAMP_SECONDS: case OP_CAST_TIMESTAMP_MILLISECONDS: case OP_CAST_TIMESTAMP_MICROSECONDS:
+        case OP_CAST_TIMESTAMP:
+          if (is_timestamp(lt)) {
+            const std::string cnt = lt == TIMESTAMP_DAYS ? "(u64)gx_days32(" + asI(x) + ")" : "(u64)" + asI(x);
+            r = "(" + cnt + " * " + std::to_string(ns_per_unit(lt)) + "ull)";
+          } else {
+            r = "(u64)" + asI(x);
+          }
+          break;
+        default: fail(GX_ERR_UNSUPPORTED, "no code for unary operator");
+      }
+      vv = always_valid ? "true" : XV;
+      if (!always_valid && n.exact_null) r = "(" + vv + " ? " + r + " : 0ull)";
+      o << ind << b << " = " << r << ";\n" << ind << v << " = " << vv << ";\n";
+      return;
+    }
+    // binary
+    const int x = n.a, y = n.b;
+    const bool lf = kind_f(x), rf = kind_f(y), anyf = lf || rf;
+    const int lt = p_.nodes[x].ktype, rt = p_.nodes[y].ktype;
+    const std::string X = B(x), Y = B(y), XV = V(x), YV = V(y);
+    switch (op) {
+      case OP_MAGIC_IF_NOT: {
+        const std::string cond = "(" + XV + " && " + nz(x) + ")";
+        o << ind << "{ const bool c_ = " << cond << ";\n";
+        o << ind << "  " << b << " = c_ ? " << Y << " : " << (rf ? "gx_B(GX_MAGIC_D)" : "(u64)GX_MAGIC_I")
+          << ";\n";
+        o << ind << "  " << v << " = c_ ? " << YV << " : false; }\n";
+        return;
+      }
+      case OP_FIRST_NON_MAGIC: {
+        const std::string magic = lf ? "(gx_D(" + X + ") == GX_MAGIC_D)" : "((i64)(" + X + ") == GX_MAGIC_I)";
+        o << ind << "{ const bool m_ = " << magic << ";\n";
+        o << ind << "  " << b << " = m_ ? " << Y << " : " << X << ";\n";
+        o << ind << "  " << v << " = m_ ? " << YV << " : " << XV << "; }\n";
+        return;
+      }
+      case OP_OR:
+        o << ind << b << " = (" << XV << " && " << YV << ") ? (u64)(" << nz(x) << " || " << nz(y) << ") : (" << XV
+          << " ? " << X << " : (" << YV << " ? " << Y << " : 0ull));\n";
+        o << ind << v << " = (" << XV << " && " << YV << ") || (" << XV << " ? " << nz(x) << " : " << YV << ");\n";
+        return;
+      case OP_IS_NOT_DISTINCT_FROM: {
+        const std::string eq = anyf ? "(" + asD(x) + " == " + asD(y) + ")" : "(" + X + " == " + Y + ")";
+        o << ind << b << " = (u64)((!" << XV << " && !" << YV << ") || (" << XV << " && " << YV << " && " << eq
+          << "));\n";
+        o << ind << v << " = true;\n";
+        return;
+      }
+      default: break;
+    }
+    vv = "(" + XV + " && " + YV + ")";
+    const bool ts_cmp = is_timestamp(lt) && is_timestamp(rt);
+    auto cmp = [&](const char* opstr) -> std::string {
+      if (ts_cmp) {
+        auto to_ns = [&](int id, int t) {
+          const std::string cnt = t == TIMESTAMP_DAYS ? "(u64)gx_days32((i64)(" + B(id) + "))" : "(u64)(" + B(id) + ")";
+          return "(i64)(" + cnt + " * " + std::to_string(ns_per_unit(t)) + "ull)";
+        };
+        return std::string("(u64)(") + to_ns(x, lt) + " " + opstr + " " + to_ns(y, rt) + ")";
+      }
+      if (anyf) return std::string("(u64)(") + asD(x) + " " + opstr + " " + asD(y) + ")";
+      return std::string("(u64)((i64)(") + X + ") " + opstr + " (i64)(" + Y + "))";
+    };
+    switch (op) {
+      case OP_AND: r = "(u64)(" + nz(x) + " && " + nz(y) + ")"; break;
+      case OP_ADD: r = anyf ? "gx_B(" + asD(x) + " + " + asD(y) + ")" : "(" + X + " + " + Y + ")"; break;
+      case OP_SUB: r = anyf ? "gx_B(" + asD(x) + " - " + asD(y) + ")" : "(" + X + " - " + Y + ")"; break;
+      case OP_MUL: r = anyf ? "gx_B(" + asD(x) + " * " + asD(y) + ")" : "(" + X + " * " + Y + ")"; break;
+      case OP_DIV:
+        r = anyf ? "gx_B(" + asD(x) + " / " + asD(y) + ")" : "gx_div_ii(" + X + ", " + Y + ")";
+        vv = "(" + vv + " && " + (rf ? "gx_D(" + Y + ") != 0.0" : "(i64)(" + Y + ") != 0LL") + ")";
+        break;
+      case OP_MOD:
+        if (anyf) {
+          r = "gx_B(fmod(" + asD(x) + ", " + asD(y) + "))";
+        } else {
+          r = "gx_mod_ii(" + X + ", " + Y + ")";
+          vv = "(" + vv + " && (i64)(" + Y + ") != 0LL)";
+        }
+        break;
+      case OP_POW: r = "gx_B(pow(" + asD(x) + ", " + asD(y) + "))"; break;
+      case OP_ROUND: r = "gx_B(gx_round_to(" + asD(x) + ", " + asD(y) + "))"; break;
+      case OP_EQ: r = cmp("=="); break;
+      case OP_NE: r = cmp("!="); break;
+      case OP_LT: r = cmp("<"); break;
+      case OP_GT: r = cmp(">"); break;
+      case OP_LE: r = cmp("<="); break;
+      case OP_GE: r = cmp(">="); break;
+      default: fail(GX_ERR_UNSUPPORTED, "no code for binary operator");
+    }
+    if (n.exact_null) {
+      o << ind << v << " = " << vv << ";\n";
+      o << ind << b << " = " << v << " ? " << r << " : 0ull;\n";
+    } else {
+      o << ind << b << " = " << r << ";\n" << ind << v << " = " << vv << ";\n";
+    }
+  }
+
+  // ids of OP / COL nodes reachable from roots, ascending (topological)
+  std::vector<int> cone(const std::vector<int>& roots) const {
+    std::set<int> seen;
+    std::function<void(int)> go = [&](int id) {
+      if (id < 0 || seen.count(id)) return;
+      seen.insert(id);
+      const Node& n = p_.nodes[id];
+      if (n.kind == Node::OP) { go(n.a); go(n.b); }
+    };
+    for (int r : roots) go(r);
+    std::vector<int> v;
+    for (int id : seen)
+      if (p_.nodes[id].kind != Node::LIT) v.push_back(id);
+    return v;
+  }
+
+  void decl(std::ostringstream& o, const std::vector<int>& ids, const std::string& ind) const {
+    for (int id : ids) o << ind << "u64 b" << id << "[GX_V]; bool v" << id << "[GX_V];\n";
+  }
+
+  // keep expression of conjunct c (index into p_.conjuncts) for slot k
+  std::string conj_keep(int cid) const {
+    if (cid < 0) return "true";
+    const Node& n = p_.nodes[cid];
+    if (n.kind == Node::LIT) return (n.lit_valid && n.lit_bits != 0) ? "inr" : "false";
+    if (p_.conjuncts.size() == 1 && cid == p_.predicate)  // the root itself: BOOL8 column semantics
+      return "(" + V(cid) + " && " + B(cid) + " != 0ull)";
+    return "(" + V(cid) + " && " + nz(cid) + ")";
+  }
+
+  // predicate phase: fills keep bits bal[k]; with short-circuit, conjuncts are
+  // evaluated in cfg order and later conjuncts skipped for all-dead warps
+  void emit_predicate(std::ostringstream& o, const std::string& ind) const {
+    std::vector<int> order;
+    if (!cfg_.conjunct_order.empty()) {
+      for (int i : cfg_.conjunct_order) order.push_back(p_.conjuncts.at(i));
+    } else {
+      order = p_.conjuncts;
+    }
+    o << ind << "bool alive[GX_V];\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) alive[k] = (w0 + k) * 32 + lane < a.n;\n";
+    std::set<int> done;
+    if (!cfg_.short_circuit) {
+      // fixed order: evaluate every conjunct for every row
+      o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
+      o << ind << "  const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+      for (int id : cone(order))
+        emit_node(o, id, ind + "  ");
+      std::string keep = "inr";
+      for (int c : order) keep += " && " + conj_keep(c);
+      o << ind << "  alive[k] = " << keep << ";\n";
+      o << ind << "}\n";
+      return;
+    }
+    o << ind << "bool any_alive = true;\n";
+    for (size_t j = 0; j < order.size(); j++) {
+      std::vector<int> ids;
+      for (int id : cone({order[j]}))
+        if (!done.count(id)) ids.push_back(id);
+      o << ind << "if (any_alive) {\n";
+      o << ind << "  u32 any_ = 0;\n";
+      o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) {\n";
+      o << ind << "    const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+      for (int id : ids) emit_node(o, id, ind + "    ");
+      o << ind << "    alive[k] = alive[k] && " << conj_keep(order[j]) << ";\n";
+      o << ind << "    any_ |= __ballot_sync(GX_FULL, alive[k]);\n";
+      o << ind << "  }\n";
+      o << ind << "  any_alive = any_ != 0u;\n";
+      o << ind << "}\n";
+      for (int id : ids) done.insert(id);
+    }
+  }
+
+  std::vector<int> predicate_cone() const { return p_.has_filter() ? cone(p_.conjuncts) : std::vector<int>{}; }
+
+  std::vector<int> output_roots() const {
+    std::vector<int> r;
+    for (const auto& o : p_.outputs)
+      if (o.kind == OutSpec::NODE) r.push_back(o.node);
+    return r;
+  }
+
+  const Plan& p_;
+  const KernelConfig& cfg_;
+};
+
+void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
+  o << "#define GX_V " << cfg.words << "\n#define GX_WARPS " << cfg.warps << "\n";
+  o << "#define GX_TILE_WORDS (GX_WARPS * GX_V)\n";
+  o << "#define GX_MAX_COLS " << GX_MAX_COLS << "\n#define GX_MAX_OUTS " << GX_MAX_OUTS << "\n";
+  o << "struct GxArgs {\n"
+       "  const void* in_data[GX_MAX_COLS]; const u32* in_mask[GX_MAX_COLS]; i64 in_off[GX_MAX_COLS];\n"
+       "  void* out_data[GX_MAX_OUTS]; u32* out_mask[GX_MAX_OUTS];\n"
+       "  i64 n; i64 capacity; u64* tile_status; unsigned long long* tile_counter; unsigned long long* out_count;\n"
+       "  int* err; u64 seed;\n};\n";
+}
+
+// phase 2 of the filter kernels: projections for the kept rows of each word,
+// written at positions pos.. (warp-uniform), plus validity bit streams
+void emit_filter_writes(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
+                        const std::string& ind) {
+  std::vector<int> proj = g.cone(g.output_roots());
+  std::set<int> have(pred_ids.begin(), pred_ids.end());
+  std::vector<int> fresh;
+  for (int id : proj)
+    if (!have.count(id)) fresh.push_back(id);
+  g.decl(o, fresh, ind);
+  o << ind << "GxBitWriter bw_[" << p.outputs.size() << "];\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << p.outputs.size() << "; j++) bw_[j].init((i64)pos);\n";
+  o << ind << "const i64 cap_words = (a.capacity + 31) >> 5;\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
+  o << ind << "  const u32 bk = bal[k];\n";
+  o << ind << "  if (bk == 0u) continue;\n";
+  o << ind << "  const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+  o << ind << "  const bool keep = (bk >> lane) & 1u;\n";
+  o << ind << "  const i64 orow = (i64)pos + __popc(bk & ((1u << lane) - 1u)); (void)orow;\n";
+  for (int id : fresh) g.emit_node(o, id, ind + "  ");
+  o << ind << "  const bool wr = keep && orow < a.capacity;\n";
+  o << ind << "  const int nb = __popc(bk);\n";
+  o << ind << "  const int q = (int)(orow - (i64)pos);\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    const OutSpec& os = p.outputs[j];
+    std::string vexpr;
+    if (os.kind == OutSpec::NODE) {
+      o << ind << "  if (wr) " << store_stmt(os.type, "a.out_data[" + std::to_string(j) + "]", "orow", g.B(os.node))
+        << "\n";
+      vexpr = g.V(os.node);
+    } else if (os.kind == OutSpec::COPY) {
+      const int c = os.col;
+      const std::string rt = raw_type(p.schema[c]);
+      o << ind << "  if (wr) ((" << rt << "*)a.out_data[" << j << "])[orow] = __ldcs((const " << rt << "*)a.in_data[" << c
+        << "] + a.in_off[" << c << "] + row);\n";
+      vexpr = p.nullable[c] ? "gx_valid(a.in_mask[" + std::to_string(c) + "], a.in_off[" + std::to_string(c) + "] + row)"
+                            : "true";
+    } else {
+      continue;  // broadcast outputs are filled after the launch
+    }
+    o << ind << "  { const u32 vb_ = __reduce_or_sync(GX_FULL, (keep && " << vexpr << ") ? (1u << (q & 31)) : 0u);\n";
+    o << ind << "    if (bw_[" << j << "].word < cap_words) bw_[" << j << "].append(a.out_mask[" << j
+      << "], vb_, nb); else { bw_[" << j << "].fill = 0; } }\n";
+  }
+  o << ind << "  pos += (u64)nb;\n";
+  o << ind << "}\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    if (p.outputs[j].kind == OutSpec::BROADCAST) continue;
+    o << ind << "if (bw_[" << j << "].word < cap_words) bw_[" << j << "].flush(a.out_mask[" << j << "]);\n";
+  }
+}
+
+}  // namespace
+
+std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg, const std::string& name) {
+  Gen g(p, cfg);
+  std::ostringstream o;
+  emit_prelude(o, cfg);
+  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name << "(const GxArgs a) {\n";
+  o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
+  o << "  const i64 nwords = (a.n + 31) >> 5;\n";
+  if (kind == KernelKind::PROJECT) {
+    std::vector<int> ids = g.cone(g.output_roots());
+    o << "  for (i64 w0 = ((i64)blockIdx.x * GX_WARPS + warp) * GX_V; w0 < nwords;"
+         " w0 += (i64)gridDim.x * GX_WARPS * GX_V) {\n";
+    g.decl(o, ids, "    ");
+    o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) {\n";
+    o << "      const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+    o << "      const i64 orow = row; (void)orow;\n";
+    for (int id : ids) g.emit_node(o, id, "      ");
+    for (size_t j = 0; j < p.outputs.size(); j++) {
+      const OutSpec& os = p.outputs[j];
+      if (os.kind != OutSpec::NODE) continue;
+      o << "      if (inr) " << store_stmt(os.type, "a.out_data[" + std::to_string(j) + "]", "row", g.B(os.node)) << "\n";
+      o << "      { const u32 vb_ = __ballot_sync(GX_FULL, inr && " << g.V(os.node) << ");\n";
+      o << "        if (lane == 0 && w0 + k < nwords) a.out_mask[" << j << "][w0 + k] = vb_; }\n";
+    }
+    o << "    }\n  }\n}\n";
+    return o.str();
+  }
+
+  const std::vector<int> pred_ids = g.predicate_cone();
+  o << "  __shared__ unsigned long long s_tile;\n";
+  o << "  __shared__ u64 s_w[GX_WARPS];\n";
+  o << "  const i64 ntiles = (nwords + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
+  if (kind == KernelKind::FUSED_FILTER) {
+    o << "  while (true) {\n";
+    o << "    if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1ull);\n";
+    o << "    __syncthreads();\n";
+    o << "    const i64 tile = (i64)s_tile;\n";
+    o << "    if (tile >= ntiles) break;\n";
+  } else {
+    o << "  for (i64 tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {\n";
+  }
+  o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  g.decl(o, pred_ids, "    ");
+  g.emit_predicate(o, "    ");
+  o << "    u32 bal[GX_V]; u32 wcnt = 0;\n";
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) { bal[k] = __ballot_sync(GX_FULL, alive[k]); wcnt += __popc(bal[k]); }\n";
+  // per-warp exclusive offsets within the tile
+  o << "    if (lane == 0) s_w[warp] = wcnt;\n";
+  o << "    __syncthreads();\n";
+  o << "    if (warp == 0) {\n";
+  o << "      u64 c = lane < GX_WARPS ? s_w[lane] : 0ull; u64 incl = c;\n";
+  o << "      #pragma unroll\n      for (int d = 1; d < 32; d <<= 1) { u64 t = __shfl_up_sync(GX_FULL, incl, d); if (lane >= d) incl += t; }\n";
+  o << "      const u64 total = __shfl_sync(GX_FULL, incl, 31);\n";
+  if (kind == KernelKind::FUSED_FILTER) {
+    o << "      const u64 excl_tile = gx_lookback(a.tile_status, tile, total, a.err, 1u << 22);\n";
+    o << "      if (tile == ntiles - 1 && lane == 0 && excl_tile != ~0ull) *a.out_count = excl_tile + total;\n";
+  } else if (kind == KernelKind::COUNT_FILTER) {
+    o << "      if (lane == 0) a.tile_status[tile] = total;\n";
+    o << "      const u64 excl_tile = 0ull;\n";
+  } else {
+    o << "      const u64 excl_tile = a.tile_status[tile];\n";
+  }
+  o << "      if (lane < GX_WARPS) s_w[lane] = excl_tile == ~0ull ? ~0ull : excl_tile + incl - c;\n";
+  o << "    }\n";
+  o << "    __syncthreads();\n";
+  if (kind != KernelKind::COUNT_FILTER) {
+    o << "    u64 pos = s_w[warp];\n";
+    o << "    if (pos == ~0ull) break;\n";  // look-back gave up: error already recorded
+    o << "    if (wcnt != 0u) {\n";
+    emit_filter_writes(o, g, p, pred_ids, "      ");
+    o << "    }\n";
+  }
+  o << "    __syncthreads();\n";  // s_tile / s_w reuse by the next tile
+  o << "  }\n}\n";
+  return o.str();
+}
+
+}  // namespace gx

@@ -1,0 +1,107 @@
+// plan.h -- expression DAG, planning and CUDA code generation.
+//
+// The reference encodes each expression separately into (left, right, out, op)
+// slot arrays with first-free slot reuse and no sharing
+// (engine/src/Interpreter/interpreter_cpp.cu:274-438), then interprets that list
+// per row.  Here all expressions of one call (filter condition + projections)
+// become one DAG with hash-consed common sub-expressions; the DAG is emitted as
+// straight-line CUDA in SSA form (the CUDA compiler allocates registers), so the
+// kernel never dispatches on operator or type at run time.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "frontend.h"
+#include "gx_common.h"
+
+namespace gx {
+
+struct Node {
+  enum Kind { COL, LIT, OP } kind = OP;
+  Op op = OP_NONE;
+  int col = -1;
+  int lit_type = EMPTY;
+  bool lit_valid = false;
+  uint64_t lit_bits = 0;
+  int vtype = EMPTY;
+  int ktype = EMPTY;
+  int a = -1, b = -1;        // operand node ids
+  int rand_id = -1;          // RAND ordinal (post-order within its expression group)
+  bool rand_out_row = false; // RAND keyed by output (compacted) row instead of input row
+  bool exact_null = false;   // data under NULL is observable (feeds CASE's magic test)
+};
+
+struct OutSpec {
+  enum Kind { NODE, COPY, BROADCAST } kind = NODE;
+  int node = -1;       // NODE
+  int col = -1;        // COPY
+  int type = EMPTY;    // output column type
+  uint64_t lit_bits = 0;
+  bool lit_valid = false;
+  // BROADCAST: the element bits of the literal in the output type
+  uint64_t lit_bits_as_element() const;
+};
+
+struct KernelConfig {
+  int warps = 8;           // warps per CTA
+  int words = 2;           // 32-row words per warp per step
+  bool short_circuit = false;
+  std::vector<int> conjunct_order;  // indices into Plan::conjuncts
+};
+
+struct Plan {
+  std::vector<int> schema;
+  std::vector<bool> nullable;
+  std::vector<Node> nodes;
+  int predicate = -1;                 // filter condition node (-1: no filter)
+  std::vector<int> conjuncts;         // top-level AND operands of the condition
+  std::vector<OutSpec> outputs;
+  bool filter_copies_all = false;     // process_filter: outputs are every input column
+  uint64_t rand_seed = 0;
+
+  bool has_filter() const { return predicate >= 0; }
+  // nodes computed per row by the kernels (outputs of kind NODE + predicate)
+  bool needs_kernel() const;
+};
+
+// Builds a plan.  condition may be empty (no filter).  When filter_all is set the
+// outputs are COPY outputs of every input column (process_filter).  RAND()
+// calls in the expressions are numbered from first_rand_id (post-order), so a
+// long expression list split over several plans keeps one numbering;
+// *rand_count (optional) receives how many the expressions used.
+Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullable, const std::string& condition,
+                const std::vector<std::string>& expressions, bool filter_all, bool rand_by_output_row,
+                int first_rand_id = 0, int* rand_count = nullptr);
+
+// Outputs per plan kernel; longer expression lists are split into several
+// plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
+constexpr int GX_OUTPUTS_PER_KERNEL = 32;
+
+enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER };
+
+// CUDA source of one plan kernel.  The kernel is named by `name`.
+std::string generate_kernel(const Plan& plan, KernelKind kind, const KernelConfig& cfg, const std::string& name);
+
+// Parameter block layout shared by generated kernels and the host launcher.
+constexpr int GX_MAX_COLS = 64;
+constexpr int GX_MAX_OUTS = 64;
+
+struct KernelArgs {
+  const void* in_data[GX_MAX_COLS];
+  const uint32_t* in_mask[GX_MAX_COLS];
+  int64_t in_off[GX_MAX_COLS];
+  void* out_data[GX_MAX_OUTS];
+  uint32_t* out_mask[GX_MAX_OUTS];
+  int64_t n;                 // input rows
+  int64_t capacity;          // output rows available (filter kernels)
+  uint64_t* tile_status;     // FUSED: look-back status; COUNT/WRITE: per-tile counts / offsets
+  unsigned long long* tile_counter;
+  unsigned long long* out_count;
+  int* err;
+  uint64_t seed;
+};
+
+}  // namespace gx

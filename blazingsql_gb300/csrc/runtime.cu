@@ -1,0 +1,471 @@
+// runtime.cu -- plan execution and the library's precompiled helper kernels.
+#include "runtime.h"
+
+#include <atomic>
+#include <cstring>
+#include <unordered_map>
+
+#include "driver.h"
+
+namespace gx {
+
+// ------------------------------------------------------------------ helpers
+void check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  cudaGetLastError();  // clear sticky-free errors
+  fail(e == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+std::atomic<bool> g_timing{false};
+std::atomic<int64_t> g_launches{0};
+thread_local double t_kernel_ms = 0.0;
+std::atomic<int> g_fail_countdown{0};
+std::mutex g_pool_mu;
+std::unordered_map<int, bool> g_pool_ready;
+
+void ensure_pool() {
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (g_pool_ready[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;  // keep freed blocks cached in the pool
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  g_pool_ready[dev] = true;
+}
+}  // namespace
+
+void debug_fail_allocation(int n) { g_fail_countdown.store(n); }
+
+void set_kernel_timing(bool on) { g_timing.store(on); }
+double kernel_ms(bool reset) {
+  const double v = t_kernel_ms;
+  if (reset) t_kernel_ms = 0.0;
+  return v;
+}
+int64_t launch_count() { return g_launches.load(); }
+
+void* dev_alloc(size_t bytes, cudaStream_t s) {
+  int c = g_fail_countdown.load();
+  while (c > 0) {
+    if (g_fail_countdown.compare_exchange_weak(c, c - 1)) {
+      if (c == 1) fail(GX_ERR_OOM, "injected allocation failure");
+      break;
+    }
+  }
+  ensure_pool();
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes ? bytes : 64, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA,
+         std::string("cudaMallocAsync(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+  }
+  return p;
+}
+
+void dev_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+std::vector<ColumnView> to_views(const gx_column_view* cols, int n) {
+  if (n < 0 || (n > 0 && !cols)) fail(GX_ERR_INVALID, "null column array");
+  std::vector<ColumnView> v;
+  for (int i = 0; i < n; i++) {
+    const gx_column_view& c = cols[i];
+    if (type_size(c.type_id) == 0) fail(GX_ERR_UNSUPPORTED, "unsupported column type " + std::to_string(c.type_id));
+    if (c.size < 0 || c.offset < 0) fail(GX_ERR_INVALID, "negative column size/offset");
+    if (c.size > 0 && !c.data) fail(GX_ERR_INVALID, "column data pointer is null");
+    if (i > 0 && c.size != cols[0].size) fail(GX_ERR_INVALID, "columns of one table must have equal sizes");
+    v.push_back({c.type_id, c.data, c.null_mask, c.offset, c.size});
+  }
+  return v;
+}
+
+static int64_t mask_words_padded(int64_t rows) {
+  int64_t w = (rows + 31) / 32;
+  w = (w + 15) / 16 * 16;
+  return w < 16 ? 16 : w;
+}
+
+gx_column alloc_column(int type, int64_t capacity, cudaStream_t s) {
+  gx_column c{};
+  c.type_id = type;
+  c.capacity = capacity;
+  c.size = 0;
+  size_t bytes = (size_t)capacity * type_size(type);
+  bytes = (bytes + 63) / 64 * 64;
+  c.data = dev_alloc(bytes ? bytes : 64, s);
+  try {
+    c.null_mask = (uint32_t*)dev_alloc((size_t)mask_words_padded(capacity) * 4, s);
+  } catch (...) {
+    dev_free(c.data, s);
+    throw;
+  }
+  return c;
+}
+
+void free_column(gx_column& c, cudaStream_t s) {
+  dev_free(c.data, s);
+  dev_free(c.null_mask, s);
+  c.data = nullptr;
+  c.null_mask = nullptr;
+}
+
+// ---------------------------------------------------- precompiled kernels
+__global__ void k_copy_mask(const uint32_t* __restrict__ src, int64_t src_bit, uint32_t* __restrict__ dst,
+                            int64_t nrows, int64_t dst_words) {
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < dst_words; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row0 = w * 32;
+    uint32_t v = 0;
+    if (row0 < nrows) {
+      if (src == nullptr) {
+        v = 0xffffffffu;
+      } else {
+        const int64_t b = src_bit + row0;
+        const int sh = (int)(b & 31);
+        const int64_t i = b >> 5;
+        const uint32_t lo = src[i];
+        // the high word is read only if bits of it are needed by a row < nrows
+        const uint32_t hi = (sh != 0 && row0 + (32 - sh) < nrows) ? src[i + 1] : 0u;
+        v = sh ? __funnelshift_r(lo, hi, sh) : lo;
+      }
+      const int64_t left = nrows - row0;
+      if (left < 32) v &= (1u << left) - 1u;
+    }
+    dst[w] = v;
+  }
+}
+
+__global__ void k_fill(void* dst, int width, uint64_t value, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    switch (width) {
+      case 1: ((uint8_t*)dst)[i] = (uint8_t)value; break;
+      case 2: ((uint16_t*)dst)[i] = (uint16_t)value; break;
+      case 4: ((uint32_t*)dst)[i] = (uint32_t)value; break;
+      default: ((uint64_t*)dst)[i] = value; break;
+    }
+  }
+}
+
+__global__ void k_fill_mask(uint32_t* dst, int64_t nrows, bool valid, int64_t dst_words) {
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < dst_words; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row0 = w * 32;
+    uint32_t v = 0;
+    if (valid && row0 < nrows) v = (nrows - row0 >= 32) ? 0xffffffffu : ((1u << (nrows - row0)) - 1u);
+    dst[w] = v;
+  }
+}
+
+// Exclusive scan of per-tile counts in place (one CTA of 1024 threads walks
+// the array in chunks); *total receives the sum.
+__global__ void __launch_bounds__(1024) k_scan_tiles(uint64_t* counts, int64_t n, unsigned long long* total) {
+  __shared__ uint64_t s_warp[32];
+  __shared__ uint64_t s_carry;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) s_carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < n; base += 1024) {
+    const int64_t i = base + t;
+    const uint64_t v = i < n ? counts[i] : 0ull;
+    uint64_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint64_t w = s_warp[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= d) w += y;
+      }
+      s_warp[lane] = w;
+    }
+    __syncthreads();
+    const uint64_t carry = s_carry;
+    const uint64_t incl = x + (warp > 0 ? s_warp[warp - 1] : 0ull);
+    if (i < n) counts[i] = carry + incl - v;
+    __syncthreads();
+    if (t == 1023) s_carry = carry + incl;
+    __syncthreads();
+  }
+  if (t == 0) *total = s_carry;
+}
+
+static int grid_for(int64_t items, int threads) {
+  int64_t g = (items + threads - 1) / threads;
+  int64_t cap = (int64_t)device_sm_count() * 8;
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+void launch_copy_mask(const uint32_t* src, int64_t src_bit, uint32_t* dst, int64_t nrows, int64_t dst_words,
+                      cudaStream_t s) {
+  k_copy_mask<<<grid_for(dst_words, 256), 256, 0, s>>>(src, src_bit, dst, nrows, dst_words);
+  g_launches.fetch_add(1);
+  check_cuda(cudaGetLastError(), "k_copy_mask launch");
+}
+
+void launch_fill(void* dst, int width, uint64_t value, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_fill<<<grid_for(n, 256), 256, 0, s>>>(dst, width, value, n);
+  g_launches.fetch_add(1);
+  check_cuda(cudaGetLastError(), "k_fill launch");
+}
+
+void launch_fill_mask(uint32_t* dst, int64_t nrows, bool valid, int64_t dst_words, cudaStream_t s) {
+  k_fill_mask<<<grid_for(dst_words, 256), 256, 0, s>>>(dst, nrows, valid, dst_words);
+  g_launches.fetch_add(1);
+  check_cuda(cudaGetLastError(), "k_fill_mask launch");
+}
+
+void launch_scan_tiles(uint64_t* counts, int64_t n, unsigned long long* total, cudaStream_t s) {
+  k_scan_tiles<<<1, 1024, 0, s>>>(counts, n, total);
+  g_launches.fetch_add(1);
+  check_cuda(cudaGetLastError(), "k_scan_tiles launch");
+}
+
+// ------------------------------------------------------------ plan execution
+static const char* kind_name(KernelKind k) {
+  switch (k) {
+    case KernelKind::PROJECT: return "gx_project";
+    case KernelKind::FUSED_FILTER: return "gx_filter_fused";
+    case KernelKind::COUNT_FILTER: return "gx_filter_count";
+    default: return "gx_filter_write";
+  }
+}
+
+JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable) const {
+  Plan p = plan_;
+  p.nullable = nullable;
+  const std::string name = kind_name(kind);
+  const std::string src = generate_kernel(p, kind, cfg_, name);
+  return jit_get(src, name, cfg_.warps * 32);
+}
+
+// Launches a plan kernel; with timing on, brackets it with events on `s`
+// (timed=true for the call's main kernel) and adds its duration to the
+// calling thread's total.
+static void launch(const JitKernel& k, int grid, cudaStream_t s, KernelArgs& args, bool timed = false) {
+  void* params[] = {&args};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool tm = timed && g_timing.load();
+  if (tm) {
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    check_cuda(cudaEventRecord(e0, s), "event record");
+  }
+  CUresult r = driver().LaunchKernel(k.fn, (unsigned)grid, 1, 1, (unsigned)k.block_threads, 1, 1, 0, (CUstream)s,
+                                     params, nullptr);
+  if (r != CUDA_SUCCESS) fail(GX_ERR_CUDA, std::string("cuLaunchKernel: ") + driver_error_string(r));
+  g_launches.fetch_add(1);
+  if (tm) {
+    check_cuda(cudaEventRecord(e1, s), "event record");
+    check_cuda(cudaEventSynchronize(e1), "event sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    t_kernel_ms += ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+}
+
+static std::vector<bool> runtime_nullable(const Plan& p, const std::vector<ColumnView>& cols) {
+  std::vector<bool> nb(cols.size());
+  for (size_t i = 0; i < cols.size(); i++) nb[i] = cols[i].mask != nullptr;
+  (void)p;
+  return nb;
+}
+
+static void fill_args_inputs(KernelArgs& a, const std::vector<ColumnView>& cols) {
+  std::memset(&a, 0, sizeof a);
+  for (size_t i = 0; i < cols.size(); i++) {
+    a.in_data[i] = cols[i].data;
+    a.in_mask[i] = cols[i].mask;
+    a.in_off[i] = cols[i].offset;
+  }
+  a.n = cols.empty() ? 0 : cols[0].size;
+}
+
+void CompiledPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                           cudaStream_t s) const {
+  if (cols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < cols.size(); i++)
+    if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
+  const bool caller_bufs = !plan_.outputs.empty() && out[0].data != nullptr;
+  if (plan_.has_filter()) {
+    run_filter(cols, out, out_rows, caller_bufs, s);
+  } else {
+    run_project(cols, out, caller_bufs, s);
+    if (out_rows) *out_rows = cols.empty() ? 0 : cols[0].size;
+  }
+}
+
+void CompiledPlan::run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs,
+                               cudaStream_t s) const {
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const int nout = (int)plan_.outputs.size();
+  std::vector<gx_column> made;
+  try {
+    for (int j = 0; j < nout; j++) {
+      if (caller_bufs) {
+        if (out[j].capacity < n || !out[j].data || !out[j].null_mask) fail(GX_ERR_CAPACITY, "output buffer too small");
+        out[j].type_id = plan_.outputs[j].type;
+      } else {
+        out[j] = alloc_column(plan_.outputs[j].type, n, s);
+        made.push_back(out[j]);
+      }
+      out[j].size = n;
+    }
+    const int64_t words = mask_words_padded(n), nwords = (n + 31) / 32;
+    for (int j = 0; j < nout; j++) {
+      const OutSpec& o = plan_.outputs[j];
+      const int w = type_size(o.type);
+      if (o.kind == OutSpec::COPY) {
+        const ColumnView& c = cols[o.col];
+        if (n > 0)
+          check_cuda(cudaMemcpyAsync(out[j].data, (const char*)c.data + c.offset * w, (size_t)n * w,
+                                     cudaMemcpyDeviceToDevice, s), "copy column");
+        launch_copy_mask(c.mask, c.offset, out[j].null_mask, n, words, s);
+      } else if (o.kind == OutSpec::BROADCAST) {
+        launch_fill(out[j].data, w, o.lit_bits_as_element(), n, s);
+        launch_fill_mask(out[j].null_mask, n, o.lit_valid, words, s);
+      } else if (words > nwords) {
+        check_cuda(cudaMemsetAsync(out[j].null_mask + nwords, 0, (size_t)(words - nwords) * 4, s), "mask pad");
+      }
+    }
+    if (n > 0 && plan_.needs_kernel()) {
+      const JitKernel k = kernel(KernelKind::PROJECT, runtime_nullable(plan_, cols));
+      KernelArgs a;
+      fill_args_inputs(a, cols);
+      for (int j = 0; j < nout; j++) {
+        a.out_data[j] = out[j].data;
+        a.out_mask[j] = out[j].null_mask;
+      }
+      a.seed = plan_.rand_seed;
+      const int64_t steps = (nwords + cfg_.words * cfg_.warps - 1) / (cfg_.words * cfg_.warps);
+      int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
+      if (grid > steps) grid = steps;
+      last.grid = (int)grid;
+      last.block = k.block_threads;
+      last.regs = k.num_regs;
+      launch(k, (int)grid, s, a, true);
+    }
+  } catch (...) {
+    for (auto& c : made) free_column(c, s);
+    throw;
+  }
+}
+
+void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                              bool caller_bufs, cudaStream_t s) const {
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const int nout = (int)plan_.outputs.size();
+  const int64_t nwords = (n + 31) / 32;
+  const int64_t tile_words = (int64_t)cfg_.warps * cfg_.words;
+  const int64_t ntiles = (nwords + tile_words - 1) / tile_words;
+  std::vector<gx_column> made;
+  void* scratch = nullptr;
+  try {
+    if (n == 0) {
+      for (int j = 0; j < nout; j++) {
+        if (!caller_bufs) {
+          out[j] = alloc_column(plan_.outputs[j].type, 0, s);
+          made.push_back(out[j]);
+        }
+        out[j].size = 0;
+        launch_fill_mask(out[j].null_mask, 0, false, mask_words_padded(0), s);
+      }
+      if (out_rows) *out_rows = 0;
+      return;
+    }
+    // scratch: [0] tile counter, [1] out count, [2] err (int), [3] total, then per-tile status
+    const size_t sbytes = (size_t)(4 + ntiles) * 8;
+    scratch = dev_alloc(sbytes, s);
+    unsigned long long* hdr = (unsigned long long*)scratch;
+    uint64_t* status = (uint64_t*)scratch + 4;
+    check_cuda(cudaMemsetAsync(scratch, 0, sbytes, s), "scratch memset");
+    const std::vector<bool> nb = runtime_nullable(plan_, cols);
+    KernelArgs a;
+    fill_args_inputs(a, cols);
+    a.tile_status = status;
+    a.tile_counter = hdr + 0;
+    a.out_count = hdr + 1;
+    a.err = (int*)(hdr + 2);
+    a.seed = plan_.rand_seed;
+    unsigned long long host_hdr[4] = {0, 0, 0, 0};
+    int64_t capacity = n;
+    const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
+    if (two_pass) {
+      const JitKernel kc = kernel(KernelKind::COUNT_FILTER, nb);
+      int64_t grid = (int64_t)device_sm_count() * kc.max_blocks_per_sm;
+      if (grid > ntiles) grid = ntiles;
+      launch(kc, (int)grid, s, a, true);
+      launch_scan_tiles(status, ntiles, hdr + 3, s);
+      check_cuda(cudaMemcpyAsync(host_hdr, hdr, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+      check_cuda(cudaStreamSynchronize(s), "count sync");
+      capacity = (int64_t)host_hdr[3];
+    }
+    if (caller_bufs) {
+      for (int j = 0; j < nout; j++) {
+        if (!out[j].data || !out[j].null_mask) fail(GX_ERR_INVALID, "caller output buffer missing");
+        out[j].type_id = plan_.outputs[j].type;
+      }
+      capacity = out[0].capacity;
+      for (int j = 1; j < nout; j++) capacity = std::min<int64_t>(capacity, out[j].capacity);
+      if (two_pass && capacity < (int64_t)host_hdr[3]) {
+        if (out_rows) *out_rows = (int64_t)host_hdr[3];
+        fail(GX_ERR_CAPACITY, "output capacity too small");
+      }
+    } else {
+      for (int j = 0; j < nout; j++) {
+        out[j] = alloc_column(plan_.outputs[j].type, capacity, s);
+        made.push_back(out[j]);
+      }
+    }
+    for (int j = 0; j < nout; j++)
+      check_cuda(cudaMemsetAsync(out[j].null_mask, 0, (size_t)mask_words_padded(capacity) * 4, s), "mask zero");
+    for (int j = 0; j < nout; j++) {
+      a.out_data[j] = out[j].data;
+      a.out_mask[j] = out[j].null_mask;
+    }
+    a.capacity = capacity;
+    const JitKernel k = kernel(two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER, nb);
+    int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
+    if (grid > ntiles) grid = ntiles;
+    last.grid = (int)grid;
+    last.block = k.block_threads;
+    last.regs = k.num_regs;
+    last.tiles = ntiles;
+    launch(k, (int)grid, s, a, true);
+    check_cuda(cudaMemcpyAsync(host_hdr, hdr, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+    check_cuda(cudaStreamSynchronize(s), "filter sync");
+    if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+    const int64_t rows = two_pass ? (int64_t)host_hdr[3] : (int64_t)host_hdr[1];
+    if (out_rows) *out_rows = rows;
+    if (rows > capacity) fail(GX_ERR_CAPACITY, "output capacity too small");
+    for (int j = 0; j < nout; j++) {
+      out[j].size = rows;
+      const OutSpec& o = plan_.outputs[j];
+      if (o.kind == OutSpec::BROADCAST) {
+        launch_fill(out[j].data, type_size(o.type), o.lit_bits_as_element(), rows, s);
+        launch_fill_mask(out[j].null_mask, rows, o.lit_valid, mask_words_padded(capacity), s);
+      }
+    }
+    dev_free(scratch, s);
+    scratch = nullptr;
+  } catch (...) {
+    if (scratch) dev_free(scratch, s);
+    for (auto& c : made) free_column(c, s);
+    throw;
+  }
+}
+
+}  // namespace gx

@@ -1,0 +1,83 @@
+// runtime.h -- plan execution on the device: output allocation, kernel
+// launches, compaction bookkeeping.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "jit.h"
+#include "plan.h"
+
+namespace gx {
+
+struct ColumnView {
+  int type;
+  const void* data;
+  const uint32_t* mask;
+  int64_t offset;
+  int64_t size;
+};
+
+std::vector<ColumnView> to_views(const gx_column_view* cols, int n);
+
+// stream-ordered device allocation from the device's memory pool; failures
+// raise GX_ERR_OOM (retryable)
+void* dev_alloc(size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+void check_cuda(cudaError_t e, const char* what);
+// host-side fault injection for tests: fail the n-th next allocation (n >= 1)
+void debug_fail_allocation(int n);
+
+// allocates an output column holding `capacity` rows (data + padded mask)
+gx_column alloc_column(int type, int64_t capacity, cudaStream_t s);
+void free_column(gx_column& c, cudaStream_t s);
+
+struct ExecStats {
+  double kernel_ms = 0;      // not measured unless requested
+  int64_t tiles = 0;
+  int grid = 0;
+  int block = 0;
+  int regs = 0;
+};
+
+class CompiledPlan {
+ public:
+  CompiledPlan(Plan p, KernelConfig cfg, int mode) : plan_(std::move(p)), cfg_(std::move(cfg)), mode_(mode) {}
+
+  // Runs the plan over `cols`.  out must hold plan.outputs.size() entries.  If
+  // out[0].data is non-null, caller-supplied buffers are used (capacity rows).
+  void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const;
+
+  const Plan& plan() const { return plan_; }
+  const KernelConfig& config() const { return cfg_; }
+  int mode() const { return mode_; }
+  mutable ExecStats last;
+
+ private:
+  JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable) const;
+  void run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs, cudaStream_t s) const;
+  void run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, bool caller_bufs,
+                  cudaStream_t s) const;
+
+  Plan plan_;
+  KernelConfig cfg_;
+  int mode_;
+};
+
+// diagnostics: per-thread kernel timing and a global launch counter
+void set_kernel_timing(bool on);
+double kernel_ms(bool reset);
+int64_t launch_count();
+
+// launch helpers for precompiled kernels (runtime.cu)
+void launch_copy_mask(const uint32_t* src, int64_t src_bit, uint32_t* dst, int64_t nrows, int64_t dst_words,
+                      cudaStream_t s);
+void launch_fill(void* dst, int width, uint64_t value, int64_t n, cudaStream_t s);
+void launch_fill_mask(uint32_t* dst, int64_t nrows, bool valid, int64_t dst_words, cudaStream_t s);
+void launch_scan_tiles(uint64_t* counts, int64_t n, unsigned long long* total, cudaStream_t s);
+
+}  // namespace gx

@@ -1,0 +1,187 @@
+"""GPU evaluator vs the CPU oracle on the same seeded inputs (bit-exact for
+integer / boolean / validity / row order and FP64 arithmetic; transcendental
+outputs within 2 ulp)."""
+import numpy as np
+import pytest
+
+import blazingsql_gb300 as g
+from blazingsql_gb300 import _native as N
+from blazingsql_gb300 import workloads as W
+from blazingsql_gb300.types import HostColumn, TypeId as T, pack_validity
+from tests.helpers import GpuEngine, OracleEngine, assert_tables_equal, random_table
+
+pytestmark = pytest.mark.gpu
+
+# outputs computed through LN / EXP / POWER / SIN (CUDA vs glibc) get this many ulps
+TRANSCENDENTAL_ULPS = 2
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    return GpuEngine()
+
+
+@pytest.fixture(scope="module")
+def ora():
+    return OracleEngine(nthreads=8)
+
+
+SIZES = [1, 31, 32, 33, 1023, 1024, 4097, 100_003]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_c1_filter_project(gpu, ora, n):
+    cols = W.host_columns("c1", n, seed=11 + n)
+    got = gpu.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+    exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+    assert_tables_equal(got, exp, what=f"c1 n={n}")
+
+
+@pytest.mark.parametrize("n", [1, 33, 4097, 65_537])
+def test_c2_filter_project(gpu, ora, n):
+    cols = W.host_columns("c2", n, seed=2 + n)
+    got = gpu.filter_project(cols, W.C2_CONDITION, W.C2_PROJECTIONS)
+    exp = ora.filter_project(cols, W.C2_CONDITION, W.C2_PROJECTIONS)
+    assert_tables_equal(got[1:], exp[1:], what="c2 int64 output")
+    assert_tables_equal(got[:1], exp[:1], ulps=TRANSCENDENTAL_ULPS, what="c2 float64 output (LN/EXP)")
+
+
+@pytest.mark.parametrize("n", [1, 1000, 70_001])
+def test_c5_filter_project(gpu, ora, n):
+    cols = W.host_columns("c5", n, seed=5)
+    got = gpu.filter_project(cols, W.C5_CONDITION, W.C5_PROJECTIONS)
+    exp = ora.filter_project(cols, W.C5_CONDITION, W.C5_PROJECTIONS)
+    assert_tables_equal(got, exp, what="c5")
+
+
+@pytest.mark.parametrize("n", [0, 1, 32, 5000])
+def test_process_filter_all_columns(gpu, ora, n):
+    cols = W.host_columns("c2", n, seed=9) if n else [HostColumn(t, np.zeros(0, dtype=np.int64 if t != T.INT8 else np.int8))
+                                                        for t in (T.INT64, T.INT8)]
+    qp = "LogicalFilter(condition=[AND(IS NOT NULL($2), <=($4, 1996-12-31))])" if n else \
+        "LogicalFilter(condition=[<($0, 3)])"
+    assert_tables_equal(gpu.process_filter(cols, qp), ora.process_filter(cols, qp), what="process_filter")
+
+
+def test_evaluate_expressions_every_operator(gpu, ora):
+    rng = np.random.default_rng(7)
+    n = 20_000
+    cols = random_table(rng, n, [(T.INT64, -10**6, 10**6), (T.FLOAT64, 0.0, 50.0), (T.INT32, -5, 6),
+                                 (T.INT8, 0, 6), (T.TIMESTAMP_DAYS, -30000, 30000),
+                                 (T.TIMESTAMP_NANOSECONDS, -10**18, 10**18), (T.FLOAT32, 0.0, 3.0),
+                                 (T.BOOL8, 0, 2), (T.UINT16, 0, 60000)], null_frac=0.1)
+    exact = ["+($0, $2)", "-($0, $2)", "*($0, $2)", "/($0, $2)", "MOD($0, $2)", "/($1, $2)", "MOD($1, 3.5)",
+             "+($1, $6)", "*($6, $6)", "/($1, $6)", "ROUND($1, 2)", "ROUND($6)", "ROUND($1, -1)",
+             "FLOOR($1)", "CEIL($1)", "ABS($0)", "ABS($1)", "NOT($7)", "IS TRUE($7)", "IS NOT TRUE($2)",
+             "IS NOT FALSE($2)", "IS_NULL($3)", "IS_NOT_NULL($3)", "AND($7, >($0, 0))", "OR($7, <($1, 0.0))",
+             "OR(<($1, 0.0), $7)", "IS_NOT_DISTINCT_FROM($2, $3)", "=($0, $1)", "<>($2, $3)", "<($1, $6)",
+             ">=($0, 1000)", "<=($4, 1996-12-31)", ">($5, 2001-09-09 01:46:40)", "=($4, $5)",
+             "CASE(>($0, 0), $0, <($0, -500000), -(0, $0), null)", "CASE(IS_NULL($2), 1.5, $1)",
+             "CASE(IS NOT NULL($2), $2, $3)", "CAST($1):INTEGER", "CAST($1):BIGINT", "CAST($0):DOUBLE",
+             "CAST($6):DOUBLE", "CAST($0):TINYINT", "CAST($1):FLOAT", "CAST($4):TIMESTAMP", "CAST($5):DATE",
+             "CAST($0):DATE", "BL_YEAR($4)", "BL_MONTH($4)", "BL_DAY($4)", "BL_DOW($4)", "BL_YEAR($5)",
+             "BL_MONTH($5)", "BL_DAY($5)", "BL_HOUR($5)", "BL_MINUTE($5)", "BL_SECOND($5)", "BL_DOW($5)",
+             "+($8, $2)", "*($8, $8)", "MOD($8, 7)", "$3", "42", "2.5", "null:INTEGER",
+             "+(*($0, 3), CASE(IS NOT NULL($2), $2, 0))", "AND(OR($7, null), >($1, 10.0))"]
+    trans = ["LN(+(ABS($1), 1.0))", "EXP(/($1, 100.0))", "POWER($1, 2)", "POWER($1, 0.5)", "SIN($1)",
+             "COS($1)", "TAN(/($1, 100.0))", "ASIN(/($1, 1000.0))", "ACOS(/($1, 1000.0))", "ATAN($1)",
+             "COT(+($1, 0.5))", "LOG10(+(ABS($1), 1.0))"]
+    got = gpu.evaluate_expressions(cols, exact)
+    exp = ora.evaluate_expressions(cols, exact)
+    for i, e in enumerate(exact):
+        assert_tables_equal([got[i]], [exp[i]], what=e)
+    got = gpu.evaluate_expressions(cols, trans)
+    exp = ora.evaluate_expressions(cols, trans)
+    for i, e in enumerate(trans):
+        assert_tables_equal([got[i]], [exp[i]], ulps=TRANSCENDENTAL_ULPS, what=e)
+
+
+def test_column_offsets(gpu, ora):
+    """Views with non-zero offsets (data and validity read at offset + row)."""
+    base = W.host_columns("c1", 5000, seed=4)
+    for off in (1, 7, 31, 32, 33, 100):
+        cols = [HostColumn(c.type_id, c.data, c.mask, off, 5000 - off - 3) for c in base]
+        got = gpu.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+        exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+        assert_tables_equal(got, exp, what=f"offset {off}")
+        got = gpu.evaluate_expressions(cols, ["$2", "+($0, $2)"])
+        exp = ora.evaluate_expressions(cols, ["$2", "+($0, $2)"])
+        assert_tables_equal(got, exp, what=f"project offset {off}")
+
+
+@pytest.mark.parametrize("mode", [N.GX_FILTER_TWO_PASS, N.GX_FILTER_SINGLE_PASS])
+@pytest.mark.parametrize("words,warps", [(1, 4), (2, 8), (4, 8), (8, 4)])
+def test_filter_modes_and_tiles(ora, mode, words, warps):
+    n = 50_001
+    cols = W.host_columns("c2", n, seed=21)
+    p = g.Plan(W.workload("c2").schema, W.C2_CONDITION, W.C2_PROJECTIONS, filter_mode=mode,
+               block_threads=warps * 32, words_per_warp=words)
+    out, rows = p.execute(cols)
+    got = [c.to_host() for c in out]
+    exp = ora.filter_project(cols, W.C2_CONDITION, W.C2_PROJECTIONS)
+    assert rows == exp[0].size
+    assert_tables_equal(got[1:], exp[1:])
+    assert_tables_equal(got[:1], exp[:1], ulps=TRANSCENDENTAL_ULPS)
+
+
+def test_short_circuit_orders_identical(ora):
+    rng = np.random.default_rng(5)
+    n = 80_000
+    schema = [T.INT64] * 4 + [T.FLOAT64] * 4
+    cols = random_table(rng, n, [(T.INT64, 0, 1000)] * 4 + [(T.FLOAT64, 0.0, 1.0)] * 4, null_frac=0.02)
+    cond = "AND(<($0, 900), >($1, 10), <>($2, 7), <($4, 1.5), >($5, -2.0), <($6, 0.0))"
+    proj = [f"${i}" for i in range(8)]
+    exp = ora.filter_project(cols, cond, proj)
+    for order in ([0, 1, 2, 3, 4, 5], [5, 4, 3, 2, 1, 0], [2, 5, 0, 3, 1, 4]):
+        p = g.Plan(schema, cond, proj, short_circuit=True, conjunct_order=order)
+        out, rows = p.execute(cols)
+        assert_tables_equal([c.to_host() for c in out], exp, what=f"order {order}")
+
+
+def test_caller_buffers_and_capacity(ora):
+    cols = W.host_columns("c1", 10_000, seed=3)
+    p = g.Plan(W.workload("c1").schema, W.C1_CONDITION, W.C1_PROJECTIONS, filter_mode=N.GX_FILTER_SINGLE_PASS)
+    # allocate caller buffers through the library (a run with library outputs), then reuse
+    out, rows = p.execute(cols)
+    assert rows > 10
+    bufs = [N.Column(c._c.type_id, 0, c._c.data, c._c.null_mask, 0, c._c.capacity) for c in out]
+    res, rows2 = p.execute(cols, out=bufs)
+    assert rows2 == rows
+    tiny = [N.Column(b.type_id, 0, b.data, b.null_mask, 0, 5) for b in bufs]
+    with pytest.raises(g.GxError) as ei:
+        p.execute(cols, out=tiny)
+    assert ei.value.code == N.GX_ERR_CAPACITY
+
+
+def test_oom_is_retryable():
+    from blazingsql_gb300.api import fail_next_allocation
+    cols = W.host_columns("c1", 1000, seed=3)
+    fail_next_allocation(1)
+    with pytest.raises(g.GxError) as ei:
+        g.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+    assert ei.value.code == N.GX_ERR_OOM and ei.value.retryable
+    # the retry succeeds
+    out = g.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+    assert out[0].size > 0
+
+
+def test_rand_matches_oracle_philox(ora):
+    cols = W.host_columns("c1", 3000, seed=1)
+    p = g.Plan(W.workload("c1").schema, None, ["RAND()", "*($1, RAND())"], rand_seed=1234)
+    out, _ = p.execute(cols)
+    r = out[0].to_host().values()
+    assert (r > 0).all() and (r <= 1).all()
+    from oracle import pyoracle
+    exp = np.array([pyoracle.philox_uniform(1234, 0, i) for i in range(3000)])
+    assert (r == exp).all()
+
+
+def test_plan_reuse_across_batches(ora):
+    p = g.Plan(W.workload("c1").schema, W.C1_CONDITION, W.C1_PROJECTIONS)
+    for n in (10, 1000, 33_333, 0, 7):
+        cols = W.host_columns("c1", n, seed=n + 1) if n else \
+            [HostColumn(T.INT64, np.zeros(0, np.int64)), HostColumn(T.FLOAT64, np.zeros(0)),
+             HostColumn(T.INT32, np.zeros(0, np.int32), pack_validity(np.zeros(0, bool)))]
+        out, rows = p.execute(cols)
+        exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+        assert_tables_equal([c.to_host() for c in out], exp, what=f"batch {n}")
