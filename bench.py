@@ -66,12 +66,13 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (host time, csv line)
+        self.window = None       # (start, end) of the timed region
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -81,9 +82,17 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
-    def __exit__(self, *a):
+    def wait_first_sample(self, timeout=10.0):
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.05)
+
+    def mark(self, start, end):
+        self.window = (start, end)
+
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
@@ -94,7 +103,12 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.window:
+            inside = [x for x in lines if self.window[0] - 0.15 <= x[0] <= self.window[1] + 0.15]
+            if inside:
+                lines = inside
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -225,12 +239,19 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            out_rows = step()
-        ev1.record(stream)
-        torch.cuda.synchronize()
+    clocks = ClockSampler(local).start()
+    clocks.wait_first_sample()
+    t_start = time.time()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        out_rows = step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_end = time.time()
+    if t_end - t_start < 0.3:  # keep one more sampling period inside the window
+        time.sleep(0.3)
+    clocks.mark(t_start, t_end)
+    clocks.stop()
     L.gx_debug_set_kernel_timing(0)
     kernel_ms_total = L.gx_debug_kernel_ms(1)
     launches = L.gx_debug_launch_count() - launches0

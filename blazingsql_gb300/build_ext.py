@@ -34,10 +34,12 @@ def _cuda_root(nvcc: str) -> str:
 
 
 def _embed_prelude() -> str:
-    src = os.path.join(CSRC, "device_rt.cuh")
+    """device_rt.inc: fp64emu.cuh + device_rt.cuh as one raw string literal."""
     dst = os.path.join(BUILD, "device_rt.inc")
-    with open(src) as f:
-        text = f.read()
+    text = ""
+    for name in ("fp64emu.cuh", "device_rt.cuh"):
+        with open(os.path.join(CSRC, name)) as f:
+            text += f.read() + "\n"
     out = 'R"GXRT(' + text + ')GXRT"\n'
     if not os.path.exists(dst) or open(dst).read() != out:
         with open(dst, "w") as f:

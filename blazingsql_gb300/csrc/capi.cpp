@@ -51,6 +51,7 @@ KernelConfig default_config() {
   KernelConfig c;
   c.warps = env_int("GX_WARPS", 8);
   c.words = env_int("GX_WORDS", 4);
+  c.emulate_fp64 = env_int("GX_NATIVE_FP64", 0) == 0;
   return c;
 }
 
@@ -158,7 +159,8 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
     k += e;
     k += '\x1f';
   }
-  k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode);
+  k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
+       std::to_string(cfg.emulate_fp64);
   return k;
 }
 

@@ -118,6 +118,7 @@ __device__ __forceinline__ i64 gx_ld_i32(const void* p, i64 i) { return (i64)__l
 __device__ __forceinline__ i64 gx_ld_u32(const void* p, i64 i) { return (i64)__ldcs((const unsigned int*)p + i); }
 __device__ __forceinline__ u64 gx_ld_64(const void* p, i64 i) { return (u64)__ldcs((const long long*)p + i); }
 __device__ __forceinline__ u64 gx_ld_f32(const void* p, i64 i) { return gx_B((double)__ldcs((const float*)p + i)); }
+__device__ __forceinline__ u64 gx_ld_f32e(const void* p, i64 i) { return gxe_f2d(__ldcs((const unsigned*)p + i)); }
 
 __device__ __forceinline__ void gx_st_8(void* p, i64 i, u64 v) { __stcs((signed char*)p + i, (signed char)v); }
 __device__ __forceinline__ void gx_st_16(void* p, i64 i, u64 v) { __stcs((short*)p + i, (short)v); }

@@ -1,0 +1,350 @@
+// fp64emu.cuh -- IEEE-754 binary64 operations computed on the integer and
+// FP32 pipes, bit-identical to the hardware's round-to-nearest-even results.
+//
+// GB300 executes FP64 at about 1/57 of its FP32 rate (measured: DFMA 0.6 Top/s,
+// DDIV 59 Gop/s vs IMAD 19 Top/s), so a plan that divides or compares doubles
+// per row is bound by the FP64 pipe long before HBM.  These routines give the
+// exact same bits as the native instructions using 32/64-bit integer
+// arithmetic: division by a float-seeded fixed-point Newton reciprocal with an
+// exact integer remainder correction (Muller et al., "Handbook of
+// Floating-Point Arithmetic", ch. 9: reciprocal iteration + remainder-based
+// correction), conversions and comparisons by bit manipulation.
+//
+// The header compiles for the host too (g++), where the tests check it against
+// the CPU's IEEE arithmetic.
+#pragma once
+
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define GXE_FN __device__ __forceinline__
+#define GXE_ON_DEVICE 1
+#else
+#include <cstdint>
+#include <cstring>
+#define GXE_FN static inline
+#define GXE_ON_DEVICE 0
+#endif
+
+typedef unsigned long long gxe_u64;
+typedef long long gxe_i64;
+
+#define GXE_SIGN 0x8000000000000000ull
+#define GXE_FRAC 0x000FFFFFFFFFFFFFull
+#define GXE_HIDDEN 0x0010000000000000ull
+#define GXE_INF 0x7FF0000000000000ull
+#define GXE_QNAN 0x7FF8000000000000ull
+
+GXE_FN gxe_u64 gxe_umulhi(gxe_u64 a, gxe_u64 b) {
+#if GXE_ON_DEVICE
+  return __umul64hi(a, b);
+#else
+  return (gxe_u64)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+GXE_FN int gxe_clz(gxe_u64 x) {
+#if GXE_ON_DEVICE
+  return __clzll((gxe_i64)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+GXE_FN float gxe_rcp_approx(float x) {
+#if GXE_ON_DEVICE
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#elif defined(GXE_TEST_PERTURB_RCP)
+  // host test mode: a seed up to +-2 ulp off (worse than rcp.approx's 1 ulp)
+  float r = 1.0f / x;
+  unsigned u;
+  std::memcpy(&u, &r, 4);
+  unsigned xb;
+  std::memcpy(&xb, &x, 4);
+  u += (unsigned)((xb * 2654435761u) >> 29) % 5u - 2u;
+  std::memcpy(&r, &u, 4);
+  return r;
+#else
+  return 1.0f / x;
+#endif
+}
+
+GXE_FN unsigned gxe_f2u(float f) {
+#if GXE_ON_DEVICE
+  return __float_as_uint(f);
+#else
+  unsigned u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
+GXE_FN float gxe_u2f(unsigned u) {
+#if GXE_ON_DEVICE
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+GXE_FN bool gxe_isnan_(gxe_u64 a) { return (a & ~GXE_SIGN) > GXE_INF; }
+
+// Rounds Q * 2^(e - 54) (Q in [2^54, 2^55), `rem` nonzero if inexact beyond Q)
+// to binary64 with round-to-nearest-even; handles overflow and subnormals.
+GXE_FN gxe_u64 gxe_round_pack(gxe_u64 sign, int e, gxe_u64 q, bool rem) {
+  int eb = e + 1023;
+  if (eb >= 1) {
+    gxe_u64 m = q >> 2;
+    const bool round = (q >> 1) & 1u;
+    const bool sticky = (q & 1u) || rem;
+    m += (round && (sticky || (m & 1u))) ? 1u : 0u;
+    if (m == (1ull << 53)) {
+      m >>= 1;
+      eb++;
+    }
+    if (eb >= 2047) return sign | GXE_INF;
+    return sign | ((gxe_u64)eb << 52) | (m & GXE_FRAC);
+  }
+  const int sh = 3 - eb;  // >= 3
+  if (sh > 55) return sign;
+  gxe_u64 m = q >> sh;
+  const bool round = (q >> (sh - 1)) & 1u;
+  const bool sticky = (q & ((1ull << (sh - 1)) - 1u)) != 0 || rem;
+  m += (round && (sticky || (m & 1u))) ? 1u : 0u;
+  return sign | m;  // m == 2^52 encodes the smallest normal
+}
+
+// x / y, correctly rounded (round to nearest even), as bits.
+GXE_FN gxe_u64 gxe_div(gxe_u64 a, gxe_u64 b) {
+  const gxe_u64 sign = (a ^ b) & GXE_SIGN;
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  gxe_u64 fa = a & GXE_FRAC, fb = b & GXE_FRAC;
+  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u) {
+    const bool nan_a = ea == 0x7FF && fa != 0, nan_b = eb == 0x7FF && fb != 0;
+    if (nan_a || nan_b) return GXE_QNAN | (nan_a ? fa : fb) | (nan_a ? (a & GXE_SIGN) : (b & GXE_SIGN));
+    const bool inf_a = ea == 0x7FF, inf_b = eb == 0x7FF;
+    const bool zero_a = ea == 0 && fa == 0, zero_b = eb == 0 && fb == 0;
+    if ((inf_a && inf_b) || (zero_a && zero_b)) return GXE_QNAN | GXE_SIGN;
+    if (inf_a || zero_b) return sign | GXE_INF;
+    if (inf_b || zero_a) return sign;
+    if (ea == 0) {
+      const int lz = gxe_clz(fa) - 11;
+      fa <<= lz;
+      ea = 1 - lz;
+    }
+    if (eb == 0) {
+      const int lz = gxe_clz(fb) - 11;
+      fb <<= lz;
+      eb = 1 - lz;
+    }
+  }
+  gxe_u64 ma = fa | GXE_HIDDEN;
+  const gxe_u64 mb = fb | GXE_HIDDEN;
+  int e = ea - eb;
+  if (ma < mb) {
+    ma <<= 1;
+    e -= 1;
+  }
+  // r ~ 2^116 / mb, seeded from an FP32 reciprocal of mb's top 24 bits
+  const unsigned d24 = (unsigned)(mb >> 29);                      // [2^23, 2^24)
+  const float df = gxe_u2f((150u << 23) | (d24 & 0x7FFFFFu));    // == (float)d24
+  const unsigned rb = gxe_f2u(gxe_rcp_approx(df));                // ~1/d24 in (2^-24, 2^-23]
+  const int rexp = (int)((rb >> 23) & 0xFF) - 127;                // -24 or -23
+  gxe_u64 r = (gxe_u64)((rb & 0x7FFFFFu) | 0x800000u) << (40 + (rexp + 24));  // * 2^(87+rexp-23)
+  if (rexp >= -23) r = ~0ull;                                     // 1/d24 == 2^-23 -> clamp 2^64
+  // two Newton steps in 64-bit fixed point: r += r * (2^116 - mb*r) / 2^116
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const gxe_u64 ph = gxe_umulhi(mb, r), pl = mb * r;
+    const gxe_u64 t = (ph << 12) | (pl >> 52);   // (mb*r) >> 52, modulo 2^64
+    const gxe_i64 err = -(gxe_i64)t;             // (2^116 - mb*r) / 2^52
+    const gxe_u64 corr = gxe_umulhi(r, (gxe_u64)(err < 0 ? -err : err));
+    r = err < 0 ? r - corr : r + corr;
+  }
+  // Q0 ~ floor(ma * 2^54 / mb) = (ma * r) >> 62, then exact correction
+  gxe_u64 q = (gxe_umulhi(ma, r) << 2) | ((ma * r) >> 62);
+  gxe_i64 rem = (gxe_i64)((ma << 54) - q * mb);  // exact: |rem| < 2^55
+  if (rem < 0) { q--; rem += (gxe_i64)mb; }
+  if (rem < 0) { q--; rem += (gxe_i64)mb; }
+  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
+  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
+  return gxe_round_pack(sign, e, q, rem != 0);
+}
+
+// x + y, correctly rounded, as bits (guard / round / sticky alignment).
+GXE_FN gxe_u64 gxe_add(gxe_u64 a, gxe_u64 b) {
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  if (ea == 0x7FF || eb == 0x7FF) {
+    if (gxe_isnan_(a)) return a | (1ull << 51);
+    if (gxe_isnan_(b)) return b | (1ull << 51);
+    if (ea == 0x7FF && eb == 0x7FF) return ((a ^ b) & GXE_SIGN) ? (GXE_QNAN | GXE_SIGN) : a;  // inf - inf
+    return ea == 0x7FF ? a : b;
+  }
+  gxe_u64 aa = a & ~GXE_SIGN, bb = b & ~GXE_SIGN;
+  if (aa < bb) {  // |a| >= |b|
+    gxe_u64 t = a; a = b; b = t;
+    t = aa; aa = bb; bb = t;
+    int te = ea; ea = eb; eb = te;
+  }
+  if (bb == 0) return aa == 0 ? (a & b & GXE_SIGN) : a;
+  const int xa = ea ? ea : 1, xb = eb ? eb : 1;
+  gxe_u64 ma = ((a & GXE_FRAC) | (ea ? GXE_HIDDEN : 0)) << 3;
+  gxe_u64 mb = ((b & GXE_FRAC) | (eb ? GXE_HIDDEN : 0)) << 3;
+  const int d = xa - xb;
+  if (d >= 58) {
+    mb = 1;
+  } else if (d > 0) {
+    const gxe_u64 lost = mb & ((1ull << d) - 1u);
+    mb = (mb >> d) | (lost != 0 ? 1u : 0u);
+  }
+  const gxe_u64 sign = a & GXE_SIGN;
+  gxe_u64 s;
+  int e = xa;
+  if (((a ^ b) & GXE_SIGN) == 0) {
+    s = ma + mb;
+    if (s >> 56) {
+      s = (s >> 1) | (s & 1u);
+      e++;
+    }
+  } else {
+    s = ma - mb;
+    if (s == 0) return 0;
+    int lz = gxe_clz(s) - 8;
+    if (lz > 0) {
+      if (e - lz < 1) lz = e - 1;
+      s <<= lz;
+      e -= lz;
+    }
+  }
+  gxe_u64 m = s >> 3;
+  const unsigned low = (unsigned)(s & 7u);
+  if (low > 4u || (low == 4u && (m & 1u))) m++;
+  if (m >> 53) {
+    m >>= 1;
+    e++;
+  }
+  if (e >= 2047) return sign | GXE_INF;
+  if (!(m & GXE_HIDDEN)) return sign | m;  // subnormal
+  return sign | ((gxe_u64)e << 52) | (m & GXE_FRAC);
+}
+
+GXE_FN gxe_u64 gxe_sub(gxe_u64 a, gxe_u64 b) { return gxe_add(a, b ^ GXE_SIGN); }
+
+// x * y, correctly rounded, as bits (106-bit product).
+GXE_FN gxe_u64 gxe_mul(gxe_u64 a, gxe_u64 b) {
+  const gxe_u64 sign = (a ^ b) & GXE_SIGN;
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  gxe_u64 fa = a & GXE_FRAC, fb = b & GXE_FRAC;
+  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u) {
+    const bool nan_a = ea == 0x7FF && fa != 0, nan_b = eb == 0x7FF && fb != 0;
+    if (nan_a) return a | (1ull << 51);
+    if (nan_b) return b | (1ull << 51);
+    const bool inf_a = ea == 0x7FF, inf_b = eb == 0x7FF;
+    const bool zero_a = ea == 0 && fa == 0, zero_b = eb == 0 && fb == 0;
+    if ((inf_a && zero_b) || (inf_b && zero_a)) return GXE_QNAN | GXE_SIGN;
+    if (inf_a || inf_b) return sign | GXE_INF;
+    if (zero_a || zero_b) return sign;
+    if (ea == 0) {
+      const int lz = gxe_clz(fa) - 11;
+      fa <<= lz;
+      ea = 1 - lz;
+    }
+    if (eb == 0) {
+      const int lz = gxe_clz(fb) - 11;
+      fb <<= lz;
+      eb = 1 - lz;
+    }
+  }
+  const gxe_u64 ma = fa | GXE_HIDDEN, mb = fb | GXE_HIDDEN;
+  const gxe_u64 hi = gxe_umulhi(ma, mb), lo = ma * mb;  // product in [2^104, 2^106)
+  if (hi >> 41) {  // >= 2^105
+    return gxe_round_pack(sign, ea + eb - 2045, (hi << 13) | (lo >> 51), (lo & ((1ull << 51) - 1u)) != 0);
+  }
+  return gxe_round_pack(sign, ea + eb - 2046, (hi << 14) | (lo >> 50), (lo & ((1ull << 50) - 1u)) != 0);
+}
+
+// (double)(int64) with round-to-nearest-even, as bits.
+GXE_FN gxe_u64 gxe_i2d(gxe_i64 v) {
+  if (v == 0) return 0;
+  const gxe_u64 sign = v < 0 ? GXE_SIGN : 0;
+  gxe_u64 u = v < 0 ? 0ull - (gxe_u64)v : (gxe_u64)v;
+  const int lz = gxe_clz(u);
+  const int msb = 63 - lz;                     // exponent
+  if (msb <= 52) return sign | ((gxe_u64)(msb + 1023) << 52) | ((u << (52 - msb)) & GXE_FRAC);
+  const int sh = msb - 52;                     // 1..11
+  gxe_u64 m = u >> sh;
+  const bool round = (u >> (sh - 1)) & 1u;
+  const bool sticky = (u & ((1ull << (sh - 1)) - 1u)) != 0;
+  m += (round && (sticky || (m & 1u))) ? 1u : 0u;
+  int eb = msb + 1023;
+  if (m == (1ull << 53)) {
+    m >>= 1;
+    eb++;
+  }
+  return sign | ((gxe_u64)eb << 52) | (m & GXE_FRAC);
+}
+
+// (double)(float) (exact), as bits.
+GXE_FN gxe_u64 gxe_f2d(unsigned f) {
+  const gxe_u64 sign = (gxe_u64)(f >> 31) << 63;
+  const unsigned ef = (f >> 23) & 0xFF, mf = f & 0x7FFFFFu;
+  if (ef == 0xFF) return sign | GXE_INF | ((gxe_u64)mf << 29) | (mf ? (1ull << 51) : 0);
+  if (ef == 0) {
+    if (mf == 0) return sign;
+    const int lz = gxe_clz((gxe_u64)mf) - 40;     // bring the leading 1 to bit 23
+    return sign | ((gxe_u64)(1 - lz - 127 + 1023) << 52) | (((gxe_u64)(mf << lz) & 0x7FFFFFu) << 29);
+  }
+  return sign | ((gxe_u64)(ef - 127 + 1023) << 52) | ((gxe_u64)mf << 29);
+}
+
+GXE_FN bool gxe_isnan(gxe_u64 a) { return (a & ~GXE_SIGN) > GXE_INF; }
+
+// total order key for non-NaN values with -0 == +0
+GXE_FN gxe_u64 gxe_key(gxe_u64 a) {
+  if ((a << 1) == 0) a = 0;
+  return (a & GXE_SIGN) ? ~a : (a | GXE_SIGN);
+}
+GXE_FN bool gxe_lt(gxe_u64 a, gxe_u64 b) { return !gxe_isnan(a) && !gxe_isnan(b) && gxe_key(a) < gxe_key(b); }
+GXE_FN bool gxe_le(gxe_u64 a, gxe_u64 b) { return !gxe_isnan(a) && !gxe_isnan(b) && gxe_key(a) <= gxe_key(b); }
+GXE_FN bool gxe_eq(gxe_u64 a, gxe_u64 b) { return !gxe_isnan(a) && !gxe_isnan(b) && gxe_key(a) == gxe_key(b); }
+GXE_FN bool gxe_nz(gxe_u64 a) { return (a << 1) != 0; }  // != 0.0 (NaN counts as nonzero)
+
+// floor / ceil (exact), as bits
+GXE_FN gxe_u64 gxe_floor(gxe_u64 a) {
+  const int e = (int)((a >> 52) & 0x7FF) - 1023;
+  if (e >= 52) return gxe_isnan(a) ? (a | (1ull << 51)) : a;  // integral, inf, nan
+  if (e < 0) {
+    if ((a << 1) == 0) return a;                                 // +-0
+    return (a & GXE_SIGN) ? 0xBFF0000000000000ull : 0;           // -1 or +0
+  }
+  const gxe_u64 fmask = GXE_FRAC >> e;
+  if ((a & fmask) == 0) return a;
+  if (a & GXE_SIGN) a += (GXE_HIDDEN >> e);  // round toward -inf in magnitude
+  return a & ~fmask;
+}
+GXE_FN gxe_u64 gxe_ceil(gxe_u64 a) {
+  const int e = (int)((a >> 52) & 0x7FF) - 1023;
+  if (e >= 52) return gxe_isnan(a) ? (a | (1ull << 51)) : a;
+  if (e < 0) {
+    if ((a << 1) == 0) return a;
+    return (a & GXE_SIGN) ? GXE_SIGN : 0x3FF0000000000000ull;    // -0 or +1
+  }
+  const gxe_u64 fmask = GXE_FRAC >> e;
+  if ((a & fmask) == 0) return a;
+  if (!(a & GXE_SIGN)) a += (GXE_HIDDEN >> e);
+  return a & ~fmask;
+}
+
+// static_cast<int64_t>(double) as the GPU does it: truncate, saturate, NaN -> 0
+GXE_FN gxe_i64 gxe_d2ll(gxe_u64 a) {
+  if (gxe_isnan(a)) return 0;
+  const int e = (int)((a >> 52) & 0x7FF) - 1023;
+  const bool neg = (a & GXE_SIGN) != 0;
+  if (e < 0) return 0;
+  if (e >= 63) return neg ? (gxe_i64)GXE_SIGN : 0x7FFFFFFFFFFFFFFFll;
+  const gxe_u64 m = (a & GXE_FRAC) | GXE_HIDDEN;
+  const gxe_u64 mag = e >= 52 ? (m << (e - 52)) : (m >> (52 - e));
+  return neg ? -(gxe_i64)mag : (gxe_i64)mag;
+}

@@ -187,6 +187,8 @@ const char* load_fn(int t) {
   }
 }
 
+const char* load_fn_emu(int t) { return t == FLOAT32 ? "gx_ld_f32e" : load_fn(t); }
+
 // store of 64-bit value bits into an output column of type t
 // (device_ptr_write_from_buffer, interpreter_ops.cuh:329-395)
 std::string store_stmt(int t, const std::string& ptr, const std::string& idx, const std::string& bits) {
@@ -209,6 +211,13 @@ std::string raw_type(int t) {
     case 4: return "unsigned int";
     default: return "unsigned long long";
   }
+}
+
+uint64_t magic_double_bits() {
+  const double m = 1.7976931348623123e+308;  // interpreter_ops.cuh:47
+  uint64_t u;
+  std::memcpy(&u, &m, 8);
+  return u;
 }
 
 int64_t ns_per_unit(int t) {
@@ -240,9 +249,25 @@ class Gen {
     return "v" + std::to_string(id) + "[k]";
   }
   bool kind_f(int id) const { return is_float(p_.nodes[id].ktype); }
-  std::string asD(int id) const { return kind_f(id) ? "gx_D(" + B(id) + ")" : "gx_I2D(" + B(id) + ")"; }
-  std::string asI(int id) const { return kind_f(id) ? "gx_D2LL(gx_D(" + B(id) + "))" : "(i64)(" + B(id) + ")"; }
-  std::string nz(int id) const { return kind_f(id) ? "(gx_D(" + B(id) + ") != 0.0)" : "(" + B(id) + " != 0ull)"; }
+  // operand as a double value (native FP64 arithmetic follows)
+  std::string asD(int id) const {
+    if (kind_f(id)) return "gx_D(" + B(id) + ")";
+    return cfg_.emulate_fp64 ? "gx_D(gxe_i2d((i64)(" + B(id) + ")))" : "gx_I2D(" + B(id) + ")";
+  }
+  // operand as the bits of its double value (integer-pipe binary64 routines follow)
+  std::string asDB(int id) const {
+    if (kind_f(id)) return B(id);
+    return cfg_.emulate_fp64 ? "gxe_i2d((i64)(" + B(id) + "))" : "gx_B(gx_I2D(" + B(id) + "))";
+  }
+  std::string asI(int id) const {
+    if (!kind_f(id)) return "(i64)(" + B(id) + ")";
+    return cfg_.emulate_fp64 ? "gxe_d2ll(" + B(id) + ")" : "gx_D2LL(gx_D(" + B(id) + "))";
+  }
+  std::string nz(int id) const {
+    if (!kind_f(id)) return "(" + B(id) + " != 0ull)";
+    return cfg_.emulate_fp64 ? "gxe_nz(" + B(id) + ")" : "(gx_D(" + B(id) + ") != 0.0)";
+  }
+  bool emu() const { return cfg_.emulate_fp64; }
 
   // statements computing node id for slot k; row / out-row expressions given
   void emit_node(std::ostringstream& o, int id, const std::string& ind) const {
@@ -251,7 +276,8 @@ class Gen {
     if (n.kind == Node::LIT) return;
     if (n.kind == Node::COL) {
       const int c = n.col;
-      o << ind << b << " = inr ? (u64)" << load_fn(p_.schema[c]) << "(a.in_data[" << c << "], a.in_off[" << c
+      o << ind << b << " = inr ? (u64)" << (emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c])) << "(a.in_data["
+        << c << "], a.in_off[" << c
         << "] + row) : 0ull;\n";
       if (p_.nullable[c]) o << ind << v << " = inr && gx_valid(a.in_mask[" << c << "], a.in_off[" << c << "] + row);\n";
       else o << ind << v << " = inr;\n";
@@ -273,17 +299,18 @@ class Gen {
       bool always_valid = false;
       switch (op) {
         case OP_IS_NOT_TRUE:
-          r = "(u64)(!(" + XV + " && " + (lf ? "gx_D(" + X + ") == 1.0" : "(i64)(" + X + ") == 1LL") + "))";
+          r = "(u64)(!(" + XV + " && " + (lf ? "(" + X + ") == 0x3ff0000000000000ull" : "(i64)(" + X + ") == 1LL") +
+              "))";
           always_valid = true;
           break;
         case OP_IS_NOT_FALSE:
-          r = "(u64)(!(" + XV + " && " + (lf ? "gx_D(" + X + ") == 0.0" : "(i64)(" + X + ") == 0LL") + "))";
+          r = "(u64)(!(" + XV + " && " + (lf ? "((" + X + ") << 1) == 0ull" : "(i64)(" + X + ") == 0LL") + "))";
           always_valid = true;
           break;
         case OP_IS_NULL: r = "(u64)(!" + XV + ")"; always_valid = true; break;
         case OP_IS_NOT_NULL: r = "(u64)(" + XV + ")"; always_valid = true; break;
-        case OP_FLOOR: r = "gx_B(floor(" + asD(x) + "))"; break;
-        case OP_CEIL: r = "gx_B(ceil(" + asD(x) + "))"; break;
+        case OP_FLOOR: r = emu() ? "gxe_floor(" + asDB(x) + ")" : "gx_B(floor(" + asD(x) + "))"; break;
+        case OP_CEIL: r = emu() ? "gxe_ceil(" + asDB(x) + ")" : "gx_B(ceil(" + asD(x) + "))"; break;
         case OP_SIN: r = "gx_B(sin(" + asD(x) + "))"; break;
         case OP_COS: r = "gx_B(cos(" + asD(x) + "))"; break;
         case OP_ASIN: r = "gx_B(asin(" + asD(x) + "))"; break;
@@ -295,7 +322,7 @@ class Gen {
         case OP_LOG10: r = "gx_B(log10(" + asD(x) + "))"; break;
         case OP_EXP: r = "gx_B(exp(" + asD(x) + "))"; break;
         case OP_ABS:
-          r = lf ? "gx_B(fabs(gx_D(" + X + ")))" : "((i64)(" + X + ") < 0LL ? 0ull - (" + X + ") : (" + X + "))";
+          r = lf ? "((" + X + ") & 0x7fffffffffffffffull)" : "((i64)(" + X + ") < 0LL ? 0ull - (" + X + ") : (" + X + "))";
           break;
         case OP_NOT: r = "(u64)(!" + nz(x) + ")"; break;
         case OP_IS_TRUE: r = "(u64)" + asI(x); break;
@@ -311,7 +338,7 @@ class Gen {
         case OP_CAST_TINYINT: case OP_CAST_SMALLINT: case OP_CAST_INTEGER: case OP_CAST_BIGINT:
           r = "(u64)" + asI(x);
           break;
-        case OP_CAST_FLOAT: case OP_CAST_DOUBLE: r = "gx_B(" + asD(x) + ")"; break;
+        case OP_CAST_FLOAT: case OP_CAST_DOUBLE: r = asDB(x); break;
         case OP_CAST_DATE: {
           long long div = lt == TIMESTAMP_SECONDS ? 86400LL : lt == TIMESTAMP_MILLISECONDS ? 86400000LL
                         : lt == TIMESTAMP_MICROSECONDS ? 86400000000LL : lt == TIMESTAMP_NANOSECONDS ? 86400000000000LL : 1;
@@ -349,7 +376,9 @@ class Gen {
         return;
       }
       case OP_FIRST_NON_MAGIC: {
-        const std::string magic = lf ? "(gx_D(" + X + ") == GX_MAGIC_D)" : "((i64)(" + X + ") == GX_MAGIC_I)";
+        // double equality with the (non-zero, finite) magic value is bit equality
+        const std::string magic = lf ? "((" + X + ") == " + hex64(magic_double_bits()) + ")"
+                                     : "((i64)(" + X + ") == GX_MAGIC_I)";
         o << ind << "{ const bool m_ = " << magic << ";\n";
         o << ind << "  " << b << " = m_ ? " << Y << " : " << X << ";\n";
         o << ind << "  " << v << " = m_ ? " << YV << " : " << XV << "; }\n";
@@ -361,7 +390,9 @@ class Gen {
         o << ind << v << " = (" << XV << " && " << YV << ") || (" << XV << " ? " << nz(x) << " : " << YV << ");\n";
         return;
       case OP_IS_NOT_DISTINCT_FROM: {
-        const std::string eq = anyf ? "(" + asD(x) + " == " + asD(y) + ")" : "(" + X + " == " + Y + ")";
+        const std::string eq = !anyf ? "(" + X + " == " + Y + ")"
+                               : emu() ? "gxe_eq(" + asDB(x) + ", " + asDB(y) + ")"
+                                       : "(" + asD(x) + " == " + asD(y) + ")";
         o << ind << b << " = (u64)((!" << XV << " && !" << YV << ") || (" << XV << " && " << YV << " && " << eq
           << "));\n";
         o << ind << v << " = true;\n";
@@ -379,17 +410,36 @@ class Gen {
         };
         return std::string("(u64)(") + to_ns(x, lt) + " " + opstr + " " + to_ns(y, rt) + ")";
       }
+      if (anyf && emu()) {
+        const std::string X2 = asDB(x), Y2 = asDB(y), o2 = opstr;
+        if (o2 == "<") return "(u64)gxe_lt(" + X2 + ", " + Y2 + ")";
+        if (o2 == ">") return "(u64)gxe_lt(" + Y2 + ", " + X2 + ")";
+        if (o2 == "<=") return "(u64)gxe_le(" + X2 + ", " + Y2 + ")";
+        if (o2 == ">=") return "(u64)gxe_le(" + Y2 + ", " + X2 + ")";
+        if (o2 == "==") return "(u64)gxe_eq(" + X2 + ", " + Y2 + ")";
+        return "(u64)(!gxe_eq(" + X2 + ", " + Y2 + "))";
+      }
       if (anyf) return std::string("(u64)(") + asD(x) + " " + opstr + " " + asD(y) + ")";
       return std::string("(u64)((i64)(") + X + ") " + opstr + " (i64)(" + Y + "))";
     };
     switch (op) {
       case OP_AND: r = "(u64)(" + nz(x) + " && " + nz(y) + ")"; break;
-      case OP_ADD: r = anyf ? "gx_B(" + asD(x) + " + " + asD(y) + ")" : "(" + X + " + " + Y + ")"; break;
-      case OP_SUB: r = anyf ? "gx_B(" + asD(x) + " - " + asD(y) + ")" : "(" + X + " - " + Y + ")"; break;
-      case OP_MUL: r = anyf ? "gx_B(" + asD(x) + " * " + asD(y) + ")" : "(" + X + " * " + Y + ")"; break;
+      case OP_ADD:
+        r = !anyf ? "(" + X + " + " + Y + ")"
+            : emu() ? "gxe_add(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " + " + asD(y) + ")";
+        break;
+      case OP_SUB:
+        r = !anyf ? "(" + X + " - " + Y + ")"
+            : emu() ? "gxe_sub(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " - " + asD(y) + ")";
+        break;
+      case OP_MUL:
+        r = !anyf ? "(" + X + " * " + Y + ")"
+            : emu() ? "gxe_mul(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " * " + asD(y) + ")";
+        break;
       case OP_DIV:
-        r = anyf ? "gx_B(" + asD(x) + " / " + asD(y) + ")" : "gx_div_ii(" + X + ", " + Y + ")";
-        vv = "(" + vv + " && " + (rf ? "gx_D(" + Y + ") != 0.0" : "(i64)(" + Y + ") != 0LL") + ")";
+        r = !anyf ? "gx_div_ii(" + X + ", " + Y + ")"
+            : emu() ? "gxe_div(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " / " + asD(y) + ")";
+        vv = "(" + vv + " && " + (rf ? nz(y) : "(i64)(" + Y + ") != 0LL") + ")";
         break;
       case OP_MOD:
         if (anyf) {

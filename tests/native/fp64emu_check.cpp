@@ -1,0 +1,97 @@
+// Checks the integer-pipe binary64 routines of fp64emu.cuh against the host
+// CPU's IEEE-754 arithmetic (SSE2, round to nearest even, no FTZ/DAZ), bit for
+// bit (any NaN matches any NaN).  Usage: fp64emu_check <cases> <seed>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <random>
+
+#include "fp64emu.cuh"
+
+static uint64_t bits(double d) { uint64_t u; std::memcpy(&u, &d, 8); return u; }
+static double dbl(uint64_t u) { double d; std::memcpy(&d, &u, 8); return d; }
+static bool same(uint64_t got, double want) {
+  if (std::isnan(want)) return gxe_isnan(got);
+  return got == bits(want);
+}
+
+static int64_t ref_d2ll(double x) {
+  if (x != x) return 0;
+  if (x >= 9223372036854775808.0) return std::numeric_limits<int64_t>::max();
+  if (x < -9223372036854775808.0) return std::numeric_limits<int64_t>::min();
+  return (int64_t)x;
+}
+
+struct Gen {
+  std::mt19937_64 rng;
+  explicit Gen(uint64_t s) : rng(s) {}
+  uint64_t u64() { return rng(); }
+  // a double drawn from a mix of strategies: uniform bits, moderate values,
+  // subnormals, extreme exponents, integers, specials
+  double any() {
+    switch (rng() % 10) {
+      case 0: return dbl(rng());
+      case 1: return dbl((rng() & 0x800FFFFFFFFFFFFFull));                       // subnormal / zero
+      case 2: return dbl((rng() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1 + rng() % 60) << 52));  // tiny normal
+      case 3: return dbl((rng() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(2046 - rng() % 60) << 52));  // huge
+      case 4: { static const double S[] = {0.0, -0.0, 1.0, -1.0, INFINITY, -INFINITY, NAN, 10.0, 1000.0, 0.5,
+                                           1.7976931348623123e+308, 2.2250738585072014e-308, 4.9e-324};
+                return S[rng() % (sizeof S / sizeof S[0])]; }
+      case 5: return (double)(int64_t)(rng() >> (rng() % 64));
+      case 6: return dbl((rng() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 + (int)(rng() % 64) - 32) << 52));
+      case 7: return dbl(0x3FF0000000000000ull | (rng() & 0xFFFFFull));        // near 1, short mantissa
+      default: { std::normal_distribution<double> n(0.0, 1e3); return n(rng); }
+    }
+  }
+};
+
+int main(int argc, char** argv) {
+  const long long cases = argc > 1 ? atoll(argv[1]) : 1000000;
+  Gen g(argc > 2 ? strtoull(argv[2], nullptr, 10) : 1);
+  long long bad = 0;
+  for (long long i = 0; i < cases; i++) {
+    const double a = g.any(), b = g.any();
+    const uint64_t q = gxe_div(bits(a), bits(b));
+    if (!same(q, a / b)) {
+      if (bad++ < 10) printf("div %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q,
+                             (unsigned long long)bits(a / b));
+    }
+    if (!same(gxe_add(bits(a), bits(b)), a + b) || !same(gxe_sub(bits(a), bits(b)), a - b)) {
+      if (bad++ < 10) printf("add/sub %.17g %.17g\n", a, b);
+    }
+    if (!same(gxe_mul(bits(a), bits(b)), a * b)) {
+      if (bad++ < 10) printf("mul %.17g * %.17g: got %016llx want %016llx\n", a, b,
+                             (unsigned long long)gxe_mul(bits(a), bits(b)), (unsigned long long)bits(a * b));
+    }
+    // close magnitudes exercise cancellation
+    const double c = a * (1.0 + (double)(g.u64() % 1000) * 1e-16);
+    if (!same(gxe_sub(bits(a), bits(c)), a - c) || !same(gxe_add(bits(a), bits(-c)), a + -c)) {
+      if (bad++ < 10) printf("cancel %.17g %.17g\n", a, c);
+    }
+    const int64_t iv = (int64_t)g.u64() >> (g.u64() % 64);
+    if (gxe_i2d(iv) != bits((double)iv)) {
+      if (bad++ < 10) printf("i2d %lld\n", (long long)iv);
+    }
+    const uint32_t fb = (uint32_t)g.u64();
+    float fv;
+    std::memcpy(&fv, &fb, 4);
+    if (!same(gxe_f2d(fb), (double)fv)) {
+      if (bad++ < 10) printf("f2d %08x\n", fb);
+    }
+    if (!same(gxe_floor(bits(a)), std::floor(a)) || !same(gxe_ceil(bits(a)), std::ceil(a))) {
+      if (bad++ < 10) printf("floor/ceil %.17g\n", a);
+    }
+    if (gxe_lt(bits(a), bits(b)) != (a < b) || gxe_le(bits(a), bits(b)) != (a <= b) ||
+        gxe_eq(bits(a), bits(b)) != (a == b) || gxe_nz(bits(a)) != (a != 0.0)) {
+      if (bad++ < 10) printf("cmp %.17g %.17g\n", a, b);
+    }
+    if (gxe_d2ll(bits(a)) != ref_d2ll(a)) {
+      if (bad++ < 10) printf("d2ll %.17g\n", a);
+    }
+  }
+  printf("cases=%lld mismatches=%lld\n", cases, bad);
+  return bad ? 1 : 0;
+}

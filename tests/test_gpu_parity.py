@@ -93,7 +93,10 @@ def test_evaluate_expressions_every_operator(gpu, ora):
     got = gpu.evaluate_expressions(cols, trans)
     exp = ora.evaluate_expressions(cols, trans)
     for i, e in enumerate(trans):
-        assert_tables_equal([got[i]], [exp[i]], ulps=TRANSCENDENTAL_ULPS, what=e)
+        # COT is cos(x) / sin(x): two transcendental roundings and a division
+        # (interpreter_ops.cuh:778-782), so its bound is the sum of the parts
+        tol = 4 if e.startswith("COT") else TRANSCENDENTAL_ULPS
+        assert_tables_equal([got[i]], [exp[i]], ulps=tol, what=e)
 
 
 def test_column_offsets(gpu, ora):
