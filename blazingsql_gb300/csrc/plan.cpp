@@ -566,8 +566,69 @@ void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
 
 // phase 2 of the filter kernels: projections for the kept rows of each word,
 // written at positions pos.. (warp-uniform), plus validity bit streams
+// stores + validity of output j for the current lane (dense rounds)
+void emit_dense_store(std::ostringstream& o, const Gen& g, const Plan& p, size_t j, const std::string& ind) {
+  const OutSpec& os = p.outputs[j];
+  std::string vexpr;
+  if (os.kind == OutSpec::NODE) {
+    o << ind << "if (wr) " << store_stmt(os.type, "a.out_data[" + std::to_string(j) + "]", "orow", g.B(os.node)) << "\n";
+    vexpr = g.V(os.node);
+  } else if (os.kind == OutSpec::COPY) {
+    const int c = os.col;
+    const std::string rt = raw_type(p.schema[c]);
+    o << ind << "if (wr) ((" << rt << "*)a.out_data[" << j << "])[orow] = __ldcs((const " << rt << "*)a.in_data[" << c
+      << "] + a.in_off[" << c << "] + row);\n";
+    vexpr = p.nullable[c] ? "gx_valid(a.in_mask[" + std::to_string(c) + "], a.in_off[" + std::to_string(c) + "] + row)"
+                          : "true";
+  } else {
+    return;  // broadcast outputs are filled after the launch
+  }
+  o << ind << "{ const u32 vb_ = __ballot_sync(GX_FULL, act && " << vexpr << ");\n";
+  o << ind << "  if (bw_[" << j << "].word < cap_words) bw_[" << j << "].append(a.out_mask[" << j
+    << "], vb_, nb); else { bw_[" << j << "].fill = 0; } }\n";
+}
+
+// Dense phase 2: the warp's kept rows, in row order, are dealt to lanes in
+// rounds of 32 (lane l of round r takes the warp's (32r + l)-th kept row), so
+// projections are computed only for surviving rows and every output store and
+// validity word of a round is contiguous.  Operands are re-read with the
+// gathered row index (predicate columns hit L1/L2).
+void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p, const std::string& ind) {
+  std::vector<int> proj = g.cone(g.output_roots());
+  o << ind << "u32 cum_[GX_V + 1]; cum_[0] = 0u;\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++) cum_[kk + 1] = cum_[kk] + __popc(bal[kk]);\n";
+  o << ind << "const u32 total_ = cum_[GX_V];\n";
+  o << ind << "GxBitWriter bw_[" << p.outputs.size() << "];\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << p.outputs.size() << "; j++) bw_[j].init((i64)pos);\n";
+  o << ind << "const i64 cap_words = (a.capacity + 31) >> 5;\n";
+  o << ind << "for (u32 base_ = 0; base_ < total_; base_ += 32u) {\n";
+  const std::string in2 = ind + "  ";
+  o << in2 << "const u32 t_ = base_ + (u32)lane; const bool act = t_ < total_;\n";
+  o << in2 << "u32 bks_ = 0u, cks_ = 0u; int sk_ = 0;\n";
+  o << in2 << "#pragma unroll\n" << in2 << "for (int kk = 0; kk < GX_V; kk++)\n";
+  o << in2 << "  if (t_ >= cum_[kk] && t_ < cum_[kk + 1]) { sk_ = kk; bks_ = bal[kk]; cks_ = cum_[kk]; }\n";
+  o << in2 << "const int src_ = act ? (int)__fns(bks_, 0u, (int)(t_ - cks_) + 1) : 0;\n";
+  o << in2 << "const i64 row = (w0 + sk_) * 32 + src_; const bool inr = act; (void)inr;\n";
+  o << in2 << "const i64 orow = (i64)pos + (i64)t_; (void)orow;\n";
+  o << in2 << "const int k = 0;\n";
+  g.decl(o, proj, in2);
+  for (int id : proj) g.emit_node(o, id, in2);
+  o << in2 << "const bool wr = act && orow < a.capacity;\n";
+  o << in2 << "const int nb = (int)min(32u, total_ - base_);\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) emit_dense_store(o, g, p, j, in2);
+  o << ind << "}\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    if (p.outputs[j].kind == OutSpec::BROADCAST) continue;
+    o << ind << "if (bw_[" << j << "].word < cap_words) bw_[" << j << "].flush(a.out_mask[" << j << "]);\n";
+  }
+}
+
 void emit_filter_writes(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
                         const std::string& ind) {
+  if (g.cfg_.dense) {
+    emit_filter_writes_dense(o, g, p, ind);
+    return;
+  }
   std::vector<int> proj = g.cone(g.output_roots());
   std::set<int> have(pred_ids.begin(), pred_ids.end());
   std::vector<int> fresh;

@@ -49,6 +49,7 @@ struct KernelConfig {
   int warps = 8;           // warps per CTA
   int words = 2;           // 32-row words per warp per step
   bool emulate_fp64 = true;  // binary64 compares / divides / conversions on the integer pipes
+  bool dense = true;         // filter kernels: projections on warp-compacted kept rows
   bool short_circuit = false;
   std::vector<int> conjunct_order;  // indices into Plan::conjuncts
 };

@@ -48,6 +48,7 @@ class CompiledPlan {
  public:
   CompiledPlan(Plan p, KernelConfig cfg, int mode) : plan_(std::move(p)), cfg_(std::move(cfg)), mode_(mode) {}
 
+
   // Runs the plan over `cols`.  out must hold plan.outputs.size() entries.  If
   // out[0].data is non-null, caller-supplied buffers are used (capacity rows).
   void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const;
