@@ -21,6 +21,11 @@ GX_ERR_TIMEOUT = 6
 GX_ERR_INVALID = 7
 GX_ERR_CAPACITY = 8
 
+# gx_plan_execute_noalloc: tile status words of its fixed scratch array, and the
+# largest batch that fits with the default 1024-row tile (8 warps x 4 words x 32)
+GX_NOALLOC_MAX_TILES = 524284
+GX_NOALLOC_MAX_ROWS = GX_NOALLOC_MAX_TILES * 1024
+
 GX_FILTER_AUTO = 0
 GX_FILTER_TWO_PASS = 1
 GX_FILTER_SINGLE_PASS = 2
@@ -95,6 +100,8 @@ def lib():
     L.gx_plan_num_conjuncts.argtypes = [C.c_void_p]
     L.gx_plan_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
                                   P(StatusInfo)]
+    L.gx_plan_execute_noalloc.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
+                                          P(StatusInfo)]
     L.gx_plan_destroy.argtypes = [C.c_void_p]
     L.gx_plan_destroy.restype = None
     L.gx_debug_kernel_source.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), C.c_char_p, C.c_int64, P(StatusInfo)]
@@ -124,7 +131,8 @@ def check(rc: int, st: StatusInfo) -> None:
 EXPORTED_SYMBOLS = [
     "gx_evaluate_expressions", "gx_process_project", "gx_process_filter", "gx_filter_project", "gx_free_columns",
     "gx_column_to_host", "gx_plan_options_init", "gx_plan_compile", "gx_plan_num_outputs", "gx_plan_output_type",
-    "gx_plan_num_conjuncts", "gx_plan_execute", "gx_plan_destroy", "gx_version", "gx_debug_kernel_source",
+    "gx_plan_num_conjuncts", "gx_plan_execute", "gx_plan_execute_noalloc", "gx_plan_destroy", "gx_version",
+    "gx_debug_kernel_source",
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
 ]

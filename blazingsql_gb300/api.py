@@ -260,6 +260,19 @@ class Plan:
             return [outs[i] for i in range(n)], rows.value
         return _wrap(outs, n, s), rows.value
 
+    def execute_noalloc(self, table: Table, out: Sequence[N.Column], stream=None):
+        """gx_plan_execute_noalloc: runs the filter plan into the caller's buffers
+        (``out``: one Column per output with data, null_mask and capacity set)
+        without any device allocation by the library.  Returns (columns, rows)."""
+        keep: list = []
+        views, nc = _views(table, keep)
+        s = _stream_handle(stream)
+        outs = (N.Column * max(1, len(out)))(*out)
+        rows = C.c_int64(0)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_plan_execute_noalloc(self._h, views, nc, outs, C.byref(rows), s, C.byref(st)), st)
+        return [outs[i] for i in range(len(out))], rows.value
+
     def kernel_source(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None) -> str:
         L = N.lib()
         st = N.StatusInfo()

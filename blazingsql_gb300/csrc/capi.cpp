@@ -195,6 +195,15 @@ struct gx_plan {
   std::shared_ptr<gx::PlanSet> ps;
 };
 
+namespace gx {
+// The compiled plan of a gx_plan with one kernel (at most GX_OUTPUTS_PER_KERNEL
+// outputs), or null.
+const CompiledPlan* single_chunk(const gx_plan* plan) {
+  if (!plan || plan->ps->chunks.size() != 1) return nullptr;
+  return plan->ps->chunks[0].get();
+}
+}  // namespace gx
+
 using namespace gx;
 
 extern "C" {

@@ -468,4 +468,70 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
   }
 }
 
+void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                                        unsigned long long* scratch, long long scratch_words, cudaStream_t s) const {
+  if (!plan_.has_filter()) fail(GX_ERR_INVALID, "the no-allocation entry point needs a plan with a condition");
+  if (cols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < cols.size(); i++)
+    if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
+  const int nout = (int)plan_.outputs.size();
+  for (int j = 0; j < nout; j++) {
+    if (!out[j].data || !out[j].null_mask || out[j].capacity < 0)
+      fail(GX_ERR_INVALID, "the no-allocation entry point writes into caller buffers: out[].data, "
+                           "out[].null_mask and out[].capacity must be set");
+    out[j].type_id = plan_.outputs[j].type;
+  }
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const int64_t nwords = (n + 31) / 32;
+  const int64_t tile_words = (int64_t)cfg_.warps * cfg_.words;
+  const int64_t ntiles = (nwords + tile_words - 1) / tile_words;
+  if (4 + ntiles > scratch_words)
+    fail(GX_ERR_INVALID, "batch of " + std::to_string(n) + " rows needs " + std::to_string(ntiles) +
+                             " tile slots; the no-allocation scratch holds " + std::to_string(scratch_words - 4) +
+                             " (at most " + std::to_string((scratch_words - 4) * tile_words * 32) + " rows)");
+  int64_t capacity = nout ? out[0].capacity : 0;
+  for (int j = 1; j < nout; j++) capacity = std::min<int64_t>(capacity, out[j].capacity);
+  for (int j = 0; j < nout; j++)
+    check_cuda(cudaMemsetAsync(out[j].null_mask, 0, (size_t)mask_words_padded(capacity) * 4, s), "mask zero");
+  if (n == 0) {
+    for (int j = 0; j < nout; j++) out[j].size = 0;
+    if (out_rows) *out_rows = 0;
+    return;
+  }
+  // the array keeps the previous call's contents: ticket, count, error flag and
+  // tile status words must start at zero
+  check_cuda(cudaMemsetAsync(scratch, 0, (size_t)(4 + ntiles) * 8, s), "scratch zero");
+  KernelArgs a;
+  fill_args_inputs(a, cols);
+  a.tile_status = (uint64_t*)scratch + 4;
+  a.tile_counter = scratch + 0;
+  a.out_count = scratch + 1;
+  a.err = (int*)(scratch + 2);
+  a.seed = plan_.rand_seed;
+  a.capacity = capacity;
+  for (int j = 0; j < nout; j++) {
+    a.out_data[j] = out[j].data;
+    a.out_mask[j] = out[j].null_mask;
+  }
+  const JitKernel k = kernel(KernelKind::FUSED_FILTER, runtime_nullable(plan_, cols));
+  int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
+  if (grid > ntiles) grid = ntiles;
+  launch(k, (int)grid, s, a, true);
+  unsigned long long host_hdr[4] = {0, 0, 0, 0};
+  check_cuda(cudaMemcpyAsync(host_hdr, scratch, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+  check_cuda(cudaStreamSynchronize(s), "filter sync");
+  if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  const int64_t rows = (int64_t)host_hdr[1];
+  if (out_rows) *out_rows = rows;
+  if (rows > capacity) fail(GX_ERR_CAPACITY, "output capacity too small");
+  for (int j = 0; j < nout; j++) {
+    out[j].size = rows;
+    const OutSpec& o = plan_.outputs[j];
+    if (o.kind == OutSpec::BROADCAST) {
+      launch_fill(out[j].data, type_size(o.type), o.lit_bits_as_element(), rows, s);
+      launch_fill_mask(out[j].null_mask, rows, o.lit_valid, mask_words_padded(capacity), s);
+    }
+  }
+}
+
 }  // namespace gx

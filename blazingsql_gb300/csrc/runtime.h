@@ -48,6 +48,11 @@ class CompiledPlan {
  public:
   CompiledPlan(Plan p, KernelConfig cfg, int mode) : plan_(std::move(p)), cfg_(std::move(cfg)), mode_(mode) {}
 
+  // Fused single-pass filter into the caller's buffers (out[j].data / null_mask /
+  // capacity), with the kernel's scratch taken from `scratch` (scratch_words
+  // 8-byte words) instead of the memory pool.  Makes no device allocation.
+  void execute_with_scratch(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                            unsigned long long* scratch, long long scratch_words, cudaStream_t s) const;
 
   // Runs the plan over `cols`.  out must hold plan.outputs.size() entries.  If
   // out[0].data is non-null, caller-supplied buffers are used (capacity rows).
@@ -68,6 +73,10 @@ class CompiledPlan {
   KernelConfig cfg_;
   int mode_;
 };
+
+// no-allocation variant of the fused filter (noalloc.cu)
+void run_filter_noalloc(const CompiledPlan& cp, const std::vector<ColumnView>& cols, gx_column* out,
+                        int64_t* out_rows, cudaStream_t s);
 
 // diagnostics: per-thread kernel timing and a global launch counter
 void set_kernel_timing(bool on);

@@ -161,6 +161,34 @@ int gx_plan_num_conjuncts(const gx_plan* plan);
 int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_columns,
                     gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
 
+/* Runs a filter plan (condition required, at most 32 outputs) into the
+ * caller's buffers without allocating any device memory.  No counterpart in
+ * the reference.
+ *
+ * For callers that cannot allocate device memory while they evaluate a batch:
+ * an engine whose own memory pool owns the whole device budget (allocations
+ * made outside it break its accounting, and fail once it has reserved the
+ * rest of the GPU), or a per-batch path that must not enter an allocator.
+ * Same kernel and results as gx_plan_execute in GX_FILTER_SINGLE_PASS mode;
+ * the kernel's scratch (row-count, ticket and error words plus one status word
+ * per 1024-row tile) comes from a fixed 4 MiB array in the library's device
+ * memory that every GPU loading the library keeps until the process exits.
+ *
+ * - out[i].data, out[i].null_mask and out[i].capacity must be set by the
+ *   caller; null_mask must hold ((capacity + 511) / 512) * 64 bytes (>= 64).
+ * - Batches needing more than GX_NOALLOC_MAX_TILES tiles (more than
+ *   536,866,816 rows with the default tile) are rejected with GX_ERR_INVALID.
+ * - All calls share the one array (it keeps the last call's contents and is
+ *   cleared at the start of each call), so calls whose work overlaps on the
+ *   GPU -- on different streams or host threads at the same time -- race:
+ *   serialise them.
+ * - The first call on each device does set-up: it looks up the array's device
+ *   address and compiles/loads the plan's kernel if no earlier call did.  Make
+ *   that first call before any stream capture. */
+#define GX_NOALLOC_MAX_TILES 524284
+int gx_plan_execute_noalloc(const gx_plan* plan, const gx_column_view* columns, int num_columns,
+                            gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
+
 void gx_plan_destroy(gx_plan* plan);
 
 /* Library version / build information string. */
