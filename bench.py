@@ -182,6 +182,87 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def learned_compare(batches: int, rows: int, seed: int = 4):
+    """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
+    through gx_learner under three policies on the same resident batches:
+    plain fixed-order two-pass, textual-order single pass (no network), and
+    learned (warm-up and relabel batches on the plain path, training included).
+    Rows/s per policy over the whole batch stream; per-batch row counts and
+    sampled outputs must agree exactly."""
+    import numpy as np
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
+    from blazingsql_gb300 import workloads as W
+    w = W.workload("c4")
+    stream = torch.cuda.current_stream()
+    data = [W.c4_batch_device(rows, seed, b) for b in range(batches)]
+    torch.cuda.synchronize()
+    plan = g.Plan(w.schema, w.condition, w.projections, nullable=[False] * 8)
+    policies = {"plain": N.GX_LEARN_POLICY_PLAIN, "textual": N.GX_LEARN_POLICY_TEXTUAL,
+                "learned": N.GX_LEARN_POLICY_LEARNED}
+    # compile every kernel variant once outside the timed passes
+    for pol in policies.values():
+        lr = g.Learner(plan, policy=pol, warmup_batches=1, relabel_every=0)
+        for b in range(2):
+            cols, _, _ = lr.execute(data[b], stream=stream)
+            for c in cols:
+                c.free()
+    torch.cuda.synchronize()
+    res = {}
+    counts = {}
+    for name, pol in policies.items():
+        lr = g.Learner(plan, policy=pol, async_training=1)
+        infos = []
+        rows_out = []
+        L = N.lib()
+        l0 = L.gx_debug_launch_count()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for b in range(batches):
+            cols, r, info = lr.execute(data[b], stream=stream)
+            rows_out.append(r)
+            infos.append(info)
+            g.api.free_columns(cols, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        counts[name] = rows_out
+        res[name] = {"rows_per_s": rows * batches / (ms / 1e3), "ms": ms,
+                     "launches": L.gx_debug_launch_count() - l0}
+        if name == "learned":
+            res[name].update({
+                "plain_batches": sum(1 for i in infos if i["path"] == 0),
+                "reruns": sum(i["reruns"] for i in infos),
+                "final_train_loss": infos[-1]["train_loss"],
+                "orders_used": len({tuple(i["order"]) for i in infos if i["path"] == 1}),
+            })
+        del lr
+    identical = counts["plain"] == counts["textual"] == counts["learned"]
+    # sampled full-output comparison
+    checks = 0
+    for b in (0, batches // 2, batches - 1):
+        outs = []
+        for pol in (N.GX_LEARN_POLICY_PLAIN, N.GX_LEARN_POLICY_TEXTUAL):
+            cols, _, _ = g.Learner(plan, policy=pol).execute(data[b], stream=stream)
+            outs.append([c.to_host() for c in cols])
+        for x, y in zip(outs[0], outs[1]):
+            identical &= bool(np.array_equal(x.data.view(np.uint8), y.data.view(np.uint8)))
+        checks += 1
+    del data
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"c4_learned_order_filter: {batches} batches x {rows} rows, 8 Zipf(1.2) columns, 6 AND conjuncts",
+        "plain_rows_per_s": res["plain"]["rows_per_s"], "textual_rows_per_s": res["textual"]["rows_per_s"],
+        "learned_rows_per_s": res["learned"]["rows_per_s"],
+        "learned_vs_plain": res["learned"]["rows_per_s"] / res["plain"]["rows_per_s"],
+        "learned_vs_textual": res["learned"]["rows_per_s"] / res["textual"]["rows_per_s"],
+        "identical_output": identical, "row_counts_checked": batches, "full_outputs_checked": checks,
+        "detail": res,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,6 +275,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=-1, help="filter mode override (0 auto, 1 two-pass, 2 single)")
+    ap.add_argument("--learned-batches", type=int, default=64, help="C4 batches (0 skips the learned comparison)")
+    ap.add_argument("--learned-rows", type=int, default=1 << 22, help="C4 rows per batch")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -223,8 +306,7 @@ def main():
     def step():
         out = g.filter_project(cols, w.condition, w.projections, stream=stream)
         rows = out[0].size
-        for c in out:
-            c.free()
+        g.api.free_columns(out, stream)
         return rows
 
     for _ in range(args.warmup):
@@ -328,6 +410,12 @@ def main():
             dist.destroy_process_group()
         return
 
+    learned = None
+    if args.learned_batches > 0:
+        del cols
+        torch.cuda.empty_cache()
+        learned = learned_compare(args.learned_batches, args.learned_rows)
+
     # ---- CPU baseline: oracle on a bounded sample --------------------------
     nthreads = os.cpu_count() or 1
     cpu_rate, reps, el = cpu_sample_rate(args.config, w, min(args.cpu_sample_rows, n), nthreads,
@@ -350,6 +438,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "learned": learned,
     }
     print(json.dumps(line), flush=True)
     if dist:

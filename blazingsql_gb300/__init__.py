@@ -4,6 +4,8 @@ The product is the native library ``_lib/libgxeval.so`` (C ABI in
 ``include/gx_eval.h``); this package is a thin host mirror over it.
 """
 from .types import HostColumn, TypeId, pack_validity, unpack_validity  # noqa: F401
-from ._native import GxError  # noqa: F401
-from .api import (DeviceColumn, NativeColumn, Plan, evaluate_expressions, filter_project,  # noqa: F401
+from ._native import (GxError, GX_LEARN_POLICY_LEARNED, GX_LEARN_POLICY_PLAIN,  # noqa: F401
+                      GX_LEARN_POLICY_TEXTUAL)
+from .api import (DeviceColumn, Learner, NativeColumn, Plan, evaluate_expressions, filter_project,  # noqa: F401
                   process_filter, process_project, version)
+from . import api  # noqa: F401

@@ -64,6 +64,21 @@ class PlanOptions(C.Structure):
                 ("conjunct_order", C.c_int32 * 16), ("rand_seed", C.c_uint64)]
 
 
+class LearnerOptions(C.Structure):
+    _fields_ = [("policy", C.c_int32), ("warmup_batches", C.c_int32), ("relabel_every", C.c_int32),
+                ("train_steps", C.c_int32), ("learning_rate", C.c_float), ("hidden", C.c_int32),
+                ("capacity_margin", C.c_double), ("capacity_slack", C.c_int64), ("sketch_stride_words", C.c_int64),
+                ("async_training", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64)]
+
+
+class LearnedBatchInfo(C.Structure):
+    _fields_ = [("path", C.c_int32), ("reruns", C.c_int32), ("rows", C.c_int64), ("predicted_rows", C.c_int64),
+                ("train_loss", C.c_float), ("num_conjuncts", C.c_int32), ("order", C.c_int32 * 16),
+                ("predicted_sel", C.c_double * 16), ("measured_sel", C.c_double * 16)]
+
+
+GX_LEARN_POLICY_LEARNED, GX_LEARN_POLICY_PLAIN, GX_LEARN_POLICY_TEXTUAL = 0, 1, 2
+
 _lib = None
 
 
@@ -118,6 +133,20 @@ def lib():
     L.gx_debug_kernel_ms.restype = C.c_double
     L.gx_debug_launch_count.argtypes = []
     L.gx_debug_launch_count.restype = C.c_int64
+    L.gx_learner_options_init.argtypes = [P(LearnerOptions)]
+    L.gx_learner_options_init.restype = None
+    L.gx_learner_create.argtypes = [C.c_void_p, P(LearnerOptions), P(StatusInfo)]
+    L.gx_learner_create.restype = C.c_void_p
+    L.gx_learner_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64),
+                                     P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
+    L.gx_learner_save.argtypes = [C.c_void_p, C.c_char_p, P(StatusInfo)]
+    L.gx_learner_load.argtypes = [C.c_void_p, C.c_char_p, P(StatusInfo)]
+    L.gx_learner_destroy.argtypes = [C.c_void_p]
+    L.gx_learner_destroy.restype = None
+    fp = P(C.c_float)
+    L.gx_debug_learner_features.argtypes = [C.c_void_p, P(ColumnView), C.c_int, fp, C.c_int, P(C.c_int),
+                                            P(C.c_double), C.c_void_p, P(StatusInfo)]
+    L.gx_debug_mlp_grad.argtypes = [C.c_int, C.c_int, C.c_int, fp, fp, C.c_int, fp, fp, fp, fp, P(StatusInfo)]
     _lib = L
     return L
 
@@ -135,6 +164,8 @@ EXPORTED_SYMBOLS = [
     "gx_debug_kernel_source",
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
+    "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_save", "gx_learner_load",
+    "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features",
 ]
 
 

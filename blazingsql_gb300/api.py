@@ -298,6 +298,111 @@ class Plan:
             pass
 
 
+class Learner:
+    """Learned conjunct ordering over a stream of batches (gx_learner_*).
+
+    Wraps a compiled filter ``Plan``; ``execute`` filters one batch and returns
+    (columns, rows, info) where ``info`` is a dict of the batch report
+    (path 0 = plain labelled batch, 1 = single pass; order, predicted and
+    measured selectivities, re-runs, training loss)."""
+
+    def __init__(self, plan: Plan, policy: int = N.GX_LEARN_POLICY_LEARNED, **options):
+        L = N.lib()
+        o = N.LearnerOptions()
+        L.gx_learner_options_init(C.byref(o))
+        o.policy = policy
+        for k, v in options.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown learner option {k!r}")
+            setattr(o, k, v)
+        st = N.StatusInfo()
+        h = L.gx_learner_create(plan._h, C.byref(o), C.byref(st))
+        if not h:
+            raise N.GxError(st.code, st.message.decode(errors="replace"))
+        self._h = h
+        self.num_outputs = plan.num_outputs
+        self.num_conjuncts = plan.num_conjuncts
+
+    def execute(self, table: Table, stream=None):
+        keep: list = []
+        views, nc = _views(table, keep)
+        s = _stream_handle(stream)
+        n = self.num_outputs
+        outs = (N.Column * max(1, n))()
+        rows = C.c_int64(0)
+        info = N.LearnedBatchInfo()
+        st = N.StatusInfo()
+        N.check(N.lib().gx_learner_execute(self._h, views, nc, outs, C.byref(rows), C.byref(info), s, C.byref(st)),
+                st)
+        k = info.num_conjuncts
+        rep = {"path": info.path, "reruns": info.reruns, "rows": info.rows, "predicted_rows": info.predicted_rows,
+               "train_loss": info.train_loss, "order": list(info.order[:k]),
+               "predicted_sel": list(info.predicted_sel[:k]), "measured_sel": list(info.measured_sel[:k])}
+        return _wrap(outs, n, s), rows.value, rep
+
+    def features(self, table: Table, stream=None):
+        """The sketch features of one batch and the per-column anchors
+        (gx_debug_learner_features)."""
+        import numpy as np
+        keep: list = []
+        views, nc = _views(table, keep)
+        f = np.zeros(32 * 11, dtype=np.float32)
+        a = np.zeros(32, dtype=np.float64)
+        k = C.c_int(0)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_debug_learner_features(self._h, views, nc, f.ctypes.data_as(C.POINTER(C.c_float)),
+                                                  f.size, C.byref(k), a.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  _stream_handle(stream), C.byref(st)), st)
+        return f[:k.value], a[:k.value // 11]
+
+    def save(self, path: str) -> None:
+        st = N.StatusInfo()
+        N.check(N.lib().gx_learner_save(self._h, path.encode(), C.byref(st)), st)
+
+    def load(self, path: str) -> None:
+        st = N.StatusInfo()
+        N.check(N.lib().gx_learner_load(self._h, path.encode(), C.byref(st)), st)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.lib().gx_learner_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def mlp_grad(F: int, H: int, O: int, params, X, Y):
+    """One forward + backward pass of the learner's MLP on the GPU
+    (gx_debug_mlp_grad).  Returns (grad, loss, z) as numpy float32 arrays."""
+    import numpy as np
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.ascontiguousarray(Y, dtype=np.float32)
+    M = X.shape[0]
+    grad = np.zeros_like(params)
+    z = np.zeros((M, O), dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    fp = C.POINTER(C.c_float)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_debug_mlp_grad(F, H, O, params.ctypes.data_as(fp), X.ctypes.data_as(fp), M,
+                                      Y.ctypes.data_as(fp), grad.ctypes.data_as(fp), loss.ctypes.data_as(fp),
+                                      z.ctypes.data_as(fp), C.byref(st)), st)
+    return grad, float(loss[0]), z
+
+
+def free_columns(cols: Sequence[NativeColumn], stream=None) -> None:
+    """Releases library-owned output columns with one gx_free_columns call."""
+    live = [c for c in cols if c._c.data]
+    if not live:
+        return
+    arr = (N.Column * len(live))(*[c._c for c in live])
+    N.lib().gx_free_columns(arr, len(live), _stream_handle(stream) if stream is not None else live[0]._stream)
+    for c in live:
+        c._c.data = None
+        c._c.null_mask = None
+
+
 def version() -> str:
     return N.lib().gx_version().decode()
 

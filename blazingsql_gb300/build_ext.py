@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgxeval.so")
 
-SOURCES = ["frontend.cpp", "plan.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "runtime.cu", "noalloc.cu"]
+SOURCES = ["frontend.cpp", "plan.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "runtime.cu", "noalloc.cu", "learned.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -394,18 +394,28 @@ void gx_plan_destroy(gx_plan* plan) { delete plan; }
 static KernelKind kind_of(int k) {
   switch (k) {
     case 0: return KernelKind::PROJECT;
-    case 1: return KernelKind::FUSED_FILTER;
-    case 2: return KernelKind::COUNT_FILTER;
+    case 1: case 4: return KernelKind::FUSED_FILTER;
+    case 2: case 5: return KernelKind::COUNT_FILTER;
     case 3: return KernelKind::WRITE_FILTER;
-    default: fail(GX_ERR_INVALID, "kernel kind must be 0..3");
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..5");
   }
 }
 
+// kinds 4 and 5 are the learner's variants: the fused pass with the conjunct
+// order taken at launch, and the count pass with per-conjunct pass counts
 static std::string debug_source(const gx_plan* plan, int kind, const uint8_t* has_mask) {
   if (!plan) fail(GX_ERR_INVALID, "null plan");
   Plan p = plan->ps->chunks.at(0)->plan();
   for (size_t i = 0; i < p.nullable.size(); i++) p.nullable[i] = has_mask ? has_mask[i] != 0 : true;
-  return generate_kernel(p, kind_of(kind), plan->ps->chunks.at(0)->config(), "gx_kernel");
+  KernelConfig cfg = plan->ps->chunks.at(0)->config();
+  if (kind == 4 || kind == 5) {
+    cfg.short_circuit = false;
+    cfg.conjunct_order.clear();
+    cfg.runtime_order = kind == 4;
+    cfg.conj_stats = kind == 5;
+    if (kind == 4) cfg.dense = true;
+  }
+  return generate_kernel(p, kind_of(kind), cfg, "gx_kernel");
 }
 
 int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,

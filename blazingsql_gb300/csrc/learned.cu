@@ -1,0 +1,920 @@
+// learned.cu -- learned conjunct ordering and output sizing for filter plans.
+//
+// Per batch: a sampled column sketch (min, max, 8-bin histogram and null
+// fraction per column, on every `stride`-th 32-row word) feeds a small FP32
+// MLP (features -> 64 -> 64 -> one output per AND conjunct) that predicts each
+// conjunct's selectivity.  The filter then runs single pass, evaluating the
+// conjuncts most-selective first with per-word short-circuit (dead 32-row words
+// skip the remaining conjuncts' column loads), into outputs sized from the
+// predicted row count; a misprediction that overflows re-runs with the exact
+// count, so results are always identical to the plain path.  The plain
+// fixed-order two-pass evaluator supplies the training labels (it counts each
+// conjunct's passing rows) on warm-up batches and every `relabel_every`-th
+// batch, and remains the fallback.  Forward, backward and Adam run in the
+// kernels below.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "learned.h"
+
+namespace gx {
+
+// ------------------------------------------------------------------ sketches
+// Each column is sketched in a signed log distance from its anchor -- the
+// constant the condition compares it with (0 when none): t = sign(d) *
+// log1p(|d|), d = x - anchor.  Features per column: min t / 16, max t / 16, the
+// 8-bin histogram of t as cumulative fractions (bins t < -8, [-8, -4), [-4, -1),
+// [-1, 0), t == 0, (0, 1], (1, 4], > 4: the bins around 0 separate x < anchor,
+// x == anchor and x > anchor, so a conjunct's pass fraction is close to a sum
+// of bins), and the null fraction.
+constexpr int kSketchBins = 8;
+constexpr int kFeatPerCol = kSketchBins + 3;   // min, max, cumulative hist[8], null fraction
+constexpr int kPartial = kSketchBins + 4;      // min, max, hist[8], valid count, null count
+
+struct SketchCols {
+  const void* data[kMaxSketchCols];
+  const uint32_t* mask[kMaxSketchCols];
+  int64_t off[kMaxSketchCols];
+  int type[kMaxSketchCols];
+  double anchor[kMaxSketchCols];
+};
+
+__device__ __forceinline__ double sketch_value(const void* d, int type, int64_t i) {
+  switch (type) {
+    case INT8: return (double)((const signed char*)d)[i];
+    case UINT8: case BOOL8: return (double)((const unsigned char*)d)[i];
+    case INT16: return (double)((const short*)d)[i];
+    case UINT16: return (double)((const unsigned short*)d)[i];
+    case INT32: case TIMESTAMP_DAYS: case DURATION_DAYS: return (double)((const int*)d)[i];
+    case UINT32: return (double)((const unsigned*)d)[i];
+    case FLOAT32: return (double)((const float*)d)[i];
+    case FLOAT64: return ((const double*)d)[i];
+    case UINT64: return (double)((const unsigned long long*)d)[i];
+    default: return (double)((const long long*)d)[i];
+  }
+}
+
+__device__ __forceinline__ int sketch_bin(float t) {
+  if (t < 0.f) return t < -8.f ? 0 : (t < -4.f ? 1 : (t < -1.f ? 2 : 3));
+  if (t == 0.f) return 4;
+  return t <= 1.f ? 5 : (t <= 4.f ? 6 : 7);
+}
+
+// Partial sketch of column blockIdx.y over this block's share of the sampled
+// words, written to partial[col][blockIdx.x][kPartial].
+__device__ void sketch_partial_block(const SketchCols& c, int64_t n, int64_t stride_words, float* partial) {
+  const int col = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nwords = (n + 31) / 32;
+  // columns without a fixed width (none among a valid plan's inputs) are not read
+  const int64_t nsamp = c.data[col] == nullptr ? 0 : (nwords + stride_words - 1) / stride_words;
+  const double anchor = c.anchor[col];
+  float mn = INFINITY, mx = -INFINITY;
+  float hist[kSketchBins];
+#pragma unroll
+  for (int i = 0; i < kSketchBins; i++) hist[i] = 0.f;
+  float valid_n = 0.f, null_n = 0.f;
+  for (int64_t s = (int64_t)blockIdx.x * 8 + warp; s < nsamp; s += (int64_t)gridDim.x * 8) {
+    const int64_t row = s * stride_words * 32 + lane;
+    if (row >= n) continue;
+    const int64_t bit = c.off[col] + row;
+    const bool valid = c.mask[col] == nullptr || ((c.mask[col][bit >> 5] >> (bit & 31)) & 1u);
+    if (!valid) {
+      null_n += 1.f;
+      continue;
+    }
+    const float d = (float)(sketch_value(c.data[col], c.type[col], c.off[col] + row) - anchor);
+    const float t = copysignf(log1pf(fabsf(d)), d);
+    mn = fminf(mn, t);
+    mx = fmaxf(mx, t);
+    const int b = sketch_bin(t);
+#pragma unroll
+    for (int i = 0; i < kSketchBins; i++) hist[i] += (i == b) ? 1.f : 0.f;
+    valid_n += 1.f;
+  }
+  __shared__ float red[8][kPartial];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    valid_n += __shfl_xor_sync(0xffffffffu, valid_n, o);
+    null_n += __shfl_xor_sync(0xffffffffu, null_n, o);
+#pragma unroll
+    for (int i = 0; i < kSketchBins; i++) hist[i] += __shfl_xor_sync(0xffffffffu, hist[i], o);
+  }
+  if (lane == 0) {
+    red[warp][0] = mn;
+    red[warp][1] = mx;
+    for (int i = 0; i < kSketchBins; i++) red[warp][2 + i] = hist[i];
+    red[warp][2 + kSketchBins] = valid_n;
+    red[warp][3 + kSketchBins] = null_n;
+  }
+  __syncthreads();
+  if (threadIdx.x < kPartial) {
+    const int k = threadIdx.x;
+    float v = red[0][k];
+    for (int w = 1; w < 8; w++) v = k == 0 ? fminf(v, red[w][k]) : (k == 1 ? fmaxf(v, red[w][k]) : v + red[w][k]);
+    partial[((int64_t)col * gridDim.x + blockIdx.x) * kPartial + k] = v;
+  }
+}
+
+// Thread `col` reduces the column's partials (written by other blocks: read
+// past L1) into its feature row.
+__device__ void sketch_final_column(const float* partial, int col, int nparts, float* f) {
+  float mn = INFINITY, mx = -INFINITY, valid_n = 0.f, null_n = 0.f;
+  float hist[kSketchBins];
+  for (int i = 0; i < kSketchBins; i++) hist[i] = 0.f;
+  for (int b = 0; b < nparts; b++) {
+    const float* p = partial + ((int64_t)col * nparts + b) * kPartial;
+    mn = fminf(mn, __ldcg(p + 0));
+    mx = fmaxf(mx, __ldcg(p + 1));
+    for (int i = 0; i < kSketchBins; i++) hist[i] += __ldcg(p + 2 + i);
+    valid_n += __ldcg(p + 2 + kSketchBins);
+    null_n += __ldcg(p + 3 + kSketchBins);
+  }
+  f[0] = valid_n > 0.f ? mn * (1.f / 16.f) : 0.f;
+  f[1] = valid_n > 0.f ? mx * (1.f / 16.f) : 0.f;
+  float cum = 0.f;
+  for (int i = 0; i < kSketchBins; i++) {
+    cum += hist[i];
+    f[2 + i] = valid_n > 0.f ? cum / valid_n : 0.f;
+  }
+  f[2 + kSketchBins] = (valid_n + null_n) > 0.f ? null_n / (valid_n + null_n) : 0.f;
+}
+
+// ------------------------------------------------------------------ MLP
+// Parameter layout (floats): W1[H*F] b1[H] W2[H*H] b2[H] W3[O*H] b3[O].
+// Output z_o; predicted selectivity s_o = sigmoid(z_o); log s_o = -softplus(-z_o).
+// The block-level routines below are run by every thread of one CTA.
+__device__ __forceinline__ float softplusf(float x) { return fmaxf(x, 0.f) + log1pf(expf(-fabsf(x))); }
+
+// forward over M samples: H1, H2 (M*H) and Z (M*O) in global memory
+__device__ void mlp_forward_block(const float* P, int F, int H, int O, const float* X, int M, float* H1, float* H2,
+                                  float* Z) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  const float* W1 = P;
+  const float* b1 = W1 + H * F;
+  const float* W2 = b1 + H;
+  const float* b2 = W2 + H * H;
+  const float* W3 = b2 + H;
+  const float* b3 = W3 + O * H;
+  for (int i = t; i < M * H; i += nt) {
+    const int m = i / H, j = i % H;
+    float a = b1[j];
+    for (int f = 0; f < F; f++) a += W1[j * F + f] * X[(int64_t)m * F + f];
+    H1[i] = fmaxf(a, 0.f);
+  }
+  __syncthreads();
+  for (int i = t; i < M * H; i += nt) {
+    const int m = i / H, j = i % H;
+    float a = b2[j];
+    for (int k = 0; k < H; k++) a += W2[j * H + k] * H1[m * H + k];
+    H2[i] = fmaxf(a, 0.f);
+  }
+  __syncthreads();
+  for (int i = t; i < M * O; i += nt) {
+    const int m = i / O, o = i % O;
+    float a = b3[o];
+    for (int k = 0; k < H; k++) a += W3[o * H + k] * H2[m * H + k];
+    Z[i] = a;
+  }
+  __syncthreads();
+}
+
+// Gradients of L = mean_{m,o} (log sigmoid(z_mo) - Y_mo)^2 into G (layout of
+// P) and the loss into *loss; sm holds M*O + 2*M*H floats.
+__device__ void mlp_backward_block(const float* P, int F, int H, int O, const float* X, int M, const float* H1,
+                                   const float* H2, const float* Z, const float* Y, float* G, float* loss, float* sm) {
+  float* dz = sm;                 // M*O
+  float* dh2 = dz + M * O;        // M*H
+  float* dh1 = dh2 + M * H;       // M*H
+  const int t = threadIdx.x, nt = blockDim.x;
+  const float* W2 = P + H * F + H;
+  const float* W3 = W2 + H * H + H;
+  float* gW1 = G;
+  float* gb1 = gW1 + H * F;
+  float* gW2 = gb1 + H;
+  float* gb2 = gW2 + H * H;
+  float* gW3 = gb2 + H;
+  float* gb3 = gW3 + O * H;
+  const float inv = 1.f / (float)(M * O);
+  for (int i = t; i < M * O; i += nt) {
+    const float z = Z[i];
+    const float ls = -softplusf(-z);
+    const float sig_neg = 1.f / (1.f + expf(z));  // d log(sigmoid(z)) / dz
+    dz[i] = 2.f * inv * (ls - Y[i]) * sig_neg;
+  }
+  __syncthreads();
+  if (t == 0) {
+    float l = 0.f;
+    for (int i = 0; i < M * O; i++) {
+      const float d = -softplusf(-Z[i]) - Y[i];
+      l += d * d;
+    }
+    *loss = l * inv;
+  }
+  for (int i = t; i < O * H; i += nt) {
+    const int o = i / H, k = i % H;
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dz[m * O + o] * H2[m * H + k];
+    gW3[i] = g;
+  }
+  for (int o = t; o < O; o += nt) {
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dz[m * O + o];
+    gb3[o] = g;
+  }
+  for (int i = t; i < M * H; i += nt) {
+    const int m = i / H, k = i % H;
+    float g = 0.f;
+    for (int o = 0; o < O; o++) g += dz[m * O + o] * W3[o * H + k];
+    dh2[i] = H2[i] > 0.f ? g : 0.f;
+  }
+  __syncthreads();
+  for (int i = t; i < H * H; i += nt) {
+    const int j = i / H, k = i % H;
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dh2[m * H + j] * H1[m * H + k];
+    gW2[i] = g;
+  }
+  for (int j = t; j < H; j += nt) {
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dh2[m * H + j];
+    gb2[j] = g;
+  }
+  for (int i = t; i < M * H; i += nt) {
+    const int m = i / H, k = i % H;
+    float g = 0.f;
+    for (int j = 0; j < H; j++) g += dh2[m * H + j] * W2[j * H + k];
+    dh1[i] = H1[i] > 0.f ? g : 0.f;
+  }
+  __syncthreads();
+  for (int i = t; i < H * F; i += nt) {
+    const int j = i / F, f = i % F;
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dh1[m * H + j] * X[(int64_t)m * F + f];
+    gW1[i] = g;
+  }
+  for (int j = t; j < H; j += nt) {
+    float g = 0.f;
+    for (int m = 0; m < M; m++) g += dh1[m * H + j];
+    gb1[j] = g;
+  }
+  __syncthreads();
+}
+
+// Sketch of every column plus, in the last block to finish, the feature rows
+// and the network's forward pass for them (one launch per batch).  grid
+// (kSketchParts, ncols); *ticket is zero on entry and left zero.
+__global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n, int64_t stride_words, int ncols,
+                                                        float* __restrict__ partial, unsigned int* ticket,
+                                                        const float* __restrict__ P, int H, int O,
+                                                        float* __restrict__ features, float* __restrict__ act,
+                                                        float* __restrict__ Z) {
+  sketch_partial_block(c, n, stride_words, partial);
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int total = gridDim.x * gridDim.y;
+    s_last = atomicAdd(ticket, 1u) == total - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if ((int)threadIdx.x < ncols) sketch_final_column(partial, threadIdx.x, gridDim.x, features + threadIdx.x * kFeatPerCol);
+  __syncthreads();
+  if (threadIdx.x == 0) *ticket = 0u;
+  if (P) mlp_forward_block(P, ncols * kFeatPerCol, H, O, features, 1, act, act + H, Z);
+}
+
+// `steps` full-batch Adam steps over the M stored examples, one CTA; the loss
+// of the last step's forward pass goes to *loss.
+__global__ void __launch_bounds__(256) k_mlp_train(float* __restrict__ P, float* __restrict__ G,
+                                                   float* __restrict__ Mo, float* __restrict__ Ve, int F, int H,
+                                                   int O, const float* __restrict__ X, int M,
+                                                   const float* __restrict__ Y, float* __restrict__ act, int steps,
+                                                   int t0, float lr, float* __restrict__ loss) {
+  extern __shared__ float sm[];
+  const int np = H * F + H + H * H + H + O * H + O;
+  float* H1 = act;
+  float* H2 = H1 + M * H;
+  float* Z = H2 + M * H;
+  for (int it = 0; it < steps; it++) {
+    mlp_forward_block(P, F, H, O, X, M, H1, H2, Z);
+    mlp_backward_block(P, F, H, O, X, M, H1, H2, Z, Y, G, loss, sm);
+    const float tt = (float)(t0 + it + 1);
+    const float c1 = 1.f - powf(0.9f, tt), c2 = 1.f - powf(0.999f, tt);
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const float g = G[i];
+      const float m = 0.9f * Mo[i] + 0.1f * g;
+      const float v = 0.999f * Ve[i] + 0.001f * g * g;
+      Mo[i] = m;
+      Ve[i] = v;
+      P[i] -= lr * (m / c1) / (sqrtf(v / c2) + 1e-8f);
+    }
+    __syncthreads();
+  }
+}
+
+// one forward + backward pass (gradient checks)
+__global__ void __launch_bounds__(256) k_mlp_grad(const float* __restrict__ P, float* __restrict__ G, int F, int H,
+                                                  int O, const float* __restrict__ X, int M,
+                                                  const float* __restrict__ Y, float* __restrict__ act,
+                                                  float* __restrict__ loss) {
+  extern __shared__ float sm[];
+  float* H1 = act;
+  float* H2 = H1 + M * H;
+  float* Z = H2 + M * H;
+  mlp_forward_block(P, F, H, O, X, M, H1, H2, Z);
+  mlp_backward_block(P, F, H, O, X, M, H1, H2, Z, Y, G, loss, sm);
+}
+
+// labelled example `slot`: the batch's features and log pass-rate per conjunct
+__global__ void k_add_example(const float* __restrict__ feat, const unsigned long long* __restrict__ counts,
+                              long long n, int F, int O, float* __restrict__ X, float* __restrict__ Y) {
+  for (int i = threadIdx.x; i < F; i += blockDim.x) X[i] = feat[i];
+  if (threadIdx.x < O) Y[threadIdx.x] = logf((float)((double)counts[threadIdx.x] / (double)n) + 1e-6f);
+}
+
+// ------------------------------------------------------------------ host side
+int mlp_param_count(int F, int H, int O) { return H * F + H + H * H + H + O * H + O; }
+
+static void check_mlp_shape(int F, int H, int O, int M) {
+  if (F <= 0 || F > 4096 || H <= 0 || O <= 0 || H > 256 || O > 256 || M <= 0 || M * H > 4096 || M * O > 1024)
+    fail(GX_ERR_INVALID, "MLP shape out of range");
+}
+
+static int backward_smem(int H, int O, int M) { return (M * O + 2 * M * H) * 4; }
+
+void mlp_grad(const float* dP, int F, int H, int O, const float* dX, int M, const float* dY, float* dG, float* dloss,
+              float* dact, cudaStream_t s) {
+  check_mlp_shape(F, H, O, M);
+  k_mlp_grad<<<1, 256, backward_smem(H, O, M), s>>>(dP, dG, F, H, O, dX, M, dY, dact, dloss);
+  check_cuda(cudaGetLastError(), "k_mlp_grad");
+  add_launches(1);
+}
+
+static void* must_alloc(size_t bytes) {
+  void* p = nullptr;
+  const cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA, "learner device buffers");
+  }
+  return p;
+}
+
+static std::shared_ptr<CompiledPlan> variant(const CompiledPlan& base, int mode, bool stats, bool runtime_order) {
+  KernelConfig c = base.config();
+  c.short_circuit = false;
+  c.conjunct_order.clear();
+  c.conj_stats = stats;
+  c.runtime_order = runtime_order;
+  if (runtime_order) c.dense = true;
+  return std::make_shared<CompiledPlan>(base.plan(), c, mode);
+}
+
+// nanoseconds per unit of a timestamp / duration type (1 for other types)
+static double unit_ns(int t) {
+  switch (t) {
+    case TIMESTAMP_DAYS: case DURATION_DAYS: return 86400e9;
+    case TIMESTAMP_SECONDS: case DURATION_SECONDS: return 1e9;
+    case TIMESTAMP_MILLISECONDS: case DURATION_MILLISECONDS: return 1e6;
+    case TIMESTAMP_MICROSECONDS: case DURATION_MICROSECONDS: return 1e3;
+    default: return 1.0;
+  }
+}
+
+static double literal_value(const Node& n) {
+  if (n.lit_type == FLOAT64 || n.lit_type == FLOAT32) {
+    double d;
+    std::memcpy(&d, &n.lit_bits, 8);
+    return d;
+  }
+  if (n.lit_type == UINT64) return (double)n.lit_bits;
+  return (double)(int64_t)n.lit_bits;
+}
+
+// The sketch anchor of each column: the first literal a conjunct compares the
+// column with (through casts), in the column's own units; 0 when none.
+std::vector<double> sketch_anchors(const Plan& p, int ncols) {
+  std::vector<double> a(ncols, 0.0);
+  std::vector<bool> set(ncols, false);
+  auto col_of = [&](int id) {
+    while (id >= 0 && p.nodes[id].kind == Node::OP && p.nodes[id].op >= OP_CAST_TINYINT &&
+           p.nodes[id].op <= OP_CAST_TIMESTAMP)
+      id = p.nodes[id].a;
+    return (id >= 0 && p.nodes[id].kind == Node::COL) ? p.nodes[id].col : -1;
+  };
+  for (int cid : p.conjuncts) {
+    const Node& n = p.nodes[cid];
+    if (n.kind != Node::OP || n.op < OP_EQ || n.op > OP_GE) continue;
+    for (int side = 0; side < 2; side++) {
+      const int ci = col_of(side == 0 ? n.a : n.b);
+      const int li = side == 0 ? n.b : n.a;
+      if (ci < 0 || ci >= ncols || set[ci] || li < 0 || p.nodes[li].kind != Node::LIT || !p.nodes[li].lit_valid)
+        continue;
+      const Node& lit = p.nodes[li];
+      double v = literal_value(lit);
+      const int ct = p.schema[ci];
+      if ((is_timestamp(ct) || is_duration(ct)) && (is_timestamp(lit.lit_type) || is_duration(lit.lit_type)))
+        v = v * unit_ns(lit.lit_type) / unit_ns(ct);
+      a[ci] = v;
+      set[ci] = true;
+    }
+  }
+  return a;
+}
+
+Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt) {
+  const Plan& p = base.plan();
+  if (!p.has_filter()) fail(GX_ERR_INVALID, "a learner needs a plan with a condition");
+  if (p.conjuncts.size() > 16) fail(GX_ERR_UNSUPPORTED, "learned ordering supports at most 16 AND conjuncts");
+  if (opt_.hidden < 1 || opt_.hidden > 256) fail(GX_ERR_INVALID, "hidden width must be 1..256");
+  if (opt_.policy < GX_LEARN_POLICY_LEARNED || opt_.policy > GX_LEARN_POLICY_TEXTUAL)
+    fail(GX_ERR_INVALID, "unknown learner policy");
+  if (opt_.stride_words < 1) opt_.stride_words = 1;
+  plain_ = variant(base, GX_FILTER_TWO_PASS, opt_.policy == GX_LEARN_POLICY_LEARNED, false);
+  fast_ = variant(base, GX_FILTER_SINGLE_PASS, false, true);
+  ncols_ = std::min((int)p.schema.size(), kMaxSketchCols);
+  nconj_ = (int)p.conjuncts.size();
+  // cost of a conjunct: bytes per row of the distinct columns its cone reads
+  for (int c = 0; c < nconj_; c++) {
+    std::vector<int> stack{p.conjuncts[c]}, seen(p.nodes.size(), 0), colseen(p.schema.size(), 0);
+    double bytes = 0;
+    while (!stack.empty()) {
+      const int id = stack.back();
+      stack.pop_back();
+      if (id < 0 || seen[id]) continue;
+      seen[id] = 1;
+      const Node& nd = p.nodes[id];
+      if (nd.kind == Node::COL && !colseen[nd.col]) {
+        colseen[nd.col] = 1;
+        bytes += type_size(p.schema[nd.col]) + 0.125;
+      } else if (nd.kind == Node::OP) {
+        stack.push_back(nd.a);
+        stack.push_back(nd.b);
+      }
+    }
+    conj_cost_.push_back(bytes > 0 ? bytes : 0.125);
+  }
+  anchors_ = sketch_anchors(p, ncols_);
+  F_ = ncols_ * kFeatPerCol;
+  H_ = opt_.hidden;
+  O_ = nconj_;
+  nparams_ = mlp_param_count(F_, H_, O_);
+  if (opt_.policy != GX_LEARN_POLICY_LEARNED) return;  // the comparison policies need no network
+  try {
+    dparams_ = (float*)must_alloc((size_t)nparams_ * 4 * 5);  // P, G, Adam m, v, inference copy
+    dgrad_ = dparams_ + nparams_;
+    dmom_ = dgrad_ + nparams_;
+    dvel_ = dmom_ + nparams_;
+    dinfer_ = dvel_ + nparams_;
+    dfeat_ = (float*)must_alloc((size_t)F_ * 4 * (1 + kTrainRing));
+    dtrainX_ = dfeat_ + F_;
+    dtrainY_ = (float*)must_alloc((size_t)O_ * 4 * kTrainRing);
+    dact_ = (float*)must_alloc((size_t)4 * (2 * kTrainRing * H_ + kTrainRing * O_ + 4));
+    dact_inf_ = (float*)must_alloc((size_t)4 * (2 * H_ + O_ + 4));
+    dpartial_ = (float*)must_alloc((size_t)4 * kPartial * kMaxSketchCols * kSketchParts);
+    dcounts_ = (unsigned long long*)must_alloc(8 * 16);
+    dticket_ = (unsigned int*)must_alloc(16);
+    check_cuda(cudaMallocHost(&hpinned_, 4 * 32), "pinned host buffer");
+    if (opt_.async_training) {
+      check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
+      check_cuda(cudaEventCreateWithFlags(&train_done_, cudaEventDisableTiming), "event");
+      check_cuda(cudaEventCreateWithFlags(&labels_ready_, cudaEventDisableTiming), "event");
+    }
+  } catch (...) {
+    release();
+    throw;
+  }
+  // uniform(-a, a) initialisation with a = sqrt(6 / fan_in), from a fixed seed
+  std::vector<float> init(nparams_, 0.f);
+  uint64_t st = 0x9E3779B97F4A7C15ull ^ (opt_.seed * 0xD1B54A32D192ED03ull);
+  auto rnd = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return ((double)(st >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+  };
+  size_t o = 0;
+  for (int i = 0; i < H_ * F_; i++) init[o++] = (float)(rnd() * std::sqrt(6.0 / F_));
+  o += H_;
+  for (int i = 0; i < H_ * H_; i++) init[o++] = (float)(rnd() * std::sqrt(6.0 / H_));
+  o += H_;
+  for (int i = 0; i < O_ * H_; i++) init[o++] = (float)(rnd() * std::sqrt(3.0 / H_));
+  try {
+    check_cuda(cudaMemcpy(dparams_, init.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "init params");
+    check_cuda(cudaMemcpy(dinfer_, init.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "init params");
+    check_cuda(cudaMemset(dmom_, 0, (size_t)nparams_ * 8), "init adam");
+    check_cuda(cudaMemset(dticket_, 0, 16), "init ticket");
+  } catch (...) {
+    release();
+    throw;
+  }
+}
+
+void Learner::release() {
+  if (train_stream_) cudaStreamSynchronize(train_stream_);
+  cudaFree(dparams_);
+  cudaFree(dfeat_);
+  cudaFree(dtrainY_);
+  cudaFree(dact_);
+  cudaFree(dact_inf_);
+  cudaFree(dpartial_);
+  cudaFree(dcounts_);
+  cudaFree(dticket_);
+  if (hpinned_) cudaFreeHost(hpinned_);
+  if (train_done_) cudaEventDestroy(train_done_);
+  if (labels_ready_) cudaEventDestroy(labels_ready_);
+  if (train_stream_) cudaStreamDestroy(train_stream_);
+  dparams_ = dfeat_ = dtrainY_ = dact_ = dact_inf_ = dpartial_ = hpinned_ = nullptr;
+  dcounts_ = nullptr;
+  dticket_ = nullptr;
+  train_done_ = labels_ready_ = nullptr;
+  train_stream_ = nullptr;
+}
+
+Learner::~Learner() { release(); }
+
+void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s) {
+  SketchCols c{};
+  for (int i = 0; i < ncols_; i++) {
+    c.data[i] = cols[i].data;
+    c.mask[i] = cols[i].mask;
+    c.off[i] = cols[i].offset;
+    c.type[i] = cols[i].type;
+    c.anchor[i] = anchors_[i];
+    if (type_size(cols[i].type) == 0) c.data[i] = nullptr;
+  }
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  dim3 grid(kSketchParts, ncols_);
+  k_sketch_predict<<<grid, 256, 0, s>>>(c, n, opt_.stride_words, ncols_, dpartial_, dticket_,
+                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_,
+                                        dact_inf_ + 2 * H_);
+  check_cuda(cudaGetLastError(), "k_sketch_predict");
+  add_launches(1);
+}
+
+std::vector<float> Learner::features(const std::vector<ColumnView>& cols, cudaStream_t s) {
+  if (!dfeat_) fail(GX_ERR_INVALID, "this learner has no network (policy is not LEARNED)");
+  if ((int)cols.size() != (int)plain_->plan().schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  std::vector<float> f(F_, 0.f);
+  if (!cols.empty() && cols[0].size > 0) sketch(cols, false, s);
+  else check_cuda(cudaMemsetAsync(dfeat_, 0, (size_t)F_ * 4, s), "features");
+  check_cuda(cudaMemcpyAsync(f.data(), dfeat_, (size_t)F_ * 4, cudaMemcpyDeviceToHost, s), "features");
+  check_cuda(cudaStreamSynchronize(s), "features");
+  return f;
+}
+
+void Learner::sync_inference_params(cudaStream_t s) {
+  if (!params_pending_) return;
+  if (train_stream_) {
+    if (cudaEventQuery(train_done_) != cudaSuccess) {
+      cudaGetLastError();  // still training: keep predicting with the previous version
+      return;
+    }
+    check_cuda(cudaStreamWaitEvent(s, train_done_, 0), "wait training");
+  }
+  check_cuda(cudaMemcpyAsync(dinfer_, dparams_, (size_t)nparams_ * 4, cudaMemcpyDeviceToDevice, s), "params copy");
+  params_pending_ = false;
+}
+
+std::vector<float> Learner::predict_log_sel(const std::vector<ColumnView>& cols, cudaStream_t s) {
+  sync_inference_params(s);
+  sketch(cols, true, s);
+  check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, s), "prediction");
+  check_cuda(cudaStreamSynchronize(s), "prediction sync");
+  std::vector<float> ls(O_);
+  for (int o = 0; o < O_; o++) {
+    const float z = hpinned_[o];
+    ls[o] = -(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z))));  // log sigmoid(z)
+  }
+  return ls;
+}
+
+void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s) {
+  const int slot = (int)(seen_ % (uint64_t)kTrainRing);
+  // the ring must not change under a training round still running
+  if (train_stream_) check_cuda(cudaStreamWaitEvent(s, train_done_, 0), "wait training");
+  k_add_example<<<1, 128, 0, s>>>(dfeat_, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
+                                  dtrainY_ + (size_t)slot * O_);
+  check_cuda(cudaGetLastError(), "k_add_example");
+  add_launches(1);
+  seen_++;
+}
+
+void Learner::train(int steps, cudaStream_t s) {
+  // full-batch Adam over every stored example (the ring's order is irrelevant)
+  const int M = (int)std::min<uint64_t>({seen_, (uint64_t)kTrainRing, (uint64_t)(4096 / H_), (uint64_t)(1024 / O_)});
+  if (M == 0 || steps <= 0) return;
+  check_mlp_shape(F_, H_, O_, M);
+  cudaStream_t ts = s;
+  if (train_stream_) {
+    check_cuda(cudaEventRecord(labels_ready_, s), "labels event");
+    check_cuda(cudaStreamWaitEvent(train_stream_, labels_ready_, 0), "wait labels");
+    ts = train_stream_;
+  }
+  float* dloss = dact_ + 2 * kTrainRing * H_ + kTrainRing * O_;
+  k_mlp_train<<<1, 256, backward_smem(H_, O_, M), ts>>>(dparams_, dgrad_, dmom_, dvel_, F_, H_, O_, dtrainX_, M,
+                                                        dtrainY_, dact_, steps, adam_t_, opt_.lr, dloss);
+  check_cuda(cudaGetLastError(), "k_mlp_train");
+  add_launches(1);
+  adam_t_ += steps;
+  check_cuda(cudaMemcpyAsync(hpinned_ + 16, dloss, 4, cudaMemcpyDeviceToHost, ts), "loss");
+  if (train_stream_) check_cuda(cudaEventRecord(train_done_, ts), "training event");
+  params_pending_ = true;
+}
+
+void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                      gx_learned_batch_info* info, cudaStream_t s) {
+  gx_learned_batch_info bi;
+  std::memset(&bi, 0, sizeof bi);
+  bi.num_conjuncts = nconj_;
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  if ((int)cols.size() != (int)plain_->plan().schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  batches_++;
+  if (opt_.policy == GX_LEARN_POLICY_PLAIN) {
+    plain_->execute(cols, out, out_rows, s);
+    bi.rows = out_rows ? *out_rows : 0;
+    if (info) *info = bi;
+    return;
+  }
+  if (opt_.policy == GX_LEARN_POLICY_TEXTUAL) {
+    ExecExtras ex;
+    std::vector<int> order(nconj_);
+    std::iota(order.begin(), order.end(), 0);
+    ex.order = order.data();
+    ex.num_order = nconj_;
+    fast_->execute(cols, out, out_rows, s, &ex);
+    for (int o = 0; o < nconj_; o++) bi.order[o] = o;
+    bi.path = 1;
+    bi.rows = out_rows ? *out_rows : 0;
+    if (info) *info = bi;
+    return;
+  }
+  const bool warm = labelled_ < (uint64_t)opt_.warmup_batches;
+  const bool relabel = !warm && opt_.relabel_every > 0 && since_label_ >= opt_.relabel_every;
+  if (warm || relabel || n == 0) {
+    since_label_ = 0;
+    // plain fixed-order two-pass evaluator: output + per-conjunct pass counts
+    check_cuda(cudaMemsetAsync(dcounts_, 0, 8 * 16, s), "counts zero");
+    ExecExtras ex;
+    ex.conj_counts = dcounts_;
+    plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    bi.path = 0;
+    if (n > 0) {
+      sketch(cols, false, s);
+      unsigned long long cnt[16] = {0};
+      check_cuda(cudaMemcpy(cnt, dcounts_, 8 * 16, cudaMemcpyDeviceToHost), "counts");
+      for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)cnt[o] / (double)n;
+      add_example(dcounts_, n, s);
+      labelled_++;
+      train(opt_.train_steps, s);
+      if (!train_stream_) {
+        check_cuda(cudaStreamSynchronize(s), "training sync");
+        loss_ = hpinned_[16];
+      }
+    }
+    if (train_stream_ && cudaEventQuery(train_done_) == cudaSuccess) loss_ = hpinned_[16];
+    cudaGetLastError();
+    bi.train_loss = loss_;
+    bi.rows = out_rows ? *out_rows : 0;
+    if (info) *info = bi;
+    return;
+  }
+  since_label_++;
+  const std::vector<float> ls = predict_log_sel(cols, s);
+  if (train_stream_ && !params_pending_) loss_ = hpinned_[16];
+  // order by rank = cost / (1 - selectivity): cheap conjuncts that remove most rows first
+  std::vector<int> order(nconj_);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<double> rank(nconj_);
+  double log_all = 0.0;
+  for (int o = 0; o < nconj_; o++) {
+    const double sel = std::exp((double)ls[o]);
+    bi.predicted_sel[o] = sel;
+    rank[o] = conj_cost_[o] / std::max(1e-9, 1.0 - sel);
+    log_all += ls[o];
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rank[a] < rank[b]; });
+  for (int o = 0; o < nconj_; o++) bi.order[o] = order[o];
+  // output capacity from the prediction (conjuncts taken as independent), with margin
+  const double pred_rows = (double)n * std::exp(std::min(0.0, log_all));
+  bi.predicted_rows = (int64_t)pred_rows;
+  ExecExtras ex;
+  ex.order = order.data();
+  ex.num_order = nconj_;
+  ex.capacity_hint =
+      (int64_t)std::min<double>((double)n, pred_rows * opt_.capacity_margin + (double)opt_.capacity_slack);
+  const bool caller_bufs = out[0].data != nullptr;
+  try {
+    fast_->execute(cols, out, out_rows, s, &ex);
+  } catch (const Error& e) {
+    if (e.code != GX_ERR_CAPACITY || caller_bufs || !out_rows) throw;
+    // misprediction: the outputs were released; re-run with the exact row count
+    bi.reruns = 1;
+    ex.capacity_hint = *out_rows;
+    for (int j = 0; j < num_outputs(); j++) out[j] = gx_column{};
+    fast_->execute(cols, out, out_rows, s, &ex);
+  }
+  bi.train_loss = loss_;
+  bi.path = 1;
+  bi.rows = out_rows ? *out_rows : 0;
+  if (info) *info = bi;
+}
+
+void Learner::save(const std::string& path) const {
+  if (!dparams_) fail(GX_ERR_INVALID, "this learner has no network (policy is not LEARNED)");
+  if (train_stream_) check_cuda(cudaStreamSynchronize(train_stream_), "training sync");
+  std::vector<float> p(nparams_);
+  check_cuda(cudaMemcpy(p.data(), dparams_, (size_t)nparams_ * 4, cudaMemcpyDeviceToHost), "save params");
+  std::ofstream f(path, std::ios::binary);
+  // header, the sketch anchors the features were computed against, the parameters
+  const int32_t hdr[6] = {0x47584D4C /* "GXML" */, 3, F_, H_, O_, ncols_};
+  f.write((const char*)hdr, sizeof hdr);
+  f.write((const char*)anchors_.data(), (std::streamsize)anchors_.size() * 8);
+  f.write((const char*)p.data(), (std::streamsize)p.size() * 4);
+  if (!f) fail(GX_ERR_INVALID, "cannot write " + path);
+}
+
+void Learner::load(const std::string& path) {
+  if (!dparams_) fail(GX_ERR_INVALID, "this learner has no network (policy is not LEARNED)");
+  std::ifstream f(path, std::ios::binary);
+  int32_t hdr[6] = {0};
+  f.read((char*)hdr, sizeof hdr);
+  if (!f || hdr[0] != 0x47584D4C || hdr[1] != 3 || hdr[2] != F_ || hdr[3] != H_ || hdr[4] != O_ || hdr[5] != ncols_)
+    fail(GX_ERR_INVALID, "model file does not match this plan: " + path);
+  std::vector<double> anchors(ncols_);
+  std::vector<float> p(nparams_);
+  f.read((char*)anchors.data(), (std::streamsize)anchors.size() * 8);
+  f.read((char*)p.data(), (std::streamsize)p.size() * 4);
+  if (f && anchors != anchors_) fail(GX_ERR_INVALID, "model file was trained for other comparison constants: " + path);
+  if (!f) fail(GX_ERR_INVALID, "truncated model file: " + path);
+  if (train_stream_) check_cuda(cudaStreamSynchronize(train_stream_), "training sync");
+  check_cuda(cudaMemcpy(dparams_, p.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "load params");
+  check_cuda(cudaMemcpy(dinfer_, p.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "load params");
+  params_pending_ = false;
+  // a loaded network is used at once
+  labelled_ = std::max<uint64_t>(labelled_, (uint64_t)opt_.warmup_batches);
+}
+
+}  // namespace gx
+
+// ------------------------------------------------------------------ C ABI
+struct gx_learner {
+  std::unique_ptr<gx::Learner> l;
+};
+
+namespace gx {
+const CompiledPlan* single_chunk(const gx_plan* plan);  // capi.cpp
+}  // namespace gx
+
+namespace {
+void put_status(gx_status_info* st, int code, const char* msg) {
+  if (!st) return;
+  st->code = code;
+  std::snprintf(st->message, sizeof st->message, "%s", msg ? msg : "");
+}
+
+template <class F>
+int guarded_call(gx_status_info* st, F&& f) {
+  try {
+    f();
+    put_status(st, GX_OK, "");
+    return GX_OK;
+  } catch (const gx::Error& e) {
+    put_status(st, e.code, e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    put_status(st, GX_ERR_OOM, "host allocation failed");
+    return GX_ERR_OOM;
+  } catch (const std::exception& e) {
+    put_status(st, GX_ERR_INVALID, e.what());
+    return GX_ERR_INVALID;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+void gx_learner_options_init(gx_learner_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  const gx::LearnerOptions d;
+  o->policy = d.policy;
+  o->warmup_batches = d.warmup_batches;
+  o->relabel_every = d.relabel_every;
+  o->train_steps = d.train_steps;
+  o->learning_rate = d.lr;
+  o->hidden = d.hidden;
+  o->capacity_margin = d.capacity_margin;
+  o->capacity_slack = d.capacity_slack;
+  o->sketch_stride_words = d.stride_words;
+  o->async_training = d.async_training ? 1 : 0;
+  o->seed = d.seed;
+}
+
+gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* options, gx_status_info* status) {
+  gx_learner* out = nullptr;
+  guarded_call(status, [&] {
+    const gx::CompiledPlan* cp = gx::single_chunk(plan);
+    if (!cp) gx::fail(GX_ERR_INVALID, "a learner needs a compiled plan with at most 32 outputs");
+    gx_learner_options o;
+    gx_learner_options_init(&o);
+    if (options) o = *options;
+    gx::LearnerOptions lo;
+    lo.policy = o.policy;
+    lo.warmup_batches = std::max(1, o.warmup_batches);
+    lo.relabel_every = std::max(0, o.relabel_every);
+    lo.train_steps = std::max(0, o.train_steps);
+    lo.lr = o.learning_rate > 0.f ? o.learning_rate : 3e-3f;
+    lo.hidden = o.hidden > 0 ? o.hidden : 64;
+    lo.capacity_margin = o.capacity_margin >= 1.0 ? o.capacity_margin : 1.0;
+    lo.capacity_slack = std::max<int64_t>(0, o.capacity_slack);
+    lo.stride_words = o.sketch_stride_words > 0 ? o.sketch_stride_words : 64;
+    lo.async_training = o.async_training != 0;
+    lo.seed = o.seed;
+    out = new gx_learner{std::make_unique<gx::Learner>(*cp, lo)};
+  });
+  return out;
+}
+
+int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int num_columns, gx_column* out,
+                       int64_t* out_rows, gx_learned_batch_info* info, void* stream, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || !out || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "null argument");
+    learner->l->execute(gx::to_views(columns, num_columns), out, out_rows, info, (cudaStream_t)stream);
+  });
+}
+
+int gx_learner_save(const gx_learner* learner, const char* path, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || !path) gx::fail(GX_ERR_INVALID, "null argument");
+    learner->l->save(path);
+  });
+}
+
+int gx_learner_load(gx_learner* learner, const char* path, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || !path) gx::fail(GX_ERR_INVALID, "null argument");
+    learner->l->load(path);
+  });
+}
+
+void gx_learner_destroy(gx_learner* learner) { delete learner; }
+
+int gx_debug_learner_features(gx_learner* learner, const gx_column_view* columns, int num_columns, float* features,
+                              int max_features, int* num_features, double* anchors, void* stream,
+                              gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || !features || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "null argument");
+    const std::vector<float> f =
+        learner->l->features(gx::to_views(columns, num_columns), (cudaStream_t)stream);
+    if ((int)f.size() > max_features) gx::fail(GX_ERR_INVALID, "feature buffer too small");
+    std::memcpy(features, f.data(), f.size() * 4);
+    if (num_features) *num_features = (int)f.size();
+    if (anchors) {
+      const std::vector<double>& a = learner->l->anchors();
+      std::memcpy(anchors, a.data(), a.size() * 8);
+    }
+  });
+}
+
+int gx_debug_mlp_grad(int F, int H, int O, const float* params, const float* X, int M, const float* Y, float* grad,
+                      float* loss, float* z, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!params || !X || !Y || !grad || !loss || !z) gx::fail(GX_ERR_INVALID, "null argument");
+    gx::check_mlp_shape(F, H, O, M);
+    const size_t np = (size_t)gx::mlp_param_count(F, H, O);
+    const size_t floats = np * 2 + (size_t)M * F + (size_t)M * O + 2 * (size_t)M * H + (size_t)M * O + 4;
+    float* d = nullptr;
+    gx::check_cuda(cudaMalloc(&d, floats * 4), "mlp check buffers");
+    float *dP = d, *dG = dP + np, *dX = dG + np, *dY = dX + (size_t)M * F, *dA = dY + (size_t)M * O,
+          *dZ = dA + 2 * (size_t)M * H, *dL = dZ + (size_t)M * O;
+    try {
+      gx::check_cuda(cudaMemcpy(dP, params, np * 4, cudaMemcpyHostToDevice), "params");
+      gx::check_cuda(cudaMemcpy(dX, X, (size_t)M * F * 4, cudaMemcpyHostToDevice), "X");
+      gx::check_cuda(cudaMemcpy(dY, Y, (size_t)M * O * 4, cudaMemcpyHostToDevice), "Y");
+      gx::mlp_grad(dP, F, H, O, dX, M, dY, dG, dL, dA, 0);
+      gx::check_cuda(cudaMemcpy(grad, dG, np * 4, cudaMemcpyDeviceToHost), "grad");
+      gx::check_cuda(cudaMemcpy(loss, dL, 4, cudaMemcpyDeviceToHost), "loss");
+      gx::check_cuda(cudaMemcpy(z, dZ, (size_t)M * O * 4, cudaMemcpyDeviceToHost), "z");
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    cudaFree(d);
+  });
+}
+
+}  // extern "C"

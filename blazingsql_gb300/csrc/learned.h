@@ -1,0 +1,105 @@
+// learned.h -- learned conjunct ordering and output sizing (learned.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "runtime.h"
+
+namespace gx {
+
+constexpr int kMaxSketchCols = 32;
+constexpr int kSketchParts = 64;  // CTAs per column of the sketch kernel
+constexpr int kTrainRing = 64;    // labelled examples kept for training
+
+struct LearnerOptions {
+  int policy = GX_LEARN_POLICY_LEARNED;
+  int warmup_batches = 8;     // labelled batches before the network is used
+  int relabel_every = 8;      // every n-th later batch runs the plain path and trains
+  int train_steps = 16;       // Adam steps per labelled batch
+  float lr = 3e-3f;
+  double capacity_margin = 1.5;   // output rows allocated = predicted x margin + slack
+  int64_t capacity_slack = 4096;
+  int64_t stride_words = 64;  // sketch reads every n-th 32-row word
+  int hidden = 64;
+  bool async_training = false;  // train on a side stream (overlapped; prediction timing then varies)
+  uint64_t seed = 1;
+};
+
+
+// Parameters of an F -> H -> H -> O ReLU MLP, flattened:
+// W1[H*F] b1[H] W2[H*H] b2[H] W3[O*H] b3[O] (row-major, out x in).
+int mlp_param_count(int F, int H, int O);
+
+// One forward + backward pass of the MLP over M rows of dX on the GPU:
+// gradient of loss = mean over M*O of (log sigmoid(z) - Y)^2 into dG, the loss
+// into *dloss; dact holds 2*M*H + M*O floats (hidden activations, then z).
+void mlp_grad(const float* dP, int F, int H, int O, const float* dX, int M, const float* dY, float* dG, float* dloss,
+              float* dact, cudaStream_t s);
+
+// Per column of the plan: the constant a conjunct compares it with (the
+// sketch's centre), 0 when none.
+std::vector<double> sketch_anchors(const Plan& p, int ncols);
+
+class Learner {
+ public:
+  // Builds from `base` the plain fixed-order two-pass variant (counting each
+  // conjunct's passes under the LEARNED policy) and the fused single-pass
+  // variant that takes the conjunct order at launch.
+  Learner(const CompiledPlan& base, const LearnerOptions& opt);
+  ~Learner();
+  Learner(const Learner&) = delete;
+  Learner& operator=(const Learner&) = delete;
+
+  void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, gx_learned_batch_info* info,
+               cudaStream_t s);
+  void save(const std::string& path) const;
+  void load(const std::string& path);
+  // the sketch features of one batch (diagnostics)
+  std::vector<float> features(const std::vector<ColumnView>& cols, cudaStream_t s);
+  const std::vector<double>& anchors() const { return anchors_; }
+  int num_conjuncts() const { return nconj_; }
+  int num_outputs() const { return (int)fast_->plan().outputs.size(); }
+
+ private:
+  // sketch features of the batch into dfeat_ (and, with predict, the network's z)
+  void sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s);
+  std::vector<float> predict_log_sel(const std::vector<ColumnView>& cols, cudaStream_t s);
+  void add_example(const unsigned long long* counts, int64_t n, cudaStream_t s);
+  void train(int steps, cudaStream_t s);
+  void sync_inference_params(cudaStream_t s);
+  void release();
+
+  std::shared_ptr<CompiledPlan> plain_, fast_;
+  LearnerOptions opt_;
+  int ncols_ = 0, nconj_ = 0, F_ = 0, H_ = 0, O_ = 0, nparams_ = 0;
+  std::vector<double> conj_cost_;  // bytes per row the conjunct's columns read
+  std::vector<double> anchors_;    // per column: the constant its sketch is centred on
+  // device buffers
+  float* dparams_ = nullptr;  // training copy; dgrad_, dmom_, dvel_ follow
+  float* dgrad_ = nullptr;
+  float* dmom_ = nullptr;
+  float* dvel_ = nullptr;
+  float* dinfer_ = nullptr;   // inference copy of the parameters
+  float* dfeat_ = nullptr;    // current batch's features
+  float* dtrainX_ = nullptr;  // ring of labelled examples
+  float* dtrainY_ = nullptr;
+  float* dact_ = nullptr;     // training activations
+  float* dact_inf_ = nullptr; // inference activations
+  float* dpartial_ = nullptr;
+  unsigned long long* dcounts_ = nullptr;
+  unsigned int* dticket_ = nullptr;  // last-block ticket of the sketch kernel
+  float* hpinned_ = nullptr;  // pinned host: predictions + loss
+  cudaStream_t train_stream_ = nullptr;
+  cudaEvent_t train_done_ = nullptr, labels_ready_ = nullptr;
+  bool params_pending_ = false;  // training finished a version not yet copied to dinfer_
+  uint64_t seen_ = 0, labelled_ = 0, batches_ = 0;
+  int since_label_ = 0;  // single-pass batches since the last labelled one
+  int adam_t_ = 0;
+  float loss_ = 0.f;
+};
+
+}  // namespace gx

@@ -508,6 +508,10 @@ class Gen {
     }
     o << ind << "bool alive[GX_V];\n";
     o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) alive[k] = (w0 + k) * 32 + lane < a.n;\n";
+    if (cfg_.runtime_order) {
+      emit_predicate_runtime_order(o, ind);
+      return;
+    }
     std::set<int> done;
     if (!cfg_.short_circuit) {
       // fixed order: evaluate every conjunct for every row
@@ -526,18 +530,70 @@ class Gen {
       std::vector<int> ids;
       for (int id : cone({order[j]}))
         if (!done.count(id)) ids.push_back(id);
+      // loads predicated on the row being alive, issued for all words before
+      // the ballots
       o << ind << "if (any_alive) {\n";
-      o << ind << "  u32 any_ = 0;\n";
       o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) {\n";
-      o << ind << "    const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+      o << ind << "    const i64 row = (w0 + k) * 32 + lane; const bool inr = alive[k]; (void)inr;\n";
       for (int id : ids) emit_node(o, id, ind + "    ");
       o << ind << "    alive[k] = alive[k] && " << conj_keep(order[j]) << ";\n";
-      o << ind << "    any_ |= __ballot_sync(GX_FULL, alive[k]);\n";
       o << ind << "  }\n";
+      o << ind << "  u32 any_ = 0;\n";
+      o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) any_ |= __ballot_sync(GX_FULL, alive[k]);\n";
       o << ind << "  any_alive = any_ != 0u;\n";
       o << ind << "}\n";
       for (int id : ids) done.insert(id);
     }
+  }
+
+  // Short-circuit evaluation in the order a.order[] given at launch: one
+  // warp-uniform switch per conjunct, each case evaluating its conjunct's whole
+  // cone (no value crosses conjuncts) for the warp's GX_V words.  Column loads
+  // are predicated on the row still being alive, so sectors whose rows all
+  // died are not read; the words' loads are issued together (no ballot between
+  // them), and the warp stops once none of its rows is alive.
+  void emit_predicate_runtime_order(std::ostringstream& o, const std::string& ind) const {
+    const int nc = (int)p_.conjuncts.size();
+    o << ind << "u32 live_[GX_V];\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) live_[k] = __ballot_sync(GX_FULL, alive[k]);\n";
+    o << ind << "for (int j_ = 0; j_ < " << nc << "; j_++) {\n";
+    o << ind << "  bool keep_[GX_V];\n";
+    o << ind << "  switch (a.order[j_]) {\n";
+    for (int c = 0; c < nc; c++) {
+      const int cid = p_.conjuncts[c];
+      o << ind << "    case " << c << ": {\n";
+      std::vector<int> ids = cone({cid});
+      decl(o, ids, ind + "      ");
+      o << ind << "      #pragma unroll\n" << ind << "      for (int k = 0; k < GX_V; k++) {\n";
+      o << ind << "        const i64 row = (w0 + k) * 32 + lane; const bool inr = alive[k]; (void)inr;\n";
+      for (int id : ids) emit_node(o, id, ind + "        ");
+      o << ind << "        keep_[k] = " << conj_keep(cid) << ";\n";
+      o << ind << "      }\n";
+      o << ind << "      break; }\n";
+    }
+    o << ind << "    default:\n";
+    o << ind << "      #pragma unroll\n" << ind << "      for (int k = 0; k < GX_V; k++) keep_[k] = false;\n";
+    o << ind << "  }\n";
+    o << ind << "  u32 any_ = 0u;\n";
+    o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) {\n";
+    o << ind << "    alive[k] = alive[k] && keep_[k];\n";
+    o << ind << "    live_[k] = __ballot_sync(GX_FULL, alive[k]);\n";
+    o << ind << "    any_ |= live_[k];\n";
+    o << ind << "  }\n";
+    o << ind << "  if (any_ == 0u) break;\n";
+    o << ind << "}\n";
+  }
+
+  // per-conjunct pass counts of this warp's rows, accumulated in shared memory
+  void emit_conj_stats(std::ostringstream& o, const std::string& ind) const {
+    const int nc = (int)p_.conjuncts.size();
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
+    o << ind << "  const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+    for (int c = 0; c < nc; c++) {
+      o << ind << "  { const u32 b_ = __ballot_sync(GX_FULL, inr && " << conj_keep(p_.conjuncts[c]) << ");\n";
+      o << ind << "    if (lane == 0) atomicAdd(&s_conj[" << c << "], (unsigned long long)__popc(b_)); }\n";
+    }
+    o << ind << "}\n";
   }
 
   std::vector<int> predicate_cone() const { return p_.has_filter() ? cone(p_.conjuncts) : std::vector<int>{}; }
@@ -561,7 +617,7 @@ void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
        "  const void* in_data[GX_MAX_COLS]; const u32* in_mask[GX_MAX_COLS]; i64 in_off[GX_MAX_COLS];\n"
        "  void* out_data[GX_MAX_OUTS]; u32* out_mask[GX_MAX_OUTS];\n"
        "  i64 n; i64 capacity; u64* tile_status; unsigned long long* tile_counter; unsigned long long* out_count;\n"
-       "  int* err; u64 seed;\n};\n";
+       "  int* err; u64 seed; unsigned long long* conj_counts; int order[16];\n};\n";
 }
 
 // phase 2 of the filter kernels: projections for the kept rows of each word,
@@ -706,7 +762,19 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     return o.str();
   }
 
+  if ((cfg.runtime_order || cfg.conj_stats) && p.conjuncts.size() > 16)
+    fail(GX_ERR_UNSUPPORTED, "learned ordering supports at most 16 AND conjuncts");
+  // dense phase 2 recomputes every output from the gathered row; the word mode
+  // would reuse predicate values that a runtime-ordered predicate never computed
+  if (cfg.runtime_order && !cfg.dense) fail(GX_ERR_INVALID, "runtime conjunct order needs dense projections");
   const std::vector<int> pred_ids = g.predicate_cone();
+  // per-conjunct pass counts (training labels) only in the plain fixed-order count pass
+  const bool stats = kind == KernelKind::COUNT_FILTER && cfg.conj_stats && !cfg.runtime_order && !cfg.short_circuit;
+  if (stats) {
+    o << "  __shared__ unsigned long long s_conj[16];\n";
+    o << "  if (threadIdx.x < 16) s_conj[threadIdx.x] = 0ull;\n";
+    o << "  __syncthreads();\n";
+  }
   o << "  __shared__ unsigned long long s_tile;\n";
   o << "  __shared__ u64 s_w[GX_WARPS];\n";
   o << "  const i64 ntiles = (nwords + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
@@ -722,6 +790,7 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   g.decl(o, pred_ids, "    ");
   g.emit_predicate(o, "    ");
+  if (stats) g.emit_conj_stats(o, "    ");
   o << "    u32 bal[GX_V]; u32 wcnt = 0;\n";
   o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) { bal[k] = __ballot_sync(GX_FULL, alive[k]); wcnt += __popc(bal[k]); }\n";
   // per-warp exclusive offsets within the tile
@@ -751,7 +820,12 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     o << "    }\n";
   }
   o << "    __syncthreads();\n";  // s_tile / s_w reuse by the next tile
-  o << "  }\n}\n";
+  o << "  }\n";
+  if (stats) {
+    o << "  __syncthreads();\n";
+    o << "  if (threadIdx.x < " << p.conjuncts.size() << ") atomicAdd(&a.conj_counts[threadIdx.x], s_conj[threadIdx.x]);\n";
+  }
+  o << "}\n";
   return o.str();
 }
 

@@ -50,6 +50,8 @@ struct KernelConfig {
   int words = 2;           // 32-row words per warp per step
   bool emulate_fp64 = true;  // binary64 compares / divides / conversions on the integer pipes
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
+  bool runtime_order = false;  // short-circuit AND conjuncts in the order given at launch (KernelArgs::order)
+  bool conj_stats = false;     // COUNT_FILTER also counts each conjunct's passing rows
   bool short_circuit = false;
   std::vector<int> conjunct_order;  // indices into Plan::conjuncts
 };
@@ -104,6 +106,8 @@ struct KernelArgs {
   unsigned long long* out_count;
   int* err;
   uint64_t seed;
+  unsigned long long* conj_counts;  // COUNT_FILTER with conj_stats: passes per conjunct
+  int32_t order[16];                // runtime conjunct order (runtime_order kernels)
 };
 
 }  // namespace gx

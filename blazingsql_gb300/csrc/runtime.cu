@@ -1,6 +1,7 @@
 // runtime.cu -- plan execution and the library's precompiled helper kernels.
 #include "runtime.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <unordered_map>
@@ -46,6 +47,8 @@ double kernel_ms(bool reset) {
   if (reset) t_kernel_ms = 0.0;
   return v;
 }
+void add_launches(int64_t n) { g_launches.fetch_add(n); }
+
 int64_t launch_count() { return g_launches.load(); }
 
 void* dev_alloc(size_t bytes, cudaStream_t s) {
@@ -108,9 +111,73 @@ gx_column alloc_column(int type, int64_t capacity, cudaStream_t s) {
   return c;
 }
 
+// Output columns of one call share one allocation (an arena) laid out as
+// [scratch | every mask | every data buffer]; the arena is released when the
+// last of its columns is freed.  Columns are found by their data pointer.
+struct OutputArena {
+  void* base;
+  int refs;
+};
+static std::mutex g_arena_mu;
+static std::unordered_map<void*, OutputArena*> g_arena_of;
+
+void* alloc_outputs(const std::vector<int>& types, int64_t capacity, size_t scratch_bytes, bool zero_masks,
+                    gx_column* out, cudaStream_t s) {
+  const int nout = (int)types.size();
+  if (nout == 0) fail(GX_ERR_INVALID, "no output columns");
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t sb = al(scratch_bytes);
+  const size_t mb = al((size_t)mask_words_padded(capacity) * 4);
+  size_t total = sb + mb * nout;
+  std::vector<size_t> doff(nout);
+  for (int j = 0; j < nout; j++) {
+    doff[j] = total;
+    total += al(std::max<size_t>(64, (size_t)capacity * type_size(types[j])));
+  }
+  char* base = (char*)dev_alloc(total, s);
+  const size_t zero = zero_masks ? sb + mb * nout : sb;
+  if (zero) {
+    const cudaError_t e = cudaMemsetAsync(base, 0, zero, s);
+    if (e != cudaSuccess) {
+      dev_free(base, s);
+      check_cuda(e, "output arena memset");
+    }
+  }
+  auto* ar = new OutputArena{base, nout};
+  std::lock_guard<std::mutex> g(g_arena_mu);
+  for (int j = 0; j < nout; j++) {
+    out[j] = gx_column{};
+    out[j].type_id = types[j];
+    out[j].data = base + doff[j];
+    out[j].null_mask = (uint32_t*)(base + sb + mb * j);
+    out[j].capacity = capacity;
+    g_arena_of[out[j].data] = ar;
+  }
+  return sb ? base : nullptr;
+}
+
 void free_column(gx_column& c, cudaStream_t s) {
-  dev_free(c.data, s);
-  dev_free(c.null_mask, s);
+  bool in_arena = false;
+  void* release = nullptr;
+  if (c.data) {
+    std::lock_guard<std::mutex> g(g_arena_mu);
+    auto it = g_arena_of.find(c.data);
+    if (it != g_arena_of.end()) {
+      in_arena = true;
+      OutputArena* ar = it->second;
+      g_arena_of.erase(it);
+      if (--ar->refs == 0) {
+        release = ar->base;
+        delete ar;
+      }
+    }
+  }
+  if (in_arena) {
+    dev_free(release, s);
+  } else {
+    dev_free(c.data, s);
+    dev_free(c.null_mask, s);
+  }
   c.data = nullptr;
   c.null_mask = nullptr;
 }
@@ -243,11 +310,23 @@ static const char* kind_name(KernelKind k) {
 }
 
 JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable) const {
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::string key = std::to_string((int)kind) + ":" + std::to_string(dev) + ":";
+  for (bool b : nullable) key += b ? '1' : '0';
+  {
+    std::lock_guard<std::mutex> g(kmu_);
+    auto it = kcache_.find(key);
+    if (it != kcache_.end()) return it->second;
+  }
   Plan p = plan_;
   p.nullable = nullable;
   const std::string name = kind_name(kind);
   const std::string src = generate_kernel(p, kind, cfg_, name);
-  return jit_get(src, name, cfg_.warps * 32);
+  const JitKernel k = jit_get(src, name, cfg_.warps * 32);
+  std::lock_guard<std::mutex> g(kmu_);
+  kcache_[key] = k;
+  return k;
 }
 
 // Launches a plan kernel; with timing on, brackets it with events on `s`
@@ -295,13 +374,13 @@ static void fill_args_inputs(KernelArgs& a, const std::vector<ColumnView>& cols)
 }
 
 void CompiledPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
-                           cudaStream_t s) const {
+                           cudaStream_t s, const ExecExtras* extras) const {
   if (cols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
   for (size_t i = 0; i < cols.size(); i++)
     if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
   const bool caller_bufs = !plan_.outputs.empty() && out[0].data != nullptr;
   if (plan_.has_filter()) {
-    run_filter(cols, out, out_rows, caller_bufs, s);
+    run_filter(cols, out, out_rows, caller_bufs, extras, s);
   } else {
     run_project(cols, out, caller_bufs, s);
     if (out_rows) *out_rows = cols.empty() ? 0 : cols[0].size;
@@ -314,13 +393,16 @@ void CompiledPlan::run_project(const std::vector<ColumnView>& cols, gx_column* o
   const int nout = (int)plan_.outputs.size();
   std::vector<gx_column> made;
   try {
+    if (!caller_bufs && nout > 0) {
+      std::vector<int> types;
+      for (const auto& o : plan_.outputs) types.push_back(o.type);
+      alloc_outputs(types, n, 0, false, out, s);
+      made.assign(out, out + nout);
+    }
     for (int j = 0; j < nout; j++) {
       if (caller_bufs) {
         if (out[j].capacity < n || !out[j].data || !out[j].null_mask) fail(GX_ERR_CAPACITY, "output buffer too small");
         out[j].type_id = plan_.outputs[j].type;
-      } else {
-        out[j] = alloc_column(plan_.outputs[j].type, n, s);
-        made.push_back(out[j]);
       }
       out[j].size = n;
     }
@@ -343,7 +425,7 @@ void CompiledPlan::run_project(const std::vector<ColumnView>& cols, gx_column* o
     }
     if (n > 0 && plan_.needs_kernel()) {
       const JitKernel k = kernel(KernelKind::PROJECT, runtime_nullable(plan_, cols));
-      KernelArgs a;
+      KernelArgs a{};
       fill_args_inputs(a, cols);
       for (int j = 0; j < nout; j++) {
         a.out_data[j] = out[j].data;
@@ -365,7 +447,7 @@ void CompiledPlan::run_project(const std::vector<ColumnView>& cols, gx_column* o
 }
 
 void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
-                              bool caller_bufs, cudaStream_t s) const {
+                              bool caller_bufs, const ExecExtras* extras, cudaStream_t s) const {
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   const int nout = (int)plan_.outputs.size();
   const int64_t nwords = (n + 31) / 32;
@@ -388,21 +470,39 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     }
     // scratch: [0] tile counter, [1] out count, [2] err (int), [3] total, then per-tile status
     const size_t sbytes = (size_t)(4 + ntiles) * 8;
-    scratch = dev_alloc(sbytes, s);
-    unsigned long long* hdr = (unsigned long long*)scratch;
-    uint64_t* status = (uint64_t*)scratch + 4;
-    check_cuda(cudaMemsetAsync(scratch, 0, sbytes, s), "scratch memset");
+    const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
+    int64_t capacity = n;
+    if (extras && extras->capacity_hint >= 0 && extras->capacity_hint < n) capacity = extras->capacity_hint;
+    // single pass into library outputs: scratch and outputs in one arena, one
+    // memset for scratch + masks; otherwise a scratch allocation of its own
+    const bool arena = !two_pass && !caller_bufs && nout > 0;
+    void* sbase = nullptr;
+    if (arena) {
+      std::vector<int> types;
+      for (const auto& o : plan_.outputs) types.push_back(o.type);
+      sbase = alloc_outputs(types, capacity, sbytes, true, out, s);
+      made.assign(out, out + nout);
+    } else {
+      scratch = dev_alloc(sbytes, s);
+      sbase = scratch;
+      check_cuda(cudaMemsetAsync(scratch, 0, sbytes, s), "scratch memset");
+    }
+    unsigned long long* hdr = (unsigned long long*)sbase;
+    uint64_t* status = (uint64_t*)sbase + 4;
     const std::vector<bool> nb = runtime_nullable(plan_, cols);
-    KernelArgs a;
+    KernelArgs a{};
     fill_args_inputs(a, cols);
     a.tile_status = status;
     a.tile_counter = hdr + 0;
     a.out_count = hdr + 1;
     a.err = (int*)(hdr + 2);
     a.seed = plan_.rand_seed;
+    for (int i = 0; i < 16; i++) a.order[i] = i;
+    if (extras) {
+      for (int i = 0; i < extras->num_order && i < 16; i++) a.order[i] = extras->order[i];
+      a.conj_counts = extras->conj_counts;
+    }
     unsigned long long host_hdr[4] = {0, 0, 0, 0};
-    int64_t capacity = n;
-    const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
     if (two_pass) {
       const JitKernel kc = kernel(KernelKind::COUNT_FILTER, nb);
       int64_t grid = (int64_t)device_sm_count() * kc.max_blocks_per_sm;
@@ -424,14 +524,14 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
         if (out_rows) *out_rows = (int64_t)host_hdr[3];
         fail(GX_ERR_CAPACITY, "output capacity too small");
       }
-    } else {
-      for (int j = 0; j < nout; j++) {
-        out[j] = alloc_column(plan_.outputs[j].type, capacity, s);
-        made.push_back(out[j]);
-      }
+      for (int j = 0; j < nout; j++)
+        check_cuda(cudaMemsetAsync(out[j].null_mask, 0, (size_t)mask_words_padded(capacity) * 4, s), "mask zero");
+    } else if (!arena && nout > 0) {
+      std::vector<int> types;
+      for (const auto& o : plan_.outputs) types.push_back(o.type);
+      alloc_outputs(types, capacity, 0, true, out, s);
+      made.assign(out, out + nout);
     }
-    for (int j = 0; j < nout; j++)
-      check_cuda(cudaMemsetAsync(out[j].null_mask, 0, (size_t)mask_words_padded(capacity) * 4, s), "mask zero");
     for (int j = 0; j < nout; j++) {
       a.out_data[j] = out[j].data;
       a.out_mask[j] = out[j].null_mask;
@@ -501,7 +601,7 @@ void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_
   // the array keeps the previous call's contents: ticket, count, error flag and
   // tile status words must start at zero
   check_cuda(cudaMemsetAsync(scratch, 0, (size_t)(4 + ntiles) * 8, s), "scratch zero");
-  KernelArgs a;
+  KernelArgs a{};
   fill_args_inputs(a, cols);
   a.tile_status = (uint64_t*)scratch + 4;
   a.tile_counter = scratch + 0;

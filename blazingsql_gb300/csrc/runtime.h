@@ -7,6 +7,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "jit.h"
@@ -36,6 +37,14 @@ void debug_fail_allocation(int n);
 gx_column alloc_column(int type, int64_t capacity, cudaStream_t s);
 void free_column(gx_column& c, cudaStream_t s);
 
+// Per-launch extras of a filter execution (learned ordering, label counting).
+struct ExecExtras {
+  const int* order = nullptr;              // runtime conjunct order (runtime_order kernels)
+  int num_order = 0;
+  unsigned long long* conj_counts = nullptr;  // device counters, one per conjunct (conj_stats count pass)
+  int64_t capacity_hint = -1;              // library-allocated outputs: rows to allocate (-1: all input rows)
+};
+
 struct ExecStats {
   double kernel_ms = 0;      // not measured unless requested
   int64_t tiles = 0;
@@ -56,7 +65,8 @@ class CompiledPlan {
 
   // Runs the plan over `cols`.  out must hold plan.outputs.size() entries.  If
   // out[0].data is non-null, caller-supplied buffers are used (capacity rows).
-  void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const;
+  void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s,
+               const ExecExtras* extras = nullptr) const;
 
   const Plan& plan() const { return plan_; }
   const KernelConfig& config() const { return cfg_; }
@@ -67,11 +77,16 @@ class CompiledPlan {
   JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable) const;
   void run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs, cudaStream_t s) const;
   void run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, bool caller_bufs,
+                  const ExecExtras* extras,
                   cudaStream_t s) const;
 
   Plan plan_;
   KernelConfig cfg_;
   int mode_;
+  // kernel handles by (kind, nullable columns, device): generating and hashing
+  // the source is host work worth skipping on every batch
+  mutable std::mutex kmu_;
+  mutable std::unordered_map<std::string, JitKernel> kcache_;
 };
 
 // no-allocation variant of the fused filter (noalloc.cu)
@@ -82,6 +97,7 @@ void run_filter_noalloc(const CompiledPlan& cp, const std::vector<ColumnView>& c
 void set_kernel_timing(bool on);
 double kernel_ms(bool reset);
 int64_t launch_count();
+void add_launches(int64_t n);  // kernels launched outside CompiledPlan (learner)
 
 // launch helpers for precompiled kernels (runtime.cu)
 void launch_copy_mask(const uint32_t* src, int64_t src_bit, uint32_t* dst, int64_t nrows, int64_t dst_words,

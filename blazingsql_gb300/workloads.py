@@ -39,10 +39,14 @@ C2_PROJECTIONS = [
     "MOD(CASE(IS NOT NULL($0), $0, $1), 997)",
 ]
 
-C4_CONJUNCT_TEMPLATES = [
-    # (column, kind, parameter) -> rendered with per-batch constants
-    "<($0, {a})", ">($1, {b})", "=($2, {c})", "<($4, {d})", ">($5, {e})", "<($6, {f})",
-]
+# Six side-effect-free AND-ed range / equality conjuncts over Zipf(1.2) columns
+# whose support is shifted per batch, so each conjunct's selectivity moves from
+# about 0.1% to about 90% between batches ($3 and $7 are carried, not tested).
+C4_CONDITION = "AND(>($0, 100000), =($1, 1000), <($2, 1000), <($4, 1000.0), >($5, 5000.0), <($6, 100.0))"
+C4_PROJECTIONS = [f"${i}" for i in range(8)]
+C4_ZIPF_S = 1.2
+C4_ZIPF_MAX_RANK = 1_000_000
+C4_BATCH_ROWS = 1 << 22
 
 C5_CUTOFF = "1998-09-02"
 C5_CONDITION = "<=($4, 1998-09-02)"
@@ -93,6 +97,14 @@ def workload(name: str, rows: Optional[int] = None) -> Workload:
         w.in_bytes_per_row = sum(_sizes(schema)) + 6 / 8
         w.out_bytes_per_row = 8 + 8 + 2 / 8
         return w
+    if name == "c4":
+        schema = [T.INT64] * 4 + [T.FLOAT64] * 4
+        w = Workload("c4_learned_order_filter", schema, [False] * 8, C4_CONDITION, list(C4_PROJECTIONS),
+                     rows or (1 << 28))
+        w.in_bytes_per_row = 64.0
+        w.out_bytes_per_row = 64 + 8 / 8
+        w.notes = {"batch_rows": C4_BATCH_ROWS, "zipf_s": C4_ZIPF_S}
+        return w
     if name == "c5":
         schema = [T.INT32, T.INT64, T.INT64, T.INT64, T.TIMESTAMP_DAYS, T.INT8, T.INT8]
         w = Workload("c5_orderline_filter_project", schema, [False] * 7, C5_CONDITION, list(C5_PROJECTIONS),
@@ -136,6 +148,76 @@ def _np_columns(name: str, n: int, seed: int) -> List[HostColumn]:
                 HostColumn(T.INT64, tax), HostColumn(T.TIMESTAMP_DAYS, ship), HostColumn(T.INT8, f1),
                 HostColumn(T.INT8, f2)]
     raise ValueError(name)
+
+
+_ZIPF_CDF = None
+
+
+def _zipf_cdf() -> np.ndarray:
+    global _ZIPF_CDF
+    if _ZIPF_CDF is None:
+        p = np.arange(1, C4_ZIPF_MAX_RANK + 1, dtype=np.float64) ** -C4_ZIPF_S
+        c = np.cumsum(p)
+        _ZIPF_CDF = c / c[-1]
+    return _ZIPF_CDF
+
+
+def c4_shifts(seed: int, batch: int) -> List[float]:
+    """Per-batch support shifts of the 8 C4 columns (value = shift + Zipf rank
+    [+ U[0,1) for the FLOAT64 columns]).  Each shift puts its conjunct's
+    boundary at a log-uniform rank, so the conjunct's selectivity varies per
+    batch; the carried columns $3 and $7 get arbitrary shifts."""
+    r = np.random.default_rng([seed, batch, 0xC4])
+
+    def logu(lo, hi):
+        return float(np.exp(r.uniform(np.log(lo), np.log(hi))))
+
+    return [
+        float(100000 - int(logu(1, 60000))),   # >($0, 100000): P(rank > k)
+        float(1000 - int(logu(1, 30))),        # =($1, 1000):   P(rank = k)
+        float(1000 - int(logu(2, 999))),       # <($2, 1000):   P(rank < k)
+        float(int(r.integers(0, 1 << 30))),
+        1000.0 - logu(1.005, 300.0),           # <($4, 1000.0)
+        5000.0 - logu(1.5, 5000.0),            # >($5, 5000.0)
+        100.0 - logu(1.005, 60.0),             # <($6, 100.0)
+        float(r.uniform(-1e6, 1e6)),
+    ]
+
+
+def c4_batch_host(n: int, seed: int, batch: int) -> List[HostColumn]:
+    """One C4 batch as numpy columns (seeded by (seed, batch))."""
+    sh = c4_shifts(seed, batch)
+    rng = np.random.default_rng([seed, batch, 1])
+    cdf = _zipf_cdf()
+    cols = []
+    for j in range(8):
+        rank = np.searchsorted(cdf, rng.random(n), side="right").astype(np.int64) + 1
+        rank = np.minimum(rank, C4_ZIPF_MAX_RANK)
+        if j < 4:
+            cols.append(HostColumn(T.INT64, rank + np.int64(sh[j])))
+        else:
+            cols.append(HostColumn(T.FLOAT64, (rank.astype(np.float64) + rng.random(n)) + sh[j]))
+    return cols
+
+
+def c4_batch_device(n: int, seed: int, batch: int, device: str = "cuda"):
+    """One C4 batch generated on the device (inverse-CDF Zipf sampling)."""
+    import torch
+    from .api import DeviceColumn
+    sh = c4_shifts(seed, batch)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed) * 1_000_003 + int(batch))
+    cdf = torch.from_numpy(_zipf_cdf()).to(device)
+    cols = []
+    for j in range(8):
+        u = torch.rand(n, generator=gen, device=device, dtype=torch.float64)
+        rank = torch.clamp(torch.searchsorted(cdf, u, right=True) + 1, max=C4_ZIPF_MAX_RANK)
+        if j < 4:
+            v = rank + int(sh[j])
+        else:
+            v = rank.to(torch.float64) + torch.rand(n, generator=gen, device=device, dtype=torch.float64) + sh[j]
+        cols.append(DeviceColumn(T.INT64 if j < 4 else T.FLOAT64, v.contiguous().view(torch.uint8), None, 0, n))
+    return cols
 
 
 def host_columns(name: str, n: int, seed: int = 1) -> List[HostColumn]:

@@ -191,13 +191,82 @@ int gx_plan_execute_noalloc(const gx_plan* plan, const gx_column_view* columns, 
 
 void gx_plan_destroy(gx_plan* plan);
 
+/* ---- learned conjunct ordering (no counterpart in the reference) ---------
+ *
+ * A learner wraps a compiled filter plan (condition = AND of side-effect-free
+ * conjuncts, at most 16) for a stream of batches of one schema, as the batched
+ * execution graph's Filter kernel produces them (BatchProcessing.cpp:371-476).
+ * Per batch it sketches every column (min, max, 8-bin histogram, null
+ * fraction of a sample of 32-row words), predicts each conjunct's selectivity
+ * with a small FP32 MLP (features -> 64 -> 64 -> conjuncts), evaluates the
+ * conjuncts in predicted order with per-word short-circuit in one fused pass
+ * into outputs sized from the predicted row count, and re-runs with the exact
+ * count when the prediction was too small.  The plain fixed-order two-pass
+ * evaluator runs the warm-up batches and every relabel_every-th batch after;
+ * its per-conjunct pass counts are the training labels, and the network is
+ * trained on the GPU after each of them.  Output is bit-identical to
+ * gx_plan_execute with the same plan whatever the policy or prediction. */
+typedef struct gx_learner gx_learner;
+
+enum {
+  GX_LEARN_POLICY_LEARNED = 0, /* network order + predicted capacity (warm-up / relabel on the plain path) */
+  GX_LEARN_POLICY_PLAIN = 1,   /* always the plain fixed-order two-pass path */
+  GX_LEARN_POLICY_TEXTUAL = 2  /* single pass, conjuncts short-circuited in textual order, full capacity */
+};
+
+typedef struct gx_learner_options {
+  int32_t policy;          /* GX_LEARN_POLICY_* */
+  int32_t warmup_batches;  /* plain labelled batches before the network is used (default 8) */
+  int32_t relabel_every;   /* later batches: every n-th runs the plain path and trains (default 8; 0 never) */
+  int32_t train_steps;     /* Adam steps per labelled batch (default 16) */
+  float learning_rate;     /* default 3e-3 */
+  int32_t hidden;          /* hidden width (default 64, at most 256) */
+  double capacity_margin;  /* rows allocated = predicted rows x margin + slack (default 1.5) */
+  int64_t capacity_slack;  /* default 4096 */
+  int64_t sketch_stride_words; /* sketch every n-th 32-row word (default 64) */
+  int32_t async_training;  /* 1: train on a side stream, overlapped with later batches */
+  int32_t reserved;
+  uint64_t seed;           /* parameter initialisation */
+} gx_learner_options;
+
+/* Per-batch report of gx_learner_execute. */
+typedef struct gx_learned_batch_info {
+  int32_t path;             /* 0 plain two-pass (labelled), 1 single pass */
+  int32_t reruns;           /* single-pass re-runs after an output-size misprediction */
+  int64_t rows;
+  int64_t predicted_rows;
+  float train_loss;         /* loss of the latest finished training round */
+  int32_t num_conjuncts;
+  int32_t order[16];        /* evaluation order used (single pass) */
+  double predicted_sel[16]; /* network's selectivity per conjunct (single pass) */
+  double measured_sel[16];  /* plain path's measured selectivity per conjunct (path 0) */
+} gx_learned_batch_info;
+
+void gx_learner_options_init(gx_learner_options* options);
+
+/* Creates a learner for a plan made by gx_plan_compile (with a condition and at
+ * most 32 outputs).  The plan may be destroyed afterwards. */
+gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* options, gx_status_info* status);
+
+/* Filters one batch; same arguments and output contract as gx_plan_execute
+ * (library-allocated outputs when out[0].data is NULL).  info may be NULL. */
+int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int num_columns, gx_column* out,
+                       int64_t* out_rows, gx_learned_batch_info* info, void* stream, gx_status_info* status);
+
+/* Network parameters to / from a file (the plan's shape must match). */
+int gx_learner_save(const gx_learner* learner, const char* path, gx_status_info* status);
+int gx_learner_load(gx_learner* learner, const char* path, gx_status_info* status);
+void gx_learner_destroy(gx_learner* learner);
+
 /* Library version / build information string. */
 const char* gx_version(void);
 
 /* ---- diagnostics (no counterpart in the reference) --------------------- */
 
 /* Generated CUDA source of a plan kernel: kind 0 project, 1 fused single-pass
- * filter, 2 filter count pass, 3 filter write pass.  Writes at most buf_len
+ * filter, 2 filter count pass, 3 filter write pass, 4 the learner's fused pass
+ * (conjunct order given at launch), 5 the learner's labelling count pass
+ * (per-conjunct pass counts).  Writes at most buf_len
  * bytes (NUL-terminated) and returns the full length, or -1 on error. */
 int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,
                                int64_t buf_len, gx_status_info* status);
@@ -227,6 +296,23 @@ int64_t gx_debug_launch_count(void);
  * CASE / ROUND / CAST-literal lowering) and writes it back as text, the way the
  * reference's parse_tree::rebuildExpression prints it. */
 int gx_debug_rebuild_expression(const char* expression, char* buf, int buf_len, gx_status_info* status);
+
+/* One forward + backward pass of the learner's MLP on the GPU, for checking
+ * gradients: params (gx_learner MLP layout W1[H*F] b1[H] W2[H*H] b2[H] W3[O*H]
+ * b3[O], row-major out x in), X[M*F], Y[M*O] are host arrays; writes the
+ * gradient of loss = mean((log sigmoid(z) - Y)^2) into grad (same layout), the
+ * loss and the outputs z[M*O].  M*H <= 4096, M*O <= 1024, H <= 256. */
+/* The learner's sketch of one batch: ncols x 11 features (per column: min and
+ * max of t / 16, the 8-bin histogram of t as cumulative fractions, the null
+ * fraction; t = sign(d) log1p(|d|), d = value - anchor, on every
+ * sketch_stride_words-th 32-row word), and optionally the per-column anchors
+ * (doubles).  LEARNED policy only. */
+int gx_debug_learner_features(gx_learner* learner, const gx_column_view* columns, int num_columns, float* features,
+                              int max_features, int* num_features, double* anchors, void* stream,
+                              gx_status_info* status);
+
+int gx_debug_mlp_grad(int F, int H, int O, const float* params, const float* X, int M, const float* Y, float* grad,
+                      float* loss, float* z, gx_status_info* status);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,247 @@
+"""Learned conjunct ordering: MLP oracle, GPU gradients, and learned-path parity.
+
+The learner must return exactly what the plain fixed-order two-pass evaluator
+returns for every batch (same rows, order, values and validity), whatever the
+network predicts; its network's forward/backward kernels must match the float64
+oracle; and the trained network must choose better conjunct orders than the
+textual order it replaces.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from blazingsql_gb300 import workloads as W
+from blazingsql_gb300.types import TypeId as T
+from oracle import mlp_ref
+
+from helpers import assert_tables_equal
+
+
+# ------------------------------------------------------------------ CPU
+def test_mlp_oracle_matches_finite_differences():
+    rng = np.random.default_rng(7)
+    F, H, O, M = 11, 8, 3, 5
+    p = rng.normal(0, 0.5, mlp_ref.param_count(F, H, O))
+    X = rng.random((M, F))
+    Y = np.log(rng.random((M, O)) * 0.9 + 1e-3)
+    g, L, _ = mlp_ref.grad(p, X, Y, F, H, O)
+    assert L == pytest.approx(mlp_ref.loss(p, X, Y, F, H, O))
+    idx = np.arange(0, len(p), 3)
+    fd = mlp_ref.finite_difference(p, X, Y, F, H, O, idx)
+    np.testing.assert_allclose(g[idx], fd, rtol=1e-5, atol=1e-8)
+
+
+def test_word_loads_counts_short_circuit():
+    keep_a = np.zeros(64, dtype=bool)
+    keep_a[3] = True          # word 0 survives conjunct a, word 1 dies
+    keep_b = np.ones(64, dtype=bool)
+    assert mlp_ref.word_loads([1, 1], [keep_a, keep_b], [0, 1]) == 2 + 1
+    assert mlp_ref.word_loads([1, 1], [keep_a, keep_b], [1, 0]) == 2 + 2
+
+
+def test_c4_generator_selectivity_ranges():
+    """Per-batch selectivities of the six conjuncts spread over about 0.1%..90%."""
+    sels = []
+    for b in range(24):
+        x = [c.data for c in W.c4_batch_host(1 << 16, 4, b)]
+        sels.append([(x[0] > 100000).mean(), (x[1] == 1000).mean(), (x[2] < 1000).mean(),
+                     (x[4] < 1000.0).mean(), (x[5] > 5000.0).mean(), (x[6] < 100.0).mean()])
+    s = np.array(sels)
+    assert s.min() < 0.01 and s.max() > 0.85
+    # the most selective conjunct changes between batches
+    assert len(set(np.argmin(s, axis=1))) >= 2
+
+
+def test_learner_kernels_compile():
+    """NVRTC compiles the learner's two kernel variants for sm_103a (no GPU)."""
+    import blazingsql_gb300 as g
+    plan = g.Plan(W.workload("c4").schema, W.C4_CONDITION, W.C4_PROJECTIONS, nullable=[False] * 8)
+    assert plan.num_conjuncts == 6
+    src = plan.kernel_source(4, [False] * 8)
+    assert "switch (a.order[j_])" in src
+    assert "s_conj" in plan.kernel_source(5, [False] * 8)
+    plan.compile_check(4, [False] * 8)
+    plan.compile_check(5, [False] * 8)
+
+
+# ------------------------------------------------------------------ GPU
+def _upload(cols):
+    from blazingsql_gb300.api import DeviceColumn
+    return [DeviceColumn.from_host(c) for c in cols]
+
+
+def _host(cols):
+    return [c.to_host() for c in cols]
+
+
+def _c4_plan(g):
+    return g.Plan(W.workload("c4").schema, W.C4_CONDITION, W.C4_PROJECTIONS, nullable=[False] * 8)
+
+
+@pytest.mark.gpu
+def test_mlp_gradients_match_oracle():
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(11)
+    for F, H, O, M in [(88, 64, 6, 64), (11, 16, 3, 7), (33, 64, 16, 1)]:
+        p = rng.normal(0, 0.3, mlp_ref.param_count(F, H, O)).astype(np.float32)
+        X = rng.random((M, F)).astype(np.float32)
+        Y = np.log(rng.random((M, O)) + 1e-6).astype(np.float32)
+        grad, loss, z = g.api.mlp_grad(F, H, O, p, X, Y)
+        eg, eloss, ez = mlp_ref.grad(p.astype(np.float64), X, Y, F, H, O)
+        np.testing.assert_allclose(z, ez, rtol=1e-4, atol=1e-4 * max(1.0, np.abs(ez).max()))
+        assert loss == pytest.approx(eloss, rel=1e-4)
+        np.testing.assert_allclose(grad, eg, rtol=1e-3, atol=1e-4 * np.abs(eg).max())
+
+
+@pytest.mark.gpu
+def test_sketch_features_match_oracle():
+    """The sketch kernels against the oracle's sketch, with the anchors taken
+    from the condition's constants; nulls and a column offset included."""
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    plan = _c4_plan(g)
+    lr = g.Learner(plan, sketch_stride_words=4)
+    for b, n in ((0, 1 << 16), (1, 40_000 + 17)):
+        host = W.c4_batch_host(n, 9, b)
+        f, anchors = lr.features(_upload(host))
+        np.testing.assert_array_equal(anchors, [100000, 1000, 1000, 0, 1000.0, 5000.0, 100.0, 0])
+        exp = mlp_ref.sketch_features([c.data for c in host], [None] * 8, anchors, 4)
+        np.testing.assert_allclose(f, exp, rtol=1e-5, atol=1e-6)
+    # nullable columns with an offset: INT32 / FLOAT64 with 20% nulls
+    other = g.Plan([T.INT32, T.FLOAT64], "AND(>($0, 10), <=($1, -2.5))", ["$0", "$1"])
+    lr2 = g.Learner(other, sketch_stride_words=2)
+    rng = np.random.default_rng(3)
+    n, off = 50_000, 37
+    x0 = rng.integers(-100, 100, n + off).astype(np.int32)
+    x1 = rng.normal(0, 10, n + off)
+    v0 = rng.random(n + off) > 0.2
+    v1 = rng.random(n + off) > 0.2
+    cols = [g.HostColumn(T.INT32, x0, g.pack_validity(v0)), g.HostColumn(T.FLOAT64, x1, g.pack_validity(v1))]
+    dev = [DeviceColumn.from_host(c) for c in cols]
+    for d in dev:
+        d.offset, d.size = off, n
+    f, anchors = lr2.features(dev)
+    np.testing.assert_array_equal(anchors, [10, -2.5])
+    exp = mlp_ref.sketch_features([x0[off:], x1[off:]], [v0[off:], v1[off:]], anchors, 2)
+    np.testing.assert_allclose(f, exp, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_learned_matches_plain_and_oracle():
+    """Warm-up, learned single-pass and relabel batches all return the plain
+    path's output; a few batches are also checked against the CPU oracle."""
+    import blazingsql_gb300 as g
+    from helpers import OracleEngine
+    plan = _c4_plan(g)
+    learned = g.Learner(plan, warmup_batches=4, relabel_every=5, train_steps=32)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    oracle = OracleEngine(nthreads=4)
+    paths = set()
+    for b in range(14):
+        host = W.c4_batch_host(1 << 16, 4, b)
+        dev = _upload(host)
+        got, rows, info = learned.execute(dev)
+        exp, erows, _ = plain.execute(dev)
+        assert rows == erows == info["rows"]
+        assert_tables_equal(_host(got), _host(exp), what=f"batch {b} path {info['path']}")
+        paths.add(info["path"])
+        if b in (0, 6, 13):
+            ref = oracle.filter_project(host, W.C4_CONDITION, W.C4_PROJECTIONS)
+            assert_tables_equal(_host(got), ref, what=f"oracle batch {b}")
+        if info["path"] == 1:
+            assert sorted(info["order"]) == list(range(6))
+    assert paths == {0, 1}
+
+
+@pytest.mark.gpu
+def test_learned_misprediction_reruns():
+    """With no capacity margin the predicted output size is often too small; the
+    single pass re-runs with the exact count and the result still matches."""
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    learned = g.Learner(plan, warmup_batches=2, relabel_every=0, train_steps=4, capacity_margin=1.0,
+                        capacity_slack=0)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    reruns = 0
+    for b in range(10):
+        dev = _upload(W.c4_batch_host(1 << 15, 5, b))
+        got, rows, info = learned.execute(dev)
+        exp, erows, _ = plain.execute(dev)
+        assert rows == erows
+        assert_tables_equal(_host(got), _host(exp), what=f"batch {b}")
+        reruns += info["reruns"]
+    assert reruns > 0
+
+
+@pytest.mark.gpu
+def test_learner_policies_agree_and_async_training():
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    textual = g.Learner(plan, policy=g.GX_LEARN_POLICY_TEXTUAL)
+    asyn = g.Learner(plan, warmup_batches=3, relabel_every=2, async_training=1)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    for b in range(8):
+        dev = _upload(W.c4_batch_host((1 << 14) + 77 * b, 6, b))
+        exp, erows, _ = plain.execute(dev)
+        for lr in (textual, asyn):
+            got, rows, _ = lr.execute(dev)
+            assert rows == erows
+            assert_tables_equal(_host(got), _host(exp), what=f"batch {b}")
+
+
+@pytest.mark.gpu
+def test_learner_save_load_and_empty_batch(tmp_path):
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    a = g.Learner(plan, warmup_batches=3, relabel_every=0, train_steps=8)
+    for b in range(3):
+        a.execute(_upload(W.c4_batch_host(1 << 14, 7, b)))
+    path = os.path.join(str(tmp_path), "c4.gxml")
+    a.save(path)
+    b_ = g.Learner(plan, warmup_batches=3, relabel_every=0)
+    b_.load(path)
+    dev = _upload(W.c4_batch_host(1 << 14, 7, 9))
+    ga, ra, ia = a.execute(dev)
+    gb, rb, ib = b_.execute(dev)
+    assert ia["path"] == ib["path"] == 1
+    assert ia["order"] == ib["order"]
+    np.testing.assert_allclose(ia["predicted_sel"], ib["predicted_sel"], rtol=1e-6)
+    assert_tables_equal(_host(ga), _host(gb))
+    # an empty batch: zero rows through the plain path
+    empty = _upload([c for c in W.c4_batch_host(0, 7, 0)])
+    cols, rows, info = a.execute(empty)
+    assert rows == 0 and all(c.size == 0 for c in cols)
+    other = g.Plan([T.INT64, T.INT64], "AND(>($0, 1), <($1, 5))", ["$0"])
+    c = g.Learner(other)
+    with pytest.raises(g.GxError):
+        c.load(path)
+
+
+@pytest.mark.gpu
+def test_trained_network_beats_textual_order():
+    """What the network gains over the method without it: over batches after
+    warm-up, its conjunct orders read fewer 32-row column words (counted on the
+    host from the batch's own pass vectors) than the textual order, and come
+    close to the per-batch best order."""
+    import itertools
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    learned = g.Learner(plan, warmup_batches=12, relabel_every=0, train_steps=48)
+    cost = [1] * 6
+    totals = {"learned": 0, "textual": 0, "best": 0}
+    for b in range(28):
+        host = W.c4_batch_host(1 << 16, 8, b)
+        _, _, info = learned.execute(_upload(host))
+        if info["path"] != 1:
+            continue
+        x = [c.data for c in host]
+        keep = [x[0] > 100000, x[1] == 1000, x[2] < 1000, x[4] < 1000.0, x[5] > 5000.0, x[6] < 100.0]
+        totals["learned"] += mlp_ref.word_loads(cost, keep, info["order"])
+        totals["textual"] += mlp_ref.word_loads(cost, keep, list(range(6)))
+        totals["best"] += min(mlp_ref.word_loads(cost, keep, list(o)) for o in itertools.permutations(range(6)))
+    assert totals["learned"] > 0
+    assert totals["learned"] <= 0.9 * totals["textual"], totals
+    assert totals["learned"] <= 1.15 * totals["best"], totals
