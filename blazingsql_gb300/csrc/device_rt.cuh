@@ -142,44 +142,99 @@ __device__ __forceinline__ u64 gx_ld_acquire(const u64* p) {
   return v;
 }
 
-// Exclusive prefix of tile `tile` given its aggregate; called by one full warp.
-// Waits are bounded: after `max_spins` polls without progress it records an
-// error in *err and returns ~0ull (callers then skip their writes).
-__device__ __forceinline__ u64 gx_lookback(u64* status, i64 tile, u64 agg, int* err, u32 max_spins) {
+__device__ __forceinline__ u64 gx_ld_relaxed(const u64* p) {
+  u64 v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Exclusive prefix of tile `tile` whose aggregate `agg` is already published
+// (gx_tile_publish); called by one full warp; publishes the tile's inclusive
+// prefix.
+// Each poll reads a window of the 128 preceding status words (4 per lane,
+// lane l holding distances 4l+1 .. 4l+4), sums the aggregates up to the
+// nearest inclusive prefix, and moves 128 tiles further back while none is in
+// the window -- with hundreds of tiles in flight the prefix frontier is that
+// far back, so a wide window saves L2 round trips.  A status word carries its
+// flag and value together, so relaxed loads suffice.  Waits are bounded: after
+// `max_spins` polls without progress it records an error in *err and returns
+// ~0ull (callers then skip their writes); a wait also ends early once *err is
+// set by another tile.
+__device__ __forceinline__ u64 gx_lookback_resolve(u64* status, i64 tile, u64 agg, int* err, u32 max_spins) {
   const int lane = threadIdx.x & 31;
-  if (tile == 0) {
-    if (lane == 0) gx_st_release(status, GX_ST_PFX | agg);
-    return 0ull;
-  }
-  if (lane == 0) gx_st_release(status + tile, GX_ST_AGG | agg);
+  if (tile == 0) return 0ull;  // published as a prefix already
   u64 excl = 0;
-  i64 pred = tile - 1;
+  i64 pred = tile - 1;  // distance 1
   u32 spins = 0;
   while (true) {
-    const i64 idx = pred - lane;
-    u64 s = idx >= 0 ? gx_ld_acquire(status + idx) : GX_ST_PFX;  // before tile 0: prefix 0
-    const u32 flag = (u32)(s >> 62);
-    const u32 not_ready = __ballot_sync(GX_FULL, flag == 0);
-    const u32 is_pfx = __ballot_sync(GX_FULL, flag == 2);
-    // lanes up to (and including) the first prefix must all be ready
-    const u32 upto = is_pfx ? ((is_pfx & (0u - is_pfx)) << 1) - 1u : GX_FULL;
-    if (not_ready & upto) {
+    u64 s[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const i64 idx = pred - (lane * 4 + i);
+      s[i] = idx >= 0 ? gx_ld_relaxed(status + idx) : GX_ST_PFX;  // before tile 0: prefix 0
+    }
+    int first_pfx = 4;
+#pragma unroll
+    for (int i = 3; i >= 0; i--)
+      if ((u32)(s[i] >> 62) == 2u) first_pfx = i;
+    const u32 has_pfx = __ballot_sync(GX_FULL, first_pfx < 4);
+    const int pl = has_pfx ? __ffs(has_pfx) - 1 : 0;
+    const int pfx_i = __shfl_sync(GX_FULL, first_pfx, pl);
+    // entries at window positions <= last (4 lane + i) are needed
+    const int last = has_pfx ? pl * 4 + pfx_i : 127;
+    bool missing = false;
+    u64 v = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (lane * 4 + i <= last) {
+        if ((u32)(s[i] >> 62) == 0u) missing = true;
+        v += s[i] & GX_ST_VAL;
+      }
+    }
+    if (__any_sync(GX_FULL, missing)) {
       if (++spins > max_spins) {
         if (lane == 0) atomicExch(err, 1);
         return ~0ull;
       }
+      // another tile already gave up: its successors never complete, stop now
+      if ((spins & 255u) == 0u && *(volatile int*)err != 0) return ~0ull;
       __nanosleep(32);
       continue;
     }
-    u64 v = ((1u << lane) & upto) ? (s & GX_ST_VAL) : 0ull;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(GX_FULL, v, o);
     excl += v;
-    if (is_pfx) break;
-    pred -= 32;
+    if (has_pfx) break;
+    pred -= 128;
   }
   if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (excl + agg));
   return excl;
+}
+
+// Publishes a tile's aggregate (tile 0: its inclusive prefix) from the
+// per-warp kept-row counts cnt[0..nw), writes each warp's exclusive offset
+// within the tile to off[], and returns the tile's total; called by one full
+// warp.
+__device__ __forceinline__ u64 gx_tile_publish(u64* status, i64 tile, const u32* cnt, u64* off, int nw) {
+  const int lane = threadIdx.x & 31;
+  const u64 c = lane < nw ? (u64)cnt[lane] : 0ull;
+  u64 incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const u64 t = __shfl_up_sync(GX_FULL, incl, d);
+    if (lane >= d) incl += t;
+  }
+  const u64 total = __shfl_sync(GX_FULL, incl, 31);
+  if (lane < nw) off[lane] = incl - c;
+  if (lane == 0) gx_st_release(status + tile, (tile == 0 ? GX_ST_PFX : GX_ST_AGG) | total);
+  return total;
+}
+
+// Publish + resolve in one step (tile loops without a pipeline).
+__device__ __forceinline__ u64 gx_lookback(u64* status, i64 tile, u64 agg, int* err, u32 max_spins) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) gx_st_release(status + tile, (tile == 0 ? GX_ST_PFX : GX_ST_AGG) | agg);
+  return gx_lookback_resolve(status, tile, agg, err, max_spins);
 }
 
 // Appends `nbits` compressed validity bits to a warp's output bit stream.

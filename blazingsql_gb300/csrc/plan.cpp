@@ -497,6 +497,28 @@ class Gen {
     return "(" + V(cid) + " && " + nz(cid) + ")";
   }
 
+  // Evaluates nodes `ids` for the warp's GX_V words: first a loop issuing every
+  // column load of every word (so the loads are in flight together), then a
+  // loop computing the operators and `tail` (a statement per word).  `inr` is
+  // the per-row condition that loads are predicated on.
+  void emit_words(std::ostringstream& o, const std::vector<int>& ids, const std::string& ind, const std::string& inr,
+                  const std::string& tail) const {
+    const std::string rowdef = "const i64 row = (w0 + k) * 32 + lane; const bool inr = " + inr + "; (void)inr;\n";
+    bool any_col = false;
+    for (int id : ids) any_col |= p_.nodes[id].kind == Node::COL;
+    if (any_col) {
+      o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n" << ind << "  " << rowdef;
+      for (int id : ids)
+        if (p_.nodes[id].kind == Node::COL) emit_node(o, id, ind + "  ");
+      o << ind << "}\n";
+    }
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n" << ind << "  " << rowdef;
+    for (int id : ids)
+      if (p_.nodes[id].kind != Node::COL) emit_node(o, id, ind + "  ");
+    if (!tail.empty()) o << ind << "  " << tail << "\n";
+    o << ind << "}\n";
+  }
+
   // predicate phase: fills keep bits bal[k]; with short-circuit, conjuncts are
   // evaluated in cfg order and later conjuncts skipped for all-dead warps
   void emit_predicate(std::ostringstream& o, const std::string& ind) const {
@@ -515,14 +537,9 @@ class Gen {
     std::set<int> done;
     if (!cfg_.short_circuit) {
       // fixed order: evaluate every conjunct for every row
-      o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
-      o << ind << "  const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
-      for (int id : cone(order))
-        emit_node(o, id, ind + "  ");
       std::string keep = "inr";
       for (int c : order) keep += " && " + conj_keep(c);
-      o << ind << "  alive[k] = " << keep << ";\n";
-      o << ind << "}\n";
+      emit_words(o, cone(order), ind, "row < a.n", "alive[k] = " + keep + ";");
       return;
     }
     o << ind << "bool any_alive = true;\n";
@@ -533,11 +550,7 @@ class Gen {
       // loads predicated on the row being alive, issued for all words before
       // the ballots
       o << ind << "if (any_alive) {\n";
-      o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) {\n";
-      o << ind << "    const i64 row = (w0 + k) * 32 + lane; const bool inr = alive[k]; (void)inr;\n";
-      for (int id : ids) emit_node(o, id, ind + "    ");
-      o << ind << "    alive[k] = alive[k] && " << conj_keep(order[j]) << ";\n";
-      o << ind << "  }\n";
+      emit_words(o, ids, ind + "  ", "alive[k]", "alive[k] = alive[k] && " + conj_keep(order[j]) + ";");
       o << ind << "  u32 any_ = 0;\n";
       o << ind << "  #pragma unroll\n" << ind << "  for (int k = 0; k < GX_V; k++) any_ |= __ballot_sync(GX_FULL, alive[k]);\n";
       o << ind << "  any_alive = any_ != 0u;\n";
@@ -564,11 +577,7 @@ class Gen {
       o << ind << "    case " << c << ": {\n";
       std::vector<int> ids = cone({cid});
       decl(o, ids, ind + "      ");
-      o << ind << "      #pragma unroll\n" << ind << "      for (int k = 0; k < GX_V; k++) {\n";
-      o << ind << "        const i64 row = (w0 + k) * 32 + lane; const bool inr = alive[k]; (void)inr;\n";
-      for (int id : ids) emit_node(o, id, ind + "        ");
-      o << ind << "        keep_[k] = " << conj_keep(cid) << ";\n";
-      o << ind << "      }\n";
+      emit_words(o, ids, ind + "      ", "alive[k]", "keep_[k] = " + conj_keep(cid) + ";");
       o << ind << "      break; }\n";
     }
     o << ind << "    default:\n";
@@ -639,9 +648,15 @@ void emit_dense_store(std::ostringstream& o, const Gen& g, const Plan& p, size_t
   } else {
     return;  // broadcast outputs are filled after the launch
   }
-  o << ind << "{ const u32 vb_ = __ballot_sync(GX_FULL, act && " << vexpr << ");\n";
-  o << ind << "  if (bw_[" << j << "].word < cap_words) bw_[" << j << "].append(a.out_mask[" << j
-    << "], vb_, nb); else { bw_[" << j << "].fill = 0; } }\n";
+  o << ind << "acc_[" << j << "] |= (u64)__ballot_sync(GX_FULL, act && " << vexpr << ") << bf_;\n";
+}
+
+// outputs that carry a validity bit stream (broadcasts are filled after the launch)
+std::vector<size_t> masked_outputs(const Plan& p) {
+  std::vector<size_t> v;
+  for (size_t j = 0; j < p.outputs.size(); j++)
+    if (p.outputs[j].kind != OutSpec::BROADCAST) v.push_back(j);
+  return v;
 }
 
 // Dense phase 2: the warp's kept rows, in row order, are dealt to lanes in
@@ -654,8 +669,13 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   o << ind << "u32 cum_[GX_V + 1]; cum_[0] = 0u;\n";
   o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++) cum_[kk + 1] = cum_[kk] + __popc(bal[kk]);\n";
   o << ind << "const u32 total_ = cum_[GX_V];\n";
-  o << ind << "GxBitWriter bw_[" << p.outputs.size() << "];\n";
-  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << p.outputs.size() << "; j++) bw_[j].init((i64)pos);\n";
+  // validity bit streams: one position shared by all outputs (every round
+  // appends the same number of bits to each), one accumulator per output; the
+  // first word may be shared with the previous warp's range and the last with
+  // the next one (atomicOr), words in between are stored
+  o << ind << "u64 acc_[" << p.outputs.size() << "];\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << p.outputs.size() << "; j++) acc_[j] = 0ull;\n";
+  o << ind << "int bf_ = (int)(pos & 31ull); i64 bword_ = (i64)(pos >> 5); bool bfirst_ = bf_ != 0;\n";
   o << ind << "const i64 cap_words = (a.capacity + 31) >> 5;\n";
   o << ind << "for (u32 base_ = 0; base_ < total_; base_ += 32u) {\n";
   const std::string in2 = ind + "  ";
@@ -668,15 +688,29 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   o << in2 << "const i64 orow = (i64)pos + (i64)t_; (void)orow;\n";
   o << in2 << "const int k = 0;\n";
   g.decl(o, proj, in2);
-  for (int id : proj) g.emit_node(o, id, in2);
+  // gathers first, then the operators
+  for (int id : proj)
+    if (p.nodes[id].kind == Node::COL) g.emit_node(o, id, in2);
+  for (int id : proj)
+    if (p.nodes[id].kind != Node::COL) g.emit_node(o, id, in2);
   o << in2 << "const bool wr = act && orow < a.capacity;\n";
   o << in2 << "const int nb = (int)min(32u, total_ - base_);\n";
   for (size_t j = 0; j < p.outputs.size(); j++) emit_dense_store(o, g, p, j, in2);
+  const std::vector<size_t> mo = masked_outputs(p);
+  o << in2 << "const int nf_ = bf_ + nb;\n";
+  o << in2 << "if (nf_ >= 32) {\n";
+  o << in2 << "  if (lane == 0 && bword_ < cap_words) {\n";
+  for (size_t j : mo)
+    o << in2 << "    if (bfirst_) atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]); else a.out_mask[" << j
+      << "][bword_] = (u32)acc_[" << j << "];\n";
+  o << in2 << "  }\n";
+  o << in2 << "  #pragma unroll\n" << in2 << "  for (int j = 0; j < " << p.outputs.size() << "; j++) acc_[j] >>= 32;\n";
+  o << in2 << "  bfirst_ = false; bword_++; bf_ = nf_ - 32;\n";
+  o << in2 << "} else {\n" << in2 << "  bf_ = nf_;\n" << in2 << "}\n";
   o << ind << "}\n";
-  for (size_t j = 0; j < p.outputs.size(); j++) {
-    if (p.outputs[j].kind == OutSpec::BROADCAST) continue;
-    o << ind << "if (bw_[" << j << "].word < cap_words) bw_[" << j << "].flush(a.out_mask[" << j << "]);\n";
-  }
+  o << ind << "if (bf_ > 0 && lane == 0 && bword_ < cap_words) {\n";
+  for (size_t j : mo) o << ind << "  atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]);\n";
+  o << ind << "}\n";
 }
 
 void emit_filter_writes(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
@@ -733,6 +767,74 @@ void emit_filter_writes(std::ostringstream& o, const Gen& g, const Plan& p, cons
   }
 }
 
+// Fused single-pass filter (dense projections) as a two-stage tile pipeline:
+// a block claims tile t+1 and evaluates its predicate before it resolves tile
+// t's output offset by look-back, so the look-back of t waits on tiles that
+// had a whole tile's time to publish, and the next tile's loads are in flight
+// meanwhile.  Tile t's keep masks stay in registers between the stages (dense
+// projections recompute outputs from the gathered rows).  A claimed tile's
+// aggregate is published before the block waits on anything, and a tile's
+// look-back only needs earlier tiles, so the pipeline cannot deadlock.
+void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids) {
+  o << "  __shared__ unsigned long long s_claim;\n";
+  o << "  __shared__ u32 s_cnt[2][GX_WARPS];\n";
+  o << "  __shared__ u64 s_off[2][GX_WARPS];\n";
+  o << "  __shared__ u64 s_base;\n";
+  o << "  const i64 ntiles = (nwords + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
+  o << "  if (threadIdx.x == 0) s_claim = atomicAdd(a.tile_counter, 1ull);\n";
+  o << "  __syncthreads();\n";
+  o << "  i64 tile = (i64)s_claim;\n";
+  o << "  if (tile >= ntiles) return;\n";
+  o << "  u32 bal[GX_V]; u32 wcnt = 0u; int par = 0; u64 ptotal = 0ull;\n";
+  o << "  {\n";
+  o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  g.decl(o, pred_ids, "    ");
+  g.emit_predicate(o, "    ");
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) { bal[k] = __ballot_sync(GX_FULL, alive[k]); wcnt += __popc(bal[k]); }\n";
+  o << "    if (lane == 0) s_cnt[0][warp] = wcnt;\n";
+  o << "  }\n";
+  o << "  __syncthreads();\n";
+  o << "  if (warp == 0) ptotal = gx_tile_publish(a.tile_status, tile, s_cnt[0], s_off[0], GX_WARPS);\n";
+  o << "  while (true) {\n";
+  o << "    if (threadIdx.x == 0) s_claim = atomicAdd(a.tile_counter, 1ull);\n";
+  o << "    __syncthreads();\n";
+  o << "    const i64 next = (i64)s_claim;\n";
+  o << "    const int npar = par ^ 1;\n";
+  o << "    u32 nbal[GX_V]; u32 nwcnt = 0u;\n";
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) nbal[k] = 0u;\n";
+  o << "    if (next < ntiles) {\n";
+  o << "      const i64 w0 = next * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  g.decl(o, pred_ids, "      ");
+  g.emit_predicate(o, "      ");
+  o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) { nbal[k] = __ballot_sync(GX_FULL, alive[k]); nwcnt += __popc(nbal[k]); }\n";
+  o << "      if (lane == 0) s_cnt[npar][warp] = nwcnt;\n";
+  o << "    }\n";
+  o << "    __syncthreads();\n";
+  o << "    if (warp == 0) {\n";
+  o << "      u64 ntotal = 0ull;\n";
+  o << "      if (next < ntiles) ntotal = gx_tile_publish(a.tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
+  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, 1u << 22);\n";
+  o << "      if (lane == 0) {\n";
+  o << "        s_base = excl;\n";
+  o << "        if (tile == ntiles - 1 && excl != ~0ull) *a.out_count = excl + ptotal;\n";
+  o << "      }\n";
+  o << "      ptotal = ntotal;\n";
+  o << "    }\n";
+  o << "    __syncthreads();\n";
+  o << "    const u64 base_t = s_base;\n";
+  o << "    if (base_t == ~0ull) break;\n";  // look-back gave up: error already recorded
+  o << "    if (wcnt != 0u) {\n";
+  o << "      u64 pos = base_t + s_off[par][warp];\n";
+  o << "      const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  emit_filter_writes_dense(o, g, p, "      ");
+  o << "    }\n";
+  o << "    if (next >= ntiles) break;\n";
+  o << "    tile = next; par = npar; wcnt = nwcnt;\n";
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) bal[k] = nbal[k];\n";
+  o << "  }\n";
+  o << "}\n";
+}
+
 }  // namespace
 
 std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg, const std::string& name) {
@@ -747,10 +849,17 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     o << "  for (i64 w0 = ((i64)blockIdx.x * GX_WARPS + warp) * GX_V; w0 < nwords;"
          " w0 += (i64)gridDim.x * GX_WARPS * GX_V) {\n";
     g.decl(o, ids, "    ");
+    // every column load of the warp's words first, then operators and stores
+    o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) {\n";
+    o << "      const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+    for (int id : ids)
+      if (p.nodes[id].kind == Node::COL) g.emit_node(o, id, "      ");
+    o << "    }\n";
     o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) {\n";
     o << "      const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
     o << "      const i64 orow = row; (void)orow;\n";
-    for (int id : ids) g.emit_node(o, id, "      ");
+    for (int id : ids)
+      if (p.nodes[id].kind != Node::COL) g.emit_node(o, id, "      ");
     for (size_t j = 0; j < p.outputs.size(); j++) {
       const OutSpec& os = p.outputs[j];
       if (os.kind != OutSpec::NODE) continue;
@@ -774,6 +883,10 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     o << "  __shared__ unsigned long long s_conj[16];\n";
     o << "  if (threadIdx.x < 16) s_conj[threadIdx.x] = 0ull;\n";
     o << "  __syncthreads();\n";
+  }
+  if (kind == KernelKind::FUSED_FILTER && cfg.dense) {
+    emit_fused_pipelined(o, g, p, pred_ids);
+    return o.str();
   }
   o << "  __shared__ unsigned long long s_tile;\n";
   o << "  __shared__ u64 s_w[GX_WARPS];\n";
