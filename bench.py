@@ -212,7 +212,7 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     res = {}
     counts = {}
     for name, pol in policies.items():
-        lr = g.Learner(plan, policy=pol, async_training=1)
+        lr = g.Learner(plan, policy=pol, async_training=1, relabel_every=16)
         infos = []
         rows_out = []
         L = N.lib()

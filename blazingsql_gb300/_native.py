@@ -122,6 +122,8 @@ def lib():
     L.gx_debug_kernel_source.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), C.c_char_p, C.c_int64, P(StatusInfo)]
     L.gx_debug_kernel_source.restype = C.c_int64
     L.gx_debug_compile_check.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(StatusInfo)]
+    L.gx_debug_kernel_resources.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(C.c_int32), P(C.c_int32),
+                                            P(C.c_int32), P(StatusInfo)]
     L.gx_debug_fail_allocation.argtypes = [C.c_int]
     L.gx_debug_fail_allocation.restype = None
     L.gx_debug_jit_stats.argtypes = [P(C.c_int64), P(C.c_double)]
@@ -165,7 +167,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_save", "gx_learner_load",
-    "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features",
+    "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
 ]
 
 

@@ -284,6 +284,15 @@ class Plan:
         L.gx_debug_kernel_source(self._h, kind, hm, buf, n + 1, C.byref(st))
         return buf.value.decode()
 
+    def resources(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None):
+        """(registers, spill bytes, static shared bytes) of a plan kernel for sm_103a."""
+        st = N.StatusInfo()
+        hm = None if has_mask is None else (C.c_uint8 * len(has_mask))(*[1 if x else 0 for x in has_mask])
+        r, sp, sh = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        N.check(N.lib().gx_debug_kernel_resources(self._h, kind, hm, C.byref(r), C.byref(sp), C.byref(sh),
+                                                  C.byref(st)), st)
+        return r.value, sp.value, sh.value
+
     def compile_check(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None) -> None:
         st = N.StatusInfo()
         hm = None if has_mask is None else (C.c_uint8 * len(has_mask))(*[1 if x else 0 for x in has_mask])

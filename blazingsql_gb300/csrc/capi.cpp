@@ -433,6 +433,16 @@ int gx_debug_compile_check(const gx_plan* plan, int kind, const uint8_t* column_
   return guarded(status, [&] { jit_compile_check(debug_source(plan, kind, column_has_mask), "gx_kernel"); });
 }
 
+int gx_debug_kernel_resources(const gx_plan* plan, int kind, const uint8_t* column_has_mask, int32_t* registers,
+                              int32_t* spill_bytes, int32_t* shared_bytes, gx_status_info* status) {
+  return guarded(status, [&] {
+    const KernelResources r = jit_resources(debug_source(plan, kind, column_has_mask), "gx_kernel");
+    if (registers) *registers = r.registers;
+    if (spill_bytes) *spill_bytes = r.spill_bytes;
+    if (shared_bytes) *shared_bytes = r.shared_bytes;
+  });
+}
+
 void gx_debug_fail_allocation(int n) { debug_fail_allocation(n); }
 
 void gx_debug_set_kernel_timing(int enable) { set_kernel_timing(enable != 0); }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <cctype>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -57,13 +58,15 @@ std::string cubin_cache_path(uint64_t h) {
   return std::string(dir) + buf;
 }
 
-std::vector<char> compile_cubin(const std::string& src, const std::string& name) {
+// ptxas_log (optional) receives the assembler's resource report
+std::vector<char> compile_cubin(const std::string& src, const std::string& name, std::string* ptxas_log = nullptr) {
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 0, nullptr, nullptr) != NVRTC_SUCCESS)
     fail(GX_ERR_CUDA, "nvrtcCreateProgram failed");
   const char* opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "-default-device", "--std=c++17",
-                        "-lineinfo"};
-  nvrtcResult r = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+                        "-lineinfo", "--ptxas-options=-v"};
+  const int nopts = (int)(sizeof(opts) / sizeof(opts[0])) - (ptxas_log ? 0 : 1);
+  nvrtcResult r = nvrtcCompileProgram(prog, nopts, opts);
   if (r != NVRTC_SUCCESS) {
     size_t ls = 0;
     nvrtcGetProgramLogSize(prog, &ls);
@@ -75,6 +78,12 @@ std::vector<char> compile_cubin(const std::string& src, const std::string& name)
       f << src;
     }
     fail(GX_ERR_CUDA, "NVRTC compile of " + name + " failed: " + log.substr(0, 400));
+  }
+  if (ptxas_log) {
+    size_t ls = 0;
+    nvrtcGetProgramLogSize(prog, &ls);
+    ptxas_log->assign(ls, '\0');
+    nvrtcGetProgramLog(prog, &(*ptxas_log)[0]);
   }
   size_t cs = 0;
   nvrtcGetCUBINSize(prog, &cs);
@@ -155,6 +164,26 @@ JitKernel jit_get(const std::string& body, const std::string& name, int block_th
 
 void jit_compile_check(const std::string& body, const std::string& name) {
   compile_cubin(std::string(kPrelude) + "\n" + body, name);
+}
+
+static int number_before(const std::string& log, const std::string& suffix) {
+  const size_t at = log.find(suffix);
+  if (at == std::string::npos) return 0;
+  size_t b = at;
+  while (b > 0 && log[b - 1] == ' ') b--;
+  size_t e = b;
+  while (b > 0 && std::isdigit((unsigned char)log[b - 1])) b--;
+  return b < e ? std::atoi(log.substr(b, e - b).c_str()) : 0;
+}
+
+KernelResources jit_resources(const std::string& body, const std::string& name) {
+  std::string log;
+  compile_cubin(std::string(kPrelude) + "\n" + body, name, &log);
+  KernelResources r;
+  r.registers = number_before(log, "registers");
+  r.spill_bytes = number_before(log, "bytes spill stores");
+  r.shared_bytes = number_before(log, "bytes smem");
+  return r;
 }
 
 const char* jit_prelude() { return kPrelude; }

@@ -20,6 +20,14 @@ struct JitKernel {
 // the device runtime prelude) for the current device.
 JitKernel jit_get(const std::string& body, const std::string& name, int block_threads);
 
+// Assembler resource report of a kernel (NVRTC + ptxas, no device needed).
+struct KernelResources {
+  int registers = 0;
+  int spill_bytes = 0;
+  int shared_bytes = 0;
+};
+KernelResources jit_resources(const std::string& body, const std::string& name);
+
 // NVRTC compile only (no device needed); throws GX_ERR_CUDA with the log.
 void jit_compile_check(const std::string& body, const std::string& name);
 

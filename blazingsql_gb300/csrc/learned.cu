@@ -126,28 +126,42 @@ __device__ void sketch_partial_block(const SketchCols& c, int64_t n, int64_t str
   }
 }
 
-// Thread `col` reduces the column's partials (written by other blocks: read
-// past L1) into its feature row.
-__device__ void sketch_final_column(const float* partial, int col, int nparts, float* f) {
+// One warp reduces column `col`'s partials (written by other blocks: read
+// past L1) into its 11 features f[] (lane 0 writes).
+__device__ void sketch_final_warp(const float* partial, int col, int nparts, float* f) {
+  const int lane = threadIdx.x & 31;
   float mn = INFINITY, mx = -INFINITY, valid_n = 0.f, null_n = 0.f;
   float hist[kSketchBins];
+#pragma unroll
   for (int i = 0; i < kSketchBins; i++) hist[i] = 0.f;
-  for (int b = 0; b < nparts; b++) {
+  for (int b = lane; b < nparts; b += 32) {
     const float* p = partial + ((int64_t)col * nparts + b) * kPartial;
     mn = fminf(mn, __ldcg(p + 0));
     mx = fmaxf(mx, __ldcg(p + 1));
+#pragma unroll
     for (int i = 0; i < kSketchBins; i++) hist[i] += __ldcg(p + 2 + i);
     valid_n += __ldcg(p + 2 + kSketchBins);
     null_n += __ldcg(p + 3 + kSketchBins);
   }
-  f[0] = valid_n > 0.f ? mn * (1.f / 16.f) : 0.f;
-  f[1] = valid_n > 0.f ? mx * (1.f / 16.f) : 0.f;
-  float cum = 0.f;
-  for (int i = 0; i < kSketchBins; i++) {
-    cum += hist[i];
-    f[2 + i] = valid_n > 0.f ? cum / valid_n : 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    valid_n += __shfl_xor_sync(0xffffffffu, valid_n, o);
+    null_n += __shfl_xor_sync(0xffffffffu, null_n, o);
+#pragma unroll
+    for (int i = 0; i < kSketchBins; i++) hist[i] += __shfl_xor_sync(0xffffffffu, hist[i], o);
   }
-  f[2 + kSketchBins] = (valid_n + null_n) > 0.f ? null_n / (valid_n + null_n) : 0.f;
+  if (lane == 0) {
+    f[0] = valid_n > 0.f ? mn * (1.f / 16.f) : 0.f;
+    f[1] = valid_n > 0.f ? mx * (1.f / 16.f) : 0.f;
+    float cum = 0.f;
+    for (int i = 0; i < kSketchBins; i++) {
+      cum += hist[i];
+      f[2 + i] = valid_n > 0.f ? cum / valid_n : 0.f;
+    }
+    f[2 + kSketchBins] = (valid_n + null_n) > 0.f ? null_n / (valid_n + null_n) : 0.f;
+  }
 }
 
 // ------------------------------------------------------------------ MLP
@@ -156,36 +170,58 @@ __device__ void sketch_final_column(const float* partial, int col, int nparts, f
 // The block-level routines below are run by every thread of one CTA.
 __device__ __forceinline__ float softplusf(float x) { return fmaxf(x, 0.f) + log1pf(expf(-fabsf(x))); }
 
+// y[m][j] = act(b[j] + sum_i W[j][i] x[m][i]) for every sample m and unit j:
+// each warp takes 4 (m, j) dot products at a time, lanes striding over i, so
+// weight rows are read coalesced and four rows' loads are in flight together.
+__device__ void dense_layer_block(const float* W, const float* bias, int In, int Out, const float* X, int M,
+                                  float* Y, bool relu) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int units = M * Out;
+  for (int u0 = warp * 4; u0 < units; u0 += nw * 4) {
+    const float* w[4];
+    const float* x[4];
+    float acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int u = min(u0 + q, units - 1);
+      w[q] = W + (int64_t)(u % Out) * In;
+      x[q] = X + (int64_t)(u / Out) * In;
+      acc[q] = 0.f;
+    }
+    for (int i = lane; i < In; i += 32) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[q] += w[q][i] * x[q][i];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    }
+    if (lane < 4 && u0 + lane < units) {
+      float v = acc[0];
+#pragma unroll
+      for (int q = 1; q < 4; q++) v = lane == q ? acc[q] : v;
+      const int u = u0 + lane;
+      v += bias[u % Out];
+      Y[u] = relu ? fmaxf(v, 0.f) : v;
+    }
+  }
+}
+
 // forward over M samples: H1, H2 (M*H) and Z (M*O) in global memory
 __device__ void mlp_forward_block(const float* P, int F, int H, int O, const float* X, int M, float* H1, float* H2,
                                   float* Z) {
-  const int t = threadIdx.x, nt = blockDim.x;
   const float* W1 = P;
   const float* b1 = W1 + H * F;
   const float* W2 = b1 + H;
   const float* b2 = W2 + H * H;
   const float* W3 = b2 + H;
   const float* b3 = W3 + O * H;
-  for (int i = t; i < M * H; i += nt) {
-    const int m = i / H, j = i % H;
-    float a = b1[j];
-    for (int f = 0; f < F; f++) a += W1[j * F + f] * X[(int64_t)m * F + f];
-    H1[i] = fmaxf(a, 0.f);
-  }
+  dense_layer_block(W1, b1, F, H, X, M, H1, true);
   __syncthreads();
-  for (int i = t; i < M * H; i += nt) {
-    const int m = i / H, j = i % H;
-    float a = b2[j];
-    for (int k = 0; k < H; k++) a += W2[j * H + k] * H1[m * H + k];
-    H2[i] = fmaxf(a, 0.f);
-  }
+  dense_layer_block(W2, b2, H, H, H1, M, H2, true);
   __syncthreads();
-  for (int i = t; i < M * O; i += nt) {
-    const int m = i / O, o = i % O;
-    float a = b3[o];
-    for (int k = 0; k < H; k++) a += W3[o * H + k] * H2[m * H + k];
-    Z[i] = a;
-  }
+  dense_layer_block(W3, b3, H, O, H2, M, Z, false);
   __syncthreads();
 }
 
@@ -277,8 +313,7 @@ __device__ void mlp_backward_block(const float* P, int F, int H, int O, const fl
 __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n, int64_t stride_words, int ncols,
                                                         float* __restrict__ partial, unsigned int* ticket,
                                                         const float* __restrict__ P, int H, int O,
-                                                        float* __restrict__ features, float* __restrict__ act,
-                                                        float* __restrict__ Z) {
+                                                        float* __restrict__ features, float* __restrict__ Z) {
   sketch_partial_block(c, n, stride_words, partial);
   __shared__ bool s_last;
   __threadfence();
@@ -290,10 +325,29 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  if ((int)threadIdx.x < ncols) sketch_final_column(partial, threadIdx.x, gridDim.x, features + threadIdx.x * kFeatPerCol);
+  // features into shared memory (the forward pass reads them) and global
+  // memory (a labelled batch's training example)
+  __shared__ float s_x[kMaxSketchCols * kFeatPerCol];
+  __shared__ float s_h[2 * 256];
+  for (int col = threadIdx.x >> 5; col < ncols; col += blockDim.x >> 5)
+    sketch_final_warp(partial, col, gridDim.x, s_x + col * kFeatPerCol);
   __syncthreads();
+  const int F = ncols * kFeatPerCol;
+  for (int i = threadIdx.x; i < F; i += blockDim.x) features[i] = s_x[i];
   if (threadIdx.x == 0) *ticket = 0u;
-  if (P) mlp_forward_block(P, ncols * kFeatPerCol, H, O, features, 1, act, act + H, Z);
+  if (P) {
+    const float* W1 = P;
+    const float* b1 = W1 + H * F;
+    const float* W2 = b1 + H;
+    const float* b2 = W2 + H * H;
+    const float* W3 = b2 + H;
+    const float* b3 = W3 + O * H;
+    dense_layer_block(W1, b1, F, H, s_x, 1, s_h, true);
+    __syncthreads();
+    dense_layer_block(W2, b2, H, H, s_h, 1, s_h + 256, true);
+    __syncthreads();
+    dense_layer_block(W3, b3, H, O, s_h + 256, 1, Z, false);
+  }
 }
 
 // `steps` full-batch Adam steps over the M stored examples, one CTA; the loss
@@ -487,7 +541,9 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     dpartial_ = (float*)must_alloc((size_t)4 * kPartial * kMaxSketchCols * kSketchParts);
     dcounts_ = (unsigned long long*)must_alloc(8 * 16);
     dticket_ = (unsigned int*)must_alloc(16);
-    check_cuda(cudaMallocHost(&hpinned_, 4 * 32), "pinned host buffer");
+    // pinned host block: predictions z[16], the loss at [16], conjunct counts from byte 256
+    check_cuda(cudaMallocHost(&hpinned_, 512), "pinned host buffer");
+    hcounts_ = (unsigned long long*)((char*)hpinned_ + 256);
     if (opt_.async_training) {
       check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
       check_cuda(cudaEventCreateWithFlags(&train_done_, cudaEventDisableTiming), "event");
@@ -559,8 +615,7 @@ void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStre
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   dim3 grid(kSketchParts, ncols_);
   k_sketch_predict<<<grid, 256, 0, s>>>(c, n, opt_.stride_words, ncols_, dpartial_, dticket_,
-                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_,
-                                        dact_inf_ + 2 * H_);
+                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_ + 2 * H_);
   check_cuda(cudaGetLastError(), "k_sketch_predict");
   add_launches(1);
 }
@@ -670,13 +725,12 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     check_cuda(cudaMemsetAsync(dcounts_, 0, 8 * 16, s), "counts zero");
     ExecExtras ex;
     ex.conj_counts = dcounts_;
+    ex.conj_counts_host = hcounts_;  // read back with the count pass's own readback
     plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
     bi.path = 0;
     if (n > 0) {
       sketch(cols, false, s);
-      unsigned long long cnt[16] = {0};
-      check_cuda(cudaMemcpy(cnt, dcounts_, 8 * 16, cudaMemcpyDeviceToHost), "counts");
-      for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)cnt[o] / (double)n;
+      for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)hcounts_[o] / (double)n;
       add_example(dcounts_, n, s);
       labelled_++;
       train(opt_.train_steps, s);

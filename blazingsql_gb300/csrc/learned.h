@@ -93,6 +93,7 @@ class Learner {
   unsigned long long* dcounts_ = nullptr;
   unsigned int* dticket_ = nullptr;  // last-block ticket of the sketch kernel
   float* hpinned_ = nullptr;  // pinned host: predictions + loss
+  unsigned long long* hcounts_ = nullptr;  // pinned host: per-conjunct pass counts
   cudaStream_t train_stream_ = nullptr;
   cudaEvent_t train_done_ = nullptr, labels_ready_ = nullptr;
   bool params_pending_ = false;  // training finished a version not yet copied to dinfer_

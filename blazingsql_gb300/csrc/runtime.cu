@@ -510,6 +510,9 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       launch(kc, (int)grid, s, a, true);
       launch_scan_tiles(status, ntiles, hdr + 3, s);
       check_cuda(cudaMemcpyAsync(host_hdr, hdr, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+      if (extras && extras->conj_counts && extras->conj_counts_host)
+        check_cuda(cudaMemcpyAsync(extras->conj_counts_host, extras->conj_counts, 16 * 8, cudaMemcpyDeviceToHost, s),
+                   "conjunct counts readback");
       check_cuda(cudaStreamSynchronize(s), "count sync");
       capacity = (int64_t)host_hdr[3];
     }

@@ -42,6 +42,7 @@ struct ExecExtras {
   const int* order = nullptr;              // runtime conjunct order (runtime_order kernels)
   int num_order = 0;
   unsigned long long* conj_counts = nullptr;  // device counters, one per conjunct (conj_stats count pass)
+  unsigned long long* conj_counts_host = nullptr;  // optional host copy of them, made before the count sync
   int64_t capacity_hint = -1;              // library-allocated outputs: rows to allocate (-1: all input rows)
 };
 

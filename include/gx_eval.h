@@ -275,6 +275,11 @@ int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* col
  * needed).  Returns GX_OK or GX_ERR_CUDA with the compiler log in status. */
 int gx_debug_compile_check(const gx_plan* plan, int kind, const uint8_t* column_has_mask, gx_status_info* status);
 
+/* Registers per thread, spill-store bytes and static shared memory of a plan
+ * kernel as the assembler reports them for sm_103a (no GPU needed). */
+int gx_debug_kernel_resources(const gx_plan* plan, int kind, const uint8_t* column_has_mask, int32_t* registers,
+                              int32_t* spill_bytes, int32_t* shared_bytes, gx_status_info* status);
+
 /* Host-side fault injection for tests: the n-th next device allocation made by
  * this library fails with GX_ERR_OOM (n <= 0 disables). */
 void gx_debug_fail_allocation(int n);
