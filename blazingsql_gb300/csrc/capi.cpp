@@ -49,10 +49,11 @@ int env_int(const char* name, int dflt) {
 
 KernelConfig default_config() {
   KernelConfig c;
-  c.warps = env_int("GX_WARPS", 8);
+  c.warps = env_int("GX_WARPS", 4);
   c.words = env_int("GX_WORDS", 4);
   c.emulate_fp64 = env_int("GX_NATIVE_FP64", 0) == 0;
   c.dense = env_int("GX_DENSE", 1) != 0;
+  c.lazy_case = env_int("GX_LAZY_CASE", 1) != 0;
   return c;
 }
 
@@ -161,7 +162,7 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
     k += '\x1f';
   }
   k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
-       std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense);
+       std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case);
   return k;
 }
 

@@ -116,6 +116,47 @@ GXE_FN gxe_u64 gxe_round_pack(gxe_u64 sign, int e, gxe_u64 q, bool rem) {
   return sign | m;  // m == 2^52 encodes the smallest normal
 }
 
+// r ~ 2^116 / mb for a significand mb in [2^52, 2^53): an FP32 reciprocal of
+// mb's top 24 bits refined by two Newton steps in 64-bit fixed point
+// (r += r * (2^116 - mb*r) / 2^116).  Any r within a few units of the exact
+// value serves gxe_div_finish, whose remainder correction absorbs the error.
+GXE_FN gxe_u64 gxe_recip_fixed(gxe_u64 mb) {
+  const unsigned d24 = (unsigned)(mb >> 29);                      // [2^23, 2^24)
+  const float df = gxe_u2f((150u << 23) | (d24 & 0x7FFFFFu));    // == (float)d24
+  const unsigned rb = gxe_f2u(gxe_rcp_approx(df));                // ~1/d24 in (2^-24, 2^-23]
+  const int rexp = (int)((rb >> 23) & 0xFF) - 127;                // -24 or -23
+  gxe_u64 r = (gxe_u64)((rb & 0x7FFFFFu) | 0x800000u) << (40 + (rexp + 24));  // * 2^(87+rexp-23)
+  if (rexp >= -23) r = ~0ull;                                     // 1/d24 == 2^-23 -> clamp 2^64
+#if GXE_ON_DEVICE
+#pragma unroll
+#endif
+  for (int it = 0; it < 2; it++) {
+    const gxe_u64 ph = gxe_umulhi(mb, r), pl = mb * r;
+    const gxe_u64 t = (ph << 12) | (pl >> 52);   // (mb*r) >> 52, modulo 2^64
+    const gxe_i64 err = -(gxe_i64)t;             // (2^116 - mb*r) / 2^52
+    const gxe_u64 corr = gxe_umulhi(r, (gxe_u64)(err < 0 ? -err : err));
+    r = err < 0 ? r - corr : r + corr;
+  }
+  return r;
+}
+
+// Quotient of significands ma, mb in [2^52, 2^53) with r = gxe_recip_fixed(mb):
+// Q0 ~ floor(ma * 2^54 / mb) = (ma * r) >> 62, exact remainder correction, then
+// rounding of the result with exponent e (before the ma < mb adjustment).
+GXE_FN gxe_u64 gxe_div_finish(gxe_u64 sign, int e, gxe_u64 ma, gxe_u64 mb, gxe_u64 r) {
+  if (ma < mb) {
+    ma <<= 1;
+    e -= 1;
+  }
+  gxe_u64 q = (gxe_umulhi(ma, r) << 2) | ((ma * r) >> 62);
+  gxe_i64 rem = (gxe_i64)((ma << 54) - q * mb);  // exact: |rem| < 2^55
+  if (rem < 0) { q--; rem += (gxe_i64)mb; }
+  if (rem < 0) { q--; rem += (gxe_i64)mb; }
+  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
+  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
+  return gxe_round_pack(sign, e, q, rem != 0);
+}
+
 // x / y, correctly rounded (round to nearest even), as bits.
 GXE_FN gxe_u64 gxe_div(gxe_u64 a, gxe_u64 b) {
   const gxe_u64 sign = (a ^ b) & GXE_SIGN;
@@ -140,37 +181,25 @@ GXE_FN gxe_u64 gxe_div(gxe_u64 a, gxe_u64 b) {
       eb = 1 - lz;
     }
   }
-  gxe_u64 ma = fa | GXE_HIDDEN;
   const gxe_u64 mb = fb | GXE_HIDDEN;
-  int e = ea - eb;
-  if (ma < mb) {
-    ma <<= 1;
-    e -= 1;
+  return gxe_div_finish(sign, ea - eb, fa | GXE_HIDDEN, mb, gxe_recip_fixed(mb));
+}
+
+// x / y for a constant y that is normal and finite, with r =
+// gxe_recip_fixed(y's significand) computed ahead: same bits as gxe_div(x, y).
+GXE_FN gxe_u64 gxe_div_r(gxe_u64 a, gxe_u64 b, gxe_u64 r) {
+  const gxe_u64 sign = (a ^ b) & GXE_SIGN;
+  int ea = (int)((a >> 52) & 0x7FF);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  gxe_u64 fa = a & GXE_FRAC;
+  if ((unsigned)(ea - 1) >= 2046u) {
+    if (ea == 0x7FF) return fa != 0 ? (GXE_QNAN | fa | (a & GXE_SIGN)) : (sign | GXE_INF);
+    if (fa == 0) return sign;
+    const int lz = gxe_clz(fa) - 11;
+    fa <<= lz;
+    ea = 1 - lz;
   }
-  // r ~ 2^116 / mb, seeded from an FP32 reciprocal of mb's top 24 bits
-  const unsigned d24 = (unsigned)(mb >> 29);                      // [2^23, 2^24)
-  const float df = gxe_u2f((150u << 23) | (d24 & 0x7FFFFFu));    // == (float)d24
-  const unsigned rb = gxe_f2u(gxe_rcp_approx(df));                // ~1/d24 in (2^-24, 2^-23]
-  const int rexp = (int)((rb >> 23) & 0xFF) - 127;                // -24 or -23
-  gxe_u64 r = (gxe_u64)((rb & 0x7FFFFFu) | 0x800000u) << (40 + (rexp + 24));  // * 2^(87+rexp-23)
-  if (rexp >= -23) r = ~0ull;                                     // 1/d24 == 2^-23 -> clamp 2^64
-  // two Newton steps in 64-bit fixed point: r += r * (2^116 - mb*r) / 2^116
-#pragma unroll
-  for (int it = 0; it < 2; it++) {
-    const gxe_u64 ph = gxe_umulhi(mb, r), pl = mb * r;
-    const gxe_u64 t = (ph << 12) | (pl >> 52);   // (mb*r) >> 52, modulo 2^64
-    const gxe_i64 err = -(gxe_i64)t;             // (2^116 - mb*r) / 2^52
-    const gxe_u64 corr = gxe_umulhi(r, (gxe_u64)(err < 0 ? -err : err));
-    r = err < 0 ? r - corr : r + corr;
-  }
-  // Q0 ~ floor(ma * 2^54 / mb) = (ma * r) >> 62, then exact correction
-  gxe_u64 q = (gxe_umulhi(ma, r) << 2) | ((ma * r) >> 62);
-  gxe_i64 rem = (gxe_i64)((ma << 54) - q * mb);  // exact: |rem| < 2^55
-  if (rem < 0) { q--; rem += (gxe_i64)mb; }
-  if (rem < 0) { q--; rem += (gxe_i64)mb; }
-  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
-  if (rem >= (gxe_i64)mb) { q++; rem -= (gxe_i64)mb; }
-  return gxe_round_pack(sign, e, q, rem != 0);
+  return gxe_div_finish(sign, ea - eb, fa | GXE_HIDDEN, (b & GXE_FRAC) | GXE_HIDDEN, r);
 }
 
 // x + y, correctly rounded, as bits (guard / round / sticky alignment).

@@ -1,6 +1,8 @@
 // plan.cpp -- expression DAG + CUDA code generation (see plan.h).
 #include "plan.h"
 
+#include "fp64emu.cuh"
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -269,6 +271,20 @@ class Gen {
   }
   bool emu() const { return cfg_.emulate_fp64; }
 
+  // a valid literal's value as binary64 bits (integer literals converted exactly
+  // as the kernels convert them)
+  uint64_t literal_double_bits(int id) const {
+    const Node& n = p_.nodes[id];
+    return kind_f(id) ? n.lit_bits : gxe_i2d((gxe_i64)n.lit_bits);
+  }
+  // a literal divisor that is a normal finite nonzero double
+  bool const_divisor(int id) const {
+    const Node& n = p_.nodes[id];
+    if (n.kind != Node::LIT || !n.lit_valid) return false;
+    const int e = (int)((literal_double_bits(id) >> 52) & 0x7FF);
+    return e >= 1 && e <= 2046;
+  }
+
   // statements computing node id for slot k; row / out-row expressions given
   void emit_node(std::ostringstream& o, int id, const std::string& ind) const {
     const Node& n = p_.nodes[id];
@@ -437,8 +453,15 @@ class Gen {
             : emu() ? "gxe_mul(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " * " + asD(y) + ")";
         break;
       case OP_DIV:
-        r = !anyf ? "gx_div_ii(" + X + ", " + Y + ")"
-            : emu() ? "gxe_div(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " / " + asD(y) + ")";
+        if (anyf && emu() && const_divisor(y)) {
+          // constant divisor: its fixed-point reciprocal is computed here
+          const uint64_t db = literal_double_bits(y);
+          r = "gxe_div_r(" + asDB(x) + ", " + hex64(db) + ", " +
+              hex64(gxe_recip_fixed((db & GXE_FRAC) | GXE_HIDDEN)) + ")";
+        } else {
+          r = !anyf ? "gx_div_ii(" + X + ", " + Y + ")"
+              : emu() ? "gxe_div(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " / " + asD(y) + ")";
+        }
         vv = "(" + vv + " && " + (rf ? nz(y) : "(i64)(" + Y + ") != 0LL") + ")";
         break;
       case OP_MOD:
@@ -607,6 +630,102 @@ class Gen {
 
   std::vector<int> predicate_cone() const { return p_.has_filter() ? cone(p_.conjuncts) : std::vector<int>{}; }
 
+  // ids of OP / COL nodes reachable from roots without descending below the
+  // nodes in `stop` (which are included themselves), ascending
+  std::vector<int> cone_stop(const std::vector<int>& roots, const std::set<int>& stop) const {
+    std::set<int> seen;
+    std::function<void(int)> go = [&](int id) {
+      if (id < 0 || seen.count(id)) return;
+      seen.insert(id);
+      const Node& n = p_.nodes[id];
+      if (n.kind == Node::OP && !stop.count(id)) { go(n.a); go(n.b); }
+    };
+    for (int r : roots) go(r);
+    std::vector<int> v;
+    for (int id : seen)
+      if (p_.nodes[id].kind != Node::LIT) v.push_back(id);
+    return v;
+  }
+
+  // A CASE branch (the value operand of a MAGIC_IF_NOT) whose subtree is used
+  // by nothing else, reads only columns and literals, and is expensive
+  // (transcendentals, divisions): the dense phase evaluates it only for the
+  // kept rows whose condition selects it, packed into full warps.  Rows whose
+  // condition is false take the magic value whatever the branch computes, so
+  // skipping them changes no result.
+  struct Lazy {
+    int consumer = -1;  // the MAGIC_IF_NOT node
+    int cond = -1;      // its condition operand
+    int root = -1;      // the branch value operand
+    std::vector<int> nodes;  // OP and COL nodes of the branch, ascending
+  };
+
+  static int op_cost(Op op) {
+    switch (op) {
+      case OP_LN: case OP_LOG10: case OP_EXP: case OP_POW: case OP_SIN: case OP_COS: case OP_TAN: case OP_ASIN:
+      case OP_ACOS: case OP_ATAN: case OP_COTAN:
+        return 64;
+      case OP_DIV: case OP_MOD: case OP_ROUND:
+        return 16;
+      default:
+        return 1;
+    }
+  }
+
+  std::vector<Lazy> lazy_branches(const std::vector<int>& roots) const {
+    std::vector<Lazy> out;
+    if (!cfg_.lazy_case) return out;
+    const std::vector<int> all = cone(roots);
+    std::map<int, std::vector<int>> users;
+    for (int id : all) {
+      const Node& n = p_.nodes[id];
+      if (n.kind != Node::OP) continue;
+      if (n.a >= 0) users[n.a].push_back(id);
+      if (n.b >= 0 && n.b != n.a) users[n.b].push_back(id);
+    }
+    const std::set<int> external(roots.begin(), roots.end());
+    std::set<int> taken;
+    // outermost consumers first (a parent's id is above its operands')
+    for (auto it = all.rbegin(); it != all.rend(); ++it) {
+      const int m = *it;
+      const Node& mn = p_.nodes[m];
+      if (mn.kind != Node::OP || mn.op != OP_MAGIC_IF_NOT || taken.count(m)) continue;
+      const int y = mn.b;
+      if (y < 0 || p_.nodes[y].kind != Node::OP || external.count(y) || taken.count(y)) continue;
+      if (users[y].size() != 1 || users[y][0] != m) continue;
+      const std::vector<int> ycone = cone({y});
+      std::set<int> S{y};
+      for (bool grown = true; grown;) {
+        grown = false;
+        for (int id : ycone) {
+          if (S.count(id) || p_.nodes[id].kind != Node::OP || external.count(id)) continue;
+          bool excl = true;
+          for (int u : users[id])
+            if (!S.count(u)) { excl = false; break; }
+          if (excl) { S.insert(id); grown = true; }
+        }
+      }
+      bool ok = true;
+      int cost = 0;
+      for (int id : ycone) {
+        const Node& n = p_.nodes[id];
+        if (n.kind != Node::OP) continue;
+        if (!S.count(id) || taken.count(id)) { ok = false; break; }
+        cost += op_cost(n.op);
+      }
+      if (!ok || cost < 32) continue;
+      Lazy lz;
+      lz.consumer = m;
+      lz.cond = mn.a;
+      lz.root = y;
+      lz.nodes = ycone;
+      for (int id : ycone)
+        if (p_.nodes[id].kind == Node::OP) taken.insert(id);
+      out.push_back(lz);
+    }
+    return out;
+  }
+
   std::vector<int> output_roots() const {
     std::vector<int> r;
     for (const auto& o : p_.outputs)
@@ -664,11 +783,100 @@ std::vector<size_t> masked_outputs(const Plan& p) {
 // projections are computed only for surviving rows and every output store and
 // validity word of a round is contiguous.  Operands are re-read with the
 // gathered row index (predicate columns hit L1/L2).
+// statements mapping kept rank t_ of the warp (0 <= t_ < total_) to its row
+void emit_rank_to_row(std::ostringstream& o, const std::string& ind) {
+  o << ind << "u32 bks_ = 0u, cks_ = 0u; int sk_ = 0;\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++)\n";
+  o << ind << "  if (t_ >= cum_[kk] && t_ < cum_[kk + 1]) { sk_ = kk; bks_ = bal[kk]; cks_ = cum_[kk]; }\n";
+  o << ind << "const int src_ = act ? (int)__fns(bks_, 0u, (int)(t_ - cks_) + 1) : 0;\n";
+  o << ind << "const i64 row = (w0 + sk_) * 32 + src_; const bool inr = act; (void)inr;\n";
+  o << ind << "const i64 orow = (i64)pos + (i64)t_; (void)orow;\n";
+  o << ind << "const int k = 0;\n";
+}
+
+// nodes ids for one row per lane: gathers first, then operators; lazy branch
+// roots (lz_root -> index) are read from the branch results in shared memory
+void emit_row_nodes(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& ids,
+                    const std::map<int, int>& lz_root, const std::string& ind) {
+  g.decl(o, ids, ind);
+  for (int id : ids)
+    if (p.nodes[id].kind == Node::COL) g.emit_node(o, id, ind);
+  for (int id : ids) {
+    if (p.nodes[id].kind == Node::COL) continue;
+    auto it = lz_root.find(id);
+    if (it != lz_root.end()) {
+      o << ind << "b" << id << "[k] = s_lzb_[" << it->second << "][warp][t_]; v" << id << "[k] = s_lzv_["
+        << it->second << "][warp][t_] != 0;\n";
+    } else {
+      g.emit_node(o, id, ind);
+    }
+  }
+}
+
+// Dense phase 2: the warp's kept rows, in row order, are dealt to lanes in
+// rounds of 32 (lane l of round r takes the warp's (32r + l)-th kept row), so
+// projections are computed only for surviving rows and every output store and
+// validity word of a round is contiguous.  Operands are re-read with the
+// gathered row index (predicate columns hit L1/L2).  Expensive CASE branches
+// (Gen::lazy_branches) are first evaluated for the kept rows whose condition
+// selects them, packed into full warps, into shared memory.
 void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p, const std::string& ind) {
-  std::vector<int> proj = g.cone(g.output_roots());
+  const std::vector<int> roots = g.output_roots();
+  const std::vector<Gen::Lazy> lz = g.lazy_branches(roots);
+  std::map<int, int> lz_root;
+  std::set<int> stop;
+  for (size_t i = 0; i < lz.size(); i++) {
+    lz_root[lz[i].root] = (int)i;
+    stop.insert(lz[i].root);
+  }
+  const std::vector<int> proj = g.cone_stop(roots, stop);
   o << ind << "u32 cum_[GX_V + 1]; cum_[0] = 0u;\n";
   o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++) cum_[kk + 1] = cum_[kk] + __popc(bal[kk]);\n";
   o << ind << "const u32 total_ = cum_[GX_V];\n";
+  if (!lz.empty()) {
+    const int nl = (int)lz.size();
+    o << ind << "__shared__ u64 s_lzb_[" << nl << "][GX_WARPS][GX_V * 32];\n";
+    o << ind << "__shared__ unsigned char s_lzv_[" << nl << "][GX_WARPS][GX_V * 32];\n";
+    // pass 1: which kept rows select each branch
+    std::vector<int> conds;
+    for (const auto& l : lz) conds.push_back(l.cond);
+    const std::vector<int> cond_ids = g.cone(conds);
+    o << ind << "u32 dmd_[" << nl << "][GX_V];\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int r_ = 0; r_ < GX_V; r_++) {\n";
+    const std::string i2 = ind + "  ";
+    o << i2 << "#pragma unroll\n" << i2 << "for (int l_ = 0; l_ < " << nl << "; l_++) dmd_[l_][r_] = 0u;\n";
+    o << i2 << "if ((u32)r_ * 32u < total_) {\n";
+    const std::string i3 = i2 + "  ";
+    o << i3 << "const u32 t_ = (u32)r_ * 32u + (u32)lane; const bool act = t_ < total_;\n";
+    emit_rank_to_row(o, i3);
+    emit_row_nodes(o, g, p, cond_ids, {}, i3);
+    for (int i = 0; i < nl; i++) {
+      const int c = lz[i].cond;
+      o << i3 << "dmd_[" << i << "][r_] = __ballot_sync(GX_FULL, act && (" << g.V(c) << " && " << g.nz(c) << "));\n";
+    }
+    o << i2 << "}\n";
+    o << ind << "}\n";
+    // pass 2: each branch over its selecting rows, 32 at a time
+    for (int i = 0; i < nl; i++) {
+      o << ind << "{\n";
+      o << i2 << "u32 dc_[GX_V + 1]; dc_[0] = 0u;\n";
+      o << i2 << "#pragma unroll\n" << i2 << "for (int r_ = 0; r_ < GX_V; r_++) dc_[r_ + 1] = dc_[r_] + __popc(dmd_[" << i
+        << "][r_]);\n";
+      o << i2 << "for (u32 db_ = 0; db_ < dc_[GX_V]; db_ += 32u) {\n";
+      o << i3 << "const u32 q_ = db_ + (u32)lane; const bool act = q_ < dc_[GX_V];\n";
+      o << i3 << "u32 dbits_ = 0u, dcs_ = 0u; int dr_ = 0;\n";
+      o << i3 << "#pragma unroll\n" << i3 << "for (int r_ = 0; r_ < GX_V; r_++)\n";
+      o << i3 << "  if (q_ >= dc_[r_] && q_ < dc_[r_ + 1]) { dr_ = r_; dbits_ = dmd_[" << i << "][r_]; dcs_ = dc_[r_]; }\n";
+      o << i3 << "const u32 t_ = (u32)dr_ * 32u + (act ? (u32)__fns(dbits_, 0u, (int)(q_ - dcs_) + 1) : 0u);\n";
+      emit_rank_to_row(o, i3);
+      emit_row_nodes(o, g, p, lz[i].nodes, {}, i3);
+      o << i3 << "if (act) { s_lzb_[" << i << "][warp][t_] = " << g.B(lz[i].root) << "; s_lzv_[" << i
+        << "][warp][t_] = " << g.V(lz[i].root) << " ? 1 : 0; }\n";
+      o << i2 << "}\n";
+      o << ind << "}\n";
+    }
+    o << ind << "__syncwarp();\n";
+  }
   // validity bit streams: one position shared by all outputs (every round
   // appends the same number of bits to each), one accumulator per output; the
   // first word may be shared with the previous warp's range and the last with
@@ -680,19 +888,8 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   o << ind << "for (u32 base_ = 0; base_ < total_; base_ += 32u) {\n";
   const std::string in2 = ind + "  ";
   o << in2 << "const u32 t_ = base_ + (u32)lane; const bool act = t_ < total_;\n";
-  o << in2 << "u32 bks_ = 0u, cks_ = 0u; int sk_ = 0;\n";
-  o << in2 << "#pragma unroll\n" << in2 << "for (int kk = 0; kk < GX_V; kk++)\n";
-  o << in2 << "  if (t_ >= cum_[kk] && t_ < cum_[kk + 1]) { sk_ = kk; bks_ = bal[kk]; cks_ = cum_[kk]; }\n";
-  o << in2 << "const int src_ = act ? (int)__fns(bks_, 0u, (int)(t_ - cks_) + 1) : 0;\n";
-  o << in2 << "const i64 row = (w0 + sk_) * 32 + src_; const bool inr = act; (void)inr;\n";
-  o << in2 << "const i64 orow = (i64)pos + (i64)t_; (void)orow;\n";
-  o << in2 << "const int k = 0;\n";
-  g.decl(o, proj, in2);
-  // gathers first, then the operators
-  for (int id : proj)
-    if (p.nodes[id].kind == Node::COL) g.emit_node(o, id, in2);
-  for (int id : proj)
-    if (p.nodes[id].kind != Node::COL) g.emit_node(o, id, in2);
+  emit_rank_to_row(o, in2);
+  emit_row_nodes(o, g, p, proj, lz_root, in2);
   o << in2 << "const bool wr = act && orow < a.capacity;\n";
   o << in2 << "const int nb = (int)min(32u, total_ - base_);\n";
   for (size_t j = 0; j < p.outputs.size(); j++) emit_dense_store(o, g, p, j, in2);
@@ -708,6 +905,7 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   o << in2 << "  bfirst_ = false; bword_++; bf_ = nf_ - 32;\n";
   o << in2 << "} else {\n" << in2 << "  bf_ = nf_;\n" << in2 << "}\n";
   o << ind << "}\n";
+  if (!lz.empty()) o << ind << "__syncwarp();\n";  // shared branch results are reused by the next tile
   o << ind << "if (bf_ > 0 && lane == 0 && bword_ < cap_words) {\n";
   for (size_t j : mo) o << ind << "  atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]);\n";
   o << ind << "}\n";

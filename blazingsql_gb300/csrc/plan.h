@@ -50,6 +50,7 @@ struct KernelConfig {
   int words = 2;           // 32-row words per warp per step
   bool emulate_fp64 = true;  // binary64 compares / divides / conversions on the integer pipes
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
+  bool lazy_case = true;     // dense phase: expensive CASE branches only for the rows that select them
   bool runtime_order = false;  // short-circuit AND conjuncts in the order given at launch (KernelArgs::order)
   bool conj_stats = false;     // COUNT_FILTER also counts each conjunct's passing rows
   bool short_circuit = false;

@@ -59,6 +59,16 @@ int main(int argc, char** argv) {
       if (bad++ < 10) printf("div %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q,
                              (unsigned long long)bits(a / b));
     }
+    // constant-divisor form: reciprocal computed ahead for a normal finite divisor
+    const int eb = (int)((bits(b) >> 52) & 0x7FF);
+    if (eb >= 1 && eb <= 2046) {
+      const uint64_t r = gxe_recip_fixed((bits(b) & GXE_FRAC) | GXE_HIDDEN);
+      const uint64_t q2 = gxe_div_r(bits(a), bits(b), r);
+      if (!same(q2, a / b)) {
+        if (bad++ < 10) printf("div_r %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q2,
+                               (unsigned long long)bits(a / b));
+      }
+    }
     if (!same(gxe_add(bits(a), bits(b)), a + b) || !same(gxe_sub(bits(a), bits(b)), a - b)) {
       if (bad++ < 10) printf("add/sub %.17g %.17g\n", a, b);
     }
