@@ -182,6 +182,78 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
+    """C3: the deep plan over execution-graph batches of log-uniform size in
+    [1K, 4M] rows, (a) one gx_plan_execute call per batch, as the batched
+    execution graph calls the filter, and (b) the batch runner: one persistent
+    kernel in a captured CUDA graph with an autotuned block shape.  Both read
+    the same resident batches; outputs are library-allocated and freed."""
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import workloads as W
+    sizes = W.c3_batch_sizes(seed, nbatches)
+    total = sum(sizes)
+    w = W.workload("c2", total)
+    stream = torch.cuda.current_stream()
+    cols = W.device_columns("c2", total, seed=seed)
+    batches = W.slice_batches(cols, sizes)
+    plan = g.Plan(w.schema, w.condition, w.projections)
+    torch.cuda.synchronize()
+
+    def per_batch():
+        rows = []
+        for b in batches:
+            out, r = plan.execute(b, stream=stream)
+            rows.append(r)
+            g.api.free_columns(out, stream)
+        return rows
+
+    per_batch()  # compile + warm
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    rows_a = per_batch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_a = e0.elapsed_time(e1)
+    # per-size-bucket rate of the per-batch path
+    buckets = {"1K-16K": [0, 0.0], "16K-256K": [0, 0.0], "256K-4M": [0, 0.0]}
+    import time
+    for b, n in zip(batches, sizes):
+        key = "1K-16K" if n < 16384 else ("16K-256K" if n < 262144 else "256K-4M")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out, _ = plan.execute(b, stream=stream)
+        g.api.free_columns(out, stream)
+        torch.cuda.synchronize()
+        buckets[key][0] += n
+        buckets[key][1] += time.perf_counter() - t0
+    runner = g.BatchRunner(plan, nbatches, total, autotune=True)
+    out, rows_b = runner.run(batches, stream=stream)  # tunes on this first run
+    for o in out:
+        g.api.free_columns(o, stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        out, rows_b = runner.run(batches, stream=stream)
+        for o in out:
+            g.api.free_columns(o, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1) / reps
+    bt, words = runner.config()
+    del batches, cols
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"c3_batched_deep_plan: {nbatches} batches, log-uniform 1K-4M rows, {total} rows in all",
+        "runner_rows_per_s": total / (ms_b / 1e3), "per_batch_calls_rows_per_s": total / (ms_a / 1e3),
+        "runner_vs_per_batch_calls": ms_a / ms_b, "runner_ms": ms_b, "per_batch_calls_ms": ms_a,
+        "identical_row_counts": rows_a == rows_b,
+        "autotuned": {"block_threads": bt, "words_per_warp": words, "vector_width": 1},
+        "per_batch_calls_bucket_rows_per_s": {k: (v[0] / v[1] if v[1] > 0 else None) for k, v in buckets.items()},
+    }
+
+
 def learned_compare(batches: int, rows: int, seed: int = 4):
     """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
     through gx_learner under three policies on the same resident batches:
@@ -277,6 +349,7 @@ def main():
     ap.add_argument("--mode", type=int, default=-1, help="filter mode override (0 auto, 1 two-pass, 2 single)")
     ap.add_argument("--learned-batches", type=int, default=64, help="C4 batches (0 skips the learned comparison)")
     ap.add_argument("--learned-rows", type=int, default=1 << 22, help="C4 rows per batch")
+    ap.add_argument("--batched-batches", type=int, default=512, help="C3 batches (0 skips the batched comparison)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -410,10 +483,19 @@ def main():
             dist.destroy_process_group()
         return
 
+    batched = None
+    if args.batched_batches > 0:
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
+        batched = batched_compare(args.batched_batches)
     learned = None
     if args.learned_batches > 0:
-        del cols
-        torch.cuda.empty_cache()
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
         learned = learned_compare(args.learned_batches, args.learned_rows)
 
     # ---- CPU baseline: oracle on a bounded sample --------------------------
@@ -438,6 +520,7 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "batched": batched,
         "learned": learned,
     }
     print(json.dumps(line), flush=True)

@@ -6,6 +6,6 @@ The product is the native library ``_lib/libgxeval.so`` (C ABI in
 from .types import HostColumn, TypeId, pack_validity, unpack_validity  # noqa: F401
 from ._native import (GxError, GX_LEARN_POLICY_LEARNED, GX_LEARN_POLICY_PLAIN,  # noqa: F401
                       GX_LEARN_POLICY_TEXTUAL)
-from .api import (DeviceColumn, Learner, NativeColumn, Plan, evaluate_expressions, filter_project,  # noqa: F401
+from .api import (BatchRunner, DeviceColumn, Learner, NativeColumn, Plan, evaluate_expressions, filter_project,  # noqa: F401
                   process_filter, process_project, version)
 from . import api  # noqa: F401

@@ -122,6 +122,13 @@ def lib():
     L.gx_debug_kernel_source.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), C.c_char_p, C.c_int64, P(StatusInfo)]
     L.gx_debug_kernel_source.restype = C.c_int64
     L.gx_debug_compile_check.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(StatusInfo)]
+    L.gx_batch_runner_create.argtypes = [C.c_void_p, C.c_int, C.c_int64, C.c_int, P(StatusInfo)]
+    L.gx_batch_runner_create.restype = C.c_void_p
+    L.gx_batch_runner_run.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_int, P(Column), P(C.c_int64),
+                                      C.c_void_p, P(StatusInfo)]
+    L.gx_batch_runner_config.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32)]
+    L.gx_batch_runner_destroy.argtypes = [C.c_void_p]
+    L.gx_batch_runner_destroy.restype = None
     L.gx_debug_kernel_resources.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(C.c_int32), P(C.c_int32),
                                             P(C.c_int32), P(StatusInfo)]
     L.gx_debug_fail_allocation.argtypes = [C.c_int]
@@ -168,6 +175,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_save", "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
+    "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",
 ]
 
 

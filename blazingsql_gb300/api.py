@@ -307,6 +307,61 @@ class Plan:
             pass
 
 
+class BatchRunner:
+    """A table of batches of one filter plan through one persistent kernel in a
+    captured CUDA graph (gx_batch_runner_*)."""
+
+    def __init__(self, plan: Plan, max_batches: int, max_total_rows: int, autotune: bool = True):
+        st = N.StatusInfo()
+        h = N.lib().gx_batch_runner_create(plan._h, max_batches, max_total_rows, 1 if autotune else 0, C.byref(st))
+        if not h:
+            raise N.GxError(st.code, st.message.decode(errors="replace"))
+        self._h = h
+        self.num_outputs = plan.num_outputs
+        self._ncols = len(plan.schema)
+
+    def run(self, batches: Sequence[Table], out: Optional[Sequence[N.Column]] = None, stream=None):
+        """Runs every batch; returns (columns per batch, rows per batch)."""
+        keep: list = []
+        nb = len(batches)
+        views = (N.ColumnView * max(1, nb * self._ncols))()
+        for b, table in enumerate(batches):
+            arr, nc = _views(table, keep)
+            if nc != self._ncols:
+                raise ValueError("batch column count does not match the plan")
+            for i in range(nc):
+                views[b * nc + i] = arr[i]
+        n = self.num_outputs
+        outs = (N.Column * max(1, nb * n))()
+        if out is not None:
+            for i, c in enumerate(out):
+                outs[i] = c
+        rows = (C.c_int64 * max(1, nb))()
+        s = _stream_handle(stream)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_batch_runner_run(self._h, views, nb, self._ncols, outs, rows, s, C.byref(st)), st)
+        if out is not None:
+            cols = [[outs[b * n + j] for j in range(n)] for b in range(nb)]
+        else:
+            cols = [[NativeColumn(N.Column(outs[b * n + j].type_id, 0, outs[b * n + j].data, outs[b * n + j].null_mask,
+                                           outs[b * n + j].size, outs[b * n + j].capacity), s) for j in range(n)]
+                    for b in range(nb)]
+        return cols, [rows[b] for b in range(nb)]
+
+    def config(self):
+        bt, w = C.c_int32(0), C.c_int32(0)
+        N.lib().gx_batch_runner_config(self._h, C.byref(bt), C.byref(w))
+        return bt.value, w.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.lib().gx_batch_runner_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class Learner:
     """Learned conjunct ordering over a stream of batches (gx_learner_*).
 

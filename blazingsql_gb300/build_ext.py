@@ -18,7 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgxeval.so")
 
-SOURCES = ["frontend.cpp", "plan.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "runtime.cu", "noalloc.cu", "learned.cu"]
+SOURCES = ["frontend.cpp", "plan.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "runtime.cu", "noalloc.cu", "learned.cu",
+           "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -398,7 +398,8 @@ static KernelKind kind_of(int k) {
     case 1: case 4: return KernelKind::FUSED_FILTER;
     case 2: case 5: return KernelKind::COUNT_FILTER;
     case 3: return KernelKind::WRITE_FILTER;
-    default: fail(GX_ERR_INVALID, "kernel kind must be 0..5");
+    case 6: return KernelKind::FUSED_BATCHED;
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..6");
   }
 }
 

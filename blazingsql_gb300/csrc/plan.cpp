@@ -1033,12 +1033,105 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "}\n";
 }
 
+// Batched persistent form of the pipelined fused filter: one launch runs a
+// whole table of batches (GxArgs per batch).  Batch b owns the tiles
+// [tile_base[b], tile_base[b + 1]) of one tile sequence that blocks claim in
+// order from one counter; every batch has its own look-back segment and row
+// counter, so a block's pending and next tiles may belong to different
+// batches, and each batch's result is exactly that of running it alone.
+void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
+                        const std::string& name) {
+  o << "struct GxBatchHdr { unsigned long long tile_counter; long long total_tiles; int nbatch; int pad; };\n";
+  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name
+    << "(const GxArgs* __restrict__ A, const long long* __restrict__ tile_base, GxBatchHdr* hdr) {\n";
+  o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
+  o << "  const i64 total_tiles = hdr->total_tiles; const int nbatch = hdr->nbatch;\n";
+  o << "  __shared__ unsigned long long s_claim;\n";
+  o << "  __shared__ u32 s_cnt[2][GX_WARPS];\n";
+  o << "  __shared__ u64 s_off[2][GX_WARPS];\n";
+  o << "  __shared__ u64 s_base;\n";
+  o << "  if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
+  o << "  __syncthreads();\n";
+  o << "  const i64 gt0 = (i64)s_claim;\n";
+  o << "  if (gt0 >= total_tiles) return;\n";
+  o << "  int pb = 0;\n";
+  o << "  while (pb + 1 < nbatch && tile_base[pb + 1] <= gt0) pb++;\n";
+  o << "  i64 tile = gt0 - tile_base[pb];\n";
+  o << "  u32 bal[GX_V]; u32 wcnt = 0u; int par = 0; u64 ptotal = 0ull;\n";
+  o << "  {\n";
+  o << "    const GxArgs& a = A[pb];\n";
+  o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  g.decl(o, pred_ids, "    ");
+  g.emit_predicate(o, "    ");
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) { bal[k] = __ballot_sync(GX_FULL, alive[k]); wcnt += __popc(bal[k]); }\n";
+  o << "    if (lane == 0) s_cnt[0][warp] = wcnt;\n";
+  o << "  }\n";
+  o << "  __syncthreads();\n";
+  o << "  if (warp == 0) ptotal = gx_tile_publish(A[pb].tile_status, tile, s_cnt[0], s_off[0], GX_WARPS);\n";
+  o << "  while (true) {\n";
+  o << "    if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
+  o << "    __syncthreads();\n";
+  o << "    const i64 ngt = (i64)s_claim;\n";
+  o << "    int nb = pb; i64 next = -1;\n";
+  o << "    if (ngt < total_tiles) {\n";
+  o << "      while (nb + 1 < nbatch && tile_base[nb + 1] <= ngt) nb++;\n";
+  o << "      next = ngt - tile_base[nb];\n";
+  o << "    }\n";
+  o << "    const int npar = par ^ 1;\n";
+  o << "    u32 nbal[GX_V]; u32 nwcnt = 0u;\n";
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) nbal[k] = 0u;\n";
+  o << "    if (next >= 0) {\n";
+  o << "      const GxArgs& a = A[nb];\n";
+  o << "      const i64 w0 = next * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  g.decl(o, pred_ids, "      ");
+  g.emit_predicate(o, "      ");
+  o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) { nbal[k] = __ballot_sync(GX_FULL, alive[k]); nwcnt += __popc(nbal[k]); }\n";
+  o << "      if (lane == 0) s_cnt[npar][warp] = nwcnt;\n";
+  o << "    }\n";
+  o << "    __syncthreads();\n";
+  o << "    if (warp == 0) {\n";
+  o << "      u64 ntotal = 0ull;\n";
+  o << "      if (next >= 0) ntotal = gx_tile_publish(A[nb].tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
+  o << "      const GxArgs& a = A[pb];\n";
+  o << "      const i64 ntiles = (((a.n + 31) >> 5) + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
+  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, 1u << 22);\n";
+  o << "      if (lane == 0) {\n";
+  o << "        s_base = excl;\n";
+  o << "        if (tile == ntiles - 1 && excl != ~0ull) *a.out_count = excl + ptotal;\n";
+  o << "      }\n";
+  o << "      ptotal = ntotal;\n";
+  o << "    }\n";
+  o << "    __syncthreads();\n";
+  o << "    const u64 base_t = s_base;\n";
+  o << "    if (base_t == ~0ull) break;\n";  // look-back gave up: error already recorded
+  o << "    if (wcnt != 0u) {\n";
+  o << "      const GxArgs& a = A[pb];\n";
+  o << "      u64 pos = base_t + s_off[par][warp];\n";
+  o << "      const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  emit_filter_writes_dense(o, g, p, "      ");
+  o << "    }\n";
+  o << "    if (next < 0) break;\n";
+  o << "    tile = next; pb = nb; par = npar; wcnt = nwcnt;\n";
+  o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) bal[k] = nbal[k];\n";
+  o << "  }\n";
+  o << "}\n";
+}
+
 }  // namespace
 
 std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg, const std::string& name) {
   Gen g(p, cfg);
   std::ostringstream o;
   emit_prelude(o, cfg);
+  if (kind == KernelKind::FUSED_BATCHED) {
+    if (!p.has_filter()) fail(GX_ERR_INVALID, "the batched kernel runs filter plans");
+    if (cfg.runtime_order || cfg.short_circuit) fail(GX_ERR_INVALID, "the batched kernel evaluates conjuncts in plan order");
+    KernelConfig c = cfg;
+    c.dense = true;
+    Gen gb(p, c);
+    emit_fused_batched(o, gb, p, gb.predicate_cone(), name);
+    return o.str();
+  }
   o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name << "(const GxArgs a) {\n";
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
   o << "  const i64 nwords = (a.n + 31) >> 5;\n";

@@ -85,7 +85,15 @@ Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullabl
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
 constexpr int GX_OUTPUTS_PER_KERNEL = 32;
 
-enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER };
+enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED };
+
+// Header of a batch table run by the FUSED_BATCHED kernel (device memory).
+struct BatchHeader {
+  unsigned long long tile_counter;  // next tile to claim, over all batches
+  long long total_tiles;
+  int nbatch;
+  int pad;
+};
 
 // CUDA source of one plan kernel.  The kernel is named by `name`.
 std::string generate_kernel(const Plan& plan, KernelKind kind, const KernelConfig& cfg, const std::string& name);

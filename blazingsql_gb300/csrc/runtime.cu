@@ -42,6 +42,7 @@ void ensure_pool() {
 void debug_fail_allocation(int n) { g_fail_countdown.store(n); }
 
 void set_kernel_timing(bool on) { g_timing.store(on); }
+bool kernel_timing_enabled() { return g_timing.load(); }
 double kernel_ms(bool reset) {
   const double v = t_kernel_ms;
   if (reset) t_kernel_ms = 0.0;
@@ -155,6 +156,44 @@ void* alloc_outputs(const std::vector<int>& types, int64_t capacity, size_t scra
   }
   return sb ? base : nullptr;
 }
+
+void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>& caps, bool zero_masks,
+                      gx_column* out, cudaStream_t s) {
+  const size_t nout = types.size();
+  if (nout == 0) return;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t mtotal = 0;
+  std::vector<size_t> moff(nout), doff(nout);
+  for (size_t j = 0; j < nout; j++) {
+    moff[j] = mtotal;
+    mtotal += al((size_t)mask_words_padded(caps[j]) * 4);
+  }
+  size_t total = mtotal;
+  for (size_t j = 0; j < nout; j++) {
+    doff[j] = total;
+    total += al(std::max<size_t>(64, (size_t)caps[j] * type_size(types[j])));
+  }
+  char* base = (char*)dev_alloc(total, s);
+  if (zero_masks) {
+    const cudaError_t e = cudaMemsetAsync(base, 0, mtotal, s);
+    if (e != cudaSuccess) {
+      dev_free(base, s);
+      check_cuda(e, "output set memset");
+    }
+  }
+  auto* ar = new OutputArena{base, (int)nout};
+  std::lock_guard<std::mutex> g(g_arena_mu);
+  for (size_t j = 0; j < nout; j++) {
+    out[j] = gx_column{};
+    out[j].type_id = types[j];
+    out[j].data = base + doff[j];
+    out[j].null_mask = (uint32_t*)(base + moff[j]);
+    out[j].capacity = caps[j];
+    g_arena_of[out[j].data] = ar;
+  }
+}
+
+int64_t mask_words_for(int64_t rows) { return mask_words_padded(rows); }
 
 void free_column(gx_column& c, cudaStream_t s) {
   bool in_arena = false;
@@ -305,6 +344,7 @@ static const char* kind_name(KernelKind k) {
     case KernelKind::PROJECT: return "gx_project";
     case KernelKind::FUSED_FILTER: return "gx_filter_fused";
     case KernelKind::COUNT_FILTER: return "gx_filter_count";
+    case KernelKind::FUSED_BATCHED: return "gx_filter_batched";
     default: return "gx_filter_write";
   }
 }
@@ -332,8 +372,7 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
 // Launches a plan kernel; with timing on, brackets it with events on `s`
 // (timed=true for the call's main kernel) and adds its duration to the
 // calling thread's total.
-static void launch(const JitKernel& k, int grid, cudaStream_t s, KernelArgs& args, bool timed = false) {
-  void* params[] = {&args};
+void launch_raw(const JitKernel& k, int grid, cudaStream_t s, void** params, bool timed) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const bool tm = timed && g_timing.load();
   if (tm) {
@@ -361,6 +400,11 @@ static std::vector<bool> runtime_nullable(const Plan& p, const std::vector<Colum
   for (size_t i = 0; i < cols.size(); i++) nb[i] = cols[i].mask != nullptr;
   (void)p;
   return nb;
+}
+
+static void launch(const JitKernel& k, int grid, cudaStream_t s, KernelArgs& args, bool timed = false) {
+  void* params[] = {&args};
+  launch_raw(k, grid, s, params, timed);
 }
 
 static void fill_args_inputs(KernelArgs& a, const std::vector<ColumnView>& cols) {

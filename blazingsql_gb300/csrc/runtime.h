@@ -28,6 +28,11 @@ std::vector<ColumnView> to_views(const gx_column_view* cols, int n);
 // stream-ordered device allocation from the device's memory pool; failures
 // raise GX_ERR_OOM (retryable)
 void* dev_alloc(size_t bytes, cudaStream_t s);
+// output columns sharing one device allocation (see alloc_outputs in runtime.cu):
+// types[i] / caps[i] per column; masks zeroed when zero_masks
+void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>& caps, bool zero_masks,
+                      gx_column* out, cudaStream_t s);
+int64_t mask_words_for(int64_t rows);  // padded 32-bit mask words an output of `rows` rows holds
 void dev_free(void* p, cudaStream_t s);
 void check_cuda(cudaError_t e, const char* what);
 // host-side fault injection for tests: fail the n-th next allocation (n >= 1)
@@ -69,6 +74,9 @@ class CompiledPlan {
   void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s,
                const ExecExtras* extras = nullptr) const;
 
+  // kernel handle of this plan for a given kind and set of columns with masks
+  JitKernel kernel_for(KernelKind kind, const std::vector<bool>& nullable) const { return kernel(kind, nullable); }
+
   const Plan& plan() const { return plan_; }
   const KernelConfig& config() const { return cfg_; }
   int mode() const { return mode_; }
@@ -96,6 +104,7 @@ void run_filter_noalloc(const CompiledPlan& cp, const std::vector<ColumnView>& c
 
 // diagnostics: per-thread kernel timing and a global launch counter
 void set_kernel_timing(bool on);
+bool kernel_timing_enabled();
 double kernel_ms(bool reset);
 int64_t launch_count();
 void add_launches(int64_t n);  // kernels launched outside CompiledPlan (learner)
@@ -106,5 +115,7 @@ void launch_copy_mask(const uint32_t* src, int64_t src_bit, uint32_t* dst, int64
 void launch_fill(void* dst, int width, uint64_t value, int64_t n, cudaStream_t s);
 void launch_fill_mask(uint32_t* dst, int64_t nrows, bool valid, int64_t dst_words, cudaStream_t s);
 void launch_scan_tiles(uint64_t* counts, int64_t n, unsigned long long* total, cudaStream_t s);
+// launches a plan kernel with an arbitrary parameter list (counted, optionally timed)
+void launch_raw(const JitKernel& k, int grid, cudaStream_t s, void** params, bool timed);
 
 }  // namespace gx

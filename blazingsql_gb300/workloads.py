@@ -150,6 +150,23 @@ def _np_columns(name: str, n: int, seed: int) -> List[HostColumn]:
     raise ValueError(name)
 
 
+def c3_batch_sizes(seed: int = 3, nbatches: int = 512, lo: int = 1024, hi: int = 4194304) -> List[int]:
+    """Execution-graph batch sizes: floor(exp(U[ln lo, ln hi])) per batch."""
+    rng = np.random.default_rng(seed)
+    return [int(np.exp(x)) for x in rng.uniform(np.log(lo), np.log(hi), nbatches)]
+
+
+def slice_batches(cols, sizes: Sequence[int]):
+    """Consecutive row ranges of one table as batches (views with offsets)."""
+    from .api import DeviceColumn
+    out = []
+    start = 0
+    for n in sizes:
+        out.append([DeviceColumn(c.type_id, c.data, c.mask, c.offset + start, n) for c in cols])
+        start += n
+    return out
+
+
 _ZIPF_CDF = None
 
 

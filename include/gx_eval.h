@@ -191,6 +191,41 @@ int gx_plan_execute_noalloc(const gx_plan* plan, const gx_column_view* columns, 
 
 void gx_plan_destroy(gx_plan* plan);
 
+/* ---- batch runner: many batches, one persistent launch (no counterpart in
+ * the reference) -------------------------------------------------------------
+ *
+ * The batched execution graph calls the filter once per batch
+ * (engine/src/execution_kernels/BatchProcessing.cpp:371-476); each call of the
+ * reference interpreter allocates, uploads, launches and synchronises
+ * (engine/src/Interpreter/interpreter_cpp.cu:440-594), which dominates batches
+ * of a few thousand rows.  A batch runner takes a whole table of batches of one
+ * plan and runs them with one persistent kernel whose blocks take tiles from
+ * every batch in turn, replayed from a captured CUDA graph (descriptor upload,
+ * scratch and mask clear, kernel, row-count readback).  Each batch's output is
+ * exactly what gx_plan_execute returns for it alone.  With autotune set, the
+ * first run of at least 2^20 rows times a few block shapes (threads per block
+ * x 32-row words per warp) on that run's batches and keeps the fastest, cached
+ * per plan, column mix and device (and in $GX_AUTOTUNE_CACHE/gx_autotune.txt
+ * when that variable names a directory).  A runner is not reentrant: one run
+ * at a time. */
+typedef struct gx_batch_runner gx_batch_runner;
+
+/* plan: a compiled filter plan (condition + at most 32 outputs); a run takes at
+ * most max_batches batches of max_total_rows rows in all. */
+gx_batch_runner* gx_batch_runner_create(const gx_plan* plan, int max_batches, int64_t max_total_rows, int autotune,
+                                        gx_status_info* status);
+
+/* columns: num_batches x num_columns views, batch-major; out: num_batches x
+ * num_outputs columns, batch-major (caller buffers when out[0].data is set,
+ * else library-owned columns sharing one allocation, each released by
+ * gx_free_columns); out_rows[b]: batch b's surviving rows. */
+int gx_batch_runner_run(gx_batch_runner* runner, const gx_column_view* columns, int num_batches, int num_columns,
+                        gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
+
+/* The block shape in use (after autotuning). */
+int gx_batch_runner_config(const gx_batch_runner* runner, int32_t* block_threads, int32_t* words_per_warp);
+void gx_batch_runner_destroy(gx_batch_runner* runner);
+
 /* ---- learned conjunct ordering (no counterpart in the reference) ---------
  *
  * A learner wraps a compiled filter plan (condition = AND of side-effect-free
@@ -266,7 +301,7 @@ const char* gx_version(void);
 /* Generated CUDA source of a plan kernel: kind 0 project, 1 fused single-pass
  * filter, 2 filter count pass, 3 filter write pass, 4 the learner's fused pass
  * (conjunct order given at launch), 5 the learner's labelling count pass
- * (per-conjunct pass counts).  Writes at most buf_len
+ * (per-conjunct pass counts), 6 the batch runner's persistent kernel.  Writes at most buf_len
  * bytes (NUL-terminated) and returns the full length, or -1 on error. */
 int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,
                                int64_t buf_len, gx_status_info* status);
