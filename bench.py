@@ -271,11 +271,14 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     data = [W.c4_batch_device(rows, seed, b) for b in range(batches)]
     torch.cuda.synchronize()
     plan = g.Plan(w.schema, w.condition, w.projections, nullable=[False] * 8)
-    policies = {"plain": N.GX_LEARN_POLICY_PLAIN, "textual": N.GX_LEARN_POLICY_TEXTUAL,
-                "learned": N.GX_LEARN_POLICY_LEARNED}
+    # learned: order from device memory, full-size outputs (no host round trip);
+    # learned_sized: prediction read back, outputs of the predicted size
+    policies = {"plain": (N.GX_LEARN_POLICY_PLAIN, 1), "textual": (N.GX_LEARN_POLICY_TEXTUAL, 1),
+                "learned": (N.GX_LEARN_POLICY_LEARNED, 0), "learned_sized": (N.GX_LEARN_POLICY_LEARNED, 1)}
     # compile every kernel variant once outside the timed passes
-    for pol in policies.values():
-        lr = g.Learner(plan, policy=pol, warmup_batches=1, relabel_every=0)
+    for pol, sized in policies.values():
+        lr = g.Learner(plan, policy=pol, warmup_batches=1, relabel_every=0, fast_words_per_warp=8,
+                       size_outputs=sized)
         for b in range(2):
             cols, _, _ = lr.execute(data[b], stream=stream)
             for c in cols:
@@ -283,8 +286,9 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     torch.cuda.synchronize()
     res = {}
     counts = {}
-    for name, pol in policies.items():
-        lr = g.Learner(plan, policy=pol, async_training=1, relabel_every=16)
+    for name, (pol, sized) in policies.items():
+        lr = g.Learner(plan, policy=pol, async_training=1, relabel_every=16, fast_words_per_warp=8,
+                       size_outputs=sized)
         infos = []
         rows_out = []
         L = N.lib()
@@ -303,7 +307,7 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
         counts[name] = rows_out
         res[name] = {"rows_per_s": rows * batches / (ms / 1e3), "ms": ms,
                      "launches": L.gx_debug_launch_count() - l0}
-        if name == "learned":
+        if name.startswith("learned"):
             res[name].update({
                 "plain_batches": sum(1 for i in infos if i["path"] == 0),
                 "reruns": sum(i["reruns"] for i in infos),
@@ -311,7 +315,7 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
                 "orders_used": len({tuple(i["order"]) for i in infos if i["path"] == 1}),
             })
         del lr
-    identical = counts["plain"] == counts["textual"] == counts["learned"]
+    identical = counts["plain"] == counts["textual"] == counts["learned"] == counts["learned_sized"]
     # sampled full-output comparison
     checks = 0
     for b in (0, batches // 2, batches - 1):
@@ -328,7 +332,9 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
         "workload": f"c4_learned_order_filter: {batches} batches x {rows} rows, 8 Zipf(1.2) columns, 6 AND conjuncts",
         "plain_rows_per_s": res["plain"]["rows_per_s"], "textual_rows_per_s": res["textual"]["rows_per_s"],
         "learned_rows_per_s": res["learned"]["rows_per_s"],
+        "learned_sized_rows_per_s": res["learned_sized"]["rows_per_s"],
         "learned_vs_plain": res["learned"]["rows_per_s"] / res["plain"]["rows_per_s"],
+        "learned_sized_vs_plain": res["learned_sized"]["rows_per_s"] / res["plain"]["rows_per_s"],
         "learned_vs_textual": res["learned"]["rows_per_s"] / res["textual"]["rows_per_s"],
         "identical_output": identical, "row_counts_checked": batches, "full_outputs_checked": checks,
         "detail": res,

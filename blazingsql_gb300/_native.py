@@ -68,7 +68,8 @@ class LearnerOptions(C.Structure):
     _fields_ = [("policy", C.c_int32), ("warmup_batches", C.c_int32), ("relabel_every", C.c_int32),
                 ("train_steps", C.c_int32), ("learning_rate", C.c_float), ("hidden", C.c_int32),
                 ("capacity_margin", C.c_double), ("capacity_slack", C.c_int64), ("sketch_stride_words", C.c_int64),
-                ("async_training", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64)]
+                ("async_training", C.c_int32), ("fast_words_per_warp", C.c_int32), ("seed", C.c_uint64),
+                ("size_outputs", C.c_int32), ("reserved", C.c_int32)]
 
 
 class LearnedBatchInfo(C.Structure):

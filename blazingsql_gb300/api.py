@@ -307,6 +307,32 @@ class Plan:
             pass
 
 
+class _BatchReport(dict):
+    """Per-batch report of the learner (a dict, filled on first access)."""
+
+    def __init__(self, info):
+        super().__init__()
+        self._info = info
+
+    def _fill(self):
+        if self._info is None:
+            return
+        info, self._info = self._info, None
+        k = info.num_conjuncts
+        self.update({"path": info.path, "reruns": info.reruns, "rows": info.rows,
+                     "predicted_rows": info.predicted_rows, "train_loss": info.train_loss,
+                     "order": list(info.order[:k]), "predicted_sel": list(info.predicted_sel[:k]),
+                     "measured_sel": list(info.measured_sel[:k])})
+
+    def __getitem__(self, key):
+        self._fill()
+        return super().__getitem__(key)
+
+    def __repr__(self):
+        self._fill()
+        return super().__repr__()
+
+
 class BatchRunner:
     """A table of batches of one filter plan through one persistent kernel in a
     captured CUDA graph (gx_batch_runner_*)."""
@@ -392,17 +418,17 @@ class Learner:
         views, nc = _views(table, keep)
         s = _stream_handle(stream)
         n = self.num_outputs
-        outs = (N.Column * max(1, n))()
-        rows = C.c_int64(0)
+        if not hasattr(self, "_outs"):
+            self._outs = (N.Column * max(1, n))()
+            self._rows = C.c_int64(0)
+            self._st = N.StatusInfo()
+        outs = self._outs
+        for i in range(n):
+            outs[i] = N.Column()
         info = N.LearnedBatchInfo()
-        st = N.StatusInfo()
-        N.check(N.lib().gx_learner_execute(self._h, views, nc, outs, C.byref(rows), C.byref(info), s, C.byref(st)),
-                st)
-        k = info.num_conjuncts
-        rep = {"path": info.path, "reruns": info.reruns, "rows": info.rows, "predicted_rows": info.predicted_rows,
-               "train_loss": info.train_loss, "order": list(info.order[:k]),
-               "predicted_sel": list(info.predicted_sel[:k]), "measured_sel": list(info.measured_sel[:k])}
-        return _wrap(outs, n, s), rows.value, rep
+        N.check(N.lib().gx_learner_execute(self._h, views, nc, outs, C.byref(self._rows), C.byref(info), s,
+                                           C.byref(self._st)), self._st)
+        return _wrap(outs, n, s), self._rows.value, _BatchReport(info)
 
     def features(self, table: Table, stream=None):
         """The sketch features of one batch and the per-column anchors

@@ -82,23 +82,37 @@ __device__ void sketch_partial_block(const SketchCols& c, int64_t n, int64_t str
 #pragma unroll
   for (int i = 0; i < kSketchBins; i++) hist[i] = 0.f;
   float valid_n = 0.f, null_n = 0.f;
-  for (int64_t s = (int64_t)blockIdx.x * 8 + warp; s < nsamp; s += (int64_t)gridDim.x * 8) {
-    const int64_t row = s * stride_words * 32 + lane;
-    if (row >= n) continue;
-    const int64_t bit = c.off[col] + row;
-    const bool valid = c.mask[col] == nullptr || ((c.mask[col][bit >> 5] >> (bit & 31)) & 1u);
-    if (!valid) {
-      null_n += 1.f;
-      continue;
-    }
-    const float d = (float)(sketch_value(c.data[col], c.type[col], c.off[col] + row) - anchor);
-    const float t = copysignf(log1pf(fabsf(d)), d);
-    mn = fminf(mn, t);
-    mx = fmaxf(mx, t);
-    const int b = sketch_bin(t);
+  const int64_t step = (int64_t)gridDim.x * 8;
+  // four sampled words per warp at a time: their loads are in flight together
+  for (int64_t s0 = (int64_t)blockIdx.x * 8 + warp; s0 < nsamp; s0 += 4 * step) {
+    double v[4];
+    int st[4];  // 0 absent, 1 null, 2 valid
 #pragma unroll
-    for (int i = 0; i < kSketchBins; i++) hist[i] += (i == b) ? 1.f : 0.f;
-    valid_n += 1.f;
+    for (int q = 0; q < 4; q++) {
+      const int64_t s = s0 + q * step;
+      const int64_t row = s * stride_words * 32 + lane;
+      st[q] = 0;
+      v[q] = 0.0;
+      if (s < nsamp && row < n) {
+        const int64_t bit = c.off[col] + row;
+        const bool valid = c.mask[col] == nullptr || ((c.mask[col][bit >> 5] >> (bit & 31)) & 1u);
+        st[q] = valid ? 2 : 1;
+        if (valid) v[q] = sketch_value(c.data[col], c.type[col], c.off[col] + row);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (st[q] == 1) null_n += 1.f;
+      if (st[q] != 2) continue;
+      const float d = (float)(v[q] - anchor);
+      const float t = copysignf(log1pf(fabsf(d)), d);
+      mn = fminf(mn, t);
+      mx = fmaxf(mx, t);
+      const int b = sketch_bin(t);
+#pragma unroll
+      for (int i = 0; i < kSketchBins; i++) hist[i] += (i == b) ? 1.f : 0.f;
+      valid_n += 1.f;
+    }
   }
   __shared__ float red[8][kPartial];
 #pragma unroll
@@ -313,7 +327,15 @@ __device__ void mlp_backward_block(const float* P, int F, int H, int O, const fl
 __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n, int64_t stride_words, int ncols,
                                                         float* __restrict__ partial, unsigned int* ticket,
                                                         const float* __restrict__ P, int H, int O,
-                                                        float* __restrict__ features, float* __restrict__ Z) {
+                                                        float* __restrict__ features, float* __restrict__ Z,
+                                                        const float* __restrict__ cost, int* __restrict__ order) {
+  // the last block reads the network's weights: one warp pulls them into L2
+  // while the sample loads are in flight
+  if (P && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 32) {
+    const int np = H * (ncols * kFeatPerCol) + H + H * H + H + O * H + O;
+    for (int i = threadIdx.x * 32; i < np; i += 32 * 32)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(P + i));
+  }
   sketch_partial_block(c, n, stride_words, partial);
   __shared__ bool s_last;
   __threadfence();
@@ -347,6 +369,31 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
     dense_layer_block(W2, b2, H, H, s_h, 1, s_h + 256, true);
     __syncthreads();
     dense_layer_block(W3, b3, H, O, s_h + 256, 1, Z, false);
+    if (order) {
+      // conjunct order from the prediction: rank = cost / (1 - selectivity),
+      // ascending, ties by index (the host computes the same ranks)
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float rank[16];
+        int ord[16];
+        for (int c = 0; c < O; c++) {
+          const float z = Z[c];
+          const float ls = -(fmaxf(-z, 0.f) + log1pf(expf(-fabsf(z))));
+          rank[c] = cost[c] / fmaxf(1e-9f, 1.f - expf(ls));
+          ord[c] = c;
+        }
+        for (int i = 1; i < O; i++) {
+          const int v = ord[i];
+          int j = i - 1;
+          while (j >= 0 && rank[ord[j]] > rank[v]) {
+            ord[j + 1] = ord[j];
+            j--;
+          }
+          ord[j + 1] = v;
+        }
+        for (int c = 0; c < O; c++) order[c] = ord[c];
+      }
+    }
   }
 }
 
@@ -427,8 +474,10 @@ static void* must_alloc(size_t bytes) {
   return p;
 }
 
-static std::shared_ptr<CompiledPlan> variant(const CompiledPlan& base, int mode, bool stats, bool runtime_order) {
+static std::shared_ptr<CompiledPlan> variant(const CompiledPlan& base, int mode, bool stats, bool runtime_order,
+                                             int words = 0) {
   KernelConfig c = base.config();
+  if (words > 0) c.words = words;
   c.short_circuit = false;
   c.conjunct_order.clear();
   c.conj_stats = stats;
@@ -498,7 +547,7 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     fail(GX_ERR_INVALID, "unknown learner policy");
   if (opt_.stride_words < 1) opt_.stride_words = 1;
   plain_ = variant(base, GX_FILTER_TWO_PASS, opt_.policy == GX_LEARN_POLICY_LEARNED, false);
-  fast_ = variant(base, GX_FILTER_SINGLE_PASS, false, true);
+  fast_ = variant(base, GX_FILTER_SINGLE_PASS, false, true, opt_.fast_words);
   ncols_ = std::min((int)p.schema.size(), kMaxSketchCols);
   nconj_ = (int)p.conjuncts.size();
   // cost of a conjunct: bytes per row of the distinct columns its cone reads
@@ -536,11 +585,15 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     dfeat_ = (float*)must_alloc((size_t)F_ * 4 * (1 + kTrainRing));
     dtrainX_ = dfeat_ + F_;
     dtrainY_ = (float*)must_alloc((size_t)O_ * 4 * kTrainRing);
+    dsnapX_ = (float*)must_alloc((size_t)(F_ + O_) * 4 * kTrainRing);
+    dsnapY_ = dsnapX_ + (size_t)F_ * kTrainRing;
     dact_ = (float*)must_alloc((size_t)4 * (2 * kTrainRing * H_ + kTrainRing * O_ + 4));
     dact_inf_ = (float*)must_alloc((size_t)4 * (2 * H_ + O_ + 4));
     dpartial_ = (float*)must_alloc((size_t)4 * kPartial * kMaxSketchCols * kSketchParts);
     dcounts_ = (unsigned long long*)must_alloc(8 * 16);
     dticket_ = (unsigned int*)must_alloc(16);
+    dcost_ = (float*)must_alloc(4 * 16 + 4 * 16);
+    dorder_ = (int*)(dcost_ + 16);
     // pinned host block: predictions z[16], the loss at [16], conjunct counts from byte 256
     check_cuda(cudaMallocHost(&hpinned_, 512), "pinned host buffer");
     hcounts_ = (unsigned long long*)((char*)hpinned_ + 256);
@@ -573,6 +626,9 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     check_cuda(cudaMemcpy(dinfer_, init.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "init params");
     check_cuda(cudaMemset(dmom_, 0, (size_t)nparams_ * 8), "init adam");
     check_cuda(cudaMemset(dticket_, 0, 16), "init ticket");
+    std::vector<float> cost(16, 0.f);
+    for (int c = 0; c < nconj_; c++) cost[c] = (float)conj_cost_[c];
+    check_cuda(cudaMemcpy(dcost_, cost.data(), 4 * 16, cudaMemcpyHostToDevice), "init costs");
   } catch (...) {
     release();
     throw;
@@ -584,18 +640,22 @@ void Learner::release() {
   cudaFree(dparams_);
   cudaFree(dfeat_);
   cudaFree(dtrainY_);
+  cudaFree(dsnapX_);
   cudaFree(dact_);
   cudaFree(dact_inf_);
   cudaFree(dpartial_);
   cudaFree(dcounts_);
   cudaFree(dticket_);
+  cudaFree(dcost_);
   if (hpinned_) cudaFreeHost(hpinned_);
   if (train_done_) cudaEventDestroy(train_done_);
   if (labels_ready_) cudaEventDestroy(labels_ready_);
   if (train_stream_) cudaStreamDestroy(train_stream_);
-  dparams_ = dfeat_ = dtrainY_ = dact_ = dact_inf_ = dpartial_ = hpinned_ = nullptr;
+  dparams_ = dfeat_ = dtrainY_ = dact_ = dact_inf_ = dpartial_ = hpinned_ = dsnapX_ = dsnapY_ = nullptr;
   dcounts_ = nullptr;
   dticket_ = nullptr;
+  dcost_ = nullptr;
+  dorder_ = nullptr;
   train_done_ = labels_ready_ = nullptr;
   train_stream_ = nullptr;
 }
@@ -615,7 +675,8 @@ void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStre
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   dim3 grid(kSketchParts, ncols_);
   k_sketch_predict<<<grid, 256, 0, s>>>(c, n, opt_.stride_words, ncols_, dpartial_, dticket_,
-                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_ + 2 * H_);
+                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_ + 2 * H_, dcost_,
+                                        predict ? dorder_ : nullptr);
   check_cuda(cudaGetLastError(), "k_sketch_predict");
   add_launches(1);
 }
@@ -659,8 +720,7 @@ std::vector<float> Learner::predict_log_sel(const std::vector<ColumnView>& cols,
 
 void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s) {
   const int slot = (int)(seen_ % (uint64_t)kTrainRing);
-  // the ring must not change under a training round still running
-  if (train_stream_) check_cuda(cudaStreamWaitEvent(s, train_done_, 0), "wait training");
+  // (a side-stream training round reads a snapshot of the ring, not the ring)
   k_add_example<<<1, 128, 0, s>>>(dfeat_, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
                                   dtrainY_ + (size_t)slot * O_);
   check_cuda(cudaGetLastError(), "k_add_example");
@@ -674,14 +734,30 @@ void Learner::train(int steps, cudaStream_t s) {
   if (M == 0 || steps <= 0) return;
   check_mlp_shape(F_, H_, O_, M);
   cudaStream_t ts = s;
+  const float* X = dtrainX_;
+  const float* Y = dtrainY_;
   if (train_stream_) {
+    // one round at a time on the side stream; a round asked for meanwhile
+    // starts once the running one has finished (execute checks)
+    if (cudaEventQuery(train_done_) != cudaSuccess) {
+      cudaGetLastError();
+      train_pending_ = true;
+      return;
+    }
+    // the round trains on a snapshot, so later batches may add examples
+    // without waiting for it
+    check_cuda(cudaMemcpyAsync(dsnapX_, dtrainX_, (size_t)M * F_ * 4, cudaMemcpyDeviceToDevice, s), "snapshot X");
+    check_cuda(cudaMemcpyAsync(dsnapY_, dtrainY_, (size_t)M * O_ * 4, cudaMemcpyDeviceToDevice, s), "snapshot Y");
     check_cuda(cudaEventRecord(labels_ready_, s), "labels event");
     check_cuda(cudaStreamWaitEvent(train_stream_, labels_ready_, 0), "wait labels");
     ts = train_stream_;
+    X = dsnapX_;
+    Y = dsnapY_;
   }
+  train_pending_ = false;
   float* dloss = dact_ + 2 * kTrainRing * H_ + kTrainRing * O_;
-  k_mlp_train<<<1, 256, backward_smem(H_, O_, M), ts>>>(dparams_, dgrad_, dmom_, dvel_, F_, H_, O_, dtrainX_, M,
-                                                        dtrainY_, dact_, steps, adam_t_, opt_.lr, dloss);
+  k_mlp_train<<<1, 256, backward_smem(H_, O_, M), ts>>>(dparams_, dgrad_, dmom_, dvel_, F_, H_, O_, X, M, Y, dact_,
+                                                        steps, adam_t_, opt_.lr, dloss);
   check_cuda(cudaGetLastError(), "k_mlp_train");
   add_launches(1);
   adam_t_ += steps;
@@ -717,6 +793,9 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     if (info) *info = bi;
     return;
   }
+  // a training round asked for while the previous one ran starts now if it can
+  if (train_pending_ && train_stream_ && cudaEventQuery(train_done_) == cudaSuccess) train(opt_.train_steps, s);
+  cudaGetLastError();
   const bool warm = labelled_ < (uint64_t)opt_.warmup_batches;
   const bool relabel = !warm && opt_.relabel_every > 0 && since_label_ >= opt_.relabel_every;
   if (warm || relabel || n == 0) {
@@ -747,6 +826,28 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     return;
   }
   since_label_++;
+  if (!opt_.size_outputs) {
+    // order decided on the device: no host round trip before the filter
+    sync_inference_params(s);
+    sketch(cols, true, s);
+    int* horder = (int*)((char*)hpinned_ + 400);
+    check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, s), "prediction");
+    check_cuda(cudaMemcpyAsync(horder, dorder_, O_ * 4, cudaMemcpyDeviceToHost, s), "order");
+    ExecExtras ex;
+    ex.order_dev = dorder_;
+    fast_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    for (int o = 0; o < O_; o++) {
+      const float z = hpinned_[o];
+      bi.predicted_sel[o] = std::exp(-(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z)))));
+      bi.order[o] = horder[o];
+    }
+    if (train_stream_ && !params_pending_) loss_ = hpinned_[16];
+    bi.train_loss = loss_;
+    bi.path = 1;
+    bi.rows = out_rows ? *out_rows : 0;
+    if (info) *info = bi;
+    return;
+  }
   const std::vector<float> ls = predict_log_sel(cols, s);
   if (train_stream_ && !params_pending_) loss_ = hpinned_[16];
   // order by rank = cost / (1 - selectivity): cheap conjuncts that remove most rows first
@@ -876,6 +977,8 @@ void gx_learner_options_init(gx_learner_options* o) {
   o->sketch_stride_words = d.stride_words;
   o->async_training = d.async_training ? 1 : 0;
   o->seed = d.seed;
+  o->fast_words_per_warp = d.fast_words;
+  o->size_outputs = d.size_outputs ? 1 : 0;
 }
 
 gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* options, gx_status_info* status) {
@@ -895,9 +998,11 @@ gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* opt
     lo.hidden = o.hidden > 0 ? o.hidden : 64;
     lo.capacity_margin = o.capacity_margin >= 1.0 ? o.capacity_margin : 1.0;
     lo.capacity_slack = std::max<int64_t>(0, o.capacity_slack);
-    lo.stride_words = o.sketch_stride_words > 0 ? o.sketch_stride_words : 64;
+    lo.stride_words = o.sketch_stride_words > 0 ? o.sketch_stride_words : 256;
     lo.async_training = o.async_training != 0;
     lo.seed = o.seed;
+    lo.fast_words = o.fast_words_per_warp > 0 ? std::min(o.fast_words_per_warp, 32) : 0;
+    lo.size_outputs = o.size_outputs != 0;
     out = new gx_learner{std::make_unique<gx::Learner>(*cp, lo)};
   });
   return out;

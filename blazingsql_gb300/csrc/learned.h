@@ -23,8 +23,10 @@ struct LearnerOptions {
   float lr = 3e-3f;
   double capacity_margin = 1.5;   // output rows allocated = predicted x margin + slack
   int64_t capacity_slack = 4096;
-  int64_t stride_words = 64;  // sketch reads every n-th 32-row word
+  int64_t stride_words = 256;  // sketch reads every n-th 32-row word
   int hidden = 64;
+  int fast_words = 0;         // words per warp of the single-pass kernel (0: the plan's)
+  bool size_outputs = true;   // prediction read back: outputs of the predicted size
   bool async_training = false;  // train on a side stream (overlapped; prediction timing then varies)
   uint64_t seed = 1;
 };
@@ -87,16 +89,21 @@ class Learner {
   float* dfeat_ = nullptr;    // current batch's features
   float* dtrainX_ = nullptr;  // ring of labelled examples
   float* dtrainY_ = nullptr;
+  float* dsnapX_ = nullptr;   // snapshot of the ring a side-stream round trains on
+  float* dsnapY_ = nullptr;
   float* dact_ = nullptr;     // training activations
   float* dact_inf_ = nullptr; // inference activations
   float* dpartial_ = nullptr;
   unsigned long long* dcounts_ = nullptr;
   unsigned int* dticket_ = nullptr;  // last-block ticket of the sketch kernel
+  float* dcost_ = nullptr;           // per conjunct: bytes per row its columns read
+  int* dorder_ = nullptr;            // the order the predict kernel chose
   float* hpinned_ = nullptr;  // pinned host: predictions + loss
   unsigned long long* hcounts_ = nullptr;  // pinned host: per-conjunct pass counts
   cudaStream_t train_stream_ = nullptr;
   cudaEvent_t train_done_ = nullptr, labels_ready_ = nullptr;
-  bool params_pending_ = false;  // training finished a version not yet copied to dinfer_
+  bool params_pending_ = false;
+  bool train_pending_ = false;   // a round was asked for while another ran  // training finished a version not yet copied to dinfer_
   uint64_t seen_ = 0, labelled_ = 0, batches_ = 0;
   int since_label_ = 0;  // single-pass batches since the last labelled one
   int adam_t_ = 0;

@@ -594,7 +594,7 @@ class Gen {
     o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) live_[k] = __ballot_sync(GX_FULL, alive[k]);\n";
     o << ind << "for (int j_ = 0; j_ < " << nc << "; j_++) {\n";
     o << ind << "  bool keep_[GX_V];\n";
-    o << ind << "  switch (a.order[j_]) {\n";
+    o << ind << "  switch (a.order_dev ? __ldg(a.order_dev + j_) : a.order[j_]) {\n";
     for (int c = 0; c < nc; c++) {
       const int cid = p_.conjuncts[c];
       o << ind << "    case " << c << ": {\n";
@@ -745,7 +745,7 @@ void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
        "  const void* in_data[GX_MAX_COLS]; const u32* in_mask[GX_MAX_COLS]; i64 in_off[GX_MAX_COLS];\n"
        "  void* out_data[GX_MAX_OUTS]; u32* out_mask[GX_MAX_OUTS];\n"
        "  i64 n; i64 capacity; u64* tile_status; unsigned long long* tile_counter; unsigned long long* out_count;\n"
-       "  int* err; u64 seed; unsigned long long* conj_counts; int order[16];\n};\n";
+       "  int* err; u64 seed; unsigned long long* conj_counts; int order[16]; const int* order_dev;\n};\n";
 }
 
 // phase 2 of the filter kernels: projections for the kept rows of each word,
@@ -784,12 +784,9 @@ std::vector<size_t> masked_outputs(const Plan& p) {
 // validity word of a round is contiguous.  Operands are re-read with the
 // gathered row index (predicate columns hit L1/L2).
 // statements mapping kept rank t_ of the warp (0 <= t_ < total_) to its row
+// through the warp's kept-row list in shared memory
 void emit_rank_to_row(std::ostringstream& o, const std::string& ind) {
-  o << ind << "u32 bks_ = 0u, cks_ = 0u; int sk_ = 0;\n";
-  o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++)\n";
-  o << ind << "  if (t_ >= cum_[kk] && t_ < cum_[kk + 1]) { sk_ = kk; bks_ = bal[kk]; cks_ = cum_[kk]; }\n";
-  o << ind << "const int src_ = act ? (int)__fns(bks_, 0u, (int)(t_ - cks_) + 1) : 0;\n";
-  o << ind << "const i64 row = (w0 + sk_) * 32 + src_; const bool inr = act; (void)inr;\n";
+  o << ind << "const i64 row = w0 * 32 + (act ? (i64)s_kept_[warp][t_] : 0); const bool inr = act; (void)inr;\n";
   o << ind << "const i64 orow = (i64)pos + (i64)t_; (void)orow;\n";
   o << ind << "const int k = 0;\n";
 }
@@ -830,9 +827,14 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
     stop.insert(lz[i].root);
   }
   const std::vector<int> proj = g.cone_stop(roots, stop);
-  o << ind << "u32 cum_[GX_V + 1]; cum_[0] = 0u;\n";
-  o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++) cum_[kk + 1] = cum_[kk] + __popc(bal[kk]);\n";
-  o << ind << "const u32 total_ = cum_[GX_V];\n";
+  // the warp's kept rows in order: offsets from its first row, by kept rank
+  o << ind << "__shared__ unsigned short s_kept_[GX_WARPS][GX_V * 32];\n";
+  o << ind << "u32 total_ = 0u;\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int kk = 0; kk < GX_V; kk++) {\n";
+  o << ind << "  if ((bal[kk] >> lane) & 1u) s_kept_[warp][total_ + __popc(bal[kk] & ((1u << lane) - 1u))] = (unsigned short)(kk * 32 + lane);\n";
+  o << ind << "  total_ += __popc(bal[kk]);\n";
+  o << ind << "}\n";
+  o << ind << "__syncwarp();\n";
   if (!lz.empty()) {
     const int nl = (int)lz.size();
     o << ind << "__shared__ u64 s_lzb_[" << nl << "][GX_WARPS][GX_V * 32];\n";
@@ -842,6 +844,7 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
     for (const auto& l : lz) conds.push_back(l.cond);
     const std::vector<int> cond_ids = g.cone(conds);
     o << ind << "u32 dmd_[" << nl << "][GX_V];\n";
+    o << ind << "__shared__ unsigned short s_dem_[GX_WARPS][GX_V * 32];\n";
     o << ind << "#pragma unroll\n" << ind << "for (int r_ = 0; r_ < GX_V; r_++) {\n";
     const std::string i2 = ind + "  ";
     o << i2 << "#pragma unroll\n" << i2 << "for (int l_ = 0; l_ < " << nl << "; l_++) dmd_[l_][r_] = 0u;\n";
@@ -859,20 +862,23 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
     // pass 2: each branch over its selecting rows, 32 at a time
     for (int i = 0; i < nl; i++) {
       o << ind << "{\n";
-      o << i2 << "u32 dc_[GX_V + 1]; dc_[0] = 0u;\n";
-      o << i2 << "#pragma unroll\n" << i2 << "for (int r_ = 0; r_ < GX_V; r_++) dc_[r_ + 1] = dc_[r_] + __popc(dmd_[" << i
-        << "][r_]);\n";
-      o << i2 << "for (u32 db_ = 0; db_ < dc_[GX_V]; db_ += 32u) {\n";
-      o << i3 << "const u32 q_ = db_ + (u32)lane; const bool act = q_ < dc_[GX_V];\n";
-      o << i3 << "u32 dbits_ = 0u, dcs_ = 0u; int dr_ = 0;\n";
-      o << i3 << "#pragma unroll\n" << i3 << "for (int r_ = 0; r_ < GX_V; r_++)\n";
-      o << i3 << "  if (q_ >= dc_[r_] && q_ < dc_[r_ + 1]) { dr_ = r_; dbits_ = dmd_[" << i << "][r_]; dcs_ = dc_[r_]; }\n";
-      o << i3 << "const u32 t_ = (u32)dr_ * 32u + (act ? (u32)__fns(dbits_, 0u, (int)(q_ - dcs_) + 1) : 0u);\n";
+      // the kept ranks selecting branch i, in order, listed in shared memory
+      o << i2 << "u32 dtot_ = 0u;\n";
+      o << i2 << "#pragma unroll\n" << i2 << "for (int r_ = 0; r_ < GX_V; r_++) {\n";
+      o << i2 << "  const u32 db_ = dmd_[" << i << "][r_];\n";
+      o << i2 << "  if ((db_ >> lane) & 1u) s_dem_[warp][dtot_ + __popc(db_ & ((1u << lane) - 1u))] = (unsigned short)(r_ * 32 + lane);\n";
+      o << i2 << "  dtot_ += __popc(db_);\n";
+      o << i2 << "}\n";
+      o << i2 << "__syncwarp();\n";
+      o << i2 << "for (u32 db_ = 0; db_ < dtot_; db_ += 32u) {\n";
+      o << i3 << "const u32 q_ = db_ + (u32)lane; const bool act = q_ < dtot_;\n";
+      o << i3 << "const u32 t_ = act ? (u32)s_dem_[warp][q_] : 0u;\n";
       emit_rank_to_row(o, i3);
       emit_row_nodes(o, g, p, lz[i].nodes, {}, i3);
       o << i3 << "if (act) { s_lzb_[" << i << "][warp][t_] = " << g.B(lz[i].root) << "; s_lzv_[" << i
         << "][warp][t_] = " << g.V(lz[i].root) << " ? 1 : 0; }\n";
       o << i2 << "}\n";
+      o << i2 << "__syncwarp();\n";  // s_dem_ is rewritten for the next branch
       o << ind << "}\n";
     }
     o << ind << "__syncwarp();\n";
@@ -905,7 +911,7 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   o << in2 << "  bfirst_ = false; bword_++; bf_ = nf_ - 32;\n";
   o << in2 << "} else {\n" << in2 << "  bf_ = nf_;\n" << in2 << "}\n";
   o << ind << "}\n";
-  if (!lz.empty()) o << ind << "__syncwarp();\n";  // shared branch results are reused by the next tile
+  o << ind << "__syncwarp();\n";  // the kept-row list and branch results are rewritten by the next tile
   o << ind << "if (bf_ > 0 && lane == 0 && bword_ < cap_words) {\n";
   for (size_t j : mo) o << ind << "  atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]);\n";
   o << ind << "}\n";

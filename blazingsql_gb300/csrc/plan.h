@@ -117,6 +117,7 @@ struct KernelArgs {
   uint64_t seed;
   unsigned long long* conj_counts;  // COUNT_FILTER with conj_stats: passes per conjunct
   int32_t order[16];                // runtime conjunct order (runtime_order kernels)
+  const int32_t* order_dev;         // if set: the order in device memory (written by an earlier kernel)
 };
 
 }  // namespace gx

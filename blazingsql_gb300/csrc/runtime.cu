@@ -544,6 +544,7 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     for (int i = 0; i < 16; i++) a.order[i] = i;
     if (extras) {
       for (int i = 0; i < extras->num_order && i < 16; i++) a.order[i] = extras->order[i];
+      a.order_dev = extras->order_dev;
       a.conj_counts = extras->conj_counts;
     }
     unsigned long long host_hdr[4] = {0, 0, 0, 0};

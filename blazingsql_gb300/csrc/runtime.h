@@ -45,6 +45,7 @@ void free_column(gx_column& c, cudaStream_t s);
 // Per-launch extras of a filter execution (learned ordering, label counting).
 struct ExecExtras {
   const int* order = nullptr;              // runtime conjunct order (runtime_order kernels)
+  const int* order_dev = nullptr;          // or the order in device memory (read by the kernel)
   int num_order = 0;
   unsigned long long* conj_counts = nullptr;  // device counters, one per conjunct (conj_stats count pass)
   unsigned long long* conj_counts_host = nullptr;  // optional host copy of them, made before the count sync

@@ -258,10 +258,14 @@ typedef struct gx_learner_options {
   int32_t hidden;          /* hidden width (default 64, at most 256) */
   double capacity_margin;  /* rows allocated = predicted rows x margin + slack (default 1.5) */
   int64_t capacity_slack;  /* default 4096 */
-  int64_t sketch_stride_words; /* sketch every n-th 32-row word (default 64) */
+  int64_t sketch_stride_words; /* sketch every n-th 32-row word (default 256) */
   int32_t async_training;  /* 1: train on a side stream, overlapped with later batches */
-  int32_t reserved;
+  int32_t fast_words_per_warp; /* 32-row words per warp of the single-pass kernel (0: the plan's) */
   uint64_t seed;           /* parameter initialisation */
+  int32_t size_outputs;    /* 1 (default): read the prediction back and allocate outputs of the predicted
+                              size (one extra host round trip per batch); 0: the kernel takes the order
+                              from device memory right after the prediction, outputs have full size */
+  int32_t reserved;
 } gx_learner_options;
 
 /* Per-batch report of gx_learner_execute. */

@@ -61,7 +61,7 @@ def test_learner_kernels_compile():
     plan = g.Plan(W.workload("c4").schema, W.C4_CONDITION, W.C4_PROJECTIONS, nullable=[False] * 8)
     assert plan.num_conjuncts == 6
     src = plan.kernel_source(4, [False] * 8)
-    assert "switch (a.order[j_])" in src
+    assert "a.order_dev + j_" in src and "a.order[j_]" in src
     assert "s_conj" in plan.kernel_source(5, [False] * 8)
     plan.compile_check(4, [False] * 8)
     plan.compile_check(5, [False] * 8)
@@ -130,13 +130,16 @@ def test_sketch_features_match_oracle():
 
 
 @pytest.mark.gpu
-def test_learned_matches_plain_and_oracle():
+@pytest.mark.parametrize("size_outputs", [1, 0])
+def test_learned_matches_plain_and_oracle(size_outputs):
     """Warm-up, learned single-pass and relabel batches all return the plain
-    path's output; a few batches are also checked against the CPU oracle."""
+    path's output; a few batches are also checked against the CPU oracle.  With
+    size_outputs=0 the kernel takes the order from device memory."""
     import blazingsql_gb300 as g
     from helpers import OracleEngine
     plan = _c4_plan(g)
-    learned = g.Learner(plan, warmup_batches=4, relabel_every=5, train_steps=32)
+    learned = g.Learner(plan, warmup_batches=4, relabel_every=5, train_steps=32, size_outputs=size_outputs,
+                        fast_words_per_warp=8)
     plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
     oracle = OracleEngine(nthreads=4)
     paths = set()
