@@ -22,9 +22,9 @@ GX_ERR_INVALID = 7
 GX_ERR_CAPACITY = 8
 
 # gx_plan_execute_noalloc: tile status words of its fixed scratch array, and the
-# largest batch that fits with the default 1024-row tile (8 warps x 4 words x 32)
+# largest batch that fits with the default 512-row tile (4 warps x 4 words x 32)
 GX_NOALLOC_MAX_TILES = 524284
-GX_NOALLOC_MAX_ROWS = GX_NOALLOC_MAX_TILES * 1024
+GX_NOALLOC_MAX_ROWS = GX_NOALLOC_MAX_TILES * 512
 
 GX_FILTER_AUTO = 0
 GX_FILTER_TWO_PASS = 1

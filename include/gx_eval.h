@@ -171,13 +171,13 @@ int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_
  * rest of the GPU), or a per-batch path that must not enter an allocator.
  * Same kernel and results as gx_plan_execute in GX_FILTER_SINGLE_PASS mode;
  * the kernel's scratch (row-count, ticket and error words plus one status word
- * per 1024-row tile) comes from a fixed 4 MiB array in the library's device
+ * per tile, 512 rows by default) comes from a fixed 4 MiB array in the library's device
  * memory that every GPU loading the library keeps until the process exits.
  *
  * - out[i].data, out[i].null_mask and out[i].capacity must be set by the
  *   caller; null_mask must hold ((capacity + 511) / 512) * 64 bytes (>= 64).
  * - Batches needing more than GX_NOALLOC_MAX_TILES tiles (more than
- *   536,866,816 rows with the default tile) are rejected with GX_ERR_INVALID.
+ *   268,433,408 rows with the default tile) are rejected with GX_ERR_INVALID.
  * - All calls share the one array (it keeps the last call's contents and is
  *   cleared at the start of each call), so calls whose work overlaps on the
  *   GPU -- on different streams or host threads at the same time -- race:
