@@ -60,12 +60,18 @@ class DeviceColumn:
         return DeviceColumn(col.type_id, data, mask, col.offset, col.size)
 
     def view(self) -> N.ColumnView:
+        # cached per (tensors, offset, size): data_ptr() calls cost microseconds per batch
+        key = (id(self.data), id(self.mask), self.offset, self.size, self.type_id)
+        cached = getattr(self, "_view_cache", None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
         v = N.ColumnView()
         v.type_id = self.type_id
         v.data = self.data.data_ptr()
         v.null_mask = self.mask.data_ptr() if self.mask is not None else None
         v.offset = self.offset
         v.size = self.size
+        self._view_cache = (key, v)
         return v
 
 

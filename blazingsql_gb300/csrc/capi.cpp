@@ -399,7 +399,8 @@ static KernelKind kind_of(int k) {
     case 2: case 5: return KernelKind::COUNT_FILTER;
     case 3: return KernelKind::WRITE_FILTER;
     case 6: return KernelKind::FUSED_BATCHED;
-    default: fail(GX_ERR_INVALID, "kernel kind must be 0..6");
+    case 7: return KernelKind::FUSED_STAGED;
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..7");
   }
 }
 
@@ -410,12 +411,17 @@ static std::string debug_source(const gx_plan* plan, int kind, const uint8_t* ha
   Plan p = plan->ps->chunks.at(0)->plan();
   for (size_t i = 0; i < p.nullable.size(); i++) p.nullable[i] = has_mask ? has_mask[i] != 0 : true;
   KernelConfig cfg = plan->ps->chunks.at(0)->config();
-  if (kind == 4 || kind == 5) {
+  if (kind == 4 || kind == 5 || kind == 7) {
     cfg.short_circuit = false;
     cfg.conjunct_order.clear();
-    cfg.runtime_order = kind == 4;
+    cfg.runtime_order = kind == 4 || kind == 7;
+    cfg.staged = kind == 7;
+    if (kind == 4) {  // as the learner builds it
+      const char* st = std::getenv("GX_STREAM");
+      cfg.stream_slots = st && *st ? std::atoi(st) : 0;
+    }
     cfg.conj_stats = kind == 5;
-    if (kind == 4) cfg.dense = true;
+    if (kind == 4 || kind == 7) cfg.dense = true;
   }
   return generate_kernel(p, kind_of(kind), cfg, "gx_kernel");
 }

@@ -120,6 +120,56 @@ __device__ __forceinline__ u64 gx_ld_64(const void* p, i64 i) { return (u64)__ld
 __device__ __forceinline__ u64 gx_ld_f32(const void* p, i64 i) { return gx_B((double)__ldcs((const float*)p + i)); }
 __device__ __forceinline__ u64 gx_ld_f32e(const void* p, i64 i) { return gxe_f2d(__ldcs((const unsigned*)p + i)); }
 
+// the same loads from a shared-memory staging buffer (staged filter kernel)
+__device__ __forceinline__ i64 gx_lds_i8(const void* p, i64 i) { return (i64)((const signed char*)p)[i]; }
+__device__ __forceinline__ i64 gx_lds_u8(const void* p, i64 i) { return (i64)((const unsigned char*)p)[i]; }
+__device__ __forceinline__ i64 gx_lds_i16(const void* p, i64 i) { return (i64)((const short*)p)[i]; }
+__device__ __forceinline__ i64 gx_lds_u16(const void* p, i64 i) { return (i64)((const unsigned short*)p)[i]; }
+__device__ __forceinline__ i64 gx_lds_i32(const void* p, i64 i) { return (i64)((const int*)p)[i]; }
+__device__ __forceinline__ i64 gx_lds_u32(const void* p, i64 i) { return (i64)((const unsigned int*)p)[i]; }
+__device__ __forceinline__ u64 gx_lds_64(const void* p, i64 i) { return (u64)((const long long*)p)[i]; }
+__device__ __forceinline__ u64 gx_lds_f32(const void* p, i64 i) { return gx_B((double)((const float*)p)[i]); }
+__device__ __forceinline__ u64 gx_lds_f32e(const void* p, i64 i) { return gxe_f2d(((const unsigned*)p)[i]); }
+
+// ---- bulk copies (TMA, 1-D) into shared memory with mbarrier completion ----
+__device__ __forceinline__ u32 gx_saddr(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void gx_mbar_init(u64* bar, u32 count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(gx_saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void gx_mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// one arrival that also announces `bytes` of bulk copies still to land
+__device__ __forceinline__ void gx_mbar_arrive_tx(u64* bar, u32 bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(gx_saddr(bar)), "r"(bytes) : "memory");
+}
+// non-blocking test of the phase with the given parity
+__device__ __forceinline__ bool gx_mbar_try_wait(u64* bar, u32 parity) {
+  u32 ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(gx_saddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+__device__ __forceinline__ void gx_bulk_g2s(void* dst, const void* src, u32 bytes, u64* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   gx_saddr(dst)),
+               "l"(src), "r"(bytes), "r"(gx_saddr(bar))
+               : "memory");
+}
+// 16-byte asynchronous global -> shared copy (L2 only), and an arrival on an
+// mbarrier once every earlier copy of this thread has landed
+__device__ __forceinline__ void gx_cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(gx_saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void gx_cp_arrive(u64* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(gx_saddr(bar)) : "memory");
+}
+// orders this thread's earlier generic-proxy accesses to shared memory before
+// later bulk copies into it
+__device__ __forceinline__ void gx_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 __device__ __forceinline__ void gx_st_8(void* p, i64 i, u64 v) { __stcs((signed char*)p + i, (signed char)v); }
 __device__ __forceinline__ void gx_st_16(void* p, i64 i, u64 v) { __stcs((short*)p + i, (short)v); }
 __device__ __forceinline__ void gx_st_32(void* p, i64 i, u64 v) { __stcs((int*)p + i, (int)v); }
@@ -209,6 +259,60 @@ __device__ __forceinline__ u64 gx_lookback_resolve(u64* status, i64 tile, u64 ag
   }
   if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (excl + agg));
   return excl;
+}
+
+// One non-blocking attempt at tile's exclusive prefix (aggregate `agg` already
+// published), continuing from (*pred, *excl): walks back while the windows are
+// complete; returns true with the prefix in *excl (and publishes the inclusive
+// prefix), or false at the first tile that has not published yet, keeping the
+// progress in *pred / *excl.  Called by one full warp; the values are
+// warp-uniform.
+__device__ __forceinline__ bool gx_lookback_poll(u64* status, i64 tile, u64 agg, i64* pred, u64* excl) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {  // published as a prefix already
+    *excl = 0ull;
+    return true;
+  }
+  i64 pr = *pred;
+  u64 ex = *excl;
+  while (true) {
+    u64 s[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const i64 idx = pr - (lane * 4 + i);
+      s[i] = idx >= 0 ? gx_ld_relaxed(status + idx) : GX_ST_PFX;
+    }
+    int first_pfx = 4;
+#pragma unroll
+    for (int i = 3; i >= 0; i--)
+      if ((u32)(s[i] >> 62) == 2u) first_pfx = i;
+    const u32 has_pfx = __ballot_sync(GX_FULL, first_pfx < 4);
+    const int pl = has_pfx ? __ffs(has_pfx) - 1 : 0;
+    const int pfx_i = __shfl_sync(GX_FULL, first_pfx, pl);
+    const int last = has_pfx ? pl * 4 + pfx_i : 127;
+    bool missing = false;
+    u64 v = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (lane * 4 + i <= last) {
+        if ((u32)(s[i] >> 62) == 0u) missing = true;
+        v += s[i] & GX_ST_VAL;
+      }
+    }
+    if (__any_sync(GX_FULL, missing)) {
+      *pred = pr;
+      *excl = ex;
+      return false;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(GX_FULL, v, o);
+    ex += v;
+    if (has_pfx) break;
+    pr -= 128;
+  }
+  if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (ex + agg));
+  *excl = ex;
+  return true;
 }
 
 // Publishes a tile's aggregate (tile 0: its inclusive prefix) from the

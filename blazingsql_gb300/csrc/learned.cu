@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -326,9 +327,10 @@ __device__ void mlp_backward_block(const float* P, int F, int H, int O, const fl
 // (kSketchParts, ncols); *ticket is zero on entry and left zero.
 __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n, int64_t stride_words, int ncols,
                                                         float* __restrict__ partial, unsigned int* ticket,
-                                                        const float* __restrict__ P, int H, int O,
+                                                        const float* P, int H, int O,
                                                         float* __restrict__ features, float* __restrict__ Z,
-                                                        const float* __restrict__ cost, int* __restrict__ order) {
+                                                        const float* __restrict__ cost, int* __restrict__ order,
+                                                        int stage_w) {
   // the last block reads the network's weights: one warp pulls them into L2
   // while the sample loads are in flight
   if (P && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 32) {
@@ -347,6 +349,19 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
   __syncthreads();
   if (!s_last) return;
   __threadfence();
+  const int F = ncols * kFeatPerCol;
+  // with dynamic shared memory for them, the weights are copied in first
+  // (their loads overlap the partials' reduction) and read from there
+  extern __shared__ float4 s_w4[];
+  const bool wsm = P && stage_w;
+  if (wsm) {
+    const int np = H * F + H + H * H + H + O * H + O;
+    const float4* P4 = reinterpret_cast<const float4*>(P);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < np / 4; i += blockDim.x) s_w4[i] = __ldg(P4 + i);
+    float* s_wf = reinterpret_cast<float*>(s_w4);
+    for (int i = (np / 4) * 4 + threadIdx.x; i < np; i += blockDim.x) s_wf[i] = __ldg(P + i);
+  }
   // features into shared memory (the forward pass reads them) and global
   // memory (a labelled batch's training example)
   __shared__ float s_x[kMaxSketchCols * kFeatPerCol];
@@ -354,7 +369,7 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
   for (int col = threadIdx.x >> 5; col < ncols; col += blockDim.x >> 5)
     sketch_final_warp(partial, col, gridDim.x, s_x + col * kFeatPerCol);
   __syncthreads();
-  const int F = ncols * kFeatPerCol;
+  if (wsm) P = reinterpret_cast<const float*>(s_w4);
   for (int i = threadIdx.x; i < F; i += blockDim.x) features[i] = s_x[i];
   if (threadIdx.x == 0) *ticket = 0u;
   if (P) {
@@ -482,7 +497,18 @@ static std::shared_ptr<CompiledPlan> variant(const CompiledPlan& base, int mode,
   c.conjunct_order.clear();
   c.conj_stats = stats;
   c.runtime_order = runtime_order;
-  if (runtime_order) c.dense = true;
+  if (runtime_order) {
+    c.dense = true;
+    // conjunct columns staged in shared memory by asynchronous copies: measured
+    // slower than direct predicated loads on the C4 batches, so on request only
+    const char* e = std::getenv("GX_STAGED");
+    c.staged = e && *e == '1';
+    // word slots in flight per warp for the short-circuit chain: measured slower
+    // than the lockstep words of a 4 x 8 block on the C4 batches (83 vs 60 us),
+    // so on request only (GX_STREAM=<slots>)
+    const char* st = std::getenv("GX_STREAM");
+    c.stream_slots = st && *st ? std::atoi(st) : 0;
+  }
   return std::make_shared<CompiledPlan>(base.plan(), c, mode);
 }
 
@@ -597,6 +623,8 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     // pinned host block: predictions z[16], the loss at [16], conjunct counts from byte 256
     check_cuda(cudaMallocHost(&hpinned_, 512), "pinned host buffer");
     hcounts_ = (unsigned long long*)((char*)hpinned_ + 256);
+    check_cuda(cudaStreamCreateWithFlags(&aux_stream_, cudaStreamNonBlocking), "aux stream");
+    check_cuda(cudaEventCreateWithFlags(&pred_ready_, cudaEventDisableTiming), "event");
     if (opt_.async_training) {
       check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
       check_cuda(cudaEventCreateWithFlags(&train_done_, cudaEventDisableTiming), "event");
@@ -651,6 +679,10 @@ void Learner::release() {
   if (train_done_) cudaEventDestroy(train_done_);
   if (labels_ready_) cudaEventDestroy(labels_ready_);
   if (train_stream_) cudaStreamDestroy(train_stream_);
+  if (pred_ready_) cudaEventDestroy(pred_ready_);
+  if (aux_stream_) cudaStreamDestroy(aux_stream_);
+  pred_ready_ = nullptr;
+  aux_stream_ = nullptr;
   dparams_ = dfeat_ = dtrainY_ = dact_ = dact_inf_ = dpartial_ = hpinned_ = dsnapX_ = dsnapY_ = nullptr;
   dcounts_ = nullptr;
   dticket_ = nullptr;
@@ -674,9 +706,12 @@ void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStre
   }
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   dim3 grid(kSketchParts, ncols_);
-  k_sketch_predict<<<grid, 256, 0, s>>>(c, n, opt_.stride_words, ncols_, dpartial_, dticket_,
-                                        predict ? dinfer_ : nullptr, H_, O_, dfeat_, dact_inf_ + 2 * H_, dcost_,
-                                        predict ? dorder_ : nullptr);
+  // weights in dynamic shared memory when they fit the default 48 KB
+  const size_t wbytes = (size_t)nparams_ * 4;
+  const bool stage_w = predict && wbytes <= 48 * 1024;
+  k_sketch_predict<<<grid, 256, stage_w ? wbytes : 0, s>>>(
+      c, n, opt_.stride_words, ncols_, dpartial_, dticket_, predict ? dinfer_ : nullptr, H_, O_, dfeat_,
+      dact_inf_ + 2 * H_, dcost_, predict ? dorder_ : nullptr, stage_w ? 1 : 0);
   check_cuda(cudaGetLastError(), "k_sketch_predict");
   add_launches(1);
 }
@@ -830,12 +865,17 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     // order decided on the device: no host round trip before the filter
     sync_inference_params(s);
     sketch(cols, true, s);
+    // the report's copy of the prediction travels on a side stream, off the
+    // filter's critical path
     int* horder = (int*)((char*)hpinned_ + 400);
-    check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, s), "prediction");
-    check_cuda(cudaMemcpyAsync(horder, dorder_, O_ * 4, cudaMemcpyDeviceToHost, s), "order");
+    check_cuda(cudaEventRecord(pred_ready_, s), "prediction event");
+    check_cuda(cudaStreamWaitEvent(aux_stream_, pred_ready_, 0), "wait prediction");
+    check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "prediction");
+    check_cuda(cudaMemcpyAsync(horder, dorder_, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "order");
     ExecExtras ex;
     ex.order_dev = dorder_;
     fast_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    check_cuda(cudaStreamSynchronize(aux_stream_), "prediction readback");
     for (int o = 0; o < O_; o++) {
       const float z = hpinned_[o];
       bi.predicted_sel[o] = std::exp(-(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z)))));

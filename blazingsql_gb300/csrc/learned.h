@@ -101,6 +101,8 @@ class Learner {
   float* hpinned_ = nullptr;  // pinned host: predictions + loss
   unsigned long long* hcounts_ = nullptr;  // pinned host: per-conjunct pass counts
   cudaStream_t train_stream_ = nullptr;
+  cudaStream_t aux_stream_ = nullptr;   // prediction readback for the batch report
+  cudaEvent_t pred_ready_ = nullptr;
   cudaEvent_t train_done_ = nullptr, labels_ready_ = nullptr;
   bool params_pending_ = false;
   bool train_pending_ = false;   // a round was asked for while another ran  // training finished a version not yet copied to dinfer_

@@ -292,9 +292,18 @@ class Gen {
     if (n.kind == Node::LIT) return;
     if (n.kind == Node::COL) {
       const int c = n.col;
-      o << ind << b << " = inr ? (u64)" << (emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c])) << "(a.in_data["
-        << c << "], a.in_off[" << c
-        << "] + row) : 0ull;\n";
+      auto st = staged_.find(c);
+      if (st != staged_.end()) {
+        // full words are staged in shared memory at (buffer, index); a partial
+        // last word is read from global memory
+        const std::string gfn = emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c]);
+        const std::string sfn = "gx_lds_" + gfn.substr(6);  // gx_ld_X -> gx_lds_X
+        o << ind << b << " = inr ? (full_word_ ? (u64)" << sfn << "(" << st->second.first << ", " << st->second.second
+          << ") : (u64)" << gfn << "(a.in_data[" << c << "], a.in_off[" << c << "] + row)) : 0ull;\n";
+      } else {
+        o << ind << b << " = inr ? (u64)" << (emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c]))
+          << "(a.in_data[" << c << "], a.in_off[" << c << "] + row) : 0ull;\n";
+      }
       if (p_.nullable[c]) o << ind << v << " = inr && gx_valid(a.in_mask[" << c << "], a.in_off[" << c << "] + row);\n";
       else o << ind << v << " = inr;\n";
       return;
@@ -554,7 +563,10 @@ class Gen {
     o << ind << "bool alive[GX_V];\n";
     o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) alive[k] = (w0 + k) * 32 + lane < a.n;\n";
     if (cfg_.runtime_order) {
-      emit_predicate_runtime_order(o, ind);
+      if (cfg_.stream_slots > 0 && streamable())
+        emit_predicate_stream(o, ind);
+      else
+        emit_predicate_runtime_order(o, ind);
       return;
     }
     std::set<int> done;
@@ -614,6 +626,106 @@ class Gen {
     o << ind << "  }\n";
     o << ind << "  if (any_ == 0u) break;\n";
     o << ind << "}\n";
+  }
+
+  // every conjunct reads exactly one column (or none)
+  bool streamable() const {
+    for (size_t c = 0; c < p_.conjuncts.size(); c++)
+      if (conjunct_columns(p_, (int)c).size() > 1) return false;
+    return true;
+  }
+
+  // Streaming short-circuit in the launch order: the warp keeps S word slots in
+  // flight, each at its own conjunct step; a slot whose word has no live row
+  // left, or has passed every conjunct, takes the warp's next word.  Each round
+  // issues the loads of every slot before evaluating any, so the warp always has
+  // S words' loads outstanding instead of a shrinking lockstep set, and the
+  // number of dependent load rounds is about (words x steps per word) / S
+  // rather than the longest chain per group of words.  Word masks live in shared
+  // memory (indexed by a slot's word).
+  void emit_predicate_stream(std::ostringstream& o, const std::string& ind) const {
+    const int nc = (int)p_.conjuncts.size();
+    const int S = cfg_.stream_slots;
+    std::vector<int> col_of(nc, -1);
+    for (int c = 0; c < nc; c++) {
+      const std::vector<int> cols = conjunct_columns(p_, c);
+      if (!cols.empty()) col_of[c] = cols[0];
+    }
+    const std::string S_ = std::to_string(S);
+    o << ind << "__shared__ u32 s_aw_[GX_WARPS][GX_V];\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
+    o << ind << "  const u32 m_ = __ballot_sync(GX_FULL, alive[k]);\n";
+    o << ind << "  if (lane == 0) s_aw_[warp][k] = m_;\n";
+    o << ind << "}\n";
+    o << ind << "__syncwarp();\n";
+    o << ind << "int sw_[" << S_ << "], sj_[" << S_ << "]; u64 val_[" << S_ << "]; bool vv_[" << S_ << "];\n";
+    o << ind << "int nx_ = 0;\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int q = 0; q < " << S_ << "; q++) {\n";
+    o << ind << "  sw_[q] = -1; sj_[q] = 0; val_[q] = 0ull; vv_[q] = false;\n";
+    o << ind << "  while (nx_ < GX_V && s_aw_[warp][nx_] == 0u) nx_++;\n";
+    o << ind << "  if (nx_ < GX_V) { sw_[q] = nx_; nx_++; }\n";
+    o << ind << "}\n";
+    o << ind << "while (true) {\n";
+    o << ind << "  bool act_ = false;\n";
+    o << ind << "  #pragma unroll\n" << ind << "  for (int q = 0; q < " << S_ << "; q++) act_ |= sw_[q] >= 0;\n";
+    o << ind << "  if (!act_) break;\n";
+    // loads of every slot
+    o << ind << "  #pragma unroll\n" << ind << "  for (int q = 0; q < " << S_ << "; q++) {\n";
+    o << ind << "    if (sw_[q] < 0) continue;\n";
+    o << ind << "    const int wk_ = sw_[q];\n";
+    o << ind << "    const i64 row = (w0 + wk_) * 32 + lane;\n";
+    o << ind << "    const bool inr = ((s_aw_[warp][wk_] >> lane) & 1u) != 0u;\n";
+    o << ind << "    switch (a.order_dev ? __ldg(a.order_dev + sj_[q]) : a.order[sj_[q]]) {\n";
+    for (int c = 0; c < nc; c++) {
+      const int col = col_of[c];
+      if (col < 0) continue;
+      const std::string gfn = emu() ? load_fn_emu(p_.schema[col]) : load_fn(p_.schema[col]);
+      o << ind << "      case " << c << ": val_[q] = inr ? (u64)" << gfn << "(a.in_data[" << col << "], a.in_off[" << col
+        << "] + row) : 0ull; vv_[q] = inr" << (p_.nullable[col] ? " && gx_valid(a.in_mask[" + std::to_string(col) +
+                                                                      "], a.in_off[" + std::to_string(col) + "] + row)"
+                                                                : std::string())
+        << "; break;\n";
+    }
+    o << ind << "      default: break;\n    }\n";
+    o << ind << "  }\n";
+    // evaluation, mask update, refill
+    o << ind << "  #pragma unroll\n" << ind << "  for (int q = 0; q < " << S_ << "; q++) {\n";
+    o << ind << "    if (sw_[q] < 0) continue;\n";
+    o << ind << "    const int wk_ = sw_[q];\n";
+    o << ind << "    const i64 row = (w0 + wk_) * 32 + lane; (void)row;\n";
+    o << ind << "    const bool inr = ((s_aw_[warp][wk_] >> lane) & 1u) != 0u;\n";
+    o << ind << "    const int k = 0;\n";
+    o << ind << "    bool keep_ = false;\n";
+    o << ind << "    switch (a.order_dev ? __ldg(a.order_dev + sj_[q]) : a.order[sj_[q]]) {\n";
+    for (int c = 0; c < nc; c++) {
+      const int cid = p_.conjuncts[c];
+      o << ind << "      case " << c << ": {\n";
+      const std::vector<int> ids = cone({cid});
+      for (int id : ids) o << ind << "        u64 b" << id << "[1]; bool v" << id << "[1];\n";
+      for (int id : ids) {
+        if (p_.nodes[id].kind == Node::COL)
+          o << ind << "        b" << id << "[0] = val_[q]; v" << id << "[0] = vv_[q];\n";
+      }
+      for (int id : ids)
+        if (p_.nodes[id].kind != Node::COL) emit_node(o, id, ind + "        ");
+      o << ind << "        keep_ = " << conj_keep(cid) << ";\n";
+      o << ind << "        break; }\n";
+    }
+    o << ind << "      default: break;\n    }\n";
+    o << ind << "    const u32 m_ = s_aw_[warp][wk_] & __ballot_sync(GX_FULL, inr && keep_);\n";
+    o << ind << "    __syncwarp();\n";
+    o << ind << "    if (lane == 0) s_aw_[warp][wk_] = m_;\n";
+    o << ind << "    __syncwarp();\n";
+    o << ind << "    sj_[q]++;\n";
+    o << ind << "    if (m_ == 0u || sj_[q] >= " << nc << ") {\n";
+    o << ind << "      sw_[q] = -1; sj_[q] = 0;\n";
+    o << ind << "      while (nx_ < GX_V && s_aw_[warp][nx_] == 0u) nx_++;\n";
+    o << ind << "      if (nx_ < GX_V) { sw_[q] = nx_; nx_++; }\n";
+    o << ind << "    }\n";
+    o << ind << "  }\n";
+    o << ind << "}\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) alive[k] = ((s_aw_[warp][k] >> lane) & 1u) != 0u;\n";
+    o << ind << "__syncwarp();\n";  // s_aw_ is rewritten by the warp's next tile
   }
 
   // per-conjunct pass counts of this warp's rows, accumulated in shared memory
@@ -735,6 +847,8 @@ class Gen {
 
   const Plan& p_;
   const KernelConfig& cfg_;
+  // columns read from a shared-memory staging buffer: col -> (buffer, index)
+  mutable std::map<int, std::pair<std::string, std::string>> staged_;
 };
 
 void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
@@ -1123,12 +1237,300 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "}\n";
 }
 
+// Staged short-circuit filter (runtime conjunct order, dense projections).
+// Each block keeps GX_D tiles in flight.  A tile's conjuncts are evaluated one
+// at a time in the launch order; before each step, warp 0 copies the 32-row
+// words of that conjunct's columns that still have a live row into the tile's
+// shared-memory slot with asynchronous copies (completion on the slot's
+// mbarrier) and the block moves on to the next slot, so the copies of several
+// tiles are in flight while it evaluates one.  (Bulk copies of one 256-byte
+// word each were measured an order of magnitude slower than 16-byte
+// asynchronous copies spread over the warp: small bulk copies serialise.)  A tile whose rows are all dead, or that has
+// passed every conjunct, publishes its aggregate at once; tiles are resolved
+// (look-back) and written in claim order, so a block never waits on one of its
+// own unpublished tiles.  A partial last word is read from global memory
+// directly.  Every column a conjunct reads must start on a 16-byte boundary
+// (the host checks and otherwise runs the unstaged kernel).
+void emit_staged_filter(std::ostringstream& o, const Gen& g, const Plan& p, const std::string& name) {
+  const int nc = (int)p.conjuncts.size();
+  std::vector<std::vector<int>> cc(nc);
+  std::vector<std::vector<int>> coff(nc);  // byte offset of each column's region in a slot, per word
+  std::vector<int> cwb(nc, 0);             // bytes per word of all the conjunct's columns
+  int wbmax = 16;
+  for (int c = 0; c < nc; c++) {
+    cc[c] = conjunct_columns(p, c);
+    for (int col : cc[c]) {
+      coff[c].push_back(cwb[c]);
+      cwb[c] += 32 * type_size(p.schema[col]);
+    }
+    wbmax = std::max(wbmax, cwb[c]);
+  }
+  o << "#define GX_T (GX_WARPS * GX_V)\n#define GX_D 4\n";
+  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name << "(const GxArgs a) {\n";
+  o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
+  o << "  const i64 nwords = (a.n + 31) >> 5;\n";
+  o << "  const i64 ntiles = (nwords + GX_T - 1) / GX_T;\n";
+  // slot layout for conjunct c: column i's words at GX_T * coff[c][i] + kw * 32 * w
+  o << "  __shared__ __align__(128) unsigned char s_buf[GX_D][GX_T * " << wbmax << "];\n";
+  o << "  __shared__ __align__(8) u64 s_bar[GX_D];\n";
+  o << "  __shared__ long long s_tile[GX_D];\n";
+  o << "  __shared__ int s_step[GX_D], s_done[GX_D], s_pend[GX_D], s_seq[GX_D];\n";
+  o << "  __shared__ u32 s_par[GX_D];\n";
+  o << "  __shared__ u32 s_alive[GX_D][GX_T];\n";
+  o << "  __shared__ u32 s_cnt[GX_WARPS];\n";
+  o << "  __shared__ u64 s_off[GX_D][GX_WARPS];\n";
+  o << "  __shared__ u64 s_total[GX_D];\n";
+  o << "  __shared__ u64 s_base;\n";
+  o << "  __shared__ int s_cseq, s_rseq, s_abort, s_ready;\n";
+  o << "  __shared__ long long s_lbpred;\n";   // look-back progress of the oldest tile
+  o << "  __shared__ u64 s_lbexcl;\n";
+  o << "  __shared__ u32 s_lbpolls;\n";
+  o << "  const u32 spin_limit = 1u << 22;\n";
+  o << "  const u32 mbar_limit = 1u << 20;  // polls of a slot's barrier (each try_wait may suspend briefly)\n";
+
+  // warp 0: copies of conjunct order[step]'s live full words of slot s, as
+  // 16-byte asynchronous copies spread over the warp's lanes; every lane then
+  // arrives on the slot's barrier when its copies have landed (32 arrivals)
+  o << "  auto issue_ = [&](int s, long long tile, int step) {\n";
+  o << "    const int cj = a.order_dev ? __ldg(a.order_dev + step) : a.order[step];\n";
+  o << "    int nwt_ = 0;\n";
+  o << "    for (int kb = 0; kb < GX_T; kb += 32) {\n";
+  o << "      const int kw = kb + lane;\n";
+  o << "      const i64 wd = tile * GX_T + kw;\n";
+  o << "      nwt_ += __popc(__ballot_sync(GX_FULL, kw < GX_T && s_alive[s][kw] != 0u && (wd + 1) * 32 <= a.n));\n";
+  o << "    }\n";
+  o << "    if (lane == 0) s_pend[s] = nwt_ != 0 ? 1 : 0;\n";
+  o << "    if (nwt_ == 0) return;\n";
+  o << "    gx_fence_async_smem();\n";
+  o << "    for (int kb = 0; kb < GX_T; kb += 32) {\n";
+  o << "      const int kwl = kb + lane;\n";
+  o << "      const u32 wm_ = __ballot_sync(GX_FULL, kwl < GX_T && s_alive[s][kwl] != 0u && (tile * GX_T + kwl + 1) * 32 <= a.n);\n";
+  o << "      const int nw_ = __popc(wm_);\n";
+  o << "      switch (cj) {\n";
+  for (int c = 0; c < nc; c++) {
+    const int ch = cwb[c] / 16;  // 16-byte chunks per word, all the conjunct's columns
+    o << "        case " << c << ":\n";
+    o << "          for (int q = lane; q < nw_ * " << ch << "; q += 32) {\n";
+    o << "            const int kw = kb + (int)__fns(wm_, 0u, q / " << ch << " + 1);\n";
+    o << "            const int ck = q % " << ch << ";\n";
+    o << "            const i64 wd = tile * GX_T + kw;\n";
+    int chk = 0;
+    for (size_t i = 0; i < cc[c].size(); i++) {
+      const int col = cc[c][i];
+      const int w = type_size(p.schema[col]);
+      const int cn = 2 * w;  // chunks of this column per word (32 * w / 16)
+      o << "            " << (i ? "else " : "") << "if (ck < " << chk + cn << ") gx_cp16(s_buf[s] + GX_T * " << coff[c][i]
+        << " + kw * " << 32 * w << " + (ck - " << chk << ") * 16, (const char*)a.in_data[" << col << "] + (a.in_off["
+        << col << "] + wd * 32) * " << w << " + (ck - " << chk << ") * 16);\n";
+      chk += cn;
+    }
+    o << "          }\n";
+    o << "          break;\n";
+  }
+  o << "        default: break;\n      }\n    }\n";
+  o << "    gx_cp_arrive(&s_bar[s]);\n";
+  o << "  };\n";
+
+  // thread 0: claim the next tile into slot s; returns whether one was claimed
+  o << "  auto claim_ = [&](int s) {\n";
+  o << "    const long long t = (long long)atomicAdd(a.tile_counter, 1ull);\n";
+  o << "    if (t >= ntiles) { s_tile[s] = -1; return; }\n";
+  o << "    s_tile[s] = t; s_step[s] = 0; s_done[s] = 0; s_pend[s] = 0; s_seq[s] = s_cseq++;\n";
+  o << "  };\n";
+  // warp 0: alive masks of a newly claimed tile (rows < n)
+  o << "  auto init_alive_ = [&](int s, long long tile) {\n";
+  o << "    for (int kw = lane; kw < GX_T; kw += 32) {\n";
+  o << "      const i64 r0 = (tile * GX_T + kw) * 32;\n";
+  o << "      const i64 left = a.n - r0;\n";
+  o << "      s_alive[s][kw] = left >= 32 ? 0xffffffffu : (left <= 0 ? 0u : ((1u << left) - 1u));\n";
+  o << "    }\n";
+  o << "    __syncwarp();\n";
+  o << "  };\n";
+
+  // setup: barriers and the first GX_D tiles
+  o << "  if (threadIdx.x == 0) {\n";
+  o << "    s_cseq = 0; s_rseq = 0; s_abort = 0;\n";
+  o << "    for (int s = 0; s < GX_D; s++) { gx_mbar_init(&s_bar[s], 32u); s_par[s] = 0u; }\n";
+  o << "    gx_mbar_init_fence();\n";
+  o << "    for (int s = 0; s < GX_D; s++) claim_(s);\n";
+  o << "  }\n";
+  o << "  __syncthreads();\n";
+  o << "  if (warp == 0) {\n";
+  o << "    for (int s = 0; s < GX_D; s++) {\n";
+  o << "      const long long t = s_tile[s];\n";
+  o << "      if (t < 0) continue;\n";
+  o << "      init_alive_(s, t);\n";
+  o << "      issue_(s, t, 0);\n";
+  o << "    }\n";
+  o << "  }\n";
+
+  o << "  while (true) {\n";
+  o << "    __syncthreads();\n";
+  o << "    bool any_ = false;\n";
+  o << "    #pragma unroll\n    for (int s = 0; s < GX_D; s++) any_ |= s_tile[s] >= 0;\n";
+  o << "    if (!any_ || s_abort) break;\n";
+  o << "    for (int s = 0; s < GX_D; s++) {\n";
+  o << "      __syncthreads();\n";
+  o << "      const long long tile = s_tile[s];\n";
+  o << "      if (tile < 0) continue;\n";
+  // ---- one conjunct step
+  o << "      if (s_done[s] == 0) {\n";
+  o << "        if (s_pend[s]) {\n";
+  o << "          const u32 par_ = s_par[s];\n";
+  o << "          u32 sp_ = 0u;\n";
+  o << "          while (!gx_mbar_try_wait(&s_bar[s], par_)) {\n";
+  o << "            if (++sp_ > mbar_limit) { atomicExch(a.err, 1); s_abort = 1; break; }\n";
+  o << "            __nanosleep(20);\n";
+  o << "          }\n";
+  o << "        }\n";
+  o << "        const int cj = a.order_dev ? __ldg(a.order_dev + s_step[s]) : a.order[s_step[s]];\n";
+  o << "        bool keep_[GX_V];\n";
+  o << "        bool inr_[GX_V];\n";
+  o << "        switch (cj) {\n";
+  for (int c = 0; c < nc; c++) {
+    const int cid = p.conjuncts[c];
+    o << "          case " << c << ": {\n";
+    g.staged_.clear();
+    for (size_t i = 0; i < cc[c].size(); i++)
+      g.staged_[cc[c][i]] = {"(const void*)(s_buf[s] + GX_T * " + std::to_string(coff[c][i]) + ")",
+                             "(i64)(kw * 32 + lane)"};
+    const std::vector<int> ids = g.cone({cid});
+    g.decl(o, ids, "            ");
+    o << "            #pragma unroll\n            for (int k = 0; k < GX_V; k++) {\n";
+    o << "              const int kw = warp * GX_V + k;\n";
+    o << "              const i64 row = (tile * GX_T + kw) * 32 + lane;\n";
+    o << "              const bool full_word_ = (tile * GX_T + kw + 1) * 32 <= a.n; (void)full_word_;\n";
+    o << "              const bool inr = ((s_alive[s][kw] >> lane) & 1u) != 0u;\n";
+    for (int id : ids)
+      if (p.nodes[id].kind == Node::COL) g.emit_node(o, id, "              ");
+    for (int id : ids)
+      if (p.nodes[id].kind != Node::COL) g.emit_node(o, id, "              ");
+    o << "              keep_[k] = " << g.conj_keep(cid) << "; inr_[k] = inr;\n";
+    o << "            }\n";
+    o << "            break; }\n";
+  }
+  g.staged_.clear();
+  o << "          default:\n";
+  o << "            #pragma unroll\n            for (int k = 0; k < GX_V; k++) { keep_[k] = false; inr_[k] = false; }\n";
+  o << "        }\n";
+  o << "        #pragma unroll\n        for (int k = 0; k < GX_V; k++) {\n";
+  o << "          const u32 nb_ = __ballot_sync(GX_FULL, inr_[k] && keep_[k]);\n";
+  o << "          if (lane == 0) s_alive[s][warp * GX_V + k] &= nb_;\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  // warp 0: next step or done
+  o << "        if (warp == 0) {\n";
+  o << "          if (lane == 0) { if (s_pend[s]) s_par[s] ^= 1u; s_step[s] += 1; }\n";
+  o << "          __syncwarp();\n";
+  o << "          u32 live_ = 0u;\n";
+  o << "          for (int kw = lane; kw < GX_T; kw += 32) live_ |= s_alive[s][kw];\n";
+  o << "          const bool anyl_ = __any_sync(GX_FULL, live_ != 0u);\n";
+  o << "          if (!anyl_ || s_step[s] >= " << nc << ") {\n";
+  o << "            if (lane == 0) { s_done[s] = 1; s_pend[s] = 0; }\n";
+  o << "          } else {\n";
+  o << "            issue_(s, tile, s_step[s]);\n";
+  o << "          }\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  o << "      }\n";
+  // ---- publish the aggregate of a finished tile
+  o << "      if (s_done[s] == 1) {\n";
+  o << "        u32 c_ = 0u;\n";
+  o << "        #pragma unroll\n        for (int k = 0; k < GX_V; k++) c_ += __popc(s_alive[s][warp * GX_V + k]);\n";
+  o << "        if (lane == 0) s_cnt[warp] = c_;\n";
+  o << "        __syncthreads();\n";
+  o << "        if (warp == 0) {\n";
+  o << "          const u64 tot_ = gx_tile_publish(a.tile_status, tile, s_cnt, s_off[s], GX_WARPS);\n";
+  o << "          if (lane == 0) { s_total[s] = tot_; s_done[s] = 2; }\n";
+  o << "          if (lane == 0 && s_seq[s] == s_rseq) { s_lbpred = tile - 1; s_lbexcl = 0ull; s_lbpolls = 0u; }\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  o << "      }\n";
+  // ---- resolve and write, in claim order
+  // the oldest tile's look-back is polled, never waited on: while predecessors
+  // are missing the block goes on with its other tiles, whose aggregates other
+  // blocks may be waiting for
+  o << "      if (s_done[s] == 2 && s_seq[s] == s_rseq) {\n";
+  o << "        if (warp == 0) {\n";
+  o << "          long long pr_ = s_lbpred; u64 ex_ = s_lbexcl;\n";
+  o << "          const bool ok_ = gx_lookback_poll(a.tile_status, tile, s_total[s], &pr_, &ex_);\n";
+  o << "          if (lane == 0) {\n";
+  o << "            s_lbpred = pr_; s_lbexcl = ex_; s_ready = ok_ ? 1 : 0;\n";
+  o << "            if (ok_) {\n";
+  o << "              s_base = ex_;\n";
+  o << "              if (tile == ntiles - 1) *a.out_count = ex_ + s_total[s];\n";
+  o << "            } else if (++s_lbpolls > spin_limit) {\n";
+  o << "              atomicExch(a.err, 1); s_abort = 1;\n";
+  o << "            } else {\n";
+  o << "              __nanosleep(64);\n";
+  o << "            }\n";
+  o << "          }\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  o << "        if (!s_ready) continue;\n";
+  o << "        {\n";
+  o << "          u32 bal[GX_V]; u32 wcnt = 0u;\n";
+  o << "          #pragma unroll\n          for (int k = 0; k < GX_V; k++) { bal[k] = s_alive[s][warp * GX_V + k]; wcnt += __popc(bal[k]); }\n";
+  o << "          if (wcnt != 0u) {\n";
+  o << "            u64 pos = s_base + s_off[s][warp];\n";
+  o << "            const i64 w0 = tile * GX_T + (i64)warp * GX_V;\n";
+  emit_filter_writes_dense(o, g, p, "            ");
+  o << "          }\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  o << "        if (threadIdx.x == 0) {\n";
+  o << "          s_rseq++;\n";
+  o << "          claim_(s);\n";
+  o << "          for (int q = 0; q < GX_D; q++)  // the next oldest, if already published\n";
+  o << "            if (s_tile[q] >= 0 && s_done[q] == 2 && s_seq[q] == s_rseq) { s_lbpred = s_tile[q] - 1; s_lbexcl = 0ull; s_lbpolls = 0u; }\n";
+  o << "        }\n";
+  o << "        __syncthreads();\n";
+  o << "        if (warp == 0 && s_tile[s] >= 0) {\n";
+  o << "          init_alive_(s, s_tile[s]);\n";
+  o << "          issue_(s, s_tile[s], 0);\n";
+  o << "        }\n";
+  o << "      }\n";
+  o << "    }\n";
+  o << "  }\n";
+  // an abandoned run (a wait gave up): let copies still in flight land before exit
+  o << "  __syncthreads();\n";
+  o << "  if (s_abort && threadIdx.x == 0) {\n";
+  o << "    for (int s = 0; s < GX_D; s++) {\n";
+  o << "      if (s_tile[s] < 0 || !s_pend[s] || s_done[s] != 0) continue;\n";
+  o << "      u32 sp_ = 0u;\n";
+  o << "      while (!gx_mbar_try_wait(&s_bar[s], s_par[s]) && ++sp_ < mbar_limit) __nanosleep(20);\n";
+  o << "    }\n";
+  o << "  }\n";
+  o << "}\n";
+}
+
 }  // namespace
+
+std::vector<int> conjunct_columns(const Plan& p, int c) {
+  std::set<int> cols;
+  std::function<void(int)> go = [&](int id) {
+    if (id < 0) return;
+    const Node& n = p.nodes[id];
+    if (n.kind == Node::COL) cols.insert(n.col);
+    if (n.kind == Node::OP) { go(n.a); go(n.b); }
+  };
+  go(p.conjuncts.at(c));
+  return std::vector<int>(cols.begin(), cols.end());
+}
 
 std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg, const std::string& name) {
   Gen g(p, cfg);
   std::ostringstream o;
   emit_prelude(o, cfg);
+  if (kind == KernelKind::FUSED_STAGED) {
+    if (!p.has_filter() || p.conjuncts.size() > 16) fail(GX_ERR_INVALID, "the staged kernel runs filters of at most 16 conjuncts");
+    KernelConfig c = cfg;
+    c.dense = true;
+    c.runtime_order = true;
+    Gen gs(p, c);
+    emit_staged_filter(o, gs, p, name);
+    return o.str();
+  }
   if (kind == KernelKind::FUSED_BATCHED) {
     if (!p.has_filter()) fail(GX_ERR_INVALID, "the batched kernel runs filter plans");
     if (cfg.runtime_order || cfg.short_circuit) fail(GX_ERR_INVALID, "the batched kernel evaluates conjuncts in plan order");

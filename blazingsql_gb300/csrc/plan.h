@@ -52,6 +52,8 @@ struct KernelConfig {
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
   bool lazy_case = true;     // dense phase: expensive CASE branches only for the rows that select them
   bool runtime_order = false;  // short-circuit AND conjuncts in the order given at launch (KernelArgs::order)
+  bool staged = false;         // runtime_order: stage conjunct columns in shared memory by bulk copies
+  int stream_slots = 0;        // runtime_order: words in flight per warp, refilled as words finish (0: lockstep)
   bool conj_stats = false;     // COUNT_FILTER also counts each conjunct's passing rows
   bool short_circuit = false;
   std::vector<int> conjunct_order;  // indices into Plan::conjuncts
@@ -85,7 +87,7 @@ Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullabl
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
 constexpr int GX_OUTPUTS_PER_KERNEL = 32;
 
-enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED };
+enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED, FUSED_STAGED };
 
 // Header of a batch table run by the FUSED_BATCHED kernel (device memory).
 struct BatchHeader {
@@ -94,6 +96,9 @@ struct BatchHeader {
   int nbatch;
   int pad;
 };
+
+// Distinct columns read by conjunct c (index into Plan::conjuncts), ascending.
+std::vector<int> conjunct_columns(const Plan& plan, int c);
 
 // CUDA source of one plan kernel.  The kernel is named by `name`.
 std::string generate_kernel(const Plan& plan, KernelKind kind, const KernelConfig& cfg, const std::string& name);

@@ -345,6 +345,7 @@ static const char* kind_name(KernelKind k) {
     case KernelKind::FUSED_FILTER: return "gx_filter_fused";
     case KernelKind::COUNT_FILTER: return "gx_filter_count";
     case KernelKind::FUSED_BATCHED: return "gx_filter_batched";
+    case KernelKind::FUSED_STAGED: return "gx_filter_staged";
     default: return "gx_filter_write";
   }
 }
@@ -400,6 +401,16 @@ static std::vector<bool> runtime_nullable(const Plan& p, const std::vector<Colum
   for (size_t i = 0; i < cols.size(); i++) nb[i] = cols[i].mask != nullptr;
   (void)p;
   return nb;
+}
+
+// bulk copies need every column a conjunct reads to start on a 16-byte boundary
+static bool staging_aligned(const Plan& p, const std::vector<ColumnView>& cols) {
+  for (size_t c = 0; c < p.conjuncts.size(); c++)
+    for (int col : conjunct_columns(p, (int)c)) {
+      const uintptr_t start = (uintptr_t)cols[col].data + (uintptr_t)(cols[col].offset * type_size(cols[col].type));
+      if (start % 16 != 0) return false;
+    }
+  return true;
 }
 
 static void launch(const JitKernel& k, int grid, cudaStream_t s, KernelArgs& args, bool timed = false) {
@@ -585,7 +596,9 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       a.out_mask[j] = out[j].null_mask;
     }
     a.capacity = capacity;
-    const JitKernel k = kernel(two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER, nb);
+    KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER;
+    if (!two_pass && cfg_.staged && cfg_.runtime_order && staging_aligned(plan_, cols)) kind = KernelKind::FUSED_STAGED;
+    const JitKernel k = kernel(kind, nb);
     int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
     if (grid > ntiles) grid = ntiles;
     last.grid = (int)grid;

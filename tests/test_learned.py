@@ -160,6 +160,49 @@ def test_learned_matches_plain_and_oracle(size_outputs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("offset,variant", [(0, "GX_STAGED"), (1, "GX_STAGED"), (2, "GX_STAGED"), (33, "GX_STAGED"),
+                                            (0, "GX_STREAM"), (33, "GX_STREAM")])
+def test_staged_single_pass_matches_plain(offset, variant, monkeypatch):
+    """The single-pass variants a learner can be asked for return the plain
+    path's rows: shared-memory staging of the conjunct columns (GX_STAGED=1,
+    used when the columns start on 16-byte boundaries; offset 1 or 33 of an
+    8-byte column runs the unstaged kernel) and streaming word slots
+    (GX_STREAM=8); ragged sizes, nulls and a column offset included."""
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    rng = np.random.default_rng(21 + offset)
+    schema = [T.INT64, T.FLOAT64, T.INT32, T.INT64]
+    cond = "AND(>($0, 500), <($1, 0.25), =(MOD($2, 3), 1), IS NOT NULL($3))"
+    plan = g.Plan(schema, cond, ["$0", "$1", "$2", "+($3, 1)"], words_per_warp=8)
+    monkeypatch.setenv(variant, "1" if variant == "GX_STAGED" else "8")
+    textual = g.Learner(plan, policy=g.GX_LEARN_POLICY_TEXTUAL, fast_words_per_warp=8)
+    learned = g.Learner(plan, warmup_batches=2, relabel_every=0, size_outputs=0, fast_words_per_warp=8)
+    monkeypatch.delenv(variant)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    for n in (1, 31, 33, 1000, 1023, 1024 * 9 + 17, 100_000):
+        total = n + offset
+        x0 = rng.integers(0, 1000, total).astype(np.int64)
+        x1 = rng.random(total)
+        x2 = rng.integers(-50, 50, total).astype(np.int32)
+        x3 = rng.integers(0, 10, total).astype(np.int64)
+        v2 = rng.random(total) > 0.1
+        v3 = rng.random(total) > 0.2
+        cols = [g.HostColumn(T.INT64, x0), g.HostColumn(T.FLOAT64, x1),
+                g.HostColumn(T.INT32, x2, g.pack_validity(v2)), g.HostColumn(T.INT64, x3, g.pack_validity(v3))]
+        dev = [DeviceColumn.from_host(c) for c in cols]
+        for d in dev:
+            d.offset, d.size = offset, n
+        exp, erows, _ = plain.execute(dev)
+        for b in range(3):  # learned: two labelled batches, then single passes
+            got, rows, info = learned.execute(dev)
+            assert rows == erows
+            assert_tables_equal(_host(got), _host(exp), what=f"learned n={n} off={offset} batch {b}")
+        got, rows, _ = textual.execute(dev)
+        assert rows == erows
+        assert_tables_equal(_host(got), _host(exp), what=f"textual n={n} off={offset}")
+
+
+@pytest.mark.gpu
 def test_learned_misprediction_reruns():
     """With no capacity margin the predicted output size is often too small; the
     single pass re-runs with the exact count and the result still matches."""
