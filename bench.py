@@ -296,7 +296,11 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+        if pol == N.GX_LEARN_POLICY_LEARNED:
+            lr.prepare(data[0], stream=stream)
         for b in range(batches):
+            if pol == N.GX_LEARN_POLICY_LEARNED and b + 1 < batches:
+                lr.prepare(data[b + 1], stream=stream)  # look-ahead: next batch's prediction
             cols, r, info = lr.execute(data[b], stream=stream)
             rows_out.append(r)
             infos.append(info)

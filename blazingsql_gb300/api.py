@@ -436,6 +436,13 @@ class Learner:
                                            C.byref(self._st)), self._st)
         return _wrap(outs, n, s), self._rows.value, _BatchReport(info)
 
+    def prepare(self, table: Table, stream=None) -> None:
+        """Look-ahead: compute the prediction of a batch a later execute() gets."""
+        keep: list = []
+        views, nc = _views(table, keep)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_learner_prepare(self._h, views, nc, _stream_handle(stream), C.byref(st)), st)
+
     def features(self, table: Table, stream=None):
         """The sketch features of one batch and the per-column anchors
         (gx_debug_learner_features)."""

@@ -608,23 +608,34 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     dmom_ = dgrad_ + nparams_;
     dvel_ = dmom_ + nparams_;
     dinfer_ = dvel_ + nparams_;
-    dfeat_ = (float*)must_alloc((size_t)F_ * 4 * (1 + kTrainRing));
-    dtrainX_ = dfeat_ + F_;
+    dtrainX_ = (float*)must_alloc((size_t)F_ * 4 * kTrainRing);
+    // prediction slots: features, z, order, partials, ticket (each part 16-float aligned)
+    const size_t fpart = ((size_t)F_ + 15) / 16 * 16;
+    const size_t ppart = (size_t)kPartial * kMaxSketchCols * kSketchParts;
+    const size_t per = fpart + 16 + 16 + ppart + 16;
+    dslots_ = (float*)must_alloc(4 * per * kPredSlots);
+    for (int q = 0; q < kPredSlots; q++) {
+      float* b = dslots_ + per * q;
+      slots_[q].feat = b;
+      slots_[q].z = b + fpart;
+      slots_[q].order = (int*)(b + fpart + 16);
+      slots_[q].partial = b + fpart + 32;
+      slots_[q].ticket = (unsigned int*)(b + fpart + 32 + ppart);
+    }
     dtrainY_ = (float*)must_alloc((size_t)O_ * 4 * kTrainRing);
     dsnapX_ = (float*)must_alloc((size_t)(F_ + O_) * 4 * kTrainRing);
     dsnapY_ = dsnapX_ + (size_t)F_ * kTrainRing;
     dact_ = (float*)must_alloc((size_t)4 * (2 * kTrainRing * H_ + kTrainRing * O_ + 4));
-    dact_inf_ = (float*)must_alloc((size_t)4 * (2 * H_ + O_ + 4));
-    dpartial_ = (float*)must_alloc((size_t)4 * kPartial * kMaxSketchCols * kSketchParts);
     dcounts_ = (unsigned long long*)must_alloc(8 * 16);
-    dticket_ = (unsigned int*)must_alloc(16);
-    dcost_ = (float*)must_alloc(4 * 16 + 4 * 16);
-    dorder_ = (int*)(dcost_ + 16);
+    dcost_ = (float*)must_alloc(4 * 16);
     // pinned host block: predictions z[16], the loss at [16], conjunct counts from byte 256
     check_cuda(cudaMallocHost(&hpinned_, 512), "pinned host buffer");
     hcounts_ = (unsigned long long*)((char*)hpinned_ + 256);
     check_cuda(cudaStreamCreateWithFlags(&aux_stream_, cudaStreamNonBlocking), "aux stream");
     check_cuda(cudaEventCreateWithFlags(&pred_ready_, cudaEventDisableTiming), "event");
+    check_cuda(cudaEventCreateWithFlags(&prep_in_, cudaEventDisableTiming), "event");
+    for (int q = 0; q < kPredSlots; q++)
+      check_cuda(cudaEventCreateWithFlags(&slots_[q].ready, cudaEventDisableTiming), "event");
     if (opt_.async_training) {
       check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
       check_cuda(cudaEventCreateWithFlags(&train_done_, cudaEventDisableTiming), "event");
@@ -653,7 +664,7 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     check_cuda(cudaMemcpy(dparams_, init.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "init params");
     check_cuda(cudaMemcpy(dinfer_, init.data(), (size_t)nparams_ * 4, cudaMemcpyHostToDevice), "init params");
     check_cuda(cudaMemset(dmom_, 0, (size_t)nparams_ * 8), "init adam");
-    check_cuda(cudaMemset(dticket_, 0, 16), "init ticket");
+    check_cuda(cudaMemset(dslots_, 0, 4 * (slots_[1].feat - slots_[0].feat) * kPredSlots), "init slots");
     std::vector<float> cost(16, 0.f);
     for (int c = 0; c < nconj_; c++) cost[c] = (float)conj_cost_[c];
     check_cuda(cudaMemcpy(dcost_, cost.data(), 4 * 16, cudaMemcpyHostToDevice), "init costs");
@@ -666,14 +677,12 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
 void Learner::release() {
   if (train_stream_) cudaStreamSynchronize(train_stream_);
   cudaFree(dparams_);
-  cudaFree(dfeat_);
+  cudaFree(dtrainX_);
+  cudaFree(dslots_);
   cudaFree(dtrainY_);
   cudaFree(dsnapX_);
   cudaFree(dact_);
-  cudaFree(dact_inf_);
-  cudaFree(dpartial_);
   cudaFree(dcounts_);
-  cudaFree(dticket_);
   cudaFree(dcost_);
   if (hpinned_) cudaFreeHost(hpinned_);
   if (train_done_) cudaEventDestroy(train_done_);
@@ -683,18 +692,23 @@ void Learner::release() {
   if (aux_stream_) cudaStreamDestroy(aux_stream_);
   pred_ready_ = nullptr;
   aux_stream_ = nullptr;
-  dparams_ = dfeat_ = dtrainY_ = dact_ = dact_inf_ = dpartial_ = hpinned_ = dsnapX_ = dsnapY_ = nullptr;
+  for (int q = 0; q < kPredSlots; q++) {
+    if (slots_[q].ready) cudaEventDestroy(slots_[q].ready);
+    slots_[q] = PredSlot{};
+  }
+  if (prep_in_) cudaEventDestroy(prep_in_);
+  prep_in_ = nullptr;
+  dparams_ = dtrainX_ = dtrainY_ = dact_ = hpinned_ = dsnapX_ = dsnapY_ = dslots_ = nullptr;
   dcounts_ = nullptr;
-  dticket_ = nullptr;
   dcost_ = nullptr;
-  dorder_ = nullptr;
   train_done_ = labels_ready_ = nullptr;
   train_stream_ = nullptr;
 }
 
 Learner::~Learner() { release(); }
 
-void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s) {
+void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot) {
+  PredSlot& ps = slots_[slot];
   SketchCols c{};
   for (int i = 0; i < ncols_; i++) {
     c.data[i] = cols[i].data;
@@ -710,21 +724,64 @@ void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStre
   const size_t wbytes = (size_t)nparams_ * 4;
   const bool stage_w = predict && wbytes <= 48 * 1024;
   k_sketch_predict<<<grid, 256, stage_w ? wbytes : 0, s>>>(
-      c, n, opt_.stride_words, ncols_, dpartial_, dticket_, predict ? dinfer_ : nullptr, H_, O_, dfeat_,
-      dact_inf_ + 2 * H_, dcost_, predict ? dorder_ : nullptr, stage_w ? 1 : 0);
+      c, n, opt_.stride_words, ncols_, ps.partial, ps.ticket, predict ? dinfer_ : nullptr, H_, O_, ps.feat, ps.z,
+      dcost_, predict ? ps.order : nullptr, stage_w ? 1 : 0);
   check_cuda(cudaGetLastError(), "k_sketch_predict");
   add_launches(1);
 }
 
 std::vector<float> Learner::features(const std::vector<ColumnView>& cols, cudaStream_t s) {
-  if (!dfeat_) fail(GX_ERR_INVALID, "this learner has no network (policy is not LEARNED)");
+  if (!dslots_) fail(GX_ERR_INVALID, "this learner has no network (policy is not LEARNED)");
   if ((int)cols.size() != (int)plain_->plan().schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
   std::vector<float> f(F_, 0.f);
-  if (!cols.empty() && cols[0].size > 0) sketch(cols, false, s);
-  else check_cuda(cudaMemsetAsync(dfeat_, 0, (size_t)F_ * 4, s), "features");
-  check_cuda(cudaMemcpyAsync(f.data(), dfeat_, (size_t)F_ * 4, cudaMemcpyDeviceToHost, s), "features");
+  if (!cols.empty() && cols[0].size > 0) sketch(cols, false, s, 0);
+  else check_cuda(cudaMemsetAsync(slots_[0].feat, 0, (size_t)F_ * 4, s), "features");
+  check_cuda(cudaMemcpyAsync(f.data(), slots_[0].feat, (size_t)F_ * 4, cudaMemcpyDeviceToHost, s), "features");
   check_cuda(cudaStreamSynchronize(s), "features");
   return f;
+}
+
+std::vector<uintptr_t> Learner::batch_key(const std::vector<ColumnView>& cols) const {
+  std::vector<uintptr_t> k;
+  for (int i = 0; i < ncols_ && i < (int)cols.size(); i++) {
+    k.push_back((uintptr_t)cols[i].data);
+    k.push_back((uintptr_t)cols[i].offset);
+    k.push_back((uintptr_t)cols[i].mask);
+  }
+  k.push_back(cols.empty() ? 0 : (uintptr_t)cols[0].size);
+  return k;
+}
+
+// The look-ahead slot holding this batch, if any: the stream waits for it and
+// the slot is released.
+int Learner::take_prepared(const std::vector<ColumnView>& cols, cudaStream_t s) {
+  bool any = false;
+  for (int q = 1; q < kPredSlots; q++) any |= slots_[q].valid;
+  if (!any) return -1;
+  const std::vector<uintptr_t> key = batch_key(cols);
+  for (int q = 1; q < kPredSlots; q++) {
+    if (!slots_[q].valid || slots_[q].key != key) continue;
+    check_cuda(cudaStreamWaitEvent(s, slots_[q].ready, 0), "wait look-ahead");
+    slots_[q].valid = false;
+    return q;
+  }
+  return -1;
+}
+
+void Learner::prepare(const std::vector<ColumnView>& cols, cudaStream_t s) {
+  if (opt_.policy != GX_LEARN_POLICY_LEARNED || !dslots_) return;
+  if ((int)cols.size() != (int)plain_->plan().schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  if (cols.empty() || cols[0].size == 0) return;
+  const int q = prep_next_;
+  prep_next_ = prep_next_ + 1 < kPredSlots ? prep_next_ + 1 : 1;
+  // the columns are ready once the caller's stream reaches this point
+  check_cuda(cudaEventRecord(prep_in_, s), "look-ahead event");
+  check_cuda(cudaStreamWaitEvent(aux_stream_, prep_in_, 0), "wait columns");
+  sync_inference_params(aux_stream_);
+  sketch(cols, true, aux_stream_, q);
+  check_cuda(cudaEventRecord(slots_[q].ready, aux_stream_), "look-ahead ready");
+  slots_[q].key = batch_key(cols);
+  slots_[q].valid = true;
 }
 
 void Learner::sync_inference_params(cudaStream_t s) {
@@ -741,9 +798,13 @@ void Learner::sync_inference_params(cudaStream_t s) {
 }
 
 std::vector<float> Learner::predict_log_sel(const std::vector<ColumnView>& cols, cudaStream_t s) {
-  sync_inference_params(s);
-  sketch(cols, true, s);
-  check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, s), "prediction");
+  int slot = take_prepared(cols, s);
+  if (slot < 0) {
+    sync_inference_params(s);
+    sketch(cols, true, s, 0);
+    slot = 0;
+  }
+  check_cuda(cudaMemcpyAsync(hpinned_, slots_[slot].z, O_ * 4, cudaMemcpyDeviceToHost, s), "prediction");
   check_cuda(cudaStreamSynchronize(s), "prediction sync");
   std::vector<float> ls(O_);
   for (int o = 0; o < O_; o++) {
@@ -753,10 +814,10 @@ std::vector<float> Learner::predict_log_sel(const std::vector<ColumnView>& cols,
   return ls;
 }
 
-void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s) {
+void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, int fslot) {
   const int slot = (int)(seen_ % (uint64_t)kTrainRing);
   // (a side-stream training round reads a snapshot of the ring, not the ring)
-  k_add_example<<<1, 128, 0, s>>>(dfeat_, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
+  k_add_example<<<1, 128, 0, s>>>(slots_[fslot].feat, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
                                   dtrainY_ + (size_t)slot * O_);
   check_cuda(cudaGetLastError(), "k_add_example");
   add_launches(1);
@@ -843,9 +904,13 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
     bi.path = 0;
     if (n > 0) {
-      sketch(cols, false, s);
+      int fs = take_prepared(cols, s);
+      if (fs < 0) {
+        sketch(cols, false, s, 0);
+        fs = 0;
+      }
       for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)hcounts_[o] / (double)n;
-      add_example(dcounts_, n, s);
+      add_example(dcounts_, n, s, fs);
       labelled_++;
       train(opt_.train_steps, s);
       if (!train_stream_) {
@@ -863,17 +928,21 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
   since_label_++;
   if (!opt_.size_outputs) {
     // order decided on the device: no host round trip before the filter
-    sync_inference_params(s);
-    sketch(cols, true, s);
+    int ps = take_prepared(cols, s);
+    if (ps < 0) {
+      sync_inference_params(s);
+      sketch(cols, true, s, 0);
+      ps = 0;
+    }
     // the report's copy of the prediction travels on a side stream, off the
     // filter's critical path
     int* horder = (int*)((char*)hpinned_ + 400);
     check_cuda(cudaEventRecord(pred_ready_, s), "prediction event");
     check_cuda(cudaStreamWaitEvent(aux_stream_, pred_ready_, 0), "wait prediction");
-    check_cuda(cudaMemcpyAsync(hpinned_, dact_inf_ + 2 * H_, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "prediction");
-    check_cuda(cudaMemcpyAsync(horder, dorder_, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "order");
+    check_cuda(cudaMemcpyAsync(hpinned_, slots_[ps].z, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "prediction");
+    check_cuda(cudaMemcpyAsync(horder, slots_[ps].order, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "order");
     ExecExtras ex;
-    ex.order_dev = dorder_;
+    ex.order_dev = slots_[ps].order;
     fast_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
     check_cuda(cudaStreamSynchronize(aux_stream_), "prediction readback");
     for (int o = 0; o < O_; o++) {
@@ -1053,6 +1122,14 @@ int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int n
   return guarded_call(status, [&] {
     if (!learner || !out || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "null argument");
     learner->l->execute(gx::to_views(columns, num_columns), out, out_rows, info, (cudaStream_t)stream);
+  });
+}
+
+int gx_learner_prepare(gx_learner* learner, const gx_column_view* columns, int num_columns, void* stream,
+                       gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "null argument");
+    learner->l->prepare(gx::to_views(columns, num_columns), (cudaStream_t)stream);
   });
 }
 

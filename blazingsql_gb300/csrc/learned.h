@@ -14,6 +14,7 @@ namespace gx {
 constexpr int kMaxSketchCols = 32;
 constexpr int kSketchParts = 64;  // CTAs per column of the sketch kernel
 constexpr int kTrainRing = 64;    // labelled examples kept for training
+constexpr int kPredSlots = 3;     // prediction buffers: 0 for in-call sketches, 1-2 for look-ahead
 
 struct LearnerOptions {
   int policy = GX_LEARN_POLICY_LEARNED;
@@ -58,6 +59,9 @@ class Learner {
 
   void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, gx_learned_batch_info* info,
                cudaStream_t s);
+  // Look-ahead: sketches (and predicts) a batch that a later execute() will
+  // receive, on a side stream, so that execute() finds its prediction ready.
+  void prepare(const std::vector<ColumnView>& cols, cudaStream_t s);
   void save(const std::string& path) const;
   void load(const std::string& path);
   // the sketch features of one batch (diagnostics)
@@ -67,10 +71,12 @@ class Learner {
   int num_outputs() const { return (int)fast_->plan().outputs.size(); }
 
  private:
-  // sketch features of the batch into dfeat_ (and, with predict, the network's z)
-  void sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s);
+  // sketch features of the batch into a prediction slot (and, with predict, the network's z and order)
+  void sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot);
   std::vector<float> predict_log_sel(const std::vector<ColumnView>& cols, cudaStream_t s);
-  void add_example(const unsigned long long* counts, int64_t n, cudaStream_t s);
+  void add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, int slot);
+  std::vector<uintptr_t> batch_key(const std::vector<ColumnView>& cols) const;
+  int take_prepared(const std::vector<ColumnView>& cols, cudaStream_t s);
   void train(int steps, cudaStream_t s);
   void sync_inference_params(cudaStream_t s);
   void release();
@@ -86,18 +92,27 @@ class Learner {
   float* dmom_ = nullptr;
   float* dvel_ = nullptr;
   float* dinfer_ = nullptr;   // inference copy of the parameters
-  float* dfeat_ = nullptr;    // current batch's features
+  struct PredSlot {
+    float* feat = nullptr;       // F features of the sketched batch
+    float* z = nullptr;          // network outputs (16)
+    int* order = nullptr;        // conjunct order (16)
+    float* partial = nullptr;    // sketch partials
+    unsigned int* ticket = nullptr;
+    cudaEvent_t ready = nullptr;
+    std::vector<uintptr_t> key;  // the batch it holds (column starts, rows)
+    bool valid = false;
+  };
+  PredSlot slots_[kPredSlots];
+  int prep_next_ = 1;
+  float* dslots_ = nullptr;   // one allocation for every slot
+  cudaEvent_t prep_in_ = nullptr;
   float* dtrainX_ = nullptr;  // ring of labelled examples
   float* dtrainY_ = nullptr;
   float* dsnapX_ = nullptr;   // snapshot of the ring a side-stream round trains on
   float* dsnapY_ = nullptr;
   float* dact_ = nullptr;     // training activations
-  float* dact_inf_ = nullptr; // inference activations
-  float* dpartial_ = nullptr;
   unsigned long long* dcounts_ = nullptr;
-  unsigned int* dticket_ = nullptr;  // last-block ticket of the sketch kernel
   float* dcost_ = nullptr;           // per conjunct: bytes per row its columns read
-  int* dorder_ = nullptr;            // the order the predict kernel chose
   float* hpinned_ = nullptr;  // pinned host: predictions + loss
   unsigned long long* hcounts_ = nullptr;  // pinned host: per-conjunct pass counts
   cudaStream_t train_stream_ = nullptr;

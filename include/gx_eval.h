@@ -292,6 +292,16 @@ gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* opt
 int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int num_columns, gx_column* out,
                        int64_t* out_rows, gx_learned_batch_info* info, void* stream, gx_status_info* status);
 
+/* Optional look-ahead for a stream of batches: sketches a batch that a later
+ * gx_learner_execute call will receive, and runs the network on it, on the
+ * learner's side stream (after `stream` reaches this point, so the columns may
+ * still be being produced there).  Call it for batch b+1 before executing batch
+ * b: the next call then finds its prediction ready instead of computing it on
+ * its critical path.  A prepared batch is recognised by its column pointers,
+ * offsets and row count; two may be pending at a time. */
+int gx_learner_prepare(gx_learner* learner, const gx_column_view* columns, int num_columns, void* stream,
+                       gx_status_info* status);
+
 /* Network parameters to / from a file (the plan's shape must match). */
 int gx_learner_save(const gx_learner* learner, const char* path, gx_status_info* status);
 int gx_learner_load(gx_learner* learner, const char* path, gx_status_info* status);

@@ -203,6 +203,32 @@ def test_staged_single_pass_matches_plain(offset, variant, monkeypatch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("size_outputs", [0, 1])
+def test_look_ahead_prepare(size_outputs):
+    """Batches prepared one step ahead give the same rows as the plain path and
+    the same order as computing the prediction in the call; a prepared batch
+    that never comes and a batch that was not prepared both still work."""
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    kw = dict(warmup_batches=3, relabel_every=4, train_steps=8, size_outputs=size_outputs)
+    ahead = g.Learner(plan, **kw)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    batches = [_upload(W.c4_batch_host(1 << 15, 12, b)) for b in range(10)]
+    ahead.prepare(batches[0])
+    for b in range(10):
+        if b + 1 < 10 and b != 5:  # batch 6 is not prepared
+            ahead.prepare(batches[b + 1])
+        if b == 7:
+            ahead.prepare(batches[2])  # prepared, never executed again
+        got, rows, info = ahead.execute(batches[b])
+        exp, erows, _ = plain.execute(batches[b])
+        assert rows == erows
+        assert_tables_equal(_host(got), _host(exp), what=f"batch {b}")
+        if info["path"] == 1:
+            assert sorted(info["order"]) == list(range(6))
+
+
+@pytest.mark.gpu
 def test_learned_misprediction_reruns():
     """With no capacity margin the predicted output size is often too small; the
     single pass re-runs with the exact count and the result still matches."""
