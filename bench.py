@@ -256,11 +256,16 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
 
 def learned_compare(batches: int, rows: int, seed: int = 4):
     """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
-    through gx_learner under three policies on the same resident batches:
-    plain fixed-order two-pass, textual-order single pass (no network), and
-    learned (warm-up and relabel batches on the plain path, training included).
-    Rows/s per policy over the whole batch stream; per-batch row counts and
-    sampled outputs must agree exactly."""
+    through gx_learner under four policies on the same resident batches:
+    plain fixed-order two-pass, textual-order single pass (no network), learned
+    (order from device memory, full-size outputs) and learned_sized (prediction
+    read back, outputs of the predicted size); the learned ones include the
+    warm-up and relabel batches on the plain path and the training.  Rows/s per
+    policy over the whole batch stream, timed around one
+    gx_learner_execute_batches call (the C ABI call a C++ caller makes; the
+    Python argument building and result wrapping stay outside) and, for
+    reference, through one gx_learner_execute per batch from Python.  Per-batch
+    row counts and sampled full outputs must agree exactly across policies."""
     import numpy as np
     import torch
     import blazingsql_gb300 as g
@@ -275,42 +280,64 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     # learned_sized: prediction read back, outputs of the predicted size
     policies = {"plain": (N.GX_LEARN_POLICY_PLAIN, 1), "textual": (N.GX_LEARN_POLICY_TEXTUAL, 1),
                 "learned": (N.GX_LEARN_POLICY_LEARNED, 0), "learned_sized": (N.GX_LEARN_POLICY_LEARNED, 1)}
-    # compile every kernel variant once outside the timed passes
+    # compile every kernel variant and grow the allocation pool once, outside
+    # the timed passes
     for pol, sized in policies.values():
         lr = g.Learner(plan, policy=pol, warmup_batches=1, relabel_every=0, fast_words_per_warp=8,
                        size_outputs=sized)
-        for b in range(2):
-            cols, _, _ = lr.execute(data[b], stream=stream)
-            for c in cols:
-                c.free()
+        for cols, _, _ in lr.execute_batches(data, stream=stream):
+            g.api.free_columns(cols, stream)
     torch.cuda.synchronize()
     res = {}
     counts = {}
+    check_batches = (0, batches // 2, batches - 1)
+    sampled = {}
+    L = N.lib()
     for name, (pol, sized) in policies.items():
-        lr = g.Learner(plan, policy=pol, async_training=1, relabel_every=16, fast_words_per_warp=8,
-                       size_outputs=sized)
-        infos = []
-        rows_out = []
-        L = N.lib()
+        def learner():
+            return g.Learner(plan, policy=pol, async_training=1, relabel_every=16, fast_words_per_warp=8,
+                             size_outputs=sized)
+        # the batch queue in one native call (what the execution graph's C++
+        # kernel does), each next batch prepared while the current one runs
+        lr = learner()
+        q = lr.queue_args(data)
         l0 = L.gx_debug_launch_count()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+        lr.run_queue(q, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        launches = L.gx_debug_launch_count() - l0
+        out = lr.queue_results(q)
+        infos = [i for _, _, i in out]
+        counts[name] = [r for _, r, _ in out]
+        for b, (cols, _, _) in enumerate(out):
+            if b in check_batches:
+                sampled.setdefault(b, []).append([c.to_host() for c in cols])
+            g.api.free_columns(cols, stream)
+        del out, lr
+        # the same queue driven from Python, one gx_learner_execute per batch
+        lr = learner()
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
         if pol == N.GX_LEARN_POLICY_LEARNED:
             lr.prepare(data[0], stream=stream)
         for b in range(batches):
             if pol == N.GX_LEARN_POLICY_LEARNED and b + 1 < batches:
                 lr.prepare(data[b + 1], stream=stream)  # look-ahead: next batch's prediction
-            cols, r, info = lr.execute(data[b], stream=stream)
-            rows_out.append(r)
-            infos.append(info)
+            cols, r, _ = lr.execute(data[b], stream=stream)
+            if r != counts[name][b]:
+                counts[name][b] = -1
             g.api.free_columns(cols, stream)
-        e1.record(stream)
+        p1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        counts[name] = rows_out
-        res[name] = {"rows_per_s": rows * batches / (ms / 1e3), "ms": ms,
-                     "launches": L.gx_debug_launch_count() - l0}
+        py_ms = p0.elapsed_time(p1)
+        del lr
+        res[name] = {"rows_per_s": rows * batches / (ms / 1e3), "ms": ms, "launches": launches,
+                     "python_loop_rows_per_s": rows * batches / (py_ms / 1e3), "python_loop_ms": py_ms}
         if name.startswith("learned"):
             res[name].update({
                 "plain_batches": sum(1 for i in infos if i["path"] == 0),
@@ -318,18 +345,14 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
                 "final_train_loss": infos[-1]["train_loss"],
                 "orders_used": len({tuple(i["order"]) for i in infos if i["path"] == 1}),
             })
-        del lr
     identical = counts["plain"] == counts["textual"] == counts["learned"] == counts["learned_sized"]
-    # sampled full-output comparison
-    checks = 0
-    for b in (0, batches // 2, batches - 1):
-        outs = []
-        for pol in (N.GX_LEARN_POLICY_PLAIN, N.GX_LEARN_POLICY_TEXTUAL):
-            cols, _, _ = g.Learner(plan, policy=pol).execute(data[b], stream=stream)
-            outs.append([c.to_host() for c in cols])
-        for x, y in zip(outs[0], outs[1]):
-            identical &= bool(np.array_equal(x.data.view(np.uint8), y.data.view(np.uint8)))
-        checks += 1
+    # full outputs of the sampled batches, every policy against the plain one
+    for b, per_policy in sampled.items():
+        for other in per_policy[1:]:
+            for x, y in zip(per_policy[0], other):
+                identical &= bool(np.array_equal(x.data.view(np.uint8), y.data.view(np.uint8)))
+                identical &= bool(np.array_equal(x.mask, y.mask))
+    checks = len(sampled)
     del data
     torch.cuda.empty_cache()
     return {

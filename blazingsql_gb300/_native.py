@@ -150,6 +150,8 @@ def lib():
     L.gx_learner_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64),
                                      P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
     L.gx_learner_prepare.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_void_p, P(StatusInfo)]
+    L.gx_learner_execute_batches.argtypes = [C.c_void_p, P(P(ColumnView)), C.c_int, C.c_int, P(Column),
+                                             P(C.c_int64), P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
     L.gx_learner_save.argtypes = [C.c_void_p, C.c_char_p, P(StatusInfo)]
     L.gx_learner_load.argtypes = [C.c_void_p, C.c_char_p, P(StatusInfo)]
     L.gx_learner_destroy.argtypes = [C.c_void_p]
@@ -176,6 +178,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_prepare", "gx_learner_save",
+    "gx_learner_execute_batches",
     "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
     "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",

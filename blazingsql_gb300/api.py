@@ -313,6 +313,13 @@ class Plan:
             pass
 
 
+class _Queue:
+    """Arguments and result arrays of one gx_learner_execute_batches call."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
 class _BatchReport(dict):
     """Per-batch report of the learner (a dict, filled on first access)."""
 
@@ -435,6 +442,43 @@ class Learner:
         N.check(N.lib().gx_learner_execute(self._h, views, nc, outs, C.byref(self._rows), C.byref(info), s,
                                            C.byref(self._st)), self._st)
         return _wrap(outs, n, s), self._rows.value, _BatchReport(info)
+
+    def execute_batches(self, tables: Sequence[Table], stream=None):
+        """A queue of batches in one native call (gx_learner_execute_batches):
+        each next batch is prepared while the current one runs.  Returns one
+        (columns, rows, info) per batch."""
+        q = self.queue_args(tables)
+        self.run_queue(q, stream)
+        return self.queue_results(q)
+
+    def queue_args(self, tables: Sequence[Table]) -> "_Queue":
+        """The native arguments of a batch queue, built once (run_queue runs it)."""
+        keep: list = []
+        nb = len(tables)
+        arrs = [_views(t, keep) for t in tables]
+        nc = arrs[0][1] if arrs else 0
+        if any(k != nc for _, k in arrs):
+            raise ValueError("every batch of a queue needs the same number of columns")
+        ptrs = (C.POINTER(N.ColumnView) * max(1, nb))(*[C.cast(a, C.POINTER(N.ColumnView)) for a, _ in arrs])
+        n = self.num_outputs
+        return _Queue(keep=(keep, arrs), ptrs=ptrs, nc=nc, nb=nb, outs=(N.Column * max(1, nb * n))(),
+                      rows=(C.c_int64 * max(1, nb))(), infos=(N.LearnedBatchInfo * max(1, nb))(), stream=0)
+
+    def run_queue(self, q: "_Queue", stream=None) -> None:
+        """The gx_learner_execute_batches call itself."""
+        q.stream = _stream_handle(stream)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_learner_execute_batches(self._h, q.ptrs, q.nc, q.nb, q.outs, q.rows, q.infos, q.stream,
+                                                   C.byref(st)), st)
+
+    def queue_results(self, q: "_Queue"):
+        n = self.num_outputs
+        res = []
+        for b in range(q.nb):
+            cols = [NativeColumn(N.Column(o.type_id, 0, o.data, o.null_mask, o.size, o.capacity), q.stream)
+                    for o in q.outs[b * n:(b + 1) * n]]
+            res.append((cols, q.rows[b], _BatchReport(q.infos[b])))
+        return res
 
     def prepare(self, table: Table, stream=None) -> None:
         """Look-ahead: compute the prediction of a batch a later execute() gets."""

@@ -264,7 +264,7 @@ __device__ void mlp_backward_block(const float* P, int F, int H, int O, const fl
     dz[i] = 2.f * inv * (ls - Y[i]) * sig_neg;
   }
   __syncthreads();
-  if (t == 0) {
+  if (loss && t == 0) {
     float l = 0.f;
     for (int i = 0; i < M * O; i++) {
       const float d = -softplusf(-Z[i]) - Y[i];
@@ -322,6 +322,10 @@ __device__ void mlp_backward_block(const float* P, int F, int H, int O, const fl
   __syncthreads();
 }
 
+__device__ void forward_and_order(const float* s_x, const float* P, int F, int H, int O,
+                                  const float* __restrict__ cost, float* s_h, float* Z, int* __restrict__ order,
+                                  float* __restrict__ report);
+
 // Sketch of every column plus, in the last block to finish, the feature rows
 // and the network's forward pass for them (one launch per batch).  grid
 // (kSketchParts, ncols); *ticket is zero on entry and left zero.
@@ -330,7 +334,7 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
                                                         const float* P, int H, int O,
                                                         float* __restrict__ features, float* __restrict__ Z,
                                                         const float* __restrict__ cost, int* __restrict__ order,
-                                                        int stage_w) {
+                                                        int stage_w, float* __restrict__ report) {
   // the last block reads the network's weights: one warp pulls them into L2
   // while the sample loads are in flight
   if (P && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 32) {
@@ -372,44 +376,95 @@ __global__ void __launch_bounds__(256) k_sketch_predict(SketchCols c, int64_t n,
   if (wsm) P = reinterpret_cast<const float*>(s_w4);
   for (int i = threadIdx.x; i < F; i += blockDim.x) features[i] = s_x[i];
   if (threadIdx.x == 0) *ticket = 0u;
-  if (P) {
-    const float* W1 = P;
-    const float* b1 = W1 + H * F;
-    const float* W2 = b1 + H;
-    const float* b2 = W2 + H * H;
-    const float* W3 = b2 + H;
-    const float* b3 = W3 + O * H;
-    dense_layer_block(W1, b1, F, H, s_x, 1, s_h, true);
-    __syncthreads();
-    dense_layer_block(W2, b2, H, H, s_h, 1, s_h + 256, true);
-    __syncthreads();
-    dense_layer_block(W3, b3, H, O, s_h + 256, 1, Z, false);
-    if (order) {
-      // conjunct order from the prediction: rank = cost / (1 - selectivity),
-      // ascending, ties by index (the host computes the same ranks)
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        float rank[16];
-        int ord[16];
-        for (int c = 0; c < O; c++) {
-          const float z = Z[c];
-          const float ls = -(fmaxf(-z, 0.f) + log1pf(expf(-fabsf(z))));
-          rank[c] = cost[c] / fmaxf(1e-9f, 1.f - expf(ls));
-          ord[c] = c;
-        }
-        for (int i = 1; i < O; i++) {
-          const int v = ord[i];
-          int j = i - 1;
-          while (j >= 0 && rank[ord[j]] > rank[v]) {
-            ord[j + 1] = ord[j];
-            j--;
-          }
-          ord[j + 1] = v;
-        }
-        for (int c = 0; c < O; c++) order[c] = ord[c];
+  if (P) forward_and_order(s_x, P, F, H, O, cost, s_h, Z, order, report);
+}
+
+// The network's forward pass on one feature row x (shared memory) by the whole
+// block, its outputs to Z, and (when `order` is given) the conjunct order
+// ranked on them, to `order` and, when given, with Z to the mapped `report`.
+// s_h: 512 floats of shared memory.
+__device__ void forward_and_order(const float* s_x, const float* P, int F, int H, int O,
+                                  const float* __restrict__ cost, float* s_h, float* Z, int* __restrict__ order,
+                                  float* __restrict__ report) {
+  const float* W1 = P;
+  const float* b1 = W1 + H * F;
+  const float* W2 = b1 + H;
+  const float* b2 = W2 + H * H;
+  const float* W3 = b2 + H;
+  const float* b3 = W3 + O * H;
+  dense_layer_block(W1, b1, F, H, s_x, 1, s_h, true);
+  __syncthreads();
+  dense_layer_block(W2, b2, H, H, s_h, 1, s_h + 256, true);
+  __syncthreads();
+  dense_layer_block(W3, b3, H, O, s_h + 256, 1, Z, false);
+  if (!order) return;
+  // conjunct order from the prediction: rank = cost / (1 - selectivity),
+  // ascending, ties by index (the host computes the same ranks)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float rank[16];
+    int ord[16];
+    for (int c = 0; c < O; c++) {
+      const float z = Z[c];
+      const float ls = -(fmaxf(-z, 0.f) + log1pf(expf(-fabsf(z))));
+      rank[c] = cost[c] / fmaxf(1e-9f, 1.f - expf(ls));
+      ord[c] = c;
+    }
+    for (int i = 1; i < O; i++) {
+      const int v = ord[i];
+      int j = i - 1;
+      while (j >= 0 && rank[ord[j]] > rank[v]) {
+        ord[j + 1] = ord[j];
+        j--;
+      }
+      ord[j + 1] = v;
+    }
+    for (int c = 0; c < O; c++) order[c] = ord[c];
+    // the batch report's copy, in mapped host memory: the host reads it
+    // after its stream synchronisation, without a copy of its own
+    if (report) {
+      for (int c = 0; c < O; c++) {
+        report[c] = Z[c];
+        reinterpret_cast<int*>(report)[16 + c] = ord[c];
       }
     }
   }
+}
+
+// Sketches of every batch of a queue in one launch: grid (parts, ncols,
+// batches), qc[b] / qn[b] batch b's columns and rows; the last block of each
+// batch (tickets[b], zero on entry) reduces the batch's partials into its
+// features (F = ncols * 11 floats at features + b * F).
+__global__ void __launch_bounds__(256) k_sketch_queue(const SketchCols* __restrict__ qc,
+                                                      const int64_t* __restrict__ qn, int64_t stride_words, int ncols,
+                                                      float* __restrict__ partial, unsigned int* tickets,
+                                                      float* __restrict__ features) {
+  const int b = blockIdx.z;
+  float* pb = partial + (size_t)b * ncols * gridDim.x * kPartial;
+  sketch_partial_block(qc[b], qn[b], stride_words, pb);
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&tickets[b], 1u) == gridDim.x * gridDim.y - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  float* f = features + (size_t)b * ncols * kFeatPerCol;
+  for (int col = threadIdx.x >> 5; col < ncols; col += blockDim.x >> 5)
+    sketch_final_warp(pb, col, gridDim.x, f + col * kFeatPerCol);
+}
+
+// One batch's prediction from its features: forward pass, order to `order`
+// (device) and the report (mapped host).  One block of 256 threads.
+__global__ void __launch_bounds__(256) k_predict(const float* __restrict__ feat, int F, const float* __restrict__ P,
+                                                 int H, int O, const float* __restrict__ cost,
+                                                 int* __restrict__ order, float* __restrict__ report) {
+  __shared__ float s_x[kMaxSketchCols * kFeatPerCol];
+  __shared__ float s_h[2 * 256];
+  __shared__ float s_z[16];
+  for (int i = threadIdx.x; i < F; i += blockDim.x) s_x[i] = feat[i];
+  __syncthreads();
+  forward_and_order(s_x, P, F, H, O, cost, s_h, s_z, order, report);
 }
 
 // `steps` full-batch Adam steps over the M stored examples, one CTA; the loss
@@ -426,7 +481,7 @@ __global__ void __launch_bounds__(256) k_mlp_train(float* __restrict__ P, float*
   float* Z = H2 + M * H;
   for (int it = 0; it < steps; it++) {
     mlp_forward_block(P, F, H, O, X, M, H1, H2, Z);
-    mlp_backward_block(P, F, H, O, X, M, H1, H2, Z, Y, G, loss, sm);
+    mlp_backward_block(P, F, H, O, X, M, H1, H2, Z, Y, G, it == steps - 1 ? loss : nullptr, sm);
     const float tt = (float)(t0 + it + 1);
     const float c1 = 1.f - powf(0.9f, tt), c2 = 1.f - powf(0.999f, tt);
     for (int i = threadIdx.x; i < np; i += blockDim.x) {
@@ -439,6 +494,59 @@ __global__ void __launch_bounds__(256) k_mlp_train(float* __restrict__ P, float*
     }
     __syncthreads();
   }
+}
+
+// Shared-memory floats of k_mlp_train_smem: parameters and gradients, the
+// examples and their labels, both hidden activations, the outputs and the
+// backward pass's scratch.
+__host__ __device__ inline size_t train_smem_floats(int F, int H, int O, int M) {
+  const size_t np = (size_t)H * F + H + (size_t)H * H + H + (size_t)O * H + O;
+  const size_t npa = (np + 3) / 4 * 4;
+  return 2 * npa + (size_t)M * F + (size_t)M * O + 2 * (size_t)M * H + (size_t)M * O +
+         ((size_t)M * O + 2 * (size_t)M * H);
+}
+
+// k_mlp_train with everything a step touches in shared memory (the Adam
+// moments stay in global memory, read and written once per step) and 1024
+// threads: the rounds are bound by dependent shared-memory arithmetic instead
+// of L1/L2 latency.
+__global__ void __launch_bounds__(1024) k_mlp_train_smem(float* __restrict__ P, float* __restrict__ Mo,
+                                                         float* __restrict__ Ve, int F, int H, int O,
+                                                         const float* __restrict__ X, int M,
+                                                         const float* __restrict__ Y, int steps, int t0, float lr,
+                                                         float* __restrict__ loss) {
+  extern __shared__ float4 sm4[];
+  float* sm = reinterpret_cast<float*>(sm4);
+  const int np = H * F + H + H * H + H + O * H + O;
+  const int npa = (np + 3) / 4 * 4;
+  float* sP = sm;
+  float* sG = sP + npa;
+  float* sX = sG + npa;
+  float* sY = sX + M * F;
+  float* sH1 = sY + M * O;
+  float* sH2 = sH1 + M * H;
+  float* sZ = sH2 + M * H;
+  float* sB = sZ + M * O;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) sP[i] = P[i];
+  for (int i = threadIdx.x; i < M * F; i += blockDim.x) sX[i] = X[i];
+  for (int i = threadIdx.x; i < M * O; i += blockDim.x) sY[i] = Y[i];
+  __syncthreads();
+  for (int it = 0; it < steps; it++) {
+    mlp_forward_block(sP, F, H, O, sX, M, sH1, sH2, sZ);
+    mlp_backward_block(sP, F, H, O, sX, M, sH1, sH2, sZ, sY, sG, it == steps - 1 ? loss : nullptr, sB);
+    const float tt = (float)(t0 + it + 1);
+    const float c1 = 1.f - powf(0.9f, tt), c2 = 1.f - powf(0.999f, tt);
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+      const float g = sG[i];
+      const float m = 0.9f * Mo[i] + 0.1f * g;
+      const float v = 0.999f * Ve[i] + 0.001f * g * g;
+      Mo[i] = m;
+      Ve[i] = v;
+      sP[i] -= lr * (m / c1) / (sqrtf(v / c2) + 1e-8f);
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < np; i += blockDim.x) P[i] = sP[i];
 }
 
 // one forward + backward pass (gradient checks)
@@ -601,7 +709,18 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
   H_ = opt_.hidden;
   O_ = nconj_;
   nparams_ = mlp_param_count(F_, H_, O_);
-  if (opt_.policy != GX_LEARN_POLICY_LEARNED) return;  // the comparison policies need no network
+  if (opt_.policy != GX_LEARN_POLICY_LEARNED) {
+    // the comparison policies need no network; the textual one may run queues
+    if (opt_.policy == GX_LEARN_POLICY_TEXTUAL) {
+      try {
+        reserve_queue(kQueueReserve);
+      } catch (...) {
+        release();
+        throw;
+      }
+    }
+    return;
+  }
   try {
     dparams_ = (float*)must_alloc((size_t)nparams_ * 4 * 5);  // P, G, Adam m, v, inference copy
     dgrad_ = dparams_ + nparams_;
@@ -628,14 +747,24 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     dact_ = (float*)must_alloc((size_t)4 * (2 * kTrainRing * H_ + kTrainRing * O_ + 4));
     dcounts_ = (unsigned long long*)must_alloc(8 * 16);
     dcost_ = (float*)must_alloc(4 * 16);
-    // pinned host block: predictions z[16], the loss at [16], conjunct counts from byte 256
-    check_cuda(cudaMallocHost(&hpinned_, 512), "pinned host buffer");
+    // pinned, mapped host block: predictions z[16], the loss at [16], conjunct
+    // counts from byte 256, each slot's report (z[16], order[16]) from byte 512
+    check_cuda(cudaHostAlloc((void**)&hpinned_, 512 + 128 * kPredSlots, cudaHostAllocMapped | cudaHostAllocPortable),
+               "pinned host buffer");
+    std::memset(hpinned_, 0, 512 + 128 * kPredSlots);
     hcounts_ = (unsigned long long*)((char*)hpinned_ + 256);
+    float* dpinned = nullptr;
+    check_cuda(cudaHostGetDevicePointer((void**)&dpinned, hpinned_, 0), "mapped host buffer");
+    for (int q = 0; q < kPredSlots; q++) {
+      slots_[q].report = hpinned_ + 128 + 32 * q;
+      slots_[q].report_dev = dpinned + 128 + 32 * q;
+    }
     check_cuda(cudaStreamCreateWithFlags(&aux_stream_, cudaStreamNonBlocking), "aux stream");
-    check_cuda(cudaEventCreateWithFlags(&pred_ready_, cudaEventDisableTiming), "event");
     check_cuda(cudaEventCreateWithFlags(&prep_in_, cudaEventDisableTiming), "event");
     for (int q = 0; q < kPredSlots; q++)
       check_cuda(cudaEventCreateWithFlags(&slots_[q].ready, cudaEventDisableTiming), "event");
+    for (int q = 0; q < 4; q++) check_cuda(cudaEventCreateWithFlags(&qev_[q], cudaEventDisableTiming), "event");
+    check_cuda(cudaEventCreateWithFlags(&qsketch_done_, cudaEventDisableTiming), "event");
     if (opt_.async_training) {
       check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
       check_cuda(cudaEventCreateWithFlags(&train_done_, cudaEventDisableTiming), "event");
@@ -668,6 +797,7 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     std::vector<float> cost(16, 0.f);
     for (int c = 0; c < nconj_; c++) cost[c] = (float)conj_cost_[c];
     check_cuda(cudaMemcpy(dcost_, cost.data(), 4 * 16, cudaMemcpyHostToDevice), "init costs");
+    reserve_queue(kQueueReserve);
   } catch (...) {
     release();
     throw;
@@ -685,12 +815,27 @@ void Learner::release() {
   cudaFree(dcounts_);
   cudaFree(dcost_);
   if (hpinned_) cudaFreeHost(hpinned_);
+  if (hqueue_) cudaFreeHost(hqueue_);
+  hqueue_ = nullptr;
+  queue_cap_ = 0;
+  cudaFree(dqsk_);
+  if (hqsk_) cudaFreeHost(hqsk_);
+  dqsk_ = hqsk_ = nullptr;
+  qsk_cap_ = 0;
+  for (int q = 0; q < 4; q++) {
+    if (qev_[q]) cudaEventDestroy(qev_[q]);
+    qev_[q] = nullptr;
+  }
+  for (int q = 0; q < 8; q++) {
+    if (qdone_[q]) cudaEventDestroy(qdone_[q]);
+    qdone_[q] = nullptr;
+  }
+  if (qsketch_done_) cudaEventDestroy(qsketch_done_);
+  qsketch_done_ = nullptr;
   if (train_done_) cudaEventDestroy(train_done_);
   if (labels_ready_) cudaEventDestroy(labels_ready_);
   if (train_stream_) cudaStreamDestroy(train_stream_);
-  if (pred_ready_) cudaEventDestroy(pred_ready_);
   if (aux_stream_) cudaStreamDestroy(aux_stream_);
-  pred_ready_ = nullptr;
   aux_stream_ = nullptr;
   for (int q = 0; q < kPredSlots; q++) {
     if (slots_[q].ready) cudaEventDestroy(slots_[q].ready);
@@ -707,8 +852,14 @@ void Learner::release() {
 
 Learner::~Learner() { release(); }
 
-void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot) {
+void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot,
+                     float* report_dev, float* report_host) {
   PredSlot& ps = slots_[slot];
+  if (!report_dev) {
+    report_dev = ps.report_dev;
+    report_host = ps.report;
+  }
+  ps.cur_report = report_host;
   SketchCols c{};
   for (int i = 0; i < ncols_; i++) {
     c.data[i] = cols[i].data;
@@ -725,7 +876,7 @@ void Learner::sketch(const std::vector<ColumnView>& cols, bool predict, cudaStre
   const bool stage_w = predict && wbytes <= 48 * 1024;
   k_sketch_predict<<<grid, 256, stage_w ? wbytes : 0, s>>>(
       c, n, opt_.stride_words, ncols_, ps.partial, ps.ticket, predict ? dinfer_ : nullptr, H_, O_, ps.feat, ps.z,
-      dcost_, predict ? ps.order : nullptr, stage_w ? 1 : 0);
+      dcost_, predict ? ps.order : nullptr, stage_w ? 1 : 0, predict ? report_dev : nullptr);
   check_cuda(cudaGetLastError(), "k_sketch_predict");
   add_launches(1);
 }
@@ -768,9 +919,12 @@ int Learner::take_prepared(const std::vector<ColumnView>& cols, cudaStream_t s) 
   return -1;
 }
 
-void Learner::prepare(const std::vector<ColumnView>& cols, cudaStream_t s) {
+void Learner::prepare(const std::vector<ColumnView>& cols, cudaStream_t s, float* report_dev, float* report_host) {
   if (opt_.policy != GX_LEARN_POLICY_LEARNED || !dslots_) return;
-  if ((int)cols.size() != (int)plain_->plan().schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  const auto& schema = plain_->plan().schema;
+  if (cols.size() != schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < cols.size(); i++)
+    if (cols[i].type != schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
   if (cols.empty() || cols[0].size == 0) return;
   const int q = prep_next_;
   prep_next_ = prep_next_ + 1 < kPredSlots ? prep_next_ + 1 : 1;
@@ -778,7 +932,7 @@ void Learner::prepare(const std::vector<ColumnView>& cols, cudaStream_t s) {
   check_cuda(cudaEventRecord(prep_in_, s), "look-ahead event");
   check_cuda(cudaStreamWaitEvent(aux_stream_, prep_in_, 0), "wait columns");
   sync_inference_params(aux_stream_);
-  sketch(cols, true, aux_stream_, q);
+  sketch(cols, true, aux_stream_, q, report_dev, report_host);
   check_cuda(cudaEventRecord(slots_[q].ready, aux_stream_), "look-ahead ready");
   slots_[q].key = batch_key(cols);
   slots_[q].valid = true;
@@ -814,14 +968,34 @@ std::vector<float> Learner::predict_log_sel(const std::vector<ColumnView>& cols,
   return ls;
 }
 
-void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, int fslot) {
+void Learner::add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, const float* feat) {
   const int slot = (int)(seen_ % (uint64_t)kTrainRing);
   // (a side-stream training round reads a snapshot of the ring, not the ring)
-  k_add_example<<<1, 128, 0, s>>>(slots_[fslot].feat, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
+  k_add_example<<<1, 128, 0, s>>>(feat, counts, (long long)n, F_, O_, dtrainX_ + (size_t)slot * F_,
                                   dtrainY_ + (size_t)slot * O_);
   check_cuda(cudaGetLastError(), "k_add_example");
   add_launches(1);
   seen_++;
+}
+
+// Dynamic shared memory the shared-memory training kernel may use on the
+// current device (its opt-in limit, raised once per device).
+static size_t train_smem_limit() {
+  static std::mutex mu;
+  static std::unordered_map<int, size_t> lim;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "device");
+  std::lock_guard<std::mutex> g(mu);
+  auto it = lim.find(dev);
+  if (it != lim.end()) return it->second;
+  int optin = 0;
+  check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared memory limit");
+  size_t v = 0;
+  if (cudaFuncSetAttribute(k_mlp_train_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) == cudaSuccess)
+    v = (size_t)optin;
+  cudaGetLastError();
+  lim[dev] = v;
+  return v;
 }
 
 void Learner::train(int steps, cudaStream_t s) {
@@ -852,8 +1026,14 @@ void Learner::train(int steps, cudaStream_t s) {
   }
   train_pending_ = false;
   float* dloss = dact_ + 2 * kTrainRing * H_ + kTrainRing * O_;
-  k_mlp_train<<<1, 256, backward_smem(H_, O_, M), ts>>>(dparams_, dgrad_, dmom_, dvel_, F_, H_, O_, X, M, Y, dact_,
-                                                        steps, adam_t_, opt_.lr, dloss);
+  const size_t smem = train_smem_floats(F_, H_, O_, M) * 4;
+  if (smem <= train_smem_limit()) {
+    k_mlp_train_smem<<<1, 1024, smem, ts>>>(dparams_, dmom_, dvel_, F_, H_, O_, X, M, Y, steps, adam_t_, opt_.lr,
+                                             dloss);
+  } else {
+    k_mlp_train<<<1, 256, backward_smem(H_, O_, M), ts>>>(dparams_, dgrad_, dmom_, dvel_, F_, H_, O_, X, M, Y, dact_,
+                                                          steps, adam_t_, opt_.lr, dloss);
+  }
   check_cuda(cudaGetLastError(), "k_mlp_train");
   add_launches(1);
   adam_t_ += steps;
@@ -862,8 +1042,18 @@ void Learner::train(int steps, cudaStream_t s) {
   params_pending_ = true;
 }
 
+void Learner::poll_training() {
+  if (train_stream_ && cudaEventQuery(train_done_) == cudaSuccess) loss_ = hpinned_[16];
+  cudaGetLastError();  // a round still running answers cudaErrorNotReady
+}
+
 void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
                       gx_learned_batch_info* info, cudaStream_t s) {
+  execute_one(cols, out, out_rows, info, s, nullptr);
+}
+
+void Learner::execute_one(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                          gx_learned_batch_info* info, cudaStream_t s, Deferred* d) {
   gx_learned_batch_info bi;
   std::memset(&bi, 0, sizeof bi);
   bi.num_conjuncts = nconj_;
@@ -882,7 +1072,8 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     std::iota(order.begin(), order.end(), 0);
     ex.order = order.data();
     ex.num_order = nconj_;
-    fast_->execute(cols, out, out_rows, s, &ex);
+    if (d) fast_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
+    else fast_->execute(cols, out, out_rows, s, &ex);
     for (int o = 0; o < nconj_; o++) bi.order[o] = o;
     bi.path = 1;
     bi.rows = out_rows ? *out_rows : 0;
@@ -897,20 +1088,38 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
   if (warm || relabel || n == 0) {
     since_label_ = 0;
     // plain fixed-order two-pass evaluator: output + per-conjunct pass counts
-    check_cuda(cudaMemsetAsync(dcounts_, 0, 8 * 16, s), "counts zero");
+    // (queued: the counters sit in the batch's zeroed header, read after the queue)
+    unsigned long long* counts = d ? d->hdr_dev + 4 : dcounts_;
     ExecExtras ex;
-    ex.conj_counts = dcounts_;
-    ex.conj_counts_host = hcounts_;  // read back with the count pass's own readback
-    plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    ex.conj_counts = counts;
+    if (d) {
+      d->labelled = true;
+      plain_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
+    } else {
+      check_cuda(cudaMemsetAsync(dcounts_, 0, 8 * 16, s), "counts zero");
+      ex.conj_counts_host = hcounts_;  // read back with the count pass's own readback
+      plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    }
     bi.path = 0;
     if (n > 0) {
-      int fs = take_prepared(cols, s);
-      if (fs < 0) {
-        sketch(cols, false, s, 0);
-        fs = 0;
+      const float* feat = nullptr;
+      if (d && d->feat) {
+        if (qsketch_pending_) {
+          check_cuda(cudaStreamWaitEvent(s, qsketch_done_, 0), "wait queue sketch");
+          qsketch_pending_ = false;
+        }
+        feat = d->feat;
+      } else {
+        int fs = take_prepared(cols, s);
+        if (fs < 0) {
+          sketch(cols, false, s, 0);
+          fs = 0;
+        }
+        feat = slots_[fs].feat;
       }
-      for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)hcounts_[o] / (double)n;
-      add_example(dcounts_, n, s, fs);
+      if (!d)
+        for (int o = 0; o < nconj_; o++) bi.measured_sel[o] = (double)hcounts_[o] / (double)n;
+      add_example(counts, n, s, feat);
       labelled_++;
       train(opt_.train_steps, s);
       if (!train_stream_) {
@@ -918,8 +1127,7 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
         loss_ = hpinned_[16];
       }
     }
-    if (train_stream_ && cudaEventQuery(train_done_) == cudaSuccess) loss_ = hpinned_[16];
-    cudaGetLastError();
+    poll_training();
     bi.train_loss = loss_;
     bi.rows = out_rows ? *out_rows : 0;
     if (info) *info = bi;
@@ -928,37 +1136,43 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
   since_label_++;
   if (!opt_.size_outputs) {
     // order decided on the device: no host round trip before the filter
-    int ps = take_prepared(cols, s);
-    if (ps < 0) {
-      sync_inference_params(s);
-      sketch(cols, true, s, 0);
-      ps = 0;
-    }
-    // the report's copy of the prediction travels on a side stream, off the
-    // filter's critical path
-    int* horder = (int*)((char*)hpinned_ + 400);
-    check_cuda(cudaEventRecord(pred_ready_, s), "prediction event");
-    check_cuda(cudaStreamWaitEvent(aux_stream_, pred_ready_, 0), "wait prediction");
-    check_cuda(cudaMemcpyAsync(hpinned_, slots_[ps].z, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "prediction");
-    check_cuda(cudaMemcpyAsync(horder, slots_[ps].order, O_ * 4, cudaMemcpyDeviceToHost, aux_stream_), "order");
     ExecExtras ex;
-    ex.order_dev = slots_[ps].order;
-    fast_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
-    check_cuda(cudaStreamSynchronize(aux_stream_), "prediction readback");
-    for (int o = 0; o < O_; o++) {
-      const float z = hpinned_[o];
-      bi.predicted_sel[o] = std::exp(-(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z)))));
-      bi.order[o] = horder[o];
+    int ps = -1;
+    if (d && d->pred_ready) {
+      check_cuda(cudaStreamWaitEvent(s, d->pred_ready, 0), "wait prediction");
+      ex.order_dev = d->order_dev;
+    } else {
+      ps = take_prepared(cols, s);
+      if (ps < 0) {
+        sync_inference_params(s);
+        sketch(cols, true, s, 0, d ? d->report_dev : nullptr, d ? d->report : nullptr);
+        ps = 0;
+      }
+      ex.order_dev = slots_[ps].order;
     }
-    if (train_stream_ && !params_pending_) loss_ = hpinned_[16];
+    if (d) fast_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
+    else fast_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+    if (!d) {
+      // the sketch kernel (ordered before the filter) left its prediction in
+      // a mapped host report
+      const float* rz = slots_[ps].cur_report;
+      const int* rorder = reinterpret_cast<const int*>(rz + 16);
+      for (int o = 0; o < O_; o++) {
+        const float z = rz[o];
+        bi.predicted_sel[o] = std::exp(-(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z)))));
+        bi.order[o] = rorder[o];
+      }
+    }
+    poll_training();
     bi.train_loss = loss_;
     bi.path = 1;
     bi.rows = out_rows ? *out_rows : 0;
     if (info) *info = bi;
     return;
   }
+  if (d) fail(GX_ERR_INVALID, "sized outputs cannot be deferred");
   const std::vector<float> ls = predict_log_sel(cols, s);
-  if (train_stream_ && !params_pending_) loss_ = hpinned_[16];
+  poll_training();
   // order by rank = cost / (1 - selectivity): cheap conjuncts that remove most rows first
   std::vector<int> order(nconj_);
   std::iota(order.begin(), order.end(), 0);
@@ -995,6 +1209,264 @@ void Learner::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
   bi.path = 1;
   bi.rows = out_rows ? *out_rows : 0;
   if (info) *info = bi;
+}
+
+// Host side of a deferred batch: the row count, the labels or the prediction,
+// all read after the queue's one synchronisation.
+void Learner::finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows,
+                         gx_learned_batch_info* info) {
+  const CompiledPlan& ran = d.labelled ? *plain_ : *fast_;
+  int64_t rows = 0;
+  ran.finish_queued(d.hdr, n, out, &rows);
+  if (out_rows) *out_rows = rows;
+  if (!info) return;
+  info->rows = rows;
+  if (d.labelled && n > 0)
+    for (int o = 0; o < nconj_; o++) info->measured_sel[o] = (double)d.hdr[4 + o] / (double)n;
+  if (!d.labelled && opt_.policy == GX_LEARN_POLICY_LEARNED) {
+    const int* rorder = reinterpret_cast<const int*>(d.report + 16);
+    for (int o = 0; o < O_; o++) {
+      const float z = d.report[o];
+      info->predicted_sel[o] = std::exp(-(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z)))));
+      info->order[o] = rorder[o];
+    }
+  }
+}
+
+bool Learner::can_defer() const {
+  const bool single_pass = opt_.policy == GX_LEARN_POLICY_TEXTUAL ||
+                           (opt_.policy == GX_LEARN_POLICY_LEARNED && !opt_.size_outputs);
+  return single_pass && fast_->can_defer() && plain_->can_defer();
+}
+
+constexpr int kQueueParts = 16;  // sketch blocks per column of a queued batch
+constexpr size_t kQueueDepth = 4;  // batches of a queue the host runs ahead of the device
+constexpr size_t kHostSlot = kQueueHeaderBytes + 128;  // per batch: header copy + mapped report
+
+Learner::QueueSketchLayout Learner::queue_sketch_layout(size_t nb) const {
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  QueueSketchLayout q;
+  q.o_n = al(nb * sizeof(SketchCols));
+  q.o_tk = q.o_n + al(nb * 8);
+  q.o_part = q.o_tk + al(nb * 4);
+  q.o_feat = q.o_part + al(nb * (size_t)ncols_ * kQueueParts * kPartial * 4);
+  q.total = q.o_feat + al(nb * (size_t)F_ * 4);
+  return q;
+}
+
+void Learner::reserve_queue(size_t nb) {
+  if (nb == 0) return;
+  if (queue_cap_ < nb) {
+    if (hqueue_) cudaFreeHost(hqueue_);
+    hqueue_ = nullptr;
+    queue_cap_ = 0;
+    check_cuda(cudaHostAlloc((void**)&hqueue_, nb * kHostSlot, cudaHostAllocMapped | cudaHostAllocPortable),
+               "pinned queue slots");
+    queue_cap_ = nb;
+  }
+  for (int q = 0; q < 8; q++)
+    if (!qdone_[q]) check_cuda(cudaEventCreateWithFlags(&qdone_[q], cudaEventDisableTiming), "event");
+  if (opt_.policy == GX_LEARN_POLICY_LEARNED && qsk_cap_ < nb) {
+    const QueueSketchLayout q = queue_sketch_layout(nb);
+    cudaFree(dqsk_);
+    if (hqsk_) cudaFreeHost(hqsk_);
+    dqsk_ = hqsk_ = nullptr;
+    qsk_cap_ = 0;
+    dqsk_ = (char*)must_alloc(q.total);
+    check_cuda(cudaMallocHost((void**)&hqsk_, q.o_part), "pinned sketch descriptors");
+    qsk_cap_ = nb;
+  }
+}
+
+void Learner::sketch_queue(const std::vector<std::vector<ColumnView>>& batches, std::vector<Deferred>& d,
+                           cudaStream_t s) {
+  const size_t nb = batches.size();
+  reserve_queue(nb);
+  const QueueSketchLayout q = queue_sketch_layout(nb);
+  const size_t o_n = q.o_n, o_tk = q.o_tk, o_part = q.o_part, o_feat = q.o_feat;
+  // the previous queue's upload has been consumed: its queue synchronised
+  std::memset(hqsk_, 0, o_part);
+  auto* desc = (SketchCols*)hqsk_;
+  auto* rows = (int64_t*)(hqsk_ + o_n);
+  for (size_t b = 0; b < nb; b++) {
+    const auto& cols = batches[b];
+    for (int i = 0; i < ncols_; i++) {
+      desc[b].data[i] = type_size(cols[i].type) == 0 ? nullptr : cols[i].data;
+      desc[b].mask[i] = cols[i].mask;
+      desc[b].off[i] = cols[i].offset;
+      desc[b].type[i] = cols[i].type;
+      desc[b].anchor[i] = anchors_[i];
+    }
+    rows[b] = cols.empty() ? 0 : cols[0].size;
+    d[b].feat = (const float*)(dqsk_ + o_feat) + b * (size_t)F_;
+  }
+  check_cuda(cudaMemcpyAsync(dqsk_, hqsk_, o_part, cudaMemcpyHostToDevice, s), "sketch descriptors");
+  // the side stream starts once the main stream has the descriptors (and the
+  // caller's columns are ready)
+  check_cuda(cudaEventRecord(prep_in_, s), "queue event");
+  check_cuda(cudaStreamWaitEvent(aux_stream_, prep_in_, 0), "wait queue");
+  k_sketch_queue<<<dim3(kQueueParts, ncols_, (unsigned)nb), 256, 0, aux_stream_>>>(
+      (const SketchCols*)dqsk_, (const int64_t*)(dqsk_ + o_n), opt_.stride_words, ncols_, (float*)(dqsk_ + o_part),
+      (unsigned int*)(dqsk_ + o_tk), (float*)(dqsk_ + o_feat));
+  check_cuda(cudaGetLastError(), "k_sketch_queue");
+  add_launches(1);
+  check_cuda(cudaEventRecord(qsketch_done_, aux_stream_), "queue sketch event");
+  qsketch_pending_ = true;
+}
+
+void Learner::predict_queued(Deferred& d, int ev, cudaStream_t) {
+  sync_inference_params(aux_stream_);
+  k_predict<<<1, 256, 0, aux_stream_>>>(d.feat, F_, dinfer_, H_, O_, dcost_, d.order_dev, d.report_dev);
+  check_cuda(cudaGetLastError(), "k_predict");
+  add_launches(1);
+  check_cuda(cudaEventRecord(qev_[ev], aux_stream_), "prediction event");
+  d.pred_ready = qev_[ev];
+}
+
+void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batches, gx_column* out,
+                              int64_t* out_rows, gx_learned_batch_info* infos, cudaStream_t s) {
+  const size_t nb = batches.size();
+  const int nout = num_outputs();
+  const auto& schema = plain_->plan().schema;
+  for (size_t b = 0; b < nb; b++) {
+    bool ok = batches[b].size() == schema.size();
+    for (size_t i = 0; ok && i < schema.size(); i++) ok = batches[b][i].type == schema[i];
+    if (!ok) fail(GX_ERR_INVALID, "batch " + std::to_string(b) + ": columns do not match the plan");
+  }
+  if (out_rows)
+    for (size_t b = 0; b < nb; b++) out_rows[b] = -1;  // set as each batch completes
+  auto rows_of = [&](size_t b) { return batches[b].empty() ? (int64_t)0 : batches[b][0].size; };
+  if (!can_defer()) {
+    // every batch completes before the next starts (sized outputs, the plain policy)
+    size_t at = 0;  // the batch being prepared or executed
+    try {
+      if (nb > 0) prepare(batches[0], s);
+      for (size_t b = 0; b < nb; b++) {
+        if (b + 1 < nb) {
+          at = b + 1;
+          prepare(batches[b + 1], s);
+        }
+        at = b;
+        execute_one(batches[b], out + b * nout, out_rows ? out_rows + b : nullptr, infos ? infos + b : nullptr, s,
+                    nullptr);
+      }
+    } catch (const Error& e) {
+      fail(e.code, "batch " + std::to_string(at) + ": " + e.what());
+    }
+    return;
+  }
+  // Queued: every batch's outputs, masks, tile statuses and headers come from
+  // one allocation cleared by one memset, and each batch puts only its
+  // kernels on the stream (no host round trip); one copy of all headers and
+  // one synchronisation complete the queue.
+  if (nb == 0) return;
+  reserve_queue(nb);
+  std::memset(hqueue_, 0, queue_cap_ * kHostSlot);
+  char* dqueue = nullptr;
+  check_cuda(cudaHostGetDevicePointer((void**)&dqueue, hqueue_, 0), "mapped queue slots");
+  std::vector<int> types;
+  for (const auto& o : fast_->plan().outputs) types.push_back(o.type);
+  std::vector<int64_t> caps(nb), status_words(nb);
+  for (size_t b = 0; b < nb; b++) {
+    caps[b] = rows_of(b);
+    status_words[b] = std::max(fast_->tiles_for(caps[b]), plain_->tiles_for(caps[b]));
+  }
+  std::vector<uint64_t*> status(nb);
+  char* base = (char*)alloc_output_queue(types, caps, status_words, out, status.data(), s);
+  std::vector<Deferred> d(nb);
+  const size_t rep0 = queue_cap_ * kQueueHeaderBytes;
+  for (size_t b = 0; b < nb; b++) {
+    d[b].hdr_dev = (unsigned long long*)(base + b * kQueueHeaderBytes);
+    d[b].status = status[b];
+    d[b].hdr = (const unsigned long long*)(hqueue_ + b * kQueueHeaderBytes);
+    d[b].report = (float*)(hqueue_ + rep0 + b * 128);
+    d[b].report_dev = (float*)(dqueue + rep0 + b * 128);
+    d[b].order_dev = (int*)(d[b].hdr_dev + 20);
+  }
+  const bool learned = opt_.policy == GX_LEARN_POLICY_LEARNED;
+  std::vector<gx_learned_batch_info> local(infos ? 0 : nb);
+  gx_learned_batch_info* inf = infos ? infos : local.data();
+  size_t at = 0;
+  size_t enqueued = 0;  // batches whose work is on the stream
+  std::string err;
+  int code = GX_OK;
+  try {
+    // every batch's sketch in one launch; each batch's prediction one step
+    // ahead on the side stream (a one-block kernel beside the running filter)
+    if (learned) {
+      sketch_queue(batches, d, s);
+      if (rows_of(0) > 0) predict_queued(d[0], 0, s);
+    }
+    for (size_t b = 0; b < nb; b++) {
+      // at most kQueueDepth batches ahead of the device: the host then sees
+      // training rounds finish while the queue runs, and later predictions
+      // use their parameters (the device never waits for the host)
+      if (b >= kQueueDepth)
+        check_cuda(cudaEventSynchronize(qdone_[(b - kQueueDepth) % 8]), "queue pacing");
+      if (learned && b + 1 < nb && rows_of(b + 1) > 0) {
+        at = b + 1;
+        predict_queued(d[b + 1], (int)((b + 1) % 4), s);
+      }
+      at = b;
+      execute_one(batches[b], out + b * nout, nullptr, inf + b, s, &d[b]);
+      check_cuda(cudaEventRecord(qdone_[b % 8], s), "batch event");
+      enqueued = b + 1;
+    }
+  } catch (const Error& e) {
+    code = e.code;
+    err = e.what();
+  }
+  // batches that never ran release their outputs (the allocation goes with the last column)
+  for (size_t c = enqueued; c < nb; c++)
+    for (int j = 0; j < nout; j++) {
+      free_column(out[c * nout + j], s);
+      out[c * nout + j] = gx_column{};
+    }
+  cudaError_t se = cudaSuccess;
+  if (enqueued > 0) se = cudaMemcpyAsync(hqueue_, base, enqueued * kQueueHeaderBytes, cudaMemcpyDeviceToHost, s);
+  if (se == cudaSuccess) se = cudaStreamSynchronize(s);
+  if (se != cudaSuccess) {
+    if (code == GX_OK) {
+      code = GX_ERR_CUDA;
+      err = std::string("queue completion: ") + cudaGetErrorString(se);
+      at = 0;
+    }
+    // no batch is known to have completed
+    for (size_t c = 0; c < enqueued; c++)
+      for (int j = 0; j < nout; j++) {
+        free_column(out[c * nout + j], s);
+        out[c * nout + j] = gx_column{};
+      }
+    enqueued = 0;
+  }
+  for (size_t b = 0; b < enqueued; b++) {
+    try {
+      finish_one(d[b], rows_of(b), out + b * nout, out_rows ? out_rows + b : nullptr, inf + b);
+    } catch (const Error& e) {
+      if (code == GX_OK) {
+        code = e.code;
+        err = e.what();
+        at = b;
+      }
+      // this batch and the later ones do not complete
+      for (size_t c = b; c < enqueued; c++) {
+        for (int j = 0; j < nout; j++) {
+          free_column(out[c * nout + j], s);
+          out[c * nout + j] = gx_column{};
+        }
+        if (out_rows) out_rows[c] = -1;
+      }
+      break;
+    }
+  }
+  if (qsketch_pending_) {
+    // no labelled batch waited for the queue sketch: the next queue's upload
+    // must not overwrite its descriptors while it runs
+    check_cuda(cudaStreamWaitEvent(s, qsketch_done_, 0), "wait queue sketch");
+    qsketch_pending_ = false;
+  }
+  poll_training();
+  if (code != GX_OK) fail((gx_status)code, "batch " + std::to_string(at) + ": " + err);
 }
 
 void Learner::save(const std::string& path) const {
@@ -1122,6 +1594,21 @@ int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int n
   return guarded_call(status, [&] {
     if (!learner || !out || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "null argument");
     learner->l->execute(gx::to_views(columns, num_columns), out, out_rows, info, (cudaStream_t)stream);
+  });
+}
+
+int gx_learner_execute_batches(gx_learner* learner, const gx_column_view* const* batches, int num_columns,
+                               int num_batches, gx_column* out, int64_t* out_rows, gx_learned_batch_info* infos,
+                               void* stream, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!learner || num_batches < 0 || (num_batches > 0 && (!batches || !out)))
+      gx::fail(GX_ERR_INVALID, "null argument");
+    std::vector<std::vector<gx::ColumnView>> b(num_batches);
+    for (int i = 0; i < num_batches; i++) {
+      if (num_columns > 0 && !batches[i]) gx::fail(GX_ERR_INVALID, "null batch");
+      b[i] = gx::to_views(batches[i], num_columns);
+    }
+    learner->l->execute_batches(b, out, out_rows, infos, (cudaStream_t)stream);
   });
 }
 

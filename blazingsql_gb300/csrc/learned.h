@@ -61,7 +61,16 @@ class Learner {
                cudaStream_t s);
   // Look-ahead: sketches (and predicts) a batch that a later execute() will
   // receive, on a side stream, so that execute() finds its prediction ready.
-  void prepare(const std::vector<ColumnView>& cols, cudaStream_t s);
+  // report_dev / report_host: where the sketch kernel leaves the prediction
+  // for the batch report (mapped host memory; default: the slot's own).
+  void prepare(const std::vector<ColumnView>& cols, cudaStream_t s, float* report_dev = nullptr,
+               float* report_host = nullptr);
+  // execute() on each batch in order, each next batch prepared while the
+  // current one runs; out holds num_outputs() columns per batch, batch-major.
+  // Single-pass policies with full-size outputs run the whole queue with one
+  // host synchronisation at the end.
+  void execute_batches(const std::vector<std::vector<ColumnView>>& batches, gx_column* out, int64_t* out_rows,
+                       gx_learned_batch_info* infos, cudaStream_t s);
   void save(const std::string& path) const;
   void load(const std::string& path);
   // the sketch features of one batch (diagnostics)
@@ -71,10 +80,40 @@ class Learner {
   int num_outputs() const { return (int)fast_->plan().outputs.size(); }
 
  private:
+  // host-side record of a batch enqueued without a synchronisation
+  struct Deferred {
+    unsigned long long* hdr_dev = nullptr;   // device, zeroed: filter header [0, 4), conjunct counts [4, 20)
+    uint64_t* status = nullptr;              // device, zeroed: tile status words
+    const unsigned long long* hdr = nullptr; // pinned host copy of hdr_dev, valid after the queue's sync
+    float* report = nullptr;                 // mapped: z[16] then order[16] (host view)
+    float* report_dev = nullptr;             // the same, device view
+    const float* feat = nullptr;             // device: the batch's sketch features (queue sketch)
+    int* order_dev = nullptr;                // device: the predicted conjunct order (in the header)
+    cudaEvent_t pred_ready = nullptr;        // recorded after the batch's prediction
+    bool labelled = false;                   // ran the plain two-pass evaluator
+  };
+  void execute_one(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
+                   gx_learned_batch_info* info, cudaStream_t s, Deferred* d);
+  void finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows, gx_learned_batch_info* info);
+  bool can_defer() const;
+  // queue buffers for up to nb batches (made at construction for kQueueReserve)
+  struct QueueSketchLayout {
+    size_t o_n = 0, o_tk = 0, o_part = 0, o_feat = 0, total = 0;
+  };
+  QueueSketchLayout queue_sketch_layout(size_t nb) const;
+  void reserve_queue(size_t nb);
+  static constexpr size_t kQueueReserve = 64;
+  // the loss of the last finished training round, when one has finished
+  void poll_training();
   // sketch features of the batch into a prediction slot (and, with predict, the network's z and order)
-  void sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot);
+  void sketch(const std::vector<ColumnView>& cols, bool predict, cudaStream_t s, int slot,
+              float* report_dev = nullptr, float* report_host = nullptr);
   std::vector<float> predict_log_sel(const std::vector<ColumnView>& cols, cudaStream_t s);
-  void add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, int slot);
+  void add_example(const unsigned long long* counts, int64_t n, cudaStream_t s, const float* feat);
+  // a queue's sketches of every batch in one launch on the side stream, and
+  // the prediction of one of its batches
+  void sketch_queue(const std::vector<std::vector<ColumnView>>& batches, std::vector<Deferred>& d, cudaStream_t s);
+  void predict_queued(Deferred& d, int ev, cudaStream_t s);
   std::vector<uintptr_t> batch_key(const std::vector<ColumnView>& cols) const;
   int take_prepared(const std::vector<ColumnView>& cols, cudaStream_t s);
   void train(int steps, cudaStream_t s);
@@ -98,6 +137,9 @@ class Learner {
     int* order = nullptr;        // conjunct order (16)
     float* partial = nullptr;    // sketch partials
     unsigned int* ticket = nullptr;
+    float* report = nullptr;      // mapped host copy of z[16] then order[16] (host view)
+    float* report_dev = nullptr;  // the same memory, device view
+    const float* cur_report = nullptr;  // where the current prediction's report goes (host view)
     cudaEvent_t ready = nullptr;
     std::vector<uintptr_t> key;  // the batch it holds (column starts, rows)
     bool valid = false;
@@ -115,9 +157,19 @@ class Learner {
   float* dcost_ = nullptr;           // per conjunct: bytes per row its columns read
   float* hpinned_ = nullptr;  // pinned host: predictions + loss
   unsigned long long* hcounts_ = nullptr;  // pinned host: per-conjunct pass counts
+  char* hqueue_ = nullptr;                 // pinned, mapped: per-batch slots of a deferred queue
+  size_t queue_cap_ = 0;                   // batches hqueue_ holds
+  // a queue's sketch: device [column descriptors | rows | tickets | partials |
+  // features] and its pinned staging for the first three
+  char* dqsk_ = nullptr;
+  char* hqsk_ = nullptr;
+  size_t qsk_cap_ = 0;                     // batches they hold
+  cudaEvent_t qev_[4] = {nullptr, nullptr, nullptr, nullptr};  // prediction events, in rotation
+  cudaEvent_t qdone_[8] = {};              // batch completion events of a queue, in rotation
+  cudaEvent_t qsketch_done_ = nullptr;
+  bool qsketch_pending_ = false;           // the main stream has not waited for the queue sketch yet
   cudaStream_t train_stream_ = nullptr;
   cudaStream_t aux_stream_ = nullptr;   // prediction readback for the batch report
-  cudaEvent_t pred_ready_ = nullptr;
   cudaEvent_t train_done_ = nullptr, labels_ready_ = nullptr;
   bool params_pending_ = false;
   bool train_pending_ = false;   // a round was asked for while another ran  // training finished a version not yet copied to dinfer_

@@ -193,6 +193,54 @@ void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>&
   }
 }
 
+void* alloc_output_queue(const std::vector<int>& types, const std::vector<int64_t>& caps,
+                         const std::vector<int64_t>& status_words, gx_column* out, uint64_t** status,
+                         cudaStream_t s) {
+  const size_t nout = types.size();
+  const size_t nb = caps.size();
+  if (nout == 0) fail(GX_ERR_INVALID, "no output columns");
+  if (nb == 0) return nullptr;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  // [headers: 256 bytes per batch | per batch: tile status, masks | data]
+  size_t total = al(nb * kQueueHeaderBytes);
+  std::vector<size_t> soff(nb), moff(nb * nout), doff(nb * nout);
+  for (size_t b = 0; b < nb; b++) {
+    soff[b] = total;
+    total += al((size_t)std::max<int64_t>(status_words[b], 1) * 8);
+    for (size_t j = 0; j < nout; j++) {
+      moff[b * nout + j] = total;
+      total += al((size_t)mask_words_padded(caps[b]) * 4);
+    }
+  }
+  const size_t zero = total;
+  for (size_t b = 0; b < nb; b++)
+    for (size_t j = 0; j < nout; j++) {
+      doff[b * nout + j] = total;
+      total += al(std::max<size_t>(64, (size_t)caps[b] * type_size(types[j])));
+    }
+  char* base = (char*)dev_alloc(total, s);
+  const cudaError_t e = cudaMemsetAsync(base, 0, zero, s);
+  if (e != cudaSuccess) {
+    dev_free(base, s);
+    check_cuda(e, "output queue memset");
+  }
+  auto* ar = new OutputArena{base, (int)(nb * nout)};
+  std::lock_guard<std::mutex> g(g_arena_mu);
+  for (size_t b = 0; b < nb; b++) {
+    status[b] = (uint64_t*)(base + soff[b]);
+    for (size_t j = 0; j < nout; j++) {
+      gx_column& c = out[b * nout + j];
+      c = gx_column{};
+      c.type_id = types[j];
+      c.data = base + doff[b * nout + j];
+      c.null_mask = (uint32_t*)(base + moff[b * nout + j]);
+      c.capacity = caps[b];
+      g_arena_of[c.data] = ar;
+    }
+  }
+  return base;
+}
+
 int64_t mask_words_for(int64_t rows) { return mask_words_padded(rows); }
 
 void free_column(gx_column& c, cudaStream_t s) {
@@ -396,6 +444,16 @@ void launch_raw(const JitKernel& k, int grid, cudaStream_t s, void** params, boo
   }
 }
 
+// The calling thread's pinned 4-word buffer for a filter's scratch header:
+// a copy into pageable memory would be staged by the driver.  A call reads it
+// back and synchronises before it returns, so one buffer per thread suffices.
+static unsigned long long* pinned_header() {
+  thread_local unsigned long long* buf = nullptr;
+  if (!buf) check_cuda(cudaMallocHost((void**)&buf, 64), "pinned header");
+  for (int i = 0; i < 4; i++) buf[i] = 0;
+  return buf;
+}
+
 static std::vector<bool> runtime_nullable(const Plan& p, const std::vector<ColumnView>& cols) {
   std::vector<bool> nb(cols.size());
   for (size_t i = 0; i < cols.size(); i++) nb[i] = cols[i].mask != nullptr;
@@ -440,6 +498,76 @@ void CompiledPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, 
     run_project(cols, out, caller_bufs, s);
     if (out_rows) *out_rows = cols.empty() ? 0 : cols[0].size;
   }
+}
+
+bool CompiledPlan::can_defer() const {
+  if (!plan_.has_filter()) return false;
+  for (const auto& o : plan_.outputs)
+    if (o.kind == OutSpec::BROADCAST) return false;
+  return true;
+}
+
+void CompiledPlan::finish_queued(const unsigned long long* hdr, int64_t n, gx_column* out, int64_t* out_rows) const {
+  if (hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  const int64_t rows = n == 0 ? 0 : mode_ == GX_FILTER_TWO_PASS ? (int64_t)hdr[3] : (int64_t)hdr[1];
+  if (out_rows) *out_rows = rows;
+  for (size_t j = 0; j < plan_.outputs.size(); j++) {
+    if (rows > out[j].capacity) fail(GX_ERR_CAPACITY, "output capacity too small");
+    out[j].size = rows;
+  }
+}
+
+int64_t CompiledPlan::tiles_for(int64_t n) const {
+  const int64_t tile_rows = (int64_t)cfg_.warps * cfg_.words * 32;
+  return (n + tile_rows - 1) / tile_rows;
+}
+
+void CompiledPlan::enqueue_filter(const std::vector<ColumnView>& cols, gx_column* out, unsigned long long* hdr,
+                                  uint64_t* tile_status, const ExecExtras* extras, cudaStream_t s) const {
+  if (!can_defer()) fail(GX_ERR_INVALID, "a queued filter needs a filter plan without literal outputs");
+  if (cols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < cols.size(); i++)
+    if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const int nout = (int)plan_.outputs.size();
+  for (int j = 0; j < nout; j++) {
+    if (!out[j].data || !out[j].null_mask || out[j].capacity < n)
+      fail(GX_ERR_INVALID, "queued filter outputs need room for every input row");
+    out[j].type_id = plan_.outputs[j].type;
+  }
+  if (n == 0) return;
+  const int64_t ntiles = tiles_for(n);
+  const std::vector<bool> nb = runtime_nullable(plan_, cols);
+  KernelArgs a{};
+  fill_args_inputs(a, cols);
+  a.tile_status = tile_status;
+  a.tile_counter = hdr + 0;
+  a.out_count = hdr + 1;
+  a.err = (int*)(hdr + 2);
+  a.seed = plan_.rand_seed;
+  a.capacity = n;
+  for (int i = 0; i < 16; i++) a.order[i] = i;
+  if (extras) {
+    for (int i = 0; i < extras->num_order && i < 16; i++) a.order[i] = extras->order[i];
+    a.order_dev = extras->order_dev;
+    a.conj_counts = extras->conj_counts;
+  }
+  for (int j = 0; j < nout; j++) {
+    a.out_data[j] = out[j].data;
+    a.out_mask[j] = out[j].null_mask;
+  }
+  const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
+  if (two_pass) {
+    const JitKernel kc = kernel(KernelKind::COUNT_FILTER, nb);
+    int64_t grid = (int64_t)device_sm_count() * kc.max_blocks_per_sm;
+    if (grid > ntiles) grid = ntiles;
+    launch(kc, (int)grid, s, a, true);
+    launch_scan_tiles(tile_status, ntiles, hdr + 3, s);
+  }
+  const JitKernel k = kernel(two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER, nb);
+  int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
+  if (grid > ntiles) grid = ntiles;
+  launch(k, (int)grid, s, a, true);
 }
 
 void CompiledPlan::run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs,
@@ -558,17 +686,17 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       a.order_dev = extras->order_dev;
       a.conj_counts = extras->conj_counts;
     }
-    unsigned long long host_hdr[4] = {0, 0, 0, 0};
+    unsigned long long* host_hdr = pinned_header();
     if (two_pass) {
       const JitKernel kc = kernel(KernelKind::COUNT_FILTER, nb);
       int64_t grid = (int64_t)device_sm_count() * kc.max_blocks_per_sm;
       if (grid > ntiles) grid = ntiles;
       launch(kc, (int)grid, s, a, true);
       launch_scan_tiles(status, ntiles, hdr + 3, s);
-      check_cuda(cudaMemcpyAsync(host_hdr, hdr, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
       if (extras && extras->conj_counts && extras->conj_counts_host)
         check_cuda(cudaMemcpyAsync(extras->conj_counts_host, extras->conj_counts, 16 * 8, cudaMemcpyDeviceToHost, s),
                    "conjunct counts readback");
+      check_cuda(cudaMemcpyAsync(host_hdr, hdr, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
       check_cuda(cudaStreamSynchronize(s), "count sync");
       capacity = (int64_t)host_hdr[3];
     }
@@ -606,7 +734,7 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     last.regs = k.num_regs;
     last.tiles = ntiles;
     launch(k, (int)grid, s, a, true);
-    check_cuda(cudaMemcpyAsync(host_hdr, hdr, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+    check_cuda(cudaMemcpyAsync(host_hdr, hdr, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
     check_cuda(cudaStreamSynchronize(s), "filter sync");
     if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
     const int64_t rows = two_pass ? (int64_t)host_hdr[3] : (int64_t)host_hdr[1];
@@ -678,8 +806,8 @@ void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_
   int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
   if (grid > ntiles) grid = ntiles;
   launch(k, (int)grid, s, a, true);
-  unsigned long long host_hdr[4] = {0, 0, 0, 0};
-  check_cuda(cudaMemcpyAsync(host_hdr, scratch, sizeof host_hdr, cudaMemcpyDeviceToHost, s), "count readback");
+  unsigned long long* host_hdr = pinned_header();
+  check_cuda(cudaMemcpyAsync(host_hdr, scratch, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
   check_cuda(cudaStreamSynchronize(s), "filter sync");
   if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
   const int64_t rows = (int64_t)host_hdr[1];

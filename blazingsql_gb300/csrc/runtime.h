@@ -33,6 +33,15 @@ void* dev_alloc(size_t bytes, cudaStream_t s);
 void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>& caps, bool zero_masks,
                       gx_column* out, cudaStream_t s);
 int64_t mask_words_for(int64_t rows);  // padded 32-bit mask words an output of `rows` rows holds
+// Outputs of a queue of filter calls in one allocation and one memset: for
+// batch b, types.size() columns of capacity caps[b] with zeroed masks
+// (out[b * types.size() + j]) and status_words[b] zeroed tile-status words
+// (status[b]); the allocation starts with a zeroed kQueueHeaderBytes header
+// per batch (the returned base).  Released when the last column is freed.
+constexpr size_t kQueueHeaderBytes = 256;
+void* alloc_output_queue(const std::vector<int>& types, const std::vector<int64_t>& caps,
+                         const std::vector<int64_t>& status_words, gx_column* out, uint64_t** status,
+                         cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 void check_cuda(cudaError_t e, const char* what);
 // host-side fault injection for tests: fail the n-th next allocation (n >= 1)
@@ -74,6 +83,21 @@ class CompiledPlan {
   // out[0].data is non-null, caller-supplied buffers are used (capacity rows).
   void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s,
                const ExecExtras* extras = nullptr) const;
+
+  // Queue form of a filter call: only the plan's kernels go on the stream (no
+  // allocation, memset, copy or synchronisation).  out[j] come from the caller
+  // with room for every input row and zeroed masks; `hdr` (4 words: tile
+  // counter, single-pass row count, error flag, two-pass row count) and
+  // `tile_status` (tiles_for(n) words) are zeroed device memory.  The call is
+  // completed by finish_queued() on a host copy of hdr once the stream has
+  // reached it.  Needs can_defer().
+  void enqueue_filter(const std::vector<ColumnView>& cols, gx_column* out, unsigned long long* hdr,
+                      uint64_t* tile_status, const ExecExtras* extras, cudaStream_t s) const;
+  void finish_queued(const unsigned long long* hdr, int64_t n, gx_column* out, int64_t* out_rows) const;
+  // a filter plan whose outputs are all computed per row (none a literal)
+  bool can_defer() const;
+  // tile-status words a filter over n rows uses
+  int64_t tiles_for(int64_t n) const;
 
   // kernel handle of this plan for a given kind and set of columns with masks
   JitKernel kernel_for(KernelKind kind, const std::vector<bool>& nullable) const { return kernel(kind, nullable); }

@@ -302,6 +302,19 @@ int gx_learner_execute(gx_learner* learner, const gx_column_view* columns, int n
 int gx_learner_prepare(gx_learner* learner, const gx_column_view* columns, int num_columns, void* stream,
                        gx_status_info* status);
 
+/* A queue of batches in one call: gx_learner_execute on batches[0] …
+ * batches[num_batches-1] in order (each num_columns views), each next batch
+ * prepared (as gx_learner_prepare) while the current one runs.  out holds
+ * (plan outputs) columns per batch, batch-major, all with data == NULL on
+ * entry (library-allocated, freed with gx_free_columns); out_rows and infos
+ * (may be NULL) one entry per batch.  Every batch's columns are checked
+ * against the plan before any batch runs.  On an error the message names the
+ * failing batch; out_rows[b] stays -1 for every batch that did not complete,
+ * and the outputs of those that did are valid and the caller's to free. */
+int gx_learner_execute_batches(gx_learner* learner, const gx_column_view* const* batches, int num_columns,
+                               int num_batches, gx_column* out, int64_t* out_rows, gx_learned_batch_info* infos,
+                               void* stream, gx_status_info* status);
+
 /* Network parameters to / from a file (the plan's shape must match). */
 int gx_learner_save(const gx_learner* learner, const char* path, gx_status_info* status);
 int gx_learner_load(gx_learner* learner, const char* path, gx_status_info* status);

@@ -229,6 +229,46 @@ def test_look_ahead_prepare(size_outputs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("policy,size_outputs", [("learned", 0), ("learned", 1), ("textual", 0)])
+def test_execute_batches_queue(policy, size_outputs):
+    """A queue of batches in one call (ragged and empty batches included) gives
+    each batch exactly the plain path's output, with the prediction reported
+    for the single-pass batches; an invalid batch is named in the error.  With
+    full-size outputs (size_outputs=0, or the textual policy) the queue runs
+    with one synchronisation at the end."""
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
+    plan = _c4_plan(g)
+    sizes = [1 << 15, 1 << 15, 1 << 15, 0, 4097, 1 << 15, 31, 1 << 15, 1 << 14, 1 << 15]
+    batches = [_upload(W.c4_batch_host(n, 21, b)) for b, n in enumerate(sizes)]
+    pol = g.GX_LEARN_POLICY_LEARNED if policy == "learned" else g.GX_LEARN_POLICY_TEXTUAL
+    learned = g.Learner(plan, policy=pol, warmup_batches=3, relabel_every=4, train_steps=8,
+                        size_outputs=size_outputs)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    out = learned.execute_batches(batches)
+    assert len(out) == len(batches)
+    for b, (got, rows, info) in enumerate(out):
+        exp, erows, _ = plain.execute(batches[b])
+        assert rows == erows, f"batch {b}"
+        assert_tables_equal(_host(got), _host(exp), what=f"batch {b}")
+        assert info["rows"] == rows
+        if info["path"] == 1:
+            assert sorted(info["order"]) == list(range(6))
+            if policy == "learned":
+                assert all(0.0 < p < 1.0 for p in info["predicted_sel"])
+        elif sizes[b] > 0:
+            assert max(info["measured_sel"]) > 0.0
+    assert any(info["path"] == 1 for _, _, info in out)
+    assert learned.execute_batches([]) == []
+    from blazingsql_gb300.api import DeviceColumn
+    from blazingsql_gb300.types import HostColumn
+    wrong = list(batches[4])
+    wrong[0] = DeviceColumn.from_host(HostColumn(T.INT32, np.zeros(4097, dtype=np.int32)))
+    with pytest.raises(N.GxError, match="batch 3"):  # column 0 of batch 3 has the wrong type
+        learned.execute_batches(list(batches[:3]) + [wrong])
+
+
+@pytest.mark.gpu
 def test_learned_misprediction_reruns():
     """With no capacity margin the predicted output size is often too small; the
     single pass re-runs with the exact count and the result still matches."""
