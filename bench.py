@@ -8,8 +8,9 @@ needed between steps).
 
 JSON line (rank 0):
   value     rows/s, inputs resident on the device, whole job over all ranks
-  e2e       rows/s through gx_filter_project with pinned HOST buffers: H2D of the
-            step's inputs + evaluation + D2H of the outputs inside the timed region
+  e2e       rows/s through gx_plan_execute_host with pinned HOST buffers: H2D of
+            the step's inputs + evaluation + D2H of the outputs inside the timed
+            region (the library overlaps them by row chunk)
   roofline  algorithmic bytes of the fused filter+project kernel / its average
             CUDA-event duration vs the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (scalar restatement of the reference's
@@ -459,10 +460,12 @@ def main():
     traffic_per_row = profile_traffic(f"{args.config}_fused_filter_project")
 
     # ---- end to end: pinned host buffers, H2D + evaluate + D2H ------------
+    # through gx_plan_execute_host: host columns in, host columns out; the
+    # library pipelines the copies in, the kernels and the copies out by chunk
     e2e = None
     if rank == 0 or world > 1:
+        from blazingsql_gb300.types import np_dtype
         host_in = []
-        dev_in = []
         h2d = 0
         for c in cols:
             hd = torch.empty(c.data.numel(), dtype=torch.uint8, pin_memory=True)
@@ -471,32 +474,18 @@ def main():
             if c.mask is not None:
                 hm = torch.empty(c.mask.numel(), dtype=torch.uint8, pin_memory=True)
                 hm.copy_(c.mask)
-            host_in.append((hd, hm))
-            dev_in.append(g.DeviceColumn(c.type_id, torch.empty_like(c.data),
-                                         None if c.mask is None else torch.empty_like(c.mask), 0, n))
-            h2d += hd.numel() + (hm.numel() if hm is not None else 0)
-        host_out = None
-        import ctypes as C
-        from blazingsql_gb300.types import np_dtype
+            host_in.append((c.type_id, hd, hm))
+            h2d += n * np_dtype(c.type_id).itemsize + (((n + 31) // 32) * 4 if hm is not None else 0)
+        hplan = g.Plan(w.schema, w.condition, w.projections)
+        otypes = hplan.output_types()
+        host_out = [(torch.empty(n * np_dtype(t).itemsize + 64, dtype=torch.uint8, pin_memory=True),
+                     torch.empty(((n + 31) // 32) * 4 + 64, dtype=torch.uint8, pin_memory=True)) for t in otypes]
+        views = [(t, hd.data_ptr(), hm.data_ptr() if hm is not None else 0, n) for t, hd, hm in host_in]
+        outs = [(hb.data_ptr(), hmk.data_ptr(), n) for hb, hmk in host_out]
 
         def e2e_step():
-            nonlocal host_out
-            for (hd, hm), d in zip(host_in, dev_in):
-                d.data.copy_(hd, non_blocking=True)
-                if hm is not None:
-                    d.mask.copy_(hm, non_blocking=True)
-            out = g.filter_project(dev_in, w.condition, w.projections, stream=stream)
-            if host_out is None:
-                host_out = [(torch.empty(n * 8 + 64, dtype=torch.uint8, pin_memory=True),
-                             torch.empty(n // 8 + 256, dtype=torch.uint8, pin_memory=True)) for _ in out]
-            d2h = 0
-            for c, (hb, hmk) in zip(out, host_out):
-                st = N.StatusInfo()
-                N.check(L.gx_column_to_host(C.byref(c._c), hb.data_ptr(), hmk.data_ptr(), stream.cuda_stream,
-                                            C.byref(st)), st)
-                d2h += c.size * np_dtype(c.type_id).itemsize + (c.size + 31) // 32 * 4
-                c.free()
-            return d2h
+            rows = hplan.execute_host(views, outs, stream=stream)
+            return sum(rows * np_dtype(t).itemsize + (rows + 31) // 32 * 4 for t in otypes)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -508,8 +497,8 @@ def main():
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
         e2e = {"value": n / (e2e_ms / 1e3) * world, "unit": "rows/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
-        del host_in, dev_in, host_out
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "gx_plan_execute_host"}
+        del host_in, host_out, hplan
 
     if rank != 0:
         if dist:

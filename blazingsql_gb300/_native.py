@@ -149,6 +149,8 @@ def lib():
     L.gx_learner_create.restype = C.c_void_p
     L.gx_learner_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64),
                                      P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
+    L.gx_plan_execute_host.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
+                                       P(StatusInfo)]
     L.gx_learner_prepare.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_void_p, P(StatusInfo)]
     L.gx_learner_execute_batches.argtypes = [C.c_void_p, P(P(ColumnView)), C.c_int, C.c_int, P(Column),
                                              P(C.c_int64), P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
@@ -178,7 +180,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_prepare", "gx_learner_save",
-    "gx_learner_execute_batches",
+    "gx_learner_execute_batches", "gx_plan_execute_host",
     "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
     "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",

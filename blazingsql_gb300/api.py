@@ -266,6 +266,36 @@ class Plan:
             return [outs[i] for i in range(n)], rows.value
         return _wrap(outs, n, s), rows.value
 
+    def execute_host(self, columns, outputs, stream=None) -> int:
+        """gx_plan_execute_host: host memory in, host memory out.
+
+        ``columns``: one (type_id, data_ptr, mask_ptr or 0, rows) per input;
+        ``outputs``: one (data_ptr, mask_ptr, capacity_rows) per output, all
+        host addresses (numpy ``ctypes.data`` or pinned torch ``data_ptr()``).
+        Returns the output row count."""
+        nc = len(columns)
+        views = (N.ColumnView * max(1, nc))()
+        for i, (t, d, m, rows) in enumerate(columns):
+            views[i].type_id = int(t)
+            views[i].data = d
+            views[i].null_mask = m or None
+            views[i].offset = 0
+            views[i].size = rows
+        n = self.num_outputs
+        outs = (N.Column * max(1, n))()
+        for j, (d, m, cap) in enumerate(outputs):
+            outs[j].data = d
+            outs[j].null_mask = m
+            outs[j].capacity = cap
+        rows = C.c_int64(0)
+        st = N.StatusInfo()
+        rc = N.lib().gx_plan_execute_host(self._h, views, nc, outs, C.byref(rows), _stream_handle(stream),
+                                          C.byref(st))
+        if rc == N.GX_ERR_CAPACITY:
+            raise N.GxError(rc, f"{st.message.decode(errors='replace')} (needed rows={rows.value})")
+        N.check(rc, st)
+        return rows.value
+
     def execute_noalloc(self, table: Table, out: Sequence[N.Column], stream=None):
         """gx_plan_execute_noalloc: runs the filter plan into the caller's buffers
         (``out``: one Column per output with data, null_mask and capacity set)

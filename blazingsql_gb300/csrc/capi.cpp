@@ -390,6 +390,29 @@ int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_
   });
 }
 
+int gx_plan_execute_host(const gx_plan* plan, const gx_column_view* host_columns, int num_columns,
+                         gx_column* host_out, int64_t* out_rows, void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!plan || !host_out) fail(GX_ERR_INVALID, "bad arguments");
+    auto cols = to_views(host_columns, num_columns);
+    // a plan of more than one kernel (over 32 outputs) runs each one in turn
+    const PlanSet& ps = *plan->ps;
+    int64_t rows = -1;
+    for (size_t c = 0; c < ps.chunks.size(); c++) {
+      int64_t r = 0;
+      try {
+        ps.chunks[c]->execute_host(cols, host_out + ps.first_output[c], &r, (cudaStream_t)stream);
+      } catch (const Error& e) {
+        if (out_rows && e.code == GX_ERR_CAPACITY) *out_rows = r;  // the count the buffers need
+        throw;
+      }
+      if (rows >= 0 && r != rows) fail(GX_ERR_CUDA, "chunks of one plan disagree on the row count");
+      rows = r;
+    }
+    if (out_rows) *out_rows = rows < 0 ? 0 : rows;
+  });
+}
+
 void gx_plan_destroy(gx_plan* plan) { delete plan; }
 
 static KernelKind kind_of(int k) {

@@ -823,4 +823,241 @@ void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_
   }
 }
 
+
+// ------------------------------------------------------------ host to host
+namespace {
+constexpr int kMaxHostChunks = 64;
+
+// Per-thread resources of host-to-host execution, made on first use and kept
+// for the thread's lifetime: a copy stream each way, an event pool, and a
+// pinned, mapped block for the chunks' row counts and the counter values.
+struct HostExecRes {
+  int device = -1;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t ev[2 * kMaxHostChunks + 2] = {};
+  unsigned long long* blk = nullptr;      // host view: [0, 64) row counts, [64, 128) counters, [128] error
+  unsigned long long* blk_dev = nullptr;  // device view
+};
+
+HostExecRes& host_exec_res() {
+  thread_local HostExecRes r;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "device");
+  if (r.device != dev) {
+    // a thread that moves to another device gets new resources (the old ones
+    // belong to the other device's context and stay with it)
+    r = HostExecRes{};
+    check_cuda(cudaStreamCreateWithFlags(&r.h2d, cudaStreamNonBlocking), "copy stream");
+    check_cuda(cudaStreamCreateWithFlags(&r.d2h, cudaStreamNonBlocking), "copy stream");
+    for (auto& e : r.ev) check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    check_cuda(cudaHostAlloc((void**)&r.blk, 2048, cudaHostAllocMapped | cudaHostAllocPortable), "pinned block");
+    check_cuda(cudaHostGetDevicePointer((void**)&r.blk_dev, r.blk, 0), "mapped block");
+    r.device = dev;
+  }
+  return r;
+}
+}  // namespace
+
+void CompiledPlan::execute_host(const std::vector<ColumnView>& hcols, gx_column* hout, int64_t* out_rows,
+                                cudaStream_t s) const {
+  if (hcols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < hcols.size(); i++) {
+    if (hcols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
+    if (hcols[i].offset != 0) fail(GX_ERR_INVALID, "host columns must start at offset 0");
+  }
+  const int nout = (int)plan_.outputs.size();
+  const int64_t n = hcols.empty() ? 0 : hcols[0].size;
+  int64_t capacity = nout ? hout[0].capacity : 0;
+  for (int j = 0; j < nout; j++) {
+    if (!hout[j].data || !hout[j].null_mask) fail(GX_ERR_INVALID, "host output buffers missing");
+    capacity = std::min<int64_t>(capacity, hout[j].capacity);
+    hout[j].type_id = plan_.outputs[j].type;
+  }
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  // device copies of the inputs
+  std::vector<size_t> in_off(hcols.size()), in_moff(hcols.size());
+  size_t in_bytes = 0;
+  const int64_t nwords = (n + 31) / 32;
+  for (size_t i = 0; i < hcols.size(); i++) {
+    in_off[i] = in_bytes;
+    in_bytes += al(std::max<size_t>(64, (size_t)n * type_size(hcols[i].type)));
+    in_moff[i] = in_bytes;
+    if (hcols[i].mask) in_bytes += al((size_t)std::max<int64_t>(nwords, 1) * 4);
+  }
+  const bool pipelined = plan_.has_filter() && can_defer() && mode_ != GX_FILTER_TWO_PASS && n > 0;
+  if (!pipelined) {
+    // whole-table form: copy in, evaluate, copy out (a plan with literal
+    // outputs or no condition, the two-pass mode, or no rows)
+    char* din = (char*)dev_alloc(std::max<size_t>(in_bytes, 64), s);
+    std::vector<gx_column> dout(nout);
+    try {
+      std::vector<ColumnView> dcols = hcols;
+      for (size_t i = 0; i < hcols.size(); i++) {
+        const size_t bytes = (size_t)n * type_size(hcols[i].type);
+        dcols[i].data = din + in_off[i];
+        if (bytes) check_cuda(cudaMemcpyAsync(din + in_off[i], hcols[i].data, bytes, cudaMemcpyHostToDevice, s), "input");
+        if (hcols[i].mask) {
+          dcols[i].mask = (const uint32_t*)(din + in_moff[i]);
+          if (nwords)
+            check_cuda(cudaMemcpyAsync(din + in_moff[i], hcols[i].mask, (size_t)nwords * 4, cudaMemcpyHostToDevice, s),
+                       "input mask");
+        }
+      }
+      int64_t rows = 0;
+      execute(dcols, dout.data(), &rows, s);
+      if (out_rows) *out_rows = rows;
+      if (rows > capacity) fail(GX_ERR_CAPACITY, "host output capacity too small");
+      for (int j = 0; j < nout; j++) {
+        const size_t bytes = (size_t)rows * type_size(dout[j].type_id);
+        if (bytes) check_cuda(cudaMemcpyAsync(hout[j].data, dout[j].data, bytes, cudaMemcpyDeviceToHost, s), "output");
+        if (rows)
+          check_cuda(cudaMemcpyAsync(hout[j].null_mask, dout[j].null_mask, (size_t)((rows + 31) / 32) * 4,
+                                     cudaMemcpyDeviceToHost, s), "output mask");
+        hout[j].size = rows;
+      }
+      check_cuda(cudaStreamSynchronize(s), "host output sync");
+    } catch (...) {
+      for (auto& c : dout)
+        if (c.data) free_column(c, s);
+      dev_free(din, s);
+      throw;
+    }
+    for (auto& c : dout) free_column(c, s);
+    dev_free(din, s);
+    return;
+  }
+  // Pipelined form: the rows are cut into chunks of whole tiles.  Chunk k's
+  // inputs go up on a copy stream, its kernel runs on `s` once they are in,
+  // and its output rows go down on the other copy stream once its row count
+  // is known, so the three overlap across chunks.  The kernels of all chunks
+  // form one tile sequence over full-size device buffers: chunk k claims the
+  // tiles [k T, (k + 1) T) from a counter that starts at k T, and its first
+  // tile's look-back finds chunk k - 1's last inclusive prefix already
+  // published, so every output row lands at its final position (and mask bit).
+  HostExecRes& R = host_exec_res();
+  const int64_t tile_rows = (int64_t)cfg_.warps * cfg_.words * 32;
+  const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
+  int64_t chunk_tiles = std::max<int64_t>((int64_t(1) << 22) / tile_rows, (ntiles + 15) / 16);
+  chunk_tiles = std::max<int64_t>(chunk_tiles, (ntiles + kMaxHostChunks - 1) / kMaxHostChunks);
+  const int64_t chunk_rows = chunk_tiles * tile_rows;
+  const int nchunks = (int)((ntiles + chunk_tiles - 1) / chunk_tiles);
+  std::vector<size_t> out_off(nout), out_moff(nout);
+  size_t total = in_bytes;
+  for (int j = 0; j < nout; j++) {
+    out_off[j] = total;
+    total += al(std::max<size_t>(64, (size_t)n * type_size(plan_.outputs[j].type)));
+  }
+  const size_t zero_from = total;  // output masks, tile statuses and the error word start zeroed
+  for (int j = 0; j < nout; j++) {
+    out_moff[j] = total;
+    total += al((size_t)mask_words_padded(n) * 4);
+  }
+  const size_t st_off = total;
+  total += al((size_t)ntiles * 8);
+  const size_t err_off = total;
+  total += 256;
+  const size_t ctr_off = total;
+  total += al((size_t)nchunks * 8);
+  char* dbase = (char*)dev_alloc(total, s);
+  unsigned long long* counts = R.blk;  // chunk k's row count after its kernel (mapped)
+  for (int k = 0; k < nchunks; k++) {
+    counts[k] = 0;
+    R.blk[64 + k] = (unsigned long long)(k * chunk_tiles);
+  }
+  R.blk[128] = 0;
+  cudaEvent_t ready = R.ev[2 * kMaxHostChunks], drained = R.ev[2 * kMaxHostChunks + 1];
+  bool launched = false;
+  int64_t rows = 0;
+  bool over = false;
+  try {
+    check_cuda(cudaMemsetAsync(dbase + zero_from, 0, ctr_off - zero_from, s), "host pipeline zero");
+    check_cuda(cudaMemcpyAsync(dbase + ctr_off, R.blk + 64, (size_t)nchunks * 8, cudaMemcpyHostToDevice, s),
+               "chunk counters");
+    check_cuda(cudaEventRecord(ready, s), "event");
+    check_cuda(cudaStreamWaitEvent(R.h2d, ready, 0), "event wait");
+    launched = true;
+    for (int k = 0; k < nchunks; k++) {
+      const int64_t r0 = k * chunk_rows, r1 = std::min<int64_t>(n, r0 + chunk_rows);
+      for (size_t i = 0; i < hcols.size(); i++) {
+        const size_t w = type_size(hcols[i].type);
+        if (w)
+          check_cuda(cudaMemcpyAsync(dbase + in_off[i] + r0 * w, (const char*)hcols[i].data + r0 * w, (r1 - r0) * w,
+                                     cudaMemcpyHostToDevice, R.h2d), "input chunk");
+        if (hcols[i].mask) {
+          const int64_t w0 = r0 / 32, w1 = (r1 + 31) / 32;
+          check_cuda(cudaMemcpyAsync(dbase + in_moff[i] + w0 * 4, hcols[i].mask + w0, (size_t)(w1 - w0) * 4,
+                                     cudaMemcpyHostToDevice, R.h2d), "input mask chunk");
+        }
+      }
+      check_cuda(cudaEventRecord(R.ev[2 * k], R.h2d), "event");
+    }
+    std::vector<bool> nb(hcols.size());
+    for (size_t i = 0; i < hcols.size(); i++) nb[i] = hcols[i].mask != nullptr;
+    const JitKernel kern = kernel(KernelKind::FUSED_FILTER, nb);
+    for (int k = 0; k < nchunks; k++) {
+      const int64_t r1 = std::min<int64_t>(n, (k + 1) * chunk_rows);
+      check_cuda(cudaStreamWaitEvent(s, R.ev[2 * k], 0), "event wait");
+      KernelArgs a{};
+      for (size_t i = 0; i < hcols.size(); i++) {
+        a.in_data[i] = dbase + in_off[i];
+        a.in_mask[i] = hcols[i].mask ? (const uint32_t*)(dbase + in_moff[i]) : nullptr;
+        a.in_off[i] = 0;
+      }
+      a.n = r1;
+      a.capacity = n;
+      a.tile_status = (uint64_t*)(dbase + st_off);
+      a.tile_counter = (unsigned long long*)(dbase + ctr_off) + k;
+      a.out_count = R.blk_dev + k;
+      a.err = (int*)(dbase + err_off);
+      a.seed = plan_.rand_seed;
+      for (int i = 0; i < 16; i++) a.order[i] = i;
+      for (int j = 0; j < nout; j++) {
+        a.out_data[j] = dbase + out_off[j];
+        a.out_mask[j] = (uint32_t*)(dbase + out_moff[j]);
+      }
+      int64_t grid = (int64_t)device_sm_count() * kern.max_blocks_per_sm;
+      grid = std::min<int64_t>(grid, std::min<int64_t>(ntiles, (k + 1) * chunk_tiles) - k * chunk_tiles);
+      launch(kern, (int)grid, s, a, true);
+      check_cuda(cudaEventRecord(R.ev[2 * k + 1], s), "event");
+    }
+    // each chunk's rows go down as soon as its count is known
+    int64_t prev = 0;
+    for (int k = 0; k < nchunks; k++) {
+      check_cuda(cudaEventSynchronize(R.ev[2 * k + 1]), "chunk sync");
+      const int64_t rk = (int64_t)((volatile unsigned long long*)counts)[k];
+      if (rk < prev) break;  // the chunk's kernel gave up (error word set): reported below
+      if (rk > capacity) over = true;
+      if (!over && rk > prev) {
+        check_cuda(cudaStreamWaitEvent(R.d2h, R.ev[2 * k + 1], 0), "event wait");
+        for (int j = 0; j < nout; j++) {
+          const size_t w = type_size(plan_.outputs[j].type);
+          check_cuda(cudaMemcpyAsync((char*)hout[j].data + prev * w, dbase + out_off[j] + prev * w,
+                                     (size_t)(rk - prev) * w, cudaMemcpyDeviceToHost, R.d2h), "output chunk");
+          const int64_t w0 = prev / 32, w1 = (rk + 31) / 32;
+          check_cuda(cudaMemcpyAsync(hout[j].null_mask + w0, dbase + out_moff[j] + w0 * 4, (size_t)(w1 - w0) * 4,
+                                     cudaMemcpyDeviceToHost, R.d2h), "output mask chunk");
+        }
+      }
+      prev = std::max(prev, rk);
+    }
+    rows = prev;
+    check_cuda(cudaEventRecord(drained, R.d2h), "event");
+    check_cuda(cudaStreamWaitEvent(s, drained, 0), "event wait");
+    check_cuda(cudaMemcpyAsync(R.blk + 128, dbase + err_off, 4, cudaMemcpyDeviceToHost, s), "error word");
+    check_cuda(cudaStreamSynchronize(s), "host pipeline sync");
+  } catch (...) {
+    if (launched) {
+      cudaStreamSynchronize(R.h2d);
+      cudaStreamSynchronize(R.d2h);
+    }
+    dev_free(dbase, s);
+    throw;
+  }
+  dev_free(dbase, s);
+  if ((int)R.blk[128] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  if (out_rows) *out_rows = rows;
+  if (over) fail(GX_ERR_CAPACITY, "host output capacity too small");
+  for (int j = 0; j < nout; j++) hout[j].size = rows;
+}
+
 }  // namespace gx

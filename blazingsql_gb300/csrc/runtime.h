@@ -94,6 +94,13 @@ class CompiledPlan {
   void enqueue_filter(const std::vector<ColumnView>& cols, gx_column* out, unsigned long long* hdr,
                       uint64_t* tile_status, const ExecExtras* extras, cudaStream_t s) const;
   void finish_queued(const unsigned long long* hdr, int64_t n, gx_column* out, int64_t* out_rows) const;
+  // Host-to-host execution: `cols` and out[j].data / null_mask are host
+  // memory (inputs at offset 0; pinned memory gives full copy bandwidth),
+  // out[j].capacity the rows the host buffers hold.  A filter plan without
+  // literal outputs runs as a pipeline of row chunks whose copies in, kernels
+  // and copies out overlap; other plans copy in, run and copy out.  Returns
+  // after the outputs are in host memory.
+  void execute_host(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const;
   // a filter plan whose outputs are all computed per row (none a literal)
   bool can_defer() const;
   // tile-status words a filter over n rows uses

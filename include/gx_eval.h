@@ -189,6 +189,25 @@ int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_
 int gx_plan_execute_noalloc(const gx_plan* plan, const gx_column_view* columns, int num_columns,
                             gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
 
+/* Runs the plan from host memory to host memory.  No counterpart in the
+ * reference, whose tables are already on the device when the evaluator runs.
+ *
+ * columns[i].data / null_mask are host pointers (offset 0; pinned memory
+ * gives the full copy bandwidth, pageable memory works at a lower rate);
+ * out[i].data / null_mask are caller host buffers holding out[i].capacity
+ * rows (null_mask: (capacity + 31) / 32 words).  A filter plan whose outputs
+ * are all computed per row runs as a pipeline of row chunks (at least 2^22
+ * rows, at most 64 chunks): each chunk's inputs are copied up on one copy
+ * stream, its kernel runs on `stream` once they are in, and its output rows
+ * are copied down on another copy stream as soon as its row count is known,
+ * so copies in, kernels and copies out overlap.  Other plans copy in, run and
+ * copy out.  Returns once the outputs are in host memory; GX_ERR_CAPACITY (and
+ * the needed count in *out_rows) when the host buffers are too small.
+ * Per-thread copy streams and a small pinned block are made on a thread's
+ * first call and kept. */
+int gx_plan_execute_host(const gx_plan* plan, const gx_column_view* columns, int num_columns,
+                         gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
+
 void gx_plan_destroy(gx_plan* plan);
 
 /* ---- batch runner: many batches, one persistent launch (no counterpart in
