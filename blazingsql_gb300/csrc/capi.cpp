@@ -52,6 +52,7 @@ KernelConfig default_config() {
   c.warps = env_int("GX_WARPS", 4);
   c.words = env_int("GX_WORDS", 4);
   c.emulate_fp64 = env_int("GX_NATIVE_FP64", 0) == 0;
+  c.native_f64_ops = env_int("GX_NATIVE_F64_OPS", -1);
   c.dense = env_int("GX_DENSE", 1) != 0;
   c.lazy_case = env_int("GX_LAZY_CASE", 1) != 0;
   return c;
@@ -162,7 +163,8 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
     k += '\x1f';
   }
   k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
-       std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case);
+       std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case) + ':' +
+       std::to_string(cfg.native_f64_ops);
   return k;
 }
 

@@ -254,22 +254,24 @@ class Gen {
   // operand as a double value (native FP64 arithmetic follows)
   std::string asD(int id) const {
     if (kind_f(id)) return "gx_D(" + B(id) + ")";
-    return cfg_.emulate_fp64 ? "gx_D(gxe_i2d((i64)(" + B(id) + ")))" : "gx_I2D(" + B(id) + ")";
+    return emu_op(kNativeConvert) ? "gx_D(gxe_i2d((i64)(" + B(id) + ")))" : "gx_I2D(" + B(id) + ")";
   }
   // operand as the bits of its double value (integer-pipe binary64 routines follow)
   std::string asDB(int id) const {
     if (kind_f(id)) return B(id);
-    return cfg_.emulate_fp64 ? "gxe_i2d((i64)(" + B(id) + "))" : "gx_B(gx_I2D(" + B(id) + "))";
+    return emu_op(kNativeConvert) ? "gxe_i2d((i64)(" + B(id) + "))" : "gx_B(gx_I2D(" + B(id) + "))";
   }
   std::string asI(int id) const {
     if (!kind_f(id)) return "(i64)(" + B(id) + ")";
-    return cfg_.emulate_fp64 ? "gxe_d2ll(" + B(id) + ")" : "gx_D2LL(gx_D(" + B(id) + "))";
+    return emu_op(kNativeConvert) ? "gxe_d2ll(" + B(id) + ")" : "gx_D2LL(gx_D(" + B(id) + "))";
   }
   std::string nz(int id) const {
     if (!kind_f(id)) return "(" + B(id) + " != 0ull)";
-    return cfg_.emulate_fp64 ? "gxe_nz(" + B(id) + ")" : "(gx_D(" + B(id) + ") != 0.0)";
+    return emu_op(kNativeCompare) ? "gxe_nz(" + B(id) + ")" : "(gx_D(" + B(id) + ") != 0.0)";
   }
   bool emu() const { return cfg_.emulate_fp64; }
+  // this class of binary64 operation runs on the integer pipes
+  bool emu_op(int cls) const { return cfg_.emulate_fp64 && !(cfg_.native_f64_ops & cls); }
 
   // a valid literal's value as binary64 bits (integer literals converted exactly
   // as the kernels convert them)
@@ -334,8 +336,8 @@ class Gen {
           break;
         case OP_IS_NULL: r = "(u64)(!" + XV + ")"; always_valid = true; break;
         case OP_IS_NOT_NULL: r = "(u64)(" + XV + ")"; always_valid = true; break;
-        case OP_FLOOR: r = emu() ? "gxe_floor(" + asDB(x) + ")" : "gx_B(floor(" + asD(x) + "))"; break;
-        case OP_CEIL: r = emu() ? "gxe_ceil(" + asDB(x) + ")" : "gx_B(ceil(" + asD(x) + "))"; break;
+        case OP_FLOOR: r = emu_op(kNativeRound) ? "gxe_floor(" + asDB(x) + ")" : "gx_B(floor(" + asD(x) + "))"; break;
+        case OP_CEIL: r = emu_op(kNativeRound) ? "gxe_ceil(" + asDB(x) + ")" : "gx_B(ceil(" + asD(x) + "))"; break;
         case OP_SIN: r = "gx_B(sin(" + asD(x) + "))"; break;
         case OP_COS: r = "gx_B(cos(" + asD(x) + "))"; break;
         case OP_ASIN: r = "gx_B(asin(" + asD(x) + "))"; break;
@@ -416,7 +418,7 @@ class Gen {
         return;
       case OP_IS_NOT_DISTINCT_FROM: {
         const std::string eq = !anyf ? "(" + X + " == " + Y + ")"
-                               : emu() ? "gxe_eq(" + asDB(x) + ", " + asDB(y) + ")"
+                               : emu_op(kNativeCompare) ? "gxe_eq(" + asDB(x) + ", " + asDB(y) + ")"
                                        : "(" + asD(x) + " == " + asD(y) + ")";
         o << ind << b << " = (u64)((!" << XV << " && !" << YV << ") || (" << XV << " && " << YV << " && " << eq
           << "));\n";
@@ -435,7 +437,7 @@ class Gen {
         };
         return std::string("(u64)(") + to_ns(x, lt) + " " + opstr + " " + to_ns(y, rt) + ")";
       }
-      if (anyf && emu()) {
+      if (anyf && emu_op(kNativeCompare)) {
         const std::string X2 = asDB(x), Y2 = asDB(y), o2 = opstr;
         if (o2 == "<") return "(u64)gxe_lt(" + X2 + ", " + Y2 + ")";
         if (o2 == ">") return "(u64)gxe_lt(" + Y2 + ", " + X2 + ")";
@@ -451,25 +453,25 @@ class Gen {
       case OP_AND: r = "(u64)(" + nz(x) + " && " + nz(y) + ")"; break;
       case OP_ADD:
         r = !anyf ? "(" + X + " + " + Y + ")"
-            : emu() ? "gxe_add(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " + " + asD(y) + ")";
+            : emu_op(kNativeAddSub) ? "gxe_add(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " + " + asD(y) + ")";
         break;
       case OP_SUB:
         r = !anyf ? "(" + X + " - " + Y + ")"
-            : emu() ? "gxe_sub(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " - " + asD(y) + ")";
+            : emu_op(kNativeAddSub) ? "gxe_sub(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " - " + asD(y) + ")";
         break;
       case OP_MUL:
         r = !anyf ? "(" + X + " * " + Y + ")"
-            : emu() ? "gxe_mul(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " * " + asD(y) + ")";
+            : emu_op(kNativeMul) ? "gxe_mul(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " * " + asD(y) + ")";
         break;
       case OP_DIV:
-        if (anyf && emu() && const_divisor(y)) {
+        if (anyf && emu_op(kNativeDiv) && const_divisor(y)) {
           // constant divisor: its fixed-point reciprocal is computed here
           const uint64_t db = literal_double_bits(y);
           r = "gxe_div_r(" + asDB(x) + ", " + hex64(db) + ", " +
               hex64(gxe_recip_fixed((db & GXE_FRAC) | GXE_HIDDEN)) + ")";
         } else {
           r = !anyf ? "gx_div_ii(" + X + ", " + Y + ")"
-              : emu() ? "gxe_div(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " / " + asD(y) + ")";
+              : emu_op(kNativeDiv) ? "gxe_div(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " / " + asD(y) + ")";
         }
         vv = "(" + vv + " && " + (rf ? nz(y) : "(i64)(" + Y + ") != 0LL") + ")";
         break;
@@ -1518,7 +1520,33 @@ std::vector<int> conjunct_columns(const Plan& p, int c) {
   return std::vector<int>(cols.begin(), cols.end());
 }
 
-std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg, const std::string& name) {
+// Which binary64 operation classes go to the FP64 pipe when the plan leaves it
+// to the library.  Both forms are exact; the choice balances the two pipes.
+// Add, subtract and multiply cost about as much natively (one FP64-pipe
+// instruction, at 1/64 of the FP32 rate) as emulated (about 25 integer
+// instructions), so moving them to the otherwise idle FP64 pipe frees the
+// integer pipes.  Conversions and compares follow when the plan has no
+// transcendental (LN / EXP / trigonometric / POWER / ROUND, which already
+// load the FP64 pipe).  Division stays emulated: natively it is a reciprocal
+// and Newton steps, several FP64-pipe instructions.  Measured on GB300:
+// 19 % on the deep plan (with LN / EXP), 10 % on the plain filter + divide.
+int auto_native_f64_ops(const Plan& p) {
+  bool transcendental = false;
+  for (const auto& n : p.nodes)
+    if (n.kind == Node::OP) switch (n.op) {
+        case OP_SIN: case OP_COS: case OP_ASIN: case OP_ACOS: case OP_TAN: case OP_COTAN: case OP_ATAN:
+        case OP_LN: case OP_LOG10: case OP_EXP: case OP_POW: case OP_ROUND:
+          transcendental = true;
+          break;
+        default: break;
+      }
+  return transcendental ? (kNativeAddSub | kNativeMul)
+                        : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare);
+}
+
+std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg_in, const std::string& name) {
+  KernelConfig cfg = cfg_in;
+  if (cfg.native_f64_ops < 0) cfg.native_f64_ops = auto_native_f64_ops(p);
   Gen g(p, cfg);
   std::ostringstream o;
   emit_prelude(o, cfg);

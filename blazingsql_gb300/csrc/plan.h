@@ -45,10 +45,17 @@ struct OutSpec {
   uint64_t lit_bits_as_element() const;
 };
 
+constexpr int kNativeAddSub = 1, kNativeMul = 2, kNativeConvert = 4, kNativeCompare = 8, kNativeRound = 16,
+              kNativeDiv = 32;
+
 struct KernelConfig {
   int warps = 8;           // warps per CTA
   int words = 2;           // 32-row words per warp per step
   bool emulate_fp64 = true;  // binary64 compares / divides / conversions on the integer pipes
+  // with emulate_fp64, operation classes that still use the FP64 pipe (both
+  // forms are exact IEEE binary64): kNativeAddSub, kNativeMul, kNativeConvert,
+  // kNativeCompare, kNativeRound, kNativeDiv; -1: chosen per plan
+  int native_f64_ops = -1;
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
   bool lazy_case = true;     // dense phase: expensive CASE branches only for the rows that select them
   bool runtime_order = false;  // short-circuit AND conjuncts in the order given at launch (KernelArgs::order)
