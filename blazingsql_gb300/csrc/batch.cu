@@ -171,6 +171,7 @@ std::shared_ptr<CompiledPlan> BatchRunner::variant(int warps, int words) {
     KernelConfig c = base_cfg_;
     c.warps = warps;
     c.words = words;
+    c.tune_shape = false;  // the runner tunes its own shape
     v = std::make_shared<CompiledPlan>(plan_, c, GX_FILTER_SINGLE_PASS);
   }
   return v;
@@ -294,7 +295,7 @@ void BatchRunner::tune(const std::vector<std::vector<ColumnView>>& batches, gx_c
     tuned_ = true;
     return;
   }
-  static const int cand[][2] = {{4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}};
+  static const int cand[][2] = {{4, 2}, {4, 4}, {4, 8}, {8, 2}, {8, 4}, {2, 8}, {1, 16}};
   float best = 1e30f;
   cudaEvent_t e0, e1;
   check_cuda(cudaEventCreate(&e0), "event");

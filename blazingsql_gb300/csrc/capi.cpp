@@ -51,6 +51,7 @@ KernelConfig default_config() {
   KernelConfig c;
   c.warps = env_int("GX_WARPS", 4);
   c.words = env_int("GX_WORDS", 4);
+  c.tune_shape = !std::getenv("GX_WARPS") && !std::getenv("GX_WORDS");
   c.emulate_fp64 = env_int("GX_NATIVE_FP64", 0) == 0;
   c.native_f64_ops = env_int("GX_NATIVE_F64_OPS", -1);
   c.dense = env_int("GX_DENSE", 1) != 0;
@@ -358,6 +359,7 @@ gx_plan* gx_plan_compile(const int32_t* column_types, const uint8_t* column_null
     KernelConfig cfg = default_config();
     if (o.block_threads > 0) cfg.warps = o.block_threads / 32;
     if (o.words_per_warp > 0) cfg.words = o.words_per_warp;
+    if (o.block_threads > 0 || o.words_per_warp > 0) cfg.tune_shape = false;
     cfg.short_circuit = o.short_circuit != 0;
     for (int i = 0; i < o.num_conjuncts && i < 16; i++) {
       if (o.conjunct_order[i] < 0 || o.conjunct_order[i] >= 16) fail(GX_ERR_INVALID, "conjunct order index out of range");

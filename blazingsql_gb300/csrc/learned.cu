@@ -601,6 +601,7 @@ static std::shared_ptr<CompiledPlan> variant(const CompiledPlan& base, int mode,
                                              int words = 0) {
   KernelConfig c = base.config();
   if (words > 0) c.words = words;
+  c.tune_shape = false;  // the learner's variants keep one shape
   c.short_circuit = false;
   c.conjunct_order.clear();
   c.conj_stats = stats;

@@ -64,6 +64,9 @@ struct KernelConfig {
   bool conj_stats = false;     // COUNT_FILTER also counts each conjunct's passing rows
   bool short_circuit = false;
   std::vector<int> conjunct_order;  // indices into Plan::conjuncts
+  // single-pass filter calls choose the block shape online among a few
+  // candidates (the shape is not fixed by the caller or the environment)
+  bool tune_shape = false;
 };
 
 struct Plan {

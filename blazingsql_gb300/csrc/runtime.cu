@@ -398,10 +398,51 @@ static const char* kind_name(KernelKind k) {
   }
 }
 
-JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable) const {
+// Candidate block shapes (warps x words) of a tuned single-pass filter: the
+// first is used until the others have been measured.  Measured on GB300: the
+// deep C2 plan is fastest at 4 x 8, the light C1 / C5 plans at 1 x 16 (no
+// block barrier between warps, more blocks per SM) or 2 x 8.
+static const CompiledPlan::Shape kShapes[] = {{4, 8}, {1, 16}, {2, 8}};
+static constexpr int kNumShapes = 3;
+
+CompiledPlan::Shape CompiledPlan::filter_shape(int64_t n, int* explore) const {
+  *explore = -1;
+  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words};
+  std::lock_guard<std::mutex> g(tmu_);
+  if (chosen_ >= 0) return kShapes[chosen_];
+  if (cand_ms_.empty()) cand_ms_.assign(kNumShapes, -1.f);
+  if (n >= kShapeTuneRows && next_cand_ < kNumShapes) {
+    *explore = next_cand_++;
+    return kShapes[*explore];
+  }
+  return kShapes[0];
+}
+
+CompiledPlan::Shape CompiledPlan::current_shape() const {
+  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words};
+  std::lock_guard<std::mutex> g(tmu_);
+  return chosen_ >= 0 ? kShapes[chosen_] : kShapes[0];
+}
+
+void CompiledPlan::shape_measured(int idx, float ms) const {
+  std::lock_guard<std::mutex> g(tmu_);
+  if (idx < 0 || idx >= (int)cand_ms_.size()) return;
+  cand_ms_[idx] = ms;
+  int best = -1;
+  for (int i = 0; i < kNumShapes; i++) {
+    if (cand_ms_[i] < 0) return;  // not all measured yet
+    if (best < 0 || cand_ms_[i] < cand_ms_[best]) best = i;
+  }
+  chosen_ = best;
+}
+
+JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable, int warps, int words) const {
+  if (warps <= 0) warps = cfg_.warps;
+  if (words <= 0) words = cfg_.words;
   int dev = 0;
   check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-  std::string key = std::to_string((int)kind) + ":" + std::to_string(dev) + ":";
+  std::string key = std::to_string((int)kind) + ":" + std::to_string(dev) + ":" + std::to_string(warps) + "x" +
+                    std::to_string(words) + ":";
   for (bool b : nullable) key += b ? '1' : '0';
   {
     std::lock_guard<std::mutex> g(kmu_);
@@ -410,9 +451,12 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
   }
   Plan p = plan_;
   p.nullable = nullable;
+  KernelConfig c = cfg_;
+  c.warps = warps;
+  c.words = words;
   const std::string name = kind_name(kind);
-  const std::string src = generate_kernel(p, kind, cfg_, name);
-  const JitKernel k = jit_get(src, name, cfg_.warps * 32);
+  const std::string src = generate_kernel(p, kind, c, name);
+  const JitKernel k = jit_get(src, name, warps * 32);
   std::lock_guard<std::mutex> g(kmu_);
   kcache_[key] = k;
   return k;
@@ -634,10 +678,16 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   const int nout = (int)plan_.outputs.size();
   const int64_t nwords = (n + 31) / 32;
-  const int64_t tile_words = (int64_t)cfg_.warps * cfg_.words;
+  const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
+  // the single-pass fused kernel's block shape (tuned online when allowed)
+  int explore = -1;
+  Shape sh{cfg_.warps, cfg_.words};
+  if (!two_pass && !(cfg_.staged && cfg_.runtime_order)) sh = filter_shape(n, &explore);
+  const int64_t tile_words = (int64_t)sh.warps * sh.words;
   const int64_t ntiles = (nwords + tile_words - 1) / tile_words;
   std::vector<gx_column> made;
   void* scratch = nullptr;
+  cudaEvent_t te0 = nullptr, te1 = nullptr;
   try {
     if (n == 0) {
       for (int j = 0; j < nout; j++) {
@@ -653,7 +703,6 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     }
     // scratch: [0] tile counter, [1] out count, [2] err (int), [3] total, then per-tile status
     const size_t sbytes = (size_t)(4 + ntiles) * 8;
-    const bool two_pass = mode_ == GX_FILTER_TWO_PASS;
     int64_t capacity = n;
     if (extras && extras->capacity_hint >= 0 && extras->capacity_hint < n) capacity = extras->capacity_hint;
     // single pass into library outputs: scratch and outputs in one arena, one
@@ -726,16 +775,29 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     a.capacity = capacity;
     KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER;
     if (!two_pass && cfg_.staged && cfg_.runtime_order && staging_aligned(plan_, cols)) kind = KernelKind::FUSED_STAGED;
-    const JitKernel k = kernel(kind, nb);
+    const JitKernel k = two_pass ? kernel(kind, nb) : kernel(kind, nb, sh.warps, sh.words);
     int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
     if (grid > ntiles) grid = ntiles;
     last.grid = (int)grid;
     last.block = k.block_threads;
     last.regs = k.num_regs;
     last.tiles = ntiles;
+    if (explore >= 0) {
+      check_cuda(cudaEventCreate(&te0), "event");
+      check_cuda(cudaEventCreate(&te1), "event");
+      check_cuda(cudaEventRecord(te0, s), "event record");
+    }
     launch(k, (int)grid, s, a, true);
+    if (explore >= 0) check_cuda(cudaEventRecord(te1, s), "event record");
     check_cuda(cudaMemcpyAsync(host_hdr, hdr, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
     check_cuda(cudaStreamSynchronize(s), "filter sync");
+    if (explore >= 0) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, te0, te1) == cudaSuccess) shape_measured(explore, ms);
+      cudaEventDestroy(te0);
+      cudaEventDestroy(te1);
+      te0 = te1 = nullptr;
+    }
     if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
     const int64_t rows = two_pass ? (int64_t)host_hdr[3] : (int64_t)host_hdr[1];
     if (out_rows) *out_rows = rows;
@@ -751,6 +813,8 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     dev_free(scratch, s);
     scratch = nullptr;
   } catch (...) {
+    if (te0) cudaEventDestroy(te0);
+    if (te1) cudaEventDestroy(te1);
     if (scratch) dev_free(scratch, s);
     for (auto& c : made) free_column(c, s);
     throw;
@@ -935,7 +999,8 @@ void CompiledPlan::execute_host(const std::vector<ColumnView>& hcols, gx_column*
   // tile's look-back finds chunk k - 1's last inclusive prefix already
   // published, so every output row lands at its final position (and mask bit).
   HostExecRes& R = host_exec_res();
-  const int64_t tile_rows = (int64_t)cfg_.warps * cfg_.words * 32;
+  const Shape sh = current_shape();
+  const int64_t tile_rows = (int64_t)sh.warps * sh.words * 32;
   const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
   int64_t chunk_tiles = std::max<int64_t>((int64_t(1) << 22) / tile_rows, (ntiles + 15) / 16);
   chunk_tiles = std::max<int64_t>(chunk_tiles, (ntiles + kMaxHostChunks - 1) / kMaxHostChunks);
@@ -993,7 +1058,7 @@ void CompiledPlan::execute_host(const std::vector<ColumnView>& hcols, gx_column*
     }
     std::vector<bool> nb(hcols.size());
     for (size_t i = 0; i < hcols.size(); i++) nb[i] = hcols[i].mask != nullptr;
-    const JitKernel kern = kernel(KernelKind::FUSED_FILTER, nb);
+    const JitKernel kern = kernel(KernelKind::FUSED_FILTER, nb, sh.warps, sh.words);
     for (int k = 0; k < nchunks; k++) {
       const int64_t r1 = std::min<int64_t>(n, (k + 1) * chunk_rows);
       check_cuda(cudaStreamWaitEvent(s, R.ev[2 * k], 0), "event wait");

@@ -71,6 +71,11 @@ struct ExecStats {
 
 class CompiledPlan {
  public:
+  struct Shape {
+    int warps, words;  // block shape of a filter kernel: warps x 32-row words per warp
+  };
+  // the single-pass filter's block shape now: the tuned one once chosen
+  Shape current_shape() const;
   CompiledPlan(Plan p, KernelConfig cfg, int mode) : plan_(std::move(p)), cfg_(std::move(cfg)), mode_(mode) {}
 
   // Fused single-pass filter into the caller's buffers (out[j].data / null_mask /
@@ -115,7 +120,19 @@ class CompiledPlan {
   mutable ExecStats last;
 
  private:
-  JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable) const;
+  // warps / words: a block shape other than the configured one (0: configured)
+  JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable, int warps = 0, int words = 0) const;
+  // Block shape of a single-pass filter call over n rows.  With tune_shape,
+  // calls of at least kShapeTuneRows rows first run each candidate once
+  // (*explore = its index; the caller reports its time to shape_measured),
+  // then every call takes the fastest.
+  Shape filter_shape(int64_t n, int* explore) const;
+  void shape_measured(int idx, float ms) const;
+  static constexpr int64_t kShapeTuneRows = int64_t(1) << 22;
+  mutable std::mutex tmu_;
+  mutable std::vector<float> cand_ms_;  // per candidate, < 0 until measured
+  mutable int next_cand_ = 0;
+  mutable int chosen_ = -1;
   void run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs, cudaStream_t s) const;
   void run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, bool caller_bufs,
                   const ExecExtras* extras,

@@ -113,7 +113,7 @@ def test_column_offsets(gpu, ora):
 
 
 @pytest.mark.parametrize("mode", [N.GX_FILTER_TWO_PASS, N.GX_FILTER_SINGLE_PASS])
-@pytest.mark.parametrize("words,warps", [(1, 4), (2, 8), (4, 8), (8, 4)])
+@pytest.mark.parametrize("words,warps", [(1, 4), (2, 8), (4, 8), (8, 4), (8, 2), (16, 1)])
 def test_filter_modes_and_tiles(ora, mode, words, warps):
     n = 50_001
     cols = W.host_columns("c2", n, seed=21)
@@ -188,3 +188,23 @@ def test_plan_reuse_across_batches(ora):
         out, rows = p.execute(cols)
         exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
         assert_tables_equal([c.to_host() for c in out], exp, what=f"batch {n}")
+
+
+def test_online_shape_tuning_same_rows(ora):
+    """The first large single-pass calls of a plan each run another block
+    shape (timed) before the plan settles on the fastest: every call returns
+    the same bytes, and the oracle's rows."""
+    n = (1 << 22) + 77
+    cols = W.host_columns("c1", n, seed=31)
+    from blazingsql_gb300.api import DeviceColumn
+    dev = [DeviceColumn.from_host(c) for c in cols]
+    p = g.Plan(W.workload("c1").schema, W.C1_CONDITION, W.C1_PROJECTIONS)
+    outs = []
+    for _ in range(5):
+        out, rows = p.execute(dev)
+        outs.append(([c.to_host() for c in out], rows))
+    for got, rows in outs[1:]:
+        assert rows == outs[0][1]
+        assert_tables_equal(got, outs[0][0])
+    exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
+    assert_tables_equal(outs[-1][0], exp)
