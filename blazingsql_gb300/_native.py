@@ -26,6 +26,7 @@ GX_ERR_CAPACITY = 8
 GX_NOALLOC_MAX_TILES = 524284
 GX_NOALLOC_MAX_ROWS = GX_NOALLOC_MAX_TILES * 512
 
+GX_AGG_SUM, GX_AGG_SUM0, GX_AGG_MIN, GX_AGG_MAX, GX_AGG_COUNT_VALID, GX_AGG_COUNT_ALL, GX_AGG_MEAN = range(7)
 GX_FILTER_AUTO = 0
 GX_FILTER_TWO_PASS = 1
 GX_FILTER_SINGLE_PASS = 2
@@ -149,6 +150,11 @@ def lib():
     L.gx_learner_create.restype = C.c_void_p
     L.gx_learner_execute.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64),
                                      P(LearnedBatchInfo), C.c_void_p, P(StatusInfo)]
+    L.gx_filter_aggregate.argtypes = [P(ColumnView), C.c_int, C.c_char_p, P(C.c_int), C.c_int, P(C.c_char_p),
+                                      P(C.c_int), C.c_int, P(Column), P(C.c_int64), C.c_void_p, P(StatusInfo)]
+    L.gx_debug_aggregate_check.argtypes = [P(C.c_int32), P(C.c_uint8), C.c_int, C.c_char_p, P(C.c_int), C.c_int,
+                                           P(C.c_char_p), P(C.c_int), C.c_int, P(C.c_int32), P(C.c_int32),
+                                           P(C.c_int32), P(StatusInfo)]
     L.gx_plan_execute_host.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
                                        P(StatusInfo)]
     L.gx_learner_prepare.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_void_p, P(StatusInfo)]
@@ -180,7 +186,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_prepare", "gx_learner_save",
-    "gx_learner_execute_batches", "gx_plan_execute_host",
+    "gx_learner_execute_batches", "gx_plan_execute_host", "gx_filter_aggregate", "gx_debug_aggregate_check",
     "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
     "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",

@@ -568,6 +568,45 @@ def mlp_grad(F: int, H: int, O: int, params, X, Y):
     return grad, float(loss[0]), z
 
 
+def filter_aggregate(table: Table, condition: Optional[str], group_columns: Sequence[int],
+                     aggregations: Sequence[Tuple[int, str]], stream=None) -> Tuple[List[NativeColumn], int]:
+    """gx_filter_aggregate: the group-by aggregation of the rows passing
+    ``condition``; ``aggregations`` holds (GX_AGG_* kind, input expression or
+    "" for COUNT(*)).  Returns (keys then aggregation columns, groups); groups
+    come in no particular order."""
+    keep: list = []
+    views, nc = _views(table, keep)
+    s = _stream_handle(stream)
+    nk, na = len(group_columns), len(aggregations)
+    keys = (C.c_int * max(1, nk))(*group_columns)
+    inputs = (C.c_char_p * max(1, na))(*[e.encode() for _, e in aggregations])
+    kinds = (C.c_int * max(1, na))(*[k for k, _ in aggregations])
+    outs = (N.Column * (nk + na))()
+    groups = C.c_int64(0)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_filter_aggregate(views, nc, condition.encode() if condition else None, keys, nk, inputs,
+                                        kinds, na, outs, C.byref(groups), s, C.byref(st)), st)
+    return _wrap(outs, nk + na, s), groups.value
+
+
+def aggregate_check(schema: Sequence[int], has_mask: Sequence[bool], condition: Optional[str],
+                    group_columns: Sequence[int], aggregations: Sequence[Tuple[int, str]]):
+    """gx_debug_aggregate_check: builds and NVRTC-compiles the aggregation
+    kernel (no GPU needed); returns (registers, spill bytes, shared bytes)."""
+    nc, nk, na = len(schema), len(group_columns), len(aggregations)
+    types = (C.c_int32 * max(1, nc))(*[int(t) for t in schema])
+    masks = (C.c_uint8 * max(1, nc))(*[1 if m else 0 for m in has_mask])
+    keys = (C.c_int * max(1, nk))(*group_columns)
+    inputs = (C.c_char_p * max(1, na))(*[e.encode() for _, e in aggregations])
+    kinds = (C.c_int * max(1, na))(*[k for k, _ in aggregations])
+    r, sp, sh = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_debug_aggregate_check(types, masks, nc, condition.encode() if condition else None, keys, nk,
+                                             inputs, kinds, na, C.byref(r), C.byref(sp), C.byref(sh),
+                                             C.byref(st)), st)
+    return r.value, sp.value, sh.value
+
+
 def free_columns(cols: Sequence[NativeColumn], stream=None) -> None:
     """Releases library-owned output columns with one gx_free_columns call."""
     live = [c for c in cols if c._c.data]

@@ -14,6 +14,7 @@
 #include "frontend.h"
 #include "plan.h"
 #include "runtime.h"
+#include "aggregate.h"
 
 namespace gx {
 namespace {
@@ -314,6 +315,76 @@ int gx_filter_project(const gx_column_view* columns, int num_columns, const char
     for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
     auto ps = plan_for("fused", cols, cond, ex, true);
     ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+  });
+}
+
+static std::shared_ptr<AggPlan> agg_plan_for(const std::vector<int>& schema, const std::vector<bool>& nullable,
+                                             const char* condition, const int* group_columns, int nk,
+                                             const char* const* agg_inputs, const int* agg_kinds, int na) {
+  if (nk < 0 || na <= 0 || (nk > 0 && !group_columns) || !agg_inputs || !agg_kinds)
+    fail(GX_ERR_INVALID, "bad aggregation arguments");
+  std::string cond = condition ? std::string(condition) : std::string();
+  if (!cond.empty()) cond = preprocess_expression(cond, schema);
+  std::vector<int> keys(group_columns, group_columns + nk);
+  std::vector<std::string> inputs;
+  std::vector<int> kinds(agg_kinds, agg_kinds + na);
+  for (int i = 0; i < na; i++) {
+    const std::string e = agg_inputs[i] ? std::string(agg_inputs[i]) : std::string();
+    inputs.push_back(e.empty() ? e : preprocess_expression(e, schema));
+  }
+  const KernelConfig cfg = default_config();
+  std::string key;
+  for (size_t i = 0; i < schema.size(); i++) key += std::to_string(schema[i]) + (nullable[i] ? "n," : "-,");
+  key += "|" + cond + "|";
+  for (int c : keys) key += std::to_string(c) + ",";
+  key += "|";
+  for (int i = 0; i < na; i++) key += std::to_string(kinds[i]) + ":" + inputs[i] + "\x1f";
+  key += "|" + std::to_string(cfg.warps) + ":" + std::to_string(cfg.words) + ":" + std::to_string(cfg.native_f64_ops);
+  static std::mutex mu;
+  static std::unordered_map<std::string, std::shared_ptr<AggPlan>> plans;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    auto it = plans.find(key);
+    if (it != plans.end()) return it->second;
+  }
+  auto p = std::make_shared<AggPlan>(schema, nullable, cond, keys, inputs, kinds, cfg);
+  std::lock_guard<std::mutex> g(mu);
+  if (plans.size() > 256) plans.clear();
+  plans[key] = p;
+  return p;
+}
+
+int gx_filter_aggregate(const gx_column_view* columns, int num_columns, const char* condition,
+                        const int* group_columns, int num_group_columns, const char* const* agg_inputs,
+                        const int* agg_kinds, int num_aggs, gx_column* out, int64_t* out_groups, void* stream,
+                        gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!out) fail(GX_ERR_INVALID, "null output array");
+    auto cols = to_views(columns, num_columns);
+    std::vector<bool> nullable;
+    for (const auto& c : cols) nullable.push_back(c.mask != nullptr);
+    auto ap = agg_plan_for(schema_of(cols), nullable, condition, group_columns, num_group_columns, agg_inputs,
+                           agg_kinds, num_aggs);
+    for (int i = 0; i < ap->num_outputs(); i++) out[i] = gx_column{};
+    ap->execute(cols, out, out_groups, (cudaStream_t)stream);
+  });
+}
+
+int gx_debug_aggregate_check(const int32_t* column_types, const uint8_t* column_has_mask, int num_columns,
+                             const char* condition, const int* group_columns, int num_group_columns,
+                             const char* const* agg_inputs, const int* agg_kinds, int num_aggs, int32_t* registers,
+                             int32_t* spill_bytes, int32_t* shared_bytes, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (num_columns < 0 || (num_columns > 0 && !column_types)) fail(GX_ERR_INVALID, "bad column types");
+    std::vector<int> schema(column_types, column_types + num_columns);
+    std::vector<bool> nullable;
+    for (int i = 0; i < num_columns; i++) nullable.push_back(column_has_mask ? column_has_mask[i] != 0 : true);
+    auto ap = agg_plan_for(schema, nullable, condition, group_columns, num_group_columns, agg_inputs, agg_kinds,
+                           num_aggs);
+    const KernelResources r = jit_resources(ap->kernel_source(nullable), "gx_filter_aggregate");
+    if (registers) *registers = r.registers;
+    if (spill_bytes) *spill_bytes = r.spill_bytes;
+    if (shared_bytes) *shared_bytes = r.shared_bytes;
   });
 }
 

@@ -374,3 +374,70 @@ struct GxBitWriter {
     if (fill > 0 && (threadIdx.x & 31) == 0) atomicOr(mask + word, (u32)acc);
   }
 };
+
+// ---------------------------------------------------------------- aggregation
+// Global group table of the fused filter + aggregate kernel (structure of
+// arrays over `cap` slots, cap a power of two).  A slot's state goes 0 (empty)
+// -> 1 (claimed, keys being written) -> 2 (keys published).
+struct GxAggArgs {
+  u32* state;
+  u32* nullm;                  // key null bits per slot
+  u64* keys;                   // [key][cap]
+  u64* acc;                    // [aggregation][cap]: sum bits / ordered min-max
+  u64* cnt;                    // [aggregation][cap]: valid inputs
+  u64* rows;                   // [cap]: rows per group
+  u64 cap;
+  int* overflow;               // set when a probe walked the whole table
+  int* err;                    // set when a wait on a claimed slot gave up
+  unsigned long long* groups;  // slots claimed
+};
+
+__device__ __forceinline__ u64 gx_mix64(u64 x) {
+  // splitmix64 finaliser
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+// binary64 bits -> a signed integer with the same order (min / max through
+// integer atomics); the map is its own inverse
+__device__ __forceinline__ long long gx_ord64(u64 b) {
+  return (long long)(b ^ (((u64)((long long)b >> 63)) & 0x7FFFFFFFFFFFFFFFull));
+}
+__device__ __forceinline__ u64 gx_unord64(long long o) {
+  return (u64)o ^ (((u64)(o >> 63)) & 0x7FFFFFFFFFFFFFFFull);
+}
+
+// Combining a value over the lanes of one peer set (lanes whose rows fall in
+// the same group; every lane of the warp takes part, a lane outside any set
+// being a set of its own).  Tree over the ranks within the set: at step s
+// the survivors (ranks multiple of s) with a rank multiple of 2s take the
+// partial of the survivor just above them.  After 5 steps rank 0 holds the
+// combination of the whole set.  surv is the lane's peer mask.
+struct GxPeers {
+  u32 surv;
+  int rank;
+  __device__ __forceinline__ void init(u32 peers) {
+    surv = peers;
+    rank = __popc(peers & ((1u << (threadIdx.x & 31)) - 1u));
+  }
+  // the lane whose partial a receiver takes at step s (its own lane otherwise)
+  __device__ __forceinline__ int partner() const {
+    const int lane = threadIdx.x & 31;
+    const u32 above = surv & ~((2u << lane) - 1u);
+    return above ? __ffs(above) - 1 : lane;
+  }
+  __device__ __forceinline__ bool receives(int s) const {
+    const int lane = threadIdx.x & 31;
+    const u32 above = surv & ~((2u << lane) - 1u);
+    return ((surv >> lane) & 1u) && ((rank / s) % 2 == 0) && above != 0u;
+  }
+  __device__ __forceinline__ void step(int s) {
+    const int lane = threadIdx.x & 31;
+    const bool stays = ((surv >> lane) & 1u) && ((rank / s) % 2 == 0);
+    surv &= __ballot_sync(0xffffffffu, stays);
+  }
+};

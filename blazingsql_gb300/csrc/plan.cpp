@@ -112,7 +112,7 @@ bool Plan::needs_kernel() const {
 
 Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullable, const std::string& condition,
                 const std::vector<std::string>& expressions, bool filter_all, bool rand_by_output_row,
-                int first_rand_id, int* rand_count) {
+                int first_rand_id, int* rand_count, bool all_nodes) {
   Plan p;
   p.schema = schema;
   p.nullable = nullable;
@@ -138,13 +138,15 @@ Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullabl
     for (const auto& text : expressions) {
       ExprPtr e = compile_expression(text, schema);
       OutSpec o;
-      if (e->kind == Expr::LIT) {
+      if (e->kind == Expr::LIT && all_nodes) {
+        fail(GX_ERR_UNSUPPORTED, "a literal aggregation input");
+      } else if (e->kind == Expr::LIT) {
         o.kind = OutSpec::BROADCAST;
         o.type = e->lit_type;
         o.lit_bits = e->lit_bits;
         o.lit_valid = e->lit_valid;
         if (o.type == EMPTY || type_size(o.type) == 0) fail(GX_ERR_TYPE, "a bare null literal has no column type");
-      } else if (e->kind == Expr::COL) {
+      } else if (e->kind == Expr::COL && !all_nodes) {
         o.kind = OutSpec::COPY;
         o.col = e->col;
         o.type = schema[e->col];
@@ -1669,4 +1671,289 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   return o.str();
 }
 
+
+// ------------------------------------------------------------ aggregation
+// Fused filter + group-by aggregation kernel (gx_filter_aggregate).  Blocks
+// claim tiles; each warp evaluates the condition on its words, lists its kept
+// rows, and deals them to lanes in rounds of 32.  A lane computes its row's
+// keys and aggregation inputs and finds the row's group in the block's hash
+// table in shared memory.  The lanes of one group then combine their inputs
+// over a tree within the warp, and the group's first lane applies them with
+// shared-memory atomics: one atomic per group and warp round.  A row whose
+// group finds no room along the probe of the block's table goes to the global
+// table directly.  When the tiles run out, each block merges its table into the
+// global one.
+static std::string agg_identity(int kind, bool flt) {
+  if (kind == 2) return "0x7FFFFFFFFFFFFFFFull";                 // MIN: +largest (ordered)
+  if (kind == 3) return "0x8000000000000000ull";                 // MAX: -largest (ordered)
+  (void)flt;
+  return "0ull";                                                 // sums (0 and +0.0 share bits)
+}
+
+std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelConfig& cfg_in,
+                                const std::string& name) {
+  KernelConfig cfg = cfg_in;
+  if (cfg.native_f64_ops < 0) cfg.native_f64_ops = auto_native_f64_ops(p);
+  cfg.short_circuit = false;
+  cfg.runtime_order = false;
+  cfg.conjunct_order.clear();
+  Gen g(p, cfg);
+  std::ostringstream o;
+  emit_prelude(o, cfg);
+  const int nk = (int)L.key_nodes.size(), na = (int)L.kinds.size(), S = L.smem_slots;
+  if (S < 16 || (S & (S - 1)) != 0) fail(GX_ERR_INVALID, "aggregation table slots must be a power of two >= 16");
+  o << "#define GXA_S " << S << "\n#define GXA_NK " << std::max(nk, 1) << "\n#define GXA_NA " << std::max(na, 1)
+    << "\n#define GXA_PROBES 32\n";
+  // key hash (null keys hash as zero with their null bit set)
+  o << "__device__ __forceinline__ u64 gxa_hash(const u64* kv, u32 kn) {\n"
+       "  u64 h = 0x9E3779B97F4A7C15ull ^ (u64)kn;\n";
+  for (int j = 0; j < nk; j++) o << "  h = gx_mix64(h ^ (kv[" << j << "] + " << (j + 1) << "ull * 0x632BE59BD9B4E019ull));\n";
+  o << "  return gx_mix64(h);\n}\n";
+  auto same_keys = [&](const std::string& ks, const std::string& stride, const std::string& pos) {
+    std::string r = "true";
+    for (int j = 0; j < nk; j++)
+      r += " && *(volatile u64*)(" + ks + " + " + std::to_string(j) + "ull * " + stride + " + " + pos + ") == kv[" +
+           std::to_string(j) + "]";
+    return r;
+  };
+  auto write_keys = [&](std::ostringstream& os, const std::string& ks, const std::string& stride,
+                        const std::string& pos, const std::string& ind) {
+    for (int j = 0; j < nk; j++)
+      os << ind << ks << "[" << j << "ull * " << stride << " + " << pos << "] = kv[" << j << "];\n";
+  };
+  // the block's table: -1 when the probe finds no room, -2 after a wait gave up
+  o << "__device__ int gxa_find_smem(u32* st, u32* nm, u64* ks, const u64* kv, u32 kn, u64 h, int* err) {\n"
+       "  u32 pos = (u32)h & (GXA_S - 1);\n"
+       "  for (int pr = 0; pr < GXA_PROBES; pr++) {\n"
+       "    u32 s = *(volatile u32*)(st + pos);\n"
+       "    if (s == 0u) {\n"
+       "      s = atomicCAS(st + pos, 0u, 1u);\n"
+       "      if (s == 0u) {\n";
+  write_keys(o, "ks", "GXA_S", "pos", "        ");
+  o << "        nm[pos] = kn;\n"
+       "        __threadfence_block();\n"
+       "        atomicExch(st + pos, 2u);\n"
+       "        return (int)pos;\n"
+       "      }\n"
+       "    }\n"
+       "    u32 spins = 0;\n"
+       "    while (s == 1u) {\n"
+       "      if (++spins > (1u << 20)) { atomicExch(err, 1); return -2; }\n"
+       "      __nanosleep(16);\n"
+       "      s = *(volatile u32*)(st + pos);\n"
+       "    }\n"
+       "    __threadfence_block();\n"
+       "    if (*(volatile u32*)(nm + pos) == kn && " << same_keys("ks", "GXA_S", "pos") << ") return (int)pos;\n"
+       "    pos = (pos + 1u) & (GXA_S - 1);\n"
+       "  }\n"
+       "  return -1;\n"
+       "}\n";
+  // the global table: -1 when the whole table was probed (overflow) or a wait gave up
+  o << "__device__ long long gxa_find_global(const GxAggArgs& g, const u64* kv, u32 kn, u64 h) {\n"
+       "  u64 pos = h & (g.cap - 1ull);\n"
+       "  for (u64 pr = 0; pr < g.cap; pr++) {\n"
+       "    u32 s = *(volatile u32*)(g.state + pos);\n"
+       "    if (s == 0u) {\n"
+       "      s = atomicCAS(g.state + pos, 0u, 1u);\n"
+       "      if (s == 0u) {\n";
+  write_keys(o, "g.keys", "g.cap", "pos", "        ");
+  o << "        g.nullm[pos] = kn;\n"
+       "        __threadfence();\n"
+       "        atomicExch(g.state + pos, 2u);\n"
+       "        atomicAdd(g.groups, 1ull);\n"
+       "        return (long long)pos;\n"
+       "      }\n"
+       "    }\n"
+       "    u32 spins = 0;\n"
+       "    while (s == 1u) {\n"
+       "      if (++spins > (1u << 22)) { atomicExch(g.err, 1); return -1; }\n"
+       "      __nanosleep(32);\n"
+       "      s = *(volatile u32*)(g.state + pos);\n"
+       "    }\n"
+       "    __threadfence();\n"
+       "    if (*(volatile u32*)(g.nullm + pos) == kn && " << same_keys("g.keys", "g.cap", "pos") << ") return (long long)pos;\n"
+       "    pos = (pos + 1ull) & (g.cap - 1ull);\n"
+       "  }\n"
+       "  atomicExch(g.overflow, 1);\n"
+       "  return -1;\n"
+       "}\n";
+
+  // per aggregation: value type, input value, identity, combine, atomic update
+  struct AggCode {
+    std::string ty, val, id, comb, atom;  // atom: format with @A@ (address) and @X@ (value)
+  };
+  std::vector<AggCode> ac(na);
+  for (int j = 0; j < na; j++) {
+    const int kind = L.kinds[j], in = L.in_nodes[j];
+    const bool flt = in >= 0 && g.kind_f(in);
+    AggCode& c = ac[j];
+    if (kind == 4 || kind == 5) continue;  // counts only
+    if (kind == 2 || kind == 3) {
+      c.ty = "long long";
+      c.val = flt ? "gx_ord64(" + g.B(in) + ")" : "(long long)(" + g.B(in) + ")";
+      c.id = kind == 2 ? "(long long)0x7FFFFFFFFFFFFFFFull" : "(long long)0x8000000000000000ull";
+      c.comb = kind == 2 ? "min" : "max";
+      c.atom = kind == 2 ? "atomicMin((long long*)(@A@), @X@);" : "atomicMax((long long*)(@A@), @X@);";
+    } else if (flt) {
+      c.ty = "double";
+      c.val = "__longlong_as_double((long long)(" + g.B(in) + "))";
+      c.id = "0.0";
+      c.comb = "+";
+      c.atom = "atomicAdd((double*)(@A@), @X@);";
+    } else {
+      c.ty = "u64";
+      c.val = "(u64)(" + g.B(in) + ")";
+      c.id = "0ull";
+      c.comb = "+";
+      c.atom = "atomicAdd((unsigned long long*)(@A@), (unsigned long long)(@X@));";
+    }
+  }
+  auto atom = [&](int j, const std::string& addr, const std::string& x) {
+    std::string a = ac[j].atom;
+    a.replace(a.find("@A@"), 3, addr);
+    a.replace(a.find("@X@"), 3, x);
+    return a;
+  };
+  auto combine = [&](int j, const std::string& x, const std::string& t) {
+    if (ac[j].comb == "+") return x + " += " + t + ";";
+    return x + " = " + ac[j].comb + "(" + x + ", " + t + ");";
+  };
+  std::vector<int> roots = L.key_nodes;
+  for (int in : L.in_nodes)
+    if (in >= 0) roots.push_back(in);
+  const std::vector<int> row_ids = g.cone(roots);
+  const std::vector<int> pred_ids = g.predicate_cone();
+
+  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name
+    << "(const GxArgs a, const GxAggArgs ga) {\n";
+  o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
+  o << "  const i64 nwords = (a.n + 31) >> 5;\n";
+  o << "  const i64 ntiles = (nwords + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
+  o << "  __shared__ u32 s_st_[GXA_S]; __shared__ u32 s_nm_[GXA_S]; __shared__ u64 s_rows_[GXA_S];\n";
+  o << "  __shared__ u64 s_ks_[GXA_NK * GXA_S]; __shared__ u64 s_acc_[GXA_NA * GXA_S];\n";
+  o << "  __shared__ u64 s_cnt_[GXA_NA * GXA_S];\n";
+  o << "  __shared__ unsigned short s_kept_[GX_WARPS][GX_V * 32];\n";
+  o << "  __shared__ unsigned long long s_claim;\n";
+  o << "  for (int i = threadIdx.x; i < GXA_S; i += blockDim.x) {\n";
+  o << "    s_st_[i] = 0u; s_nm_[i] = 0u; s_rows_[i] = 0ull;\n";
+  for (int j = 0; j < na; j++)
+    o << "    s_acc_[" << j << " * GXA_S + i] = " << agg_identity(L.kinds[j], false) << "; s_cnt_[" << j
+      << " * GXA_S + i] = 0ull;\n";
+  o << "  }\n  __syncthreads();\n";
+  o << "  while (true) {\n";
+  o << "    if (threadIdx.x == 0) s_claim = atomicAdd(a.tile_counter, 1ull);\n";
+  o << "    __syncthreads();\n";
+  o << "    const i64 tile = (i64)s_claim;\n";
+  o << "    __syncthreads();\n";
+  o << "    if (tile >= ntiles) break;\n";
+  o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
+  o << "    u32 bal[GX_V];\n";
+  o << "    {\n";
+  if (p.has_filter()) {
+    g.decl(o, pred_ids, "      ");
+    g.emit_predicate(o, "      ");
+  } else {
+    o << "      bool alive[GX_V];\n";
+    o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) alive[k] = (w0 + k) * 32 + lane < a.n;\n";
+  }
+  o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) bal[k] = __ballot_sync(GX_FULL, alive[k]);\n";
+  o << "    }\n";
+  o << "    u32 total_ = 0u;\n";
+  o << "    #pragma unroll\n    for (int kk = 0; kk < GX_V; kk++) {\n";
+  o << "      if ((bal[kk] >> lane) & 1u) s_kept_[warp][total_ + __popc(bal[kk] & ((1u << lane) - 1u))] = "
+       "(unsigned short)(kk * 32 + lane);\n";
+  o << "      total_ += __popc(bal[kk]);\n";
+  o << "    }\n";
+  o << "    __syncwarp();\n";
+  o << "    const u64 pos = 0ull; (void)pos;\n";
+  o << "    for (u32 base_ = 0; base_ < total_; base_ += 32u) {\n";
+  const std::string in2 = "      ";
+  o << in2 << "const u32 t_ = base_ + (u32)lane; const bool act = t_ < total_;\n";
+  emit_rank_to_row(o, in2);
+  emit_row_nodes(o, g, p, row_ids, {}, in2);
+  o << in2 << "u64 kv[GXA_NK]; u32 kn_ = 0u; kv[0] = 0ull;\n";
+  for (int j = 0; j < nk; j++) {
+    const int id = L.key_nodes[j];
+    o << in2 << "kv[" << j << "] = " << g.V(id) << " ? (u64)(" << g.B(id) << ") : 0ull; if (!(" << g.V(id)
+      << ")) kn_ |= " << (1u << j) << "u;\n";
+  }
+  o << in2 << "const u64 h_ = gxa_hash(kv, kn_);\n";
+  o << in2 << "const int sl_ = act ? gxa_find_smem(s_st_, s_nm_, s_ks_, kv, kn_, h_, ga.err) : -3;\n";
+  o << in2 << "const bool sm_ = sl_ >= 0;\n";
+  o << in2 << "const u32 peers_ = __match_any_sync(GX_FULL, sm_ ? (u32)sl_ : (0x80000000u | (u32)lane));\n";
+  o << in2 << "GxPeers pr_; pr_.init(peers_);\n";
+  for (int j = 0; j < na; j++) {
+    const int in = L.in_nodes[j];
+    const std::string vj = in >= 0 ? "(sm_ && " + g.V(in) + ")" : "sm_";
+    o << in2 << "const bool vl" << j << "_ = " << vj << ";\n";
+    o << in2 << "const u64 c" << j << "_ = (u64)__popc(__ballot_sync(GX_FULL, vl" << j << "_) & peers_);\n";
+    if (!ac[j].ty.empty())
+      o << in2 << ac[j].ty << " x" << j << "_ = vl" << j << "_ ? " << ac[j].val << " : " << ac[j].id << ";\n";
+  }
+  o << in2 << "#pragma unroll\n" << in2 << "for (int s_ = 1; s_ < 32; s_ <<= 1) {\n";
+  o << in2 << "  const int src_ = pr_.partner(); const bool rcv_ = pr_.receives(s_);\n";
+  for (int j = 0; j < na; j++) {
+    if (ac[j].ty.empty()) continue;
+    o << in2 << "  { const " << ac[j].ty << " t_ = __shfl_sync(GX_FULL, x" << j << "_, src_); if (rcv_) "
+      << combine(j, "x" + std::to_string(j) + "_", "t_") << " }\n";
+  }
+  o << in2 << "  pr_.step(s_);\n";
+  o << in2 << "}\n";
+  o << in2 << "if (sm_ && pr_.rank == 0) {\n";
+  o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
+  for (int j = 0; j < na; j++) {
+    o << in2 << "  if (c" << j << "_ != 0ull) {\n";
+    o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
+      << "_);\n";
+    if (!ac[j].ty.empty())
+      o << in2 << "    " << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", "x" + std::to_string(j) + "_")
+        << "\n";
+    o << in2 << "  }\n";
+  }
+  o << in2 << "}\n";
+  // rows whose group found no room in the block's table go to the global one
+  o << in2 << "if (act && sl_ == -1) {\n";
+  o << in2 << "  const long long gs_ = gxa_find_global(ga, kv, kn_, h_);\n";
+  o << in2 << "  if (gs_ >= 0) {\n";
+  o << in2 << "    atomicAdd((unsigned long long*)(ga.rows + gs_), 1ull);\n";
+  for (int j = 0; j < na; j++) {
+    const int in = L.in_nodes[j];
+    const std::string vj = in >= 0 ? g.V(in) : "true";
+    o << in2 << "    if (" << vj << ") {\n";
+    o << in2 << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), 1ull);\n";
+    if (!ac[j].ty.empty())
+      o << in2 << "      " << atom(j, "ga.acc + " + std::to_string(j) + "ull * ga.cap + gs_", ac[j].val) << "\n";
+    o << in2 << "    }\n";
+  }
+  o << in2 << "  }\n";
+  o << in2 << "}\n";
+  o << "    }\n";  // rounds
+  o << "  }\n";    // tiles
+  // merge the block's table into the global one
+  o << "  __syncthreads();\n";
+  o << "  for (int i = threadIdx.x; i < GXA_S; i += blockDim.x) {\n";
+  o << "    if (s_st_[i] != 2u || s_rows_[i] == 0ull) continue;\n";
+  o << "    u64 kv[GXA_NK]; kv[0] = 0ull;\n";
+  for (int j = 0; j < nk; j++) o << "    kv[" << j << "] = s_ks_[" << j << " * GXA_S + i];\n";
+  o << "    const u32 kn_ = s_nm_[i];\n";
+  o << "    const long long gs_ = gxa_find_global(ga, kv, kn_, gxa_hash(kv, kn_));\n";
+  o << "    if (gs_ < 0) continue;\n";
+  o << "    atomicAdd((unsigned long long*)(ga.rows + gs_), (unsigned long long)s_rows_[i]);\n";
+  for (int j = 0; j < na; j++) {
+    o << "    if (s_cnt_[" << j << " * GXA_S + i] != 0ull) {\n";
+    o << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), (unsigned long long)s_cnt_["
+      << j << " * GXA_S + i]);\n";
+    if (!ac[j].ty.empty()) {
+      std::string x;
+      if (ac[j].ty == "double") x = "__longlong_as_double((long long)s_acc_[" + std::to_string(j) + " * GXA_S + i])";
+      else if (ac[j].ty == "long long") x = "(long long)s_acc_[" + std::to_string(j) + " * GXA_S + i]";
+      else x = "s_acc_[" + std::to_string(j) + " * GXA_S + i]";
+      o << "      " << atom(j, "ga.acc + " + std::to_string(j) + "ull * ga.cap + gs_", x) << "\n";
+    }
+    o << "    }\n";
+  }
+  o << "  }\n";
+  o << "}\n";
+  return o.str();
+}
 }  // namespace gx

@@ -91,7 +91,22 @@ struct Plan {
 // *rand_count (optional) receives how many the expressions used.
 Plan build_plan(const std::vector<int>& schema, const std::vector<bool>& nullable, const std::string& condition,
                 const std::vector<std::string>& expressions, bool filter_all, bool rand_by_output_row,
-                int first_rand_id = 0, int* rand_count = nullptr);
+                int first_rand_id = 0, int* rand_count = nullptr, bool all_nodes = false);
+// (all_nodes: every expression, a bare column reference included, becomes a
+// NODE output computed in the kernel -- the aggregation kernel reads values
+// from nodes only; a bare literal is rejected there)
+
+// Fused filter + group-by aggregation (gx_filter_aggregate): the plan's
+// outputs are the key columns then the non-empty aggregation inputs, all NODE
+// outputs.  The kernel keeps a hash table of groups per block in shared memory
+// and merges it into a global table (GxAggArgs) when the block finishes.
+struct AggLayout {
+  std::vector<int> key_nodes;   // node of each key column
+  std::vector<int> kinds;       // gx_agg_kind per aggregation
+  std::vector<int> in_nodes;    // input node per aggregation (-1: COUNT(*))
+  int smem_slots = 256;         // shared-memory table slots per block (power of two)
+};
+std::string generate_agg_kernel(const Plan& plan, const AggLayout& L, const KernelConfig& cfg, const std::string& name);
 
 // Outputs per plan kernel; longer expression lists are split into several
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).

@@ -32,6 +32,10 @@ void* dev_alloc(size_t bytes, cudaStream_t s);
 // types[i] / caps[i] per column; masks zeroed when zero_masks
 void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>& caps, bool zero_masks,
                       gx_column* out, cudaStream_t s);
+// output columns of one call in one allocation: [scratch | masks | data];
+// returns the scratch (scratch_bytes > 0) or nullptr
+void* alloc_outputs(const std::vector<int>& types, int64_t capacity, size_t scratch_bytes, bool zero_masks,
+                    gx_column* out, cudaStream_t s);
 int64_t mask_words_for(int64_t rows);  // padded 32-bit mask words an output of `rows` rows holds
 // Outputs of a queue of filter calls in one allocation and one memset: for
 // batch b, types.size() columns of capacity caps[b] with zeroed masks

@@ -210,6 +210,57 @@ int gx_plan_execute_host(const gx_plan* plan, const gx_column_view* columns, int
 
 void gx_plan_destroy(gx_plan* plan);
 
+/* ---- fused filter + group-by aggregation ---------------------------------
+ *
+ * The aggregation step of a Filter -> Projection -> Aggregate chain in one
+ * device pass: ral::operators::compute_aggregations_with_groupby
+ * (engine/src/operators/GroupBy.cpp:316-416), or compute_aggregations_without_groupby
+ * (GroupBy.cpp:217-314) when there are no group columns, applied to the rows of
+ * `columns` that pass `condition`, with each aggregation input expression
+ * (what the reference evaluates through evaluate_expressions,
+ * GroupBy.cpp:246-250 / :348-352) computed in the same pass.  No column of
+ * the filtered table or of the aggregation inputs is materialised.
+ *
+ * - group_columns: input column indices of the keys (integer, BOOL8,
+ *   timestamp or duration columns); NULL keys form their own group
+ *   (cudf::null_policy::INCLUDE, GroupBy.cpp:380).
+ * - agg_inputs[i]: a RexNode expression over the input columns, or "" for
+ *   COUNT(*) (GX_AGG_COUNT_ALL).
+ * - Output: out[0 .. num_group_columns) the key columns (their input types),
+ *   then out[num_group_columns + i] aggregation i.  Types: COUNT -> INT64;
+ *   SUM / SUM0 -> INT64 for an integer input, FLOAT64 for a floating one (the
+ *   widening of GroupBy.cpp:33-40); MIN / MAX -> the input expression's type;
+ *   MEAN -> FLOAT64.  SUM / MIN / MAX / MEAN of a group without a valid input
+ *   are NULL; SUM0 is 0 there (GroupBy.cpp:394-397); COUNT_VALID counts valid
+ *   inputs, COUNT_ALL rows.  Integer sums wrap (two's complement).
+ * - With group columns the groups come out in no particular order (as the
+ *   reference's hash group-by); *out_groups receives their number.  Without
+ *   group columns there is exactly one output row, empty input included.
+ * - Floating-point sums and means add in an order that depends on the GPU's
+ *   scheduling (as cudf's hash aggregation does): results agree with a
+ *   sequential sum to rounding, not bit for bit.  Everything else is exact. */
+typedef enum gx_agg_kind {
+  GX_AGG_SUM = 0, GX_AGG_SUM0 = 1, GX_AGG_MIN = 2, GX_AGG_MAX = 3,
+  GX_AGG_COUNT_VALID = 4, GX_AGG_COUNT_ALL = 5, GX_AGG_MEAN = 6
+} gx_agg_kind;
+
+#define GX_AGG_MAX_KEYS 8
+#define GX_AGG_MAX_AGGS 24
+
+int gx_filter_aggregate(const gx_column_view* columns, int num_columns, const char* condition,
+                        const int* group_columns, int num_group_columns, const char* const* agg_inputs,
+                        const int* agg_kinds, int num_aggs, gx_column* out, int64_t* out_groups, void* stream,
+                        gx_status_info* status);
+
+/* Builds the aggregation kernel of a gx_filter_aggregate call for a column
+ * schema (types, which columns carry a mask) and compiles it with NVRTC (no
+ * GPU needed); registers, spill bytes and static shared memory per thread /
+ * block from ptxas (each may be NULL). */
+int gx_debug_aggregate_check(const int32_t* column_types, const uint8_t* column_has_mask, int num_columns,
+                             const char* condition, const int* group_columns, int num_group_columns,
+                             const char* const* agg_inputs, const int* agg_kinds, int num_aggs, int32_t* registers,
+                             int32_t* spill_bytes, int32_t* shared_bytes, gx_status_info* status);
+
 /* ---- batch runner: many batches, one persistent launch (no counterpart in
  * the reference) -------------------------------------------------------------
  *
