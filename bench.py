@@ -255,6 +255,98 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
     }
 
 
+def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
+    """Fused filter + group-by aggregation (gx_filter_aggregate) on the
+    order-line columns with TPC-H Q1's aggregation shape (C5 condition, keys
+    $5, $6, nine aggregations), inputs resident: rows/s and HBM GB/s of the
+    aggregation kernel against the measured peak.  Beside it, the filter +
+    projection of the same rows (gx_filter_project of the C5 plan), which
+    materialises what an unfused aggregation would read back.  A sample's
+    groups are checked against the CPU oracle."""
+    import numpy as np
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
+    from blazingsql_gb300 import workloads as W
+    from blazingsql_gb300.types import is_float, unpack_validity
+    L = N.lib()
+    stream = torch.cuda.current_stream()
+    w = W.workload("c5", rows)
+    cols = W.device_columns("c5", rows, seed=seed)
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        for _ in range(4):  # warm-up: JIT and the plan's block-shape trials
+            fn()
+        torch.cuda.synchronize()
+        L.gx_debug_kernel_ms(1)
+        L.gx_debug_set_kernel_timing(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        L.gx_debug_set_kernel_timing(0)
+        return e0.elapsed_time(e1) / reps, L.gx_debug_kernel_ms(1) / reps
+
+    def agg():
+        out, groups = g.filter_aggregate(cols, W.C5_CONDITION, W.C5_AGG_KEYS, W.C5_AGGREGATIONS, stream=stream)
+        g.api.free_columns(out, stream)
+
+    def fp():
+        out = g.filter_project(cols, W.C5_CONDITION, W.C5_PROJECTIONS, stream=stream)
+        g.api.free_columns(out, stream)
+
+    agg_ms, agg_kernel_ms = timed(agg)
+    fp_ms, fp_kernel_ms = timed(fp)
+    in_bytes = rows * w.in_bytes_per_row
+    peak, peak_kind = measured_peak_hbm()
+    achieved = in_bytes / (agg_kernel_ms / 1e3) / 1e9
+    # parity on a sample: the groups of the first 2^18 rows against the oracle
+    from oracle import agg_ref
+    from blazingsql_gb300.types import HostColumn, np_dtype
+    ns = min(rows, 1 << 18)
+    out, groups = g.filter_aggregate(W.slice_batches(cols, [ns])[0], W.C5_CONDITION, W.C5_AGG_KEYS,
+                                     W.C5_AGGREGATIONS, stream=stream)
+    got = [c.to_host() for c in out]
+    g.api.free_columns(out, stream)
+    sample = []
+    for c in cols:  # the first ns rows only
+        dt = np_dtype(c.type_id)
+        data = c.data[:ns * dt.itemsize].cpu().numpy().view(dt).copy()
+        mask = None if c.mask is None else c.mask[:((ns + 31) // 32) * 4].cpu().numpy().view(np.uint32).copy()
+        sample.append(HostColumn(c.type_id, data, mask))
+    exp = agg_ref.filter_aggregate(sample, W.C5_CONDITION, W.C5_AGG_KEYS, W.C5_AGGREGATIONS)
+    ok = groups == len(exp[0].data)
+    if ok:
+        nk = len(W.C5_AGG_KEYS)
+        keyset = lambda cs: [tuple(int(cs[j].data[r]) for j in range(nk)) for r in range(len(cs[0].data))]
+        order = sorted(range(groups), key=lambda r: keyset(got)[r])
+        for x, y in zip(got, exp):
+            dx = np.asarray(x.data[:groups])[order]
+            dy = np.asarray(y.data[:groups])
+            vx = unpack_validity(x.mask, groups)[order]
+            vy = unpack_validity(y.mask, groups)
+            ok &= bool(np.array_equal(vx, vy))
+            if is_float(x.type_id):
+                ok &= bool(np.allclose(dx[vx], dy[vy], rtol=1e-9, atol=0))
+            else:
+                ok &= bool(np.array_equal(dx[vx], dy[vy]))
+    del cols
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"c5_q1_filter_aggregate: {rows} rows, 7 columns, keys $5 $6, 9 aggregations",
+        "rows_per_s": rows / (agg_ms / 1e3), "ms": agg_ms, "kernel_ms": agg_kernel_ms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "algorithmic_bytes": in_bytes},
+        "groups": groups, "oracle_sample_rows": ns, "matches_oracle": bool(ok),
+        "filter_project_rows_per_s": rows / (fp_ms / 1e3), "filter_project_ms": fp_ms,
+        "filter_project_kernel_ms": fp_kernel_ms,
+        "fused_vs_filter_project": fp_ms / agg_ms,
+    }
+
+
 def learned_compare(batches: int, rows: int, seed: int = 4):
     """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
     through gx_learner under four policies on the same resident batches:
@@ -384,6 +476,8 @@ def main():
     ap.add_argument("--learned-batches", type=int, default=64, help="C4 batches (0 skips the learned comparison)")
     ap.add_argument("--learned-rows", type=int, default=1 << 22, help="C4 rows per batch")
     ap.add_argument("--batched-batches", type=int, default=512, help="C3 batches (0 skips the batched comparison)")
+    ap.add_argument("--agg-rows", type=int, default=1 << 27,
+                    help="rows of the fused filter + aggregation measurement (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -512,6 +606,13 @@ def main():
             cols = None
             torch.cuda.empty_cache()
         batched = batched_compare(args.batched_batches)
+    aggregate = None
+    if args.agg_rows > 0:
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
+        aggregate = aggregate_compare(args.agg_rows)
     learned = None
     if args.learned_batches > 0:
         if cols is not None:
@@ -544,6 +645,7 @@ def main():
         "clocks": clocks.summary(),
         "batched": batched,
         "learned": learned,
+        "aggregate": aggregate,
     }
     print(json.dumps(line), flush=True)
     if dist:

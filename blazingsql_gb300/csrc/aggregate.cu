@@ -11,6 +11,7 @@
 #include "aggregate.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "jit.h"
@@ -40,6 +41,7 @@ struct AggFinal {
   int nk, na;
   int key_w[kMaxKeys];
   int kind[kMaxAggs];
+  int acc_of[kMaxAggs];  // accumulator of aggregation j (-1: the group's row count)
   int in_flt[kMaxAggs];
   int out_w[kMaxAggs];
   int out_f32[kMaxAggs];
@@ -75,8 +77,9 @@ __device__ void write_row(const AggFinal& f, long long i, uint64_t p) {
   }
   for (int j = 0; j < f.na; j++) {
     const int o = f.nk + j;
-    const uint64_t c = i >= 0 ? f.t.cnt[j * cap + i] : 0ull;
-    const uint64_t a = i >= 0 ? f.t.acc[j * cap + i] : 0ull;
+    const int q = f.acc_of[j];
+    const uint64_t c = i < 0 ? 0ull : (q < 0 ? f.t.rows[i] : f.t.cnt[q * cap + i]);
+    const uint64_t a = (i < 0 || q < 0) ? 0ull : f.t.acc[q * cap + i];
     const int kind = f.kind[j];
     if (kind == 4 || kind == 5) {  // COUNT_VALID, COUNT_ALL
       store_w(f.out_data[o], p, 8, c);
@@ -160,19 +163,40 @@ AggPlan::AggPlan(const std::vector<int>& schema, const std::vector<bool>& nullab
   }
   plan_ = build_plan(schema, nullable, condition, exprs, false, false, 0, nullptr, true);
   for (size_t j = 0; j < key_cols.size(); j++) layout_.key_nodes.push_back(plan_.outputs[j].node);
+  // accumulators: one per (sum | min | max, input node); SUM, SUM0 and MEAN of
+  // one input share a sum, COUNT(x) takes the valid count of any accumulator
+  // on x (a count-only one when there is none), COUNT(*) the group's rows
   size_t next = key_cols.size();
   for (size_t i = 0; i < kinds.size(); i++) {
-    layout_.kinds.push_back(kinds[i]);
     int node = -1;
     if (kinds[i] != 5) node = plan_.outputs[next++].node;
-    layout_.in_nodes.push_back(node);
-    const bool flt = node >= 0 && is_float(plan_.nodes[node].ktype);
-    in_float_.push_back(flt);
+    agg_node_.push_back(node);
+    in_float_.push_back(node >= 0 && is_float(plan_.nodes[node].ktype));
   }
+  auto acc_for = [&](int cls, int node) {
+    for (size_t q = 0; q < layout_.kinds.size(); q++)
+      if (layout_.kinds[q] == cls && layout_.in_nodes[q] == node) return (int)q;
+    layout_.kinds.push_back(cls);
+    layout_.in_nodes.push_back(node);
+    return (int)layout_.kinds.size() - 1;
+  };
+  acc_of_.assign(kinds.size(), -1);
+  for (size_t i = 0; i < kinds.size(); i++) {
+    const int k = kinds[i];
+    if (k == 0 || k == 1 || k == 6) acc_of_[i] = acc_for(0, agg_node_[i]);
+    else if (k == 2 || k == 3) acc_of_[i] = acc_for(k, agg_node_[i]);
+  }
+  for (size_t i = 0; i < kinds.size(); i++) {
+    if (kinds[i] != 4) continue;
+    for (size_t q = 0; q < layout_.kinds.size() && acc_of_[i] < 0; q++)
+      if (layout_.in_nodes[q] == agg_node_[i]) acc_of_[i] = (int)q;
+    if (acc_of_[i] < 0) acc_of_[i] = acc_for(4, agg_node_[i]);
+  }
+  agg_kind_ = kinds;
   // output types: keys keep theirs; COUNT INT64; SUM widened; MEAN FLOAT64; MIN/MAX the input's
   out_types_ = key_types_;
   for (size_t i = 0; i < kinds.size(); i++) {
-    const int k = kinds[i], node = layout_.in_nodes[i];
+    const int k = kinds[i], node = agg_node_[i];
     if (k == 4 || k == 5) out_types_.push_back(INT64);
     else if (k == 6) out_types_.push_back(FLOAT64);
     else if (k == 0 || k == 1) out_types_.push_back(in_float_[i] ? FLOAT64 : INT64);
@@ -183,11 +207,17 @@ AggPlan::AggPlan(const std::vector<int>& schema, const std::vector<bool>& nullab
     }
   }
   // shared-memory table: as many slots (a power of two, at most 256) as fit in
-  // about 40 KB next to the kept-row lists
-  const size_t per_slot = 4 + 4 + 8 + 8 * std::max<size_t>(key_cols.size(), 1) + 16 * kinds.size();
+  // about 8 KB: a larger table costs blocks per SM (the kernel is instruction
+  // bound, so occupancy matters more than spilling medium-cardinality groups
+  // to the global table)
+  const size_t per_slot = 4 + 4 + 8 + 8 * std::max<size_t>(key_cols.size(), 1) +
+                          16 * std::max<size_t>(layout_.kinds.size(), 1);
   int slots = 256;
-  while (slots > 16 && (size_t)slots * per_slot > 40 * 1024) slots >>= 1;
+  const int budget = std::getenv("GX_AGG_SMEM_KB") ? std::atoi(std::getenv("GX_AGG_SMEM_KB")) : 8;
+  while (slots > 16 && (size_t)slots * per_slot > (size_t)budget * 1024) slots >>= 1;
   layout_.smem_slots = slots;
+  const char* wc = std::getenv("GX_AGG_COMBINE");
+  layout_.warp_combine = !(wc && *wc == '0');
 }
 
 std::string AggPlan::kernel_source(const std::vector<bool>& nullable) const {
@@ -217,8 +247,9 @@ void AggPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
   for (size_t i = 0; i < cols.size(); i++)
     if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
   const int64_t n = cols.empty() ? 0 : cols[0].size;
-  const int nk = (int)layout_.key_nodes.size(), na = (int)layout_.kinds.size();
-  const int nout = nk + na;
+  const int nk = (int)layout_.key_nodes.size(), na = (int)layout_.kinds.size();  // na: accumulators
+  const int nagg = (int)agg_kind_.size();
+  const int nout = nk + nagg;
   std::vector<bool> nb(cols.size());
   for (size_t i = 0; i < cols.size(); i++) nb[i] = cols[i].mask != nullptr;
   const JitKernel k = kernel(nb);  // compiled before any allocation of this call
@@ -306,10 +337,11 @@ void AggPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     made.assign(out, out + nout);
     AggFinal f{};
     f.nk = nk;
-    f.na = na;
+    f.na = nagg;
     for (int j = 0; j < nk; j++) f.key_w[j] = type_size(key_types_[j]);
-    for (int j = 0; j < na; j++) {
-      f.kind[j] = layout_.kinds[j];
+    for (int j = 0; j < nagg; j++) {
+      f.kind[j] = agg_kind_[j];
+      f.acc_of[j] = acc_of_[j];
       f.in_flt[j] = in_float_[j] ? 1 : 0;
       f.out_w[j] = type_size(out_types_[nk + j]);
       f.out_f32[j] = out_types_[nk + j] == FLOAT32 ? 1 : 0;

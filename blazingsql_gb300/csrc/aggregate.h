@@ -40,7 +40,10 @@ class AggPlan {
   AggLayout layout_;
   KernelConfig cfg_;
   std::vector<int> key_types_;
-  std::vector<bool> in_float_;
+  std::vector<int> agg_kind_;   // gx_agg_kind per aggregation
+  std::vector<int> agg_node_;   // input node per aggregation (-1: COUNT(*))
+  std::vector<int> acc_of_;     // accumulator per aggregation (-1: the group's rows)
+  std::vector<bool> in_float_;  // per aggregation: floating-point input
   std::vector<int> out_types_;
   mutable std::mutex mu_;
   mutable std::unordered_map<std::string, JitKernel> kcache_;

@@ -340,6 +340,9 @@ static std::shared_ptr<AggPlan> agg_plan_for(const std::vector<int>& schema, con
   key += "|";
   for (int i = 0; i < na; i++) key += std::to_string(kinds[i]) + ":" + inputs[i] + "\x1f";
   key += "|" + std::to_string(cfg.warps) + ":" + std::to_string(cfg.words) + ":" + std::to_string(cfg.native_f64_ops);
+  const char* wc = std::getenv("GX_AGG_COMBINE");
+  key += (wc && *wc == '0') ? ":direct" : ":combine";
+  if (const char* kb = std::getenv("GX_AGG_SMEM_KB")) key += std::string(":smem") + kb;
   static std::mutex mu;
   static std::unordered_map<std::string, std::shared_ptr<AggPlan>> plans;
   {

@@ -1880,37 +1880,52 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   o << in2 << "const u64 h_ = gxa_hash(kv, kn_);\n";
   o << in2 << "const int sl_ = act ? gxa_find_smem(s_st_, s_nm_, s_ks_, kv, kn_, h_, ga.err) : -3;\n";
   o << in2 << "const bool sm_ = sl_ >= 0;\n";
-  o << in2 << "const u32 peers_ = __match_any_sync(GX_FULL, sm_ ? (u32)sl_ : (0x80000000u | (u32)lane));\n";
-  o << in2 << "GxPeers pr_; pr_.init(peers_);\n";
-  for (int j = 0; j < na; j++) {
-    const int in = L.in_nodes[j];
-    const std::string vj = in >= 0 ? "(sm_ && " + g.V(in) + ")" : "sm_";
-    o << in2 << "const bool vl" << j << "_ = " << vj << ";\n";
-    o << in2 << "const u64 c" << j << "_ = (u64)__popc(__ballot_sync(GX_FULL, vl" << j << "_) & peers_);\n";
-    if (!ac[j].ty.empty())
-      o << in2 << ac[j].ty << " x" << j << "_ = vl" << j << "_ ? " << ac[j].val << " : " << ac[j].id << ";\n";
+  if (!L.warp_combine) {
+    // every lane applies its own row with shared-memory atomics
+    o << in2 << "if (sm_) {\n";
+    o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], 1ull);\n";
+    for (int j = 0; j < na; j++) {
+      const int in = L.in_nodes[j];
+      o << in2 << "  if (" << (in >= 0 ? g.V(in) : std::string("true")) << ") {\n";
+      o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], 1ull);\n";
+      if (!ac[j].ty.empty())
+        o << in2 << "    " << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", ac[j].val) << "\n";
+      o << in2 << "  }\n";
+    }
+    o << in2 << "}\n";
+  } else {
+    o << in2 << "const u32 peers_ = __match_any_sync(GX_FULL, sm_ ? (u32)sl_ : (0x80000000u | (u32)lane));\n";
+    o << in2 << "GxPeers pr_; pr_.init(peers_);\n";
+    for (int j = 0; j < na; j++) {
+      const int in = L.in_nodes[j];
+      const std::string vj = in >= 0 ? "(sm_ && " + g.V(in) + ")" : "sm_";
+      o << in2 << "const bool vl" << j << "_ = " << vj << ";\n";
+      o << in2 << "const u64 c" << j << "_ = (u64)__popc(__ballot_sync(GX_FULL, vl" << j << "_) & peers_);\n";
+      if (!ac[j].ty.empty())
+        o << in2 << ac[j].ty << " x" << j << "_ = vl" << j << "_ ? " << ac[j].val << " : " << ac[j].id << ";\n";
+    }
+    o << in2 << "#pragma unroll\n" << in2 << "for (int s_ = 1; s_ < 32; s_ <<= 1) {\n";
+    o << in2 << "  const int src_ = pr_.partner(); const bool rcv_ = pr_.receives(s_);\n";
+    for (int j = 0; j < na; j++) {
+      if (ac[j].ty.empty()) continue;
+      o << in2 << "  { const " << ac[j].ty << " t_ = __shfl_sync(GX_FULL, x" << j << "_, src_); if (rcv_) "
+        << combine(j, "x" + std::to_string(j) + "_", "t_") << " }\n";
+    }
+    o << in2 << "  pr_.step(s_);\n";
+    o << in2 << "}\n";
+    o << in2 << "if (sm_ && pr_.rank == 0) {\n";
+    o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
+    for (int j = 0; j < na; j++) {
+      o << in2 << "  if (c" << j << "_ != 0ull) {\n";
+      o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
+        << "_);\n";
+      if (!ac[j].ty.empty())
+        o << in2 << "    "
+          << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", "x" + std::to_string(j) + "_") << "\n";
+      o << in2 << "  }\n";
+    }
+    o << in2 << "}\n";
   }
-  o << in2 << "#pragma unroll\n" << in2 << "for (int s_ = 1; s_ < 32; s_ <<= 1) {\n";
-  o << in2 << "  const int src_ = pr_.partner(); const bool rcv_ = pr_.receives(s_);\n";
-  for (int j = 0; j < na; j++) {
-    if (ac[j].ty.empty()) continue;
-    o << in2 << "  { const " << ac[j].ty << " t_ = __shfl_sync(GX_FULL, x" << j << "_, src_); if (rcv_) "
-      << combine(j, "x" + std::to_string(j) + "_", "t_") << " }\n";
-  }
-  o << in2 << "  pr_.step(s_);\n";
-  o << in2 << "}\n";
-  o << in2 << "if (sm_ && pr_.rank == 0) {\n";
-  o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
-  for (int j = 0; j < na; j++) {
-    o << in2 << "  if (c" << j << "_ != 0ull) {\n";
-    o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
-      << "_);\n";
-    if (!ac[j].ty.empty())
-      o << in2 << "    " << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", "x" + std::to_string(j) + "_")
-        << "\n";
-    o << in2 << "  }\n";
-  }
-  o << in2 << "}\n";
   // rows whose group found no room in the block's table go to the global one
   o << in2 << "if (act && sl_ == -1) {\n";
   o << in2 << "  const long long gs_ = gxa_find_global(ga, kv, kn_, h_);\n";

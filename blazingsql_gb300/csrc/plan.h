@@ -105,6 +105,9 @@ struct AggLayout {
   std::vector<int> kinds;       // gx_agg_kind per aggregation
   std::vector<int> in_nodes;    // input node per aggregation (-1: COUNT(*))
   int smem_slots = 256;         // shared-memory table slots per block (power of two)
+  // the lanes of one group combine their inputs over a warp tree before one
+  // lane applies them (true), or every lane applies its own row (false)
+  bool warp_combine = true;
 };
 std::string generate_agg_kernel(const Plan& plan, const AggLayout& L, const KernelConfig& cfg, const std::string& name);
 

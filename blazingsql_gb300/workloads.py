@@ -39,6 +39,16 @@ C2_PROJECTIONS = [
     "MOD(CASE(IS NOT NULL($0), $0, $1), 997)",
 ]
 
+# TPC-H Q1's aggregation shape over the order-line columns (C5), grouped by
+# the two flag columns: (gx_agg_kind, input expression); kinds 0 SUM, 2 MIN,
+# 3 MAX, 5 COUNT(*), 6 MEAN.  Inputs are the quantity, price, charge
+# (price x (100 - discount) x (100 + tax), exact INT64), unit price,
+# discount fraction and ship date.
+C5_AGG_KEYS = [5, 6]
+C5_AGGREGATIONS = [(0, "$0"), (0, "$1"), (0, "*(*($1, -(100, $2)), +(100, $3))"),
+                   (0, "/(CAST($1):DOUBLE, CAST($0):DOUBLE)"), (6, "$0"), (6, "/(CAST($2):DOUBLE, 100.0)"),
+                   (5, ""), (2, "$4"), (3, "/(CAST($1):DOUBLE, CAST($0):DOUBLE)")]
+
 # Six side-effect-free AND-ed range / equality conjuncts over Zipf(1.2) columns
 # whose support is shifted per batch, so each conjunct's selectivity moves from
 # about 0.1% to about 90% between batches ($3 and $7 are carried, not tested).

@@ -20,9 +20,7 @@ from helpers import random_table
 SUM, SUM0, MIN, MAX, COUNT_VALID, COUNT_ALL, MEAN = range(7)
 
 # the TPC-H Q1 shape over the order-line columns: group by the two flags
-Q1_AGGS = [(SUM, "$0"), (SUM, "$1"), (SUM, "*(*($1, -(100, $2)), +(100, $3))"),
-           (SUM, "/(CAST($1):DOUBLE, CAST($0):DOUBLE)"), (MEAN, "$0"), (MEAN, "/(CAST($2):DOUBLE, 100.0)"),
-           (COUNT_ALL, ""), (MIN, "$4"), (MAX, "/(CAST($1):DOUBLE, CAST($0):DOUBLE)")]
+Q1_AGGS = W.C5_AGGREGATIONS
 
 
 def _sorted(cols, nk):
