@@ -259,10 +259,10 @@ def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
     """Fused filter + group-by aggregation (gx_filter_aggregate) on the
     order-line columns with TPC-H Q1's aggregation shape (C5 condition, keys
     $5, $6, nine aggregations), inputs resident: rows/s and HBM GB/s of the
-    aggregation kernel against the measured peak.  Beside it, the filter +
-    projection of the same rows (gx_filter_project of the C5 plan), which
-    materialises what an unfused aggregation would read back.  A sample's
-    groups are checked against the CPU oracle."""
+    aggregation kernel against the measured peak.  Beside it the unfused
+    chain: gx_filter_project materialises the keys and aggregation inputs, and
+    gx_filter_aggregate reads them back; and the C5 filter + projection alone.
+    A sample's groups are checked against the CPU oracle."""
     import numpy as np
     import torch
     import blazingsql_gb300 as g
@@ -294,11 +294,28 @@ def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
         out, groups = g.filter_aggregate(cols, W.C5_CONDITION, W.C5_AGG_KEYS, W.C5_AGGREGATIONS, stream=stream)
         g.api.free_columns(out, stream)
 
+    # unfused: the filter + projection materialises the keys and the
+    # aggregation inputs, then an aggregation reads them back
+    nk = len(W.C5_AGG_KEYS)
+    mat = [f"${c}" for c in W.C5_AGG_KEYS]
+    agg2 = []
+    for kind, e in W.C5_AGGREGATIONS:
+        if e and e not in mat:
+            mat.append(e)
+        agg2.append((kind, f"${mat.index(e)}" if e else ""))
+
+    def unfused():
+        out = g.filter_project(cols, W.C5_CONDITION, mat, stream=stream)
+        res, _ = g.filter_aggregate(out, None, list(range(nk)), agg2, stream=stream)
+        g.api.free_columns(res, stream)
+        g.api.free_columns(out, stream)
+
     def fp():
         out = g.filter_project(cols, W.C5_CONDITION, W.C5_PROJECTIONS, stream=stream)
         g.api.free_columns(out, stream)
 
     agg_ms, agg_kernel_ms = timed(agg)
+    unfused_ms, unfused_kernel_ms = timed(unfused)
     fp_ms, fp_kernel_ms = timed(fp)
     in_bytes = rows * w.in_bytes_per_row
     peak, peak_kind = measured_peak_hbm()
@@ -343,7 +360,8 @@ def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
         "groups": groups, "oracle_sample_rows": ns, "matches_oracle": bool(ok),
         "filter_project_rows_per_s": rows / (fp_ms / 1e3), "filter_project_ms": fp_ms,
         "filter_project_kernel_ms": fp_kernel_ms,
-        "fused_vs_filter_project": fp_ms / agg_ms,
+        "unfused_ms": unfused_ms, "unfused_kernel_ms": unfused_kernel_ms,
+        "fused_vs_unfused": unfused_ms / agg_ms,
     }
 
 
