@@ -211,6 +211,9 @@ AggPlan::AggPlan(const std::vector<int>& schema, const std::vector<bool>& nullab
   // instruction bound.  Measured on GB300 at 2^26 order-line rows: the Q1 shape
   // (6 groups) takes 2.48 / 2.49 / 3.01 ms with 8 / 20 / 40 KB tables; grouped
   // by ship date (2557 groups, mostly in the global table) 8.1 / 8.8 / 16.8 ms.
+  const size_t per_slot = 4 + 4 + 8 + 8 * std::max<size_t>(key_cols.size(), 1) +
+                          16 * std::max<size_t>(layout_.kinds.size(), 1);
+  int slots = 256;
   const int budget = std::getenv("GX_AGG_SMEM_KB") ? std::atoi(std::getenv("GX_AGG_SMEM_KB")) : 8;
   while (slots > 16 && (size_t)slots * per_slot > (size_t)budget * 1024) slots >>= 1;
   layout_.smem_slots = slots;
