@@ -155,6 +155,10 @@ def lib():
     L.gx_debug_aggregate_check.argtypes = [P(C.c_int32), P(C.c_uint8), C.c_int, C.c_char_p, P(C.c_int), C.c_int,
                                            P(C.c_char_p), P(C.c_int), C.c_int, P(C.c_int32), P(C.c_int32),
                                            P(C.c_int32), P(StatusInfo)]
+    L.gx_skip_data_rewrite.argtypes = [C.c_char_p, P(C.c_int), C.c_int, C.c_int, C.c_char_p, C.c_int, P(C.c_int),
+                                       P(StatusInfo)]
+    L.gx_skip_data_filter.argtypes = [P(ColumnView), P(C.c_char_p), C.c_int, P(C.c_char_p), C.c_int, C.c_char_p,
+                                      P(Column), P(C.c_int64), P(C.c_int), C.c_void_p, P(StatusInfo)]
     L.gx_plan_execute_host.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(Column), P(C.c_int64), C.c_void_p,
                                        P(StatusInfo)]
     L.gx_learner_prepare.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_void_p, P(StatusInfo)]
@@ -187,6 +191,7 @@ EXPORTED_SYMBOLS = [
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_prepare", "gx_learner_save",
     "gx_learner_execute_batches", "gx_plan_execute_host", "gx_filter_aggregate", "gx_debug_aggregate_check",
+    "gx_skip_data_rewrite", "gx_skip_data_filter",
     "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
     "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",

@@ -589,6 +589,39 @@ def filter_aggregate(table: Table, condition: Optional[str], group_columns: Sequ
     return _wrap(outs, nk + na, s), groups.value
 
 
+def skip_data_rewrite(condition: str, dropped: Sequence[int] = (), prefix_form: bool = False) -> Tuple[str, bool]:
+    """gx_skip_data_rewrite: the row-group statistics form of a condition
+    (no GPU).  Returns (text, usable)."""
+    d = (C.c_int * max(1, len(dropped)))(*dropped)
+    buf = C.create_string_buffer(8192)
+    usable = C.c_int(0)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_skip_data_rewrite(condition.encode(), d, len(dropped), 1 if prefix_form else 0, buf,
+                                         len(buf), C.byref(usable), C.byref(st)), st)
+    return buf.value.decode(), bool(usable.value)
+
+
+def skip_data_filter(metadata: Table, metadata_names: Sequence[str], column_names: Sequence[str],
+                     table_scan: str, stream=None):
+    """gx_skip_data_filter: the (file, row group) ids a TableScan's condition
+    cannot rule out, from the row-group statistics table.  Returns
+    (columns, rows), or (None, 0) when the condition allows no pruning."""
+    keep: list = []
+    views, nc = _views(metadata, keep)
+    mnames = (C.c_char_p * max(1, nc))(*[x.encode() for x in metadata_names])
+    cnames = (C.c_char_p * max(1, len(column_names)))(*[x.encode() for x in column_names])
+    outs = (N.Column * 2)()
+    rows = C.c_int64(0)
+    unusable = C.c_int(0)
+    s = _stream_handle(stream)
+    st = N.StatusInfo()
+    N.check(N.lib().gx_skip_data_filter(views, mnames, nc, cnames, len(column_names), table_scan.encode(), outs,
+                                        C.byref(rows), C.byref(unusable), s, C.byref(st)), st)
+    if unusable.value:
+        return None, 0
+    return _wrap(outs, 2, s), rows.value
+
+
 def aggregate_check(schema: Sequence[int], has_mask: Sequence[bool], condition: Optional[str],
                     group_columns: Sequence[int], aggregations: Sequence[Tuple[int, str]]):
     """gx_debug_aggregate_check: builds and NVRTC-compiles the aggregation

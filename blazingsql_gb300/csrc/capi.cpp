@@ -391,6 +391,87 @@ int gx_debug_aggregate_check(const int32_t* column_types, const uint8_t* column_
   });
 }
 
+int gx_skip_data_rewrite(const char* condition, const int* dropped_columns, int num_dropped, int prefix_form,
+                         char* buf, int buf_len, int* usable, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!condition || (num_dropped > 0 && !dropped_columns)) fail(GX_ERR_INVALID, "bad arguments");
+    std::vector<int> dropped(dropped_columns, dropped_columns + std::max(num_dropped, 0));
+    std::string prefix;
+    const std::string text = skip_data_rewrite(condition, dropped, &prefix);
+    if (usable) *usable = text.empty() ? 0 : 1;
+    const std::string& r = prefix_form ? prefix : text;
+    if (buf && buf_len > 0) std::snprintf(buf, (size_t)buf_len, "%s", r.c_str());
+  });
+}
+
+int gx_skip_data_filter(const gx_column_view* metadata, const char* const* metadata_names, int num_metadata_columns,
+                        const char* const* column_names, int num_columns, const char* table_scan, gx_column* out,
+                        int64_t* out_rows, int* unusable, void* stream, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!metadata || !metadata_names || num_metadata_columns < 2 || !column_names || num_columns < 0 || !table_scan ||
+        !out || !unusable)
+      fail(GX_ERR_INVALID, "bad arguments");
+    *unusable = 1;
+    out[0] = gx_column{};
+    out[1] = gx_column{};
+    if (out_rows) *out_rows = 0;
+    const std::string scan(table_scan);
+    std::string cond = named_expression(scan, "condition");
+    if (cond.empty()) cond = named_expression(scan, "filters");
+    if (cond.empty()) return;  // no condition: every row group is read
+    std::vector<int> projected;
+    const std::string projects = named_expression(scan, "projects");
+    if (projects.empty()) {
+      for (int i = 0; i < num_columns; i++) projected.push_back(i);
+    } else {
+      for (const auto& item : split_expression_list(projects, true)) projected.push_back(std::stoi(item));
+    }
+    auto meta = to_views(metadata, num_metadata_columns);
+    const int64_t rows = meta[0].size;
+    auto find = [&](const std::string& name) {
+      for (int i = 0; i < num_metadata_columns; i++)
+        if (metadata_names[i] && name == metadata_names[i]) return i;
+      return -1;
+    };
+    // [min, max] per projected column (a dummy pair for one without
+    // statistics, dropped from the condition), then the two id columns
+    std::vector<ColumnView> table;
+    std::vector<int> dropped;
+    void* dummy = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (size_t i = 0; i < projected.size(); i++) {
+      const int c = projected[i];
+      if (c < 0 || c >= num_columns || !column_names[c]) fail(GX_ERR_INVALID, "projected column out of range");
+      const std::string suffix = std::to_string(c) + "_" + column_names[c];
+      const int mn = find("min_" + suffix), mx = find("max_" + suffix);
+      if (mn >= 0 && mx >= 0) {
+        table.push_back(meta[mn]);
+        table.push_back(meta[mx]);
+      } else {
+        dropped.push_back((int)i);
+        if (!dummy) dummy = dev_alloc((size_t)std::max<int64_t>(rows, 1), s);
+        table.push_back({INT8, dummy, nullptr, 0, rows});
+        table.push_back({INT8, dummy, nullptr, 0, rows});
+      }
+    }
+    const int id0 = (int)table.size();
+    table.push_back(meta[num_metadata_columns - 2]);
+    table.push_back(meta[num_metadata_columns - 1]);
+    try {
+      const std::string expr = skip_data_rewrite(cond, dropped, nullptr);
+      if (!expr.empty()) {
+        auto ps = plan_for("skipdata", table, expr, {"$" + std::to_string(id0), "$" + std::to_string(id0 + 1)}, false);
+        ps->execute(table, out, out_rows, s);
+        *unusable = 0;
+      }
+    } catch (...) {
+      dev_free(dummy, s);
+      throw;
+    }
+    dev_free(dummy, s);
+  });
+}
+
 void gx_free_columns(gx_column* columns, int num_columns, void* stream) {
   if (!columns) return;
   for (int i = 0; i < num_columns; i++) free_column(columns[i], (cudaStream_t)stream);

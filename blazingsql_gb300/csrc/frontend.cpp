@@ -869,4 +869,117 @@ std::string rebuild(const ExprPtr& e) {
   return e->token + "(" + s + ")";
 }
 
+
+// ---------------------------------------------------------------- skip data
+// Row-group pruning predicate (ral::skip_data, engine/src/skip_data/
+// SkipDataProcessor.cpp): a TableScan condition over column $i becomes a
+// condition over its row-group statistics, $2i = min and $2i+1 = max.
+namespace {
+
+ExprPtr sd_none() {
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::OP;
+  e->token = "NONE";
+  return e;
+}
+
+bool sd_unary(const std::string& token) {
+  if (token == "NONE") return true;
+  auto it = op_table().find(token);
+  return it != op_table().end() && op_is_unary(it->second);
+}
+
+// skip_data_drop_transformer (:23-45): every node named v becomes NONE
+ExprPtr sd_drop(ExprPtr e, const std::string& v) {
+  if (e->kind == Expr::OP)
+    for (auto& c : e->ch) c = sd_drop(c, v);
+  if (e->token == v) return sd_none();
+  return e;
+}
+
+// skip_data_reducer (:167-212) with is_unsupported_binary_op / is_exclusion_unary_op
+// (skip_data/utils.cpp:12-37), children first
+ExprPtr sd_reduce(ExprPtr e) {
+  if (e->kind != Expr::OP) return e;
+  for (auto& c : e->ch) c = sd_reduce(c);
+  static const char* kSupported[] = {"=", ">", ">=", "<", "<=", "+", "-", "AND", "OR"};
+  bool supported = false;
+  for (const char* t : kSupported) supported |= e->token == t;
+  if (!supported || e->ch.size() != 2) return sd_none();
+  const bool l = e->ch[0]->kind == Expr::OP && sd_unary(e->ch[0]->token);
+  const bool r = e->ch[1]->kind == Expr::OP && sd_unary(e->ch[1]->token);
+  if (l && !r) return e->token == "AND" ? e->ch[1] : sd_none();
+  if (r && !l) return e->token == "AND" ? e->ch[0] : sd_none();
+  if (l && r) return sd_none();
+  return e;
+}
+
+ExprPtr sd_op(const std::string& token, ExprPtr a, ExprPtr b) {
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::OP;
+  e->token = token;
+  e->ch = {std::move(a), std::move(b)};
+  return e;
+}
+
+// transform_inc (:69-101): a column to its min (k 0) or max (k 1) statistic,
+// the "&&&" pair of a transformed sum / difference to its min or max form
+ExprPtr sd_inc(const ExprPtr& n, int k) {
+  if (n->kind == Expr::COL) {
+    auto e = std::make_shared<Expr>(*n);
+    e->col = 2 * n->col + k;
+    e->token = "$" + std::to_string(e->col);
+    return e;
+  }
+  if (n->kind == Expr::OP && n->token == "&&&") return n->ch[k];
+  return n;
+}
+
+// skip_data_transformer (:48-165), children first
+ExprPtr sd_transform(ExprPtr e) {
+  if (e->kind != Expr::OP) return e;
+  for (auto& c : e->ch) c = sd_transform(c);
+  const std::string& op = e->token;
+  if (e->ch.size() != 2) return e;
+  const ExprPtr& n = e->ch[0];
+  const ExprPtr& m = e->ch[1];
+  if (op == "=")
+    return sd_op("AND", sd_op("<=", sd_inc(n, 0), sd_inc(m, 1)), sd_op(">=", sd_inc(n, 1), sd_inc(m, 0)));
+  if (op == "<" || op == "<=") return sd_op(op, sd_inc(n, 0), sd_inc(m, 1));
+  if (op == ">" || op == ">=") return sd_op(op, sd_inc(n, 1), sd_inc(m, 0));
+  if (op == "+" || op == "-")
+    return sd_op("&&&", sd_op(op, sd_inc(n, 0), sd_inc(m, 0)), sd_op(op, sd_inc(n, 1), sd_inc(m, 1)));
+  return e;
+}
+
+// tokenizer_helper (parser/expression_tree.hpp:164-179): prefix form
+std::string sd_prefix(const ExprPtr& e) {
+  if (e->kind != Expr::OP || e->token.empty()) return e->token;
+  std::string s;
+  for (const auto& c : e->ch) s += (s.empty() ? "" : " ") + sd_prefix(c);
+  return e->token + (s.empty() ? "" : " " + s);
+}
+
+}  // namespace
+
+std::string skip_data_rewrite(const std::string& condition, const std::vector<int>& dropped,
+                              std::string* prefix_form) {
+  // replace_calcite_regex + expand_if_logical_op, then the parse tree
+  // (process_skipdata_for_table, SkipDataProcessor.cpp:270-271, 310)
+  const std::string norm = normalize_calcite(condition);
+  Parser p(norm);
+  ExprPtr root = p.expr();
+  nest_logical(root, norm.find("FLOOR") == std::string::npos);
+  for (int c : dropped) root = sd_drop(root, "$" + std::to_string(c));
+  // apply_skip_data_rules (:220-232)
+  root = sd_reduce(root);
+  if (root->token == "NONE") {
+    if (prefix_form) *prefix_form = "NONE";
+    return "";
+  }
+  root = sd_transform(root);
+  if (prefix_form) *prefix_form = sd_prefix(root);
+  return rebuild(root);
+}
+
 }  // namespace gx

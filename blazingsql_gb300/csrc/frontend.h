@@ -60,4 +60,15 @@ std::string rebuild(const ExprPtr& e);
 // Parse + lower without typing (used by tests of the lowering rules).
 ExprPtr parse_and_lower(const std::string& text);
 
+// The row-group pruning form of a TableScan condition (ral::skip_data,
+// engine/src/skip_data/SkipDataProcessor.cpp:215-232 and :23-212): operands
+// $i listed in `dropped` (columns without statistics) are removed, operators
+// other than = < <= > >= + - AND OR are removed (an AND keeps its other side,
+// anything else loses the whole comparison), then each comparison is
+// restated over $2i (min) and $2i+1 (max) of the columns.  Returns the new
+// condition's text, or "" when nothing usable is left; *prefix_form (optional)
+// receives the tree in the reference's prefix notation ("NONE" when unusable).
+std::string skip_data_rewrite(const std::string& condition, const std::vector<int>& dropped,
+                              std::string* prefix_form);
+
 }  // namespace gx

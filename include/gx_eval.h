@@ -261,6 +261,32 @@ int gx_debug_aggregate_check(const int32_t* column_types, const uint8_t* column_
                              const char* const* agg_inputs, const int* agg_kinds, int num_aggs, int32_t* registers,
                              int32_t* spill_bytes, int32_t* shared_bytes, gx_status_info* status);
 
+/* ---- skip-data: row groups a TableScan's condition can skip ---------------
+ *
+ * ral::skip_data::process_skipdata_for_table (engine/src/skip_data/
+ * SkipDataProcessor.cpp:252-350).  `metadata` is the table of row-group
+ * statistics with its column names: "min_<i>_<name>" / "max_<i>_<name>" per
+ * input column i that has statistics, and as its last two columns the file
+ * handle index and the row-group index.  column_names are the scanned
+ * table's column names.  The scan's condition=[..] (or filters=[..]) over its
+ * projects=[[..]] columns is restated over the statistics (a comparison over
+ * a column becomes one over its min and max; operators that cannot be
+ * restated are removed, an AND keeping its other side) and evaluated on the
+ * GPU over the metadata rows.  out[0], out[1] receive the two id columns of
+ * the row groups that may hold matching rows; *unusable is 1 (and out empty)
+ * when the condition allows no pruning (read every row group), as the
+ * reference's `true` result. */
+int gx_skip_data_filter(const gx_column_view* metadata, const char* const* metadata_names, int num_metadata_columns,
+                        const char* const* column_names, int num_columns, const char* table_scan, gx_column* out,
+                        int64_t* out_rows, int* unusable, void* stream, gx_status_info* status);
+
+/* The statistics form of a condition alone (no GPU): columns listed in
+ * dropped_columns have no statistics; buf receives the rewritten condition
+ * text, or with prefix_form the reference's prefix notation of the tree
+ * (as its tests print it); *usable is 0 when nothing usable is left. */
+int gx_skip_data_rewrite(const char* condition, const int* dropped_columns, int num_dropped, int prefix_form,
+                         char* buf, int buf_len, int* usable, gx_status_info* status);
+
 /* ---- batch runner: many batches, one persistent launch (no counterpart in
  * the reference) -------------------------------------------------------------
  *

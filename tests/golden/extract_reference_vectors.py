@@ -124,6 +124,30 @@ def extract(root):
                              "pairs": [{"input": re.search(r'query_part_%d = "(.*)";' % k, blk).group(1),
                                         "expected": re.search(r'expected_%d = "(.*)";' % k, blk).group(1)}
                                        for k in (1, 2)]}
+    # skip-data rewrite: the prefix-notation trees of the reference's tests,
+    # with the operands dropped before the rules where a test drops some
+    sd = "engine/tests/skipdata/expression_tree_test.cpp"
+    L = _lines(root, sd)
+    text = "\n".join(L)
+    cases = []
+    for m in re.finditer(r"TEST_F\(ExpressionTreeTest, (\w+)\)", text):
+        start = m.start()
+        nxt = text.find("TEST_F(", m.end())
+        blk = text[start:nxt if nxt >= 0 else len(text)]
+        # tests commented out line by line start with //
+        line_start = text.rfind("\n", 0, start) + 1
+        if text[line_start:start].strip().startswith("//"):
+            continue
+        pre = re.search(r'std::string prefix = "([^"]*)"', blk)
+        exp = re.search(r'std::string expected = "([^"]*)"', blk)
+        if not pre or not exp:
+            continue
+        drops = [int(x) for x in re.findall(r'drop_value\(tree, "\$(\d+)"\)', blk)]
+        first = text.count("\n", 0, start) + 1
+        last = first + blk.count("\n")
+        cases.append({"name": m.group(1), "input": pre.group(1), "expected": exp.group(1), "dropped": drops,
+                      "source": f"{sd}:{first}-{last}"})
+    out["skip_data_rewrite"] = {"source": sd, "cases": cases}
     return out
 
 
