@@ -208,3 +208,20 @@ def test_online_shape_tuning_same_rows(ora):
         assert_tables_equal(got, outs[0][0])
     exp = ora.filter_project(cols, W.C1_CONDITION, W.C1_PROJECTIONS)
     assert_tables_equal(outs[-1][0], exp)
+
+
+@pytest.mark.parametrize("query,spec", [
+    # the filter statements BatchJoinProcessing.cpp splits off inequality joins
+    # (its comments at :127, :132, :137), run by process_filter on the joined batch
+    ("LogicalFilter(condition=[>($5, $2)])", [(T.INT64, -50, 50)] * 6),
+    ("LogicalFilter(condition=[OR(AND($8, $9, $2, $3), AND($8, $9, $4, $5), AND($8, $9, $6, $5))])",
+     [(T.INT64, 0, 9)] * 2 + [(T.BOOL8, 0, 2)] * 8),
+    ("LogicalFilter(condition=[OR(AND(IS NULL($1), IS NULL($3)), IS TRUE(=($1 , $3)))])",
+     [(T.INT32, 0, 4)] * 4),
+])
+def test_post_join_filter_statements(gpu, ora, query, spec):
+    rng = np.random.default_rng(13)
+    cols = random_table(rng, 20_011, spec, null_frac=0.15)
+    got = gpu.process_filter(cols, query)
+    exp = ora.process_filter(cols, query)
+    assert_tables_equal(got, exp, what=query)
