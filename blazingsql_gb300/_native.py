@@ -47,7 +47,8 @@ class GxError(RuntimeError):
 
 class ColumnView(C.Structure):
     _fields_ = [("type_id", C.c_int32), ("reserved", C.c_int32), ("data", C.c_void_p),
-                ("null_mask", C.c_void_p), ("offset", C.c_int64), ("size", C.c_int64)]
+                ("null_mask", C.c_void_p), ("offset", C.c_int64), ("size", C.c_int64),
+                ("string_offsets", C.c_void_p)]
 
 
 class Column(C.Structure):

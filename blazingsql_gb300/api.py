@@ -20,7 +20,7 @@ from typing import List, Optional, Sequence, Tuple, Union
 import numpy as np
 
 from . import _native as N
-from .types import HostColumn, TypeId, np_dtype
+from .types import HostColumn, TypeId, np_dtype, pack_validity
 
 
 def _torch():
@@ -43,10 +43,27 @@ def _stream_handle(stream) -> int:
 class DeviceColumn:
     """A borrowed device column: raw byte tensors for data and validity words."""
     type_id: int
-    data: object                  # torch.uint8 tensor on the device
+    data: object                  # torch.uint8 tensor on the device (STRING: the characters)
     mask: Optional[object]        # torch.uint8 tensor (uint32 words) or None
     offset: int
     size: int
+    str_offsets: Optional[object] = None  # STRING: torch.int32 tensor of size + 1 offsets
+
+    @staticmethod
+    def from_strings(values: Sequence[Optional[str]], device: str = "cuda") -> "DeviceColumn":
+        """A STRING column (cudf layout: int32 offsets + UTF-8 characters);
+        None entries are NULL."""
+        torch = _torch()
+        enc = [b"" if v is None else v.encode("utf-8") for v in values]
+        offs = np.zeros(len(enc) + 1, dtype=np.int32)
+        offs[1:] = np.cumsum([len(e) for e in enc])
+        chars = np.frombuffer(b"".join(enc) or b"\0", dtype=np.uint8)
+        mask = None
+        if any(v is None for v in values):
+            mask = torch.from_numpy(pack_validity(np.array([v is not None for v in values])).view(np.uint8)
+                                    .copy()).to(device)
+        return DeviceColumn(TypeId.STRING, torch.from_numpy(chars.copy()).to(device), mask, 0, len(values),
+                            torch.from_numpy(offs).to(device))
 
     @staticmethod
     def from_host(col: HostColumn, device: str = "cuda") -> "DeviceColumn":
@@ -61,7 +78,7 @@ class DeviceColumn:
 
     def view(self) -> N.ColumnView:
         # cached per (tensors, offset, size): data_ptr() calls cost microseconds per batch
-        key = (id(self.data), id(self.mask), self.offset, self.size, self.type_id)
+        key = (id(self.data), id(self.mask), self.offset, self.size, self.type_id, id(self.str_offsets))
         cached = getattr(self, "_view_cache", None)
         if cached is not None and cached[0] == key:
             return cached[1]
@@ -71,6 +88,7 @@ class DeviceColumn:
         v.null_mask = self.mask.data_ptr() if self.mask is not None else None
         v.offset = self.offset
         v.size = self.size
+        v.string_offsets = self.str_offsets.data_ptr() if self.str_offsets is not None else None
         self._view_cache = (key, v)
         return v
 

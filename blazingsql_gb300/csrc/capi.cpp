@@ -15,6 +15,7 @@
 #include "plan.h"
 #include "runtime.h"
 #include "aggregate.h"
+#include "str_prepass.h"
 
 namespace gx {
 namespace {
@@ -225,6 +226,33 @@ void gx_plan_options_init(gx_plan_options* o) {
   o->use_tma = -1;
 }
 
+// The string pre-pass of one call: the columns it computed, released (stream
+// ordered) when the call's work has been enqueued.
+struct StringPrepass {
+  std::vector<gx_column> made;
+  cudaStream_t s = nullptr;
+  ~StringPrepass() {
+    for (auto& c : made) free_column(c, s);
+  }
+};
+
+// String operators over string columns in `cond` / `exprs` become columns
+// appended to `cols` (function_evaluator_transformer, LogicalProject.cpp:671-742).
+static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std::vector<std::string>& exprs,
+                           StringPrepass& pp) {
+  const std::vector<int> schema = schema_of(cols);
+  std::vector<std::string> texts;
+  if (cond) texts.push_back(*cond);
+  texts.insert(texts.end(), exprs.begin(), exprs.end());
+  std::vector<StringOp> ops;
+  rewrite_string_ops(texts, schema, ops);
+  if (ops.empty()) return;
+  size_t i = 0;
+  if (cond) *cond = texts[i++];
+  for (auto& e : exprs) e = texts[i++];
+  pp.made = run_string_prepass(cols, ops, pp.s);
+}
+
 int gx_evaluate_expressions(const gx_column_view* columns, int num_columns, const char* const* expressions,
                             int num_expressions, gx_column* out, void* stream, gx_status_info* status) {
   return guarded(status, [&] {
@@ -237,6 +265,9 @@ int gx_evaluate_expressions(const gx_column_view* columns, int num_columns, cons
     }
     if (ex.empty()) return;
     for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
+    StringPrepass pp;
+    pp.s = (cudaStream_t)stream;
+    string_prepass(cols, nullptr, ex, pp);
     auto ps = plan_for("eval", cols, "", ex, false);
     int64_t rows = 0;
     ps->execute(cols, out, &rows, (cudaStream_t)stream);
@@ -313,6 +344,9 @@ int gx_filter_project(const gx_column_view* columns, int num_columns, const char
       ex.push_back(preprocess_expression(expressions[i], schema));
     }
     for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
+    StringPrepass pp;
+    pp.s = (cudaStream_t)stream;
+    string_prepass(cols, &cond, ex, pp);
     auto ps = plan_for("fused", cols, cond, ex, true);
     ps->execute(cols, out, out_rows, (cudaStream_t)stream);
   });

@@ -1,6 +1,8 @@
 // frontend.cpp -- RexNode text -> typed expression tree (see frontend.h).
 #include "frontend.h"
 
+#include <functional>
+
 #include <cctype>
 #include <cerrno>
 #include <cmath>
@@ -980,6 +982,99 @@ std::string skip_data_rewrite(const std::string& condition, const std::vector<in
   root = sd_transform(root);
   if (prefix_form) *prefix_form = sd_prefix(root);
   return rebuild(root);
+}
+
+
+// ---------------------------------------------------------------- string pre-pass
+namespace {
+
+std::string unquote(const std::string& t) {
+  if (t.size() >= 2 && (t.front() == '\'' || t.front() == '"') && t.back() == t.front()) {
+    std::string r;
+    const std::string in = t.substr(1, t.size() - 2);
+    for (size_t i = 0; i < in.size(); i++) {
+      r += in[i];
+      if (in[i] == '\'' && i + 1 < in.size() && in[i + 1] == '\'') i++;  // '' -> '
+    }
+    return r;
+  }
+  return t;
+}
+
+bool is_string_literal(const ExprPtr& e) {
+  return e->kind == Expr::LIT && !e->token.empty() && (e->token.front() == '\'' || e->token.front() == '"');
+}
+
+}  // namespace
+
+void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>& schema,
+                        std::vector<StringOp>& ops) {
+  bool any = false;
+  for (int t : schema) any |= t == STRING;
+  if (!any) return;
+  auto strcol = [&](const ExprPtr& c) {
+    return c->kind == Expr::COL && c->col >= 0 && c->col < (int)schema.size() && schema[c->col] == STRING;
+  };
+  for (auto& text : texts) {
+    if (text.empty()) continue;
+    const std::string norm = normalize_calcite(text);
+    Parser p(norm);
+    ExprPtr root = p.expr();
+    nest_logical(root, norm.find("FLOOR") == std::string::npos);
+    bool touched = false;
+    std::function<ExprPtr(ExprPtr)> walk = [&](ExprPtr e) -> ExprPtr {
+      if (e->kind == Expr::COL) {
+        if (strcol(e))
+          fail(GX_ERR_UNSUPPORTED, "string column " + e->token +
+                                       " used outside LIKE, CHAR_LENGTH or a comparison with a string literal");
+        return e;
+      }
+      if (e->kind != Expr::OP) return e;
+      StringOp op;
+      bool hit = false;
+      const std::string& t = e->token;
+      if (t == "LIKE" && e->ch.size() == 2 && strcol(e->ch[0]) && is_string_literal(e->ch[1])) {
+        op.kind = StringOp::LIKE;
+        op.col = e->ch[0]->col;
+        op.literal = unquote(e->ch[1]->token);
+        // the reference hands the pattern to a regular-expression engine
+        // (LogicalProject.cpp:31-47, 128-131); only '%' and '_' are restated here
+        if (op.literal.find_first_of(".^$*+?()[]{}|\\") != std::string::npos)
+          fail(GX_ERR_UNSUPPORTED, "LIKE pattern with regular-expression characters: " + op.literal);
+        hit = true;
+      } else if (t == "CHAR_LENGTH" && e->ch.size() == 1 && strcol(e->ch[0])) {
+        op.kind = StringOp::CHAR_LENGTH;
+        op.col = e->ch[0]->col;
+        hit = true;
+      } else if ((t == "=" || t == "<>" || t == "<" || t == "<=" || t == ">" || t == ">=") && e->ch.size() == 2 &&
+                 ((strcol(e->ch[0]) && is_string_literal(e->ch[1])) ||
+                  (is_string_literal(e->ch[0]) && strcol(e->ch[1])))) {
+        const bool swapped = !strcol(e->ch[0]);
+        std::string o = t;
+        if (swapped) o = o == "<" ? ">" : o == ">" ? "<" : o == "<=" ? ">=" : o == ">=" ? "<=" : o;
+        op.kind = o == "=" ? StringOp::EQ : o == "<>" ? StringOp::NE : o == "<" ? StringOp::LT
+                : o == "<=" ? StringOp::LE : o == ">" ? StringOp::GT : StringOp::GE;
+        op.col = e->ch[swapped ? 1 : 0]->col;
+        op.literal = unquote(e->ch[swapped ? 0 : 1]->token);
+        hit = true;
+      }
+      if (hit) {
+        size_t k = 0;
+        while (k < ops.size() && !(ops[k] == op)) k++;
+        if (k == ops.size()) ops.push_back(op);
+        auto c = std::make_shared<Expr>();
+        c->kind = Expr::COL;
+        c->col = (int)(schema.size() + k);
+        c->token = "$" + std::to_string(c->col);
+        touched = true;
+        return c;
+      }
+      for (auto& c : e->ch) c = walk(c);
+      return e;
+    };
+    root = walk(root);
+    if (touched) text = rebuild(root);
+  }
 }
 
 }  // namespace gx

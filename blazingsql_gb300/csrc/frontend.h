@@ -60,6 +60,25 @@ std::string rebuild(const ExprPtr& e);
 // Parse + lower without typing (used by tests of the lowering rules).
 ExprPtr parse_and_lower(const std::string& text);
 
+// A string operator of the string pre-pass: LIKE(col, 'pattern'), a
+// comparison of a string column with a string literal, or CHAR_LENGTH(col).
+struct StringOp {
+  enum Kind { LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH };
+  Kind kind = LIKE;
+  int col = -1;
+  std::string literal;  // the pattern / literal, quotes removed
+  bool operator==(const StringOp& o) const { return kind == o.kind && col == o.col && literal == o.literal; }
+};
+
+// The string pre-pass of function_evaluator_transformer
+// (LogicalProject.cpp:671-742): in each (preprocessed) expression text, every
+// string operator over a STRING column of `schema` becomes the column
+// $(schema.size() + i) of op i (shared by equal operators).  A string column
+// used anywhere else fails with GX_ERR_UNSUPPORTED.  Texts without string
+// columns are returned as they are.
+void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>& schema,
+                        std::vector<StringOp>& ops);
+
 // The row-group pruning form of a TableScan condition (ral::skip_data,
 // engine/src/skip_data/SkipDataProcessor.cpp:215-232 and :23-212): operands
 // $i listed in `dropped` (columns without statistics) are removed, operators

@@ -80,11 +80,16 @@ std::vector<ColumnView> to_views(const gx_column_view* cols, int n) {
   std::vector<ColumnView> v;
   for (int i = 0; i < n; i++) {
     const gx_column_view& c = cols[i];
-    if (type_size(c.type_id) == 0) fail(GX_ERR_UNSUPPORTED, "unsupported column type " + std::to_string(c.type_id));
+    const bool str = c.type_id == STRING;
+    if (str && !c.string_offsets) fail(GX_ERR_INVALID, "a string column needs its offsets");
+    if (!str && type_size(c.type_id) == 0)
+      fail(GX_ERR_UNSUPPORTED, "unsupported column type " + std::to_string(c.type_id));
     if (c.size < 0 || c.offset < 0) fail(GX_ERR_INVALID, "negative column size/offset");
-    if (c.size > 0 && !c.data) fail(GX_ERR_INVALID, "column data pointer is null");
+    if (!str && c.size > 0 && !c.data) fail(GX_ERR_INVALID, "column data pointer is null");
     if (i > 0 && c.size != cols[0].size) fail(GX_ERR_INVALID, "columns of one table must have equal sizes");
-    v.push_back({c.type_id, c.data, c.null_mask, c.offset, c.size});
+    ColumnView cv{c.type_id, c.data, c.null_mask, c.offset, c.size};
+    if (str) cv.str_offsets = c.string_offsets;
+    v.push_back(cv);
   }
   return v;
 }

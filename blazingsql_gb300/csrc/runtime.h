@@ -21,6 +21,7 @@ struct ColumnView {
   const uint32_t* mask;
   int64_t offset;
   int64_t size;
+  const int32_t* str_offsets = nullptr;  // STRING columns: cudf offsets (data = characters)
 };
 
 std::vector<ColumnView> to_views(const gx_column_view* cols, int n);

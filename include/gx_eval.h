@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GX_ABI_VERSION 1
+#define GX_ABI_VERSION 2
 
 /* cudf::type_id numbering (cudf 21.08) */
 enum gx_type_id {
@@ -65,10 +65,16 @@ typedef struct gx_status_info {
 typedef struct gx_column_view {
   int32_t type_id;          /* enum gx_type_id */
   int32_t reserved;
-  const void* data;         /* device memory */
+  const void* data;         /* device memory (GX_TYPE_STRING: the characters) */
   const uint32_t* null_mask;/* device memory or NULL */
-  int64_t offset;           /* in elements */
+  int64_t offset;           /* in elements (rows) */
   int64_t size;             /* rows */
+  /* GX_TYPE_STRING only (cudf's strings column: offsets child + chars): device
+   * int32 offsets, row r spanning data[string_offsets[offset + r]] up to
+   * data[string_offsets[offset + r + 1]]; NULL for every other type.  String
+   * columns are inputs of the string pre-pass (LIKE, CHAR_LENGTH, = / <> with a
+   * string literal) of gx_evaluate_expressions and gx_filter_project. */
+  const int32_t* string_offsets;
 } gx_column_view;
 
 typedef struct gx_column {
