@@ -120,9 +120,29 @@ class NativeColumn:
         v = N.ColumnView()
         v.type_id, v.data, v.null_mask, v.offset, v.size = self._c.type_id, self._c.data, self._c.null_mask, 0, \
             self._c.size
+        v.string_offsets = self._c.string_offsets
         return v
 
+    def to_strings(self) -> List[Optional[str]]:
+        """A STRING column's rows (None where NULL)."""
+        if self.type_id != TypeId.STRING:
+            raise TypeError("not a string column")
+        n = self.size
+        offs = np.zeros(n + 1, dtype=np.int32)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_string_offsets_to_host(C.byref(self._c), offs.ctypes.data, self._stream, C.byref(st)), st)
+        chars = np.zeros(max(int(self._c.string_bytes), 1), dtype=np.uint8)
+        nwords = max(16, ((n + 31) // 32 + 15) // 16 * 16)
+        mask = np.zeros(nwords, dtype=np.uint32)
+        N.check(N.lib().gx_column_to_host(C.byref(self._c), chars.ctypes.data, mask.ctypes.data, self._stream,
+                                          C.byref(st)), st)
+        raw = chars.tobytes()
+        return [raw[offs[i]:offs[i + 1]].decode("utf-8") if (mask[i >> 5] >> (i & 31)) & 1 else None
+                for i in range(n)]
+
     def to_host(self) -> HostColumn:
+        if self.type_id == TypeId.STRING:
+            raise TypeError("a string column: use to_strings()")
         dt = np_dtype(self.type_id)
         data = np.empty(max(self.size, 1), dtype=dt)
         nwords = max(16, ((self.size + 31) // 32 + 15) // 16 * 16)
@@ -137,6 +157,7 @@ class NativeColumn:
             N.lib().gx_free_columns(C.byref(self._c), 1, self._stream)
             self._c.data = None
             self._c.null_mask = None
+            self._c.string_offsets = None
 
     def __del__(self):
         try:
@@ -161,7 +182,8 @@ def _views(table: Table, keep: list):
 
 def _wrap(outs, n: int, stream: int) -> List[NativeColumn]:
     return [NativeColumn(N.Column(outs[i].type_id, 0, outs[i].data, outs[i].null_mask, outs[i].size,
-                                  outs[i].capacity), stream) for i in range(n)]
+                                  outs[i].capacity, outs[i].string_offsets, outs[i].string_bytes), stream)
+            for i in range(n)]
 
 
 def evaluate_expressions(table: Table, expressions: Sequence[str], stream=None) -> List[NativeColumn]:

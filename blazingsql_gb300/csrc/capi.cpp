@@ -215,7 +215,7 @@ using namespace gx;
 extern "C" {
 
 const char* gx_version(void) {
-  static const char* v = "gx-eval 0.1 (sm_103a; NVRTC plan kernels; abi " "1" ")";
+  static const char* v = "gx-eval 0.1 (sm_103a; NVRTC plan kernels; abi " "2" ")";
   return v;
 }
 
@@ -227,14 +227,24 @@ void gx_plan_options_init(gx_plan_options* o) {
 }
 
 // The string pre-pass of one call: the columns it computed, released (stream
-// ordered) when the call's work has been enqueued.
+// ordered) when the call's work has been enqueued, unless an output took one.
 struct StringPrepass {
   std::vector<gx_column> made;
   cudaStream_t s = nullptr;
   ~StringPrepass() {
-    for (auto& c : made) free_column(c, s);
+    for (auto& c : made)
+      if (c.data || c.null_mask) free_column(c, s);
   }
 };
+
+// A CASE condition of the pre-pass evaluated into a BOOL8 column.
+static gx_column eval_condition(const std::vector<ColumnView>& cols, const std::string& text, cudaStream_t s) {
+  auto ps = plan_for("eval", cols, "", {text}, false);
+  gx_column out{};
+  int64_t rows = 0;
+  ps->execute(cols, &out, &rows, s);
+  return out;
+}
 
 // String operators over string columns in `cond` / `exprs` become columns
 // appended to `cols` (function_evaluator_transformer, LogicalProject.cpp:671-742).
@@ -250,7 +260,98 @@ static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std
   size_t i = 0;
   if (cond) *cond = texts[i++];
   for (auto& e : exprs) e = texts[i++];
-  pp.made = run_string_prepass(cols, ops, pp.s);
+  const cudaStream_t s = pp.s;
+  pp.made = run_string_prepass(cols, ops, s, [s](const std::vector<ColumnView>& c, const std::string& t) {
+    return eval_condition(c, t, s);
+  });
+}
+
+// evaluate_expressions / process_filter / filter + project over a table that
+// may hold string columns.  The string pre-pass runs first.  Expressions that
+// are a whole string column or string literal are string outputs: without a
+// condition a string column is copied (the reference deep-copies `$i`
+// outputs, LogicalProject.cpp:829, and moves a computed one, :885-887) and a
+// literal repeated (:825); with a condition the plan kernel also writes each
+// kept row's input row (GX_ROW_INDEX), and the string outputs are gathered
+// through it (apply_boolean_mask's gather, LogicalFilter.cpp:22-29).  Every
+// other expression runs in one plan kernel.
+static void evaluate_with_strings(std::vector<ColumnView> cols, std::string cond, std::vector<std::string> ex,
+                                  bool filtering, gx_column* out, int64_t* out_rows, cudaStream_t s,
+                                  const char* kind, bool rand_by_out) {
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const size_t ncols0 = cols.size();
+  StringPrepass pp;
+  pp.s = s;
+  string_prepass(cols, filtering ? &cond : nullptr, ex, pp);
+  if (filtering) {
+    const int c = passthrough_column(cond);
+    if ((c >= 0 && c < (int)cols.size() && cols[c].type == STRING) || string_literal_value(cond, nullptr))
+      fail(GX_ERR_TYPE, "the condition is a string");
+  }
+  // classify the outputs: -2 plan output, -1 string literal, >= 0 string column
+  std::vector<int> src(ex.size(), -2);
+  std::vector<std::string> lit(ex.size());
+  std::vector<std::string> num;
+  std::vector<int> num_pos;
+  bool gather = false;
+  for (size_t i = 0; i < ex.size(); i++) {
+    const int c = passthrough_column(ex[i]);
+    if (c >= 0 && c < (int)cols.size() && cols[c].type == STRING) {
+      src[i] = c;
+      gather |= filtering;
+    } else if (string_literal_value(ex[i], &lit[i])) {
+      src[i] = -1;
+    } else {
+      num.push_back(ex[i]);
+      num_pos.push_back((int)i);
+    }
+  }
+  // a filter whose outputs are all literals still needs its row count
+  const bool row_index = filtering && (gather || num.empty());
+  if (row_index) num.push_back("GX_ROW_INDEX()");
+  std::vector<gx_column> tmp(num.size());
+  for (auto& c : tmp) c = gx_column{};
+  for (size_t i = 0; i < ex.size(); i++) out[i] = gx_column{};
+  int64_t rows = n;
+  try {
+    if (!num.empty()) {
+      auto ps = plan_for(kind, cols, filtering ? cond : std::string(), num, rand_by_out);
+      ps->execute(cols, tmp.data(), &rows, s);
+      for (size_t j = 0; j < num_pos.size(); j++) {
+        out[num_pos[j]] = tmp[j];
+        tmp[j] = gx_column{};
+      }
+    }
+    const int32_t* map = row_index ? (const int32_t*)tmp.back().data : nullptr;
+    for (size_t i = 0; i < ex.size(); i++) {
+      if (src[i] == -2) continue;
+      StrSource a, none;
+      if (src[i] == -1) {
+        a.kind = StrSource::LITERAL;
+        a.literal = lit[i];
+        out[i] = build_strings(a, none, nullptr, nullptr, rows, s);
+        continue;
+      }
+      const size_t k = (size_t)src[i] - ncols0;
+      if (!filtering && src[i] >= (int)ncols0 && k < pp.made.size() && pp.made[k].data) {
+        out[i] = pp.made[k];  // a computed string column moves to the output
+        pp.made[k] = gx_column{};
+        continue;
+      }
+      a.kind = StrSource::COLUMN;
+      a.col = cols[src[i]];
+      out[i] = build_strings(a, none, filtering ? map : nullptr, nullptr, rows, s);
+    }
+  } catch (...) {
+    for (size_t i = 0; i < ex.size(); i++)
+      if (out[i].data || out[i].null_mask) free_column(out[i], s);
+    for (auto& c : tmp)
+      if (c.data || c.null_mask) free_column(c, s);
+    throw;
+  }
+  for (auto& c : tmp)
+    if (c.data || c.null_mask) free_column(c, s);
+  if (out_rows) *out_rows = rows;
 }
 
 int gx_evaluate_expressions(const gx_column_view* columns, int num_columns, const char* const* expressions,
@@ -264,13 +365,7 @@ int gx_evaluate_expressions(const gx_column_view* columns, int num_columns, cons
       ex.emplace_back(expressions[i]);
     }
     if (ex.empty()) return;
-    for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
-    StringPrepass pp;
-    pp.s = (cudaStream_t)stream;
-    string_prepass(cols, nullptr, ex, pp);
-    auto ps = plan_for("eval", cols, "", ex, false);
-    int64_t rows = 0;
-    ps->execute(cols, out, &rows, (cudaStream_t)stream);
+    evaluate_with_strings(cols, "", ex, false, out, nullptr, (cudaStream_t)stream, "eval", false);
   });
 }
 
@@ -288,10 +383,8 @@ int gx_process_project(const gx_column_view* columns, int num_columns, const cha
       if (e.find(" OVER ") != std::string::npos) fail(GX_ERR_UNSUPPORTED, "window functions are out of scope");
       e = preprocess_expression(e, schema);
     }
-    for (size_t i = 0; i < exprs.size(); i++) out[i] = gx_column{};
-    auto ps = plan_for("eval", cols, "", exprs, false);
-    int64_t rows = 0;
-    ps->execute(cols, out, &rows, (cudaStream_t)stream);
+    if (!exprs.empty())
+      evaluate_with_strings(cols, "", exprs, false, out, nullptr, (cudaStream_t)stream, "eval", false);
     *num_out = (int)exprs.size();
     if (out_names && name_len > 0)
       for (size_t i = 0; i < names.size(); i++)
@@ -304,11 +397,23 @@ int gx_process_filter(const gx_column_view* columns, int num_columns, const char
   return guarded(status, [&] {
     if (!query_part || (num_columns > 0 && !out)) fail(GX_ERR_INVALID, "bad arguments");
     auto cols = to_views(columns, num_columns);
+    const cudaStream_t s = (cudaStream_t)stream;
     const int64_t n = cols.empty() ? 0 : cols[0].size;
     if (n == 0) {  // LogicalFilter.cpp:36-38: empty input -> empty_like, no parsing
-      for (int i = 0; i < num_columns; i++) {
-        out[i] = alloc_column(cols[i].type, 0, (cudaStream_t)stream);
-        launch_fill_mask(out[i].null_mask, 0, false, 16, (cudaStream_t)stream);
+      for (int i = 0; i < num_columns; i++) out[i] = gx_column{};
+      try {
+        for (int i = 0; i < num_columns; i++) {
+          if (cols[i].type == STRING) {
+            out[i] = build_strings(StrSource{}, StrSource{}, nullptr, nullptr, 0, s);
+          } else {
+            out[i] = alloc_column(cols[i].type, 0, s);
+            launch_fill_mask(out[i].null_mask, 0, false, 16, s);
+          }
+        }
+      } catch (...) {
+        for (int i = 0; i < num_columns; i++)
+          if (out[i].data || out[i].null_mask) free_column(out[i], s);
+        throw;
       }
       if (out_rows) *out_rows = 0;
       return;
@@ -320,12 +425,8 @@ int gx_process_filter(const gx_column_view* columns, int num_columns, const char
     cond = preprocess_expression(cond, schema_of(cols));
     // every input column compacted = the projections $0..$k-1 of the filtered rows
     std::vector<std::string> all;
-    for (int i = 0; i < num_columns; i++) {
-      out[i] = gx_column{};
-      all.push_back("$" + std::to_string(i));
-    }
-    auto ps = plan_for("filter", cols, cond, all, false);
-    ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+    for (int i = 0; i < num_columns; i++) all.push_back("$" + std::to_string(i));
+    evaluate_with_strings(cols, cond, all, true, out, out_rows, s, "filter", false);
   });
 }
 
@@ -343,12 +444,7 @@ int gx_filter_project(const gx_column_view* columns, int num_columns, const char
       if (!expressions[i]) fail(GX_ERR_INVALID, "null expression");
       ex.push_back(preprocess_expression(expressions[i], schema));
     }
-    for (int i = 0; i < num_expressions; i++) out[i] = gx_column{};
-    StringPrepass pp;
-    pp.s = (cudaStream_t)stream;
-    string_prepass(cols, &cond, ex, pp);
-    auto ps = plan_for("fused", cols, cond, ex, true);
-    ps->execute(cols, out, out_rows, (cudaStream_t)stream);
+    evaluate_with_strings(cols, cond, ex, !cond.empty(), out, out_rows, (cudaStream_t)stream, "fused", true);
   });
 }
 
@@ -516,7 +612,8 @@ int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_m
   return guarded(status, [&] {
     if (!column) fail(GX_ERR_INVALID, "null column");
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t bytes = (size_t)column->size * type_size(column->type_id);
+    const size_t bytes = column->type_id == STRING ? (size_t)column->string_bytes
+                                                   : (size_t)column->size * type_size(column->type_id);
     if (bytes && host_data)
       check_cuda(cudaMemcpyAsync(host_data, column->data, bytes, cudaMemcpyDeviceToHost, s), "column to host");
     if (host_mask) {
@@ -525,6 +622,19 @@ int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_m
         check_cuda(cudaMemcpyAsync(host_mask, column->null_mask, words * 4, cudaMemcpyDeviceToHost, s), "mask to host");
     }
     check_cuda(cudaStreamSynchronize(s), "column to host sync");
+  });
+}
+
+int gx_string_offsets_to_host(const gx_column* column, int32_t* host_offsets, void* stream,
+                              gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!column || !host_offsets) fail(GX_ERR_INVALID, "null argument");
+    if (column->type_id != STRING || !column->string_offsets) fail(GX_ERR_TYPE, "not a string column");
+    cudaStream_t s = (cudaStream_t)stream;
+    check_cuda(cudaMemcpyAsync(host_offsets, column->string_offsets, (size_t)(column->size + 1) * 4,
+                               cudaMemcpyDeviceToHost, s),
+               "offsets to host");
+    check_cuda(cudaStreamSynchronize(s), "offsets to host sync");
   });
 }
 

@@ -505,6 +505,7 @@ class Parser {
       Token tt = tok_;
       accept(T_IDENT);
       e->lit_type = type_from_token(tt.v);
+      e->lit_type_token = tt.v;
     } else {
       e->lit_type = infer_literal_type(t);
     }
@@ -518,7 +519,7 @@ class Parser {
 // ---------------------------------------------------------------- operators
 const std::unordered_map<std::string, Op>& op_table() {
   static const std::unordered_map<std::string, Op> M = {
-      {"BLZ_RND", OP_RAND}, {"NOT", OP_NOT}, {"IS NOT TRUE", OP_IS_NOT_TRUE}, {"IS NOT FALSE", OP_IS_NOT_FALSE},
+      {"BLZ_RND", OP_RAND}, {"GX_ROW_INDEX", OP_ROW_INDEX}, {"NOT", OP_NOT}, {"IS NOT TRUE", OP_IS_NOT_TRUE}, {"IS NOT FALSE", OP_IS_NOT_FALSE},
       {"IS TRUE", OP_IS_TRUE}, {"SIN", OP_SIN}, {"ASIN", OP_ASIN}, {"COS", OP_COS}, {"ACOS", OP_ACOS},
       {"TAN", OP_TAN}, {"ATAN", OP_ATAN}, {"COT", OP_COTAN}, {"FLOOR", OP_FLOOR}, {"CEIL", OP_CEIL},
       {"ABS", OP_ABS}, {"LOG10", OP_LOG10}, {"LN", OP_LN}, {"EXP", OP_EXP}, {"BL_YEAR", OP_YEAR},
@@ -690,6 +691,10 @@ void annotate(Expr& e, const std::vector<int>& schema) {
   e.op = op_of(e.token);
   if (e.op == OP_RAND) {
     e.vtype = e.ktype = FLOAT64;
+    return;
+  }
+  if (e.op == OP_ROW_INDEX) {
+    e.vtype = e.ktype = INT32;
     return;
   }
   if (op_is_unary(e.op)) {
@@ -1005,16 +1010,67 @@ bool is_string_literal(const ExprPtr& e) {
   return e->kind == Expr::LIT && !e->token.empty() && (e->token.front() == '\'' || e->token.front() == '"');
 }
 
+// rebuild() keeping literals' explicit types, so a rewritten text types its
+// literals as the original did
+std::string rebuild_typed(const ExprPtr& e) {
+  if (e->kind == Expr::LIT) return e->lit_type_token.empty() ? e->token : e->token + ":" + e->lit_type_token;
+  if (e->kind != Expr::OP) return e->token;
+  std::string s;
+  for (const auto& c : e->ch) s += (s.empty() ? "" : ", ") + rebuild_typed(c);
+  return e->token + "(" + s + ")";
+}
+
+bool is_null_literal(const ExprPtr& e) { return e->kind == Expr::LIT && e->token == "null"; }
+
 }  // namespace
+
+int passthrough_column(const std::string& text) {
+  size_t b = 0, e = text.size();
+  while (b < e && std::isspace((unsigned char)text[b])) b++;
+  while (e > b && std::isspace((unsigned char)text[e - 1])) e--;
+  if (e - b < 2 || text[b] != '$') return -1;
+  for (size_t i = b + 1; i < e; i++)
+    if (!std::isdigit((unsigned char)text[i])) return -1;
+  return e - b > 10 ? -1 : std::atoi(text.c_str() + b + 1);
+}
+
+bool string_literal_value(const std::string& text, std::string* value) {
+  if (text.find('\'') == std::string::npos) return false;
+  const std::string norm = normalize_calcite(text);
+  Parser p(norm);
+  ExprPtr root = p.expr();
+  if (!is_string_literal(root)) return false;
+  if (value) *value = unquote(root->token);
+  return true;
+}
 
 void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>& schema,
                         std::vector<StringOp>& ops) {
   bool any = false;
   for (int t : schema) any |= t == STRING;
+  for (const auto& t : texts) any |= t.find('\'') != std::string::npos;
   if (!any) return;
+  // the schema grows by one column per operator
+  std::vector<int> types = schema;
   auto strcol = [&](const ExprPtr& c) {
-    return c->kind == Expr::COL && c->col >= 0 && c->col < (int)schema.size() && schema[c->col] == STRING;
+    return c->kind == Expr::COL && c->col >= 0 && c->col < (int)types.size() && types[c->col] == STRING;
   };
+  auto column_of = [&](const StringOp& op) {
+    size_t k = 0;
+    while (k < ops.size() && !(ops[k] == op)) k++;
+    if (k == ops.size()) {
+      ops.push_back(op);
+      types.push_back(op.result_type());
+    }
+    auto c = std::make_shared<Expr>();
+    c->kind = Expr::COL;
+    c->col = (int)(schema.size() + k);
+    c->token = "$" + std::to_string(c->col);
+    return c;
+  };
+  // a CASE operand evaluate_string_case_when_else takes: a string column, a
+  // string literal or a null literal (LogicalProject.cpp:616-623)
+  auto string_operand = [&](const ExprPtr& e) { return strcol(e) || is_string_literal(e) || is_null_literal(e); };
   for (auto& text : texts) {
     if (text.empty()) continue;
     const std::string norm = normalize_calcite(text);
@@ -1023,16 +1079,10 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
     nest_logical(root, norm.find("FLOOR") == std::string::npos);
     bool touched = false;
     std::function<ExprPtr(ExprPtr)> walk = [&](ExprPtr e) -> ExprPtr {
-      if (e->kind == Expr::COL) {
-        if (strcol(e))
-          fail(GX_ERR_UNSUPPORTED, "string column " + e->token +
-                                       " used outside LIKE, CHAR_LENGTH or a comparison with a string literal");
-        return e;
-      }
       if (e->kind != Expr::OP) return e;
-      StringOp op;
-      bool hit = false;
+      for (auto& c : e->ch) c = walk(c);
       const std::string& t = e->token;
+      StringOp op;
       if (t == "LIKE" && e->ch.size() == 2 && strcol(e->ch[0]) && is_string_literal(e->ch[1])) {
         op.kind = StringOp::LIKE;
         op.col = e->ch[0]->col;
@@ -1041,39 +1091,74 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
         // (LogicalProject.cpp:31-47, 128-131); only '%' and '_' are restated here
         if (op.literal.find_first_of(".^$*+?()[]{}|\\") != std::string::npos)
           fail(GX_ERR_UNSUPPORTED, "LIKE pattern with regular-expression characters: " + op.literal);
-        hit = true;
       } else if (t == "CHAR_LENGTH" && e->ch.size() == 1 && strcol(e->ch[0])) {
         op.kind = StringOp::CHAR_LENGTH;
         op.col = e->ch[0]->col;
-        hit = true;
       } else if ((t == "=" || t == "<>" || t == "<" || t == "<=" || t == ">" || t == ">=") && e->ch.size() == 2 &&
-                 ((strcol(e->ch[0]) && is_string_literal(e->ch[1])) ||
-                  (is_string_literal(e->ch[0]) && strcol(e->ch[1])))) {
+                 (strcol(e->ch[0]) || strcol(e->ch[1])) &&
+                 (strcol(e->ch[0]) || is_string_literal(e->ch[0])) &&
+                 (strcol(e->ch[1]) || is_string_literal(e->ch[1]))) {
         const bool swapped = !strcol(e->ch[0]);
         std::string o = t;
         if (swapped) o = o == "<" ? ">" : o == ">" ? "<" : o == "<=" ? ">=" : o == ">=" ? "<=" : o;
         op.kind = o == "=" ? StringOp::EQ : o == "<>" ? StringOp::NE : o == "<" ? StringOp::LT
                 : o == "<=" ? StringOp::LE : o == ">" ? StringOp::GT : StringOp::GE;
-        op.col = e->ch[swapped ? 1 : 0]->col;
-        op.literal = unquote(e->ch[swapped ? 0 : 1]->token);
-        hit = true;
-      }
-      if (hit) {
-        size_t k = 0;
-        while (k < ops.size() && !(ops[k] == op)) k++;
-        if (k == ops.size()) ops.push_back(op);
-        auto c = std::make_shared<Expr>();
-        c->kind = Expr::COL;
-        c->col = (int)(schema.size() + k);
-        c->token = "$" + std::to_string(c->col);
+        const ExprPtr& l = e->ch[swapped ? 1 : 0];
+        const ExprPtr& r = e->ch[swapped ? 0 : 1];
+        op.col = l->col;
+        if (strcol(r)) op.col2 = r->col;
+        else op.literal = unquote(r->token);
+      } else if (t == "CASE" && e->ch.size() >= 3 && e->ch.size() % 2 == 1) {
+        // CASE(c1, v1, ..., ck, vk, else) is FIRST_NON_MAGIC(MAGIC_IF_NOT(c1,
+        // v1), ...) nested to the right (expression_tree.hpp:200-220); from
+        // the innermost pair out, each pair whose THEN and ELSE are string
+        // operands becomes a string column, until one is not
+        ExprPtr cur = e->ch.back();
+        size_t i = e->ch.size() - 1;
+        bool folded = false;
+        while (i >= 2 && string_operand(e->ch[i - 1]) && string_operand(cur) &&
+               !(is_null_literal(e->ch[i - 1]) && is_null_literal(cur))) {
+          const ExprPtr& c = e->ch[i - 2];
+          const ExprPtr& v = e->ch[i - 1];
+          if (c->kind == Expr::LIT)  // RAL_EXPECTS, LogicalProject.cpp:627
+            fail(GX_ERR_UNSUPPORTED, "CASE operator not supported for condition expression literals");
+          StringOp cs;
+          cs.kind = StringOp::CASE;
+          cs.cond = rebuild_typed(c);
+          if (strcol(v)) cs.col = v->col;
+          else if (is_null_literal(v)) cs.then_null = true;
+          else cs.literal = unquote(v->token);
+          if (strcol(cur)) cs.col2 = cur->col;
+          else if (is_null_literal(cur)) cs.else_null = true;
+          else cs.literal2 = unquote(cur->token);
+          cur = column_of(cs);
+          folded = true;
+          i -= 2;
+        }
+        if (!folded) return e;
         touched = true;
-        return c;
+        if (i == 0) return cur;
+        e->ch.resize(i);
+        e->ch.push_back(cur);
+        return e;
+      } else {
+        return e;
       }
-      for (auto& c : e->ch) c = walk(c);
-      return e;
+      touched = true;
+      return column_of(op);
     };
     root = walk(root);
-    if (touched) text = rebuild(root);
+    // a string column left anywhere but the root is an unsupported use
+    std::function<void(const ExprPtr&, bool)> check = [&](const ExprPtr& e, bool top) {
+      if (strcol(e) && !top)
+        fail(GX_ERR_UNSUPPORTED, "string column " + e->token +
+                                     " used outside LIKE, CHAR_LENGTH, a comparison or a CASE with string results");
+      if (e->kind == Expr::LIT && is_string_literal(e) && !top)
+        fail(GX_ERR_UNSUPPORTED, "string literal " + e->token + " used outside a string operator");
+      for (const auto& c : e->ch) check(c, false);
+    };
+    check(root, true);
+    if (touched) text = rebuild_typed(root);
   }
 }
 

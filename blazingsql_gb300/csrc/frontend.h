@@ -28,6 +28,7 @@ struct Expr {
   int lit_type = EMPTY;       // LIT: declared / inferred type
   bool lit_valid = false;     // LIT: false for a null literal
   uint64_t lit_bits = 0;      // LIT: value as the kernel reads it (int64 or double bits)
+  std::string lit_type_token; // LIT: the explicit ":TYPE" of the text, if any
   int vtype = EMPTY;          // result type as expr_output_type_visitor computes it
   int ktype = EMPTY;          // result type as perform_interpreter_operation computes it
   std::vector<ExprPtr> ch;
@@ -60,24 +61,46 @@ std::string rebuild(const ExprPtr& e);
 // Parse + lower without typing (used by tests of the lowering rules).
 ExprPtr parse_and_lower(const std::string& text);
 
-// A string operator of the string pre-pass: LIKE(col, 'pattern'), a
-// comparison of a string column with a string literal, or CHAR_LENGTH(col).
+// A string operator of the string pre-pass: LIKE(col, 'pattern'),
+// CHAR_LENGTH(col), a comparison of a string column with a string literal or
+// with another string column, or a CASE whose result is a string.
 struct StringOp {
-  enum Kind { LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH };
+  enum Kind { LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH, CASE };
   Kind kind = LIKE;
-  int col = -1;
-  std::string literal;  // the pattern / literal, quotes removed
-  bool operator==(const StringOp& o) const { return kind == o.kind && col == o.col && literal == o.literal; }
+  int col = -1;         // the string column; CASE: the THEN column, or -1
+  std::string literal;  // the pattern / literal, quotes removed; CASE: the THEN literal
+  int col2 = -1;        // comparisons: the right-hand string column; CASE: the ELSE column, or -1
+  // CASE only: `cond` (text over the columns before this operator) selects
+  // THEN where it is true, ELSE where it is false or NULL
+  // (evaluate_string_case_when_else, LogicalProject.cpp:612-659); an operand
+  // without a column is its literal, or NULL when *_null is set
+  std::string cond;
+  std::string literal2;  // the ELSE literal
+  bool then_null = false, else_null = false;
+  bool operator==(const StringOp& o) const {
+    return kind == o.kind && col == o.col && literal == o.literal && col2 == o.col2 && cond == o.cond &&
+           literal2 == o.literal2 && then_null == o.then_null && else_null == o.else_null;
+  }
+  int result_type() const { return kind == CASE ? STRING : kind == CHAR_LENGTH ? INT32 : BOOL8; }
 };
 
 // The string pre-pass of function_evaluator_transformer
-// (LogicalProject.cpp:671-742): in each (preprocessed) expression text, every
-// string operator over a STRING column of `schema` becomes the column
-// $(schema.size() + i) of op i (shared by equal operators).  A string column
-// used anywhere else fails with GX_ERR_UNSUPPORTED.  Texts without string
-// columns are returned as they are.
+// (LogicalProject.cpp:671-742), children before parents as the reference's
+// node_transformer visits them: in each (preprocessed) expression text, every
+// string operator becomes the column $(schema.size() + i) of op i (shared by
+// equal operators), so a later operator can read an earlier one's column.
+// A string column (read or made) may then remain only as a whole expression
+// (a string output); anywhere else it fails with GX_ERR_UNSUPPORTED.
+// Texts without string columns or string literals are returned as they are.
 void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>& schema,
                         std::vector<StringOp>& ops);
+
+// The column a (rewritten) expression text passes through whole ("$n"), or -1.
+int passthrough_column(const std::string& text);
+
+// True when the whole expression is a string literal; *value receives it
+// without quotes.
+bool string_literal_value(const std::string& text, std::string* value);
 
 // The row-group pruning form of a TableScan condition (ral::skip_data,
 // engine/src/skip_data/SkipDataProcessor.cpp:215-232 and :23-212): operands

@@ -39,6 +39,7 @@ inline int type_size(int t) {
 enum Op : int32_t {
   OP_NONE = 0,
   OP_RAND,
+  OP_ROW_INDEX,  // internal: the input row of the current row (compaction maps)
   // unary
   OP_NOT, OP_ABS, OP_FLOOR, OP_CEIL, OP_SIN, OP_COS, OP_ASIN, OP_ACOS, OP_TAN, OP_COTAN, OP_ATAN,
   OP_LN, OP_LOG10, OP_EXP, OP_YEAR, OP_MONTH, OP_DAY, OP_DAYOFWEEK, OP_HOUR, OP_MINUTE, OP_SECOND,

@@ -320,6 +320,11 @@ class Gen {
       o << ind << v << " = true;\n";
       return;
     }
+    if (op == OP_ROW_INDEX) {
+      o << ind << b << " = (u64)row;\n";
+      o << ind << v << " = true;\n";
+      return;
+    }
     if (op_is_unary(op)) {
       const int x = n.a;
       const int lt = p_.nodes[x].ktype;

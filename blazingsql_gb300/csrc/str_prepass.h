@@ -1,9 +1,12 @@
 // str_prepass.h -- the string pre-pass (str_prepass.cu): string operators over string
-// columns evaluated into BOOL8 / INT32 columns before the plan kernels run.
+// columns evaluated into BOOL8 / INT32 / string columns before the plan kernels
+// run, and the builder of string output columns (copies, gathers, CASE).
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include <functional>
+#include <string>
 #include <vector>
 
 #include "frontend.h"
@@ -11,15 +14,39 @@
 
 namespace gx {
 
-// one operator over string column `op.col`, writing `out` (library column of
-// op.size rows: BOOL8, INT32 for CHAR_LENGTH); pattern_dev holds op.literal
-void launch_string_op(const ColumnView& col, const StringOp& op, const void* pattern_dev, gx_column& out,
-                      cudaStream_t s);
+// one operator over string column `op.col` (and `col2`, the right-hand column
+// of a comparison of two columns, or null), writing `out` (library column of
+// col.size rows: BOOL8, INT32 for CHAR_LENGTH); pattern_dev holds op.literal
+void launch_string_op(const ColumnView& col, const ColumnView* col2, const StringOp& op, const void* pattern_dev,
+                      gx_column& out, cudaStream_t s);
+
+// Where the rows of a string column being built come from: a string column
+// (`col`), a literal (`literal`, host bytes that build_strings copies to the
+// device) or NULL.
+struct StrSource {
+  enum Kind { COLUMN = 0, LITERAL = 1, NUL = 2 } kind = NUL;
+  ColumnView col{};
+  std::string literal;
+};
+
+// Builds a cudf strings column of `rows` rows (library-owned: characters in
+// `data`, offsets in `string_offsets`, validity always present):
+//  * map set: row o is a's row map[o] (a gather, a: a column);
+//  * cond set (a BOOL8 view of `rows` rows): row o is a's where cond is valid
+//    and true, else b's (cudf::copy_if_else, which the reference's string CASE
+//    calls, LogicalProject.cpp:639-655);
+//  * neither: row o is a's row o (a copy, or a literal repeated).
+// A NULL row is empty.  Returns once the column is complete on the stream
+// (the character count is read back to size the characters).
+gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* map, const ColumnView* cond,
+                        int64_t rows, cudaStream_t s);
 
 // Evaluates `ops` over `cols` and appends their columns to `cols` (column
-// ncols + i is op i).  The returned columns are the caller's to free once the
-// work that reads them has been enqueued.
-std::vector<gx_column> run_string_prepass(std::vector<ColumnView>& cols, const std::vector<StringOp>& ops,
-                                          cudaStream_t s);
+// ncols + i is op i).  eval_bool evaluates a CASE condition's text over the
+// columns so far into a BOOL8 column.  The returned columns are the caller's
+// to free once the work that reads them has been enqueued.
+std::vector<gx_column> run_string_prepass(
+    std::vector<ColumnView>& cols, const std::vector<StringOp>& ops, cudaStream_t s,
+    const std::function<gx_column(const std::vector<ColumnView>&, const std::string&)>& eval_bool);
 
 }  // namespace gx

@@ -72,8 +72,9 @@ typedef struct gx_column_view {
   /* GX_TYPE_STRING only (cudf's strings column: offsets child + chars): device
    * int32 offsets, row r spanning data[string_offsets[offset + r]] up to
    * data[string_offsets[offset + r + 1]]; NULL for every other type.  String
-   * columns are inputs of the string pre-pass (LIKE, CHAR_LENGTH, = / <> with a
-   * string literal) of gx_evaluate_expressions and gx_filter_project. */
+   * columns are read by the string pre-pass (LIKE, CHAR_LENGTH, comparisons,
+   * CASE with string results), passed through as outputs ($i) and compacted
+   * by gx_process_filter / gx_filter_project. */
   const int32_t* string_offsets;
 } gx_column_view;
 
@@ -84,6 +85,13 @@ typedef struct gx_column {
   uint32_t* null_mask;      /* device memory owned by this library, always present */
   int64_t size;             /* rows */
   int64_t capacity;         /* rows the buffers can hold (>= size) */
+  /* GX_TYPE_STRING outputs (a cudf strings column): `data` holds the
+   * characters, string_offsets the size + 1 int32 offsets (row r spans
+   * data[string_offsets[r]] up to data[string_offsets[r + 1]]; a NULL row is
+   * empty) and string_bytes = string_offsets[size].  All three are owned by
+   * the column and released by gx_free_columns.  NULL / 0 for other types. */
+  int32_t* string_offsets;
+  int64_t string_bytes;
 } gx_column;
 
 /* ---- reference-shaped entry points ------------------------------------ */
@@ -120,9 +128,14 @@ int gx_filter_project(const gx_column_view* columns, int num_columns, const char
 /* Releases columns returned by this library (stream-ordered). */
 void gx_free_columns(gx_column* columns, int num_columns, void* stream);
 
-/* Copies a column's first `size` rows and its mask words to host memory. */
+/* Copies a column's first `size` rows and its mask words to host memory.  For
+ * a GX_TYPE_STRING column host_data receives the string_bytes characters. */
 int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_mask,
                       void* stream, gx_status_info* status);
+
+/* The size + 1 offsets of a GX_TYPE_STRING column, to host memory. */
+int gx_string_offsets_to_host(const gx_column* column, int32_t* host_offsets, void* stream,
+                              gx_status_info* status);
 
 /* ---- compiled plans (batched execution-graph path) --------------------- */
 

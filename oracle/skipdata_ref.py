@@ -75,9 +75,17 @@ def parse(text: str) -> Node:
                     skip()
             pos += 1
             return Node(name, args)
-        m = re.match(r"'[^']*'|[^,()\s]+", s[pos:])
+        m = re.match(r"'[^']*'(?::[A-Z]+)?|[^,()\s]+", s[pos:])
         pos += m.end()
-        return Node(m.group(0).split(":")[0])
+        tok = m.group(0)
+        if tok.startswith("'"):
+            q = tok.rindex("'")
+            n = Node(tok[:q + 1])
+            n.suffix = tok[q + 2:]
+        else:
+            n = Node(tok.split(":")[0])
+            n.suffix = tok.split(":", 1)[1] if ":" in tok else ""
+        return n
 
     root = expr()
     return _nest(root)
@@ -156,10 +164,12 @@ def prefix(n: Node) -> str:
     return n.value
 
 
-def rebuild(n: Node) -> str:
+def rebuild(n: Node, typed: bool = False) -> str:
+    """Text of a tree; typed keeps literals' explicit ":TYPE"."""
     if n.op:
-        return n.value + "(" + ", ".join(rebuild(c) for c in n.children) + ")"
-    return n.value
+        return n.value + "(" + ", ".join(rebuild(c, typed) for c in n.children) + ")"
+    suffix = getattr(n, "suffix", "")
+    return n.value + (":" + suffix if typed and suffix and not n.var else "")
 
 
 def rewrite(condition: str, dropped: Sequence[int] = ()) -> Tuple[str, str]:

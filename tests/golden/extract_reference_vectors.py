@@ -148,7 +148,73 @@ def extract(root):
         cases.append({"name": m.group(1), "input": pre.group(1), "expected": exp.group(1), "dropped": drops,
                       "source": f"{sd}:{first}-{last}"})
     out["skip_data_rewrite"] = {"source": sd, "cases": cases}
+    # tables with string columns: filters that compact them and CASEs with
+    # string results (their inputs, query and expected columns)
+    out["string_tables"] = [
+        _string_table_test(root, "engine/tests/new-tests/filter_tests.cpp", "LogicalFilterWithStringsTest", "NoNulls"),
+        _string_table_test(root, "engine/tests/new-tests/filter_tests.cpp", "LogicalFilterWithStringsTest",
+                           "IneqWithNulls"),
+        _string_table_test(root, "engine/tests/new-tests/process_project.cpp", "ProjectTestString",
+                           "test_string_case"),
+        _string_table_test(root, "engine/tests/new-tests/process_project.cpp", "ProjectTestString",
+                           "test_string_nested_case"),
+    ]
     return out
+
+
+def _brace_groups(text):
+    """Top-level {...} groups of a wrapper's argument text."""
+    groups, depth, start = [], 0, None
+    for i, ch in enumerate(text):
+        if ch == '"':
+            continue
+        if ch == "{":
+            depth += 1
+            if depth == 1 or (depth == 2 and text.lstrip().startswith("{{")):
+                start = i + 1
+        elif ch == "}":
+            if start is not None and (depth == 1 or (depth == 2 and text.lstrip().startswith("{{"))):
+                groups.append(text[start:i])
+                start = None
+            depth -= 1
+    return groups
+
+
+def _wrapper_columns(block):
+    cols = []
+    pat = r'(strings_column_wrapper|fixed_width_column_wrapper<(\w+)>)\s+(\w+)\s*[\({](.*?)[\)}];'
+    for m in re.finditer(pat, block, re.S):
+        kind = "string" if m.group(1).startswith("strings") else m.group(2)
+        body = m.group(4)
+        groups = _brace_groups(body)
+        if kind == "string":
+            values = [bytes(v, "utf-8").decode("unicode_escape") for v in re.findall(r'"((?:[^"\\]|\\.)*)"', groups[0])]
+        elif kind == "bool":
+            values = [1 if w == "true" else 0 for w in re.findall(r"true|false", groups[0])]
+        else:
+            values = _numbers(groups[0])
+        valid = _numbers(groups[1]) if len(groups) > 1 else None
+        cols.append({"name": m.group(3), "kind": kind, "values": values, "valid": valid})
+    return cols
+
+
+def _string_table_test(root, rel, fixture, name):
+    L = _lines(root, rel)
+    text = "\n".join(L)
+    m = re.search(r"TEST_F\(%s, %s\)" % (fixture, name), text)
+    nxt = text.find("TEST_F(", m.end())
+    end = nxt if nxt >= 0 else len(text)
+    nxt_t = text.find("template", m.end())
+    if 0 <= nxt_t < end:
+        end = nxt_t
+    blk = text[m.start():end]
+    first = text.count("\n", 0, m.start()) + 1
+    last = first + blk.rstrip().count("\n")
+    cols = _wrapper_columns(blk)
+    query = re.search(r'"(Logical\w+\(.*?\))"', blk).group(1)
+    return {"name": f"{fixture}.{name}", "source": f"{rel}:{first}-{last}", "query": query,
+            "inputs": [c for c in cols if not c["name"].startswith("expected")],
+            "expected": [c for c in cols if c["name"].startswith("expected")]}
 
 
 def main():

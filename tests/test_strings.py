@@ -1,16 +1,25 @@
-"""String pre-pass: LIKE, CHAR_LENGTH and comparisons with string literals
-over cudf-layout string columns, evaluated on the GPU before the plan kernel,
-against the CPU oracle (oracle/strings_ref.py), which follows the reference's
-LIKE-to-regex translation and string_view comparisons."""
+"""Strings on the evaluator's path, against the CPU oracle
+(oracle/strings_ref.py) and the reference's own string-table tests:
+the string pre-pass (LIKE, CHAR_LENGTH, comparisons with string literals and
+between string columns, CASE with string results) evaluated on the GPU before
+the plan kernel, and string output columns (copies, literals, and the
+compaction of string columns by process_filter / filter_project)."""
 from __future__ import annotations
+
+import json
+import os
+import re
 
 import numpy as np
 import pytest
 
-from blazingsql_gb300.types import HostColumn, TypeId as T
+from blazingsql_gb300.types import HostColumn, TypeId as T, pack_validity
 from oracle import strings_ref
 
-from helpers import assert_tables_equal
+from helpers import assert_columns_equal, assert_tables_equal
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.json")))
+STRING_TABLES = {t["name"]: t for t in GOLD["string_tables"]}
 
 ALPHA = ["a", "b", "c", "é", "ab", "PROMO", "\n", "%", "x_y", "ß"]
 
@@ -73,6 +82,206 @@ def test_filter_with_like_matches_oracle():
     assert_tables_equal(got, exp, what="filter with LIKE")
 
 
+def _gold_table(t):
+    """(host columns with None at string positions, {position: strings}) of a golden test's inputs."""
+    cols, strings = [], {}
+    for i, c in enumerate(t["inputs"]):
+        valid = np.array(c["valid"], dtype=bool) if c["valid"] is not None else None
+        if c["kind"] == "string":
+            strings[i] = [v if valid is None or valid[k] else None for k, v in enumerate(c["values"])]
+            cols.append(None)
+        else:
+            assert c["kind"] == "int32_t"
+            cols.append(HostColumn(T.INT32, np.array(c["values"], dtype=np.int32),
+                                   pack_validity(valid) if valid is not None else None))
+    return cols, strings
+
+
+def _gold_expected(c):
+    valid = c["valid"]
+    if c["kind"] == "string":
+        return [v if valid is None or valid[k] else None for k, v in enumerate(c["values"])]
+    t = {"int32_t": T.INT32, "bool": T.BOOL8}[c["kind"]]
+    dt = np.int32 if t == T.INT32 else np.uint8
+    return HostColumn(t, np.array(c["values"], dtype=dt),
+                      pack_validity(np.array(valid, dtype=bool)) if valid is not None else None)
+
+
+def _compare(got, exp, what):
+    """got: HostColumn or list of strings (oracle) / NativeColumn (GPU); exp likewise."""
+    assert len(got) == len(exp), what
+    for i, (g, e) in enumerate(zip(got, exp)):
+        if hasattr(g, "to_strings") and g.type_id == T.STRING:
+            g = g.to_strings()
+        elif hasattr(g, "to_host"):
+            g = g.to_host()
+        if isinstance(e, list):
+            assert isinstance(g, list), f"{what} col {i}: expected strings"
+            assert g == e, f"{what} col {i}: {g[:8]} vs {e[:8]}"
+        else:
+            assert_columns_equal(g, e, 0, f"{what} col {i}")
+
+
+def _project_expr(query):
+    return re.fullmatch(r"LogicalProject\(EXPR\$0=\[(.*)\]\)", query).group(1)
+
+
+@pytest.mark.parametrize("name", sorted(STRING_TABLES))
+def test_reference_string_tables_oracle(name):
+    """The oracle reproduces the reference's string-table tests (filter_tests.cpp:174-215,
+    process_project.cpp:447-485)."""
+    t = STRING_TABLES[name]
+    cols, strings = _gold_table(t)
+    exp = [_gold_expected(c) for c in t["expected"]]
+    if t["query"].startswith("LogicalFilter"):
+        cond = re.search(r"condition=\[(.*)\]\)", t["query"]).group(1)
+        got, rows = strings_ref.process_filter(cols, strings, cond)
+        assert rows == len(t["expected"][0]["values"])
+    else:
+        got = strings_ref.evaluate_expressions(cols, strings, [_project_expr(t["query"])])
+    _compare(got, exp, name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(STRING_TABLES))
+def test_reference_string_tables_gpu(name):
+    """The reference's string-table tests through process_filter / process_project."""
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    t = STRING_TABLES[name]
+    cols, strings = _gold_table(t)
+    dev = [DeviceColumn.from_strings(strings[i]) if c is None else DeviceColumn.from_host(c)
+           for i, c in enumerate(cols)]
+    exp = [_gold_expected(c) for c in t["expected"]]
+    if t["query"].startswith("LogicalFilter"):
+        got = g.process_filter(dev, t["query"])
+    else:
+        got, _ = g.process_project(dev, t["query"])
+    _compare(got, exp, name)
+
+
+def _mixed_table(rng, n):
+    s0 = _strings(rng, n)
+    s3 = _strings(rng, n, 0.3)
+    x1 = HostColumn(T.INT64, rng.integers(-50, 50, n).astype(np.int64))
+    v2 = rng.random(n) > 0.1
+    x2 = HostColumn(T.FLOAT64, rng.normal(0, 10, n), pack_validity(v2))
+    return [None, x1, x2, None], {0: s0, 3: s3}
+
+
+def _device(cols, strings):
+    from blazingsql_gb300.api import DeviceColumn
+    return [DeviceColumn.from_strings(strings[i]) if c is None else DeviceColumn.from_host(c)
+            for i, c in enumerate(cols)]
+
+
+STRING_EXPRS = [
+    "$0", "$3", "'lit'", "$1",
+    "CASE(>($1, 0), $0, 'neg')", "CASE(>($1, 0), 'pos', $3)", "CASE(>($1, 0), $0, $3)",
+    "CASE(IS NULL($2), null, $0)", "CASE(<($2, 0.0), $3, null)",
+    "CASE(>($1, 20), 'big', <($1, -20), $0, =($1, 0), 'zero', $3)",
+    "CASE(LIKE($0, '%a%'), $3, 'no a')",
+    "=(CASE(>($1, 0), $0, 'x'), 'x')",
+    "CHAR_LENGTH(CASE(>($1, 0), $0, 'éé'))",
+    "=($0, $3)", "<($0, $3)", ">=($3, $0)", "<>($0, $3)",
+    "CASE(>($1, 0), +($1, 1), -($1, 1))",
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 37, 4099, 100_003])
+def test_string_outputs_match_oracle(n):
+    """String outputs (copies, literals, CASE with string results) and
+    column-to-column string comparisons."""
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(100 + n)
+    cols, strings = _mixed_table(rng, n)
+    got = g.evaluate_expressions(_device(cols, strings), STRING_EXPRS)
+    exp = strings_ref.evaluate_expressions(cols, strings, STRING_EXPRS)
+    _compare(got, exp, f"string outputs n={n}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 37, 4099, 100_003])
+def test_filter_compacts_string_columns(n):
+    """process_filter keeps every column, string columns included, in order."""
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(200 + n)
+    cols, strings = _mixed_table(rng, n)
+    dev = _device(cols, strings)
+    for cond in ["AND(>($1, 0), LIKE($0, '%b%'))", ">($3, 'b')", "OR(IS NULL($2), =($0, $3))", "<($1, 100)",
+                 "<($1, -100)"]:
+        got = g.process_filter(dev, f"LogicalFilter(condition=[{cond}])")
+        exp, rows = strings_ref.process_filter(cols, strings, cond)
+        assert got[0].size == rows
+        _compare(got, exp, f"process_filter {cond} n={n}")
+
+
+@pytest.mark.gpu
+def test_filter_project_string_outputs():
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(7)
+    n = 50_001
+    cols, strings = _mixed_table(rng, n)
+    cond = "AND(>($1, -10), NOT(LIKE($3, 'a%')))"
+    exprs = ["$3", "*($2, 2.0)", "CASE(>($1, 0), $0, 'neg')", "'k'", "$0", "CHAR_LENGTH($0)"]
+    got = g.filter_project(_device(cols, strings), cond, exprs)
+    exp, rows = strings_ref.filter_project(cols, strings, cond, exprs)
+    assert got[0].size == rows
+    _compare(got, exp, "filter_project with string outputs")
+
+
+@pytest.mark.gpu
+def test_string_column_views_with_offset():
+    """Views starting inside a string column (offset > 0): offsets and masks
+    are read from the view's first row."""
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    rng = np.random.default_rng(9)
+    n, k = 5000, 77
+    full = _strings(rng, n + k)
+    fx = HostColumn(T.INT64, rng.integers(-50, 50, n + k).astype(np.int64))
+    sc = DeviceColumn.from_strings(full)
+    xc = DeviceColumn.from_host(fx)
+    dev = [DeviceColumn(sc.type_id, sc.data, sc.mask, k, n, sc.str_offsets),
+           DeviceColumn(xc.type_id, xc.data, xc.mask, k, n)]
+    cols = [None, HostColumn(T.INT64, fx.data[k:].copy())]
+    strings = {0: full[k:]}
+    exprs = ["$0", "CASE(>($1, 0), $0, 'z')", "LIKE($0, '%a%')"]
+    _compare(g.evaluate_expressions(dev, exprs), strings_ref.evaluate_expressions(cols, strings, exprs), "offset view")
+    got = g.process_filter(dev, "LogicalFilter(condition=[>($1, 0)])")
+    exp, _ = strings_ref.process_filter(cols, strings, ">($1, 0)")
+    _compare(got, exp, "offset view filter")
+
+
+@pytest.mark.gpu
+def test_string_empty_inputs():
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    dev = [DeviceColumn.from_strings([]), DeviceColumn.from_host(HostColumn(T.INT32, np.zeros(0, np.int32)))]
+    out = g.process_filter(dev, "LogicalFilter(condition=[=($0, 'a')])")
+    assert [c.size for c in out] == [0, 0] and out[0].to_strings() == []
+    dev = [DeviceColumn.from_strings(["", None, ""]), DeviceColumn.from_host(HostColumn(T.INT32, np.arange(3, dtype=np.int32)))]
+    out = g.evaluate_expressions(dev, ["$0", "CASE(>($1, 0), $0, '')"])
+    assert out[0].to_strings() == ["", None, ""]
+    assert out[1].to_strings() == ["", None, ""]
+    out = g.process_filter(dev, "LogicalFilter(condition=[<($1, 0)])")
+    assert out[0].to_strings() == [] and out[1].size == 0
+
+
+def test_string_rewrite_oracle_rules():
+    """Children-first rewriting: a string CASE becomes a column that an
+    enclosing comparison then reads; CASE pairs fold from the innermost."""
+    texts, ops = strings_ref.rewrite(["=(CASE(=(MOD($0, 2), 0), $1, 'LOL'), 'LOL')"], [1], 2)
+    assert texts == ["$3"]
+    assert ops[0][0] == "CASE" and ops[1] == ("EQ", 2, "LOL")
+    texts, ops = strings_ref.rewrite(["CASE(>($0, 1), 'a', >($0, 0), $1, 'c')"], [1], 2)
+    assert texts == ["$3"] and [o[0] for o in ops] == ["CASE", "CASE"]
+    assert ops[1][2] == ("lit", "a") and ops[1][3] == ("col", 2)
+    with pytest.raises(ValueError):
+        strings_ref.rewrite(["+(CASE(>($0, 1), $1, 'a'), 1)"], [1], 2)
+
+
 @pytest.mark.gpu
 def test_string_errors():
     import blazingsql_gb300 as g
@@ -80,6 +289,10 @@ def test_string_errors():
     from blazingsql_gb300.api import DeviceColumn
     dev = [DeviceColumn.from_strings(["a", "b"]), DeviceColumn.from_host(HostColumn(T.INT64, np.arange(2)))]
     with pytest.raises(N.GxError, match="string column"):
-        g.evaluate_expressions(dev, ["$0"])                   # a string output is not produced
+        g.evaluate_expressions(dev, ["+($0, 1)"])            # a string column in arithmetic
     with pytest.raises(N.GxError, match="regular-expression"):
         g.evaluate_expressions(dev, ["LIKE($0, 'a.b')"])     # the reference's regex semantics are not restated
+    with pytest.raises(N.GxError, match="condition expression literals"):
+        g.evaluate_expressions(dev, ["CASE(true, $0, 'x')"])  # LogicalProject.cpp:627
+    with pytest.raises(N.GxError, match="condition is a string"):
+        g.process_filter(dev, "LogicalFilter(condition=[$0])")
