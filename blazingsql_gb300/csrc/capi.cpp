@@ -58,6 +58,7 @@ KernelConfig default_config() {
   c.native_f64_ops = env_int("GX_NATIVE_F64_OPS", -1);
   c.dense = env_int("GX_DENSE", 1) != 0;
   c.lazy_case = env_int("GX_LAZY_CASE", 1) != 0;
+  c.max_regs = env_int("GX_MAX_REGS", 0);
   return c;
 }
 
@@ -167,7 +168,7 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
   }
   k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
        std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case) + ':' +
-       std::to_string(cfg.native_f64_ops);
+       std::to_string(cfg.native_f64_ops) + ':' + std::to_string(cfg.max_regs);
   return k;
 }
 

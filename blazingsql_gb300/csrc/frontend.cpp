@@ -127,6 +127,9 @@ std::string normalize_calcite(const std::string& in) {
   replace_all(s, "HOUR TO SECOND", "SECOND");
   replace_all(s, "MINUTE TO SECOND", "SECOND");
   replace_all(s, "/INT(", "/(");
+  replace_all(s, "TRIM(FLAG(BOTH),", "TRIM(\"BOTH\",");
+  replace_all(s, "TRIM(FLAG(LEADING),", "TRIM(\"LEADING\",");
+  replace_all(s, "TRIM(FLAG(TRAILING),", "TRIM(\"TRAILING\",");
   return s;
 }
 
@@ -795,7 +798,8 @@ std::string preprocess_expression(const std::string& text, const std::vector<int
   for (char c : e) dollars += c == '$';
   if (!e.empty() && e[0] == '-' && dollars == 1 && e.find(',') == std::string::npos && e.size() >= 2)
     e = e.substr(0, 2) + "0, " + e.substr(2);
-  if (e.find("CONCAT") != std::string::npos) fail(GX_ERR_UNSUPPORTED, "string operator out of scope: CONCAT");
+  // convert_nary_to_binary_concat (:1620) happens in the string pre-pass
+  // (rewrite_string_ops nests an n-ary CONCAT before evaluating it)
   if (e.find("CURRENT_DATE") != std::string::npos || e.find("CURRENT_TIME") != std::string::npos)
     fail(GX_ERR_UNSUPPORTED, "CURRENT_DATE/CURRENT_TIMESTAMP need an engine context");
   // convert_ms_to_ns_units (expression_utils.cpp:1316-1350)
@@ -1071,6 +1075,126 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
   // a CASE operand evaluate_string_case_when_else takes: a string column, a
   // string literal or a null literal (LogicalProject.cpp:616-623)
   auto string_operand = [&](const ExprPtr& e) { return strcol(e) || is_string_literal(e) || is_null_literal(e); };
+  auto int_literal = [&](const ExprPtr& e, int* v) {
+    if (e->kind != Expr::LIT || e->token.empty() || is_string_literal(e) || is_null_literal(e)) return false;
+    char* end = nullptr;
+    const long long x = std::strtoll(e->token.c_str(), &end, 10);
+    if (!end || *end != '\0' || x < INT32_MIN || x > INT32_MAX) return false;
+    *v = (int)x;
+    return true;
+  };
+  auto need_strcol = [&](const ExprPtr& e, const char* fn) {
+    if (!strcol(e))
+      fail(GX_ERR_UNSUPPORTED, std::string(fn) + " argument must be a column of type string");
+  };
+  // the functions of evaluate_string_functions (LogicalProject.cpp:103-603)
+  // other than LIKE; false when `e` is none of them
+  std::function<bool(const ExprPtr&, StringOp&)> string_function = [&](const ExprPtr& e, StringOp& op) {
+    const std::string& t = e->token;
+    const auto& a = e->ch;
+    if (t == "SUBSTRING" && (a.size() == 2 || a.size() == 3)) {
+      // :212-220: start = max(start, 1) - 1; stop = start + length when a length >= 0 is given
+      int st = 0, len = -1;
+      need_strcol(a[0], "SUBSTRING");
+      if (!int_literal(a[1], &st) || (a.size() == 3 && !int_literal(a[2], &len)))
+        fail(GX_ERR_UNSUPPORTED, "SUBSTRING with non-literal positions");
+      op.kind = StringOp::SLICE;
+      op.col = a[0]->col;
+      op.i0 = std::max(st, 1) - 1;
+      op.i0_valid = true;
+      op.i1 = len >= 0 ? op.i0 + len : 0;
+      op.i1_valid = a.size() == 3 && len >= 0;
+      return true;
+    }
+    if ((t == "LEFT" || t == "RIGHT") && a.size() == 2) {
+      int n = 0;
+      need_strcol(a[0], t.c_str());
+      if (!int_literal(a[1], &n)) fail(GX_ERR_UNSUPPORTED, t + " with a non-literal length");
+      n = std::max(n, 0);
+      op.kind = StringOp::SLICE;
+      op.col = a[0]->col;
+      if (t == "LEFT") {  // :186-191: [0, n)
+        op.i0 = 0;
+        op.i1 = n;
+        op.i0_valid = op.i1_valid = true;
+      } else {  // :200-201: [-n, end), or [0, 0) when n < 1
+        op.i0 = -n;
+        op.i0_valid = true;
+        op.i1 = 0;
+        op.i1_valid = n < 1;
+      }
+      return true;
+    }
+    if (t == "REVERSE" && a.size() == 1) {  // :573-585: step -1
+      need_strcol(a[0], "REVERSE");
+      op.kind = StringOp::SLICE;
+      op.col = a[0]->col;
+      op.step = -1;
+      return true;
+    }
+    if ((t == "UPPER" || t == "LOWER" || t == "INITCAP") && a.size() == 1) {
+      need_strcol(a[0], t.c_str());
+      op.kind = t == "UPPER" ? StringOp::UPPER : t == "LOWER" ? StringOp::LOWER : StringOp::INITCAP;
+      op.col = a[0]->col;
+      return true;
+    }
+    if (t == "TRIM" && a.size() == 3 && is_string_literal(a[0]) && is_string_literal(a[1])) {
+      need_strcol(a[2], "TRIM");
+      const std::string side = unquote(a[0]->token);
+      op.kind = StringOp::TRIM;
+      op.col = a[2]->col;
+      op.i0 = side == "LEADING" ? 1 : side == "TRAILING" ? 2 : 0;
+      op.literal = unquote(a[1]->token);
+      return true;
+    }
+    if (t == "REPLACE" && a.size() == 3) {
+      need_strcol(a[0], "REPLACE");
+      if (!is_string_literal(a[1]) || !is_string_literal(a[2]))
+        fail(GX_ERR_UNSUPPORTED, "REPLACE with non-literal target or replacement");
+      op.kind = StringOp::REPLACE;
+      op.col = a[0]->col;
+      op.literal = unquote(a[1]->token);
+      op.literal2 = unquote(a[2]->token);
+      if (op.literal.empty()) fail(GX_ERR_UNSUPPORTED, "REPLACE with an empty target");
+      return true;
+    }
+    if ((t == "CONCAT" || t == "||") && a.size() == 2) {
+      if (is_string_literal(a[0]) && is_string_literal(a[1]))  // :311
+        fail(GX_ERR_UNSUPPORTED, "CONCAT operator between literals is not supported");
+      for (const auto& x : a)
+        if (!strcol(x) && !is_string_literal(x))
+          fail(GX_ERR_UNSUPPORTED, "CONCAT of something other than strings");
+      op.kind = StringOp::CONCAT;
+      if (strcol(a[0])) op.col = a[0]->col;
+      else op.literal = unquote(a[0]->token);
+      if (strcol(a[1])) op.col2 = a[1]->col;
+      else op.literal2 = unquote(a[1]->token);
+      return true;
+    }
+    if ((t == "CAST_VARCHAR" || t == "CAST_CHAR") && a.size() == 1) {
+      if (a[0]->kind == Expr::LIT) fail(GX_ERR_UNSUPPORTED, "CAST operator not supported for literals");
+      op.kind = StringOp::TO_STRING;
+      if (a[0]->kind == Expr::COL) op.col = a[0]->col;
+      else op.cond = rebuild_typed(a[0]);
+      return true;
+    }
+    static const std::map<std::string, int> parse_types = {
+        {"CAST_TINYINT", INT8}, {"CAST_SMALLINT", INT16}, {"CAST_INTEGER", INT32}, {"CAST_BIGINT", INT64},
+        {"CAST_DATE", TIMESTAMP_DAYS}, {"CAST_TIMESTAMP_SECONDS", TIMESTAMP_SECONDS},
+        {"CAST_TIMESTAMP_MILLISECONDS", TIMESTAMP_MILLISECONDS},
+        {"CAST_TIMESTAMP_MICROSECONDS", TIMESTAMP_MICROSECONDS}, {"CAST_TIMESTAMP", TIMESTAMP_NANOSECONDS},
+        {"CAST_FLOAT", FLOAT32}, {"CAST_DOUBLE", FLOAT64}};
+    auto pt = parse_types.find(t);
+    if (pt != parse_types.end() && a.size() == 1 && strcol(a[0])) {
+      if (pt->second == FLOAT32 || pt->second == FLOAT64)
+        fail(GX_ERR_UNSUPPORTED, "CAST of a string column to a floating-point type");
+      op.kind = StringOp::PARSE;
+      op.col = a[0]->col;
+      op.type = pt->second;
+      return true;
+    }
+    return false;
+  };
   for (auto& text : texts) {
     if (text.empty()) continue;
     const std::string norm = normalize_calcite(text);
@@ -1080,6 +1204,19 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
     bool touched = false;
     std::function<ExprPtr(ExprPtr)> walk = [&](ExprPtr e) -> ExprPtr {
       if (e->kind != Expr::OP) return e;
+      if (e->token == "CONCAT" && e->ch.size() > 2) {
+        // CONCAT(a, b, c) -> CONCAT(CONCAT(a, b), c) (convert_nary_to_binary_concat,
+        // expression_utils.cpp:1620)
+        ExprPtr cur = e->ch[0];
+        for (size_t k = 1; k < e->ch.size(); k++) {
+          auto n = std::make_shared<Expr>();
+          n->kind = Expr::OP;
+          n->token = "CONCAT";
+          n->ch = {cur, e->ch[k]};
+          cur = n;
+        }
+        e = cur;
+      }
       for (auto& c : e->ch) c = walk(c);
       const std::string& t = e->token;
       StringOp op;
@@ -1108,6 +1245,15 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
         op.col = l->col;
         if (strcol(r)) op.col2 = r->col;
         else op.literal = unquote(r->token);
+      } else if ((t == "CAST_VARCHAR" || t == "CAST_CHAR") && e->ch.size() == 1 && e->ch[0]->kind == Expr::LIT &&
+                 !is_null_literal(e->ch[0])) {
+        // CAST(literal):VARCHAR is a VARCHAR literal before the pre-pass runs
+        // (transform_cast_literal, expression_tree.hpp:238-256)
+        auto l = std::make_shared<Expr>(*e->ch[0]);
+        if (!is_string_literal(l)) l->token = "'" + l->token + "'";
+        l->lit_type_token.clear();
+        touched = true;
+        return l;
       } else if (t == "CASE" && e->ch.size() >= 3 && e->ch.size() % 2 == 1) {
         // CASE(c1, v1, ..., ck, vk, else) is FIRST_NON_MAGIC(MAGIC_IF_NOT(c1,
         // v1), ...) nested to the right (expression_tree.hpp:200-220); from
@@ -1141,7 +1287,7 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
         e->ch.resize(i);
         e->ch.push_back(cur);
         return e;
-      } else {
+      } else if (!string_function(e, op)) {
         return e;
       }
       touched = true;

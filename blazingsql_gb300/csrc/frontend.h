@@ -61,27 +61,49 @@ std::string rebuild(const ExprPtr& e);
 // Parse + lower without typing (used by tests of the lowering rules).
 ExprPtr parse_and_lower(const std::string& text);
 
-// A string operator of the string pre-pass: LIKE(col, 'pattern'),
-// CHAR_LENGTH(col), a comparison of a string column with a string literal or
-// with another string column, or a CASE whose result is a string.
+// A string operator of the string pre-pass (the operators of
+// evaluate_string_functions, LogicalProject.cpp:103-603, and the
+// interpreter's string comparisons).
 struct StringOp {
-  enum Kind { LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH, CASE };
+  enum Kind {
+    LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH,
+    CASE,       // THEN (col / literal / null) where cond is true, else ELSE (col2 / literal2 / null)
+    SLICE,      // cudf::strings::slice_strings by characters: [i0, i1) with validity flags, step (+1 / -1)
+    UPPER, LOWER, INITCAP,
+    TRIM,       // side i0 (0 both, 1 leading, 2 trailing), characters to strip in `literal`
+    REPLACE,    // every `literal` by `literal2`
+    CONCAT,     // (col | literal) followed by (col2 | literal2)
+    TO_STRING,  // CAST to VARCHAR of column `col` (or of the expression `cond`), formatted by its type
+    PARSE       // CAST of string column `col` to `type` (integers, DATE, TIMESTAMPs)
+  };
   Kind kind = LIKE;
-  int col = -1;         // the string column; CASE: the THEN column, or -1
-  std::string literal;  // the pattern / literal, quotes removed; CASE: the THEN literal
+  int col = -1;         // the (first) string column; CASE: the THEN column, or -1
+  std::string literal;  // pattern / literal, quotes removed; CASE: the THEN literal
   int col2 = -1;        // comparisons: the right-hand string column; CASE: the ELSE column, or -1
-  // CASE only: `cond` (text over the columns before this operator) selects
-  // THEN where it is true, ELSE where it is false or NULL
+  // CASE: `cond` (text over the columns before this operator) selects THEN
+  // where it is true, ELSE where it is false or NULL
   // (evaluate_string_case_when_else, LogicalProject.cpp:612-659); an operand
-  // without a column is its literal, or NULL when *_null is set
+  // without a column is its literal, or NULL when *_null is set.
+  // TO_STRING: the expression whose column is formatted when col < 0.
   std::string cond;
-  std::string literal2;  // the ELSE literal
+  std::string literal2;  // the ELSE / second literal
   bool then_null = false, else_null = false;
+  int i0 = 0, i1 = 0, step = 1;
+  bool i0_valid = false, i1_valid = false;
+  int type = 0;  // PARSE: the result type
   bool operator==(const StringOp& o) const {
     return kind == o.kind && col == o.col && literal == o.literal && col2 == o.col2 && cond == o.cond &&
-           literal2 == o.literal2 && then_null == o.then_null && else_null == o.else_null;
+           literal2 == o.literal2 && then_null == o.then_null && else_null == o.else_null && i0 == o.i0 &&
+           i1 == o.i1 && step == o.step && i0_valid == o.i0_valid && i1_valid == o.i1_valid && type == o.type;
   }
-  int result_type() const { return kind == CASE ? STRING : kind == CHAR_LENGTH ? INT32 : BOOL8; }
+  int result_type() const {
+    switch (kind) {
+      case CHAR_LENGTH: return INT32;
+      case PARSE: return type;
+      case LIKE: case EQ: case NE: case LT: case LE: case GT: case GE: return BOOL8;
+      default: return STRING;
+    }
+  }
 };
 
 // The string pre-pass of function_evaluator_transformer

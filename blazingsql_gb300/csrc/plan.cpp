@@ -862,6 +862,14 @@ class Gen {
 
 void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
   o << "#define GX_V " << cfg.words << "\n#define GX_WARPS " << cfg.warps << "\n";
+  // a register cap becomes a resident-block count in the launch bounds; without
+  // one the bounds name the block size only (a minimum of one block lets ptxas
+  // take more registers than its default choice)
+  if (cfg.max_regs > 0)
+    o << "#define GX_LB __launch_bounds__(GX_WARPS * 32, "
+      << std::max(1, 65536 / (cfg.max_regs * cfg.warps * 32)) << ")\n";
+  else
+    o << "#define GX_LB __launch_bounds__(GX_WARPS * 32)\n";
   o << "#define GX_TILE_WORDS (GX_WARPS * GX_V)\n";
   o << "#define GX_MAX_COLS " << GX_MAX_COLS << "\n#define GX_MAX_OUTS " << GX_MAX_OUTS << "\n";
   o << "struct GxArgs {\n"
@@ -1171,7 +1179,7 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
 void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
                         const std::string& name) {
   o << "struct GxBatchHdr { unsigned long long tile_counter; long long total_tiles; int nbatch; int pad; };\n";
-  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name
+  o << "extern \"C\" __global__ void GX_LB " << name
     << "(const GxArgs* __restrict__ A, const long long* __restrict__ tile_base, GxBatchHdr* hdr) {\n";
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
   o << "  const i64 total_tiles = hdr->total_tiles; const int nbatch = hdr->nbatch;\n";
@@ -1275,7 +1283,7 @@ void emit_staged_filter(std::ostringstream& o, const Gen& g, const Plan& p, cons
     wbmax = std::max(wbmax, cwb[c]);
   }
   o << "#define GX_T (GX_WARPS * GX_V)\n#define GX_D 4\n";
-  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name << "(const GxArgs a) {\n";
+  o << "extern \"C\" __global__ void GX_LB " << name << "(const GxArgs a) {\n";
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
   o << "  const i64 nwords = (a.n + 31) >> 5;\n";
   o << "  const i64 ntiles = (nwords + GX_T - 1) / GX_T;\n";
@@ -1575,7 +1583,7 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     emit_fused_batched(o, gb, p, gb.predicate_cone(), name);
     return o.str();
   }
-  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name << "(const GxArgs a) {\n";
+  o << "extern \"C\" __global__ void GX_LB " << name << "(const GxArgs a) {\n";
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
   o << "  const i64 nwords = (a.n + 31) >> 5;\n";
   if (kind == KernelKind::PROJECT) {
@@ -1829,7 +1837,7 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   const std::vector<int> row_ids = g.cone(roots);
   const std::vector<int> pred_ids = g.predicate_cone();
 
-  o << "extern \"C\" __global__ void __launch_bounds__(GX_WARPS * 32) " << name
+  o << "extern \"C\" __global__ void GX_LB " << name
     << "(const GxArgs a, const GxAggArgs ga) {\n";
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
   o << "  const i64 nwords = (a.n + 31) >> 5;\n";

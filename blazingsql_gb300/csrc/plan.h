@@ -67,6 +67,9 @@ struct KernelConfig {
   // single-pass filter calls choose the block shape online among a few
   // candidates (the shape is not fixed by the caller or the environment)
   bool tune_shape = false;
+  // registers per thread the kernel is held to (0: the compiler's choice),
+  // as launch bounds asking for 65536 / (max_regs x threads) resident blocks
+  int max_regs = 0;
 };
 
 struct Plan {

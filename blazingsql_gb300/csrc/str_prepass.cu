@@ -284,6 +284,400 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_str_write(BuildArgs a) {
   }
 }
 
+// ------------------------------------------------------ string transforms
+// Row-wise string functions (slices, case, trim, replace, concatenation,
+// formatting of typed values), a thread per row: the same three launches as
+// build_strings, each row's bytes produced by xform_row (sizing when d is
+// null, writing otherwise).
+struct XformArgs {
+  int kind;  // StringOp::Kind
+  BuildSrc a, b;
+  const void* num;  // TO_STRING: the typed column
+  const uint32_t* num_mask;
+  int64_t num_off;
+  int num_type;
+  int i0, i1, step, i0v, i1v;
+  const unsigned char* s1;  // TRIM: characters to strip; REPLACE: target
+  int l1;
+  const unsigned char* s2;  // REPLACE: replacement
+  int l2;
+  int64_t m;
+  int32_t* out_offs;
+  uint32_t* out_mask;
+  unsigned char* out_chars;
+  uint64_t* block_sums;
+  int* flags;  // bit 0: UPPER / LOWER / INITCAP met a non-ASCII byte
+};
+
+__device__ __forceinline__ void source_row(const BuildSrc& s, int64_t o, const unsigned char*& p, int& len,
+                                           bool& valid) {
+  p = nullptr;
+  len = 0;
+  valid = false;
+  if (s.kind == StrSource::NUL) return;
+  if (s.kind == StrSource::LITERAL) {
+    p = s.lit;
+    len = s.lit_len;
+    valid = true;
+    return;
+  }
+  const int64_t q = s.off + o;
+  if (!bit_of(s.mask, q)) return;
+  const int32_t b0 = s.offs[q];
+  p = s.chars + b0;
+  len = s.offs[q + 1] - b0;
+  valid = true;
+}
+
+__device__ __forceinline__ int put(unsigned char* d, int at, const unsigned char* src, int n) {
+  if (d)
+    for (int i = 0; i < n; i++) d[at + i] = src[i];
+  return at + n;
+}
+
+// the character (as its byte count) of strip set `set` that matches s[i..]
+__device__ bool in_set(const unsigned char* s, int i, int k, const unsigned char* set, int sl) {
+  if (sl == 0) return k == 1 && s[i] <= ' ';  // no characters given: whitespace
+  for (int j = 0; j < sl;) {
+    const int cl = utf8_len(set[j]);
+    if (cl == k) {
+      bool eq = true;
+      for (int t = 0; t < k; t++) eq = eq && set[j + t] == s[i + t];
+      if (eq) return true;
+    }
+    j += cl;
+  }
+  return false;
+}
+
+__device__ int civil_digits(unsigned char* d, int at, int64_t v, int width) {
+  unsigned char buf[24];
+  int n = 0;
+  uint64_t u = (uint64_t)v;
+  do {
+    buf[n++] = (unsigned char)('0' + u % 10);
+    u /= 10;
+  } while (u);
+  while (n < width) buf[n++] = '0';
+  if (d)
+    for (int i = 0; i < n; i++) d[at + i] = buf[n - 1 - i];
+  return at + n;
+}
+
+// days since 1970-01-01 -> (y, m, d): the proleptic Gregorian conversion of
+// H. Hinnant's "chrono-Compatible Low-Level Date Algorithms" (civil_from_days)
+__device__ void civil_from_days(int64_t z, int64_t& y, int& m, int& dd) {
+  z += 719468;
+  const int64_t era = (z >= 0 ? z : z - 146096) / 146097;
+  const int64_t doe = z - era * 146097;
+  const int64_t yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+  y = yoe + era * 400;
+  const int64_t doy = doe - (365 * yoe + yoe / 4 - yoe / 100);
+  const int64_t mp = (5 * doy + 2) / 153;
+  dd = (int)(doy - (153 * mp + 2) / 5 + 1);
+  m = (int)(mp < 10 ? mp + 3 : mp - 9);
+  y += m <= 2;
+}
+
+__device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {
+  const int64_t q = a / b;
+  return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
+
+// formats row o of the typed column (cast_to_str_functor, LogicalProject.cpp:62-92)
+__device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
+  const int64_t q = a.num_off + o;
+  valid = bit_of(a.num_mask, q);
+  if (!valid) return 0;
+  int at = 0;
+  switch (a.num_type) {
+    case BOOL8: {  // cudf::strings::from_booleans: "true" / "false"
+      const bool v = ((const uint8_t*)a.num)[q] != 0;
+      const unsigned char* t = (const unsigned char*)(v ? "true" : "false");
+      return put(d, 0, t, v ? 4 : 5);
+    }
+    case INT8: case INT16: case INT32: case INT64: {  // cudf::strings::from_integers
+      int64_t v = a.num_type == INT8 ? ((const int8_t*)a.num)[q] : a.num_type == INT16 ? ((const int16_t*)a.num)[q]
+                : a.num_type == INT32 ? ((const int32_t*)a.num)[q] : ((const int64_t*)a.num)[q];
+      uint64_t u = (uint64_t)v;
+      if (v < 0) {
+        if (d) d[at] = '-';
+        at++;
+        u = 0 - u;
+      }
+      return civil_digits(d, at, (int64_t)u, 1);
+    }
+    case UINT8: case UINT16: case UINT32: case UINT64: {
+      const uint64_t u = a.num_type == UINT8 ? ((const uint8_t*)a.num)[q] : a.num_type == UINT16
+                       ? ((const uint16_t*)a.num)[q] : a.num_type == UINT32 ? ((const uint32_t*)a.num)[q]
+                       : ((const uint64_t*)a.num)[q];
+      return civil_digits(d, 0, (int64_t)u, 1);
+    }
+    default: break;
+  }
+  // timestamps: "%Y-%m-%d" for days, "%Y-%m-%d %H:%M:%S" otherwise
+  int64_t days, sod = 0;
+  if (a.num_type == TIMESTAMP_DAYS) {
+    days = ((const int32_t*)a.num)[q];
+  } else {
+    const int64_t v = ((const int64_t*)a.num)[q];
+    const int64_t per = a.num_type == TIMESTAMP_SECONDS ? 1 : a.num_type == TIMESTAMP_MILLISECONDS ? 1000
+                      : a.num_type == TIMESTAMP_MICROSECONDS ? 1000000 : 1000000000;
+    const int64_t secs = floor_div(v, per);
+    days = floor_div(secs, 86400);
+    sod = secs - days * 86400;
+  }
+  int64_t y;
+  int m, dd;
+  civil_from_days(days, y, m, dd);
+  const unsigned char dash = '-', colon = ':', space = ' ';
+  at = civil_digits(d, 0, y, 4);
+  at = put(d, at, &dash, 1);
+  at = civil_digits(d, at, m, 2);
+  at = put(d, at, &dash, 1);
+  at = civil_digits(d, at, dd, 2);
+  if (a.num_type != TIMESTAMP_DAYS) {
+    at = put(d, at, &space, 1);
+    at = civil_digits(d, at, sod / 3600, 2);
+    at = put(d, at, &colon, 1);
+    at = civil_digits(d, at, sod / 60 % 60, 2);
+    at = put(d, at, &colon, 1);
+    at = civil_digits(d, at, sod % 60, 2);
+  }
+  return at;
+}
+
+__device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
+  if (a.kind == StringOp::TO_STRING) return format_value(a, o, d, valid);
+  const unsigned char* p;
+  int n;
+  source_row(a.a, o, p, n, valid);
+  if (a.kind == StringOp::CONCAT) {  // cudf::strings::concatenate: NULL if either side is
+    const unsigned char* p2;
+    int n2;
+    bool v2;
+    source_row(a.b, o, p2, n2, v2);
+    valid = valid && v2;
+    if (!valid) return 0;
+    return put(d, put(d, 0, p, n), p2, n2);
+  }
+  if (!valid) return 0;
+  switch (a.kind) {
+    case StringOp::SLICE: {  // cudf::strings::slice_strings, characters [begin, end) by step
+      int L = 0;
+      for (int i = 0; i < n; i += utf8_len(p[i])) L++;
+      if (a.step < 0) {  // the whole string, characters in reverse order
+        int at = 0, e = n;
+        while (e > 0) {
+          int b = e - 1;
+          while (b > 0 && (p[b] & 0xC0) == 0x80) b--;
+          at = put(d, at, p + b, e - b);
+          e = b;
+        }
+        return at;
+      }
+      int b = 0, e = L;
+      if (a.i0v) b = a.i0 >= 0 ? (a.i0 < L ? a.i0 : L) : (L + a.i0 >= 0 ? L + a.i0 : 0);
+      if (a.i1v) e = a.i1 >= 0 ? (a.i1 < L ? a.i1 : L) : (L + a.i1 >= 0 ? L + a.i1 : 0);
+      if (b >= e) return 0;
+      int bb = 0, c = 0;
+      while (c < b) { bb += utf8_len(p[bb]); c++; }
+      int eb = bb;
+      while (c < e) { eb += utf8_len(p[eb]); c++; }
+      return put(d, 0, p + bb, eb - bb);
+    }
+    case StringOp::UPPER: case StringOp::LOWER: case StringOp::INITCAP: {
+      bool word = false;  // INITCAP: inside a run of letters (cudf::strings::title)
+      for (int i = 0; i < n; i++) {
+        unsigned char c = p[i];
+        if (c >= 0x80) {
+          if (!d) atomicOr(a.flags, 1);
+        } else {
+          const bool up = c >= 'A' && c <= 'Z', lo = c >= 'a' && c <= 'z';
+          bool to_up = a.kind == StringOp::UPPER;
+          if (a.kind == StringOp::INITCAP) to_up = !word;
+          if (up || lo) {
+            if (to_up && lo) c = (unsigned char)(c - 32);
+            if (!to_up && up) c = (unsigned char)(c + 32);
+          }
+          word = up || lo;
+        }
+        if (d) d[i] = c;
+      }
+      return n;
+    }
+    case StringOp::TRIM: {  // cudf::strings::strip
+      int b = 0, e = n;
+      if (a.i0 != 2)
+        while (b < e && in_set(p, b, utf8_len(p[b]), a.s1, a.l1)) b += utf8_len(p[b]);
+      if (a.i0 != 1)
+        while (e > b) {
+          int k = e - 1;
+          while (k > b && (p[k] & 0xC0) == 0x80) k--;
+          if (!in_set(p, k, e - k, a.s1, a.l1)) break;
+          e = k;
+        }
+      return put(d, 0, p + b, e - b);
+    }
+    case StringOp::REPLACE: {  // cudf::strings::replace, every occurrence, left to right
+      int at = 0, i = 0;
+      while (i < n) {
+        bool hit = i + a.l1 <= n;
+        for (int t = 0; hit && t < a.l1; t++) hit = p[i + t] == a.s1[t];
+        if (hit) {
+          at = put(d, at, a.s2, a.l2);
+          i += a.l1;
+        } else {
+          at = put(d, at, p + i, 1);
+          i++;
+        }
+      }
+      return at;
+    }
+    default: return 0;
+  }
+}
+
+__global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
+  __shared__ uint64_t s_sum[kBuildWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
+  uint64_t total = 0;
+  for (int k = 0; k < kBuildWords; k++) {
+    const int64_t o = (w0 + k) * 32 + lane;
+    if ((w0 + k) * 32 >= a.m) break;
+    bool valid = false;
+    int len = 0;
+    if (o < a.m) len = xform_row(a, o, nullptr, valid);
+    const uint32_t word = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0) a.out_mask[w0 + k] = word;
+    total += (uint64_t)warp_sum(len);
+  }
+  if (lane == 0) s_sum[warp] = total;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t t = 0;
+    for (int i = 0; i < kBuildWarps; i++) t += s_sum[i];
+    a.block_sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
+  __shared__ uint64_t s_sum[kBuildWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
+  int lens[kBuildWords];
+  uint64_t total = 0;
+  for (int k = 0; k < kBuildWords; k++) {
+    lens[k] = 0;
+    const int64_t o = (w0 + k) * 32 + lane;
+    if ((w0 + k) * 32 >= a.m) break;
+    bool valid = false;
+    if (o < a.m) lens[k] = xform_row(a, o, nullptr, valid);
+    total += (uint64_t)warp_sum(lens[k]);
+  }
+  if (lane == 0) s_sum[warp] = total;
+  __syncthreads();
+  uint64_t pos = a.block_sums[blockIdx.x];
+  for (int i = 0; i < warp; i++) pos += s_sum[i];
+  for (int k = 0; k < kBuildWords; k++) {
+    const int64_t o = (w0 + k) * 32 + lane;
+    if ((w0 + k) * 32 >= a.m) break;
+    const int len = lens[k];
+    int incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += y;
+    }
+    const uint64_t dst = pos + (uint64_t)(incl - len);
+    if (o < a.m) {
+      a.out_offs[o] = (int32_t)dst;
+      if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
+      bool valid = false;
+      if (len > 0) xform_row(a, o, a.out_chars + dst, valid);
+    }
+    pos += (uint64_t)__shfl_sync(0xffffffffu, incl, 31);
+  }
+}
+
+// string -> integer / DATE / TIMESTAMP (cudf::strings::to_integers and
+// to_timestamps with "%Y-%m-%d" / "%Y-%m-%d %H:%M:%S", LogicalProject.cpp:379-528)
+struct ParseArgs {
+  BuildSrc a;
+  int type;
+  int64_t m;
+  void* out;
+  uint32_t* out_mask;
+};
+
+// digits from s[0..n) up to the first non-digit
+__device__ __forceinline__ int64_t leading_digits(const unsigned char* s, int n) {
+  uint64_t v = 0;
+  for (int i = 0; i < n; i++) {
+    if (s[i] < '0' || s[i] > '9') break;
+    v = v * 10 + (uint64_t)(s[i] - '0');
+  }
+  return (int64_t)v;
+}
+
+// days since 1970-01-01 of (y, m, d): H. Hinnant's days_from_civil
+__device__ int64_t days_from_civil(int64_t y, int64_t m, int64_t d) {
+  y -= m <= 2;
+  const int64_t era = (y >= 0 ? y : y - 399) / 400;
+  const int64_t yoe = y - era * 400;
+  const int64_t doy = (153 * (m + (m > 2 ? -3 : 9)) + 2) / 5 + d - 1;
+  const int64_t doe = yoe * 365 + yoe / 4 - yoe / 100 + doy;
+  return era * 146097 + doe - 719468;
+}
+
+__global__ void k_parse(ParseArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwords = (a.m + 31) / 32;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; w < nwords;
+       w += ((int64_t)gridDim.x * blockDim.x) / 32) {
+    const int64_t r = w * 32 + lane;
+    bool valid = false;
+    if (r < a.m) {
+      const unsigned char* p;
+      int n;
+      source_row(a.a, r, p, n, valid);
+      int64_t v = 0;
+      if (valid && (a.type == TIMESTAMP_DAYS || a.type == TIMESTAMP_SECONDS || a.type == TIMESTAMP_MILLISECONDS ||
+                    a.type == TIMESTAMP_MICROSECONDS || a.type == TIMESTAMP_NANOSECONDS)) {
+        // fields at fixed places of the format; a field past the end of the string is 0
+        auto field = [&](int at, int len) { return at < n ? leading_digits(p + at, min(len, n - at)) : 0; };
+        const int64_t days = days_from_civil(field(0, 4), field(5, 2), field(8, 2));
+        if (a.type == TIMESTAMP_DAYS) {
+          v = days;
+        } else {
+          const int64_t secs = days * 86400 + field(11, 2) * 3600 + field(14, 2) * 60 + field(17, 2);
+          const int64_t per = a.type == TIMESTAMP_SECONDS ? 1 : a.type == TIMESTAMP_MILLISECONDS ? 1000
+                            : a.type == TIMESTAMP_MICROSECONDS ? 1000000 : 1000000000;
+          v = secs * per;
+        }
+      } else if (valid && n > 0) {
+        int i = 0;
+        bool neg = false;
+        if (p[0] == '-' || p[0] == '+') {
+          neg = p[0] == '-';
+          i = 1;
+        }
+        const uint64_t u = (uint64_t)leading_digits(p + i, n - i);
+        v = (int64_t)(neg ? 0 - u : u);
+      }
+      switch (a.type) {
+        case INT8: ((int8_t*)a.out)[r] = (int8_t)v; break;
+        case INT16: ((int16_t*)a.out)[r] = (int16_t)v; break;
+        case INT32: case TIMESTAMP_DAYS: ((int32_t*)a.out)[r] = (int32_t)v; break;
+        default: ((int64_t*)a.out)[r] = v; break;
+      }
+    }
+    const uint32_t word = __ballot_sync(0xffffffffu, r < a.m && valid);
+    if (lane == 0) a.out_mask[w] = word;
+  }
+}
+
 BuildSrc device_source(const StrSource& s, const unsigned char* lit_dev) {
   BuildSrc b{};
   b.kind = s.kind;
@@ -372,6 +766,107 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
   return out;
 }
 
+gx_column build_transform(const StringOp& op, const StrSource& a, const StrSource& b, const ColumnView* num,
+                          int64_t rows, cudaStream_t s) {
+  if (rows < 0 || rows > INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string columns hold at most 2^31 - 1 rows");
+  const int64_t nblocks = (rows + kBuildRows - 1) / kBuildRows;
+  const int64_t words = mask_words_for(rows);
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  // [mask | offsets | block sums + total + flags | a, b, literal, literal2]
+  const size_t mask_b = al((size_t)words * 4), offs_b = al((size_t)(rows + 1) * 4);
+  const size_t sums_b = al((size_t)(nblocks + 2) * 8);
+  std::string lits[4] = {a.kind == StrSource::LITERAL ? a.literal : std::string(),
+                         b.kind == StrSource::LITERAL ? b.literal : std::string(), op.literal, op.literal2};
+  size_t loff[4], lb = 0;
+  for (int i = 0; i < 4; i++) {
+    loff[i] = lb;
+    lb += al(lits[i].size() + 1);
+  }
+  char* base = (char*)dev_alloc(mask_b + offs_b + sums_b + lb, s);
+  gx_column out{};
+  out.type_id = STRING;
+  out.null_mask = (uint32_t*)base;
+  out.string_offsets = (int32_t*)(base + mask_b);
+  out.size = rows;
+  out.capacity = rows;
+  try {
+    uint64_t* sums = (uint64_t*)(base + mask_b + offs_b);
+    unsigned char* ldev = (unsigned char*)(base + mask_b + offs_b + sums_b);
+    check_cuda(cudaMemsetAsync(base, 0, mask_b + offs_b + sums_b, s), "string column clear");
+    for (int i = 0; i < 4; i++)
+      if (!lits[i].empty())
+        check_cuda(cudaMemcpyAsync(ldev + loff[i], lits[i].data(), lits[i].size(), cudaMemcpyHostToDevice, s),
+                   "string literal");
+    XformArgs x{};
+    x.kind = op.kind;
+    x.a = device_source(a, ldev + loff[0]);
+    x.b = device_source(b, ldev + loff[1]);
+    if (num) {
+      x.num = num->data;
+      x.num_mask = num->mask;
+      x.num_off = num->offset;
+      x.num_type = num->type;
+    }
+    x.i0 = op.i0;
+    x.i1 = op.i1;
+    x.step = op.step;
+    x.i0v = op.i0_valid;
+    x.i1v = op.i1_valid;
+    x.s1 = ldev + loff[2];
+    x.l1 = (int)op.literal.size();
+    x.s2 = ldev + loff[3];
+    x.l2 = (int)op.literal2.size();
+    x.m = rows;
+    x.out_offs = out.string_offsets;
+    x.out_mask = out.null_mask;
+    x.block_sums = sums;
+    x.flags = (int*)(sums + nblocks + 1);
+    uint64_t host[2] = {0, 0};
+    if (rows > 0) {
+      k_xf_sizes<<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      check_cuda(cudaGetLastError(), "k_xf_sizes");
+      launch_scan_tiles(sums, nblocks, (unsigned long long*)(sums + nblocks), s);
+      check_cuda(cudaMemcpyAsync(host, sums + nblocks, 16, cudaMemcpyDeviceToHost, s), "string size");
+      add_launches(1);
+    }
+    check_cuda(cudaStreamSynchronize(s), "string size sync");
+    if (host[1] & 1) fail(GX_ERR_UNSUPPORTED, "UPPER / LOWER / INITCAP of non-ASCII text");
+    const uint64_t total = host[0];
+    if (total > (uint64_t)INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string column over 2^31 - 1 characters");
+    out.data = dev_alloc(al(total ? total : 1), s);
+    out.string_bytes = (int64_t)total;
+    if (rows > 0) {
+      x.out_chars = (unsigned char*)out.data;
+      k_xf_write<<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      check_cuda(cudaGetLastError(), "k_xf_write");
+      add_launches(1);
+    }
+  } catch (...) {
+    if (out.data) dev_free(out.data, s);
+    dev_free(base, s);
+    throw;
+  }
+  return out;
+}
+
+void launch_parse(const ColumnView& col, int type, gx_column& out, cudaStream_t s) {
+  ParseArgs a{};
+  StrSource src;
+  src.kind = StrSource::COLUMN;
+  src.col = col;
+  a.a = device_source(src, nullptr);
+  a.type = type;
+  a.m = col.size;
+  a.out = out.data;
+  a.out_mask = out.null_mask;
+  if (a.m == 0) return;
+  const int64_t warps = (a.m + 31) / 32;
+  const int grid = (int)std::min<int64_t>((warps + 7) / 8, 152 * 32);
+  k_parse<<<grid, 256, 0, s>>>(a);
+  check_cuda(cudaGetLastError(), "k_parse");
+  add_launches(1);
+}
+
 void launch_string_op(const ColumnView& col, const ColumnView* col2, const StringOp& op, const void* pattern_dev,
                       gx_column& out, cudaStream_t s) {
   StrArgs a{};
@@ -451,6 +946,58 @@ std::vector<gx_column> run_string_prepass(
           throw;
         }
         free_column(mask, s);
+      } else if (op.kind == StringOp::TO_STRING) {
+        gx_column tmp{};
+        ColumnView v = op.col >= 0 ? cols.at(op.col) : ColumnView{};
+        if (op.col < 0) {
+          tmp = eval_bool(cols, op.cond);
+          v = ColumnView{tmp.type_id, tmp.data, tmp.null_mask, 0, n, tmp.string_offsets};
+        }
+        try {
+          if (v.type == STRING) {
+            StrSource a, none;
+            a.kind = StrSource::COLUMN;
+            a.col = v;
+            out = build_strings(a, none, nullptr, nullptr, n, s);
+          } else {
+            if (v.type == FLOAT32 || v.type == FLOAT64)
+              fail(GX_ERR_UNSUPPORTED, "CAST of a floating-point value to VARCHAR");
+            if (type_size(v.type) == 0 || v.type >= DURATION_DAYS)
+              fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(v.type));
+            out = build_transform(op, StrSource{}, StrSource{}, &v, n, s);
+          }
+        } catch (...) {
+          if (tmp.data || tmp.null_mask) free_column(tmp, s);
+          throw;
+        }
+        if (tmp.data || tmp.null_mask) free_column(tmp, s);
+      } else if (op.kind == StringOp::SLICE || op.kind == StringOp::UPPER || op.kind == StringOp::LOWER ||
+                 op.kind == StringOp::INITCAP || op.kind == StringOp::TRIM || op.kind == StringOp::REPLACE ||
+                 op.kind == StringOp::CONCAT) {
+        StrSource a, b;
+        if (op.col >= 0) {
+          a.kind = StrSource::COLUMN;
+          a.col = string_col(op.col);
+        } else {
+          a.kind = StrSource::LITERAL;
+          a.literal = op.literal;
+        }
+        if (op.kind == StringOp::CONCAT) {
+          if (op.col2 >= 0) {
+            b.kind = StrSource::COLUMN;
+            b.col = string_col(op.col2);
+          } else {
+            b.kind = StrSource::LITERAL;
+            b.literal = op.literal2;
+          }
+        }
+        StringOp xo = op;
+        if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
+        out = build_transform(xo, a, b, nullptr, n, s);
+      } else if (op.kind == StringOp::PARSE) {
+        const ColumnView c = string_col(op.col);
+        out = alloc_column(op.type, n, s);
+        launch_parse(c, op.type, out, s);
       } else {
         const ColumnView c = string_col(op.col);  // a copy: cols grows below
         ColumnView c2{};

@@ -44,7 +44,9 @@ def _none() -> Node:
     return Node("NONE", [])
 
 
-def parse(text: str) -> Node:
+def parse(text: str, fn_types: bool = False) -> Node:
+    """fn_types: a function's result type ("CAST($0):VARCHAR") joins its name
+    ("CAST_VARCHAR"), as the evaluator's parser names such operators."""
     s = text.strip()
     pos = 0
 
@@ -60,7 +62,7 @@ def parse(text: str) -> Node:
             m = re.match(r"\$\d+", s[pos:])
             pos += m.end()
             return Node(m.group(0), var=True)
-        m = re.match(r"[A-Za-z_][A-Za-z_ ]*(?=\()|[=<>+\-*/]+(?=\()", s[pos:])
+        m = re.match(r"[A-Za-z_][A-Za-z_ ]*(?=\()|[=<>+\-*/|]+(?=\()", s[pos:])
         if m:
             name = m.group(0).strip()
             pos += m.end() + 1
@@ -74,6 +76,10 @@ def parse(text: str) -> Node:
                     args.append(expr())
                     skip()
             pos += 1
+            if fn_types and pos < len(s) and s[pos] == ":":
+                m = re.match(r":([A-Z_]+)", s[pos:])
+                pos += m.end()
+                name += "_" + m.group(1)
             return Node(name, args)
         m = re.match(r"'[^']*'(?::[A-Z]+)?|[^,()\s]+", s[pos:])
         pos += m.end()

@@ -16,6 +16,20 @@ operator by a synthetic column $k, computed by evaluate_string_functions
     parser/expression_tree.hpp:200-220, innermost pair first):
     cudf::copy_if_else(a, b, c), c evaluated by evaluate_expressions into a
     BOOL8 column; a NULL or false c selects b;
+  - SUBSTRING / LEFT / RIGHT / REVERSE: cudf::strings::slice_strings by
+    characters with the start / stop of :186-220 and :573-585;
+  - CONCAT / || (n-ary CONCAT nested to the left first,
+    expression_utils.cpp:1620): NULL if either side is;
+  - TRIM (strip of the given characters, or of characters <= ' ' when none
+    are given), REPLACE (every occurrence, left to right), UPPER / LOWER /
+    INITCAP (ASCII);
+  - CAST to VARCHAR (cast_to_str_functor, :62-92): "true" / "false", decimal
+    integers, "%Y-%m-%d" for dates and "%Y-%m-%d %H:%M:%S" for timestamps;
+  - CAST of a string column to an integer (cudf::strings::to_integers: an
+    optional sign, then digits up to the first other character, wrapped to
+    the type) or to DATE / TIMESTAMP (to_timestamps with "%Y-%m-%d" /
+    "%Y-%m-%d %H:%M:%S": each field read from its place in the format, up to
+    its first non-digit, 0 past the end of the string);
 and the interpreter compares string columns with string literals or with
 each other as string_view (interpreter_ops.cuh:623-719): bytes in
 lexicographic order.  A NULL string gives NULL.  The rest of the expression
@@ -76,7 +90,7 @@ def rewrite(texts: Sequence[str], string_cols: Sequence[int], ncols: int) -> Tup
     def key(op):
         if op not in ops:
             ops.append(op)
-            kinds[ncols + ops.index(op)] = STRING if op[0] == "CASE" else "num"
+            kinds[ncols + ops.index(op)] = STRING if op[0] in STRING_RESULTS else "num"
         return Node(f"${ncols + ops.index(op)}", var=True)
 
     def strcol(n):
@@ -89,11 +103,27 @@ def rewrite(texts: Sequence[str], string_cols: Sequence[int], ncols: int) -> Tup
             return ("null",)
         return ("lit", _unquote(n.value))
 
+    def int_lit(x):
+        if x.op or x.var or not re.fullmatch(r"-?\d+", x.value):
+            raise ValueError("non-literal position")
+        return int(x.value)
+
     def walk(n: Node) -> Node:
         if not n.op:
             return n
+        if n.value == "CONCAT" and len(n.children) > 2:
+            cur = n.children[0]
+            for c in n.children[1:]:
+                cur = Node("CONCAT", [cur, c])
+            n = cur
         n.children = [walk(c) for c in n.children]
         a = n.children
+        fn = string_function(n.value, a, strcol, int_lit)
+        if fn is not None:
+            return key(fn)
+        if n.value in ("CAST_VARCHAR", "CAST_CHAR") and len(a) == 1 and not a[0].op and not a[0].var \
+                and not _is_null(a[0]):
+            return Node(a[0].value if _is_lit(a[0]) else "'" + a[0].value + "'")
         if n.value == "LIKE" and len(a) == 2 and strcol(a[0]) and _is_lit(a[1]):
             return key(("LIKE", int(a[0].value[1:]), _unquote(a[1].value)))
         if n.value == "CHAR_LENGTH" and len(a) == 1 and strcol(a[0]):
@@ -138,10 +168,147 @@ def rewrite(texts: Sequence[str], string_cols: Sequence[int], ncols: int) -> Tup
         if not t:
             out.append(t)
             continue
-        root = walk(parse(t))
+        for side in ("BOTH", "LEADING", "TRAILING"):  # replace_calcite_regex (expression_utils.cpp:1096-1098)
+            t = t.replace(f"TRIM(FLAG({side}),", f'TRIM("{side}",')
+        root = walk(parse(t, fn_types=True))
         check(root, True)
         out.append(rebuild(root, typed=True))
     return out, ops
+
+
+STRING_RESULTS = {"CASE", "SLICE", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE", "CONCAT", "TO_STRING"}
+PARSE_TYPES = {"CAST_TINYINT": T.INT8, "CAST_SMALLINT": T.INT16, "CAST_INTEGER": T.INT32, "CAST_BIGINT": T.INT64,
+               "CAST_DATE": T.TIMESTAMP_DAYS, "CAST_TIMESTAMP_SECONDS": T.TIMESTAMP_SECONDS,
+               "CAST_TIMESTAMP_MILLISECONDS": T.TIMESTAMP_MILLISECONDS,
+               "CAST_TIMESTAMP_MICROSECONDS": T.TIMESTAMP_MICROSECONDS, "CAST_TIMESTAMP": T.TIMESTAMP_NANOSECONDS}
+
+
+def string_function(name, a, strcol, int_lit):
+    """The operator tuple of one of evaluate_string_functions' functions, or None."""
+    if name == "SUBSTRING" and len(a) in (2, 3) and strcol(a[0]):
+        start = max(int_lit(a[1]), 1) - 1
+        length = int_lit(a[2]) if len(a) == 3 else -1
+        return ("SLICE", int(a[0].value[1:]), start, start + length if length >= 0 else None, 1)
+    if name == "LEFT" and len(a) == 2 and strcol(a[0]):
+        return ("SLICE", int(a[0].value[1:]), 0, max(int_lit(a[1]), 0), 1)
+    if name == "RIGHT" and len(a) == 2 and strcol(a[0]):
+        k = max(int_lit(a[1]), 0)
+        return ("SLICE", int(a[0].value[1:]), -k, 0 if k < 1 else None, 1)
+    if name == "REVERSE" and len(a) == 1 and strcol(a[0]):
+        return ("SLICE", int(a[0].value[1:]), None, None, -1)
+    if name in ("UPPER", "LOWER", "INITCAP") and len(a) == 1 and strcol(a[0]):
+        return (name, int(a[0].value[1:]))
+    if name == "TRIM" and len(a) == 3 and strcol(a[2]):
+        return ("TRIM", int(a[2].value[1:]), _unquote(a[0].value), _unquote(a[1].value))
+    if name == "REPLACE" and len(a) == 3 and strcol(a[0]):
+        return ("REPLACE", int(a[0].value[1:]), _unquote(a[1].value), _unquote(a[2].value))
+    if name in ("CONCAT", "||") and len(a) == 2:
+        def operand(x):
+            if strcol(x):
+                return ("col", int(x.value[1:]))
+            if _is_lit(x):
+                return ("lit", _unquote(x.value))
+            raise ValueError("CONCAT of something other than strings")
+        return ("CONCAT", operand(a[0]), operand(a[1]))
+    if name in ("CAST_VARCHAR", "CAST_CHAR") and len(a) == 1 and (a[0].var or a[0].op):
+        return ("TO_STRING", int(a[0].value[1:]) if a[0].var else rebuild(a[0], typed=True))
+    if name in PARSE_TYPES and len(a) == 1 and strcol(a[0]):
+        return ("PARSE", int(a[0].value[1:]), PARSE_TYPES[name])
+    return None
+
+
+def _slice(v: str, start, stop, step):
+    """cudf::strings::slice_strings of one string, by characters."""
+    L = len(v)
+    if step < 0:
+        return v[::-1]
+    b = 0 if start is None else (min(start, L) if start >= 0 else max(L + start, 0))
+    e = L if stop is None else (min(stop, L) if stop >= 0 else max(L + stop, 0))
+    return v[b:e] if b < e else ""
+
+
+def _initcap(v: str) -> str:
+    out, word = [], False
+    for ch in v:
+        letter = ch.isascii() and ch.isalpha()
+        out.append((ch.lower() if word else ch.upper()) if letter else ch)
+        word = letter
+    return "".join(out)
+
+
+def _trim(v: str, side: str, chars: str) -> str:
+    def strip_me(c):
+        return ord(c) <= 32 if chars == "" else c in chars
+    b, e = 0, len(v)
+    if side != "TRAILING":
+        while b < e and strip_me(v[b]):
+            b += 1
+    if side != "LEADING":
+        while e > b and strip_me(v[e - 1]):
+            e -= 1
+    return v[b:e]
+
+
+def _civil(days: int) -> Tuple[int, int, int]:
+    import datetime
+    d = datetime.date(1970, 1, 1) + datetime.timedelta(days=days)
+    return d.year, d.month, d.day
+
+
+def format_value(t: int, x) -> str:
+    """cast_to_str_functor for one valid value."""
+    if t == T.BOOL8:
+        return "true" if x else "false"
+    if t in (T.INT8, T.INT16, T.INT32, T.INT64, T.UINT8, T.UINT16, T.UINT32, T.UINT64):
+        return str(int(x))
+    if t == T.TIMESTAMP_DAYS:
+        y, m, d = _civil(int(x))
+        return f"{y:04d}-{m:02d}-{d:02d}"
+    per = {T.TIMESTAMP_SECONDS: 1, T.TIMESTAMP_MILLISECONDS: 1000, T.TIMESTAMP_MICROSECONDS: 10 ** 6,
+           T.TIMESTAMP_NANOSECONDS: 10 ** 9}[t]
+    secs = int(x) // per
+    days, sod = secs // 86400, secs % 86400
+    y, m, d = _civil(days)
+    return f"{y:04d}-{m:02d}-{d:02d} {sod // 3600:02d}:{sod // 60 % 60:02d}:{sod % 60:02d}"
+
+
+def _digits(b: bytes) -> int:
+    v = 0
+    for c in b:
+        if not 48 <= c <= 57:
+            break
+        v = v * 10 + c - 48
+    return v
+
+
+def _days_from_civil(y: int, m: int, d: int) -> int:
+    y -= m <= 2
+    era = (y if y >= 0 else y - 399) // 400
+    yoe = y - era * 400
+    doy = (153 * (m + (-3 if m > 2 else 9)) + 2) // 5 + d - 1
+    doe = yoe * 365 + yoe // 4 - yoe // 100 + doy
+    return era * 146097 + doe - 719468
+
+
+def parse_value(t: int, v: str) -> int:
+    """to_integers / to_timestamps of one valid string."""
+    b = v.encode("utf-8")
+    if t in (T.INT8, T.INT16, T.INT32, T.INT64):
+        neg = b[:1] == b"-"
+        x = _digits(b[1:] if b[:1] in (b"-", b"+") else b)
+        x = (-x if neg else x) % (1 << 64)
+        bits = {T.INT8: 8, T.INT16: 16, T.INT32: 32, T.INT64: 64}[t]
+        x %= 1 << bits
+        return x - (1 << bits) if x >= 1 << (bits - 1) else x
+
+    def field(at, n):
+        return _digits(b[at:at + n]) if at < len(b) else 0
+    days = _days_from_civil(field(0, 4), field(5, 2), field(8, 2))
+    if t == T.TIMESTAMP_DAYS:
+        return days
+    secs = days * 86400 + field(11, 2) * 3600 + field(14, 2) * 60 + field(17, 2)
+    return secs * {T.TIMESTAMP_SECONDS: 1, T.TIMESTAMP_MILLISECONDS: 1000, T.TIMESTAMP_MICROSECONDS: 10 ** 6,
+                   T.TIMESTAMP_NANOSECONDS: 10 ** 9}[t]
 
 
 def evaluate_op(op, values: Sequence[Optional[str]], values2: Optional[Sequence[Optional[str]]] = None
@@ -201,6 +368,33 @@ def prepass(cols: Sequence, strings: dict, texts: Sequence[str], nthreads: int =
             a, b = src(op[2]), src(op[3])
             strings[k] = [a[i] if pick[i] else b[i] for i in range(n)]
             table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] in ("SLICE", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE"):
+            src = strings[op[1]]
+            f = {"SLICE": lambda v: _slice(v, op[2], op[3], op[4]), "UPPER": lambda v: v.upper(),
+                 "LOWER": lambda v: v.lower(), "INITCAP": _initcap,
+                 "TRIM": lambda v: _trim(v, op[2], op[3]), "REPLACE": lambda v: v.replace(op[2], op[3])}[op[0]]
+            strings[k] = [None if v is None else f(v) for v in src]
+            table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] == "CONCAT":
+            def side(o):
+                return strings[o[1]] if o[0] == "col" else [o[1]] * n
+            l, r = side(op[1]), side(op[2])
+            strings[k] = [None if x is None or y is None else x + y for x, y in zip(l, r)]
+            table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] == "TO_STRING":
+            if isinstance(op[1], int) and op[1] in strings:
+                strings[k] = list(strings[op[1]])
+            else:
+                c = table[op[1]] if isinstance(op[1], int) else pyoracle.evaluate_expressions(table, [op[1]], nthreads)[0]
+                valid = unpack_validity(c.mask, n) if c.mask is not None else np.ones(n, dtype=bool)
+                strings[k] = [format_value(c.type_id, c.data[i]) if valid[i] else None for i in range(n)]
+            table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] == "PARSE":
+            src, t = strings[op[1]], op[2]
+            valid = np.array([v is not None for v in src])
+            from blazingsql_gb300.types import np_dtype
+            data = np.array([parse_value(t, v) if v is not None else 0 for v in src], dtype=np_dtype(t))
+            table.append(HostColumn(t, data, pack_validity(valid)))
         else:
             rhs = op[2]
             if isinstance(rhs, tuple):

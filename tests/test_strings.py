@@ -269,6 +269,111 @@ def test_string_empty_inputs():
     assert out[0].to_strings() == [] and out[1].size == 0
 
 
+def _function_table(rng, n):
+    """String, numeric and temporal columns for the string functions."""
+    s0 = _strings(rng, n)
+    s3 = [None if v is None else " " * int(rng.integers(0, 3)) + v + " " * int(rng.integers(0, 3))
+          for v in _strings(rng, n, 0.2)]
+    nums = ["-12", "+7", "300", "12ab", "", "abc", "99999999999", "-0", "2147483648", "-9223372036854775808"]
+    s9 = [None if rng.random() < 0.1 else nums[int(rng.integers(0, len(nums)))] for _ in range(n)]
+    days = rng.integers(-1000, 20000, n)
+    s10 = [None if rng.random() < 0.1 else str(np.datetime64("1970-01-01") + np.timedelta64(int(d), "D")) for d in days]
+    secs = rng.integers(0, 2_000_000_000, n)
+    s11 = [None if rng.random() < 0.1 else str(np.datetime64(int(x), "s")).replace("T", " ") for x in secs]
+    ascii_alpha = list("abcXYZ 09-_.")
+    s12 = [None if rng.random() < 0.1 else "".join(rng.choice(ascii_alpha, int(rng.integers(0, 9))))
+           for _ in range(n)]
+    v = rng.random(n) > 0.1
+    cols = [None,
+            HostColumn(T.INT64, np.concatenate([[np.iinfo(np.int64).min], rng.integers(-10**12, 10**12, n - 1)])[:n]
+                       .astype(np.int64), pack_validity(v)),
+            HostColumn(T.FLOAT64, rng.normal(0, 10, n)),
+            None,
+            HostColumn(T.BOOL8, (rng.random(n) > 0.5).astype(np.uint8), pack_validity(rng.random(n) > 0.1)),
+            HostColumn(T.INT32, rng.integers(-2**31, 2**31 - 1, n).astype(np.int32)),
+            HostColumn(T.TIMESTAMP_DAYS, rng.integers(-5000, 40000, n).astype(np.int32)),
+            HostColumn(T.TIMESTAMP_SECONDS, rng.integers(0, 4_000_000_000, n).astype(np.int64)),
+            HostColumn(T.TIMESTAMP_MILLISECONDS, rng.integers(-10**12, 4 * 10**12, n).astype(np.int64)),
+            None, None, None, None]
+    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12}
+
+
+FUNCTION_EXPRS = [
+    "SUBSTRING($0, 2, 3)", "SUBSTRING($0, 0)", "SUBSTRING($0, 3)", "SUBSTRING($0, -1, 2)", "SUBSTRING($0, 2, 0)",
+    "LEFT($0, 2)", "LEFT($0, 0)", "RIGHT($0, 2)", "RIGHT($0, 0)", "RIGHT($0, 10)", "REVERSE($0)",
+    "TRIM(FLAG(BOTH), ' ', $3)", "TRIM(FLAG(LEADING), 'ab', $0)", "TRIM(FLAG(TRAILING), 'é ', $3)",
+    "REPLACE($0, 'ab', 'X')", "REPLACE($3, ' ', '')",
+    "CONCAT($0, $3)", "||($0, '-')", "CONCAT('<', $0, '|', $3, '>')",
+    "CAST($1):VARCHAR", "CAST($4):VARCHAR", "CAST($5):VARCHAR", "CAST($6):VARCHAR", "CAST($7):VARCHAR",
+    "CAST($8):VARCHAR", "CAST(+($1, 7)):VARCHAR", "CAST($0):VARCHAR", "CAST(5):VARCHAR",
+    "CAST($9):INTEGER", "CAST($9):BIGINT", "CAST($9):TINYINT", "CAST($9):SMALLINT", "CAST($10):DATE",
+    "CAST($11):TIMESTAMP", "CAST($11):TIMESTAMP_SECONDS",
+    "=(SUBSTRING($0, 1, 2), 'ab')", "CHAR_LENGTH(CONCAT($0, $3))", "+(CAST($9):INTEGER, 1)",
+    "UPPER($12)", "LOWER($12)", "INITCAP($12)", "CASE(>($5, 0), UPPER($12), REVERSE($0))",
+]
+
+
+def test_string_functions_oracle_rules():
+    """Slices by characters (cudf slice_strings), formatting and parsing rules of the oracle."""
+    assert strings_ref._slice("héllo", 1, 4, 1) == "éll"
+    assert strings_ref._slice("abc", -2, None, 1) == "bc"          # RIGHT($0, 2)
+    assert strings_ref._slice("abc", 0, 0, 1) == ""                # RIGHT($0, 0)
+    assert strings_ref._slice("aé", None, None, -1) == "éa"        # REVERSE, by characters
+    assert strings_ref.parse_value(T.INT8, "300") == 44            # wrapped to the type
+    assert strings_ref.parse_value(T.INT32, "-12ab") == -12        # digits up to the first other character
+    assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "1996-12-31") == 9861
+    assert strings_ref.format_value(T.TIMESTAMP_SECONDS, 851990400 + 3661) == "1996-12-31 01:01:01"
+    assert strings_ref.format_value(T.TIMESTAMP_MILLISECONDS, -1) == "1969-12-31 23:59:59"
+    texts, ops = strings_ref.rewrite(["CONCAT($0, '-', $1)"], [0, 1], 2)
+    assert texts == ["$3"] and [o[0] for o in ops] == ["CONCAT", "CONCAT"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 37, 4099, 60_001])
+def test_string_functions_match_oracle(n):
+    """SUBSTRING / LEFT / RIGHT / REVERSE / TRIM / REPLACE / CONCAT / UPPER /
+    LOWER / INITCAP and CASTs to and from VARCHAR against the oracle."""
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(300 + n)
+    cols, strings = _function_table(rng, n)
+    got = g.evaluate_expressions(_device(cols, strings), FUNCTION_EXPRS)
+    exp = strings_ref.evaluate_expressions(cols, strings, FUNCTION_EXPRS)
+    _compare(got, exp, f"string functions n={n}")
+
+
+@pytest.mark.gpu
+def test_string_functions_in_filters():
+    import blazingsql_gb300 as g
+    rng = np.random.default_rng(11)
+    n = 30_011
+    cols, strings = _function_table(rng, n)
+    dev = _device(cols, strings)
+    cond = "AND(=(LEFT($12, 1), 'a'), >(CAST($9):INTEGER, 0))"
+    exprs = ["CONCAT($0, '/', CAST($5):VARCHAR)", "$12", "CAST($10):DATE", "REVERSE($3)"]
+    got = g.filter_project(dev, cond, exprs)
+    exp, rows = strings_ref.filter_project(cols, strings, cond, exprs)
+    assert got[0].size == rows
+    _compare(got, exp, "string functions under a filter")
+
+
+@pytest.mark.gpu
+def test_string_function_errors():
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
+    from blazingsql_gb300.api import DeviceColumn
+    dev = [DeviceColumn.from_strings(["é", "b"]), DeviceColumn.from_host(HostColumn(T.FLOAT64, np.arange(2.0)))]
+    with pytest.raises(N.GxError, match="non-ASCII"):
+        g.evaluate_expressions(dev, ["UPPER($0)"])
+    with pytest.raises(N.GxError, match="floating-point"):
+        g.evaluate_expressions(dev, ["CAST($1):VARCHAR"])
+    with pytest.raises(N.GxError, match="floating-point"):
+        g.evaluate_expressions(dev, ["CAST($0):DOUBLE"])
+    with pytest.raises(N.GxError, match="non-literal"):
+        g.evaluate_expressions(dev, ["SUBSTRING($0, CAST($1):INTEGER)"])
+    with pytest.raises(N.GxError, match="between literals"):
+        g.evaluate_expressions(dev, ["CONCAT('a', 'b')"])
+
+
 def test_string_rewrite_oracle_rules():
     """Children-first rewriting: a string CASE becomes a column that an
     enclosing comparison then reads; CASE pairs fold from the innermost."""
