@@ -365,6 +365,135 @@ def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
     }
 
 
+def _string_column(torch, gen, phrases, rows, device):
+    """A cudf-layout string column whose rows are drawn from `phrases` (built on the device)."""
+    from blazingsql_gb300.api import DeviceColumn
+    from blazingsql_gb300.types import TypeId
+    width = max(len(p) for p in phrases)
+    tab = torch.zeros((len(phrases), width), dtype=torch.uint8)
+    for i, ph in enumerate(phrases):
+        tab[i, :len(ph)] = torch.tensor(list(ph.encode()), dtype=torch.uint8)
+    tab = tab.to(device)
+    plen = torch.tensor([len(ph) for ph in phrases], dtype=torch.int32, device=device)
+    ids = torch.randint(0, len(phrases), (rows,), generator=gen, device=device)
+    lens = plen[ids]
+    offs = torch.zeros(rows + 1, dtype=torch.int32, device=device)
+    offs[1:] = torch.cumsum(lens, 0, dtype=torch.int32)
+    keep = torch.arange(width, device=device, dtype=torch.int32)[None, :] < lens[:, None]
+    chars = torch.masked_select(tab[ids], keep)
+    del keep
+    return DeviceColumn(TypeId.STRING, chars if chars.numel() else torch.zeros(1, dtype=torch.uint8, device=device),
+                        None, 0, rows, offs)
+
+
+STRING_CONDITION = "AND(<=($4, 1998-09-02), NOT(LIKE($8, '%ke%q%')))"
+STRING_PROJECTIONS = ["$7", "SUBSTRING($8, 1, 10)", "CONCAT($7, '-', CAST($0):VARCHAR)",
+                      "*(*($1, -(100, $2)), +(100, $3))"]
+
+
+def strings_compare(rows: int, seed: int = 6, reps: int = 5):
+    """String columns on the path: the order-line columns plus a mode column
+    (7 short tokens) and a comment column (10-43 characters of random words),
+    filtered by a date and a LIKE on the comment, projecting the mode
+    (gathered), SUBSTRING of the comment, CONCAT of the mode with a formatted
+    integer, and the exact charge.  Inputs resident; the whole
+    gx_filter_project call is timed (string pre-pass, plan kernel, string
+    builders), its compulsory bytes against the measured HBM peak.  A sample
+    is checked against the CPU oracle and timed there."""
+    import numpy as np
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import workloads as W
+    from blazingsql_gb300.types import HostColumn, TypeId, np_dtype
+    rng = np.random.default_rng(seed)
+    letters = np.array(list("abcdefghijklmnopqrstuvwxyz"))
+    words = ["".join(rng.choice(letters, int(rng.integers(3, 10)))) for _ in range(200)]
+    comments = []
+    while len(comments) < 512:
+        ph = ""
+        target = int(rng.integers(10, 44))
+        while len(ph) < target:
+            ph = (ph + " " + words[int(rng.integers(0, len(words)))]).strip()
+        comments.append(ph[:target].strip() or "x")
+    modes = ["".join(rng.choice(letters, int(rng.integers(3, 8)))).upper() for _ in range(7)]
+    stream = torch.cuda.current_stream()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    cols = W.device_columns("c5", rows, seed=seed) + [_string_column(torch, gen, modes, rows, "cuda"),
+                                                      _string_column(torch, gen, comments, rows, "cuda")]
+    torch.cuda.synchronize()
+
+    def fp():
+        return g.filter_project(cols, STRING_CONDITION, STRING_PROJECTIONS, stream=stream)
+
+    for _ in range(4):
+        g.api.free_columns(fp(), stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        out = fp()
+        g.api.free_columns(out, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out = fp()
+    kept = out[0].size
+    # compulsory bytes: the referenced columns once, every output once
+    used = [0, 1, 2, 3, 4, 7, 8]
+    in_bytes = 0
+    for i in used:
+        c = cols[i]
+        in_bytes += c.data.numel() + (c.str_offsets.numel() * 4 if c.str_offsets is not None else 0)
+    out_bytes = 0
+    for c in out:
+        out_bytes += (c._c.string_bytes + 4 * (c.size + 1)) if c.type_id == TypeId.STRING else \
+            c.size * np_dtype(c.type_id).itemsize
+        out_bytes += (c.size + 7) // 8
+    g.api.free_columns(out, stream)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = (in_bytes + out_bytes) / (ms / 1e3) / 1e9
+    # the first ns rows against the oracle, and the oracle's rate on them
+    import time
+    from oracle import strings_ref
+    ns = min(rows, 1 << 14)
+    sample = W.slice_batches(cols, [ns])[0]
+    got = g.filter_project(sample, STRING_CONDITION, STRING_PROJECTIONS, stream=stream)
+    hc, hs = [], {}
+    for i, c in enumerate(cols):
+        if c.type_id == TypeId.STRING:
+            o = c.str_offsets[:ns + 1].cpu().numpy()
+            ch = c.data[:int(o[-1])].cpu().numpy().tobytes()
+            hs[i] = [ch[o[r]:o[r + 1]].decode() for r in range(ns)]
+            hc.append(None)
+        else:
+            dt = np_dtype(c.type_id)
+            hc.append(HostColumn(c.type_id, c.data[:ns * dt.itemsize].cpu().numpy().view(dt).copy()))
+    t0 = time.time()
+    exp, erows = strings_ref.filter_project(hc, hs, STRING_CONDITION, STRING_PROJECTIONS, nthreads=1)
+    oracle_s = time.time() - t0
+    ok = got[0].size == erows
+    for gc, ec in zip(got, exp):
+        if not ok:
+            break
+        if gc.type_id == TypeId.STRING:
+            ok = gc.to_strings() == ec
+        else:
+            h = gc.to_host()
+            ok = bool(np.array_equal(np.asarray(h.data[:erows]), np.asarray(ec.data[:erows])))
+    g.api.free_columns(got, stream)
+    del cols
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"order-line columns + 2 string columns: {rows} rows; filter {STRING_CONDITION}; "
+                    f"projections {STRING_PROJECTIONS}",
+        "rows_per_s": rows / (ms / 1e3), "ms": ms, "selectivity": kept / rows,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "algorithmic_bytes": in_bytes + out_bytes},
+        "oracle_sample_rows": ns, "matches_oracle": bool(ok), "oracle_rows_per_s": ns / oracle_s,
+    }
+
+
 def learned_compare(batches: int, rows: int, seed: int = 4):
     """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
     through gx_learner under four policies on the same resident batches:
@@ -494,6 +623,8 @@ def main():
     ap.add_argument("--learned-batches", type=int, default=64, help="C4 batches (0 skips the learned comparison)")
     ap.add_argument("--learned-rows", type=int, default=1 << 22, help="C4 rows per batch")
     ap.add_argument("--batched-batches", type=int, default=512, help="C3 batches (0 skips the batched comparison)")
+    ap.add_argument("--string-rows", type=int, default=1 << 25,
+                    help="rows of the string-column filter + project (0 skips it)")
     ap.add_argument("--agg-rows", type=int, default=1 << 27,
                     help="rows of the fused filter + aggregation measurement (0 skips it)")
     args = ap.parse_args()
@@ -631,6 +762,13 @@ def main():
             cols = None
             torch.cuda.empty_cache()
         aggregate = aggregate_compare(args.agg_rows)
+    strings = None
+    if args.string_rows > 0:
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
+        strings = strings_compare(args.string_rows)
     learned = None
     if args.learned_batches > 0:
         if cols is not None:
@@ -664,6 +802,7 @@ def main():
         "batched": batched,
         "learned": learned,
         "aggregate": aggregate,
+        "strings": strings,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -69,8 +69,10 @@ __device__ bool like_match(const unsigned char* s, int n, const unsigned char* p
 
 __device__ int compare_bytes(const unsigned char* s, int n, const unsigned char* p, int m) {
   const int k = n < m ? n : m;
-  for (int i = 0; i < k; i++)
-    if (s[i] != p[i]) return s[i] < p[i] ? -1 : 1;
+  for (int i = 0; i < k; i++) {
+    const unsigned char c = s[i];
+    if (c != p[i]) return c < p[i] ? -1 : 1;
+  }
   return n < m ? -1 : (n > m ? 1 : 0);
 }
 
@@ -147,8 +149,8 @@ __global__ void k_string_op(StrArgs a) {
 // A strings column is built in three launches: row sizes and validity (and a
 // character total per block), an exclusive scan of the block totals, then
 // offsets and characters.  A block covers kBuildWarps x kBuildWords 32-row
-// words; a warp copies the characters of its rows one row at a time, lanes
-// on consecutive bytes.
+// words.  A warp's rows are copied together by warp_copy when they are long,
+// a lane per row when they are short.
 constexpr int kBuildWarps = 8, kBuildWords = 8;
 constexpr int64_t kBuildRows = kBuildWarps * kBuildWords * 32;
 
@@ -157,6 +159,7 @@ struct BuildSrc {
   const unsigned char* chars;
   const uint32_t* mask;
   int64_t off;
+  int64_t end;  // the view's row end (off + size): its characters end at offs[end]
   const unsigned char* lit;
   int32_t lit_len;
   int32_t kind;  // StrSource::Kind
@@ -209,6 +212,36 @@ __device__ __forceinline__ int warp_sum(int v) {
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
   return v;
+}
+
+// Rows longer than this on average (bytes) are copied by warp_copy; shorter
+// ones by a lane each, which takes fewer instructions.
+constexpr int kWarpCopyBytes = 32;
+
+// The characters of a warp's 32 rows as one contiguous range of `total`
+// bytes at out: lane l's row starts at byte ex (its exclusive prefix) and is
+// n1 bytes from p1 followed by the rest from p2.  Lanes copy consecutive bytes
+// (coalesced loads and stores), each finding its byte's row by a binary search
+// over the lanes' prefixes.
+__device__ __forceinline__ void warp_copy(unsigned char* out, int ex, int n1, const unsigned char* p1,
+                                          const unsigned char* p2, int total, int lane) {
+  for (int base = 0; base < total; base += 32) {
+    const int k = base + lane;
+    int lo = 0;  // the last lane whose row starts at or before byte k
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int e = __shfl_sync(0xffffffffu, ex, lo + step);
+      if (e <= k) lo += step;
+    }
+    const int exj = __shfl_sync(0xffffffffu, ex, lo);
+    const int n1j = __shfl_sync(0xffffffffu, n1, lo);
+    const unsigned char* a1 = (const unsigned char*)__shfl_sync(0xffffffffu, (unsigned long long)p1, lo);
+    const unsigned char* a2 = (const unsigned char*)__shfl_sync(0xffffffffu, (unsigned long long)p2, lo);
+    if (k < total) {
+      const int r = k - exj;
+      out[k] = r < n1j ? a1[r] : a2[r - n1j];
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kBuildWarps * 32) k_str_sizes(BuildArgs a) {
@@ -273,14 +306,12 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_str_write(BuildArgs a) {
       a.out_offs[o] = (int32_t)dst;
       if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
     }
-    for (int j = 0; j < 32; j++) {
-      const int lj = __shfl_sync(0xffffffffu, len, j);
-      if (lj == 0) continue;
-      const unsigned char* pj = (const unsigned char*)__shfl_sync(0xffffffffu, (unsigned long long)p, j);
-      const uint64_t dj = __shfl_sync(0xffffffffu, (unsigned long long)dst, j);
-      for (int b = lane; b < lj; b += 32) a.out_chars[dj + b] = pj[b];
-    }
-    pos += (uint64_t)__shfl_sync(0xffffffffu, incl, 31);
+    const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+    if (wtot > 32 * kWarpCopyBytes)  // long rows: the warp copies them together
+      warp_copy(a.out_chars + pos, incl - len, len, p, nullptr, wtot, lane);
+    else  // short rows: a lane copies its own
+      for (int i = 0; i < len; i++) a.out_chars[dst + i] = p[i];
+    pos += (uint64_t)wtot;
   }
 }
 
@@ -447,44 +478,96 @@ __device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, boo
   return at;
 }
 
-__device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
-  if (a.kind == StringOp::TO_STRING) return format_value(a, o, d, valid);
+// The functions whose result is one or two byte ranges of their inputs
+// (slices by a positive step, TRIM, CONCAT): the row is n1 bytes at p1, then
+// len - n1 bytes at p2.  Returns len.
+__device__ __forceinline__ bool is_segment_kind(const XformArgs& a) {
+  return (a.kind == StringOp::SLICE && a.step > 0) || a.kind == StringOp::TRIM || a.kind == StringOp::CONCAT;
+}
+
+__device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char*& p1, int& n1,
+                              const unsigned char*& p2, bool& valid) {
   const unsigned char* p;
   int n;
   source_row(a.a, o, p, n, valid);
+  p1 = p2 = nullptr;
+  n1 = 0;
   if (a.kind == StringOp::CONCAT) {  // cudf::strings::concatenate: NULL if either side is
-    const unsigned char* p2;
-    int n2;
+    const unsigned char* q;
+    int m;
     bool v2;
-    source_row(a.b, o, p2, n2, v2);
+    source_row(a.b, o, q, m, v2);
     valid = valid && v2;
     if (!valid) return 0;
-    return put(d, put(d, 0, p, n), p2, n2);
+    p1 = p;
+    n1 = n;
+    p2 = q;
+    return n + m;
   }
   if (!valid) return 0;
+  if (a.kind == StringOp::SLICE) {  // cudf::strings::slice_strings, characters [begin, end)
+    int L = 0;
+    for (int i = 0; i < n; i++) L += (p[i] & 0xC0) != 0x80;
+    int b = 0, e = L;
+    if (a.i0v) b = a.i0 >= 0 ? (a.i0 < L ? a.i0 : L) : (L + a.i0 >= 0 ? L + a.i0 : 0);
+    if (a.i1v) e = a.i1 >= 0 ? (a.i1 < L ? a.i1 : L) : (L + a.i1 >= 0 ? L + a.i1 : 0);
+    if (b >= e) return 0;
+    int bb = 0, c = 0;
+    while (c < b) { bb += utf8_len(p[bb]); c++; }
+    int eb = bb;
+    while (c < e) { eb += utf8_len(p[eb]); c++; }
+    p1 = p + bb;
+    n1 = eb - bb;
+    return n1;
+  }
+  // TRIM: cudf::strings::strip
+  int b = 0, e = n;
+  if (a.i0 != 2)
+    while (b < e) {
+      const int k = utf8_len(p[b]);
+      if (!in_set(p, b, k, a.s1, a.l1)) break;
+      b += k;
+    }
+  if (a.i0 != 1)
+    while (e > b) {
+      int k = e - 1;
+      while (k > b && (p[k] & 0xC0) == 0x80) k--;
+      if (!in_set(p, k, e - k, a.s1, a.l1)) break;
+      e = k;
+    }
+  p1 = p + b;
+  n1 = e - b;
+  return n1;
+}
+
+__device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
+  if (a.kind == StringOp::TO_STRING) return format_value(a, o, d, valid);
+  if (is_segment_kind(a)) {
+    const unsigned char *p1, *p2;
+    int n1;
+    const int len = xform_segments(a, o, p1, n1, p2, valid);
+    if (d) {
+      put(d, 0, p1, n1);
+      put(d, n1, p2, len - n1);
+    }
+    return len;
+  }
+  const unsigned char* p;
+  int n;
+  source_row(a.a, o, p, n, valid);
+  if (!valid) return 0;
   switch (a.kind) {
-    case StringOp::SLICE: {  // cudf::strings::slice_strings, characters [begin, end) by step
-      int L = 0;
-      for (int i = 0; i < n; i += utf8_len(p[i])) L++;
-      if (a.step < 0) {  // the whole string, characters in reverse order
-        int at = 0, e = n;
-        while (e > 0) {
-          int b = e - 1;
-          while (b > 0 && (p[b] & 0xC0) == 0x80) b--;
-          at = put(d, at, p + b, e - b);
-          e = b;
-        }
-        return at;
+    case StringOp::SLICE: {  // a negative step: the whole string, characters in reverse order
+      int at = 0, e = n;
+      while (e > 0) {
+        int b = e - 1;
+        while (b > 0 && (p[b] & 0xC0) == 0x80) b--;
+        if (d)
+          for (int i = b; i < e; i++) d[at + i - b] = p[i];
+        at += e - b;
+        e = b;
       }
-      int b = 0, e = L;
-      if (a.i0v) b = a.i0 >= 0 ? (a.i0 < L ? a.i0 : L) : (L + a.i0 >= 0 ? L + a.i0 : 0);
-      if (a.i1v) e = a.i1 >= 0 ? (a.i1 < L ? a.i1 : L) : (L + a.i1 >= 0 ? L + a.i1 : 0);
-      if (b >= e) return 0;
-      int bb = 0, c = 0;
-      while (c < b) { bb += utf8_len(p[bb]); c++; }
-      int eb = bb;
-      while (c < e) { eb += utf8_len(p[eb]); c++; }
-      return put(d, 0, p + bb, eb - bb);
+      return at;
     }
     case StringOp::UPPER: case StringOp::LOWER: case StringOp::INITCAP: {
       bool word = false;  // INITCAP: inside a run of letters (cudf::strings::title)
@@ -506,19 +589,6 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
       }
       return n;
     }
-    case StringOp::TRIM: {  // cudf::strings::strip
-      int b = 0, e = n;
-      if (a.i0 != 2)
-        while (b < e && in_set(p, b, utf8_len(p[b]), a.s1, a.l1)) b += utf8_len(p[b]);
-      if (a.i0 != 1)
-        while (e > b) {
-          int k = e - 1;
-          while (k > b && (p[k] & 0xC0) == 0x80) k--;
-          if (!in_set(p, k, e - k, a.s1, a.l1)) break;
-          e = k;
-        }
-      return put(d, 0, p + b, e - b);
-    }
     case StringOp::REPLACE: {  // cudf::strings::replace, every occurrence, left to right
       int at = 0, i = 0;
       while (i < n) {
@@ -528,7 +598,8 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
           at = put(d, at, a.s2, a.l2);
           i += a.l1;
         } else {
-          at = put(d, at, p + i, 1);
+          if (d) d[at] = p[i];
+          at++;
           i++;
         }
       }
@@ -566,15 +637,14 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
-  int lens[kBuildWords];
   uint64_t total = 0;
   for (int k = 0; k < kBuildWords; k++) {
-    lens[k] = 0;
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
     bool valid = false;
-    if (o < a.m) lens[k] = xform_row(a, o, nullptr, valid);
-    total += (uint64_t)warp_sum(lens[k]);
+    int len = 0;
+    if (o < a.m) len = xform_row(a, o, nullptr, valid);
+    total += (uint64_t)warp_sum(len);
   }
   if (lane == 0) s_sum[warp] = total;
   __syncthreads();
@@ -583,7 +653,11 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
-    const int len = lens[k];
+    const bool seg = is_segment_kind(a);  // warp-uniform
+    const unsigned char *p1 = nullptr, *p2 = nullptr;
+    int n1 = 0, len = 0;
+    bool valid = false;
+    if (o < a.m) len = seg ? xform_segments(a, o, p1, n1, p2, valid) : xform_row(a, o, nullptr, valid);
     int incl = len;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -594,10 +668,17 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
     if (o < a.m) {
       a.out_offs[o] = (int32_t)dst;
       if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
-      bool valid = false;
-      if (len > 0) xform_row(a, o, a.out_chars + dst, valid);
     }
-    pos += (uint64_t)__shfl_sync(0xffffffffu, incl, 31);
+    const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+    if (seg && wtot > 32 * kWarpCopyBytes) {  // long rows: the warp copies them together
+      warp_copy(a.out_chars + pos, incl - len, n1, p1, p2, wtot, lane);
+    } else if (seg) {
+      for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
+      for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
+    } else if (o < a.m && len > 0) {
+      xform_row(a, o, a.out_chars + dst, valid);
+    }
+    pos += (uint64_t)wtot;
   }
 }
 
@@ -687,6 +768,7 @@ BuildSrc device_source(const StrSource& s, const unsigned char* lit_dev) {
     b.chars = (const unsigned char*)s.col.data;
     b.mask = s.col.mask;
     b.off = s.col.offset;
+    b.end = s.col.offset + s.col.size;
   } else if (s.kind == StrSource::LITERAL) {
     b.lit = lit_dev;
     b.lit_len = (int32_t)s.literal.size();
@@ -901,14 +983,16 @@ std::vector<gx_column> run_string_prepass(
   if (ops.empty()) return made;
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   size_t pbytes = 0;
-  for (const auto& op : ops) pbytes += (op.literal.size() + 15) / 16 * 16;
+  // a 16-byte aligned slot of 16 bytes or more per literal
+  auto slot = [](size_t len) { return (std::max<size_t>(len, 1) + 15) / 16 * 16; };
+  for (const auto& op : ops) pbytes += slot(op.literal.size());
   std::string host(std::max<size_t>(pbytes, 16), '\0');
   std::vector<size_t> poff;
   size_t at = 0;
   for (const auto& op : ops) {
     poff.push_back(at);
     std::memcpy(&host[at], op.literal.data(), op.literal.size());
-    at += (op.literal.size() + 15) / 16 * 16;
+    at += slot(op.literal.size());
   }
   char* pdev = (char*)dev_alloc(host.size(), s);
   auto string_col = [&](int c) {

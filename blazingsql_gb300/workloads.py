@@ -172,7 +172,7 @@ def slice_batches(cols, sizes: Sequence[int]):
     out = []
     start = 0
     for n in sizes:
-        out.append([DeviceColumn(c.type_id, c.data, c.mask, c.offset + start, n) for c in cols])
+        out.append([DeviceColumn(c.type_id, c.data, c.mask, c.offset + start, n, c.str_offsets) for c in cols])
         start += n
     return out
 
