@@ -31,9 +31,14 @@ __device__ __forceinline__ int utf8_len(unsigned char c) {
 
 // The LIKE pattern's regular expression searched in s: '%' between other
 // pattern characters is a run of characters but a newline, '_' one character
-// but a newline.  A leading '%' (no '^' anchor) lets the match start
-// anywhere, a trailing one (no '$' anchor) end anywhere, newlines included.
-// Greedy with backtracking to the last '%'.
+// but a newline.  A trailing '%' (no '$' anchor) lets the match end anywhere.
+// A leading '%' (no '^' anchor) lets it start anywhere: each start t is tried
+// in turn.  From a start, a greedy match that backtracks to its last inner
+// '%' (the classic wildcard algorithm; inner '%'s cannot cross a newline, so
+// none of them can take over where the last one stops).  A start fails over
+// to the next when a newline or a mismatch before the first inner '%' stops
+// it; when the last inner '%' has run to the end of s, no later start can
+// match either.
 __device__ bool like_match(const unsigned char* s, int n, const unsigned char* p, int m) {
   if (m == 0) return true;
   int lead = 0;  // the leading run of '%'
@@ -41,29 +46,32 @@ __device__ bool like_match(const unsigned char* s, int n, const unsigned char* p
   if (lead == m) return true;
   int tail = m;  // pattern positions >= tail are the trailing run of '%'
   while (tail > lead && p[tail - 1] == '%') tail--;
-  int i = 0, j = lead, star_j = lead > 0 ? lead - 1 : -1, star_i = 0;
-  while (true) {
-    if (j >= tail) {
-      if (tail < m || i == n) return true;  // a trailing '%' takes any rest
-    } else if (i < n) {
-      if (p[j] == '%') {
-        star_j = j++;
-        star_i = i;
-        continue;
+  for (int t = 0;; t += utf8_len(s[t])) {
+    int i = t, j = lead, star_j = -1, star_i = 0;
+    while (true) {
+      if (j >= tail) {
+        if (tail < m || i == n) return true;  // a trailing '%' takes any rest
+      } else if (i < n) {
+        if (p[j] == '%') {
+          star_j = j++;
+          star_i = i;
+          continue;
+        }
+        if (p[j] == '_' ? s[i] != '\n' : p[j] == s[i]) {
+          i += p[j] == '_' ? utf8_len(s[i]) : 1;
+          j++;
+          continue;
+        }
       }
-      if (p[j] == '_' ? s[i] != '\n' : p[j] == s[i]) {
-        i += p[j] == '_' ? utf8_len(s[i]) : 1;
-        j++;
-        continue;
-      }
+      // retry from the last inner '%' one character further
+      if (star_j < 0) break;                  // no inner '%' yet: the next start
+      if (star_i >= n) return false;          // ran to the end: no start can match
+      if (s[star_i] == '\n') break;           // an inner '%' stops at a newline
+      star_i += utf8_len(s[star_i]);
+      i = star_i;
+      j = star_j + 1;
     }
-    // retry from the last '%' one character further; an inner '%' stops at a
-    // newline, the leading one does not
-    if (star_j < 0 || star_i >= n) return false;
-    if (star_j >= lead && s[star_i] == '\n') return false;
-    star_i += utf8_len(s[star_i]);
-    i = star_i;
-    j = star_j + 1;
+    if (lead == 0 || t >= n) return false;
   }
 }
 

@@ -65,6 +65,23 @@ def test_string_operators_match_oracle(n):
 
 
 @pytest.mark.gpu
+def test_like_exhaustive_small_cases():
+    """Every string of up to 5 characters over {a, b, newline} against LIKE
+    patterns whose inner '%' must restart after a newline (the regular
+    expression's search tries every start; '%' and '_' never cover a newline)."""
+    import itertools
+    import blazingsql_gb300 as g
+    from blazingsql_gb300.api import DeviceColumn
+    strs = [""] + ["".join(t) for k in range(1, 6) for t in itertools.product("ab\n", repeat=k)]
+    pats = ["%a%a", "%b%_", "%%_%_", "%_%__", "%%b%a", "%a%_", "%_%a", "%_%b%", "a%b", "%a_b%", "_%", "%_",
+            "a%", "%ab", "%a%b%a%", "__", "%b", "b%a%", "%", ""]
+    exprs = [f"LIKE($0, '{p}')" for p in pats]
+    got = g.evaluate_expressions([DeviceColumn.from_strings(strs)], exprs)
+    exp = strings_ref.evaluate_expressions([None], {0: strs}, exprs)
+    _compare(got, exp, "LIKE small cases")
+
+
+@pytest.mark.gpu
 def test_filter_with_like_matches_oracle():
     import blazingsql_gb300 as g
     from blazingsql_gb300.api import DeviceColumn
