@@ -1191,6 +1191,24 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
       op.kind = StringOp::PARSE;
       op.col = a[0]->col;
       op.type = pt->second;
+      // to_timestamps' formats for the CASTs (LogicalProject.cpp:468-528)
+      if (pt->second == TIMESTAMP_DAYS) op.literal = "%Y-%m-%d";
+      else if (pt->second != INT8 && pt->second != INT16 && pt->second != INT32 && pt->second != INT64)
+        op.literal = "%Y-%m-%d %H:%M:%S";
+      return true;
+    }
+    if ((t == "TO_DATE" || t == "TO_TIMESTAMP") && a.size() == 2) {
+      // :530-552: a string column and a string format
+      if (!strcol(a[0]) || !is_string_literal(a[1]))
+        fail(GX_ERR_UNSUPPORTED, t + " operator arguments must be a column and a string format");
+      op.kind = StringOp::PARSE;
+      op.col = a[0]->col;
+      op.type = t == "TO_DATE" ? TIMESTAMP_DAYS : TIMESTAMP_NANOSECONDS;
+      op.literal = unquote(a[1]->token);
+      const std::string& f = op.literal;
+      if (f.find("%Y") == std::string::npos || f.find("%m") == std::string::npos ||
+          f.find("%d") == std::string::npos)
+        fail(GX_ERR_UNSUPPORTED, t + " format without %Y, %m and %d: " + f);
       return true;
     }
     return false;

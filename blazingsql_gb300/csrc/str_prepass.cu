@@ -692,12 +692,18 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
 
 // string -> integer / DATE / TIMESTAMP (cudf::strings::to_integers and
 // to_timestamps with "%Y-%m-%d" / "%Y-%m-%d %H:%M:%S", LogicalProject.cpp:379-528)
+constexpr int kMaxFormatItems = 32;
 struct ParseArgs {
   BuildSrc a;
   int type;
   int64_t m;
   void* out;
   uint32_t* out_mask;
+  // DATE / TIMESTAMP: the format's items in order, each a field (index into
+  // Y m d H M S) or a literal (-1), and its width in bytes
+  int nitems;
+  signed char field[kMaxFormatItems];
+  unsigned char width[kMaxFormatItems];
 };
 
 // digits from s[0..n) up to the first non-digit
@@ -734,13 +740,20 @@ __global__ void k_parse(ParseArgs a) {
       int64_t v = 0;
       if (valid && (a.type == TIMESTAMP_DAYS || a.type == TIMESTAMP_SECONDS || a.type == TIMESTAMP_MILLISECONDS ||
                     a.type == TIMESTAMP_MICROSECONDS || a.type == TIMESTAMP_NANOSECONDS)) {
-        // fields at fixed places of the format; a field past the end of the string is 0
-        auto field = [&](int at, int len) { return at < n ? leading_digits(p + at, min(len, n - at)) : 0; };
-        const int64_t days = days_from_civil(field(0, 4), field(5, 2), field(8, 2));
+        // the format's items in order, each taking its width (less at the end of
+        // the string); a field reads its digits up to the first non-digit
+        int64_t f[6] = {0, 0, 0, 0, 0, 0};
+        int at = 0;
+        for (int k = 0; k < a.nitems; k++) {
+          const int w = max(0, min((int)a.width[k], n - at));
+          if (a.field[k] >= 0) f[a.field[k]] = leading_digits(p + at, w);
+          at += w;
+        }
+        const int64_t days = days_from_civil(f[0], f[1], f[2]);
         if (a.type == TIMESTAMP_DAYS) {
           v = days;
         } else {
-          const int64_t secs = days * 86400 + field(11, 2) * 3600 + field(14, 2) * 60 + field(17, 2);
+          const int64_t secs = days * 86400 + f[3] * 3600 + f[4] * 60 + f[5];
           const int64_t per = a.type == TIMESTAMP_SECONDS ? 1 : a.type == TIMESTAMP_MILLISECONDS ? 1000
                             : a.type == TIMESTAMP_MICROSECONDS ? 1000000 : 1000000000;
           v = secs * per;
@@ -939,8 +952,27 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
   return out;
 }
 
-void launch_parse(const ColumnView& col, int type, gx_column& out, cudaStream_t s) {
+void launch_parse(const ColumnView& col, int type, const std::string& format, gx_column& out, cudaStream_t s) {
   ParseArgs a{};
+  // cudf::strings::to_timestamps' items: %Y 4 bytes, %m %d %H %M %S 2, any
+  // other character (and %%) 1
+  for (size_t i = 0; i < format.size(); i++) {
+    if (a.nitems == kMaxFormatItems) fail(GX_ERR_UNSUPPORTED, "timestamp format too long: " + format);
+    int field = -1, width = 1;
+    if (format[i] == '%' && i + 1 < format.size()) {
+      const char c = format[++i];
+      static const char* kFields = "YmdHMS";
+      const char* at = c == '%' ? nullptr : std::strchr(kFields, c);
+      if (c != '%' && !at) fail(GX_ERR_UNSUPPORTED, std::string("timestamp format specifier %") + c);
+      if (at) {
+        field = (int)(at - kFields);
+        width = c == 'Y' ? 4 : 2;
+      }
+    }
+    a.field[a.nitems] = (signed char)field;
+    a.width[a.nitems] = (unsigned char)width;
+    a.nitems++;
+  }
   StrSource src;
   src.kind = StrSource::COLUMN;
   src.col = col;
@@ -1089,7 +1121,7 @@ std::vector<gx_column> run_string_prepass(
       } else if (op.kind == StringOp::PARSE) {
         const ColumnView c = string_col(op.col);
         out = alloc_column(op.type, n, s);
-        launch_parse(c, op.type, out, s);
+        launch_parse(c, op.type, op.literal, out, s);
       } else {
         const ColumnView c = string_col(op.col);  // a copy: cols grows below
         ColumnView c2{};

@@ -213,7 +213,13 @@ def string_function(name, a, strcol, int_lit):
     if name in ("CAST_VARCHAR", "CAST_CHAR") and len(a) == 1 and (a[0].var or a[0].op):
         return ("TO_STRING", int(a[0].value[1:]) if a[0].var else rebuild(a[0], typed=True))
     if name in PARSE_TYPES and len(a) == 1 and strcol(a[0]):
-        return ("PARSE", int(a[0].value[1:]), PARSE_TYPES[name])
+        t = PARSE_TYPES[name]
+        fmt = None if t in (T.INT8, T.INT16, T.INT32, T.INT64) else \
+            ("%Y-%m-%d" if t == T.TIMESTAMP_DAYS else "%Y-%m-%d %H:%M:%S")
+        return ("PARSE", int(a[0].value[1:]), t, fmt)
+    if name in ("TO_DATE", "TO_TIMESTAMP") and len(a) == 2 and strcol(a[0]) and _is_lit(a[1]):
+        return ("PARSE", int(a[0].value[1:]), T.TIMESTAMP_DAYS if name == "TO_DATE" else T.TIMESTAMP_NANOSECONDS,
+                _unquote(a[1].value))
     return None
 
 
@@ -290,7 +296,21 @@ def _days_from_civil(y: int, m: int, d: int) -> int:
     return era * 146097 + doe - 719468
 
 
-def parse_value(t: int, v: str) -> int:
+def _format_items(fmt: str):
+    """to_timestamps' items: (field index in Y m d H M S or None, width)."""
+    items, i = [], 0
+    while i < len(fmt):
+        if fmt[i] == "%" and i + 1 < len(fmt):
+            c = fmt[i + 1]
+            i += 2
+            items.append(("YmdHMS".index(c), 4 if c == "Y" else 2) if c != "%" else (None, 1))
+        else:
+            items.append((None, 1))
+            i += 1
+    return items
+
+
+def parse_value(t: int, v: str, fmt: Optional[str] = None) -> int:
     """to_integers / to_timestamps of one valid string."""
     b = v.encode("utf-8")
     if t in (T.INT8, T.INT16, T.INT32, T.INT64):
@@ -301,12 +321,16 @@ def parse_value(t: int, v: str) -> int:
         x %= 1 << bits
         return x - (1 << bits) if x >= 1 << (bits - 1) else x
 
-    def field(at, n):
-        return _digits(b[at:at + n]) if at < len(b) else 0
-    days = _days_from_civil(field(0, 4), field(5, 2), field(8, 2))
+    f, at = [0] * 6, 0
+    for field, width in _format_items(fmt or ("%Y-%m-%d" if t == T.TIMESTAMP_DAYS else "%Y-%m-%d %H:%M:%S")):
+        w = max(0, min(width, len(b) - at))
+        if field is not None:
+            f[field] = _digits(b[at:at + w])
+        at += w
+    days = _days_from_civil(f[0], f[1], f[2])
     if t == T.TIMESTAMP_DAYS:
         return days
-    secs = days * 86400 + field(11, 2) * 3600 + field(14, 2) * 60 + field(17, 2)
+    secs = days * 86400 + f[3] * 3600 + f[4] * 60 + f[5]
     return secs * {T.TIMESTAMP_SECONDS: 1, T.TIMESTAMP_MILLISECONDS: 1000, T.TIMESTAMP_MICROSECONDS: 10 ** 6,
                    T.TIMESTAMP_NANOSECONDS: 10 ** 9}[t]
 
@@ -393,7 +417,7 @@ def prepass(cols: Sequence, strings: dict, texts: Sequence[str], nthreads: int =
             src, t = strings[op[1]], op[2]
             valid = np.array([v is not None for v in src])
             from blazingsql_gb300.types import np_dtype
-            data = np.array([parse_value(t, v) if v is not None else 0 for v in src], dtype=np_dtype(t))
+            data = np.array([parse_value(t, v, op[3]) if v is not None else 0 for v in src], dtype=np_dtype(t))
             table.append(HostColumn(t, data, pack_validity(valid)))
         else:
             rhs = op[2]

@@ -311,8 +311,9 @@ def _function_table(rng, n):
             HostColumn(T.TIMESTAMP_DAYS, rng.integers(-5000, 40000, n).astype(np.int32)),
             HostColumn(T.TIMESTAMP_SECONDS, rng.integers(0, 4_000_000_000, n).astype(np.int64)),
             HostColumn(T.TIMESTAMP_MILLISECONDS, rng.integers(-10**12, 4 * 10**12, n).astype(np.int64)),
-            None, None, None, None]
-    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12}
+            None, None, None, None, None]
+    s13 = [None if v is None else f"{v[8:10]}/{v[5:7]}/{v[:4]}" for v in s10]  # day/month/year
+    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12, 13: s13}
 
 
 FUNCTION_EXPRS = [
@@ -327,6 +328,8 @@ FUNCTION_EXPRS = [
     "CAST($11):TIMESTAMP", "CAST($11):TIMESTAMP_SECONDS",
     "=(SUBSTRING($0, 1, 2), 'ab')", "CHAR_LENGTH(CONCAT($0, $3))", "+(CAST($9):INTEGER, 1)",
     "UPPER($12)", "LOWER($12)", "INITCAP($12)", "CASE(>($5, 0), UPPER($12), REVERSE($0))",
+    "TO_DATE($10, '%Y-%m-%d')", "TO_TIMESTAMP($11, '%Y-%m-%d %H:%M:%S')", "TO_DATE($13, '%d/%m/%Y')",
+    "TO_TIMESTAMP($13, '%d/%m/%Y')", "TO_DATE($11, '%Y%%%m%d')",
 ]
 
 
@@ -341,6 +344,8 @@ def test_string_functions_oracle_rules():
     assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "1996-12-31") == 9861
     assert strings_ref.format_value(T.TIMESTAMP_SECONDS, 851990400 + 3661) == "1996-12-31 01:01:01"
     assert strings_ref.format_value(T.TIMESTAMP_MILLISECONDS, -1) == "1969-12-31 23:59:59"
+    assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "31/12/1996", "%d/%m/%Y") == 9861
+    assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "1996-12", "%Y-%m-%d") == strings_ref._days_from_civil(1996, 12, 0)
     texts, ops = strings_ref.rewrite(["CONCAT($0, '-', $1)"], [0, 1], 2)
     assert texts == ["$3"] and [o[0] for o in ops] == ["CONCAT", "CONCAT"]
 
@@ -389,6 +394,10 @@ def test_string_function_errors():
         g.evaluate_expressions(dev, ["SUBSTRING($0, CAST($1):INTEGER)"])
     with pytest.raises(N.GxError, match="between literals"):
         g.evaluate_expressions(dev, ["CONCAT('a', 'b')"])
+    with pytest.raises(N.GxError, match="without"):
+        g.evaluate_expressions(dev, ["TO_DATE($0, '%Y-%m')"])
+    with pytest.raises(N.GxError, match="specifier"):
+        g.evaluate_expressions(dev, ["TO_TIMESTAMP($0, '%Y-%m-%d %I')"])
 
 
 def test_string_rewrite_oracle_rules():
