@@ -1158,19 +1158,6 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
       if (op.literal.empty()) fail(GX_ERR_UNSUPPORTED, "REPLACE with an empty target");
       return true;
     }
-    if ((t == "CONCAT" || t == "||") && a.size() == 2) {
-      if (is_string_literal(a[0]) && is_string_literal(a[1]))  // :311
-        fail(GX_ERR_UNSUPPORTED, "CONCAT operator between literals is not supported");
-      for (const auto& x : a)
-        if (!strcol(x) && !is_string_literal(x))
-          fail(GX_ERR_UNSUPPORTED, "CONCAT of something other than strings");
-      op.kind = StringOp::CONCAT;
-      if (strcol(a[0])) op.col = a[0]->col;
-      else op.literal = unquote(a[0]->token);
-      if (strcol(a[1])) op.col2 = a[1]->col;
-      else op.literal2 = unquote(a[1]->token);
-      return true;
-    }
     if ((t == "CAST_VARCHAR" || t == "CAST_CHAR") && a.size() == 1) {
       if (a[0]->kind == Expr::LIT) fail(GX_ERR_UNSUPPORTED, "CAST operator not supported for literals");
       op.kind = StringOp::TO_STRING;
@@ -1222,18 +1209,45 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
     bool touched = false;
     std::function<ExprPtr(ExprPtr)> walk = [&](ExprPtr e) -> ExprPtr {
       if (e->kind != Expr::OP) return e;
-      if (e->token == "CONCAT" && e->ch.size() > 2) {
-        // CONCAT(a, b, c) -> CONCAT(CONCAT(a, b), c) (convert_nary_to_binary_concat,
-        // expression_utils.cpp:1620)
-        ExprPtr cur = e->ch[0];
-        for (size_t k = 1; k < e->ch.size(); k++) {
-          auto n = std::make_shared<Expr>();
-          n->kind = Expr::OP;
-          n->token = "CONCAT";
-          n->ch = {cur, e->ch[k]};
-          cur = n;
+      if ((e->token == "CONCAT" || e->token == "||") && e->ch.size() >= 2) {
+        // The reference nests CONCAT(a, b, c) as CONCAT(CONCAT(a, b), c)
+        // (convert_nary_to_binary_concat, expression_utils.cpp:1620) and
+        // evaluates each pair, NULL if either side is.  That is one
+        // concatenation of all parts, NULL if any is: nested CONCATs are
+        // flattened into parts, up to kMaxConcatParts per operator.  Its
+        // innermost pair of literals is still refused (:311).
+        std::vector<ExprPtr> parts;
+        std::function<void(const ExprPtr&)> flat = [&](const ExprPtr& x) {
+          if (x->kind == Expr::OP && (x->token == "CONCAT" || x->token == "||") && x->ch.size() >= 2) {
+            if (is_string_literal(x->ch[0]) && is_string_literal(x->ch[1]))
+              fail(GX_ERR_UNSUPPORTED, "CONCAT operator between literals is not supported");
+            for (const auto& c : x->ch) flat(c);
+          } else {
+            parts.push_back(walk(x));
+          }
+        };
+        flat(e);
+        for (const auto& x : parts)
+          if (!strcol(x) && !is_string_literal(x))
+            fail(GX_ERR_UNSUPPORTED, "CONCAT of something other than strings");
+        ExprPtr cur;
+        for (size_t k = 0; k < parts.size();) {
+          StringOp op;
+          op.kind = StringOp::CONCAT;
+          std::vector<ExprPtr> group;
+          if (cur) group.push_back(cur);
+          while (k < parts.size() && (int)group.size() < kMaxConcatParts) group.push_back(parts[k++]);
+          for (size_t g = 0; g < group.size(); g++) {
+            const int c = strcol(group[g]) ? group[g]->col : -1;
+            const std::string lit = c < 0 ? unquote(group[g]->token) : std::string();
+            if (g == 0) { op.col = c; op.literal = lit; }
+            else if (g == 1) { op.col2 = c; op.literal2 = lit; }
+            else { op.more_cols.push_back(c); op.more_lits.push_back(lit); }
+          }
+          cur = column_of(op);
         }
-        e = cur;
+        touched = true;
+        return cur;
       }
       for (auto& c : e->ch) c = walk(c);
       const std::string& t = e->token;

@@ -61,6 +61,8 @@ std::string rebuild(const ExprPtr& e);
 // Parse + lower without typing (used by tests of the lowering rules).
 ExprPtr parse_and_lower(const std::string& text);
 
+constexpr int kMaxConcatParts = 8;  // parts one CONCAT operator of the pre-pass joins
+
 // A string operator of the string pre-pass (the operators of
 // evaluate_string_functions, LogicalProject.cpp:103-603, and the
 // interpreter's string comparisons).
@@ -91,10 +93,14 @@ struct StringOp {
   int i0 = 0, i1 = 0, step = 1;
   bool i0_valid = false, i1_valid = false;
   int type = 0;  // PARSE: the result type
+  // CONCAT of more than two parts: parts 3, 4, ... (a column, or -1 and the literal)
+  std::vector<int> more_cols;
+  std::vector<std::string> more_lits;
   bool operator==(const StringOp& o) const {
     return kind == o.kind && col == o.col && literal == o.literal && col2 == o.col2 && cond == o.cond &&
            literal2 == o.literal2 && then_null == o.then_null && else_null == o.else_null && i0 == o.i0 &&
-           i1 == o.i1 && step == o.step && i0_valid == o.i0_valid && i1_valid == o.i1_valid && type == o.type;
+           i1 == o.i1 && step == o.step && i0_valid == o.i0_valid && i1_valid == o.i1_valid && type == o.type &&
+           more_cols == o.more_cols && more_lits == o.more_lits;
   }
   int result_type() const {
     switch (kind) {

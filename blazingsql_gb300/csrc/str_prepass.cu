@@ -46,7 +46,12 @@ __device__ bool like_match(const unsigned char* s, int n, const unsigned char* p
   if (lead == m) return true;
   int tail = m;  // pattern positions >= tail are the trailing run of '%'
   while (tail > lead && p[tail - 1] == '%') tail--;
+  const int c0 = p[lead] == '_' ? -1 : p[lead];  // a match starts with this byte, when not -1
   for (int t = 0;; t += utf8_len(s[t])) {
+    if (lead > 0 && c0 >= 0) {  // next start: the next c0
+      while (t < n && s[t] != c0) t++;
+      if (t >= n) return false;
+    }
     int i = t, j = lead, star_j = -1, star_i = 0;
     while (true) {
       if (j >= tail) {
@@ -331,6 +336,8 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_str_write(BuildArgs a) {
 struct XformArgs {
   int kind;  // StringOp::Kind
   BuildSrc a, b;
+  BuildSrc more[kMaxConcatParts - 2];  // CONCAT: parts 3, 4, ...
+  int nmore;
   const void* num;  // TO_STRING: the typed column
   const uint32_t* num_mask;
   int64_t num_off;
@@ -490,7 +497,8 @@ __device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, boo
 // (slices by a positive step, TRIM, CONCAT): the row is n1 bytes at p1, then
 // len - n1 bytes at p2.  Returns len.
 __device__ __forceinline__ bool is_segment_kind(const XformArgs& a) {
-  return (a.kind == StringOp::SLICE && a.step > 0) || a.kind == StringOp::TRIM || a.kind == StringOp::CONCAT;
+  return (a.kind == StringOp::SLICE && a.step > 0) || a.kind == StringOp::TRIM ||
+         (a.kind == StringOp::CONCAT && a.nmore == 0);
 }
 
 __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char*& p1, int& n1,
@@ -559,6 +567,19 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
       put(d, n1, p2, len - n1);
     }
     return len;
+  }
+  if (a.kind == StringOp::CONCAT) {  // more than two parts, NULL if any is
+    int at = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxConcatParts; k++) {  // unrolled: the parts stay in parameter space
+      if (k >= 2 + a.nmore) break;
+      const unsigned char* q;
+      int m;
+      source_row(k == 0 ? a.a : k == 1 ? a.b : a.more[k >= 2 ? k - 2 : 0], o, q, m, valid);
+      if (!valid) return 0;
+      at = put(d, at, q, m);
+    }
+    return at;
   }
   const unsigned char* p;
   int n;
@@ -870,7 +891,8 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
 }
 
 gx_column build_transform(const StringOp& op, const StrSource& a, const StrSource& b, const ColumnView* num,
-                          int64_t rows, cudaStream_t s) {
+                          int64_t rows, cudaStream_t s, const std::vector<StrSource>& more) {
+  if (more.size() > (size_t)(kMaxConcatParts - 2)) fail(GX_ERR_INVALID, "too many CONCAT parts");
   if (rows < 0 || rows > INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string columns hold at most 2^31 - 1 rows");
   const int64_t nblocks = (rows + kBuildRows - 1) / kBuildRows;
   const int64_t words = mask_words_for(rows);
@@ -878,10 +900,14 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
   // [mask | offsets | block sums + total + flags | a, b, literal, literal2]
   const size_t mask_b = al((size_t)words * 4), offs_b = al((size_t)(rows + 1) * 4);
   const size_t sums_b = al((size_t)(nblocks + 2) * 8);
-  std::string lits[4] = {a.kind == StrSource::LITERAL ? a.literal : std::string(),
-                         b.kind == StrSource::LITERAL ? b.literal : std::string(), op.literal, op.literal2};
-  size_t loff[4], lb = 0;
-  for (int i = 0; i < 4; i++) {
+  std::vector<std::string> lits = {a.kind == StrSource::LITERAL ? a.literal : std::string(),
+                                   b.kind == StrSource::LITERAL ? b.literal : std::string(), op.literal,
+                                   op.literal2};
+  for (const auto& x : more) lits.push_back(x.kind == StrSource::LITERAL ? x.literal : std::string());
+  const int nl = (int)lits.size();
+  std::vector<size_t> loff(nl);
+  size_t lb = 0;
+  for (int i = 0; i < nl; i++) {
     loff[i] = lb;
     lb += al(lits[i].size() + 1);
   }
@@ -896,7 +922,7 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     uint64_t* sums = (uint64_t*)(base + mask_b + offs_b);
     unsigned char* ldev = (unsigned char*)(base + mask_b + offs_b + sums_b);
     check_cuda(cudaMemsetAsync(base, 0, mask_b + offs_b + sums_b, s), "string column clear");
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < nl; i++)
       if (!lits[i].empty())
         check_cuda(cudaMemcpyAsync(ldev + loff[i], lits[i].data(), lits[i].size(), cudaMemcpyHostToDevice, s),
                    "string literal");
@@ -904,6 +930,8 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     x.kind = op.kind;
     x.a = device_source(a, ldev + loff[0]);
     x.b = device_source(b, ldev + loff[1]);
+    x.nmore = (int)more.size();
+    for (size_t k = 0; k < more.size(); k++) x.more[k] = device_source(more[k], ldev + loff[4 + k]);
     if (num) {
       x.num = num->data;
       x.num_mask = num->mask;
@@ -1088,7 +1116,7 @@ std::vector<gx_column> run_string_prepass(
               fail(GX_ERR_UNSUPPORTED, "CAST of a floating-point value to VARCHAR");
             if (type_size(v.type) == 0 || v.type >= DURATION_DAYS)
               fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(v.type));
-            out = build_transform(op, StrSource{}, StrSource{}, &v, n, s);
+            out = build_transform(op, StrSource{}, StrSource{}, &v, n, s, {});
           }
         } catch (...) {
           if (tmp.data || tmp.null_mask) free_column(tmp, s);
@@ -1115,9 +1143,21 @@ std::vector<gx_column> run_string_prepass(
             b.literal = op.literal2;
           }
         }
+        std::vector<StrSource> more;
+        for (size_t k = 0; k < op.more_cols.size(); k++) {
+          StrSource x;
+          if (op.more_cols[k] >= 0) {
+            x.kind = StrSource::COLUMN;
+            x.col = string_col(op.more_cols[k]);
+          } else {
+            x.kind = StrSource::LITERAL;
+            x.literal = op.more_lits[k];
+          }
+          more.push_back(x);
+        }
         StringOp xo = op;
         if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
-        out = build_transform(xo, a, b, nullptr, n, s);
+        out = build_transform(xo, a, b, nullptr, n, s, more);
       } else if (op.kind == StringOp::PARSE) {
         const ColumnView c = string_col(op.col);
         out = alloc_column(op.type, n, s);

@@ -322,6 +322,7 @@ FUNCTION_EXPRS = [
     "TRIM(FLAG(BOTH), ' ', $3)", "TRIM(FLAG(LEADING), 'ab', $0)", "TRIM(FLAG(TRAILING), 'é ', $3)",
     "REPLACE($0, 'ab', 'X')", "REPLACE($3, ' ', '')",
     "CONCAT($0, $3)", "||($0, '-')", "CONCAT('<', $0, '|', $3, '>')",
+    "CONCAT(CONCAT($0, 'x'), ||($3, $12), $0)", "CONCAT($0, '1', $3, '2', $12, '3', $0, '4', $3, '5')",
     "CAST($1):VARCHAR", "CAST($4):VARCHAR", "CAST($5):VARCHAR", "CAST($6):VARCHAR", "CAST($7):VARCHAR",
     "CAST($8):VARCHAR", "CAST(+($1, 7)):VARCHAR", "CAST($0):VARCHAR", "CAST(5):VARCHAR",
     "CAST($9):INTEGER", "CAST($9):BIGINT", "CAST($9):TINYINT", "CAST($9):SMALLINT", "CAST($10):DATE",
@@ -394,6 +395,8 @@ def test_string_function_errors():
         g.evaluate_expressions(dev, ["SUBSTRING($0, CAST($1):INTEGER)"])
     with pytest.raises(N.GxError, match="between literals"):
         g.evaluate_expressions(dev, ["CONCAT('a', 'b')"])
+    with pytest.raises(N.GxError, match="between literals"):
+        g.evaluate_expressions(dev, ["CONCAT('a', 'b', $0)"])  # its innermost pair
     with pytest.raises(N.GxError, match="without"):
         g.evaluate_expressions(dev, ["TO_DATE($0, '%Y-%m')"])
     with pytest.raises(N.GxError, match="specifier"):
