@@ -68,13 +68,25 @@ __device__ bool like_match(const unsigned char* s, int n, const unsigned char* p
           continue;
         }
       }
-      // retry from the last inner '%' one character further
-      if (star_j < 0) break;                  // no inner '%' yet: the next start
-      if (star_i >= n) return false;          // ran to the end: no start can match
-      if (s[star_i] == '\n') break;           // an inner '%' stops at a newline
-      star_i += utf8_len(s[star_i]);
+      // retry from the last inner '%' one character further, and on to the
+      // next byte that can continue the match (when a literal follows it)
+      if (star_j < 0) break;  // no inner '%' yet: the next start
+      const int nj = star_j + 1;
+      const int cj = (nj < tail && p[nj] != '_' && p[nj] != '%') ? p[nj] : -1;
+      bool next_start = false;
+      while (true) {
+        if (star_i >= n) return false;  // ran to the end: no start can match
+        if (s[star_i] == '\n') {        // an inner '%' stops at a newline
+          next_start = true;
+          break;
+        }
+        star_i += utf8_len(s[star_i]);
+        if (cj < 0 || star_i >= n || s[star_i] == cj) break;
+      }
+      if (next_start) break;
+      if (star_i >= n && cj >= 0) return false;
       i = star_i;
-      j = star_j + 1;
+      j = nj;
     }
     if (lead == 0 || t >= n) return false;
   }
