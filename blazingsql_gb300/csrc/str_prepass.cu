@@ -19,7 +19,9 @@
 #include "str_prepass.h"
 
 #include <algorithm>
+#include <array>
 #include <cstring>
+#include <map>
 
 namespace gx {
 
@@ -115,12 +117,22 @@ struct StrArgs {
   const unsigned char* pat;
   int plen;
   int op;  // StringOp::Kind
+  // LIKE as a byte automaton (LikeDfa), or null: [byte class 256 | flags S |
+  // transitions S x C], copied to shared memory by each block
+  const unsigned char* dfa;
+  int dfa_states, dfa_classes, dfa_start;
   void* out;
   uint32_t* out_mask;
 };
 
 // one warp per 32 rows: a lane per row, the warp's validity word by ballot
 __global__ void k_string_op(StrArgs a) {
+  extern __shared__ unsigned char s_dfa[];
+  if (a.dfa) {  // uniform over the block
+    const int bytes = 256 + a.dfa_states * (1 + a.dfa_classes);
+    for (int i = threadIdx.x; i < bytes; i += blockDim.x) s_dfa[i] = a.dfa[i];
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31;
   const int64_t nwords = (a.n + 31) / 32;
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; w < nwords;
@@ -148,7 +160,17 @@ __global__ void k_string_op(StrArgs a) {
       } else {
         bool v = false;
         if (valid) {
-          if (a.op == StringOp::LIKE) {
+          if (a.op == StringOp::LIKE && a.dfa) {
+            // a table step per byte, the same instructions in every lane
+            const unsigned char* flags = s_dfa + 256;
+            const unsigned char* tr = flags + a.dfa_states;
+            int st = a.dfa_start;
+            for (int i = 0; i < len; i++) {
+              st = tr[st * a.dfa_classes + s_dfa[s[i]]];
+              if (flags[st] & 2) break;  // absorbing: decided
+            }
+            v = flags[st] & 1;
+          } else if (a.op == StringOp::LIKE) {
             v = like_match(s, len, pat, plen);
           } else {
             const int c = compare_bytes(s, len, pat, plen);
@@ -1029,9 +1051,121 @@ void launch_parse(const ColumnView& col, int type, const std::string& format, gx
   add_launches(1);
 }
 
+// ----------------------------------------------------------- LIKE automaton
+// The LIKE pattern's regular expression (see like_match) as a byte automaton
+// for the search: an NFA over the pattern's middle (between its leading and
+// trailing '%' runs) whose states are (token k, continuation bytes still due
+// for a '_' character), a new start after every byte when the pattern starts
+// with '%', made deterministic by subset construction, with an absorbing
+// accept state when it ends with '%'.  Bytes that behave alike share a class.
+// False (the matcher is used) for a middle over 15 bytes or over 128 states.
+struct LikeDfa {
+  int states = 0, classes = 0, start = 0;
+  std::string blob;  // [class of each byte 256 | flags per state | transitions states x classes]
+};
+
+static int host_utf8_len(unsigned char c) {
+  return c < 0x80 ? 1 : (c >> 5) == 0x6 ? 2 : (c >> 4) == 0xE ? 3 : (c >> 3) == 0x1E ? 4 : 1;
+}
+
+static bool build_like_dfa(const std::string& pat, LikeDfa& d) {
+  const int m = (int)pat.size();
+  int lead = 0;
+  while (lead < m && pat[lead] == '%') lead++;
+  if (lead == m) return false;  // every string matches: the matcher answers at once
+  int tail = m;
+  while (tail > lead && pat[tail - 1] == '%') tail--;
+  const std::string tok = pat.substr(lead, tail - lead);
+  const int M = (int)tok.size();
+  if (M > 15) return false;
+  const bool anchored_start = lead == 0, anchored_end = tail == m;
+  auto bit = [](int k, int c) { return 1ull << (k * 4 + c); };
+  auto closure = [&](uint64_t x) {
+    for (int k = 0; k < M; k++)
+      if ((x & bit(k, 0)) && tok[k] == '%') x |= bit(k + 1, 0);
+    return x;
+  };
+  const uint64_t start = closure(bit(0, 0)), acc = bit(M, 0);
+  const uint64_t kAccept = ~0ull;  // the absorbing accept state of a pattern ending with '%'
+  auto step = [&](uint64_t S, unsigned char b) {
+    uint64_t nx = 0;
+    for (int k = 0; k < M; k++)
+      for (int c = 0; c < 4; c++) {
+        if (!(S & bit(k, c))) continue;
+        if (c > 0) {  // inside a '_' character
+          if ((b & 0xC0) == 0x80) nx |= c > 1 ? bit(k, c - 1) : bit(k + 1, 0);
+          continue;
+        }
+        const unsigned char t = (unsigned char)tok[k];
+        if (t == '%') {
+          if (b != '\n') nx |= bit(k, 0);
+        } else if (t == '_') {
+          if (b == '\n' || (b & 0xC0) == 0x80) continue;
+          const int L = host_utf8_len(b);
+          nx |= L == 1 ? bit(k + 1, 0) : bit(k, L - 1);
+        } else if (b == t) {
+          nx |= bit(k + 1, 0);
+        }
+      }
+    nx = closure(nx);
+    if (!anchored_start) nx |= start;
+    return nx;
+  };
+  std::map<uint64_t, int> id;
+  std::vector<uint64_t> sets;
+  auto sid = [&](uint64_t S) {
+    if (!anchored_end && (S & acc)) S = kAccept;
+    auto it = id.find(S);
+    if (it != id.end()) return it->second;
+    id[S] = (int)sets.size();
+    sets.push_back(S);
+    return (int)sets.size() - 1;
+  };
+  d.start = sid(start);
+  std::vector<std::array<int, 256>> tr;
+  for (size_t i = 0; i < sets.size(); i++) {
+    if (sets.size() > 128) return false;
+    std::array<int, 256> row{};
+    for (int b = 0; b < 256; b++) row[b] = sets[i] == kAccept ? (int)i : sid(step(sets[i], (unsigned char)b));
+    tr.push_back(row);
+  }
+  if (sets.size() > 128) return false;
+  d.states = (int)sets.size();
+  // byte classes: bytes whose transitions agree in every state
+  std::map<std::vector<int>, int> cls_of;
+  std::vector<int> cls(256);
+  for (int b = 0; b < 256; b++) {
+    std::vector<int> col(d.states);
+    for (int i = 0; i < d.states; i++) col[i] = tr[i][b];
+    auto it = cls_of.find(col);
+    if (it == cls_of.end()) it = cls_of.emplace(col, (int)cls_of.size()).first;
+    cls[b] = it->second;
+  }
+  d.classes = (int)cls_of.size();
+  d.blob.assign(256 + d.states * (1 + d.classes), '\0');
+  for (int b = 0; b < 256; b++) d.blob[b] = (char)cls[b];
+  for (int i = 0; i < d.states; i++) {
+    const uint64_t S = sets[i];
+    const bool accept = S == kAccept || (S & acc);
+    const bool absorbing = S == kAccept || (S == 0 && anchored_start);
+    d.blob[256 + i] = (char)((accept ? 1 : 0) | (absorbing ? 2 : 0));
+  }
+  for (int b = 0; b < 256; b++)
+    for (int i = 0; i < d.states; i++) d.blob[256 + d.states + i * d.classes + cls[b]] = (char)tr[i][b];
+  return true;
+}
+
 void launch_string_op(const ColumnView& col, const ColumnView* col2, const StringOp& op, const void* pattern_dev,
-                      gx_column& out, cudaStream_t s) {
+                      gx_column& out, cudaStream_t s, const LikeDfa* dfa) {
   StrArgs a{};
+  size_t smem = 0;
+  if (dfa) {  // pattern_dev holds the automaton
+    a.dfa = (const unsigned char*)pattern_dev;
+    a.dfa_states = dfa->states;
+    a.dfa_classes = dfa->classes;
+    a.dfa_start = dfa->start;
+    smem = dfa->blob.size();
+  }
   a.offs = col.str_offsets;
   a.chars = (const unsigned char*)col.data;
   a.off = col.offset;
@@ -1051,7 +1185,7 @@ void launch_string_op(const ColumnView& col, const ColumnView* col2, const Strin
   if (a.n == 0) return;
   const int64_t warps = (a.n + 31) / 32;
   const int grid = (int)std::min<int64_t>((warps + 7) / 8, 152 * 32);
-  k_string_op<<<grid, 256, 0, s>>>(a);
+  k_string_op<<<grid, 256, smem, s>>>(a);
   check_cuda(cudaGetLastError(), "k_string_op");
   add_launches(1);
 }
@@ -1062,17 +1196,25 @@ std::vector<gx_column> run_string_prepass(
   std::vector<gx_column> made;
   if (ops.empty()) return made;
   const int64_t n = cols.empty() ? 0 : cols[0].size;
+  // each operator's device bytes: its literal, or a LIKE pattern's automaton
+  std::vector<LikeDfa> dfas(ops.size());
+  std::vector<const std::string*> bytes(ops.size());
+  for (size_t i = 0; i < ops.size(); i++) {
+    bytes[i] = &ops[i].literal;
+    if (ops[i].kind == StringOp::LIKE && ops[i].col2 < 0 && build_like_dfa(ops[i].literal, dfas[i]))
+      bytes[i] = &dfas[i].blob;
+  }
   size_t pbytes = 0;
-  // a 16-byte aligned slot of 16 bytes or more per literal
+  // a 16-byte aligned slot of 16 bytes or more per operator
   auto slot = [](size_t len) { return (std::max<size_t>(len, 1) + 15) / 16 * 16; };
-  for (const auto& op : ops) pbytes += slot(op.literal.size());
+  for (const auto* b : bytes) pbytes += slot(b->size());
   std::string host(std::max<size_t>(pbytes, 16), '\0');
   std::vector<size_t> poff;
   size_t at = 0;
-  for (const auto& op : ops) {
+  for (const auto* b : bytes) {
     poff.push_back(at);
-    std::memcpy(&host[at], op.literal.data(), op.literal.size());
-    at += slot(op.literal.size());
+    std::memcpy(&host[at], b->data(), b->size());
+    at += slot(b->size());
   }
   char* pdev = (char*)dev_alloc(host.size(), s);
   auto string_col = [&](int c) {
@@ -1179,7 +1321,8 @@ std::vector<gx_column> run_string_prepass(
         ColumnView c2{};
         if (op.col2 >= 0) c2 = string_col(op.col2);
         out = alloc_column(op.result_type(), n, s);
-        launch_string_op(c, op.col2 >= 0 ? &c2 : nullptr, op, pdev + poff[i], out, s);
+        launch_string_op(c, op.col2 >= 0 ? &c2 : nullptr, op, pdev + poff[i], out, s,
+                         dfas[i].states ? &dfas[i] : nullptr);
       }
       made.push_back(out);
       cols.push_back(ColumnView{out.type_id, out.data, out.null_mask, 0, n, out.string_offsets});

@@ -14,11 +14,14 @@
 
 namespace gx {
 
+struct LikeDfa;
+
 // one operator over string column `op.col` (and `col2`, the right-hand column
 // of a comparison of two columns, or null), writing `out` (library column of
-// col.size rows: BOOL8, INT32 for CHAR_LENGTH); pattern_dev holds op.literal
+// col.size rows: BOOL8, INT32 for CHAR_LENGTH); pattern_dev holds op.literal,
+// or for a LIKE with an automaton (dfa) the automaton's bytes
 void launch_string_op(const ColumnView& col, const ColumnView* col2, const StringOp& op, const void* pattern_dev,
-                      gx_column& out, cudaStream_t s);
+                      gx_column& out, cudaStream_t s, const LikeDfa* dfa = nullptr);
 
 // Where the rows of a string column being built come from: a string column
 // (`col`), a literal (`literal`, host bytes that build_strings copies to the

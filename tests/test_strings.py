@@ -74,7 +74,9 @@ def test_like_exhaustive_small_cases():
     from blazingsql_gb300.api import DeviceColumn
     strs = [""] + ["".join(t) for k in range(1, 6) for t in itertools.product("ab\n", repeat=k)]
     pats = ["%a%a", "%b%_", "%%_%_", "%_%__", "%%b%a", "%a%_", "%_%a", "%_%b%", "a%b", "%a_b%", "_%", "%_",
-            "a%", "%ab", "%a%b%a%", "__", "%b", "b%a%", "%", ""]
+            "a%", "%ab", "%a%b%a%", "__", "%b", "b%a%", "%", "",
+            # middles over 15 bytes: the backtracking matcher instead of the automaton
+            "%a%b%a%b%_%b%a%b%a", "a%a%a%a%a%a%a%a%a%", "%_%_%_%_%_%_%_%_%"]
     exprs = [f"LIKE($0, '{p}')" for p in pats]
     got = g.evaluate_expressions([DeviceColumn.from_strings(strs)], exprs)
     exp = strings_ref.evaluate_expressions([None], {0: strs}, exprs)
