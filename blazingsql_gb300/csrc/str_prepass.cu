@@ -555,6 +555,21 @@ __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char
     return n + m;
   }
   if (!valid) return 0;
+  if (a.kind == StringOp::SLICE && a.i0v && a.i1v && a.i0 >= 0 && a.i1 >= 0) {
+    // [i0, i1) from the front (SUBSTRING with a length, LEFT): walk at most i1
+    // characters; the same clipping as below, without counting the rest
+    int i = 0, c = 0, bb = 0;
+    while (i < n && c < a.i1) {
+      if (c == a.i0) bb = i;
+      i += utf8_len(p[i]);
+      c++;
+    }
+    if (a.i0 >= c) return 0;  // begins at or after the end
+    i = min(i, n);
+    p1 = p + bb;
+    n1 = i - bb;
+    return n1;
+  }
   if (a.kind == StringOp::SLICE) {  // cudf::strings::slice_strings, characters [begin, end)
     int L = 0;
     for (int i = 0; i < n; i++) L += (p[i] & 0xC0) != 0x80;
