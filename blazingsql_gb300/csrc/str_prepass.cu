@@ -430,17 +430,18 @@ __device__ bool in_set(const unsigned char* s, int i, int k, const unsigned char
   return false;
 }
 
-__device__ int civil_digits(unsigned char* d, int at, int64_t v, int width) {
-  unsigned char buf[24];
-  int n = 0;
+// the decimal digits of v (as unsigned), zero-padded to `width`, at d + at;
+// counted first, then written from the last digit (no buffer)
+__device__ __forceinline__ int civil_digits(unsigned char* d, int at, int64_t v, int width) {
   uint64_t u = (uint64_t)v;
-  do {
-    buf[n++] = (unsigned char)('0' + u % 10);
-    u /= 10;
-  } while (u);
-  while (n < width) buf[n++] = '0';
+  int n = 1;
+  for (uint64_t t = u; t >= 10; t /= 10) n++;
+  if (n < width) n = width;
   if (d)
-    for (int i = 0; i < n; i++) d[at + i] = buf[n - 1 - i];
+    for (int i = n - 1; i >= 0; i--) {
+      d[at + i] = (unsigned char)('0' + u % 10);
+      u /= 10;
+    }
   return at + n;
 }
 
