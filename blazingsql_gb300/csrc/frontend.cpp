@@ -1216,19 +1216,29 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
         // concatenation of all parts, NULL if any is: nested CONCATs are
         // flattened into parts, up to kMaxConcatParts per operator.  Its
         // innermost pair of literals is still refused (:311).
+        // a part CAST($k):VARCHAR of a typed column stays that column: the
+        // CONCAT formats it in place (the pre-pass would format it into a
+        // string column first)
         std::vector<ExprPtr> parts;
+        std::vector<bool> formatted;
         std::function<void(const ExprPtr&)> flat = [&](const ExprPtr& x) {
           if (x->kind == Expr::OP && (x->token == "CONCAT" || x->token == "||") && x->ch.size() >= 2) {
             if (is_string_literal(x->ch[0]) && is_string_literal(x->ch[1]))
               fail(GX_ERR_UNSUPPORTED, "CONCAT operator between literals is not supported");
             for (const auto& c : x->ch) flat(c);
+          } else if (x->kind == Expr::OP && (x->token == "CAST_VARCHAR" || x->token == "CAST_CHAR") &&
+                     x->ch.size() == 1 && x->ch[0]->kind == Expr::COL && x->ch[0]->col >= 0 &&
+                     x->ch[0]->col < (int)types.size() && types[x->ch[0]->col] != STRING) {
+            parts.push_back(x->ch[0]);
+            formatted.push_back(true);
           } else {
             parts.push_back(walk(x));
+            formatted.push_back(false);
           }
         };
         flat(e);
-        for (const auto& x : parts)
-          if (!strcol(x) && !is_string_literal(x))
+        for (size_t k = 0; k < parts.size(); k++)
+          if (!formatted[k] && !strcol(parts[k]) && !is_string_literal(parts[k]))
             fail(GX_ERR_UNSUPPORTED, "CONCAT of something other than strings");
         ExprPtr cur;
         for (size_t k = 0; k < parts.size();) {
@@ -1238,7 +1248,7 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
           if (cur) group.push_back(cur);
           while (k < parts.size() && (int)group.size() < kMaxConcatParts) group.push_back(parts[k++]);
           for (size_t g = 0; g < group.size(); g++) {
-            const int c = strcol(group[g]) ? group[g]->col : -1;
+            const int c = group[g]->kind == Expr::COL ? group[g]->col : -1;
             const std::string lit = c < 0 ? unquote(group[g]->token) : std::string();
             if (g == 0) { op.col = c; op.literal = lit; }
             else if (g == 1) { op.col2 = c; op.literal2 = lit; }

@@ -207,6 +207,8 @@ struct BuildSrc {
   const uint32_t* mask;
   int64_t off;
   int64_t end;  // the view's row end (off + size): its characters end at offs[end]
+  const void* num;  // FORMAT: the typed column's data (mask, off as above)
+  int32_t num_type;
   const unsigned char* lit;
   int32_t lit_len;
   int32_t kind;  // StrSource::Kind
@@ -466,20 +468,21 @@ __device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {
 }
 
 // formats row o of the typed column (cast_to_str_functor, LogicalProject.cpp:62-92)
-__device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
-  const int64_t q = a.num_off + o;
-  valid = bit_of(a.num_mask, q);
+__device__ int format_typed(const void* num, const uint32_t* mask, int64_t off, int type, int64_t o,
+                             unsigned char* d, bool& valid) {
+  const int64_t q = off + o;
+  valid = bit_of(mask, q);
   if (!valid) return 0;
   int at = 0;
-  switch (a.num_type) {
+  switch (type) {
     case BOOL8: {  // cudf::strings::from_booleans: "true" / "false"
-      const bool v = ((const uint8_t*)a.num)[q] != 0;
+      const bool v = ((const uint8_t*)num)[q] != 0;
       const unsigned char* t = (const unsigned char*)(v ? "true" : "false");
       return put(d, 0, t, v ? 4 : 5);
     }
     case INT8: case INT16: case INT32: case INT64: {  // cudf::strings::from_integers
-      int64_t v = a.num_type == INT8 ? ((const int8_t*)a.num)[q] : a.num_type == INT16 ? ((const int16_t*)a.num)[q]
-                : a.num_type == INT32 ? ((const int32_t*)a.num)[q] : ((const int64_t*)a.num)[q];
+      int64_t v = type == INT8 ? ((const int8_t*)num)[q] : type == INT16 ? ((const int16_t*)num)[q]
+                : type == INT32 ? ((const int32_t*)num)[q] : ((const int64_t*)num)[q];
       uint64_t u = (uint64_t)v;
       if (v < 0) {
         if (d) d[at] = '-';
@@ -489,21 +492,21 @@ __device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, boo
       return civil_digits(d, at, (int64_t)u, 1);
     }
     case UINT8: case UINT16: case UINT32: case UINT64: {
-      const uint64_t u = a.num_type == UINT8 ? ((const uint8_t*)a.num)[q] : a.num_type == UINT16
-                       ? ((const uint16_t*)a.num)[q] : a.num_type == UINT32 ? ((const uint32_t*)a.num)[q]
-                       : ((const uint64_t*)a.num)[q];
+      const uint64_t u = type == UINT8 ? ((const uint8_t*)num)[q] : type == UINT16
+                       ? ((const uint16_t*)num)[q] : type == UINT32 ? ((const uint32_t*)num)[q]
+                       : ((const uint64_t*)num)[q];
       return civil_digits(d, 0, (int64_t)u, 1);
     }
     default: break;
   }
   // timestamps: "%Y-%m-%d" for days, "%Y-%m-%d %H:%M:%S" otherwise
   int64_t days, sod = 0;
-  if (a.num_type == TIMESTAMP_DAYS) {
-    days = ((const int32_t*)a.num)[q];
+  if (type == TIMESTAMP_DAYS) {
+    days = ((const int32_t*)num)[q];
   } else {
-    const int64_t v = ((const int64_t*)a.num)[q];
-    const int64_t per = a.num_type == TIMESTAMP_SECONDS ? 1 : a.num_type == TIMESTAMP_MILLISECONDS ? 1000
-                      : a.num_type == TIMESTAMP_MICROSECONDS ? 1000000 : 1000000000;
+    const int64_t v = ((const int64_t*)num)[q];
+    const int64_t per = type == TIMESTAMP_SECONDS ? 1 : type == TIMESTAMP_MILLISECONDS ? 1000
+                      : type == TIMESTAMP_MICROSECONDS ? 1000000 : 1000000000;
     const int64_t secs = floor_div(v, per);
     days = floor_div(secs, 86400);
     sod = secs - days * 86400;
@@ -517,7 +520,7 @@ __device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, boo
   at = civil_digits(d, at, m, 2);
   at = put(d, at, &dash, 1);
   at = civil_digits(d, at, dd, 2);
-  if (a.num_type != TIMESTAMP_DAYS) {
+  if (type != TIMESTAMP_DAYS) {
     at = put(d, at, &space, 1);
     at = civil_digits(d, at, sod / 3600, 2);
     at = put(d, at, &colon, 1);
@@ -528,12 +531,17 @@ __device__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, boo
   return at;
 }
 
+__device__ __forceinline__ int format_value(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
+  return format_typed(a.num, a.num_mask, a.num_off, a.num_type, o, d, valid);
+}
+
 // The functions whose result is one or two byte ranges of their inputs
 // (slices by a positive step, TRIM, CONCAT): the row is n1 bytes at p1, then
 // len - n1 bytes at p2.  Returns len.
 __device__ __forceinline__ bool is_segment_kind(const XformArgs& a) {
   return (a.kind == StringOp::SLICE && a.step > 0) || a.kind == StringOp::TRIM ||
-         (a.kind == StringOp::CONCAT && a.nmore == 0);
+         (a.kind == StringOp::CONCAT && a.nmore == 0 && a.a.kind != StrSource::FORMAT &&
+          a.b.kind != StrSource::FORMAT);
 }
 
 __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char*& p1, int& n1,
@@ -618,14 +626,20 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
     }
     return len;
   }
-  if (a.kind == StringOp::CONCAT) {  // more than two parts, NULL if any is
+  if (a.kind == StringOp::CONCAT) {  // more than two parts or a formatted part, NULL if any is
     int at = 0;
 #pragma unroll
     for (int k = 0; k < kMaxConcatParts; k++) {  // unrolled: the parts stay in parameter space
       if (k >= 2 + a.nmore) break;
+      const BuildSrc& ps = k == 0 ? a.a : k == 1 ? a.b : a.more[k >= 2 ? k - 2 : 0];
+      if (ps.kind == StrSource::FORMAT) {  // CAST(column):VARCHAR in place
+        at += format_typed(ps.num, ps.mask, ps.off, ps.num_type, o, d ? d + at : nullptr, valid);
+        if (!valid) return 0;
+        continue;
+      }
       const unsigned char* q;
       int m;
-      source_row(k == 0 ? a.a : k == 1 ? a.b : a.more[k >= 2 ? k - 2 : 0], o, q, m, valid);
+      source_row(ps, o, q, m, valid);
       if (!valid) return 0;
       at = put(d, at, q, m);
     }
@@ -864,6 +878,15 @@ BuildSrc device_source(const StrSource& s, const unsigned char* lit_dev) {
   } else if (s.kind == StrSource::LITERAL) {
     b.lit = lit_dev;
     b.lit_len = (int32_t)s.literal.size();
+  } else if (s.kind == StrSource::FORMAT) {
+    if (s.col.type == FLOAT32 || s.col.type == FLOAT64)
+      fail(GX_ERR_UNSUPPORTED, "CAST of a floating-point value to VARCHAR");
+    if (s.col.type == STRING || type_size(s.col.type) == 0 || s.col.type >= DURATION_DAYS)
+      fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(s.col.type));
+    b.num = s.col.data;
+    b.mask = s.col.mask;
+    b.off = s.col.offset;
+    b.num_type = s.col.type;
   }
   return b;
 }
@@ -1296,35 +1319,25 @@ std::vector<gx_column> run_string_prepass(
       } else if (op.kind == StringOp::SLICE || op.kind == StringOp::UPPER || op.kind == StringOp::LOWER ||
                  op.kind == StringOp::INITCAP || op.kind == StringOp::TRIM || op.kind == StringOp::REPLACE ||
                  op.kind == StringOp::CONCAT) {
-        StrSource a, b;
-        if (op.col >= 0) {
-          a.kind = StrSource::COLUMN;
-          a.col = string_col(op.col);
-        } else {
-          a.kind = StrSource::LITERAL;
-          a.literal = op.literal;
-        }
-        if (op.kind == StringOp::CONCAT) {
-          if (op.col2 >= 0) {
-            b.kind = StrSource::COLUMN;
-            b.col = string_col(op.col2);
-          } else {
-            b.kind = StrSource::LITERAL;
-            b.literal = op.literal2;
-          }
-        }
-        std::vector<StrSource> more;
-        for (size_t k = 0; k < op.more_cols.size(); k++) {
+        // a part: a string column, a literal, or (CONCAT) a typed column to format
+        auto part = [&](int c, const std::string& lit) {
           StrSource x;
-          if (op.more_cols[k] >= 0) {
-            x.kind = StrSource::COLUMN;
-            x.col = string_col(op.more_cols[k]);
-          } else {
+          if (c < 0) {
             x.kind = StrSource::LITERAL;
-            x.literal = op.more_lits[k];
+            x.literal = lit;
+          } else if (op.kind == StringOp::CONCAT && cols.at(c).type != STRING) {
+            x.kind = StrSource::FORMAT;
+            x.col = cols.at(c);
+          } else {
+            x.kind = StrSource::COLUMN;
+            x.col = string_col(c);
           }
-          more.push_back(x);
-        }
+          return x;
+        };
+        StrSource a = part(op.col, op.literal), b;
+        if (op.kind == StringOp::CONCAT) b = part(op.col2, op.literal2);
+        std::vector<StrSource> more;
+        for (size_t k = 0; k < op.more_cols.size(); k++) more.push_back(part(op.more_cols[k], op.more_lits[k]));
         StringOp xo = op;
         if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
         out = build_transform(xo, a, b, nullptr, n, s, more);

@@ -25,9 +25,10 @@ void launch_string_op(const ColumnView& col, const ColumnView* col2, const Strin
 
 // Where the rows of a string column being built come from: a string column
 // (`col`), a literal (`literal`, host bytes that build_strings copies to the
-// device) or NULL.
+// device), NULL, or (a CONCAT part) a typed column `col` formatted as CAST to
+// VARCHAR formats it.
 struct StrSource {
-  enum Kind { COLUMN = 0, LITERAL = 1, NUL = 2 } kind = NUL;
+  enum Kind { COLUMN = 0, LITERAL = 1, NUL = 2, FORMAT = 3 } kind = NUL;
   ColumnView col{};
   std::string literal;
 };

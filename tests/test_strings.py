@@ -325,6 +325,7 @@ FUNCTION_EXPRS = [
     "REPLACE($0, 'ab', 'X')", "REPLACE($3, ' ', '')",
     "CONCAT($0, $3)", "||($0, '-')", "CONCAT('<', $0, '|', $3, '>')",
     "CONCAT(CONCAT($0, 'x'), ||($3, $12), $0)", "CONCAT($0, '1', $3, '2', $12, '3', $0, '4', $3, '5')",
+    "CONCAT($0, '#', CAST($5):VARCHAR, CAST($6):VARCHAR, CAST($4):VARCHAR)", "||(CAST($1):VARCHAR, $3)",
     "CAST($1):VARCHAR", "CAST($4):VARCHAR", "CAST($5):VARCHAR", "CAST($6):VARCHAR", "CAST($7):VARCHAR",
     "CAST($8):VARCHAR", "CAST(+($1, 7)):VARCHAR", "CAST($0):VARCHAR", "CAST(5):VARCHAR",
     "CAST($9):INTEGER", "CAST($9):BIGINT", "CAST($9):TINYINT", "CAST($9):SMALLINT", "CAST($10):DATE",
