@@ -1540,11 +1540,13 @@ std::vector<int> conjunct_columns(const Plan& p, int c) {
 // Add, subtract and multiply cost about as much natively (one FP64-pipe
 // instruction, at 1/64 of the FP32 rate) as emulated (about 25 integer
 // instructions), so moving them to the otherwise idle FP64 pipe frees the
-// integer pipes.  Conversions and compares follow when the plan has no
-// transcendental (LN / EXP / trigonometric / POWER / ROUND, which already
-// load the FP64 pipe).  Division stays emulated: natively it is a reciprocal
-// and Newton steps, several FP64-pipe instructions.  Measured on GB300:
-// 19 % on the deep plan (with LN / EXP), 10 % on the plain filter + divide.
+// integer pipes.  Integer-to-double conversions go there too.  Compares go
+// there only when the plan has no transcendental (LN / EXP / trigonometric /
+// POWER / ROUND, which already load the FP64 pipe): with one they cost more
+// time there than they free.  Division stays emulated: natively it is a
+// reciprocal and Newton steps, several FP64-pipe instructions.  Measured on
+// GB300 against all-emulated: 25 % on the deep plan (with LN / EXP; the
+// conversions are 6.5 % of it), 10 % on the plain filter + divide.
 int auto_native_f64_ops(const Plan& p) {
   bool transcendental = false;
   for (const auto& n : p.nodes)
@@ -1555,7 +1557,7 @@ int auto_native_f64_ops(const Plan& p) {
           break;
         default: break;
       }
-  return transcendental ? (kNativeAddSub | kNativeMul)
+  return transcendental ? (kNativeAddSub | kNativeMul | kNativeConvert)
                         : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare);
 }
 
