@@ -109,6 +109,7 @@ def lib():
     L.gx_free_columns.restype = None
     L.gx_column_to_host.argtypes = [P(Column), C.c_void_p, C.c_void_p, C.c_void_p, P(StatusInfo)]
     L.gx_string_offsets_to_host.argtypes = [P(Column), C.c_void_p, C.c_void_p, P(StatusInfo)]
+    L.gx_debug_like_automaton.argtypes = [C.c_char_p, C.c_char_p, C.c_int64, P(C.c_int32), P(StatusInfo)]
     L.gx_plan_options_init.argtypes = [P(PlanOptions)]
     L.gx_plan_options_init.restype = None
     L.gx_plan_compile.argtypes = [P(C.c_int32), P(C.c_uint8), C.c_int, C.c_char_p, P(C.c_char_p), C.c_int,
@@ -187,7 +188,7 @@ def check(rc: int, st: StatusInfo) -> None:
 # every symbol declared in include/gx_eval.h
 EXPORTED_SYMBOLS = [
     "gx_evaluate_expressions", "gx_process_project", "gx_process_filter", "gx_filter_project", "gx_free_columns",
-    "gx_column_to_host", "gx_string_offsets_to_host", "gx_plan_options_init", "gx_plan_compile", "gx_plan_num_outputs", "gx_plan_output_type",
+    "gx_column_to_host", "gx_string_offsets_to_host", "gx_debug_like_automaton", "gx_plan_options_init", "gx_plan_compile", "gx_plan_num_outputs", "gx_plan_output_type",
     "gx_plan_num_conjuncts", "gx_plan_execute", "gx_plan_execute_noalloc", "gx_plan_destroy", "gx_version",
     "gx_debug_kernel_source",
     "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_jit_stats", "gx_debug_rebuild_expression",

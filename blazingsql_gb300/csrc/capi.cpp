@@ -626,6 +626,14 @@ int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_m
   });
 }
 
+int gx_debug_like_automaton(const char* pattern, const char* text, int64_t text_len, int32_t* result,
+                            gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!pattern || (!text && text_len > 0) || text_len < 0 || !result) fail(GX_ERR_INVALID, "bad arguments");
+    *result = like_dfa_host_match(pattern, (const unsigned char*)text, text_len);
+  });
+}
+
 int gx_string_offsets_to_host(const gx_column* column, int32_t* host_offsets, void* stream,
                               gx_status_info* status) {
   return guarded(status, [&] {

@@ -1194,6 +1194,21 @@ static bool build_like_dfa(const std::string& pat, LikeDfa& d) {
   return true;
 }
 
+int like_dfa_host_match(const std::string& pattern, const unsigned char* text, int64_t n) {
+  LikeDfa d;
+  if (!build_like_dfa(pattern, d)) return -1;
+  // the same walk as k_string_op's
+  const unsigned char* cls = (const unsigned char*)d.blob.data();
+  const unsigned char* flags = cls + 256;
+  const unsigned char* tr = flags + d.states;
+  int st = d.start;
+  for (int64_t i = 0; i < n; i++) {
+    st = tr[st * d.classes + cls[text[i]]];
+    if (flags[st] & 2) break;
+  }
+  return flags[st] & 1;
+}
+
 void launch_string_op(const ColumnView& col, const ColumnView* col2, const StringOp& op, const void* pattern_dev,
                       gx_column& out, cudaStream_t s, const LikeDfa* dfa) {
   StrArgs a{};

@@ -16,6 +16,11 @@ namespace gx {
 
 struct LikeDfa;
 
+// LIKE of `text` through the pattern's byte automaton, run on the host as the
+// kernel runs it: 1 match, 0 no match, -1 when the pattern is left to the
+// backtracking matcher (no automaton)
+int like_dfa_host_match(const std::string& pattern, const unsigned char* text, int64_t n);
+
 // one operator over string column `op.col` (and `col2`, the right-hand column
 // of a comparison of two columns, or null), writing `out` (library column of
 // col.size rows: BOOL8, INT32 for CHAR_LENGTH); pattern_dev holds op.literal,

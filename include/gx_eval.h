@@ -133,6 +133,13 @@ void gx_free_columns(gx_column* columns, int num_columns, void* stream);
 int gx_column_to_host(const gx_column* column, void* host_data, uint32_t* host_mask,
                       void* stream, gx_status_info* status);
 
+/* LIKE(text, 'pattern') through the byte automaton the string pre-pass
+ * builds for the pattern, evaluated on the host exactly as the kernel walks it
+ * (no GPU needed): *result = 1 match, 0 no match, -1 when the pattern runs on
+ * the backtracking matcher instead. */
+int gx_debug_like_automaton(const char* pattern, const char* text, int64_t text_len, int32_t* result,
+                            gx_status_info* status);
+
 /* The size + 1 offsets of a GX_TYPE_STRING column, to host memory. */
 int gx_string_offsets_to_host(const gx_column* column, int32_t* host_offsets, void* stream,
                               gx_status_info* status);

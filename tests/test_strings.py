@@ -83,6 +83,33 @@ def test_like_exhaustive_small_cases():
     _compare(got, exp, "LIKE small cases")
 
 
+def test_like_automaton_host_matches_regex():
+    """The byte automaton built for a LIKE pattern, walked on the host as the
+    kernel walks it, against the reference's regular expression on random
+    strings and patterns (newlines, multi-byte characters, '%' and '_')."""
+    import ctypes as C
+    import random
+    from blazingsql_gb300 import _native as N
+    lib = N.lib()
+    rnd = random.Random(7)
+    res, st = C.c_int32(), N.StatusInfo()
+    checked = 0
+    for _ in range(100_000):
+        s = "".join(rnd.choice(["a", "b", "c", "\n", "é", "ß"]) for _ in range(rnd.randint(0, 10)))
+        p = "".join(rnd.choice(["a", "b", "%", "_", "é"]) for _ in range(rnd.randint(0, 7)))
+        b = s.encode()
+        N.check(lib.gx_debug_like_automaton(p.encode(), b, len(b), C.byref(res), C.byref(st)), st)
+        if res.value < 0:
+            continue
+        exp = re.search(strings_ref._py_regex(strings_ref.like_to_regex(p)), s) is not None
+        assert bool(res.value) == exp, (s, p)
+        checked += 1
+    assert checked > 80_000  # the rest: empty or all-% patterns, which every string matches
+    # a middle over 15 bytes is left to the backtracking matcher
+    N.check(lib.gx_debug_like_automaton(b"%abcdefghijklmnopq%", b"x", 1, C.byref(res), C.byref(st)), st)
+    assert res.value == -1
+
+
 @pytest.mark.gpu
 def test_filter_with_like_matches_oracle():
     import blazingsql_gb300 as g
