@@ -59,6 +59,10 @@ KernelConfig default_config() {
   c.dense = env_int("GX_DENSE", 1) != 0;
   c.lazy_case = env_int("GX_LAZY_CASE", 1) != 0;
   c.max_regs = env_int("GX_MAX_REGS", 0);
+  c.use_tma = env_int("GX_TMA", 0);  // opt-in until it beats the direct-load kernel
+  c.tma_warps = env_int("GX_TMA_WARPS", c.tma_warps);
+  c.tma_words = env_int("GX_TMA_WORDS", c.tma_words);
+  c.stages = env_int("GX_TMA_STAGES", c.stages);
   return c;
 }
 
@@ -168,7 +172,8 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
   }
   k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
        std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case) + ':' +
-       std::to_string(cfg.native_f64_ops) + ':' + std::to_string(cfg.max_regs);
+       std::to_string(cfg.native_f64_ops) + ':' + std::to_string(cfg.max_regs) + ':' + std::to_string(cfg.use_tma) +
+       ':' + std::to_string(cfg.tma_warps) + 'x' + std::to_string(cfg.tma_words) + 'x' + std::to_string(cfg.stages);
   return k;
 }
 
@@ -669,6 +674,7 @@ gx_plan* gx_plan_compile(const int32_t* column_types, const uint8_t* column_null
     if (o.words_per_warp > 0) cfg.words = o.words_per_warp;
     if (o.block_threads > 0 || o.words_per_warp > 0) cfg.tune_shape = false;
     cfg.short_circuit = o.short_circuit != 0;
+    if (o.use_tma == 0 || o.use_tma == 1) cfg.use_tma = o.use_tma;
     for (int i = 0; i < o.num_conjuncts && i < 16; i++) {
       if (o.conjunct_order[i] < 0 || o.conjunct_order[i] >= 16) fail(GX_ERR_INVALID, "conjunct order index out of range");
       cfg.conjunct_order.push_back(o.conjunct_order[i]);
@@ -735,7 +741,8 @@ static KernelKind kind_of(int k) {
     case 3: return KernelKind::WRITE_FILTER;
     case 6: return KernelKind::FUSED_BATCHED;
     case 7: return KernelKind::FUSED_STAGED;
-    default: fail(GX_ERR_INVALID, "kernel kind must be 0..7");
+    case 8: return KernelKind::FUSED_TMA;
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..8");
   }
 }
 
@@ -757,6 +764,10 @@ static std::string debug_source(const gx_plan* plan, int kind, const uint8_t* ha
     }
     cfg.conj_stats = kind == 5;
     if (kind == 4 || kind == 7) cfg.dense = true;
+  }
+  if (kind == 8) {  // the tile-staged kernel at the plan's configured shape
+    cfg.warps = cfg.tma_warps;
+    cfg.words = cfg.tma_words;
   }
   return generate_kernel(p, kind_of(kind), cfg, "gx_kernel");
 }

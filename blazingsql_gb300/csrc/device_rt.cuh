@@ -170,6 +170,88 @@ __device__ __forceinline__ void gx_cp_arrive(u64* bar) {
 // later bulk copies into it
 __device__ __forceinline__ void gx_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// bounded wait for the phase of the given parity: each mbarrier.try_wait
+// suspends the thread for at most about a microsecond (its time hint) unless
+// the phase completes first; false once `max_polls` of them have failed (about
+// max_polls microseconds) -- the caller then records an error instead of
+// waiting forever
+__device__ __forceinline__ bool gx_mbar_wait(u64* bar, u32 parity, u32 max_polls) {
+  for (u32 i = 0; i < max_polls; i++) {
+    u32 ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(gx_saddr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// one plain arrival on an mbarrier (release)
+__device__ __forceinline__ void gx_mbar_arrive(u64* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(gx_saddr(bar)) : "memory");
+}
+
+// Named barrier 1 over `nthreads` threads (whole warps) that also ANDs a
+// predicate over them: the consumer warps of the tile-staged kernels meet
+// here without the producer and resolver warps.
+__device__ __forceinline__ bool gx_bar_and(bool v, u32 nthreads) {
+  u32 r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((u32)v), "r"(nthreads)
+      : "memory");
+  return r != 0u;
+}
+
+// ---- tile staging: the dynamic shared memory of the tile-staged kernels -----
+// A tile's rows of every column a plan reads are copied here by bulk copies
+// (one per column and tile); the kernels read them back by byte offset.
+extern __shared__ __align__(128) unsigned char gx_smem[];
+__device__ __forceinline__ i64 gx_sld_i8(u32 o) { return (i64)*(const signed char*)(gx_smem + o); }
+__device__ __forceinline__ i64 gx_sld_u8(u32 o) { return (i64)*(const unsigned char*)(gx_smem + o); }
+__device__ __forceinline__ i64 gx_sld_i16(u32 o) { return (i64)*(const short*)(gx_smem + o); }
+__device__ __forceinline__ i64 gx_sld_u16(u32 o) { return (i64)*(const unsigned short*)(gx_smem + o); }
+__device__ __forceinline__ i64 gx_sld_i32(u32 o) { return (i64)*(const int*)(gx_smem + o); }
+__device__ __forceinline__ i64 gx_sld_u32(u32 o) { return (i64)*(const unsigned int*)(gx_smem + o); }
+__device__ __forceinline__ u64 gx_sld_64(u32 o) { return (u64)*(const long long*)(gx_smem + o); }
+__device__ __forceinline__ u64 gx_sld_f32(u32 o) { return gx_B((double)*(const float*)(gx_smem + o)); }
+__device__ __forceinline__ u64 gx_sld_f32e(u32 o) { return gxe_f2d(*(const unsigned*)(gx_smem + o)); }
+
+// Bulk copy of the bytes [lo, hi) of a column into shared memory at `dst`
+// (16-byte aligned): the copy covers the 16-byte blocks that hold them, so it
+// starts lo % 16 bytes early.  Every block copied holds at least one byte of
+// [lo, hi), so no block reaches outside the pages that hold the column.
+// Returns the bytes the copy moves (0 for an empty range); with issue false it
+// only computes them.
+__device__ __forceinline__ u32 gx_bulk_span(u32 dst, u64 lo, u64 hi, u64* bar, bool issue) {
+  if (hi <= lo) return 0u;
+  const u64 s = lo & ~15ull, e = (hi + 15ull) & ~15ull;
+  const u32 bytes = (u32)(e - s);
+  if (issue)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(s), "r"(bytes), "r"(gx_saddr(bar))
+                 : "memory");
+  return bytes;
+}
+
+// Exclusive offset of warp `w`'s count among cnt[0..nw) (nw <= 32) and the
+// total, computed by every lane of the calling warp from the shared counts.
+__device__ __forceinline__ u32 gx_block_excl(const u32* cnt, int nw, u32* total, int w) {
+  const int lane = threadIdx.x & 31;
+  const u32 c = lane < nw ? cnt[lane] : 0u;
+  u32 incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const u32 t = __shfl_up_sync(GX_FULL, incl, d);
+    if (lane >= d) incl += t;
+  }
+  *total = __shfl_sync(GX_FULL, incl, 31);
+  return __shfl_sync(GX_FULL, incl - c, w & 31);
+}
+
 __device__ __forceinline__ void gx_st_8(void* p, i64 i, u64 v) { __stcs((signed char*)p + i, (signed char)v); }
 __device__ __forceinline__ void gx_st_16(void* p, i64 i, u64 v) { __stcs((short*)p + i, (short)v); }
 __device__ __forceinline__ void gx_st_32(void* p, i64 i, u64 v) { __stcs((int*)p + i, (int)v); }
@@ -256,6 +338,63 @@ __device__ __forceinline__ u64 gx_lookback_resolve(u64* status, i64 tile, u64 ag
     excl += v;
     if (has_pfx) break;
     pred -= 128;
+  }
+  if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (excl + agg));
+  return excl;
+}
+
+// The same wait with a window of 32 x PER predecessors per poll (lane l reads
+// distances PER l + 1 .. PER l + PER).  `known` / `known_incl`: a tile before
+// `tile` whose inclusive prefix the caller already has (its block's previous
+// tile; -1 and 0 when it has none): the walk treats it as a published prefix
+// and never reads further back, so it spans at most the tiles other blocks
+// claimed since.
+template <int PER>
+__device__ __forceinline__ u64 gx_lookback_wide(u64* status, i64 tile, u64 agg, int* err, u32 max_spins,
+                                                i64 known = -1, u64 known_incl = 0ull) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) return 0ull;  // published as a prefix already
+  u64 excl = 0;
+  i64 pred = tile - 1;
+  u32 spins = 0;
+  while (true) {
+    u64 s[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const i64 idx = pred - (lane * PER + i);
+      s[i] = idx > known ? gx_ld_relaxed(status + idx) : (idx == known ? (GX_ST_PFX | known_incl) : GX_ST_PFX);
+    }
+    int first_pfx = PER;
+#pragma unroll
+    for (int i = PER - 1; i >= 0; i--)
+      if ((u32)(s[i] >> 62) == 2u) first_pfx = i;
+    const u32 has_pfx = __ballot_sync(GX_FULL, first_pfx < PER);
+    const int pl = has_pfx ? __ffs(has_pfx) - 1 : 0;
+    const int pfx_i = __shfl_sync(GX_FULL, first_pfx, pl);
+    const int last = has_pfx ? pl * PER + pfx_i : 32 * PER - 1;
+    bool missing = false;
+    u64 v = 0;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      if (lane * PER + i <= last) {
+        if ((u32)(s[i] >> 62) == 0u) missing = true;
+        v += s[i] & GX_ST_VAL;
+      }
+    }
+    if (__any_sync(GX_FULL, missing)) {
+      if (++spins > max_spins) {
+        if (lane == 0) atomicExch(err, 1);
+        return ~0ull;
+      }
+      if ((spins & 255u) == 0u && *(volatile int*)err != 0) return ~0ull;
+      __nanosleep(32);
+      continue;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(GX_FULL, v, o);
+    excl += v;
+    if (has_pfx) break;
+    pred -= 32 * PER;
   }
   if (lane == 0) gx_st_release(status + tile, GX_ST_PFX | (excl + agg));
   return excl;

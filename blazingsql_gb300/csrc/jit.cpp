@@ -73,8 +73,10 @@ std::vector<char> compile_cubin(const std::string& src, const std::string& name,
     std::string log(ls, '\0');
     nvrtcGetProgramLog(prog, &log[0]);
     nvrtcDestroyProgram(&prog);
-    if (std::getenv("GX_JIT_DUMP")) {
-      std::ofstream f("/tmp/gx_failed_kernel.cu");
+    // GX_JIT_DUMP names a directory that receives the failing source
+    const char* dump = std::getenv("GX_JIT_DUMP");
+    if (dump && *dump) {
+      std::ofstream f(std::string(dump) + "/gx_failed_" + name + ".cu");
       f << src;
     }
     fail(GX_ERR_CUDA, "NVRTC compile of " + name + " failed: " + log.substr(0, 400));
@@ -110,13 +112,13 @@ int device_sm_count() {
   return n;
 }
 
-JitKernel jit_get(const std::string& body, const std::string& name, int block_threads) {
+JitKernel jit_get(const std::string& body, const std::string& name, int block_threads, unsigned dyn_smem) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) fail(GX_ERR_CUDA, "no CUDA device");
   const std::string src = std::string(kPrelude) + "\n" + body;
   const uint64_t h = fnv1a(src);
   char keybuf[64];
-  std::snprintf(keybuf, sizeof keybuf, "%016llx:%d", (unsigned long long)h, dev);
+  std::snprintf(keybuf, sizeof keybuf, "%016llx:%d:%u", (unsigned long long)h, dev, dyn_smem);
   const std::string key(keybuf);
   {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -143,7 +145,12 @@ JitKernel jit_get(const std::string& body, const std::string& name, int block_th
   const DriverApi& d = driver();
   check_cu(d.ModuleLoadData(&e.mod, cubin.data()), "cuModuleLoadData");
   check_cu(d.ModuleGetFunction(&e.k.fn, e.mod, name.c_str()), "cuModuleGetFunction");
-  check_cu(d.OccupancyMaxActiveBlocksPerMultiprocessor(&e.k.max_blocks_per_sm, e.k.fn, block_threads, 0),
+  // static + dynamic shared memory above 48 KiB needs the opt-in; set it for every dynamic size
+  if (dyn_smem > 0u)
+    check_cu(d.FuncSetAttribute(e.k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem),
+             "cuFuncSetAttribute(max dynamic shared memory)");
+  e.k.dyn_smem = dyn_smem;
+  check_cu(d.OccupancyMaxActiveBlocksPerMultiprocessor(&e.k.max_blocks_per_sm, e.k.fn, block_threads, dyn_smem),
            "cuOccupancyMaxActiveBlocksPerMultiprocessor");
   d.FuncGetAttribute(&e.k.num_regs, CU_FUNC_ATTRIBUTE_NUM_REGS, e.k.fn);
   e.k.block_threads = block_threads;

@@ -13,12 +13,14 @@ struct JitKernel {
   int max_blocks_per_sm = 0;   // occupancy at the kernel's block size
   int block_threads = 0;
   int num_regs = 0;
+  unsigned dyn_smem = 0;       // dynamic shared memory per block, bytes
   double compile_ms = 0.0;
 };
 
 // Compiles (or fetches from cache) kernel `name` defined in `body` (appended to
 // the device runtime prelude) for the current device.
-JitKernel jit_get(const std::string& body, const std::string& name, int block_threads);
+// dyn_smem: dynamic shared memory bytes each launch of the kernel gets.
+JitKernel jit_get(const std::string& body, const std::string& name, int block_threads, unsigned dyn_smem = 0);
 
 // Assembler resource report of a kernel (NVRTC + ptxas, no device needed).
 struct KernelResources {

@@ -296,6 +296,18 @@ class Gen {
     if (n.kind == Node::LIT) return;
     if (n.kind == Node::COL) {
       const int c = n.col;
+      if (tile_mode_) {
+        // the tile's rows of column c are in shared memory: element trow at
+        // byte offset sd_<c> + trow * width, validity bit trow of the tile's
+        // re-aligned mask words vmw_<c>
+        const std::string gfn = emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c]);
+        const std::string sfn = "gx_sld_" + gfn.substr(6);  // gx_ld_X -> gx_sld_X
+        o << ind << b << " = inr ? (u64)" << sfn << "(sd_" << c << " + trow * " << type_size(p_.schema[c])
+          << "u) : 0ull;\n";
+        if (p_.nullable[c]) o << ind << v << " = inr && ((vmw_" << c << "[trow >> 5] >> (trow & 31u)) & 1u);\n";
+        else o << ind << v << " = inr;\n";
+        return;
+      }
       auto st = staged_.find(c);
       if (st != staged_.end()) {
         // full words are staged in shared memory at (buffer, index); a partial
@@ -544,7 +556,10 @@ class Gen {
   // the per-row condition that loads are predicated on.
   void emit_words(std::ostringstream& o, const std::vector<int>& ids, const std::string& ind, const std::string& inr,
                   const std::string& tail) const {
-    const std::string rowdef = "const i64 row = (w0 + k) * 32 + lane; const bool inr = " + inr + "; (void)inr;\n";
+    const std::string rowdef =
+        tile_mode_ ? "const u32 trow = (u32)(wl0 + k) * 32u + (u32)lane; const i64 row = tb0 + (i64)trow; "
+                     "const bool inr = " + inr + "; (void)inr; (void)row;\n"
+                   : "const i64 row = (w0 + k) * 32 + lane; const bool inr = " + inr + "; (void)inr;\n";
     bool any_col = false;
     for (int id : ids) any_col |= p_.nodes[id].kind == Node::COL;
     if (any_col) {
@@ -858,6 +873,9 @@ class Gen {
   const KernelConfig& cfg_;
   // columns read from a shared-memory staging buffer: col -> (buffer, index)
   mutable std::map<int, std::pair<std::string, std::string>> staged_;
+  // tile-staged kernels: every column is read from the tile's shared-memory
+  // stage (row trow of the tile; see emit_fused_tma)
+  mutable bool tile_mode_ = false;
 };
 
 void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
@@ -1168,6 +1186,401 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) bal[k] = nbal[k];\n";
   o << "  }\n";
   o << "}\n";
+}
+
+// Columns read by the predicate and the outputs (COPY outputs included), ascending.
+std::vector<int> referenced_columns(const Plan& p) {
+  std::set<int> cols, seen;
+  std::function<void(int)> go = [&](int id) {
+    if (id < 0 || seen.count(id)) return;
+    seen.insert(id);
+    const Node& n = p.nodes[id];
+    if (n.kind == Node::COL) cols.insert(n.col);
+    if (n.kind == Node::OP) { go(n.a); go(n.b); }
+  };
+  if (p.has_filter()) go(p.predicate);
+  for (const auto& os : p.outputs) {
+    if (os.kind == OutSpec::NODE) go(os.node);
+    if (os.kind == OutSpec::COPY) cols.insert(os.col);
+  }
+  return std::vector<int>(cols.begin(), cols.end());
+}
+
+// Store of an output value into its shared-memory staging slot at byte
+// offset `off`, with the conversion store_stmt applies to a global store.
+std::string sstore_stmt(int t, const std::string& off, const std::string& bits) {
+  const std::string at = "(gx_smem + " + off + ")";
+  switch (t) {
+    case BOOL8: return "*(unsigned char*)" + at + " = (unsigned char)((" + bits + ") != 0ull);";
+    case INT8: case UINT8: return "*(unsigned char*)" + at + " = (unsigned char)(" + bits + ");";
+    case INT16: case UINT16: return "*(unsigned short*)" + at + " = (unsigned short)(" + bits + ");";
+    case INT32: case UINT32: case TIMESTAMP_DAYS: case DURATION_DAYS:
+      return "*(unsigned*)" + at + " = (unsigned)(" + bits + ");";
+    case FLOAT32: return "*(float*)" + at + " = (float)gx_D(" + bits + ");";
+    default: return "*(u64*)" + at + " = (" + bits + ");";
+  }
+}
+
+// kept rank t_ of the consumer warp -> its tile row, and its rank tk_ among
+// the tile's kept rows
+void emit_ws_rank_row(std::ostringstream& o, const std::string& in) {
+  o << in << "const u32 trow = act ? (u32)s_kept_w[warp][t_] : 0u; const i64 row = tb0 + (i64)trow; const bool inr = act;"
+             " (void)row; (void)inr;\n";
+  o << in << "const u32 tk_ = woff + t_; (void)tk_;\n";
+  o << in << "const int k = 0;\n";
+}
+
+// Projections of one consumer warp's kept rows of a tile (wcnt rows, tile
+// rows in s_kept_w[warp]), computed in rounds of 32 and staged in shared
+// memory at the rows' tile-level kept ranks (woff + rank): data in the output's
+// slot, validity as one byte per row.  Expensive CASE branches are first
+// evaluated for the warp's kept rows whose condition selects them, packed into
+// full rounds (per-warp lists, no block barrier).
+void emit_ws_dense(std::ostringstream& o, const Gen& g, const Plan& p, const TileLayout& L, const std::string& ind) {
+  const std::vector<int> roots = g.output_roots();
+  const std::vector<Gen::Lazy> lz = g.lazy_branches(roots);
+  std::map<int, int> lz_root;
+  std::set<int> stop;
+  for (size_t i = 0; i < lz.size(); i++) {
+    lz_root[lz[i].root] = (int)i;
+    stop.insert(lz[i].root);
+  }
+  const std::vector<int> proj = g.cone_stop(roots, stop);
+  const std::string i2 = ind + "  ", i3 = i2 + "  ";
+  if (!lz.empty()) {
+    const int nl = (int)lz.size();
+    std::vector<int> conds;
+    for (const auto& l : lz) conds.push_back(l.cond);
+    const std::vector<int> cond_ids = g.cone(conds);
+    o << ind << "u32 dmd_[" << nl << "][GX_V];\n";
+    o << ind << "#pragma unroll\n" << ind << "for (int r_ = 0; r_ < GX_V; r_++) {\n";
+    o << i2 << "#pragma unroll\n" << i2 << "for (int l_ = 0; l_ < " << nl << "; l_++) dmd_[l_][r_] = 0u;\n";
+    o << i2 << "if ((u32)r_ * 32u < wcnt) {\n";
+    o << i3 << "const u32 t_ = (u32)r_ * 32u + (u32)lane; const bool act = t_ < wcnt;\n";
+    emit_ws_rank_row(o, i3);
+    emit_row_nodes(o, g, p, cond_ids, {}, i3);
+    for (int i = 0; i < nl; i++) {
+      const int c = lz[i].cond;
+      o << i3 << "dmd_[" << i << "][r_] = __ballot_sync(GX_FULL, act && (" << g.V(c) << " && " << g.nz(c) << "));\n";
+    }
+    o << i2 << "}\n";
+    o << ind << "}\n";
+    for (int i = 0; i < nl; i++) {
+      o << ind << "{\n";
+      o << i2 << "u32 dtot_ = 0u;\n";
+      o << i2 << "#pragma unroll\n" << i2 << "for (int r_ = 0; r_ < GX_V; r_++) {\n";
+      o << i3 << "const u32 db_ = dmd_[" << i << "][r_];\n";
+      o << i3 << "if ((db_ >> lane) & 1u) s_dem_[warp][dtot_ + __popc(db_ & ((1u << lane) - 1u))] = "
+                 "(unsigned short)(r_ * 32 + lane);\n";
+      o << i3 << "dtot_ += __popc(db_);\n";
+      o << i2 << "}\n";
+      o << i2 << "__syncwarp();\n";
+      o << i2 << "for (u32 db_ = 0; db_ < dtot_; db_ += 32u) {\n";
+      o << i3 << "const u32 q_ = db_ + (u32)lane; const bool act = q_ < dtot_;\n";
+      o << i3 << "const u32 t_ = act ? (u32)s_dem_[warp][q_] : 0u;\n";
+      emit_ws_rank_row(o, i3);
+      emit_row_nodes(o, g, p, lz[i].nodes, {}, i3);
+      o << i3 << "if (act) { s_lzb_[" << i << "][warp][t_] = " << g.B(lz[i].root) << "; s_lzv_[" << i
+        << "][warp][t_] = " << g.V(lz[i].root) << " ? 1 : 0; }\n";
+      o << i2 << "}\n";
+      o << i2 << "__syncwarp();\n";  // s_dem_ is rewritten for the next branch
+      o << ind << "}\n";
+    }
+  }
+  o << ind << "for (u32 base_ = 0; base_ < wcnt; base_ += 32u) {\n";
+  o << i2 << "const u32 t_ = base_ + (u32)lane; const bool act = t_ < wcnt;\n";
+  emit_ws_rank_row(o, i2);
+  emit_row_nodes(o, g, p, proj, lz_root, i2);
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    const OutSpec& os = p.outputs[j];
+    if (os.kind == OutSpec::BROADCAST) continue;
+    const std::string w = std::to_string(L.out_width[j]);
+    const std::string doff = "ost + " + std::to_string(L.out_off[j]) + "u + tk_ * " + w + "u";
+    const std::string voff = "ost + " + std::to_string(L.out_valid_off[j]) + "u + tk_";
+    if (os.kind == OutSpec::NODE) {
+      o << i2 << "if (act) { " << sstore_stmt(os.type, doff, g.B(os.node)) << " gx_smem[" << voff << "] = "
+        << g.V(os.node) << " ? 1 : 0; }\n";
+    } else {
+      const int c = os.col;
+      const std::string cs = std::to_string(c), rt = raw_type(p.schema[c]);
+      const std::string vexpr = p.nullable[c] ? "((vmw_" + cs + "[trow >> 5] >> (trow & 31u)) & 1u)" : "1u";
+      o << i2 << "if (act) { *(" << rt << "*)(gx_smem + " << doff << ") = *(const " << rt << "*)(gx_smem + sd_" << cs
+        << " + trow * " << w << "u); gx_smem[" << voff << "] = (unsigned char)" << vexpr << "; }\n";
+    }
+  }
+  o << ind << "}\n";
+}
+
+// Write-out of a tile's staged outputs (K_w rows at output rows base_w..) by
+// every consumer warp: data element by element (coalesced), validity words
+// rebuilt from the staged bytes by ballots; the first and last words of the
+// tile's range may be shared with the neighbouring tiles and are OR-ed in
+// atomically (the masks were zeroed before the launch).
+void emit_ws_writeout(std::ostringstream& o, const Plan& p, const TileLayout& L, const std::string& ind) {
+  const std::string i2 = ind + "  ";
+  o << ind << "const u32 tid_ = (u32)warp * 32u + (u32)lane;\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    if (p.outputs[j].kind == OutSpec::BROADCAST) continue;
+    const std::string rt = raw_type(p.outputs[j].kind == OutSpec::COPY ? p.schema[p.outputs[j].col] : p.outputs[j].type);
+    o << ind << "for (u32 t = tid_; t < K_w; t += GX_WARPS * 32u) {\n";
+    o << i2 << "const i64 orow = (i64)base_w + (i64)t;\n";
+    o << i2 << "if (orow < a.capacity) __stcs((" << rt << "*)a.out_data[" << j << "] + orow, *(const " << rt
+      << "*)(gx_smem + osw + " << L.out_off[j] << "u + t * " << L.out_width[j] << "u));\n";
+    o << ind << "}\n";
+  }
+  o << ind << "const u32 bf_ = (u32)(base_w & 31ull); const u32 nw_ = K_w ? (bf_ + K_w + 31u) >> 5 : 0u;\n";
+  o << ind << "const i64 w0_ = (i64)(base_w >> 5); const i64 cap_words = (a.capacity + 31) >> 5;\n";
+  o << ind << "for (u32 kw = (u32)warp; kw < nw_; kw += GX_WARPS) {\n";
+  o << i2 << "const int t = (int)(kw * 32u + (u32)lane) - (int)bf_;\n";
+  o << i2 << "const bool in_ = t >= 0 && (u32)t < K_w;\n";
+  o << i2 << "const bool shared_ = (kw == 0u && bf_ != 0u) || kw + 1u == nw_;\n";
+  for (size_t j = 0; j < p.outputs.size(); j++) {
+    if (p.outputs[j].kind == OutSpec::BROADCAST) continue;
+    o << i2 << "{ const u32 word_ = __ballot_sync(GX_FULL, in_ && gx_smem[osw + " << L.out_valid_off[j]
+      << "u + (u32)(in_ ? t : 0)] != 0);\n";
+    o << i2 << "  if (lane == 0 && w0_ + (i64)kw < cap_words) { if (shared_) atomicOr(a.out_mask[" << j
+      << "] + w0_ + kw, word_); else a.out_mask[" << j << "][w0_ + kw] = word_; } }\n";
+  }
+  o << ind << "}\n";
+}
+
+// Tile-staged fused filter + project (single pass, stable order), with the
+// warps of a block in three roles.
+//
+//  * warp 0 (producer): claims tiles in order from the ticket and, for each,
+//    issues one bulk copy per column (its data bytes, and its mask words when
+//    it has a mask) into the next free stage of a GX_NS-stage ring in shared
+//    memory, completing on the stage's "full" mbarrier; it reuses a stage once
+//    every consumer warp has arrived on the stage's "empty" mbarrier.
+//  * warp 1 (resolver): for each tile, once the consumers have published its
+//    aggregate, resolves its output offset by decoupled look-back -- a
+//    512-wide window per poll that stops at the block's previous tile, whose
+//    inclusive prefix it already has -- and hands it back through a "based"
+//    mbarrier.
+//  * warps 2.. (consumers): slot j of their loop evaluates the predicate of
+//    the block's j-th tile from shared memory (lane per row; the mask words are
+//    first re-aligned to the tile's rows), lists each warp's kept rows, meets
+//    at one named barrier to total the tile (one thread publishes the
+//    aggregate and passes it to the resolver); then computes the projections
+//    of the (j-1)-th tile's kept rows into a ring of shared-memory output
+//    staging buffers and releases that tile's stage; then writes the
+//    (j - GX_NR)-th tile's staged outputs to their final rows.
+//
+// A block thus publishes its newest aggregate before it waits on any
+// look-back, and a tile's look-back waits only on earlier tiles, so the kernel
+// cannot deadlock.  Every wait is bounded: a look-back that gives up records
+// error 1 (the block goes on without writing that tile); a copy or hand-over
+// wait that gives up records error 2, and the consumers wait (bounded) for the
+// copies still in flight to land before the block returns.
+void emit_fused_tma(std::ostringstream& o, const Gen& g, const Plan& p, const TileLayout& L, const std::string& name) {
+  g.tile_mode_ = true;
+  const std::vector<int> pred_ids = g.predicate_cone();
+  const std::vector<Gen::Lazy> lz = g.lazy_branches(g.output_roots());
+  const int nl = (int)lz.size();
+  o << "#undef GX_LB\n#define GX_LB __launch_bounds__((GX_WARPS + 2) * 32)\n";
+  o << "#define GX_TR " << L.tile_rows << "\n#define GX_NS " << L.stages << "\n#define GX_STAGE " << L.stage_bytes
+    << "u\n#define GX_OBASE " << L.out_base << "u\n#define GX_OSTAGE " << L.out_stage_bytes << "u\n#define GX_NR "
+    << L.out_stages << "\n#define GX_RR (GX_NR + 1)\n";
+  o << "#define GX_WAIT (1u << 21)\n";
+  // the copies of one tile into the stage at shared address stg
+  o << "__device__ __forceinline__ void gx_issue_tile_(const GxArgs& a, long long t, u32 stg, u64* bar) {\n";
+  o << "  const i64 r0 = (i64)t * GX_TR; const i64 r1 = min(a.n, r0 + (i64)GX_TR);\n";
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const int c = L.cols[i];
+    const std::string cs = std::to_string(c), w = std::to_string(type_size(p.schema[c]));
+    o << "  const u64 lo" << cs << " = (u64)a.in_data[" << cs << "] + (u64)(a.in_off[" << cs << "] + r0) * " << w
+      << "ull, hi" << cs << " = (u64)a.in_data[" << cs << "] + (u64)(a.in_off[" << cs << "] + r1) * " << w << "ull;\n";
+    if (L.mask_off[i] != UINT32_MAX)
+      o << "  const u64 mlo" << cs << " = (u64)(a.in_mask[" << cs << "] + ((a.in_off[" << cs << "] + r0) >> 5)), mhi"
+        << cs << " = (u64)(a.in_mask[" << cs << "] + ((a.in_off[" << cs << "] + r1 - 1) >> 5) + 1);\n";
+  }
+  o << "  u32 tot = 0u;\n";
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const std::string cs = std::to_string(L.cols[i]);
+    o << "  tot += gx_bulk_span(0u, lo" << cs << ", hi" << cs << ", bar, false);\n";
+    if (L.mask_off[i] != UINT32_MAX) o << "  tot += gx_bulk_span(0u, mlo" << cs << ", mhi" << cs << ", bar, false);\n";
+  }
+  o << "  gx_mbar_arrive_tx(bar, tot);\n";
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const std::string cs = std::to_string(L.cols[i]);
+    o << "  gx_bulk_span(stg + " << L.data_off[i] << "u, lo" << cs << ", hi" << cs << ", bar, true);\n";
+    if (L.mask_off[i] != UINT32_MAX)
+      o << "  gx_bulk_span(stg + " << L.mask_off[i] << "u, mlo" << cs << ", mhi" << cs << ", bar, true);\n";
+  }
+  o << "}\n";
+
+  o << "extern \"C\" __global__ void GX_LB " << name << "(const GxArgs a) {\n";
+  o << "  const int lane = threadIdx.x & 31; const int wid_ = threadIdx.x >> 5;\n";
+  o << "  const i64 ntiles = (a.n + GX_TR - 1) / GX_TR;\n";
+  o << "  __shared__ __align__(8) u64 s_full_[GX_NS];\n";
+  o << "  __shared__ __align__(8) u64 s_empty_[GX_NS];\n";
+  o << "  __shared__ __align__(8) u64 s_counted_[GX_RR];\n";
+  o << "  __shared__ __align__(8) u64 s_based_[GX_RR];\n";
+  o << "  __shared__ long long s_tile_[GX_NS];\n";
+  o << "  __shared__ long long s_rtile_[GX_RR];\n";
+  o << "  __shared__ u64 s_ragg_[GX_RR];\n";
+  o << "  __shared__ u64 s_base_[GX_RR];\n";
+  o << "  __shared__ u32 s_cnt_[2][GX_WARPS];\n";
+  o << "  __shared__ unsigned short s_kept_[2][GX_WARPS][GX_V * 32];\n";
+  if (L.num_masked > 0) o << "  __shared__ u32 s_vm_[2][" << L.num_masked << "][GX_TR / 32];\n";
+  if (nl > 0) {
+    o << "  __shared__ unsigned short s_dem_[GX_WARPS][GX_V * 32];\n";
+    o << "  __shared__ u64 s_lzb_[" << nl << "][GX_WARPS][GX_V * 32];\n";
+    o << "  __shared__ unsigned char s_lzv_[" << nl << "][GX_WARPS][GX_V * 32];\n";
+  }
+  o << "  const u32 smem0_ = gx_saddr(gx_smem);\n";
+  // bulk copies land on 16-byte boundaries of the dynamic shared memory
+  o << "  if ((smem0_ & 15u) != 0u) { if (threadIdx.x == 0) atomicExch(a.err, 3); return; }\n";
+  o << "  if (threadIdx.x == 0) {\n";
+  o << "    for (int q = 0; q < GX_NS; q++) { gx_mbar_init(&s_full_[q], 1u); gx_mbar_init(&s_empty_[q], GX_WARPS); }\n";
+  o << "    for (int q = 0; q < GX_RR; q++) { gx_mbar_init(&s_counted_[q], 1u); gx_mbar_init(&s_based_[q], 1u); }\n";
+  o << "    gx_mbar_init_fence();\n";
+  o << "  }\n";
+  o << "  __syncthreads();\n";
+  // ---- producer
+  o << "  if (wid_ == 0) {\n";
+  o << "    if (lane == 0) {\n";
+  o << "      for (int j = 0; ; j++) {\n";
+  o << "        const int q = j % GX_NS;\n";
+  o << "        if (j >= GX_NS && !gx_mbar_wait(&s_empty_[q], (u32)(j / GX_NS - 1) & 1u, GX_WAIT)) {\n";
+  o << "          atomicExch(a.err, 2);\n";
+  o << "          break;\n";
+  o << "        }\n";
+  o << "        long long t = (long long)atomicAdd(a.tile_counter, 1ull);\n";
+  o << "        if (t >= ntiles) t = -1;\n";
+  o << "        s_tile_[q] = t;\n";
+  o << "        if (t < 0) { gx_mbar_arrive(&s_full_[q]); break; }\n";
+  o << "        gx_fence_async_smem();\n";
+  o << "        gx_issue_tile_(a, t, smem0_ + (u32)q * GX_STAGE, &s_full_[q]);\n";
+  o << "      }\n";
+  o << "    }\n";
+  o << "    return;\n";
+  o << "  }\n";
+  // ---- resolver
+  o << "  if (wid_ == 1) {\n";
+  o << "    long long tk = -1; u64 pk = 0ull;\n";  // the block's last resolved tile and its inclusive prefix
+  o << "    for (int j = 0; ; j++) {\n";
+  o << "      const int b = j % GX_RR;\n";
+  o << "      if (!gx_mbar_wait(&s_counted_[b], (u32)(j / GX_RR) & 1u, GX_WAIT)) {\n";
+  o << "        if (lane == 0) atomicExch(a.err, 2);\n";
+  o << "        return;\n";
+  o << "      }\n";
+  o << "      const long long t = s_rtile_[b]; const u64 agg = s_ragg_[b];\n";
+  o << "      if (t < 0) return;\n";
+  o << "      const u64 ex = gx_lookback_wide<16>(a.tile_status, t, agg, a.err, 1u << 22, tk, pk);\n";
+  o << "      if (ex != ~0ull) { tk = t; pk = ex + agg; } else { tk = -1; pk = 0ull; }\n";
+  o << "      if (lane == 0) {\n";
+  o << "        s_base_[b] = ex;\n";
+  o << "        if (t == ntiles - 1 && ex != ~0ull) *a.out_count = ex + agg;\n";
+  o << "        gx_mbar_arrive(&s_based_[b]);\n";
+  o << "      }\n";
+  o << "      __syncwarp();\n";
+  o << "    }\n";
+  o << "  }\n";
+  // ---- consumers
+  o << "  const int warp = wid_ - 2;\n";
+  // per-column shifts: the byte of element 0 within its 16-byte block, and
+  // for masks the byte of the first word within its block and the bit of row
+  // 0 within that word -- the same for every tile (tiles are multiples of 128 rows)
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const int c = L.cols[i];
+    const std::string cs = std::to_string(c);
+    o << "  const u32 h_" << cs << " = (u32)(((u64)a.in_data[" << cs << "] + (u64)a.in_off[" << cs << "] * "
+      << type_size(p.schema[c]) << "ull) & 15ull);\n";
+    if (L.mask_off[i] != UINT32_MAX) {
+      o << "  const u32 mh_" << cs << " = (u32)((u64)(a.in_mask[" << cs << "] + (a.in_off[" << cs << "] >> 5)) & 15ull);\n";
+      o << "  const u32 ms_" << cs << " = (u32)(a.in_off[" << cs << "] & 31);\n";
+    }
+  }
+  o << "  long long tile_p = -1; u32 wcnt_p = 0u, woff_p = 0u;\n";  // the (j-1)-th tile, awaiting its projections
+  o << "  for (int j = 0; ; j++) {\n";
+  o << "    const int q = j % GX_NS; const int vp = j & 1; const int rr = j % GX_RR;\n";
+  o << "    const bool ok_ = gx_mbar_wait(&s_full_[q], (u32)(j / GX_NS) & 1u, GX_WAIT);\n";
+  o << "    const long long tile = ok_ ? s_tile_[q] : -1;\n";
+  o << "    u32 wcnt = 0u;\n";
+  o << "    if (tile >= 0) {\n";
+  o << "      const i64 tb0 = (i64)tile * GX_TR; const int wl0 = warp * GX_V;\n";
+  o << "      const u32 stg = (u32)q * GX_STAGE;\n";
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const std::string cs = std::to_string(L.cols[i]);
+    o << "      const u32 sd_" << cs << " = stg + " << L.data_off[i] << "u + h_" << cs << "; (void)sd_" << cs << ";\n";
+    if (L.mask_off[i] != UINT32_MAX) {
+      o << "      const u32* vmw_" << cs << " = s_vm_[vp][" << L.mask_index[i] << "]; (void)vmw_" << cs << ";\n";
+      o << "      if (lane < GX_V) {\n";
+      o << "        const u32 wk_ = (u32)(wl0 + lane);\n";
+      o << "        const u32* raw_ = (const u32*)(gx_smem + stg + " << L.mask_off[i] << "u + mh_" << cs << ");\n";
+      o << "        s_vm_[vp][" << L.mask_index[i] << "][wk_] = __funnelshift_r(raw_[wk_], raw_[wk_ + 1], ms_" << cs
+        << ");\n";
+      o << "      }\n";
+    }
+  }
+  o << "      __syncwarp();\n";
+  o << "      const i64 w0 = (i64)tile * GX_TILE_WORDS + wl0;\n";
+  g.decl(o, pred_ids, "      ");
+  g.emit_predicate(o, "      ");
+  o << "      u32 r_ = 0u;\n";
+  o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) {\n";
+  o << "        const u32 bk_ = __ballot_sync(GX_FULL, alive[k]);\n";
+  o << "        if ((bk_ >> lane) & 1u) s_kept_[vp][warp][r_ + __popc(bk_ & ((1u << lane) - 1u))] = "
+       "(unsigned short)((wl0 + k) * 32 + lane);\n";
+  o << "        r_ += __popc(bk_);\n";
+  o << "      }\n";
+  o << "      wcnt = r_;\n";
+  o << "      __syncwarp();\n";
+  o << "    }\n";
+  o << "    if (lane == 0) s_cnt_[vp][warp] = wcnt;\n";
+  o << "    if (!gx_bar_and(ok_, GX_WARPS * 32)) {\n";
+  // a copy never landed: wait (bounded) for the copies in flight, then leave
+  o << "      if (warp == 0 && lane == 0) atomicExch(a.err, 2);\n";
+  o << "      for (int d_ = 0; d_ < GX_NS; d_++) gx_mbar_wait(&s_full_[(j + d_) % GX_NS], (u32)((j + d_) / GX_NS) & 1u, "
+       "GX_WAIT);\n";
+  o << "      return;\n";
+  o << "    }\n";
+  o << "    u32 tot_ = 0u, woff = 0u;\n";
+  o << "    if (tile >= 0) woff = gx_block_excl(s_cnt_[vp], GX_WARPS, &tot_, warp);\n";
+  o << "    if (warp == 0 && lane == 0) {\n";
+  o << "      if (tile >= 0) gx_st_release(a.tile_status + tile, (tile == 0 ? GX_ST_PFX : GX_ST_AGG) | (u64)tot_);\n";
+  o << "      s_rtile_[rr] = tile; s_ragg_[rr] = (u64)tot_;\n";
+  o << "      gx_mbar_arrive(&s_counted_[rr]);\n";
+  o << "    }\n";
+  // projections of the previous slot's tile
+  o << "    if (tile_p >= 0) {\n";
+  o << "      const int jp = j - 1; const int qp = jp % GX_NS; const int pp = jp & 1;\n";
+  o << "      const u32 ost = GX_OBASE + (u32)(jp % GX_NR) * GX_OSTAGE;\n";
+  o << "      const u32 wcnt = wcnt_p, woff = woff_p;\n";
+  o << "      const i64 tb0 = (i64)tile_p * GX_TR;\n";
+  o << "      const u32 stg = (u32)qp * GX_STAGE;\n";
+  o << "      const unsigned short (*s_kept_w)[GX_V * 32] = s_kept_[pp];\n";
+  for (size_t i = 0; i < L.cols.size(); i++) {
+    const std::string cs = std::to_string(L.cols[i]);
+    o << "      const u32 sd_" << cs << " = stg + " << L.data_off[i] << "u + h_" << cs << "; (void)sd_" << cs << ";\n";
+    if (L.mask_off[i] != UINT32_MAX)
+      o << "      const u32* vmw_" << cs << " = s_vm_[pp][" << L.mask_index[i] << "]; (void)vmw_" << cs << ";\n";
+  }
+  emit_ws_dense(o, g, p, L, "      ");
+  o << "      __syncwarp();\n";
+  o << "      if (lane == 0) gx_mbar_arrive(&s_empty_[qp]);\n";
+  o << "    }\n";
+  // after the last tile every staged tile is written out, the one just
+  // projected included: all consumer warps must have staged it first
+  o << "    if (tile < 0) gx_bar_and(true, GX_WARPS * 32);\n";
+  o << "    for (int jw = j - GX_NR; jw <= (tile >= 0 ? j - GX_NR : j - 1); jw++) {\n";
+  o << "      if (jw < 0) continue;\n";
+  o << "      const int pr = jw % GX_RR;\n";
+  o << "      if (s_rtile_[pr] < 0) continue;\n";
+  o << "      const bool okb = gx_mbar_wait(&s_based_[pr], (u32)(jw / GX_RR) & 1u, GX_WAIT);\n";
+  o << "      if (!okb && warp == 0 && lane == 0) atomicExch(a.err, 2);\n";
+  o << "      const u64 base_w = okb ? s_base_[pr] : ~0ull;\n";
+  o << "      if (base_w != ~0ull) {\n";
+  o << "        const u32 K_w = (u32)s_ragg_[pr]; const u32 osw = GX_OBASE + (u32)(jw % GX_NR) * GX_OSTAGE;\n";
+  emit_ws_writeout(o, p, L, "        ");
+  o << "      }\n";
+  o << "    }\n";
+  o << "    if (tile < 0) break;\n";
+  o << "    tile_p = tile; wcnt_p = wcnt; woff_p = woff;\n";
+  o << "  }\n";
+  o << "}\n";
+  g.tile_mode_ = false;
 }
 
 // Batched persistent form of the pipelined fused filter: one launch runs a
@@ -1523,6 +1936,49 @@ void emit_staged_filter(std::ostringstream& o, const Gen& g, const Plan& p, cons
 
 }  // namespace
 
+TileLayout tile_layout(const Plan& p, int warps, int words, int stages) {
+  TileLayout L;
+  L.tile_rows = warps * words * 32;
+  L.stages = stages;
+  if (L.tile_rows % 128 != 0) fail(GX_ERR_INVALID, "tile-staged kernels need tiles of a multiple of 128 rows");
+  if (stages < 2) fail(GX_ERR_INVALID, "tile-staged kernels need at least 2 stages");
+  if (warps > 32) fail(GX_ERR_INVALID, "tile-staged kernels take at most 32 consumer warps");
+  L.cols = referenced_columns(p);
+  uint32_t off = 0;
+  for (int c : L.cols) {
+    // data: the tile's bytes from the 16-byte block of its first element up to
+    // the block past its last; mask: its words plus the next one (re-alignment
+    // to the tile's rows reads one word ahead), from the first word's block
+    L.data_off.push_back(off);
+    off += (uint32_t)L.tile_rows * (uint32_t)type_size(p.schema[c]) + 32u;
+    if (p.nullable[c]) {
+      L.mask_off.push_back(off);
+      L.mask_index.push_back(L.num_masked++);
+      off += (uint32_t)L.tile_rows / 8u + 32u;
+    } else {
+      L.mask_off.push_back(UINT32_MAX);
+      L.mask_index.push_back(-1);
+    }
+  }
+  L.stage_bytes = (off + 127u) & ~127u;
+  // output staging: per non-literal output its data slot and one validity
+  // byte per row, by the row's kept rank within the tile
+  uint32_t oo = 0;
+  for (const auto& os : p.outputs) {
+    const int t = os.kind == OutSpec::COPY ? p.schema[os.col] : os.type;
+    const uint32_t w = os.kind == OutSpec::BROADCAST ? 0u : (uint32_t)type_size(t);
+    L.out_width.push_back(w);
+    L.out_off.push_back(oo);
+    oo += ((uint32_t)L.tile_rows * w + 15u) & ~15u;
+    L.out_valid_off.push_back(oo);
+    if (os.kind != OutSpec::BROADCAST) oo += (uint32_t)L.tile_rows;
+  }
+  L.out_stage_bytes = (oo + 127u) & ~127u;
+  L.out_base = L.stage_bytes * (uint32_t)stages;
+  L.dyn_smem = L.out_base + (uint32_t)L.out_stages * L.out_stage_bytes;
+  return L;
+}
+
 std::vector<int> conjunct_columns(const Plan& p, int c) {
   std::set<int> cols;
   std::function<void(int)> go = [&](int id) {
@@ -1574,6 +2030,14 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     c.runtime_order = true;
     Gen gs(p, c);
     emit_staged_filter(o, gs, p, name);
+    return o.str();
+  }
+  if (kind == KernelKind::FUSED_TMA) {
+    if (!p.has_filter()) fail(GX_ERR_INVALID, "the tile-staged kernel runs filter plans");
+    if (cfg.runtime_order || cfg.short_circuit || !cfg.dense)
+      fail(GX_ERR_INVALID, "the tile-staged kernel evaluates conjuncts in plan order with dense projections");
+    const TileLayout L = tile_layout(p, cfg.warps, cfg.words, cfg.stages);
+    emit_fused_tma(o, g, p, L, name);
     return o.str();
   }
   if (kind == KernelKind::FUSED_BATCHED) {

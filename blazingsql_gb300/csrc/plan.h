@@ -70,6 +70,14 @@ struct KernelConfig {
   // registers per thread the kernel is held to (0: the compiler's choice),
   // as launch bounds asking for 65536 / (max_regs x threads) resident blocks
   int max_regs = 0;
+  // Single-pass filters on the tile-staged kernel (FUSED_TMA): -1 when the
+  // plan qualifies (fixed conjunct order, dense projections), 0 never, 1 always
+  // when it qualifies; its consumer warps, 32-row words per consumer warp and
+  // input stages (>= 2) of its shared-memory tile ring
+  int use_tma = -1;
+  int tma_warps = 8;
+  int tma_words = 2;
+  int stages = 3;
 };
 
 struct Plan {
@@ -118,7 +126,32 @@ std::string generate_agg_kernel(const Plan& plan, const AggLayout& L, const Kern
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
 constexpr int GX_OUTPUTS_PER_KERNEL = 32;
 
-enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED, FUSED_STAGED };
+enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED, FUSED_STAGED, FUSED_TMA };
+
+// Shared-memory layout of the tile-staged fused filter (FUSED_TMA): a ring of
+// `stages` input stages, each holding one tile (consumer warps x words x 32
+// rows) of every column the plan reads -- its data bytes and, for a column
+// with a validity mask, its mask words -- copied in by one bulk copy per
+// column and tile; then a ring of output staging buffers.
+struct TileLayout {
+  int tile_rows = 0;
+  int stages = 0;
+  std::vector<int> cols;             // staged columns, ascending
+  std::vector<uint32_t> data_off;    // per staged column: data slot offset within a stage
+  std::vector<uint32_t> mask_off;    // mask slot offset (UINT32_MAX: no mask)
+  std::vector<int> mask_index;       // index among the masked staged columns (-1: none)
+  int num_masked = 0;
+  uint32_t stage_bytes = 0;
+  // output staging: out_stages buffers of out_stage_bytes from out_base, each
+  // with a data slot (out_off) and validity bytes (out_valid_off) per output
+  std::vector<uint32_t> out_width, out_off, out_valid_off;
+  uint32_t out_stage_bytes = 0;
+  uint32_t out_base = 0;
+  int out_stages = 3;                // a tile is written out this many tiles after its projections
+  uint32_t dyn_smem = 0;             // stages x stage_bytes + out_stages x out_stage_bytes
+};
+// (plan.nullable tells which columns carry a mask at run time)
+TileLayout tile_layout(const Plan& plan, int warps, int words, int stages);
 
 // Header of a batch table run by the FUSED_BATCHED kernel (device memory).
 struct BatchHeader {

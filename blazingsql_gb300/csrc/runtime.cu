@@ -399,6 +399,7 @@ static const char* kind_name(KernelKind k) {
     case KernelKind::COUNT_FILTER: return "gx_filter_count";
     case KernelKind::FUSED_BATCHED: return "gx_filter_batched";
     case KernelKind::FUSED_STAGED: return "gx_filter_staged";
+    case KernelKind::FUSED_TMA: return "gx_filter_tma";
     default: return "gx_filter_write";
   }
 }
@@ -447,7 +448,7 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
   int dev = 0;
   check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   std::string key = std::to_string((int)kind) + ":" + std::to_string(dev) + ":" + std::to_string(warps) + "x" +
-                    std::to_string(words) + ":";
+                    std::to_string(words) + "x" + std::to_string(cfg_.stages) + ":";
   for (bool b : nullable) key += b ? '1' : '0';
   {
     std::lock_guard<std::mutex> g(kmu_);
@@ -461,7 +462,10 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
   c.words = words;
   const std::string name = kind_name(kind);
   const std::string src = generate_kernel(p, kind, c, name);
-  const JitKernel k = jit_get(src, name, warps * 32);
+  // the tile-staged kernel runs a producer and a resolver warp beside its consumer warps
+  const bool tma = kind == KernelKind::FUSED_TMA;
+  const unsigned dyn = tma ? tile_layout(p, warps, words, c.stages).dyn_smem : 0u;
+  const JitKernel k = jit_get(src, name, (tma ? warps + 2 : warps) * 32, dyn);
   std::lock_guard<std::mutex> g(kmu_);
   kcache_[key] = k;
   return k;
@@ -478,8 +482,8 @@ void launch_raw(const JitKernel& k, int grid, cudaStream_t s, void** params, boo
     check_cuda(cudaEventCreate(&e1), "event");
     check_cuda(cudaEventRecord(e0, s), "event record");
   }
-  CUresult r = driver().LaunchKernel(k.fn, (unsigned)grid, 1, 1, (unsigned)k.block_threads, 1, 1, 0, (CUstream)s,
-                                     params, nullptr);
+  CUresult r = driver().LaunchKernel(k.fn, (unsigned)grid, 1, 1, (unsigned)k.block_threads, 1, 1, k.dyn_smem,
+                                     (CUstream)s, params, nullptr);
   if (r != CUDA_SUCCESS) fail(GX_ERR_CUDA, std::string("cuLaunchKernel: ") + driver_error_string(r));
   g_launches.fetch_add(1);
   if (tm) {
@@ -501,6 +505,18 @@ static unsigned long long* pinned_header() {
   if (!buf) check_cuda(cudaMallocHost((void**)&buf, 64), "pinned header");
   for (int i = 0; i < 4; i++) buf[i] = 0;
   return buf;
+}
+
+// The error word a filter kernel leaves in its scratch header: 1 a look-back
+// wait gave up, 2 a wait for a tile's bulk copies (or a hand-over between the
+// warps of a tile-staged block) gave up, 3 the dynamic shared memory was not
+// 16-byte aligned (nothing was copied).
+static void raise_kernel_error(unsigned long long word) {
+  const int e = (int)(word & 0xffffffffull);
+  if (e == 0) return;
+  if (e == 1) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  if (e == 2) fail(GX_ERR_TIMEOUT, "tile-staged kernel: a wait for bulk copies or a warp hand-over timed out");
+  fail(GX_ERR_CUDA, "tile-staged kernel: dynamic shared memory not 16-byte aligned");
 }
 
 static std::vector<bool> runtime_nullable(const Plan& p, const std::vector<ColumnView>& cols) {
@@ -557,13 +573,36 @@ bool CompiledPlan::can_defer() const {
 }
 
 void CompiledPlan::finish_queued(const unsigned long long* hdr, int64_t n, gx_column* out, int64_t* out_rows) const {
-  if (hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  raise_kernel_error(hdr[2]);
   const int64_t rows = n == 0 ? 0 : mode_ == GX_FILTER_TWO_PASS ? (int64_t)hdr[3] : (int64_t)hdr[1];
   if (out_rows) *out_rows = rows;
   for (size_t j = 0; j < plan_.outputs.size(); j++) {
     if (rows > out[j].capacity) fail(GX_ERR_CAPACITY, "output capacity too small");
     out[j].size = rows;
   }
+}
+
+// Single-pass filters run on the tile-staged kernel (FUSED_TMA) unless the
+// plan evaluates its conjuncts in a runtime order, projects per word, keys
+// RAND by output row (the output row is known only at the write-out), was told
+// not to, reads a column that is not fixed-width or not naturally aligned, or
+// its tile ring does not fit in shared memory.
+bool CompiledPlan::tma_path(const std::vector<ColumnView>& cols) const {
+  if (cfg_.use_tma == 0 || mode_ == GX_FILTER_TWO_PASS || !plan_.has_filter()) return false;
+  if (!cfg_.dense || cfg_.runtime_order || cfg_.short_circuit || cfg_.staged) return false;
+  for (const Node& nd : plan_.nodes)
+    if (nd.kind == Node::OP && nd.op == OP_RAND && nd.rand_out_row) return false;
+  // elements are read from shared memory at their natural alignment
+  for (const ColumnView& c : cols) {
+    const int w = type_size(c.type);
+    if (w > 1 && ((uintptr_t)c.data + (uintptr_t)(c.offset * w)) % (uintptr_t)w != 0) return false;
+  }
+  Plan p = plan_;
+  p.nullable = runtime_nullable(plan_, cols);
+  const TileLayout L = tile_layout(p, cfg_.tma_warps, cfg_.tma_words, cfg_.stages);
+  for (int c : L.cols)
+    if (type_size(p.schema[c]) == 0) return false;  // only fixed-width columns are staged
+  return L.dyn_smem <= kTmaMaxDynSmem;
 }
 
 int64_t CompiledPlan::tiles_for(int64_t n) const {
@@ -687,7 +726,10 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
   // the single-pass fused kernel's block shape (tuned online when allowed)
   int explore = -1;
   Shape sh{cfg_.warps, cfg_.words};
-  if (!two_pass && !(cfg_.staged && cfg_.runtime_order)) sh = filter_shape(n, &explore);
+  const std::vector<bool> nb = runtime_nullable(plan_, cols);
+  const bool tma = !two_pass && tma_path(cols);
+  if (tma) sh = {cfg_.tma_warps, cfg_.tma_words};
+  else if (!two_pass && !(cfg_.staged && cfg_.runtime_order)) sh = filter_shape(n, &explore);
   const int64_t tile_words = (int64_t)sh.warps * sh.words;
   const int64_t ntiles = (nwords + tile_words - 1) / tile_words;
   std::vector<gx_column> made;
@@ -726,7 +768,6 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     }
     unsigned long long* hdr = (unsigned long long*)sbase;
     uint64_t* status = (uint64_t*)sbase + 4;
-    const std::vector<bool> nb = runtime_nullable(plan_, cols);
     KernelArgs a{};
     fill_args_inputs(a, cols);
     a.tile_status = status;
@@ -778,7 +819,7 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       a.out_mask[j] = out[j].null_mask;
     }
     a.capacity = capacity;
-    KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : KernelKind::FUSED_FILTER;
+    KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : tma ? KernelKind::FUSED_TMA : KernelKind::FUSED_FILTER;
     if (!two_pass && cfg_.staged && cfg_.runtime_order && staging_aligned(plan_, cols)) kind = KernelKind::FUSED_STAGED;
     const JitKernel k = two_pass ? kernel(kind, nb) : kernel(kind, nb, sh.warps, sh.words);
     int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
@@ -803,7 +844,7 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       cudaEventDestroy(te1);
       te0 = te1 = nullptr;
     }
-    if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+    raise_kernel_error(host_hdr[2]);
     const int64_t rows = two_pass ? (int64_t)host_hdr[3] : (int64_t)host_hdr[1];
     if (out_rows) *out_rows = rows;
     if (rows > capacity) fail(GX_ERR_CAPACITY, "output capacity too small");
@@ -878,7 +919,7 @@ void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_
   unsigned long long* host_hdr = pinned_header();
   check_cuda(cudaMemcpyAsync(host_hdr, scratch, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
   check_cuda(cudaStreamSynchronize(s), "filter sync");
-  if (host_hdr[2] != 0) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+  raise_kernel_error(host_hdr[2]);
   const int64_t rows = (int64_t)host_hdr[1];
   if (out_rows) *out_rows = rows;
   if (rows > capacity) fail(GX_ERR_CAPACITY, "output capacity too small");

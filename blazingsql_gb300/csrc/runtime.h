@@ -115,6 +115,11 @@ class CompiledPlan {
   bool can_defer() const;
   // tile-status words a filter over n rows uses
   int64_t tiles_for(int64_t n) const;
+  // single-pass calls over these columns run on the tile-staged kernel
+  bool tma_path(const std::vector<ColumnView>& cols) const;
+  // dynamic shared memory a tile ring may take (the rest of the 227 KiB a
+  // block can have holds the kernel's kept-row lists and branch results)
+  static constexpr unsigned kTmaMaxDynSmem = 176u * 1024u;
 
   // kernel handle of this plan for a given kind and set of columns with masks
   JitKernel kernel_for(KernelKind kind, const std::vector<bool>& nullable) const { return kernel(kind, nullable); }

@@ -451,7 +451,8 @@ const char* gx_version(void);
  * filter, 2 filter count pass, 3 filter write pass, 4 the learner's fused pass
  * (conjunct order given at launch), 5 the learner's labelling count pass
  * (per-conjunct pass counts), 6 the batch runner's persistent kernel, 7 the
- * learner's staged fused pass (conjunct columns copied to shared memory by TMA).  Writes at most buf_len
+ * learner's staged fused pass (conjunct columns copied to shared memory by TMA), 8 the tile-staged
+ * single-pass filter (every column's tile copied to shared memory by bulk copies).  Writes at most buf_len
  * bytes (NUL-terminated) and returns the full length, or -1 on error. */
 int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,
                                int64_t buf_len, gx_status_info* status);
