@@ -387,7 +387,7 @@ __device__ __forceinline__ u64 gx_lookback_wide(u64* status, i64 tile, u64 agg, 
         return ~0ull;
       }
       if ((spins & 255u) == 0u && *(volatile int*)err != 0) return ~0ull;
-      __nanosleep(32);
+      __nanosleep(200);  // a wide window re-read costs L2 bandwidth: poll less often
       continue;
     }
 #pragma unroll

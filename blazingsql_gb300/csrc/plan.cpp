@@ -1353,10 +1353,10 @@ void emit_ws_writeout(std::ostringstream& o, const Plan& p, const TileLayout& L,
 //    memory, completing on the stage's "full" mbarrier; it reuses a stage once
 //    every consumer warp has arrived on the stage's "empty" mbarrier.
 //  * warp 1 (resolver): for each tile, once the consumers have published its
-//    aggregate, resolves its output offset by decoupled look-back -- a
-//    512-wide window per poll that stops at the block's previous tile, whose
-//    inclusive prefix it already has -- and hands it back through a "based"
-//    mbarrier.
+//    aggregate and the block's next tile has been counted too, resolves its
+//    output offset by decoupled look-back -- a 256-wide window per poll that
+//    stops at the block's previous tile, whose inclusive prefix it already
+//    has -- and hands it back through a "based" mbarrier.
 //  * warps 2.. (consumers): slot j of their loop evaluates the predicate of
 //    the block's j-th tile from shared memory (lane per row; the mask words are
 //    first re-aligned to the tile's rows), lists each warp's kept rows, meets
@@ -1467,7 +1467,10 @@ void emit_fused_tma(std::ostringstream& o, const Gen& g, const Plan& p, const Ti
   o << "      }\n";
   o << "      const long long t = s_rtile_[b]; const u64 agg = s_ragg_[b];\n";
   o << "      if (t < 0) return;\n";
-  o << "      const u64 ex = gx_lookback_wide<16>(a.tile_status, t, agg, a.err, 1u << 22, tk, pk);\n";
+  // start once the block's next tile is counted too: by then the tiles other
+  // blocks claimed before this one have mostly published their aggregates
+  o << "      gx_mbar_wait(&s_counted_[(j + 1) % GX_RR], (u32)((j + 1) / GX_RR) & 1u, GX_WAIT);\n";
+  o << "      const u64 ex = gx_lookback_wide<8>(a.tile_status, t, agg, a.err, 1u << 22, tk, pk);\n";
   o << "      if (ex != ~0ull) { tk = t; pk = ex + agg; } else { tk = -1; pk = 0ull; }\n";
   o << "      if (lane == 0) {\n";
   o << "        s_base_[b] = ex;\n";
