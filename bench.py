@@ -151,14 +151,61 @@ def cpu_sample_rate(name, w, sample_rows, nthreads, min_seconds=10.0, seed=7):
     return sample_rows * reps / el, reps, el
 
 
+def full_parity(name, w, cols, stream):
+    """The whole step's output against the oracle on the same rows: validity
+    and integer data bit for bit, float data bit for bit except, for the deep
+    plan, the rows whose CASE branch goes through LN / EXP (CUDA's log / exp
+    against glibc, within 2 ulp)."""
+    import numpy as np
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import workloads as W
+    from blazingsql_gb300.types import is_float
+    from oracle import pyoracle
+    out = g.filter_project(cols, w.condition, w.projections, stream=stream)
+    got = [c.to_host() for c in out]
+    g.api.free_columns(out, stream)
+    host = W.device_to_host(cols)
+    t0 = time.perf_counter()
+    exp, rows = pyoracle.filter_project(host, w.condition, w.projections, os.cpu_count() or 1, 0)
+    oracle_s = time.perf_counter() - t0
+    loose = W.c2_transcendental_rows(host) if name == "c2" else np.zeros(rows, dtype=bool)
+    ok = len(got) == len(exp) and all(a.size == rows for a in got)
+    bad_rows, worst = 0, 0.0
+    for a, b in zip(got, exp):
+        if not ok:
+            break
+        va, vb = a.valid(), b.valid()
+        bad = va != vb
+        x, y = a.values(), b.values()
+        if is_float(a.type_id):
+            it = np.int64 if x.dtype == np.float64 else np.int32
+            xi, yi = x.view(it).astype(np.int64), y.view(it).astype(np.int64)
+            xi = np.where(xi < 0, np.int64(-2**63) - xi, xi) if it == np.int64 else xi
+            yi = np.where(yi < 0, np.int64(-2**63) - yi, yi) if it == np.int64 else yi
+            d = np.abs(xi - yi).astype(np.float64)
+            nan_ok = np.isnan(x) == np.isnan(y)
+            d = np.where(np.isnan(x) & np.isnan(y), 0.0, d)
+            bad |= vb & ((~loose & (d != 0)) | ~nan_ok | (loose & (d > 2)))
+            if (vb & loose).any():
+                worst = max(worst, float(d[vb & loose].max()))
+        else:
+            bad |= vb & (x != y)
+        bad_rows += int(bad.sum())
+    del host, got, exp
+    return {"rows": w.rows, "out_rows": int(rows), "matches_oracle": bool(ok and bad_rows == 0),
+            "mismatched_rows": bad_rows, "transcendental_rows": int(loose.sum()),
+            "max_ulp_transcendental_rows": worst, "exact_elsewhere": True, "oracle_seconds": oracle_s}
+
+
 def run_reference(args, world, rank):
-    """CPU reference arm: the oracle port on the host cores, rank 0 only."""
+    """CPU reference arm: the oracle port on all host cores, rank 0 only, on
+    the same rows as our arm (the full workload unless --ref-rows is set)."""
     if rank != 0:
         return
     from blazingsql_gb300 import workloads as W
-    w = W.workload(args.config)
+    w = W.workload(args.config, args.rows or None)
     nthreads = os.cpu_count() or 1
-    sample = args.cpu_sample_rows
+    sample = args.ref_rows or w.rows
     from oracle import pyoracle
     cols = W.host_columns(args.config, sample, seed=7)
     for _ in range(args.warmup):
@@ -174,10 +221,12 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": "filter_project_rows_per_s", "value": value, "unit": "rows/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
-        "config": {"workload": w.name, "rows_per_step": sample, "sample_of_rows": w.rows, "host_threads": nthreads},
+        "config": {"workload": w.name, "rows_per_step": sample, "rows_of_workload": w.rows,
+                   "host_threads": nthreads},
         "cpu_baseline": {"value": value, "unit": "rows/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{sample} rows of {w.name} per step (the reference's GPU interpreter needs "
-                                   f"libcudf 21.08, not installable offline; the oracle restates it in C++)"},
+                         "sample": f"{sample} rows of {w.name} per step, the whole step's rows (the reference's GPU "
+                                   f"interpreter needs libcudf 21.08, not installable offline; the oracle restates "
+                                   f"it in C++)"},
         "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -617,6 +666,8 @@ def main():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--rows", type=int, default=0, help="override rows per step")
     ap.add_argument("--cpu-sample-rows", type=int, default=1 << 22)
+    ap.add_argument("--ref-rows", type=int, default=0, help="reference arm rows per step (default: the workload's)")
+    ap.add_argument("--parity", type=int, default=1, help="compare the whole step's output with the oracle")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=-1, help="filter mode override (0 auto, 1 two-pass, 2 single)")
@@ -748,6 +799,9 @@ def main():
             dist.destroy_process_group()
         return
 
+    # ---- parity of the whole step against the oracle -------------------------
+    parity = full_parity(args.config, w, cols, stream) if args.parity else None
+
     batched = None
     if args.batched_batches > 0:
         if cols is not None:
@@ -797,6 +851,7 @@ def main():
         "cpu_baseline": {"value": cpu_rate, "unit": "rows/s", "cores": nthreads, "kind": "port",
                          "sample": f"{min(args.cpu_sample_rows, n)} rows of {w.name}, {reps} reps in {el:.1f} s"},
         "e2e": e2e,
+        "parity": parity,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "batched": batched,

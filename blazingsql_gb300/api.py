@@ -349,6 +349,15 @@ class Plan:
         N.check(N.lib().gx_plan_execute_noalloc(self._h, views, nc, outs, C.byref(rows), s, C.byref(st)), st)
         return [outs[i] for i in range(len(out))], rows.value
 
+    def wait_test(self, table: Table, first_tile: int, spin_limit: int) -> int:
+        """gx_debug_filter_timeout: runs the plan with the tile ticket starting
+        at ``first_tile`` and bounded waits of ``spin_limit`` polls; returns the
+        status code (GX_ERR_TIMEOUT when a wait gave up)."""
+        keep: list = []
+        views, nc = _views(table, keep)
+        st = N.StatusInfo()
+        return N.lib().gx_debug_filter_timeout(self._h, views, nc, first_tile, spin_limit, C.byref(st))
+
     def kernel_source(self, kind: int = 1, has_mask: Optional[Sequence[bool]] = None) -> str:
         L = N.lib()
         st = N.StatusInfo()

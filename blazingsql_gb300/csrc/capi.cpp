@@ -799,6 +799,26 @@ int gx_debug_kernel_resources(const gx_plan* plan, int kind, const uint8_t* colu
 
 void gx_debug_fail_allocation(int n) { debug_fail_allocation(n); }
 
+int gx_debug_filter_timeout(const gx_plan* plan, const gx_column_view* columns, int num_columns, int64_t first_tile,
+                            uint32_t spin_limit, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!plan) fail(GX_ERR_INVALID, "null plan");
+    const CompiledPlan& cp = *plan->ps->chunks.at(0);
+    if (!cp.plan().has_filter()) fail(GX_ERR_INVALID, "the wait test runs a filter plan");
+    auto cols = to_views(columns, num_columns);
+    std::vector<gx_column> out(cp.plan().outputs.size());
+    for (auto& c : out) std::memset(&c, 0, sizeof c);
+    ExecExtras ex;
+    ex.first_tile = first_tile;
+    ex.spin_limit = spin_limit;
+    int64_t rows = 0;
+    cp.execute(cols, out.data(), &rows, nullptr, &ex);
+    // reached only when no wait gave up: release the outputs
+    for (auto& c : out) free_column(c, nullptr);
+    cudaStreamSynchronize(nullptr);
+  });
+}
+
 void gx_debug_set_kernel_timing(int enable) { set_kernel_timing(enable != 0); }
 
 double gx_debug_kernel_ms(int reset) { return kernel_ms(reset != 0); }

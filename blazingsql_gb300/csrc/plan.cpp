@@ -894,7 +894,10 @@ void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
        "  const void* in_data[GX_MAX_COLS]; const u32* in_mask[GX_MAX_COLS]; i64 in_off[GX_MAX_COLS];\n"
        "  void* out_data[GX_MAX_OUTS]; u32* out_mask[GX_MAX_OUTS];\n"
        "  i64 n; i64 capacity; u64* tile_status; unsigned long long* tile_counter; unsigned long long* out_count;\n"
-       "  int* err; u64 seed; unsigned long long* conj_counts; int order[16]; const int* order_dev;\n};\n";
+       "  int* err; u64 seed; unsigned long long* conj_counts; int order[16]; const int* order_dev;\n"
+       "  u32 spin_limit;\n};\n"
+       // polls a bounded wait makes before it gives up (0: the default)
+       "#define GX_SPINS (a.spin_limit ? a.spin_limit : (1u << 22))\n";
 }
 
 // phase 2 of the filter kernels: projections for the kept rows of each word,
@@ -1166,7 +1169,7 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "    if (warp == 0) {\n";
   o << "      u64 ntotal = 0ull;\n";
   o << "      if (next < ntiles) ntotal = gx_tile_publish(a.tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
-  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, 1u << 22);\n";
+  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, GX_SPINS);\n";
   o << "      if (lane == 0) {\n";
   o << "        s_base = excl;\n";
   o << "        if (tile == ntiles - 1 && excl != ~0ull) *a.out_count = excl + ptotal;\n";
@@ -1470,7 +1473,7 @@ void emit_fused_tma(std::ostringstream& o, const Gen& g, const Plan& p, const Ti
   // start once the block's next tile is counted too: by then the tiles other
   // blocks claimed before this one have mostly published their aggregates
   o << "      gx_mbar_wait(&s_counted_[(j + 1) % GX_RR], (u32)((j + 1) / GX_RR) & 1u, GX_WAIT);\n";
-  o << "      const u64 ex = gx_lookback_wide<8>(a.tile_status, t, agg, a.err, 1u << 22, tk, pk);\n";
+  o << "      const u64 ex = gx_lookback_wide<8>(a.tile_status, t, agg, a.err, GX_SPINS, tk, pk);\n";
   o << "      if (ex != ~0ull) { tk = t; pk = ex + agg; } else { tk = -1; pk = 0ull; }\n";
   o << "      if (lane == 0) {\n";
   o << "        s_base_[b] = ex;\n";
@@ -1647,7 +1650,7 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "      if (next >= 0) ntotal = gx_tile_publish(A[nb].tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
   o << "      const GxArgs& a = A[pb];\n";
   o << "      const i64 ntiles = (((a.n + 31) >> 5) + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
-  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, 1u << 22);\n";
+  o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, GX_SPINS);\n";
   o << "      if (lane == 0) {\n";
   o << "        s_base = excl;\n";
   o << "        if (tile == ntiles - 1 && excl != ~0ull) *a.out_count = excl + ptotal;\n";
@@ -2125,7 +2128,7 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   o << "      #pragma unroll\n      for (int d = 1; d < 32; d <<= 1) { u64 t = __shfl_up_sync(GX_FULL, incl, d); if (lane >= d) incl += t; }\n";
   o << "      const u64 total = __shfl_sync(GX_FULL, incl, 31);\n";
   if (kind == KernelKind::FUSED_FILTER) {
-    o << "      const u64 excl_tile = gx_lookback(a.tile_status, tile, total, a.err, 1u << 22);\n";
+    o << "      const u64 excl_tile = gx_lookback(a.tile_status, tile, total, a.err, GX_SPINS);\n";
     o << "      if (tile == ntiles - 1 && lane == 0 && excl_tile != ~0ull) *a.out_count = excl_tile + total;\n";
   } else if (kind == KernelKind::COUNT_FILTER) {
     o << "      if (lane == 0) a.tile_status[tile] = total;\n";

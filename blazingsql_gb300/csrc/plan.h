@@ -187,6 +187,7 @@ struct KernelArgs {
   unsigned long long* conj_counts;  // COUNT_FILTER with conj_stats: passes per conjunct
   int32_t order[16];                // runtime conjunct order (runtime_order kernels)
   const int32_t* order_dev;         // if set: the order in device memory (written by an earlier kernel)
+  uint32_t spin_limit;              // polls a bounded device wait makes before it gives up (0: default)
 };
 
 }  // namespace gx

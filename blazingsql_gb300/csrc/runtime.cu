@@ -782,6 +782,13 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
       a.conj_counts = extras->conj_counts;
     }
     unsigned long long* host_hdr = pinned_header();
+    if (extras) {
+      a.spin_limit = extras->spin_limit;
+      if (extras->first_tile > 0 && !two_pass) {
+        host_hdr[0] = (unsigned long long)extras->first_tile;
+        check_cuda(cudaMemcpyAsync(hdr, host_hdr, 8, cudaMemcpyHostToDevice, s), "ticket start");
+      }
+    }
     if (two_pass) {
       const JitKernel kc = kernel(KernelKind::COUNT_FILTER, nb);
       int64_t grid = (int64_t)device_sm_count() * kc.max_blocks_per_sm;

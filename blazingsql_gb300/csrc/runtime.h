@@ -64,6 +64,11 @@ struct ExecExtras {
   unsigned long long* conj_counts = nullptr;  // device counters, one per conjunct (conj_stats count pass)
   unsigned long long* conj_counts_host = nullptr;  // optional host copy of them, made before the count sync
   int64_t capacity_hint = -1;              // library-allocated outputs: rows to allocate (-1: all input rows)
+  // diagnostics: the tile ticket starts here, so tiles before it are never
+  // claimed and their look-back status is never published; and the polls a
+  // bounded device wait makes before it gives up (0: default)
+  int64_t first_tile = 0;
+  uint32_t spin_limit = 0;
 };
 
 struct ExecStats {

@@ -247,6 +247,25 @@ def c4_batch_device(n: int, seed: int, batch: int, device: str = "cuda"):
     return cols
 
 
+C2_LAST_DAY = 9861  # 1996-12-31 in days since 1970-01-01, the bound of C2_CONDITION
+
+
+def c2_keep_mask(cols: Sequence[HostColumn]) -> np.ndarray:
+    """Rows of a C2 table that pass C2_CONDITION ($2 valid, $4 valid and on or
+    before 1996-12-31)."""
+    return cols[2].valid() & cols[4].valid() & (cols[4].values() <= C2_LAST_DAY)
+
+
+def c2_transcendental_rows(cols: Sequence[HostColumn]) -> np.ndarray:
+    """For each output row of the C2 plan (the kept rows, in order): whether
+    its first projection takes a CASE branch through LN ($5 NULL) or EXP
+    ($5 = 0).  Only those rows' values come from CUDA's log / exp; every
+    other row is exact binary64 arithmetic and must match bit for bit."""
+    keep = c2_keep_mask(cols)
+    v5, d5 = cols[5].valid()[keep], cols[5].values()[keep]
+    return (~v5) | (d5 == 0)
+
+
 def host_columns(name: str, n: int, seed: int = 1) -> List[HostColumn]:
     """Seeded numpy columns (CPU oracle, parity tests)."""
     return _np_columns(name, n, seed)

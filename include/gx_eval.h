@@ -470,6 +470,17 @@ int gx_debug_kernel_resources(const gx_plan* plan, int kind, const uint8_t* colu
  * this library fails with GX_ERR_OOM (n <= 0 disables). */
 void gx_debug_fail_allocation(int n);
 
+/* Test of the bounded device waits, with no fault and no endless wait: runs a
+ * single-pass filter plan over the columns (library outputs, released again)
+ * with its tile ticket starting at first_tile, so tiles 0 .. first_tile-1 are
+ * never claimed and never publish their look-back status, and with every
+ * bounded wait giving up after spin_limit polls (0: the default).  With
+ * first_tile >= 1 and more rows than first_tile tiles the look-backs of the
+ * claimed tiles cannot finish: the kernel must return and the call report
+ * GX_ERR_TIMEOUT, leaving the device usable. */
+int gx_debug_filter_timeout(const gx_plan* plan, const gx_column_view* columns, int num_columns, int64_t first_tile,
+                            uint32_t spin_limit, gx_status_info* status);
+
 /* JIT statistics: number of NVRTC compilations and their total milliseconds. */
 void gx_debug_jit_stats(int64_t* compiles, double* total_ms);
 

@@ -97,6 +97,33 @@ def assert_columns_equal(got: HostColumn, exp: HostColumn, ulps: float = 0, what
                                f"{e[bad[:5]].tolist()}")
 
 
+def assert_columns_mixed(got: HostColumn, exp: HostColumn, loose_rows: np.ndarray, ulps: float,
+                         what: str = "") -> float:
+    """Validity bit-exact everywhere; float data bit-exact on the valid rows
+    outside ``loose_rows`` and within ``ulps`` on the valid rows inside it (the
+    rows whose value comes from a transcendental).  Returns the largest ulp
+    distance seen on the loose rows."""
+    assert got.type_id == exp.type_id and got.size == exp.size, f"{what}: type/size differ"
+    gv, ev = got.valid(), exp.valid()
+    bad = np.nonzero(gv != ev)[0]
+    assert bad.size == 0, f"{what}: validity differs at rows {bad[:10].tolist()}"
+    loose = np.asarray(loose_rows, dtype=bool)
+    exact = ev & ~loose
+    it = np.int64 if got.values().dtype == np.float64 else np.int32
+    g, e = got.values(), exp.values()
+    bad = np.nonzero(exact & (g.view(it) != e.view(it)))[0]
+    assert bad.size == 0, (f"{what}: {bad.size} exact rows differ, e.g. rows {bad[:5].tolist()}: "
+                           f"{g[bad[:5]].tolist()} vs {e[bad[:5]].tolist()}")
+    lv = ev & loose
+    gl, el = g[lv], e[lv]
+    gn, en = np.isnan(gl), np.isnan(el)
+    assert np.array_equal(gn, en), f"{what}: NaN mismatch on transcendental rows"
+    d = ulp_distance(gl[~gn], el[~en])
+    worst = float(d.max()) if d.size else 0.0
+    assert worst <= ulps, f"{what}: max ulp distance {worst} > {ulps} on transcendental rows"
+    return worst
+
+
 def assert_tables_equal(got: Sequence[HostColumn], exp: Sequence[HostColumn], ulps: float = 0,
                         what: str = "") -> None:
     assert len(got) == len(exp), f"{what}: {len(got)} columns vs {len(exp)}"
