@@ -292,9 +292,31 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
     torch.cuda.synchronize()
     ms_b = e0.elapsed_time(e1) / reps
     bt, words = runner.config()
+    # the runner's own rate per batch-size bucket: the same runner over the
+    # bucket's batches alone
+    runner_buckets = {}
+    for key, lo, hi in (("1K-16K", 0, 16384), ("16K-256K", 16384, 262144), ("256K-4M", 262144, 1 << 40)):
+        sel = [b for b, n in zip(batches, sizes) if lo <= n < hi]
+        nrows = sum(n for n in sizes if lo <= n < hi)
+        if not sel:
+            continue
+        out, _ = runner.run(sel, stream=stream)
+        for o in out:
+            g.api.free_columns(o, stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            out, _ = runner.run(sel, stream=stream)
+            for o in out:
+                g.api.free_columns(o, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        runner_buckets[key] = {"batches": len(sel), "rows": nrows,
+                               "rows_per_s": nrows / (e0.elapsed_time(e1) / reps / 1e3)}
     del batches, cols
     torch.cuda.empty_cache()
     return {
+        "runner_bucket_rows_per_s": runner_buckets,
         "workload": f"c3_batched_deep_plan: {nbatches} batches, log-uniform 1K-4M rows, {total} rows in all",
         "runner_rows_per_s": total / (ms_b / 1e3), "per_batch_calls_rows_per_s": total / (ms_a / 1e3),
         "runner_vs_per_batch_calls": ms_a / ms_b, "runner_ms": ms_b, "per_batch_calls_ms": ms_a,
@@ -302,6 +324,106 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
         "autotuned": {"block_threads": bt, "words_per_warp": words, "vector_width": 1},
         "per_batch_calls_bucket_rows_per_s": {k: (v[0] / v[1] if v[1] > 0 else None) for k, v in buckets.items()},
     }
+
+
+def single_config(name: str, rows: int, reps: int = 10):
+    """One configuration's fused filter + project over resident inputs, one
+    batch per call: rows/s and the kernel's HBM fraction (CUDA events around
+    the kernel inside the library)."""
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
+    from blazingsql_gb300 import workloads as W
+    L = N.lib()
+    stream = torch.cuda.current_stream()
+    w = W.workload(name, rows)
+    cols = W.device_columns(name, rows, seed=1)
+    torch.cuda.synchronize()
+
+    def step():
+        out = g.filter_project(cols, w.condition, w.projections, stream=stream)
+        r = out[0].size
+        g.api.free_columns(out, stream)
+        return r
+
+    for _ in range(4):  # warm-up: JIT and the plan's block-shape trials
+        out_rows = step()
+    torch.cuda.synchronize()
+    L.gx_debug_kernel_ms(1)
+    L.gx_debug_set_kernel_timing(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        out_rows = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    L.gx_debug_set_kernel_timing(0)
+    kms = L.gx_debug_kernel_ms(1) / reps
+    ms = e0.elapsed_time(e1) / reps
+    alg = w.algorithmic_bytes(rows, out_rows)
+    peak, _ = measured_peak_hbm()
+    del cols
+    torch.cuda.empty_cache()
+    return {"workload": f"{w.name}: {rows} rows, one batch per call", "rows_per_s": rows / (ms / 1e3),
+            "ms_per_call": ms, "kernel_ms": kms, "out_rows": out_rows,
+            "roofline": {"bound": "hbm", "achieved": alg / (kms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (kms / 1e3) / 1e9 / peak, "algorithmic_bytes": alg}}
+
+
+def c5_batches(rows: int = 600_000_000, batch_rows: int = 1 << 22, reps: int = 3):
+    """The order-line configuration as it is specified: 600M rows in 4M-row
+    batches (the last one partial), run by the batch runner (one persistent
+    kernel for all batches in a captured CUDA graph), beside one
+    gx_plan_execute call per batch; inputs resident, outputs library-owned."""
+    import torch
+    import blazingsql_gb300 as g
+    from blazingsql_gb300 import workloads as W
+    stream = torch.cuda.current_stream()
+    w = W.workload("c5", rows)
+    cols = W.device_columns("c5", rows, seed=5)
+    sizes = [batch_rows] * (rows // batch_rows) + ([rows % batch_rows] if rows % batch_rows else [])
+    batches = W.slice_batches(cols, sizes)
+    plan = g.Plan(w.schema, w.condition, w.projections)
+    torch.cuda.synchronize()
+    runner = g.BatchRunner(plan, len(sizes), rows, autotune=True)
+    out, r = runner.run(batches, stream=stream)  # tunes on this first run
+    for o in out:
+        g.api.free_columns(o, stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        out, r = runner.run(batches, stream=stream)
+        for o in out:
+            g.api.free_columns(o, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_runner = e0.elapsed_time(e1) / reps
+    out_rows = sum(r)
+    for b in batches[:2]:  # warm the per-call path
+        o, _ = plan.execute(b, stream=stream)
+        g.api.free_columns(o, stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    calls_rows = 0
+    for b in batches:
+        o, rr = plan.execute(b, stream=stream)
+        calls_rows += rr
+        g.api.free_columns(o, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_calls = e0.elapsed_time(e1)
+    alg = w.algorithmic_bytes(rows, out_rows)
+    peak, _ = measured_peak_hbm()
+    bt, words = runner.config()
+    del batches, cols, runner
+    torch.cuda.empty_cache()
+    return {"workload": f"{w.name}: {rows} rows in {len(sizes)} batches of {batch_rows} rows",
+            "runner_rows_per_s": rows / (ms_runner / 1e3), "runner_ms": ms_runner,
+            "per_batch_calls_rows_per_s": rows / (ms_calls / 1e3), "per_batch_calls_ms": ms_calls,
+            "identical_row_counts": calls_rows == out_rows, "out_rows": out_rows,
+            "runner_hbm_frac": alg / (ms_runner / 1e3) / 1e9 / peak,
+            "autotuned": {"block_threads": bt, "words_per_warp": words}}
 
 
 def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
@@ -668,6 +790,8 @@ def main():
     ap.add_argument("--cpu-sample-rows", type=int, default=1 << 22)
     ap.add_argument("--ref-rows", type=int, default=0, help="reference arm rows per step (default: the workload's)")
     ap.add_argument("--parity", type=int, default=1, help="compare the whole step's output with the oracle")
+    ap.add_argument("--c1-rows", type=int, default=1 << 24, help="C1 rows (0 skips the C1 key)")
+    ap.add_argument("--c5-rows", type=int, default=600_000_000, help="C5 rows (0 skips the C5 key)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=-1, help="filter mode override (0 auto, 1 two-pass, 2 single)")
@@ -823,6 +947,20 @@ def main():
             cols = None
             torch.cuda.empty_cache()
         strings = strings_compare(args.string_rows)
+    c1 = None
+    if args.c1_rows > 0:
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
+        c1 = single_config("c1", args.c1_rows)
+    c5 = None
+    if args.c5_rows > 0:
+        if cols is not None:
+            del cols
+            cols = None
+            torch.cuda.empty_cache()
+        c5 = {"single_call": single_config("c5", min(args.c5_rows, 1 << 28)), "batched": c5_batches(args.c5_rows)}
     learned = None
     if args.learned_batches > 0:
         if cols is not None:
@@ -858,6 +996,8 @@ def main():
         "learned": learned,
         "aggregate": aggregate,
         "strings": strings,
+        "c1": c1,
+        "c5": c5,
     }
     print(json.dumps(line), flush=True)
     if dist:
