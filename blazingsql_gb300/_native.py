@@ -139,6 +139,9 @@ def lib():
                                             P(C.c_int32), P(StatusInfo)]
     L.gx_debug_fail_allocation.argtypes = [C.c_int]
     L.gx_debug_fail_allocation.restype = None
+    L.gx_set_current_timestamp.argtypes = [C.c_char_p, P(StatusInfo)]
+    L.gx_debug_preprocess_expression.argtypes = [C.c_char_p, P(C.c_int32), C.c_int, C.c_int, C.c_char_p, C.c_int,
+                                                 P(StatusInfo)]
     L.gx_debug_filter_timeout.argtypes = [C.c_void_p, P(ColumnView), C.c_int, C.c_int64, C.c_uint32, P(StatusInfo)]
     L.gx_debug_jit_stats.argtypes = [P(C.c_int64), P(C.c_double)]
     L.gx_debug_jit_stats.restype = None
@@ -192,7 +195,8 @@ EXPORTED_SYMBOLS = [
     "gx_column_to_host", "gx_string_offsets_to_host", "gx_debug_like_automaton", "gx_plan_options_init", "gx_plan_compile", "gx_plan_num_outputs", "gx_plan_output_type",
     "gx_plan_num_conjuncts", "gx_plan_execute", "gx_plan_execute_noalloc", "gx_plan_destroy", "gx_version",
     "gx_debug_kernel_source",
-    "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_filter_timeout", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
+    "gx_debug_compile_check", "gx_debug_fail_allocation", "gx_debug_filter_timeout", "gx_set_current_timestamp",
+    "gx_debug_preprocess_expression", "gx_debug_jit_stats", "gx_debug_rebuild_expression",
     "gx_debug_set_kernel_timing", "gx_debug_kernel_ms", "gx_debug_launch_count",
     "gx_learner_options_init", "gx_learner_create", "gx_learner_execute", "gx_learner_prepare", "gx_learner_save",
     "gx_learner_execute_batches", "gx_plan_execute_host", "gx_filter_aggregate", "gx_debug_aggregate_check",

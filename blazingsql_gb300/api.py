@@ -701,6 +701,23 @@ def free_columns(cols: Sequence[NativeColumn], stream=None) -> None:
         c._c.null_mask = None
 
 
+def set_current_timestamp(timestamp: Optional[str]) -> None:
+    """The calling thread's query timestamp for CURRENT_DATE / CURRENT_TIMESTAMP
+    ("YYYY-MM-DD hh:mm:ss[.fraction]"; None clears it)."""
+    st = N.StatusInfo()
+    N.check(N.lib().gx_set_current_timestamp(timestamp.encode() if timestamp else None, C.byref(st)), st)
+
+
+def preprocess(expression: str, schema: Sequence[int] = (), stages: int = 31) -> str:
+    """preprocess_expression's text rewrites (gx_debug_preprocess_expression)."""
+    st = N.StatusInfo()
+    buf = C.create_string_buffer(8192)
+    types = (C.c_int32 * max(1, len(schema)))(*[int(t) for t in schema])
+    N.check(N.lib().gx_debug_preprocess_expression(expression.encode(), types, len(schema), stages, buf, 8192,
+                                                   C.byref(st)), st)
+    return buf.value.decode()
+
+
 def version() -> str:
     return N.lib().gx_version().decode()
 

@@ -825,6 +825,20 @@ double gx_debug_kernel_ms(int reset) { return kernel_ms(reset != 0); }
 
 int64_t gx_debug_launch_count(void) { return launch_count(); }
 
+int gx_set_current_timestamp(const char* timestamp, gx_status_info* status) {
+  return guarded(status, [&] { set_current_timestamp(timestamp ? std::string(timestamp) : std::string()); });
+}
+
+int gx_debug_preprocess_expression(const char* expression, const int32_t* column_types, int num_columns, int stages,
+                                   char* buf, int buf_len, gx_status_info* status) {
+  return guarded(status, [&] {
+    if (!expression || !buf || buf_len <= 0 || num_columns < 0 || (num_columns > 0 && !column_types))
+      fail(GX_ERR_INVALID, "bad arguments");
+    std::vector<int> schema(column_types, column_types + num_columns);
+    std::snprintf(buf, (size_t)buf_len, "%s", preprocess_stages(expression, schema, stages).c_str());
+  });
+}
+
 int gx_debug_rebuild_expression(const char* expression, char* buf, int buf_len, gx_status_info* status) {
   return guarded(status, [&] {
     if (!expression || !buf || buf_len <= 0) fail(GX_ERR_INVALID, "bad arguments");

@@ -791,26 +791,79 @@ void split_projections(const std::string& plan, std::vector<std::string>& names,
   }
 }
 
+namespace {
+thread_local std::string t_current_timestamp;  // the calling thread's query timestamp ("" = none)
+
+std::string replaced_all(std::string s, const std::string& from, const std::string& to) {
+  size_t p = 0;
+  while ((p = s.find(from, p)) != std::string::npos) {
+    s.replace(p, from.size(), to);
+    p += to.size();
+  }
+  return s;
+}
+}  // namespace
+
+void set_current_timestamp(const std::string& ts) {
+  if (!ts.empty()) {
+    // "YYYY-MM-DD hh:mm:ss[.f...]": the form the engine Context keeps
+    auto digits = [&](size_t a, size_t n) {
+      for (size_t i = a; i < a + n; i++)
+        if (i >= ts.size() || ts[i] < '0' || ts[i] > '9') return false;
+      return true;
+    };
+    const bool ok = ts.size() >= 19 && digits(0, 4) && ts[4] == '-' && digits(5, 2) && ts[7] == '-' &&
+                    digits(8, 2) && ts[10] == ' ' && digits(11, 2) && ts[13] == ':' && digits(14, 2) &&
+                    ts[16] == ':' && digits(17, 2) && (ts.size() == 19 || (ts[19] == '.' && digits(20, ts.size() - 20)));
+    if (!ok) fail(GX_ERR_INVALID, "current timestamp must look like YYYY-MM-DD hh:mm:ss[.fraction]: " + ts);
+  }
+  t_current_timestamp = ts;
+}
+
+std::string current_timestamp() { return t_current_timestamp; }
+
 std::string preprocess_expression(const std::string& text, const std::vector<int>& schema) {
+  return preprocess_stages(text, schema, kPreAll);
+}
+
+std::string preprocess_stages(const std::string& text, const std::vector<int>& schema, int stages) {
   std::string e = text;
   // fill_minus_op_with_zero (expression_utils.cpp:1155-1164)
-  size_t dollars = 0;
-  for (char c : e) dollars += c == '$';
-  if (!e.empty() && e[0] == '-' && dollars == 1 && e.find(',') == std::string::npos && e.size() >= 2)
-    e = e.substr(0, 2) + "0, " + e.substr(2);
+  if (stages & kPreMinus) {
+    size_t dollars = 0;
+    for (char c : e) dollars += c == '$';
+    if (!e.empty() && e[0] == '-' && dollars == 1 && e.find(',') == std::string::npos && e.size() >= 2)
+      e = e.substr(0, 2) + "0, " + e.substr(2);
+  }
   // convert_nary_to_binary_concat (:1620) happens in the string pre-pass
   // (rewrite_string_ops nests an n-ary CONCAT before evaluating it)
-  if (e.find("CURRENT_DATE") != std::string::npos || e.find("CURRENT_TIME") != std::string::npos)
-    fail(GX_ERR_UNSUPPORTED, "CURRENT_DATE/CURRENT_TIMESTAMP need an engine context");
+  // get_current_date_or_timestamp (expression_utils.cpp:1494-1518): the
+  // query's timestamp replaces CURRENT_TIMESTAMP (to milliseconds) or
+  // CURRENT_DATE (the date); CURRENT_TIME means CURRENT_TIMESTAMP; when both
+  // appear only CURRENT_DATE is replaced, as there
+  if ((stages & kPreCurrent) &&
+      (e.find("CURRENT_DATE") != std::string::npos || e.find("CURRENT_TIME") != std::string::npos)) {
+    if (t_current_timestamp.empty())
+      fail(GX_ERR_UNSUPPORTED,
+           "CURRENT_DATE/CURRENT_TIMESTAMP need the query's timestamp: set it with gx_set_current_timestamp");
+    if (e.find("CURRENT_TIMESTAMP") == std::string::npos) e = replaced_all(e, "CURRENT_TIME", "CURRENT_TIMESTAMP");
+    std::string ts = t_current_timestamp.substr(0, 23), what = "CURRENT_TIMESTAMP";
+    if (e.find("CURRENT_DATE") != std::string::npos) {
+      what = "CURRENT_DATE";
+      ts = ts.substr(0, 10);
+    }
+    e = replaced_all(e, what, ts);
+  }
   // convert_ms_to_ns_units (expression_utils.cpp:1316-1350)
-  const bool cast_ts = e.find("CAST(") != std::string::npos && e.find(":TIMESTAMP") != std::string::npos;
-  const bool cast_dt = e.find("CAST(") != std::string::npos && e.find(":DATE") != std::string::npos;
+  const bool ms_ns = (stages & kPreMsToNs) != 0;
+  const bool cast_ts = ms_ns && e.find("CAST(") != std::string::npos && e.find(":TIMESTAMP") != std::string::npos;
+  const bool cast_dt = ms_ns && e.find("CAST(") != std::string::npos && e.find(":DATE") != std::string::npos;
   if (cast_ts || cast_dt) {
     bool done = false;
     if (e.find("Reinterpret(") != std::string::npos) {
       for (const char* u : {"86400000", "3600000", "60000", "1000"}) {
         if (e.find(u) != std::string::npos) {
-          e = replace_first(e, u, std::string(u) + "000000");
+          e = replaced_all(e, u, std::string(u) + "000000");
           done = true;
           break;
         }
@@ -820,13 +873,13 @@ std::string preprocess_expression(const std::string& text, const std::vector<int
     if (!done && ip != std::string::npos) {
       size_t sp = e.find(", ") + 2;
       std::string tv = e.substr(sp, ip - sp);
-      e = replace_first(e, tv, tv + "000000");
+      e = replaced_all(e, tv, tv + "000000");
     }
   }
   if (schema.empty()) return e;
   // reinterpret_timestamp (expression_utils.cpp:1371-1420)
   const std::string key = "Reinterpret(-(";
-  size_t rp = e.find(key);
+  size_t rp = (stages & kPreReinterpret) ? e.find(key) : std::string::npos;
   if (rp != std::string::npos) {
     std::string red = e.substr(rp + key.size());
     red = red.substr(0, red.find("))"));
@@ -848,13 +901,13 @@ std::string preprocess_expression(const std::string& text, const std::vector<int
         const char* unit = schema[col] == TIMESTAMP_SECONDS ? "TIMESTAMP_SECONDS"
                          : schema[col] == TIMESTAMP_MILLISECONDS ? "TIMESTAMP_MILLISECONDS"
                          : schema[col] == TIMESTAMP_MICROSECONDS ? "TIMESTAMP_MICROSECONDS" : "TIMESTAMP";
-        e = replace_first(e, ts, "CAST(" + ts + "):" + unit);
+        e = replaced_all(e, ts, "CAST(" + ts + "):" + unit);
       }
     }
   }
   // apply_interval_conversion (expression_utils.cpp:1425-1460)
   const std::string iv = ":INTERVAL";
-  if (e.find(iv) != std::string::npos) {
+  if ((stages & kPreInterval) && e.find(iv) != std::string::npos) {
     if (e.find('+') != std::string::npos || e.find('-') != std::string::npos) {
       size_t sp = 0;
       if (e.find("+($") != std::string::npos) sp = e.find("+($") + 3;
@@ -863,11 +916,11 @@ std::string preprocess_expression(const std::string& text, const std::vector<int
       ne = ne.substr(0, ne.find(", "));
       long long col = parse_ll(ne, 0, INT32_MAX);
       if ((size_t)col >= schema.size()) fail(GX_ERR_PARSE, "column index out of range in interval");
-      if (schema[col] == DURATION_SECONDS) e = replace_first(e, "000" + iv, iv);
-      else if (schema[col] == DURATION_MICROSECONDS) e = replace_first(e, "000" + iv, "000000" + iv);
-      else if (schema[col] == DURATION_NANOSECONDS) e = replace_first(e, "000" + iv, "000000000" + iv);
+      if (schema[col] == DURATION_SECONDS) e = replaced_all(e, "000" + iv, iv);
+      else if (schema[col] == DURATION_MICROSECONDS) e = replaced_all(e, "000" + iv, "000000" + iv);
+      else if (schema[col] == DURATION_NANOSECONDS) e = replaced_all(e, "000" + iv, "000000000" + iv);
     } else if (e.find('$') == std::string::npos && e.find("000:INTERVAL") != std::string::npos) {
-      e = replace_first(e, "000" + iv, iv);
+      e = replaced_all(e, "000" + iv, iv);
     }
   }
   return e;

@@ -40,6 +40,17 @@ ExprPtr compile_expression(const std::string& text, const std::vector<int>& sche
 
 // preprocess_expression (expression_utils.cpp:1624-1632)
 std::string preprocess_expression(const std::string& text, const std::vector<int>& schema);
+// the same with only some of its rewrites: unary minus, CURRENT_DATE /
+// CURRENT_TIMESTAMP, millisecond-to-nanosecond units, Reinterpret casts,
+// interval units (expression_utils.cpp:1155-1164, 1494-1518, 1316-1350,
+// 1371-1420, 1425-1460)
+constexpr int kPreMinus = 1, kPreCurrent = 2, kPreMsToNs = 4, kPreReinterpret = 8, kPreInterval = 16, kPreAll = 31;
+std::string preprocess_stages(const std::string& text, const std::vector<int>& schema, int stages);
+// The calling thread's query timestamp ("YYYY-MM-DD hh:mm:ss[.fraction]", as the
+// engine Context keeps it, Context.h:47; empty: none), which CURRENT_DATE,
+// CURRENT_TIME and CURRENT_TIMESTAMP take in the calls that thread makes.
+void set_current_timestamp(const std::string& ts);
+std::string current_timestamp();
 
 // get_named_expression (expression_utils.cpp:537-547)
 std::string named_expression(const std::string& query_part, const std::string& name);

@@ -915,15 +915,19 @@ void CompiledPlan::execute_with_scratch(const std::vector<ColumnView>& cols, gx_
   a.err = (int*)(scratch + 2);
   a.seed = plan_.rand_seed;
   a.capacity = capacity;
+  for (int i = 0; i < 16; i++) a.order[i] = i;  // plan order (as run_filter)
   for (int j = 0; j < nout; j++) {
     a.out_data[j] = out[j].data;
     a.out_mask[j] = out[j].null_mask;
   }
+  // the configured block shape (cfg_.warps x cfg_.words, 512-row tiles by
+  // default), never the online-tuned one: the scratch's tile limit is fixed
   const JitKernel k = kernel(KernelKind::FUSED_FILTER, runtime_nullable(plan_, cols));
   int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
   if (grid > ntiles) grid = ntiles;
   launch(k, (int)grid, s, a, true);
-  unsigned long long* host_hdr = pinned_header();
+  // read back into this frame, not a pinned block: this path allocates nothing
+  unsigned long long host_hdr[4] = {0, 0, 0, 0};
   check_cuda(cudaMemcpyAsync(host_hdr, scratch, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
   check_cuda(cudaStreamSynchronize(s), "filter sync");
   raise_kernel_error(host_hdr[2]);

@@ -125,6 +125,16 @@ int gx_filter_project(const gx_column_view* columns, int num_columns, const char
                       const char* const* expressions, int num_expressions,
                       gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
 
+/* The query's current timestamp, "YYYY-MM-DD hh:mm:ss[.fraction]" (the value
+ * BlazingSQL's engine Context keeps, Context::getCurrentTimestamp,
+ * engine/src/execution_graph/Context.h:47), for the calls the calling thread
+ * makes afterwards: CURRENT_TIMESTAMP (and CURRENT_TIME) becomes it to the
+ * millisecond and CURRENT_DATE its date, as get_current_date_or_timestamp does
+ * (engine/src/parser/expression_utils.cpp:1494-1518).  NULL or "" clears it;
+ * without one such expressions are rejected with GX_ERR_UNSUPPORTED.  It stands
+ * in for the Context* the reference's process_filter / process_project take. */
+int gx_set_current_timestamp(const char* timestamp, gx_status_info* status);
+
 /* Releases columns returned by this library (stream-ordered). */
 void gx_free_columns(gx_column* columns, int num_columns, void* stream);
 
@@ -195,15 +205,23 @@ int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_
  * an engine whose own memory pool owns the whole device budget (allocations
  * made outside it break its accounting, and fail once it has reserved the
  * rest of the GPU), or a per-batch path that must not enter an allocator.
- * Same kernel and results as gx_plan_execute in GX_FILTER_SINGLE_PASS mode;
- * the kernel's scratch (row-count, ticket and error words plus one status word
- * per tile, 512 rows by default) comes from a fixed 4 MiB array in the library's device
- * memory that every GPU loading the library keeps until the process exits.
+ * Same results as gx_plan_execute in GX_FILTER_SINGLE_PASS mode, from the same
+ * direct-load fused filter kernel at the configured block shape (4 warps x 4
+ * words, 512-row tiles, unless GX_WARPS / GX_WORDS say otherwise; never the
+ * shape gx_plan_execute may pick online); the kernel's scratch (row-count,
+ * ticket and error words plus one status word per tile) comes from a fixed
+ * 4 MiB array in the library's device memory that every GPU loading the library
+ * keeps until the process exits.
  *
  * - out[i].data, out[i].null_mask and out[i].capacity must be set by the
  *   caller; null_mask must hold ((capacity + 511) / 512) * 64 bytes (>= 64).
  * - Batches needing more than GX_NOALLOC_MAX_TILES tiles (more than
- *   268,433,408 rows with the default tile) are rejected with GX_ERR_INVALID.
+ *   268,433,408 rows with the default 512-row tile) are rejected with
+ *   GX_ERR_INVALID.  When the selected rows exceed the outputs' capacity the
+ *   call returns GX_ERR_CAPACITY with the needed count in *out_rows and writes
+ *   nothing past the buffers.
+ * - The call waits for its stream to finish the batch before it returns (it
+ *   reads the row count back into host memory of its own stack frame).
  * - All calls share the one array (it keeps the last call's contents and is
  *   cleared at the start of each call), so calls whose work overlaps on the
  *   GPU -- on different streams or host threads at the same time -- race:
@@ -493,6 +511,13 @@ double gx_debug_kernel_ms(int reset);
 
 /* Number of device kernels this library has launched (all threads). */
 int64_t gx_debug_launch_count(void);
+
+/* The text rewrites of preprocess_expression (engine/src/parser/expression_utils.cpp:1624-1632) on one
+ * expression for a column schema, only those in `stages`: 1 unary minus, 2 CURRENT_DATE /
+ * CURRENT_TIMESTAMP, 4 millisecond-to-nanosecond units, 8 Reinterpret casts, 16 interval units
+ * (31: all, as every entry point applies them). */
+int gx_debug_preprocess_expression(const char* expression, const int32_t* column_types, int num_columns, int stages,
+                                   char* buf, int buf_len, gx_status_info* status);
 
 /* Parses and lowers one RexNode expression (normalisation, AND/OR nesting,
  * CASE / ROUND / CAST-literal lowering) and writes it back as text, the way the

@@ -217,6 +217,17 @@ static std::string replace_first(const std::string& s, const std::string& from, 
   if (p != std::string::npos) r.replace(p, from.size(), to);
   return r;
 }
+// StringUtil::replace (io/src/Util/StringUtil.cpp:371-380): every occurrence,
+// left to right, scanning on after each replacement
+static std::string string_replace(const std::string& s, const std::string& from, const std::string& to) {
+  std::string r = s;
+  size_t p = 0;
+  while ((p = r.find(from, p)) != std::string::npos) {
+    r.replace(p, from.size(), to);
+    p += to.size();
+  }
+  return r;
+}
 static std::string ltrim(const std::string& s) {
   size_t i = 0;
   while (i < s.size() && std::isspace((unsigned char)s[i])) i++;
@@ -402,14 +413,14 @@ static std::string convert_ms_to_ns_units(std::string e) {
   const std::string ns = "000000";
   if (e.find("Reinterpret(") != std::string::npos) {
     for (const char* u : {"86400000", "3600000", "60000", "1000"}) {
-      if (e.find(u) != std::string::npos) return replace_first(e, u, std::string(u) + ns);
+      if (e.find(u) != std::string::npos) return string_replace(e, u, std::string(u) + ns);
     }
   }
   size_t ip = e.find(":INTERVAL");
   if (ip != std::string::npos) {
     size_t sp = e.find(", ") + 2;
     std::string tv = e.substr(sp, ip - sp);
-    return replace_first(e, tv, tv + ns);
+    return string_replace(e, tv, tv + ns);
   }
   return e;
 }
@@ -458,7 +469,7 @@ static std::string reinterpret_timestamp(std::string e, const std::vector<int>& 
   const char* unit = schema[col] == TIMESTAMP_SECONDS ? "TIMESTAMP_SECONDS"
                    : schema[col] == TIMESTAMP_MILLISECONDS ? "TIMESTAMP_MILLISECONDS"
                    : schema[col] == TIMESTAMP_MICROSECONDS ? "TIMESTAMP_MICROSECONDS" : "TIMESTAMP";
-  return replace_first(e, ts, "CAST(" + ts + "):" + unit);
+  return string_replace(e, ts, "CAST(" + ts + "):" + unit);
 }
 
 // apply_interval_conversion (expression_utils.cpp:1425-1460)
@@ -473,12 +484,12 @@ static std::string apply_interval_conversion(std::string e, const std::vector<in
     ne = ne.substr(0, ne.find(", "));
     int col = std::stoi(ne);
     if (col < 0 || (size_t)col >= schema.size()) throw Error(E_PARSE, "column index out of range in interval");
-    if (schema[col] == DURATION_SECONDS) return replace_first(e, "000" + iv, iv);
-    if (schema[col] == DURATION_MICROSECONDS) return replace_first(e, "000" + iv, "000000" + iv);
-    if (schema[col] == DURATION_NANOSECONDS) return replace_first(e, "000" + iv, "000000000" + iv);
+    if (schema[col] == DURATION_SECONDS) return string_replace(e, "000" + iv, iv);
+    if (schema[col] == DURATION_MICROSECONDS) return string_replace(e, "000" + iv, "000000" + iv);
+    if (schema[col] == DURATION_NANOSECONDS) return string_replace(e, "000" + iv, "000000000" + iv);
     return e;
   }
-  if (e.find("$") == std::string::npos && e.find("000:INTERVAL") != std::string::npos) return replace_first(e, "000" + iv, iv);
+  if (e.find("$") == std::string::npos && e.find("000:INTERVAL") != std::string::npos) return string_replace(e, "000" + iv, iv);
   return e;
 }
 

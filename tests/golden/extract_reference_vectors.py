@@ -118,6 +118,25 @@ def extract(root):
         if e:
             pairs.append({"input": e.group(1), "expected": x.group(1) if x else e.group(1)})
     out["fill_minus_op_with_zero"] = {"source": f"{eu}:243-278", "pairs": pairs}
+    # preprocess rewrites: convert_ms_to_ns_units and reinterpret_timestamp,
+    # each test's input, expected text (its input when it expects no change)
+    # and schema (cudf type names, in order)
+    text = "\n".join(L)
+    pre = []
+    for m in re.finditer(r"TEST_F\(ExpressionUtilsTest, (\w+)\)", text):
+        nxt = text.find("TEST_F(", m.end())
+        blk = text[m.start():nxt if nxt >= 0 else len(text)]
+        fn = re.search(r"out_expression = (convert_ms_to_ns_units|reinterpret_timestamp)\(", blk)
+        if not fn:
+            continue
+        inp = re.search(r'std::string expression = "(.*)";', blk).group(1)
+        exp = re.search(r'std::string expected_str = "(.*)";', blk)
+        first = text.count("\n", 0, m.start()) + 1
+        pre.append({"name": m.group(1), "function": fn.group(1), "input": inp,
+                    "expected": exp.group(1) if exp else inp,
+                    "schema": re.findall(r"cudf::type_id::(\w+)", blk),
+                    "source": f"{eu}:{first}-{first + blk.count(chr(10))}"})
+    out["preprocess_rewrites"] = pre
     gq = [i for i, l in enumerate(L) if "getting_query_part" in l][0]
     blk = "\n".join(L[gq:gq + 14])
     out["get_query_part"] = {"source": f"{eu}:{gq + 1}-{gq + 14}",

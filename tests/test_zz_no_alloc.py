@@ -66,12 +66,48 @@ def test_noalloc_matches_regular_entry_point(workload):
         del keep
 
 
+def _tile_rows():
+    """Rows per tile of the no-allocation path: its configured block shape."""
+    import os
+    return int(os.environ.get("GX_WARPS") or 4) * int(os.environ.get("GX_WORDS") or 4) * 32
+
+
+def test_noalloc_capacity_too_small_writes_nothing_past_the_buffers():
+    torch = pytest.importorskip("torch")
+    w = W.workload("c1")
+    plan = g.Plan(w.schema, w.condition, w.projections)
+    n = 50_000
+    cols = W.host_columns("c1", n, seed=9)
+    dev = [g.DeviceColumn.from_host(c) for c in cols]
+    _, need = plan.execute(dev)
+    cap = need // 2
+    canary, keep, bufs = 64, [], []
+    for t in plan.output_types():
+        dbytes = cap * np_dtype(t).itemsize
+        mbytes = max(64, (cap + 511) // 512 * 64)
+        d = torch.full((dbytes + canary,), 0xAB, dtype=torch.uint8, device="cuda")
+        m = torch.full((mbytes + canary,), 0xAB, dtype=torch.uint8, device="cuda")
+        keep.append((d, m, dbytes, mbytes))
+        bufs.append(N.Column(t, 0, d.data_ptr(), m.data_ptr(), 0, cap))
+    keep_v: list = []
+    views, nc = g.api._views(dev, keep_v)
+    outs = (N.Column * len(bufs))(*bufs)
+    rows = C.c_int64(0)
+    st = N.StatusInfo()
+    rc = N.lib().gx_plan_execute_noalloc(plan._h, views, nc, outs, C.byref(rows), None, C.byref(st))
+    assert rc == N.GX_ERR_CAPACITY
+    assert rows.value == need
+    for d, m, dbytes, mbytes in keep:
+        assert (d[dbytes:].cpu().numpy() == 0xAB).all(), "data written past the caller's buffer"
+        assert (m[mbytes:].cpu().numpy() == 0xAB).all(), "mask written past the caller's buffer"
+
+
 def test_noalloc_rejects_oversized_batch():
     torch = pytest.importorskip("torch")
     w = W.workload("c1")
     plan = g.Plan(w.schema, w.condition, w.projections)
     tiny = torch.zeros(64, dtype=torch.uint8, device="cuda")
-    too_many = N.GX_NOALLOC_MAX_ROWS + 1
+    too_many = N.GX_NOALLOC_MAX_TILES * _tile_rows() + 1
     views = [g.DeviceColumn(t, tiny, None, 0, too_many) for t in w.schema]
     keep, bufs = _caller_buffers(torch, plan.output_types(), 16)
     with pytest.raises(g.GxError) as ei:
