@@ -876,6 +876,29 @@ class Gen {
   // tile-staged kernels: every column is read from the tile's shared-memory
   // stage (row trow of the tile; see emit_fused_tma)
   mutable bool tile_mode_ = false;
+
+  // validity of node id is true for every row in range (no NULL can arise):
+  // non-nullable columns, valid literals, and operators that propagate only
+  // their operands' validity or divide by a nonzero literal
+  bool never_null(int id) const {
+    const Node& n = p_.nodes[id];
+    if (n.kind == Node::LIT) return n.lit_valid;
+    if (n.kind == Node::COL) return !p_.nullable[n.col];
+    switch (n.op) {
+      case OP_RAND: case OP_ROW_INDEX:
+      case OP_IS_NOT_TRUE: case OP_IS_NOT_FALSE: case OP_IS_NULL: case OP_IS_NOT_NULL: case OP_IS_NOT_DISTINCT_FROM:
+        return true;
+      case OP_MAGIC_IF_NOT: return false;
+      default: break;
+    }
+    if (op_is_unary(n.op)) return never_null(n.a);
+    if (!never_null(n.a) || !never_null(n.b)) return false;
+    if (n.op == OP_DIV || (n.op == OP_MOD && !kind_f(n.a) && !kind_f(n.b))) {
+      const Node& d = p_.nodes[n.b];
+      return d.kind == Node::LIT && d.lit_valid && (d.lit_bits & 0x7fffffffffffffffull) != 0;
+    }
+    return true;
+  }
 };
 
 void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
@@ -901,25 +924,23 @@ void emit_prelude(std::ostringstream& o, const KernelConfig& cfg) {
 }
 
 // phase 2 of the filter kernels: projections for the kept rows of each word,
-// written at positions pos.. (warp-uniform), plus validity bit streams
-// stores + validity of output j for the current lane (dense rounds)
-void emit_dense_store(std::ostringstream& o, const Gen& g, const Plan& p, size_t j, const std::string& ind) {
+// written at positions pos.. (warp-uniform), plus validity bit streams.
+// Stores output j for the current lane (dense rounds) and returns its validity
+// expression for the round's ballot ("" for a broadcast output, filled after
+// the launch).
+std::string emit_dense_store(std::ostringstream& o, const Gen& g, const Plan& p, size_t j, const std::string& ind) {
   const OutSpec& os = p.outputs[j];
-  std::string vexpr;
   if (os.kind == OutSpec::NODE) {
     o << ind << "if (wr) " << store_stmt(os.type, "a.out_data[" + std::to_string(j) + "]", "orow", g.B(os.node)) << "\n";
-    vexpr = g.V(os.node);
-  } else if (os.kind == OutSpec::COPY) {
-    const int c = os.col;
-    const std::string rt = raw_type(p.schema[c]);
-    o << ind << "if (wr) ((" << rt << "*)a.out_data[" << j << "])[orow] = __ldcs((const " << rt << "*)a.in_data[" << c
-      << "] + a.in_off[" << c << "] + row);\n";
-    vexpr = p.nullable[c] ? "gx_valid(a.in_mask[" + std::to_string(c) + "], a.in_off[" + std::to_string(c) + "] + row)"
-                          : "true";
-  } else {
-    return;  // broadcast outputs are filled after the launch
+    return g.V(os.node);
   }
-  o << ind << "acc_[" << j << "] |= (u64)__ballot_sync(GX_FULL, act && " << vexpr << ") << bf_;\n";
+  if (os.kind != OutSpec::COPY) return "";
+  const int c = os.col;
+  const std::string rt = raw_type(p.schema[c]);
+  o << ind << "if (wr) ((" << rt << "*)a.out_data[" << j << "])[orow] = __ldcs((const " << rt << "*)a.in_data[" << c
+    << "] + a.in_off[" << c << "] + row);\n";
+  return p.nullable[c] ? "gx_valid(a.in_mask[" + std::to_string(c) + "], a.in_off[" + std::to_string(c) + "] + row)"
+                       : "true";
 }
 
 // outputs that carry a validity bit stream (broadcasts are filled after the launch)
@@ -1036,11 +1057,25 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
     o << ind << "__syncwarp();\n";
   }
   // validity bit streams: one position shared by all outputs (every round
-  // appends the same number of bits to each), one accumulator per output; the
-  // first word may be shared with the previous warp's range and the last with
-  // the next one (atomicOr), words in between are stored
-  o << ind << "u64 acc_[" << p.outputs.size() << "];\n";
-  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << p.outputs.size() << "; j++) acc_[j] = 0ull;\n";
+  // appends the same number of bits to each), one accumulator per output
+  // whose validity varies and one shared by the outputs that are never NULL;
+  // the first word may be shared with the previous warp's range and the last
+  // with the next one (atomicOr), words in between are stored
+  const std::vector<size_t> mo = masked_outputs(p);
+  std::vector<int> slot(p.outputs.size(), -1);
+  int nslots = 0, nn_slot = -1;
+  for (size_t j : mo) {
+    const OutSpec& os = p.outputs[j];
+    if (os.kind == OutSpec::COPY ? !p.nullable[os.col] : g.never_null(os.node)) {
+      if (nn_slot < 0) nn_slot = nslots++;
+      slot[j] = nn_slot;
+    } else {
+      slot[j] = nslots++;
+    }
+  }
+  const int nacc = std::max(nslots, 1);
+  o << ind << "u64 acc_[" << nacc << "];\n";
+  o << ind << "#pragma unroll\n" << ind << "for (int j = 0; j < " << nacc << "; j++) acc_[j] = 0ull;\n";
   o << ind << "int bf_ = (int)(pos & 31ull); i64 bword_ = (i64)(pos >> 5); bool bfirst_ = bf_ != 0;\n";
   o << ind << "const i64 cap_words = (a.capacity + 31) >> 5;\n";
   o << ind << "for (u32 base_ = 0; base_ < total_; base_ += 32u) {\n";
@@ -1050,22 +1085,29 @@ void emit_filter_writes_dense(std::ostringstream& o, const Gen& g, const Plan& p
   emit_row_nodes(o, g, p, proj, lz_root, in2);
   o << in2 << "const bool wr = act && orow < a.capacity;\n";
   o << in2 << "const int nb = (int)min(32u, total_ - base_);\n";
-  for (size_t j = 0; j < p.outputs.size(); j++) emit_dense_store(o, g, p, j, in2);
-  const std::vector<size_t> mo = masked_outputs(p);
+  std::vector<std::string> vexpr(p.outputs.size());
+  for (size_t j = 0; j < p.outputs.size(); j++) vexpr[j] = emit_dense_store(o, g, p, j, in2);
+  for (int sl = 0; sl < nslots; sl++) {
+    std::string e = "act";
+    if (sl != nn_slot)
+      for (size_t j : mo)
+        if (slot[j] == sl) e = "act && " + vexpr[j];
+    o << in2 << "acc_[" << sl << "] |= (u64)__ballot_sync(GX_FULL, " << e << ") << bf_;\n";
+  }
   o << in2 << "const int nf_ = bf_ + nb;\n";
   o << in2 << "if (nf_ >= 32) {\n";
   o << in2 << "  if (lane == 0 && bword_ < cap_words) {\n";
   for (size_t j : mo)
-    o << in2 << "    if (bfirst_) atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]); else a.out_mask[" << j
-      << "][bword_] = (u32)acc_[" << j << "];\n";
+    o << in2 << "    if (bfirst_) atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << slot[j] << "]); else a.out_mask["
+      << j << "][bword_] = (u32)acc_[" << slot[j] << "];\n";
   o << in2 << "  }\n";
-  o << in2 << "  #pragma unroll\n" << in2 << "  for (int j = 0; j < " << p.outputs.size() << "; j++) acc_[j] >>= 32;\n";
+  o << in2 << "  #pragma unroll\n" << in2 << "  for (int j = 0; j < " << nacc << "; j++) acc_[j] >>= 32;\n";
   o << in2 << "  bfirst_ = false; bword_++; bf_ = nf_ - 32;\n";
   o << in2 << "} else {\n" << in2 << "  bf_ = nf_;\n" << in2 << "}\n";
   o << ind << "}\n";
   o << ind << "__syncwarp();\n";  // the kept-row list and branch results are rewritten by the next tile
   o << ind << "if (bf_ > 0 && lane == 0 && bword_ < cap_words) {\n";
-  for (size_t j : mo) o << ind << "  atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << j << "]);\n";
+  for (size_t j : mo) o << ind << "  atomicOr(a.out_mask[" << j << "] + bword_, (u32)acc_[" << slot[j] << "]);\n";
   o << ind << "}\n";
 }
 

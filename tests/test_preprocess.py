@@ -73,7 +73,9 @@ def test_current_date_evaluates_as_the_literal():
     cols = [HostColumn(T.TIMESTAMP_DAYS, days), HostColumn(T.TIMESTAMP_MILLISECONDS, ms)]
     g.api.set_current_timestamp("2021-05-14 10:11:12.345678")
     try:
-        got = GpuEngine().evaluate_expressions(cols, [">=($0, CURRENT_DATE)", "<($1, CURRENT_TIMESTAMP)"])
+        # process_project preprocesses its expressions (evaluate_expressions takes them preprocessed)
+        got = GpuEngine().process_project(
+            cols, "LogicalProject(d=[>=($0, CURRENT_DATE)], t=[<($1, CURRENT_TIMESTAMP)])")
     finally:
         g.api.set_current_timestamp(None)
     exp = OracleEngine(2).evaluate_expressions(cols, [">=($0, 2021-05-14)", "<($1, 2021-05-14 10:11:12.345)"])
