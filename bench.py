@@ -240,6 +240,7 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
     the same resident batches; outputs are library-allocated and freed."""
     import torch
     import blazingsql_gb300 as g
+    from blazingsql_gb300 import _native as N
     from blazingsql_gb300 import workloads as W
     sizes = W.c3_batch_sizes(seed, nbatches)
     total = sum(sizes)
@@ -279,18 +280,41 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
         buckets[key][0] += n
         buckets[key][1] += time.perf_counter() - t0
     runner = g.BatchRunner(plan, nbatches, total, autotune=True)
-    out, rows_b = runner.run(batches, stream=stream)  # tunes on this first run
-    for o in out:
-        g.api.free_columns(o, stream)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(reps):
-        out, rows_b = runner.run(batches, stream=stream)
-        for o in out:
-            g.api.free_columns(o, stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_b = e0.elapsed_time(e1) / reps
+    L = N.lib()
+    nout = plan.num_outputs
+
+    def runner_pass(bound, count):
+        """One runner call over bound batches (library-allocated outputs, freed
+        with one call); returns the rows per batch."""
+        outs, rows = runner.run(bound, stream=stream, raw=True)
+        g.api.free_column_array(outs, count * nout, stream)
+        return rows
+
+    def runner_time(bound, count):
+        """(call ms, kernel ms) per run: the call through the C ABI with its
+        output allocation, descriptor upload, graph launch, readback and free,
+        and the persistent kernel alone (CUDA events around it)."""
+        runner_pass(bound, count)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            runner_pass(bound, count)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        call_ms = e0.elapsed_time(e1) / reps
+        L.gx_debug_kernel_ms(1)
+        L.gx_debug_set_kernel_timing(1)
+        try:
+            for _ in range(reps):
+                runner_pass(bound, count)
+        finally:
+            L.gx_debug_set_kernel_timing(0)
+        return call_ms, L.gx_debug_kernel_ms(1) / reps
+
+    bound_all = runner.bind(batches)
+    rows_b = runner_pass(bound_all, nbatches)  # tunes on this first run
+    ms_b, kms_b = runner_time(bound_all, nbatches)
+    rows_b = runner_pass(bound_all, nbatches)
     bt, words = runner.config()
     # the runner's own rate per batch-size bucket: the same runner over the
     # bucket's batches alone
@@ -300,19 +324,9 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
         nrows = sum(n for n in sizes if lo <= n < hi)
         if not sel:
             continue
-        out, _ = runner.run(sel, stream=stream)
-        for o in out:
-            g.api.free_columns(o, stream)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(reps):
-            out, _ = runner.run(sel, stream=stream)
-            for o in out:
-                g.api.free_columns(o, stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        runner_buckets[key] = {"batches": len(sel), "rows": nrows,
-                               "rows_per_s": nrows / (e0.elapsed_time(e1) / reps / 1e3)}
+        cms, kms = runner_time(runner.bind(sel), len(sel))
+        runner_buckets[key] = {"batches": len(sel), "rows": nrows, "rows_per_s": nrows / (cms / 1e3),
+                               "kernel_rows_per_s": nrows / (kms / 1e3)}
     del batches, cols
     torch.cuda.empty_cache()
     return {
@@ -320,6 +334,7 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
         "workload": f"c3_batched_deep_plan: {nbatches} batches, log-uniform 1K-4M rows, {total} rows in all",
         "runner_rows_per_s": total / (ms_b / 1e3), "per_batch_calls_rows_per_s": total / (ms_a / 1e3),
         "runner_vs_per_batch_calls": ms_a / ms_b, "runner_ms": ms_b, "per_batch_calls_ms": ms_a,
+        "runner_kernel_ms": kms_b, "runner_kernel_rows_per_s": total / (kms_b / 1e3),
         "identical_row_counts": rows_a == rows_b,
         "autotuned": {"block_threads": bt, "words_per_warp": words, "vector_width": 1},
         "per_batch_calls_bucket_rows_per_s": {k: (v[0] / v[1] if v[1] > 0 else None) for k, v in buckets.items()},
@@ -386,21 +401,21 @@ def c5_batches(rows: int = 600_000_000, batch_rows: int = 1 << 22, reps: int = 3
     plan = g.Plan(w.schema, w.condition, w.projections)
     torch.cuda.synchronize()
     runner = g.BatchRunner(plan, len(sizes), rows, autotune=True)
-    out, r = runner.run(batches, stream=stream)  # tunes on this first run
-    for o in out:
-        g.api.free_columns(o, stream)
+    bound = runner.bind(batches)
+    nout = plan.num_outputs
+    outs, r = runner.run(bound, stream=stream, raw=True)  # tunes on this first run
+    g.api.free_column_array(outs, len(sizes) * nout, stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(reps):
-        out, r = runner.run(batches, stream=stream)
-        for o in out:
-            g.api.free_columns(o, stream)
+        outs, r = runner.run(bound, stream=stream, raw=True)
+        g.api.free_column_array(outs, len(sizes) * nout, stream)
     e1.record(stream)
     torch.cuda.synchronize()
     ms_runner = e0.elapsed_time(e1) / reps
     out_rows = sum(r)
-    for b in batches[:2]:  # warm the per-call path
+    for b in batches[:4]:  # warm the per-call path: its block-shape tuning compiles three candidates
         o, _ = plan.execute(b, stream=stream)
         g.api.free_columns(o, stream)
     torch.cuda.synchronize()

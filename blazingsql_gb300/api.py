@@ -425,6 +425,21 @@ class _BatchReport(dict):
         return super().__repr__()
 
 
+class BoundBatches:
+    """A list of batches as one array of C column views (BatchRunner.bind)."""
+
+    def __init__(self, views, count: int, keep: list):
+        self.views = views
+        self.count = count
+        self._keep = keep
+
+
+def free_column_array(outs, count: int, stream=None) -> None:
+    """Releases `count` library-owned columns of a C array with one call."""
+    if count > 0:
+        N.lib().gx_free_columns(outs, count, _stream_handle(stream))
+
+
 class BatchRunner:
     """A table of batches of one filter plan through one persistent kernel in a
     captured CUDA graph (gx_batch_runner_*)."""
@@ -438,8 +453,10 @@ class BatchRunner:
         self.num_outputs = plan.num_outputs
         self._ncols = len(plan.schema)
 
-    def run(self, batches: Sequence[Table], out: Optional[Sequence[N.Column]] = None, stream=None):
-        """Runs every batch; returns (columns per batch, rows per batch)."""
+    def bind(self, batches: Sequence[Table]) -> "BoundBatches":
+        """The C views of a list of batches, built once for repeated runs (an
+        engine holds these as plain arrays; building them per call is host
+        work that is not the runner's)."""
         keep: list = []
         nb = len(batches)
         views = (N.ColumnView * max(1, nb * self._ncols))()
@@ -449,6 +466,16 @@ class BatchRunner:
                 raise ValueError("batch column count does not match the plan")
             for i in range(nc):
                 views[b * nc + i] = arr[i]
+        return BoundBatches(views, nb, keep)
+
+    def run(self, batches, out: Optional[Sequence[N.Column]] = None, stream=None, raw: bool = False):
+        """Runs every batch (a list of tables or the result of ``bind``);
+        returns (columns per batch, rows per batch).  With ``raw`` the columns
+        are returned as one C array of ``gx_column`` (free it with
+        ``free_column_array``)."""
+        bound = batches if isinstance(batches, BoundBatches) else self.bind(batches)
+        nb = bound.count
+        views = bound.views
         n = self.num_outputs
         outs = (N.Column * max(1, nb * n))()
         if out is not None:
@@ -458,6 +485,8 @@ class BatchRunner:
         s = _stream_handle(stream)
         st = N.StatusInfo()
         N.check(N.lib().gx_batch_runner_run(self._h, views, nb, self._ncols, outs, rows, s, C.byref(st)), st)
+        if raw:
+            return outs, list(rows[:nb])
         if out is not None:
             cols = [[outs[b * n + j] for j in range(n)] for b in range(nb)]
         else:
