@@ -684,9 +684,11 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     """C4: the skewed 6-conjunct filter over `batches` batches of `rows` rows,
     through gx_learner under four policies on the same resident batches:
     plain fixed-order two-pass, textual-order single pass (no network), learned
-    (order from device memory, full-size outputs) and learned_sized (prediction
-    read back, outputs of the predicted size); the learned ones include the
-    warm-up and relabel batches on the plain path and the training.  Rows/s per
+    (order from device memory, full-size outputs) and learned_sized (outputs of
+    the predicted size, allocated as each batch's prediction is read); the
+    learned ones include the labelled warm-up and relabel batches (the plain
+    fixed-order evaluator in one pass that counts each conjunct's passes) and
+    the training.  Rows/s per
     policy over the whole batch stream, timed around one
     gx_learner_execute_batches call (the C ABI call a C++ caller makes; the
     Python argument building and result wrapping stay outside) and, for
@@ -721,8 +723,9 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     L = N.lib()
     for name, (pol, sized) in policies.items():
         def learner():
-            return g.Learner(plan, policy=pol, async_training=1, relabel_every=16, fast_words_per_warp=8,
-                             size_outputs=sized)
+            # 4 labelled warm-up batches, then one every 32 batches (5 of 64)
+            return g.Learner(plan, policy=pol, async_training=1, warmup_batches=4, relabel_every=32,
+                             fast_words_per_warp=8, size_outputs=sized)
         # the batch queue in one native call (what the execution graph's C++
         # kernel does), each next batch prepared while the current one runs
         lr = learner()

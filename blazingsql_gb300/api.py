@@ -105,6 +105,11 @@ class NativeColumn:
         return self._c.type_id
 
     @property
+    def capacity(self) -> int:
+        """Rows the column's buffers hold (at least size)."""
+        return self._c.capacity
+
+    @property
     def size(self) -> int:
         return self._c.size
 

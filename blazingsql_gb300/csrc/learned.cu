@@ -8,10 +8,11 @@
 // skip the remaining conjuncts' column loads), into outputs sized from the
 // predicted row count; a misprediction that overflows re-runs with the exact
 // count, so results are always identical to the plain path.  The plain
-// fixed-order two-pass evaluator supplies the training labels (it counts each
-// conjunct's passing rows) on warm-up batches and every `relabel_every`-th
-// batch, and remains the fallback.  Forward, backward and Adam run in the
-// kernels below.
+// fixed-order evaluator supplies the training labels on warm-up batches and
+// every `relabel_every`-th batch: in one fused pass (no short-circuit, every
+// conjunct evaluated for every row) that also counts each conjunct's passing
+// rows.  The plain fixed-order two-pass evaluator remains the PLAIN policy and
+// the judge.  Forward, backward and Adam run in the kernels below.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -681,7 +682,8 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
   if (opt_.policy < GX_LEARN_POLICY_LEARNED || opt_.policy > GX_LEARN_POLICY_TEXTUAL)
     fail(GX_ERR_INVALID, "unknown learner policy");
   if (opt_.stride_words < 1) opt_.stride_words = 1;
-  plain_ = variant(base, GX_FILTER_TWO_PASS, opt_.policy == GX_LEARN_POLICY_LEARNED, false);
+  plain_ = variant(base, GX_FILTER_TWO_PASS, false, false);
+  label_ = variant(base, GX_FILTER_SINGLE_PASS, true, false, opt_.fast_words);
   fast_ = variant(base, GX_FILTER_SINGLE_PASS, false, true, opt_.fast_words);
   ncols_ = std::min((int)p.schema.size(), kMaxSketchCols);
   nconj_ = (int)p.conjuncts.size();
@@ -764,7 +766,7 @@ Learner::Learner(const CompiledPlan& base, const LearnerOptions& opt) : opt_(opt
     check_cuda(cudaEventCreateWithFlags(&prep_in_, cudaEventDisableTiming), "event");
     for (int q = 0; q < kPredSlots; q++)
       check_cuda(cudaEventCreateWithFlags(&slots_[q].ready, cudaEventDisableTiming), "event");
-    for (int q = 0; q < 4; q++) check_cuda(cudaEventCreateWithFlags(&qev_[q], cudaEventDisableTiming), "event");
+    for (int q = 0; q < kPredEvents; q++) check_cuda(cudaEventCreateWithFlags(&qev_[q], cudaEventDisableTiming), "event");
     check_cuda(cudaEventCreateWithFlags(&qsketch_done_, cudaEventDisableTiming), "event");
     if (opt_.async_training) {
       check_cuda(cudaStreamCreateWithFlags(&train_stream_, cudaStreamNonBlocking), "training stream");
@@ -823,7 +825,7 @@ void Learner::release() {
   if (hqsk_) cudaFreeHost(hqsk_);
   dqsk_ = hqsk_ = nullptr;
   qsk_cap_ = 0;
-  for (int q = 0; q < 4; q++) {
+  for (int q = 0; q < kPredEvents; q++) {
     if (qev_[q]) cudaEventDestroy(qev_[q]);
     qev_[q] = nullptr;
   }
@@ -1088,18 +1090,20 @@ void Learner::execute_one(const std::vector<ColumnView>& cols, gx_column* out, i
   const bool relabel = !warm && opt_.relabel_every > 0 && since_label_ >= opt_.relabel_every;
   if (warm || relabel || n == 0) {
     since_label_ = 0;
-    // plain fixed-order two-pass evaluator: output + per-conjunct pass counts
-    // (queued: the counters sit in the batch's zeroed header, read after the queue)
+    // the plain fixed-order evaluator in one pass (every conjunct evaluated for
+    // every row): output + per-conjunct pass counts (queued: the counters sit in
+    // the batch's zeroed header, read after the queue)
     unsigned long long* counts = d ? d->hdr_dev + 4 : dcounts_;
     ExecExtras ex;
     ex.conj_counts = counts;
     if (d) {
       d->labelled = true;
-      plain_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
+      if (!out[0].data) alloc_batch_outputs(out, n, s);  // a queue with outputs made per batch
+      label_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
     } else {
       check_cuda(cudaMemsetAsync(dcounts_, 0, 8 * 16, s), "counts zero");
-      ex.conj_counts_host = hcounts_;  // read back with the count pass's own readback
-      plain_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
+      ex.conj_counts_host = hcounts_;  // read back with the pass's own readback
+      label_->execute(cols, out, out_rows, s, &ex);  // synchronises the stream
     }
     bi.path = 0;
     if (n > 0) {
@@ -1171,7 +1175,32 @@ void Learner::execute_one(const std::vector<ColumnView>& cols, gx_column* out, i
     if (info) *info = bi;
     return;
   }
-  if (d) fail(GX_ERR_INVALID, "sized outputs cannot be deferred");
+  if (d) {
+    // queued: the prediction was made on the side stream while the previous
+    // batch ran; the host reads it (mapped report), sizes the outputs and puts
+    // the filter on the stream without waiting for the device
+    if (!d->pred_ready) fail(GX_ERR_INVALID, "queued batch without a prediction");
+    check_cuda(cudaEventSynchronize(d->pred_ready), "prediction wait");
+    double log_all = 0.0;
+    for (int o = 0; o < O_; o++) {
+      const float z = d->report[o];
+      log_all += -(std::max(-z, 0.f) + std::log1p(std::exp(-std::fabs(z))));  // log sigmoid(z)
+    }
+    const double pred_rows = (double)n * std::exp(std::min(0.0, log_all));
+    d->pred_rows = (int64_t)pred_rows;
+    d->capacity =
+        (int64_t)std::min<double>((double)n, pred_rows * opt_.capacity_margin + (double)opt_.capacity_slack);
+    alloc_batch_outputs(out, d->capacity, s);
+    check_cuda(cudaStreamWaitEvent(s, d->pred_ready, 0), "wait prediction");
+    ExecExtras ex;
+    ex.order_dev = d->order_dev;
+    fast_->enqueue_filter(cols, out, d->hdr_dev, d->status, &ex, s);
+    poll_training();
+    bi.train_loss = loss_;
+    bi.path = 1;
+    if (info) *info = bi;
+    return;
+  }
   const std::vector<float> ls = predict_log_sel(cols, s);
   poll_training();
   // order by rank = cost / (1 - selectivity): cheap conjuncts that remove most rows first
@@ -1214,13 +1243,25 @@ void Learner::execute_one(const std::vector<ColumnView>& cols, gx_column* out, i
 
 // Host side of a deferred batch: the row count, the labels or the prediction,
 // all read after the queue's one synchronisation.
-void Learner::finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows,
+void Learner::alloc_batch_outputs(gx_column* out, int64_t capacity, cudaStream_t s) const {
+  std::vector<int> types;
+  for (const auto& o : fast_->plan().outputs) types.push_back(o.type);
+  alloc_output_set(types, std::vector<int64_t>(types.size(), capacity), true, out, s);
+}
+
+bool Learner::finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows,
                          gx_learned_batch_info* info) {
-  const CompiledPlan& ran = d.labelled ? *plain_ : *fast_;
+  const CompiledPlan& ran = d.labelled ? *label_ : *fast_;
+  if (info && d.pred_rows >= 0) info->predicted_rows = d.pred_rows;
+  // (a kernel error word is raised by finish_queued below)
+  if (!d.labelled && d.capacity >= 0 && n > 0 && d.hdr[2] == 0 && (int64_t)d.hdr[1] > d.capacity) {
+    if (out_rows) *out_rows = (int64_t)d.hdr[1];
+    return false;
+  }
   int64_t rows = 0;
   ran.finish_queued(d.hdr, n, out, &rows);
   if (out_rows) *out_rows = rows;
-  if (!info) return;
+  if (!info) return true;
   info->rows = rows;
   if (d.labelled && n > 0)
     for (int o = 0; o < nconj_; o++) info->measured_sel[o] = (double)d.hdr[4 + o] / (double)n;
@@ -1232,12 +1273,12 @@ void Learner::finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* 
       info->order[o] = rorder[o];
     }
   }
+  return true;
 }
 
 bool Learner::can_defer() const {
-  const bool single_pass = opt_.policy == GX_LEARN_POLICY_TEXTUAL ||
-                           (opt_.policy == GX_LEARN_POLICY_LEARNED && !opt_.size_outputs);
-  return single_pass && fast_->can_defer() && plain_->can_defer();
+  const bool single_pass = opt_.policy == GX_LEARN_POLICY_TEXTUAL || opt_.policy == GX_LEARN_POLICY_LEARNED;
+  return single_pass && fast_->can_defer() && label_->can_defer();
 }
 
 constexpr int kQueueParts = 16;  // sketch blocks per column of a queued batch
@@ -1338,7 +1379,7 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
     for (size_t b = 0; b < nb; b++) out_rows[b] = -1;  // set as each batch completes
   auto rows_of = [&](size_t b) { return batches[b].empty() ? (int64_t)0 : batches[b][0].size; };
   if (!can_defer()) {
-    // every batch completes before the next starts (sized outputs, the plain policy)
+    // every batch completes before the next starts (the plain policy)
     size_t at = 0;  // the batch being prepared or executed
     try {
       if (nb > 0) prepare(batches[0], s);
@@ -1359,8 +1400,13 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
   // Queued: every batch's outputs, masks, tile statuses and headers come from
   // one allocation cleared by one memset, and each batch puts only its
   // kernels on the stream (no host round trip); one copy of all headers and
-  // one synchronisation complete the queue.
+  // one synchronisation complete the queue.  With outputs sized from the
+  // predictions, the headers and statuses are one allocation and each batch's
+  // outputs are allocated when its prediction is read (the side stream makes
+  // it while the previous batch runs); a batch whose rows overflow its
+  // prediction runs again after the queue with the exact row count.
   if (nb == 0) return;
+  const bool sized = opt_.policy == GX_LEARN_POLICY_LEARNED && opt_.size_outputs;
   reserve_queue(nb);
   std::memset(hqueue_, 0, queue_cap_ * kHostSlot);
   char* dqueue = nullptr;
@@ -1370,10 +1416,16 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
   std::vector<int64_t> caps(nb), status_words(nb);
   for (size_t b = 0; b < nb; b++) {
     caps[b] = rows_of(b);
-    status_words[b] = std::max(fast_->tiles_for(caps[b]), plain_->tiles_for(caps[b]));
+    status_words[b] = std::max(fast_->tiles_for(caps[b]), label_->tiles_for(caps[b]));
   }
   std::vector<uint64_t*> status(nb);
-  char* base = (char*)alloc_output_queue(types, caps, status_words, out, status.data(), s);
+  char* base = nullptr;
+  if (sized) {
+    base = (char*)alloc_queue_scratch(status_words, status.data(), s);
+    for (size_t c = 0; c < nb * (size_t)nout; c++) out[c] = gx_column{};
+  } else {
+    base = (char*)alloc_output_queue(types, caps, status_words, out, status.data(), s);
+  }
   std::vector<Deferred> d(nb);
   const size_t rep0 = queue_cap_ * kQueueHeaderBytes;
   for (size_t b = 0; b < nb; b++) {
@@ -1392,11 +1444,13 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
   std::string err;
   int code = GX_OK;
   try {
-    // every batch's sketch in one launch; each batch's prediction one step
-    // ahead on the side stream (a one-block kernel beside the running filter)
+    // every batch's sketch in one launch; each batch's prediction kPredAhead
+    // batches ahead on the side stream, so that the one-block prediction
+    // kernel never sits between two filters (it runs beside them)
     if (learned) {
       sketch_queue(batches, d, s);
-      if (rows_of(0) > 0) predict_queued(d[0], 0, s);
+      for (size_t b = 0; b < std::min<size_t>(nb, kPredAhead); b++)
+        if (rows_of(b) > 0) predict_queued(d[b], (int)(b % kPredEvents), s);
     }
     for (size_t b = 0; b < nb; b++) {
       // at most kQueueDepth batches ahead of the device: the host then sees
@@ -1404,9 +1458,10 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
       // use their parameters (the device never waits for the host)
       if (b >= kQueueDepth)
         check_cuda(cudaEventSynchronize(qdone_[(b - kQueueDepth) % 8]), "queue pacing");
-      if (learned && b + 1 < nb && rows_of(b + 1) > 0) {
-        at = b + 1;
-        predict_queued(d[b + 1], (int)((b + 1) % 4), s);
+      const size_t pb = b + kPredAhead;
+      if (learned && pb < nb && rows_of(pb) > 0) {
+        at = pb;
+        predict_queued(d[pb], (int)(pb % kPredEvents), s);
       }
       at = b;
       execute_one(batches[b], out + b * nout, nullptr, inf + b, s, &d[b]);
@@ -1442,7 +1497,25 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
   }
   for (size_t b = 0; b < enqueued; b++) {
     try {
-      finish_one(d[b], rows_of(b), out + b * nout, out_rows ? out_rows + b : nullptr, inf + b);
+      int64_t rows = 0;
+      if (!finish_one(d[b], rows_of(b), out + b * nout, &rows, inf + b)) {
+        // misprediction: the batch runs again into outputs of its exact row count
+        for (int j = 0; j < nout; j++) {
+          free_column(out[b * nout + j], s);
+          out[b * nout + j] = gx_column{};
+        }
+        ExecExtras ex;
+        std::vector<int> order(nconj_);
+        const int* rorder = reinterpret_cast<const int*>(d[b].report + 16);
+        for (int o = 0; o < nconj_; o++) order[o] = rorder[o];
+        ex.order = order.data();
+        ex.num_order = nconj_;
+        ex.capacity_hint = rows;
+        fast_->execute(batches[b], out + b * nout, &rows, s, &ex);
+        inf[b].reruns = 1;
+        inf[b].rows = rows;
+      }
+      if (out_rows) out_rows[b] = rows;
     } catch (const Error& e) {
       if (code == GX_OK) {
         code = e.code;
@@ -1466,6 +1539,8 @@ void Learner::execute_batches(const std::vector<std::vector<ColumnView>>& batche
     check_cuda(cudaStreamWaitEvent(s, qsketch_done_, 0), "wait queue sketch");
     qsketch_pending_ = false;
   }
+
+  if (sized) dev_free(base, s);  // headers and statuses (the outputs are the columns')
   poll_training();
   if (code != GX_OK) fail((gx_status)code, "batch " + std::to_string(at) + ": " + err);
 }

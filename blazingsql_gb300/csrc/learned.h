@@ -90,11 +90,17 @@ class Learner {
     const float* feat = nullptr;             // device: the batch's sketch features (queue sketch)
     int* order_dev = nullptr;                // device: the predicted conjunct order (in the header)
     cudaEvent_t pred_ready = nullptr;        // recorded after the batch's prediction
-    bool labelled = false;                   // ran the plain two-pass evaluator
+    bool labelled = false;                   // ran the plain fixed-order evaluator (labels)
+    int64_t capacity = -1;                   // sized outputs: rows allocated from the prediction
+    int64_t pred_rows = -1;                  // sized outputs: the predicted row count
   };
   void execute_one(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows,
                    gx_learned_batch_info* info, cudaStream_t s, Deferred* d);
-  void finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows, gx_learned_batch_info* info);
+  // false when the batch's outputs, sized from its prediction, were too small
+  // (its row count is then in *out_rows and it must run again)
+  bool finish_one(const Deferred& d, int64_t n, gx_column* out, int64_t* out_rows, gx_learned_batch_info* info);
+  // the batch's outputs in one allocation of `capacity` rows, masks zeroed
+  void alloc_batch_outputs(gx_column* out, int64_t capacity, cudaStream_t s) const;
   bool can_defer() const;
   // queue buffers for up to nb batches (made at construction for kQueueReserve)
   struct QueueSketchLayout {
@@ -120,7 +126,11 @@ class Learner {
   void sync_inference_params(cudaStream_t s);
   void release();
 
-  std::shared_ptr<CompiledPlan> plain_, fast_;
+  // plain_: the fixed-order two-pass evaluator (the PLAIN policy, and the
+  // judge); label_: the fixed-order single pass that also counts each
+  // conjunct's passing rows (labelled batches); fast_: the single pass in the
+  // order given at launch
+  std::shared_ptr<CompiledPlan> plain_, label_, fast_;
   LearnerOptions opt_;
   int ncols_ = 0, nconj_ = 0, F_ = 0, H_ = 0, O_ = 0, nparams_ = 0;
   std::vector<double> conj_cost_;  // bytes per row the conjunct's columns read
@@ -164,7 +174,9 @@ class Learner {
   char* dqsk_ = nullptr;
   char* hqsk_ = nullptr;
   size_t qsk_cap_ = 0;                     // batches they hold
-  cudaEvent_t qev_[4] = {nullptr, nullptr, nullptr, nullptr};  // prediction events, in rotation
+  static constexpr int kPredAhead = 3;  // a queued batch's prediction is made this many batches ahead
+  static constexpr int kPredEvents = 8;  // prediction events, in rotation (> kPredAhead)
+  cudaEvent_t qev_[kPredEvents] = {};
   cudaEvent_t qdone_[8] = {};              // batch completion events of a queue, in rotation
   cudaEvent_t qsketch_done_ = nullptr;
   bool qsketch_pending_ = false;           // the main stream has not waited for the queue sketch yet

@@ -1174,6 +1174,21 @@ void emit_filter_writes(std::ostringstream& o, const Gen& g, const Plan& p, cons
 // aggregate is published before the block waits on anything, and a tile's
 // look-back only needs earlier tiles, so the pipeline cannot deadlock.
 void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids) {
+  // with conj_stats (fixed order, every conjunct evaluated for every row): each
+  // conjunct's passing rows, counted per warp in registers and added to
+  // a.conj_counts once per warp at the end
+  const bool stats = g.cfg_.conj_stats && !g.cfg_.runtime_order && !g.cfg_.short_circuit;
+  const int nc = (int)p.conjuncts.size();
+  auto count_conjuncts = [&](const std::string& ind) {
+    if (!stats) return;
+    o << ind << "#pragma unroll\n" << ind << "for (int k = 0; k < GX_V; k++) {\n";
+    o << ind << "  const i64 row = (w0 + k) * 32 + lane; const bool inr = row < a.n; (void)inr;\n";
+    for (int c = 0; c < nc; c++)
+      o << ind << "  cst_[" << c << "] += (u32)__popc(__ballot_sync(GX_FULL, inr && " << g.conj_keep(p.conjuncts[c])
+        << "));\n";
+    o << ind << "}\n";
+  };
+  if (stats) o << "  u32 cst_[" << nc << "] = {};\n";
   o << "  __shared__ unsigned long long s_claim;\n";
   o << "  __shared__ u32 s_cnt[2][GX_WARPS];\n";
   o << "  __shared__ u64 s_off[2][GX_WARPS];\n";
@@ -1188,6 +1203,7 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   g.decl(o, pred_ids, "    ");
   g.emit_predicate(o, "    ");
+  count_conjuncts("    ");
   o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) { bal[k] = __ballot_sync(GX_FULL, alive[k]); wcnt += __popc(bal[k]); }\n";
   o << "    if (lane == 0) s_cnt[0][warp] = wcnt;\n";
   o << "  }\n";
@@ -1204,6 +1220,7 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "      const i64 w0 = next * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   g.decl(o, pred_ids, "      ");
   g.emit_predicate(o, "      ");
+  count_conjuncts("      ");
   o << "      #pragma unroll\n      for (int k = 0; k < GX_V; k++) { nbal[k] = __ballot_sync(GX_FULL, alive[k]); nwcnt += __popc(nbal[k]); }\n";
   o << "      if (lane == 0) s_cnt[npar][warp] = nwcnt;\n";
   o << "    }\n";
@@ -1230,6 +1247,12 @@ void emit_fused_pipelined(std::ostringstream& o, const Gen& g, const Plan& p, co
   o << "    tile = next; par = npar; wcnt = nwcnt;\n";
   o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) bal[k] = nbal[k];\n";
   o << "  }\n";
+  if (stats) {
+    o << "  if (lane == 0) {\n";
+    for (int c = 0; c < nc; c++)
+      o << "    if (cst_[" << c << "]) atomicAdd(&a.conj_counts[" << c << "], (unsigned long long)cst_[" << c << "]);\n";
+    o << "  }\n";
+  }
   o << "}\n";
 }
 

@@ -198,6 +198,26 @@ void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>&
   }
 }
 
+void* alloc_queue_scratch(const std::vector<int64_t>& status_words, uint64_t** status, cudaStream_t s) {
+  const size_t nb = status_words.size();
+  if (nb == 0) return nullptr;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t total = al(nb * kQueueHeaderBytes);
+  std::vector<size_t> soff(nb);
+  for (size_t b = 0; b < nb; b++) {
+    soff[b] = total;
+    total += al((size_t)std::max<int64_t>(status_words[b], 1) * 8);
+  }
+  char* base = (char*)dev_alloc(total, s);
+  const cudaError_t e = cudaMemsetAsync(base, 0, total, s);
+  if (e != cudaSuccess) {
+    dev_free(base, s);
+    check_cuda(e, "queue scratch memset");
+  }
+  for (size_t b = 0; b < nb; b++) status[b] = (uint64_t*)(base + soff[b]);
+  return base;
+}
+
 void* alloc_output_queue(const std::vector<int>& types, const std::vector<int64_t>& caps,
                          const std::vector<int64_t>& status_words, gx_column* out, uint64_t** status,
                          cudaStream_t s) {
@@ -618,10 +638,14 @@ void CompiledPlan::enqueue_filter(const std::vector<ColumnView>& cols, gx_column
     if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
   const int64_t n = cols.empty() ? 0 : cols[0].size;
   const int nout = (int)plan_.outputs.size();
+  // outputs may hold fewer rows than the batch (sized from a prediction): the
+  // kernel writes nothing past the smallest capacity and finish_queued reports
+  // a row count above it as GX_ERR_CAPACITY
+  int64_t capacity = n;
   for (int j = 0; j < nout; j++) {
-    if (!out[j].data || !out[j].null_mask || out[j].capacity < n)
-      fail(GX_ERR_INVALID, "queued filter outputs need room for every input row");
+    if (!out[j].data || !out[j].null_mask) fail(GX_ERR_INVALID, "queued filter outputs missing");
     out[j].type_id = plan_.outputs[j].type;
+    capacity = std::min<int64_t>(capacity, out[j].capacity);
   }
   if (n == 0) return;
   const int64_t ntiles = tiles_for(n);
@@ -633,7 +657,7 @@ void CompiledPlan::enqueue_filter(const std::vector<ColumnView>& cols, gx_column
   a.out_count = hdr + 1;
   a.err = (int*)(hdr + 2);
   a.seed = plan_.rand_seed;
-  a.capacity = n;
+  a.capacity = capacity;
   for (int i = 0; i < 16; i++) a.order[i] = i;
   if (extras) {
     for (int i = 0; i < extras->num_order && i < 16; i++) a.order[i] = extras->order[i];
@@ -842,6 +866,9 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     }
     launch(k, (int)grid, s, a, true);
     if (explore >= 0) check_cuda(cudaEventRecord(te1, s), "event record");
+    if (!two_pass && extras && extras->conj_counts && extras->conj_counts_host)
+      check_cuda(cudaMemcpyAsync(extras->conj_counts_host, extras->conj_counts, 16 * 8, cudaMemcpyDeviceToHost, s),
+                 "conjunct counts readback");
     check_cuda(cudaMemcpyAsync(host_hdr, hdr, 4 * 8, cudaMemcpyDeviceToHost, s), "count readback");
     check_cuda(cudaStreamSynchronize(s), "filter sync");
     if (explore >= 0) {

@@ -47,6 +47,10 @@ constexpr size_t kQueueHeaderBytes = 256;
 void* alloc_output_queue(const std::vector<int>& types, const std::vector<int64_t>& caps,
                          const std::vector<int64_t>& status_words, gx_column* out, uint64_t** status,
                          cudaStream_t s);
+// The headers and tile-status words of a queue without its outputs (a queue
+// whose outputs are allocated batch by batch): the same layout, zeroed; the
+// caller releases the returned base with dev_free once the queue completed.
+void* alloc_queue_scratch(const std::vector<int64_t>& status_words, uint64_t** status, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 void check_cuda(cudaError_t e, const char* what);
 // host-side fault injection for tests: fail the n-th next allocation (n >= 1)

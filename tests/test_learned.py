@@ -289,6 +289,55 @@ def test_learned_misprediction_reruns():
 
 
 @pytest.mark.gpu
+def test_queued_sized_outputs_rerun_on_misprediction():
+    """A queue with outputs sized from the predictions and no capacity margin:
+    batches whose rows overflow their prediction run again after the queue,
+    and every batch still equals the plain path; the outputs of the others
+    hold no more rows than the prediction allowed."""
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+    learned = g.Learner(plan, warmup_batches=2, relabel_every=0, train_steps=4, capacity_margin=1.0,
+                        capacity_slack=0, size_outputs=1)
+    plain = g.Learner(plan, policy=g.GX_LEARN_POLICY_PLAIN)
+    batches = [_upload(W.c4_batch_host(1 << 15, 5, b)) for b in range(10)]
+    out = learned.execute_batches(batches)
+    reruns = 0
+    for b, (got, rows, info) in enumerate(out):
+        exp, erows, _ = plain.execute(batches[b])
+        assert rows == erows, f"batch {b}"
+        assert_tables_equal(_host(got), _host(exp), what=f"batch {b}")
+        reruns += info["reruns"]
+        if info["path"] == 1 and not info["reruns"]:
+            assert got[0].capacity <= max(rows, info["predicted_rows"]) + 1
+    assert reruns > 0
+
+
+@pytest.mark.gpu
+def test_labels_are_exact_conjunct_counts():
+    """The labelled batches' measured selectivities are each conjunct's exact
+    pass fraction over the batch (counted in the fused single pass), for a
+    direct call and inside a queue."""
+    import blazingsql_gb300 as g
+    plan = _c4_plan(g)
+
+    def expected(host):
+        x = [c.data for c in host]
+        keep = [x[0] > 100000, x[1] == 1000, x[2] < 1000, x[4] < 1000.0, x[5] > 5000.0, x[6] < 100.0]
+        return [float(np.count_nonzero(k)) / len(k) for k in keep]
+
+    hosts = [W.c4_batch_host((1 << 15) + 333 * b, 9, b) for b in range(3)]
+    direct = g.Learner(plan, warmup_batches=3, relabel_every=0, train_steps=2)
+    for h in hosts:
+        _, _, info = direct.execute(_upload(h))
+        assert info["path"] == 0
+        np.testing.assert_array_equal(np.array(info["measured_sel"][:6]), np.array(expected(h)))
+    queued = g.Learner(plan, warmup_batches=3, relabel_every=0, train_steps=2)
+    for h, (_, _, info) in zip(hosts, queued.execute_batches([_upload(h) for h in hosts])):
+        assert info["path"] == 0
+        np.testing.assert_array_equal(np.array(info["measured_sel"][:6]), np.array(expected(h)))
+
+
+@pytest.mark.gpu
 def test_learner_policies_agree_and_async_training():
     import blazingsql_gb300 as g
     plan = _c4_plan(g)
