@@ -120,6 +120,19 @@ __device__ __forceinline__ u64 gx_ld_64(const void* p, i64 i) { return (u64)__ld
 __device__ __forceinline__ u64 gx_ld_f32(const void* p, i64 i) { return gx_B((double)__ldcs((const float*)p + i)); }
 __device__ __forceinline__ u64 gx_ld_f32e(const void* p, i64 i) { return gxe_f2d(__ldcs((const unsigned*)p + i)); }
 
+// the same loads with the default cache policy, for a column the predicate
+// reads and the projections read again by kept row: its lines stay in L2
+// between the two (a streaming load marks them first to evict)
+__device__ __forceinline__ i64 gx_ldg_i8(const void* p, i64 i) { return (i64)__ldg((const signed char*)p + i); }
+__device__ __forceinline__ i64 gx_ldg_u8(const void* p, i64 i) { return (i64)__ldg((const unsigned char*)p + i); }
+__device__ __forceinline__ i64 gx_ldg_i16(const void* p, i64 i) { return (i64)__ldg((const short*)p + i); }
+__device__ __forceinline__ i64 gx_ldg_u16(const void* p, i64 i) { return (i64)__ldg((const unsigned short*)p + i); }
+__device__ __forceinline__ i64 gx_ldg_i32(const void* p, i64 i) { return (i64)__ldg((const int*)p + i); }
+__device__ __forceinline__ i64 gx_ldg_u32(const void* p, i64 i) { return (i64)__ldg((const unsigned int*)p + i); }
+__device__ __forceinline__ u64 gx_ldg_64(const void* p, i64 i) { return (u64)__ldg((const long long*)p + i); }
+__device__ __forceinline__ u64 gx_ldg_f32(const void* p, i64 i) { return gx_B((double)__ldg((const float*)p + i)); }
+__device__ __forceinline__ u64 gx_ldg_f32e(const void* p, i64 i) { return gxe_f2d(__ldg((const unsigned*)p + i)); }
+
 // the same loads from a shared-memory staging buffer (staged filter kernel)
 __device__ __forceinline__ i64 gx_lds_i8(const void* p, i64 i) { return (i64)((const signed char*)p)[i]; }
 __device__ __forceinline__ i64 gx_lds_u8(const void* p, i64 i) { return (i64)((const unsigned char*)p)[i]; }

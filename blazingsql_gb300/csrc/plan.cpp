@@ -317,8 +317,9 @@ class Gen {
         o << ind << b << " = inr ? (full_word_ ? (u64)" << sfn << "(" << st->second.first << ", " << st->second.second
           << ") : (u64)" << gfn << "(a.in_data[" << c << "], a.in_off[" << c << "] + row)) : 0ull;\n";
       } else {
-        o << ind << b << " = inr ? (u64)" << (emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c]))
-          << "(a.in_data[" << c << "], a.in_off[" << c << "] + row) : 0ull;\n";
+        std::string fn = emu() ? load_fn_emu(p_.schema[c]) : load_fn(p_.schema[c]);
+        if (reread_cols_.count(c)) fn = "gx_ldg_" + fn.substr(6);  // gx_ld_X -> gx_ldg_X
+        o << ind << b << " = inr ? (u64)" << fn << "(a.in_data[" << c << "], a.in_off[" << c << "] + row) : 0ull;\n";
       }
       if (p_.nullable[c]) o << ind << v << " = inr && gx_valid(a.in_mask[" << c << "], a.in_off[" << c << "] + row);\n";
       else o << ind << v << " = inr;\n";
@@ -876,6 +877,9 @@ class Gen {
   // tile-staged kernels: every column is read from the tile's shared-memory
   // stage (row trow of the tile; see emit_fused_tma)
   mutable bool tile_mode_ = false;
+  // columns whose data both the predicate and the projections read: loaded
+  // with the default cache policy so the projections' re-read hits L2
+  mutable std::set<int> reread_cols_;
 
   // validity of node id is true for every row in range (no NULL can arise):
   // non-nullable columns, valid literals, and operators that propagate only
@@ -2092,6 +2096,16 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   KernelConfig cfg = cfg_in;
   if (cfg.native_f64_ops < 0) cfg.native_f64_ops = auto_native_f64_ops(p);
   Gen g(p, cfg);
+  if (p.has_filter() && cfg.dense) {
+    // predicate columns the dense projections read again by kept row
+    std::set<int> pred_cols;
+    for (int id : g.predicate_cone())
+      if (p.nodes[id].kind == Node::COL) pred_cols.insert(p.nodes[id].col);
+    for (int id : g.cone(g.output_roots()))
+      if (p.nodes[id].kind == Node::COL && pred_cols.count(p.nodes[id].col)) g.reread_cols_.insert(p.nodes[id].col);
+    for (const auto& os : p.outputs)
+      if (os.kind == OutSpec::COPY && pred_cols.count(os.col)) g.reread_cols_.insert(os.col);
+  }
   std::ostringstream o;
   emit_prelude(o, cfg);
   if (kind == KernelKind::FUSED_STAGED) {
