@@ -723,8 +723,9 @@ def learned_compare(batches: int, rows: int, seed: int = 4):
     L = N.lib()
     for name, (pol, sized) in policies.items():
         def learner():
-            # 4 labelled warm-up batches, then one every 32 batches (5 of 64)
-            return g.Learner(plan, policy=pol, async_training=1, warmup_batches=4, relabel_every=32,
+            # trained online on its first 4 batches (labelled by the plain
+            # fixed-order pass), then the network alone orders the rest
+            return g.Learner(plan, policy=pol, async_training=1, warmup_batches=4, relabel_every=0,
                              fast_words_per_warp=8, size_outputs=sized)
         # the batch queue in one native call (what the execution graph's C++
         # kernel does), each next batch prepared while the current one runs

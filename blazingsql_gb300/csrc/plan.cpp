@@ -2097,10 +2097,18 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   if (cfg.native_f64_ops < 0) cfg.native_f64_ops = auto_native_f64_ops(p);
   Gen g(p, cfg);
   if (p.has_filter() && cfg.dense) {
-    // predicate columns the dense projections read again by kept row
+    // columns whose data the predicate reads (not only their validity, as
+    // IS [NOT] NULL does) and the dense projections read again by kept row
     std::set<int> pred_cols;
-    for (int id : g.predicate_cone())
-      if (p.nodes[id].kind == Node::COL) pred_cols.insert(p.nodes[id].col);
+    const std::vector<int> pc = g.predicate_cone();
+    for (int id : pc) {
+      const Node& n = p.nodes[id];
+      if (n.kind != Node::OP || n.op == OP_IS_NULL || n.op == OP_IS_NOT_NULL) continue;
+      for (int x : {n.a, n.b})
+        if (x >= 0 && p.nodes[x].kind == Node::COL) pred_cols.insert(p.nodes[x].col);
+    }
+    for (int c : p.conjuncts)  // a BOOL8 column as a conjunct is read as data
+      if (p.nodes[c].kind == Node::COL) pred_cols.insert(p.nodes[c].col);
     for (int id : g.cone(g.output_roots()))
       if (p.nodes[id].kind == Node::COL && pred_cols.count(p.nodes[id].col)) g.reread_cols_.insert(p.nodes[id].col);
     for (const auto& os : p.outputs)

@@ -431,14 +431,18 @@ static const char* kind_name(KernelKind k) {
 static const CompiledPlan::Shape kShapes[] = {{4, 8}, {1, 16}, {2, 8}};
 static constexpr int kNumShapes = 3;
 
+// The first large call runs the first candidate unmeasured (it pays the
+// first touches of fresh output memory), the next ones measure each candidate.
 CompiledPlan::Shape CompiledPlan::filter_shape(int64_t n, int* explore) const {
   *explore = -1;
   if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words};
   std::lock_guard<std::mutex> g(tmu_);
   if (chosen_ >= 0) return kShapes[chosen_];
   if (cand_ms_.empty()) cand_ms_.assign(kNumShapes, -1.f);
-  if (n >= kShapeTuneRows && next_cand_ < kNumShapes) {
-    *explore = next_cand_++;
+  if (n >= kShapeTuneRows && next_cand_ <= kNumShapes) {
+    const int k = next_cand_++;
+    if (k == 0) return kShapes[0];  // warm-up
+    *explore = k - 1;
     return kShapes[*explore];
   }
   return kShapes[0];
@@ -480,7 +484,10 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
   KernelConfig c = cfg_;
   c.warps = warps;
   c.words = words;
-  const std::string name = kind_name(kind);
+  // the single pass in a conjunct order given at launch (learned ordering) is
+  // named apart, so that profiles can tell it from the fixed-order pass
+  const std::string name =
+      kind == KernelKind::FUSED_FILTER && c.runtime_order ? std::string("gx_filter_ordered") : kind_name(kind);
   const std::string src = generate_kernel(p, kind, c, name);
   // the tile-staged kernel runs a producer and a resolver warp beside its consumer warps
   const bool tma = kind == KernelKind::FUSED_TMA;

@@ -142,9 +142,10 @@ class CompiledPlan {
   // warps / words: a block shape other than the configured one (0: configured)
   JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable, int warps = 0, int words = 0) const;
   // Block shape of a single-pass filter call over n rows.  With tune_shape,
-  // calls of at least kShapeTuneRows rows first run each candidate once
-  // (*explore = its index; the caller reports its time to shape_measured),
-  // then every call takes the fastest.
+  // calls of at least kShapeTuneRows rows first run the first candidate once
+  // unmeasured (a warm-up), then each candidate once (*explore = its index;
+  // the caller reports its time to shape_measured), then every call takes the
+  // fastest.
   Shape filter_shape(int64_t n, int* explore) const;
   void shape_measured(int idx, float ms) const;
   static constexpr int64_t kShapeTuneRows = int64_t(1) << 22;
