@@ -316,6 +316,29 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
     ms_b, kms_b = runner_time(bound_all, nbatches)
     rows_b = runner_pass(bound_all, nbatches)
     bt, words = runner.config()
+    # the batch stream: the persistent kernel fed batch by batch while it runs
+    # (each push from this Python loop: ctypes argument building plus three
+    # asynchronous copies), with the runner's tuned shape; timed from the
+    # kernel's launch to the returned outputs
+    bstream = g.BatchStream(plan, nbatches, total, block_threads=bt, words_per_warp=words)
+
+    def stream_pass():
+        bstream.start(stream)
+        for b in batches:
+            bstream.push(b)
+        out = bstream.finish()
+        g.api.free_columns([c for cols, _ in out for c in cols], stream)
+        return [r for _, r in out]
+
+    rows_s = stream_pass()
+    stream_ms = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        stream_pass()
+        stream_ms.append((time.perf_counter() - t0) * 1e3)
+    ms_s = min(stream_ms)
+    del bstream
     # the runner's own rate per batch-size bucket: the same runner over the
     # bucket's batches alone
     runner_buckets = {}
@@ -335,6 +358,7 @@ def batched_compare(nbatches: int = 512, seed: int = 3, reps: int = 3):
         "runner_rows_per_s": total / (ms_b / 1e3), "per_batch_calls_rows_per_s": total / (ms_a / 1e3),
         "runner_vs_per_batch_calls": ms_a / ms_b, "runner_ms": ms_b, "per_batch_calls_ms": ms_a,
         "runner_kernel_ms": kms_b, "runner_kernel_rows_per_s": total / (kms_b / 1e3),
+        "stream_rows_per_s": total / (ms_s / 1e3), "stream_ms": ms_s, "stream_identical_row_counts": rows_s == rows_b,
         "identical_row_counts": rows_a == rows_b,
         "autotuned": {"block_threads": bt, "words_per_warp": words, "vector_width": 1},
         "per_batch_calls_bucket_rows_per_s": {k: (v[0] / v[1] if v[1] > 0 else None) for k, v in buckets.items()},

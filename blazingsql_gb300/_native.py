@@ -135,6 +135,14 @@ def lib():
     L.gx_batch_runner_config.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32)]
     L.gx_batch_runner_destroy.argtypes = [C.c_void_p]
     L.gx_batch_runner_destroy.restype = None
+    L.gx_batch_stream_create.argtypes = [C.c_void_p, C.c_int, C.c_int64, C.c_int, C.c_int, P(StatusInfo)]
+    L.gx_batch_stream_create.restype = C.c_void_p
+    L.gx_batch_stream_start.argtypes = [C.c_void_p, C.c_void_p, P(StatusInfo)]
+    L.gx_batch_stream_push.argtypes = [C.c_void_p, P(ColumnView), C.c_int, P(C.c_int), P(StatusInfo)]
+    L.gx_batch_stream_finish.argtypes = [C.c_void_p, P(Column), P(C.c_int64), C.c_int, P(StatusInfo)]
+    L.gx_batch_stream_destroy.argtypes = [C.c_void_p]
+    L.gx_batch_stream_destroy.restype = None
+    L.gx_debug_batch_stream_wait_polls.argtypes = [C.c_void_p, C.c_uint32]
     L.gx_debug_kernel_resources.argtypes = [C.c_void_p, C.c_int, P(C.c_uint8), P(C.c_int32), P(C.c_int32),
                                             P(C.c_int32), P(StatusInfo)]
     L.gx_debug_fail_allocation.argtypes = [C.c_int]
@@ -204,6 +212,8 @@ EXPORTED_SYMBOLS = [
     "gx_learner_load",
     "gx_learner_destroy", "gx_debug_mlp_grad", "gx_debug_learner_features", "gx_debug_kernel_resources",
     "gx_batch_runner_create", "gx_batch_runner_run", "gx_batch_runner_config", "gx_batch_runner_destroy",
+    "gx_batch_stream_create", "gx_batch_stream_start", "gx_batch_stream_push", "gx_batch_stream_finish",
+    "gx_batch_stream_destroy", "gx_debug_batch_stream_wait_polls",
 ]
 
 

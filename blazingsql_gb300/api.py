@@ -514,6 +514,68 @@ class BatchRunner:
             pass
 
 
+class BatchStream:
+    """A persistent kernel of one filter plan fed batch by batch while it runs
+    (gx_batch_stream_*): ``start`` launches it, ``push`` hands it a batch (the
+    batch's columns must stay alive until ``finish``), ``finish`` closes the
+    queue and returns (columns, rows) per pushed batch."""
+
+    def __init__(self, plan: Plan, max_batches: int, max_total_rows: int, block_threads: int = 0,
+                 words_per_warp: int = 0):
+        st = N.StatusInfo()
+        h = N.lib().gx_batch_stream_create(plan._h, max_batches, max_total_rows, block_threads, words_per_warp,
+                                           C.byref(st))
+        if not h:
+            raise N.GxError(st.code, st.message.decode(errors="replace"))
+        self._h = h
+        self.num_outputs = plan.num_outputs
+        self._ncols = len(plan.schema)
+        self._keep: list = []
+        self._count = 0
+        self._stream = 0
+
+    def start(self, stream=None) -> None:
+        st = N.StatusInfo()
+        self._stream = _stream_handle(stream)
+        N.check(N.lib().gx_batch_stream_start(self._h, self._stream, C.byref(st)), st)
+        self._keep, self._count = [], 0
+
+    def push(self, table: Table) -> int:
+        views, nc = _views(table, self._keep)
+        self._keep.append(views)
+        idx = C.c_int(-1)
+        st = N.StatusInfo()
+        N.check(N.lib().gx_batch_stream_push(self._h, views, nc, C.byref(idx), C.byref(st)), st)
+        self._count += 1
+        return idx.value
+
+    def finish(self):
+        n = self.num_outputs
+        nb = self._count
+        outs = (N.Column * max(1, nb * n))()
+        rows = (C.c_int64 * max(1, nb))()
+        st = N.StatusInfo()
+        try:
+            N.check(N.lib().gx_batch_stream_finish(self._h, outs, rows, nb, C.byref(st)), st)
+        finally:
+            self._keep, self._count = [], 0
+        return [([NativeColumn(N.Column(outs[b * n + j].type_id, 0, outs[b * n + j].data, outs[b * n + j].null_mask,
+                                        outs[b * n + j].size, outs[b * n + j].capacity), self._stream)
+                  for j in range(n)], rows[b]) for b in range(nb)]
+
+    def set_wait_polls(self, polls: int) -> None:
+        """Test hook: polls (about 2 us apart) the kernel waits for a batch."""
+        N.lib().gx_debug_batch_stream_wait_polls(self._h, polls)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.lib().gx_batch_stream_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class Learner:
     """Learned conjunct ordering over a stream of batches (gx_learner_*).
 

@@ -399,11 +399,250 @@ void BatchRunner::run(const std::vector<std::vector<ColumnView>>& batches, gx_co
   }
 }
 
+
+// ------------------------------------------------------------------ stream
+BatchStream::BatchStream(const CompiledPlan& base, int max_batches, int64_t max_rows, int warps, int words)
+    : plan_(base.plan()), max_batches_(max_batches), max_rows_(max_rows) {
+  if (!plan_.has_filter()) fail(GX_ERR_INVALID, "a batch stream runs plans with a condition");
+  if (!base.can_defer()) fail(GX_ERR_INVALID, "a batch stream needs a plan without literal outputs");
+  if (max_batches < 1 || max_rows < 0) fail(GX_ERR_INVALID, "bad batch stream limits");
+  KernelConfig c = base.config();
+  c.short_circuit = false;
+  c.conjunct_order.clear();
+  c.runtime_order = false;
+  c.conj_stats = false;
+  c.dense = true;
+  c.tune_shape = false;
+  if (warps > 0) c.warps = warps;
+  if (words > 0) c.words = words;
+  if (c.warps < 1 || c.warps > 32 || c.words < 1 || c.words > 32) fail(GX_ERR_INVALID, "bad block shape");
+  variant_ = std::make_shared<CompiledPlan>(plan_, c, GX_FILTER_SINGLE_PASS);
+  tile_rows_ = (int64_t)c.warps * c.words * 32;
+  max_tiles_ = max_rows_ / tile_rows_ + max_batches_ + 1;
+  // a batch's output rows start on a 32-row boundary (its mask words are its own)
+  arena_rows_ = max_rows_ + 32 * (int64_t)max_batches_;
+  // the kernel reads validity through a mask pointer that may be null, so one
+  // kernel serves batches with and without masks
+  kernel_ = variant_->kernel_for(KernelKind::FUSED_STREAM, std::vector<bool>(plan_.schema.size(), true));
+  auto dmalloc = [](void** p, size_t b, const char* what) {
+    const cudaError_t e = cudaMalloc(p, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(e == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA, what);
+    }
+  };
+  try {
+    dmalloc((void**)&dargs_, kStreamArgsStride * max_batches_, "stream descriptors");
+    dmalloc((void**)&dbase_, 8 * (size_t)(max_batches_ + 1), "stream tile offsets");
+    dmalloc((void**)&dhdr_, sizeof(BatchHeader), "stream header");
+    dmalloc((void**)&dscratch_, 8 * (size_t)(4 * max_batches_ + max_tiles_), "stream scratch");
+    dmalloc((void**)&dwerr_, 16, "stream wait flag");
+    check_cuda(cudaMallocHost((void**)&hargs_, kStreamArgsStride * max_batches_), "pinned descriptors");
+    check_cuda(cudaMallocHost((void**)&hbase_, 8 * (size_t)(max_batches_ + 1)), "pinned tile offsets");
+    check_cuda(cudaMallocHost((void**)&hpub_, 8 * (size_t)max_batches_), "pinned published counts");
+    check_cuda(cudaMallocHost((void**)&hflag_, 16), "pinned flags");
+    check_cuda(cudaMallocHost((void**)&hres_, 8 * 4 * (size_t)max_batches_), "pinned results");
+    check_cuda(cudaStreamCreateWithFlags(&push_stream_, cudaStreamNonBlocking), "push stream");
+    check_cuda(cudaEventCreateWithFlags(&started_, cudaEventDisableTiming), "event");
+  } catch (...) {
+    release();
+    throw;
+  }
+}
+
+BatchStream::~BatchStream() {
+  if (running_) {
+    // close the queue so the kernel stops before its buffers go
+    hflag_[0] = 1;
+    cudaMemcpyAsync(&dhdr_->pad, hflag_, 4, cudaMemcpyHostToDevice, push_stream_);
+    cudaStreamSynchronize(push_stream_);
+    cudaStreamSynchronize(s_);
+    dev_free(arena_, s_);
+    cudaStreamSynchronize(s_);
+  }
+  release();
+}
+
+void BatchStream::release() {
+  if (push_stream_) cudaStreamDestroy(push_stream_);
+  if (started_) cudaEventDestroy(started_);
+  cudaFree(dargs_);
+  cudaFree(dbase_);
+  cudaFree(dhdr_);
+  cudaFree(dscratch_);
+  cudaFree(dwerr_);
+  if (hargs_) cudaFreeHost(hargs_);
+  if (hbase_) cudaFreeHost(hbase_);
+  if (hpub_) cudaFreeHost(hpub_);
+  if (hflag_) cudaFreeHost(hflag_);
+  if (hres_) cudaFreeHost(hres_);
+  push_stream_ = nullptr;
+  started_ = nullptr;
+  dargs_ = nullptr;
+  dbase_ = nullptr;
+  dhdr_ = nullptr;
+  dscratch_ = nullptr;
+  dwerr_ = nullptr;
+  hargs_ = nullptr;
+  hbase_ = nullptr;
+  hpub_ = nullptr;
+  hflag_ = nullptr;
+  hres_ = nullptr;
+}
+
+void BatchStream::start(cudaStream_t s) {
+  if (running_) fail(GX_ERR_INVALID, "the batch stream is already running");
+  const int nout = num_outputs();
+  // this session's outputs: [masks of every output | data of every output]
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  moff_.assign(nout, 0);
+  doff_.assign(nout, 0);
+  size_t total = 0;
+  for (int j = 0; j < nout; j++) {
+    moff_[j] = total;
+    total += al((size_t)(arena_rows_ / 32 + 16) * 4);
+  }
+  const size_t masks = total;
+  for (int j = 0; j < nout; j++) {
+    doff_[j] = total;
+    total += al(std::max<size_t>(64, (size_t)arena_rows_ * type_size(plan_.outputs[j].type)));
+  }
+  arena_ = (char*)dev_alloc(total, s);
+  try {
+    check_cuda(cudaMemsetAsync(arena_, 0, masks, s), "stream masks");
+    check_cuda(cudaMemsetAsync(dscratch_, 0, 8 * (size_t)(4 * max_batches_ + max_tiles_), s), "stream scratch");
+    // tile offsets of unpublished batches read as INT64_MAX-like (0x7f..7f)
+    check_cuda(cudaMemsetAsync(dbase_, 0x7f, 8 * (size_t)(max_batches_ + 1), s), "stream offsets");
+    check_cuda(cudaMemsetAsync(dbase_, 0, 8, s), "stream offsets");
+    check_cuda(cudaMemsetAsync(dhdr_, 0, sizeof(BatchHeader), s), "stream header");
+    check_cuda(cudaMemsetAsync(dwerr_, 0, 16, s), "stream wait flag");
+    check_cuda(cudaEventRecord(started_, s), "stream event");
+    check_cuda(cudaStreamWaitEvent(push_stream_, started_, 0), "stream wait");
+    KernelArgs* pa = dargs_;
+    long long* pb = dbase_;
+    BatchHeader* ph = dhdr_;
+    int* pw = dwerr_;
+    unsigned polls = wait_polls_;
+    void* params[] = {&pa, &pb, &ph, &pw, &polls};
+    const int grid = device_sm_count() * kernel_.max_blocks_per_sm;
+    launch_raw(kernel_, grid, s, params, false);
+  } catch (...) {
+    dev_free(arena_, s);
+    arena_ = nullptr;
+    throw;
+  }
+  add_launches(1);
+  hbase_[0] = 0;
+  s_ = s;
+  running_ = true;
+  count_ = 0;
+  tiles_ = 0;
+  rows_used_ = 0;
+  row_off_.clear();
+  rows_in_.clear();
+}
+
+int BatchStream::push(const std::vector<ColumnView>& cols) {
+  if (!running_) fail(GX_ERR_INVALID, "the batch stream is not running");
+  if (count_ >= max_batches_) fail(GX_ERR_INVALID, "more batches than the stream was created for");
+  if (cols.size() != plan_.schema.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+  for (size_t i = 0; i < cols.size(); i++)
+    if (cols[i].type != plan_.schema[i]) fail(GX_ERR_INVALID, "column type does not match the plan");
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  const int64_t tiles = (n + tile_rows_ - 1) / tile_rows_;
+  const int64_t need = (std::max<int64_t>(n, 1) + 31) / 32 * 32;  // distinct, word-aligned output rows
+  if (tiles_ + tiles > max_tiles_ || rows_used_ + need > arena_rows_)
+    fail(GX_ERR_INVALID, "batches exceed the stream's row limit");
+  const int b = count_;
+  const int nout = num_outputs();
+  KernelArgs& a = *(KernelArgs*)((char*)hargs_ + (size_t)b * kStreamArgsStride);
+  std::memset(&a, 0, sizeof a);
+  for (size_t i = 0; i < cols.size(); i++) {
+    a.in_data[i] = cols[i].data;
+    a.in_mask[i] = cols[i].mask;
+    a.in_off[i] = cols[i].offset;
+  }
+  for (int j = 0; j < nout; j++) {
+    a.out_data[j] = arena_ + doff_[j] + (size_t)rows_used_ * type_size(plan_.outputs[j].type);
+    a.out_mask[j] = (uint32_t*)(arena_ + moff_[j]) + rows_used_ / 32;
+  }
+  a.n = n;
+  a.capacity = n;
+  a.tile_status = dscratch_ + 4 * (size_t)max_batches_ + tiles_;
+  a.out_count = (unsigned long long*)(dscratch_ + 4 * (size_t)b + 1);
+  a.err = (int*)(dscratch_ + 4 * (size_t)b + 2);
+  a.seed = plan_.rand_seed;
+  for (int i = 0; i < 16; i++) a.order[i] = i;
+  hbase_[b + 1] = tiles_ + tiles;
+  hpub_[b] = tiles_ + tiles;
+  // descriptor and offsets first; the published tile count last (the kernel
+  // reads a batch's descriptor only after seeing its tiles published)
+  check_cuda(cudaMemcpyAsync((char*)dargs_ + (size_t)b * kStreamArgsStride, &a, sizeof(KernelArgs),
+                             cudaMemcpyHostToDevice, push_stream_),
+             "stream descriptor");
+  check_cuda(cudaMemcpyAsync(dbase_ + b + 1, hbase_ + b + 1, 8, cudaMemcpyHostToDevice, push_stream_),
+             "stream offsets");
+  check_cuda(cudaMemcpyAsync(&dhdr_->total_tiles, hpub_ + b, 8, cudaMemcpyHostToDevice, push_stream_),
+             "stream publish");
+  row_off_.push_back(rows_used_);
+  rows_in_.push_back(n);
+  tiles_ += tiles;
+  rows_used_ += need;
+  return count_++;
+}
+
+void BatchStream::finish(gx_column* out, int64_t* out_rows, int max_out_batches) {
+  if (!running_) fail(GX_ERR_INVALID, "the batch stream is not running");
+  if (count_ > max_out_batches) fail(GX_ERR_INVALID, "output array too small for the pushed batches");
+  running_ = false;
+  hflag_[0] = 1;
+  const int nb = count_;
+  const int nout = num_outputs();
+  cudaError_t e = cudaMemcpyAsync(&dhdr_->pad, hflag_, 4, cudaMemcpyHostToDevice, push_stream_);
+  if (e == cudaSuccess && nb > 0)
+    e = cudaMemcpyAsync(hres_, dscratch_, 8 * 4 * (size_t)nb, cudaMemcpyDeviceToHost, s_);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hflag_ + 1, dwerr_, 4, cudaMemcpyDeviceToHost, s_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(push_stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+  if (e != cudaSuccess) {
+    dev_free(arena_, s_);
+    arena_ = nullptr;
+    check_cuda(e, "stream finish");
+  }
+  int64_t err = hflag_[1] ? 1 : 0;
+  for (int b = 0; b < nb; b++) err |= (int64_t)(hres_[4 * (size_t)b + 2] & 0xFFFFFFFFull);
+  if (err || nb == 0) {
+    dev_free(arena_, s_);
+    arena_ = nullptr;
+    if (hflag_[1]) fail(GX_ERR_TIMEOUT, "the stream's kernel waited too long for a batch");
+    if (err) fail(GX_ERR_TIMEOUT, "compaction look-back wait timed out");
+    return;
+  }
+  for (int b = 0; b < nb; b++) {
+    const int64_t rows = (int64_t)hres_[4 * (size_t)b + 1];
+    if (out_rows) out_rows[b] = rows;
+    for (int j = 0; j < nout; j++) {
+      gx_column& c = out[(size_t)b * nout + j];
+      c = gx_column{};
+      c.type_id = plan_.outputs[j].type;
+      c.data = arena_ + doff_[j] + (size_t)row_off_[b] * type_size(plan_.outputs[j].type);
+      c.null_mask = (uint32_t*)(arena_ + moff_[j]) + row_off_[b] / 32;
+      c.size = rows;
+      c.capacity = std::max<int64_t>(rows_in_[b], 0);
+    }
+  }
+  adopt_output_views(arena_, out, nb * nout);
+  arena_ = nullptr;
+}
+
 }  // namespace gx
 
 // ------------------------------------------------------------------ C ABI
 struct gx_batch_runner {
   std::unique_ptr<gx::BatchRunner> r;
+};
+struct gx_batch_stream {
+  std::unique_ptr<gx::BatchStream> s;
 };
 
 namespace gx {
@@ -470,5 +709,50 @@ int gx_batch_runner_config(const gx_batch_runner* runner, int32_t* block_threads
 }
 
 void gx_batch_runner_destroy(gx_batch_runner* runner) { delete runner; }
+
+gx_batch_stream* gx_batch_stream_create(const gx_plan* plan, int max_batches, int64_t max_total_rows,
+                                        int block_threads, int words_per_warp, gx_status_info* status) {
+  gx_batch_stream* out = nullptr;
+  guarded_call(status, [&] {
+    const gx::CompiledPlan* cp = gx::single_chunk(plan);
+    if (!cp) gx::fail(GX_ERR_INVALID, "a batch stream needs a compiled plan with at most 32 outputs");
+    if (block_threads % 32 != 0) gx::fail(GX_ERR_INVALID, "block_threads must be a multiple of 32");
+    out = new gx_batch_stream{std::make_unique<gx::BatchStream>(*cp, max_batches, max_total_rows, block_threads / 32,
+                                                                 words_per_warp)};
+  });
+  return out;
+}
+
+int gx_batch_stream_start(gx_batch_stream* st, void* stream, gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!st) gx::fail(GX_ERR_INVALID, "null batch stream");
+    st->s->start((cudaStream_t)stream);
+  });
+}
+
+int gx_batch_stream_push(gx_batch_stream* st, const gx_column_view* columns, int num_columns, int* batch_index,
+                         gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!st || num_columns < 0 || (num_columns > 0 && !columns)) gx::fail(GX_ERR_INVALID, "bad arguments");
+    const int b = st->s->push(gx::to_views(columns, num_columns));
+    if (batch_index) *batch_index = b;
+  });
+}
+
+int gx_batch_stream_finish(gx_batch_stream* st, gx_column* out, int64_t* out_rows, int max_batches,
+                           gx_status_info* status) {
+  return guarded_call(status, [&] {
+    if (!st || (max_batches > 0 && !out)) gx::fail(GX_ERR_INVALID, "bad arguments");
+    st->s->finish(out, out_rows, max_batches);
+  });
+}
+
+void gx_batch_stream_destroy(gx_batch_stream* st) { delete st; }
+
+int gx_debug_batch_stream_wait_polls(gx_batch_stream* st, uint32_t polls) {
+  if (!st) return GX_ERR_INVALID;
+  st->s->set_wait_polls(polls);
+  return GX_OK;
+}
 
 }  // extern "C"

@@ -67,4 +67,66 @@ class BatchRunner {
   CUfunction captured_fn_ = nullptr;
 };
 
+// A queue of batches of one filter plan evaluated by one persistent kernel
+// (FUSED_STREAM) that runs while the host appends batches: start() launches
+// the kernel, which waits for work; push() copies a batch's descriptor and
+// tile offsets to the device and then publishes its tiles (ordered copies on a
+// side stream, no host synchronisation); finish() closes the queue, waits for
+// the kernel and returns every batch's output.  Each batch's output is what
+// gx_plan_execute returns for it alone.  A kernel that waits longer than
+// wait_polls x ~2 us for a batch gives up (GX_ERR_TIMEOUT at finish).
+class BatchStream {
+ public:
+  BatchStream(const CompiledPlan& base, int max_batches, int64_t max_rows, int warps, int words);
+  ~BatchStream();
+  BatchStream(const BatchStream&) = delete;
+  BatchStream& operator=(const BatchStream&) = delete;
+
+  void start(cudaStream_t s);
+  // the batch's columns must stay valid until finish(); returns its index
+  int push(const std::vector<ColumnView>& cols);
+  // out: num_outputs() columns per pushed batch (batch-major), all views of
+  // one allocation released with the last of them; out_rows: rows per batch
+  void finish(gx_column* out, int64_t* out_rows, int max_out_batches);
+  int pushed() const { return count_; }
+  bool running() const { return running_; }
+  int num_outputs() const { return (int)plan_.outputs.size(); }
+  void set_wait_polls(unsigned polls) { wait_polls_ = polls; }
+
+ private:
+  void release();
+  Plan plan_;
+  std::shared_ptr<CompiledPlan> variant_;
+  JitKernel kernel_{};
+  int max_batches_;
+  int64_t max_rows_;
+  int64_t tile_rows_ = 0;
+  int64_t max_tiles_ = 0;
+  int64_t arena_rows_ = 0;
+  unsigned wait_polls_ = 1u << 22;
+  // session state
+  bool running_ = false;
+  cudaStream_t s_ = nullptr;
+  int count_ = 0;
+  int64_t tiles_ = 0, rows_used_ = 0;
+  char* arena_ = nullptr;               // this session's outputs: every output's masks, then data
+  std::vector<size_t> moff_, doff_;     // per output: byte offset of its mask / data region
+  std::vector<int64_t> row_off_, rows_in_;
+  // device
+  KernelArgs* dargs_ = nullptr;
+  long long* dbase_ = nullptr;
+  BatchHeader* dhdr_ = nullptr;
+  uint64_t* dscratch_ = nullptr;        // per batch 4 words (row count at [1], error at [2]), then tile statuses
+  int* dwerr_ = nullptr;
+  // pinned host staging of the pushes' copies (one slot per batch: a copy may
+  // run after the host moved on)
+  KernelArgs* hargs_ = nullptr;
+  long long* hbase_ = nullptr;
+  long long* hpub_ = nullptr;
+  int* hflag_ = nullptr;                // [0] = 1 (closes the queue), [1] = the kernel's wait error
+  unsigned long long* hres_ = nullptr;
+  cudaStream_t push_stream_ = nullptr;
+  cudaEvent_t started_ = nullptr;
+};
+
 }  // namespace gx

@@ -742,7 +742,8 @@ static KernelKind kind_of(int k) {
     case 6: return KernelKind::FUSED_BATCHED;
     case 7: return KernelKind::FUSED_STAGED;
     case 8: return KernelKind::FUSED_TMA;
-    default: fail(GX_ERR_INVALID, "kernel kind must be 0..8");
+    case 9: return KernelKind::FUSED_STREAM;
+    default: fail(GX_ERR_INVALID, "kernel kind must be 0..9");
   }
 }
 

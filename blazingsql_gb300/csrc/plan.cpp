@@ -1664,27 +1664,71 @@ void emit_fused_tma(std::ostringstream& o, const Gen& g, const Plan& p, const Ti
 // order from one counter; every batch has its own look-back segment and row
 // counter, so a block's pending and next tiles may belong to different
 // batches, and each batch's result is exactly that of running it alone.
+// (streaming: the host appends batches while the kernel runs -- descriptors,
+// tile offsets, then the published tile count, each by an ordered copy -- and
+// closes the queue by setting hdr->pad; a block that claims a tile past the
+// published count waits for it (bounded: `wait_polls` polls 2 us apart, then
+// *werr = 1) or, once the queue is closed without it, stops.  Tile offsets of
+// unpublished batches hold INT64_MAX, so a lookup never passes the last
+// published batch.)
 void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, const std::vector<int>& pred_ids,
-                        const std::string& name) {
+                        const std::string& name, bool streaming = false) {
   o << "struct GxBatchHdr { unsigned long long tile_counter; long long total_tiles; int nbatch; int pad; };\n";
-  o << "extern \"C\" __global__ void GX_LB " << name
-    << "(const GxArgs* __restrict__ A, const long long* __restrict__ tile_base, GxBatchHdr* hdr) {\n";
+  // a batch's descriptor: streaming descriptors sit kArgsStride bytes apart,
+  // so that no cache line holds two of them (one is written while the kernel
+  // may have read its neighbour)
+  if (streaming)
+    o << "#define GX_BATCH(b) (*(const GxArgs*)((const char*)A + (size_t)(b) * " << kStreamArgsStride << "u))\n";
+  else
+    o << "#define GX_BATCH(b) (A[(b)])\n";
+  if (streaming) {
+    o << "extern \"C\" __global__ void GX_LB " << name
+      << "(const GxArgs* A, const volatile long long* tile_base, GxBatchHdr* hdr, int* werr, unsigned wait_polls) {\n";
+    o << "  const int nbatch = 0x7fffffff; (void)nbatch;\n";
+    // claim a tile; -1 once the queue is closed below it (or the wait gave up)
+    o << "  auto claim_ = [&]() -> long long {\n";
+    o << "    long long t = (long long)atomicAdd(&hdr->tile_counter, 1ull);\n";
+    o << "    unsigned polls = 0;\n";
+    o << "    while (true) {\n";
+    o << "      if (t < *(volatile long long*)&hdr->total_tiles) break;\n";
+    o << "      if (*(volatile int*)&hdr->pad != 0) {\n";  // closed: the published count is final
+    o << "        if (t < *(volatile long long*)&hdr->total_tiles) break;\n";
+    o << "        return -1;\n";
+    o << "      }\n";
+    o << "      if (*(volatile int*)werr != 0) return -1;\n";
+    o << "      if (++polls > wait_polls) { atomicExch(werr, 1); return -1; }\n";
+    o << "      __nanosleep(2000);\n";
+    o << "    }\n";
+    o << "    __threadfence();\n";  // the batch's descriptor and tile offsets were copied before its tiles were published
+    o << "    return t;\n";
+    o << "  };\n";
+  } else {
+    o << "extern \"C\" __global__ void GX_LB " << name
+      << "(const GxArgs* __restrict__ A, const long long* __restrict__ tile_base, GxBatchHdr* hdr) {\n";
+    o << "  const i64 total_tiles = hdr->total_tiles; const int nbatch = hdr->nbatch;\n";
+  }
   o << "  const int lane = threadIdx.x & 31; const int warp = threadIdx.x >> 5;\n";
-  o << "  const i64 total_tiles = hdr->total_tiles; const int nbatch = hdr->nbatch;\n";
   o << "  __shared__ unsigned long long s_claim;\n";
   o << "  __shared__ u32 s_cnt[2][GX_WARPS];\n";
   o << "  __shared__ u64 s_off[2][GX_WARPS];\n";
   o << "  __shared__ u64 s_base;\n";
-  o << "  if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
-  o << "  __syncthreads();\n";
-  o << "  const i64 gt0 = (i64)s_claim;\n";
-  o << "  if (gt0 >= total_tiles) return;\n";
+  if (streaming) {
+    o << "  if (threadIdx.x == 0) s_claim = (unsigned long long)claim_();\n";
+    o << "  __syncthreads();\n";
+    o << "  const i64 gt0 = (i64)s_claim;\n";
+    o << "  if (gt0 < 0) return;\n";
+  } else {
+    o << "  if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
+    o << "  __syncthreads();\n";
+    o << "  const i64 gt0 = (i64)s_claim;\n";
+    o << "  if (gt0 >= total_tiles) return;\n";
+  }
   o << "  int pb = 0;\n";
   o << "  while (pb + 1 < nbatch && tile_base[pb + 1] <= gt0) pb++;\n";
   o << "  i64 tile = gt0 - tile_base[pb];\n";
   o << "  u32 bal[GX_V]; u32 wcnt = 0u; int par = 0; u64 ptotal = 0ull;\n";
   o << "  {\n";
-  o << "    const GxArgs& a = A[pb];\n";
+  o << "    const GxArgs& a = GX_BATCH(pb);\n";
   o << "    const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   g.decl(o, pred_ids, "    ");
   g.emit_predicate(o, "    ");
@@ -1692,13 +1736,14 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "    if (lane == 0) s_cnt[0][warp] = wcnt;\n";
   o << "  }\n";
   o << "  __syncthreads();\n";
-  o << "  if (warp == 0) ptotal = gx_tile_publish(A[pb].tile_status, tile, s_cnt[0], s_off[0], GX_WARPS);\n";
+  o << "  if (warp == 0) ptotal = gx_tile_publish(GX_BATCH(pb).tile_status, tile, s_cnt[0], s_off[0], GX_WARPS);\n";
   o << "  while (true) {\n";
-  o << "    if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
+  if (streaming) o << "    if (threadIdx.x == 0) s_claim = (unsigned long long)claim_();\n";
+  else o << "    if (threadIdx.x == 0) s_claim = atomicAdd(&hdr->tile_counter, 1ull);\n";
   o << "    __syncthreads();\n";
   o << "    const i64 ngt = (i64)s_claim;\n";
   o << "    int nb = pb; i64 next = -1;\n";
-  o << "    if (ngt < total_tiles) {\n";
+  o << "    if (" << (streaming ? "ngt >= 0" : "ngt < total_tiles") << ") {\n";
   o << "      while (nb + 1 < nbatch && tile_base[nb + 1] <= ngt) nb++;\n";
   o << "      next = ngt - tile_base[nb];\n";
   o << "    }\n";
@@ -1706,7 +1751,7 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "    u32 nbal[GX_V]; u32 nwcnt = 0u;\n";
   o << "    #pragma unroll\n    for (int k = 0; k < GX_V; k++) nbal[k] = 0u;\n";
   o << "    if (next >= 0) {\n";
-  o << "      const GxArgs& a = A[nb];\n";
+  o << "      const GxArgs& a = GX_BATCH(nb);\n";
   o << "      const i64 w0 = next * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   g.decl(o, pred_ids, "      ");
   g.emit_predicate(o, "      ");
@@ -1716,8 +1761,8 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "    __syncthreads();\n";
   o << "    if (warp == 0) {\n";
   o << "      u64 ntotal = 0ull;\n";
-  o << "      if (next >= 0) ntotal = gx_tile_publish(A[nb].tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
-  o << "      const GxArgs& a = A[pb];\n";
+  o << "      if (next >= 0) ntotal = gx_tile_publish(GX_BATCH(nb).tile_status, next, s_cnt[npar], s_off[npar], GX_WARPS);\n";
+  o << "      const GxArgs& a = GX_BATCH(pb);\n";
   o << "      const i64 ntiles = (((a.n + 31) >> 5) + GX_TILE_WORDS - 1) / GX_TILE_WORDS;\n";
   o << "      const u64 excl = gx_lookback_resolve(a.tile_status, tile, ptotal, a.err, GX_SPINS);\n";
   o << "      if (lane == 0) {\n";
@@ -1730,7 +1775,7 @@ void emit_fused_batched(std::ostringstream& o, const Gen& g, const Plan& p, cons
   o << "    const u64 base_t = s_base;\n";
   o << "    if (base_t == ~0ull) break;\n";  // look-back gave up: error already recorded
   o << "    if (wcnt != 0u) {\n";
-  o << "      const GxArgs& a = A[pb];\n";
+  o << "      const GxArgs& a = GX_BATCH(pb);\n";
   o << "      u64 pos = base_t + s_off[par][warp];\n";
   o << "      const i64 w0 = tile * GX_TILE_WORDS + (i64)warp * GX_V;\n";
   emit_filter_writes_dense(o, g, p, "      ");
@@ -2133,13 +2178,14 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
     emit_fused_tma(o, g, p, L, name);
     return o.str();
   }
-  if (kind == KernelKind::FUSED_BATCHED) {
+  if (kind == KernelKind::FUSED_BATCHED || kind == KernelKind::FUSED_STREAM) {
     if (!p.has_filter()) fail(GX_ERR_INVALID, "the batched kernel runs filter plans");
     if (cfg.runtime_order || cfg.short_circuit) fail(GX_ERR_INVALID, "the batched kernel evaluates conjuncts in plan order");
     KernelConfig c = cfg;
     c.dense = true;
     Gen gb(p, c);
-    emit_fused_batched(o, gb, p, gb.predicate_cone(), name);
+    gb.reread_cols_ = g.reread_cols_;
+    emit_fused_batched(o, gb, p, gb.predicate_cone(), name, kind == KernelKind::FUSED_STREAM);
     return o.str();
   }
   o << "extern \"C\" __global__ void GX_LB " << name << "(const GxArgs a) {\n";

@@ -126,7 +126,11 @@ std::string generate_agg_kernel(const Plan& plan, const AggLayout& L, const Kern
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
 constexpr int GX_OUTPUTS_PER_KERNEL = 32;
 
-enum class KernelKind { PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED, FUSED_STAGED, FUSED_TMA };
+// FUSED_STREAM: the batched kernel fed by a queue that the host extends while
+// it runs (BatchStream, batch.cu)
+enum class KernelKind {
+  PROJECT, FUSED_FILTER, COUNT_FILTER, WRITE_FILTER, FUSED_BATCHED, FUSED_STAGED, FUSED_TMA, FUSED_STREAM
+};
 
 // Shared-memory layout of the tile-staged fused filter (FUSED_TMA): a ring of
 // `stages` input stages, each holding one tile (consumer warps x words x 32
@@ -189,5 +193,9 @@ struct KernelArgs {
   const int32_t* order_dev;         // if set: the order in device memory (written by an earlier kernel)
   uint32_t spin_limit;              // polls a bounded device wait makes before it gives up (0: default)
 };
+
+// Bytes between two batch descriptors of a batch stream (a multiple of the
+// 128-byte cache line, at least sizeof(KernelArgs)).
+constexpr size_t kStreamArgsStride = (sizeof(KernelArgs) + 255) / 256 * 256;
 
 }  // namespace gx

@@ -198,6 +198,13 @@ void alloc_output_set(const std::vector<int>& types, const std::vector<int64_t>&
   }
 }
 
+void adopt_output_views(void* base, gx_column* cols, int n) {
+  if (n <= 0) return;
+  auto* ar = new OutputArena{base, n};
+  std::lock_guard<std::mutex> g(g_arena_mu);
+  for (int i = 0; i < n; i++) g_arena_of[cols[i].data] = ar;
+}
+
 void* alloc_queue_scratch(const std::vector<int64_t>& status_words, uint64_t** status, cudaStream_t s) {
   const size_t nb = status_words.size();
   if (nb == 0) return nullptr;
@@ -420,6 +427,7 @@ static const char* kind_name(KernelKind k) {
     case KernelKind::FUSED_BATCHED: return "gx_filter_batched";
     case KernelKind::FUSED_STAGED: return "gx_filter_staged";
     case KernelKind::FUSED_TMA: return "gx_filter_tma";
+    case KernelKind::FUSED_STREAM: return "gx_filter_stream";
     default: return "gx_filter_write";
   }
 }

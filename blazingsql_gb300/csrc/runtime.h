@@ -47,6 +47,9 @@ constexpr size_t kQueueHeaderBytes = 256;
 void* alloc_output_queue(const std::vector<int>& types, const std::vector<int64_t>& caps,
                          const std::vector<int64_t>& status_words, gx_column* out, uint64_t** status,
                          cudaStream_t s);
+// Makes n columns that view distinct parts of one allocation `base` (from
+// dev_alloc) owners of it: the allocation is released with the last of them.
+void adopt_output_views(void* base, gx_column* cols, int n);
 // The headers and tile-status words of a queue without its outputs (a queue
 // whose outputs are allocated batch by batch): the same layout, zeroed; the
 // caller releases the returned base with dev_free once the queue completed.

@@ -366,6 +366,47 @@ int gx_batch_runner_run(gx_batch_runner* runner, const gx_column_view* columns, 
 int gx_batch_runner_config(const gx_batch_runner* runner, int32_t* block_threads, int32_t* words_per_warp);
 void gx_batch_runner_destroy(gx_batch_runner* runner);
 
+/* ---- batch stream: a persistent kernel fed while it runs ------------------
+ *
+ * The batched execution graph hands the Filter kernel batches one by one as
+ * they come out of the previous kernel (engine/src/execution_kernels/
+ * BatchProcessing.cpp:371-476, run by execution_graph/executor.cpp:217-255);
+ * the reference launches the interpreter per batch.  A batch stream keeps one
+ * persistent kernel running per plan: gx_batch_stream_start launches it and it
+ * waits for work; each gx_batch_stream_push hands it one more batch (its
+ * descriptor and tile offsets are copied to the device, then its tiles are
+ * published, by ordered asynchronous copies on a side stream -- no host
+ * synchronisation), and the kernel's blocks take the new tiles as they
+ * appear; gx_batch_stream_finish closes the queue, waits for the kernel and
+ * returns every batch's output, each exactly what gx_plan_execute returns for
+ * it alone.  A pushed batch's columns must stay valid until finish.  The
+ * kernel gives up after waiting about 8 s for a batch that does not come
+ * (finish then returns GX_ERR_TIMEOUT).  One session at a time per stream
+ * object.  No counterpart in the reference. */
+typedef struct gx_batch_stream gx_batch_stream;
+
+/* plan: a compiled filter plan (condition, at most 32 outputs, no literal
+ * outputs); a session takes at most max_batches batches of max_total_rows rows
+ * in all; block_threads / words_per_warp: the kernel's block shape (0: the
+ * plan's). */
+gx_batch_stream* gx_batch_stream_create(const gx_plan* plan, int max_batches, int64_t max_total_rows,
+                                        int block_threads, int words_per_warp, gx_status_info* status);
+/* Starts a session: launches the kernel on `stream`. */
+int gx_batch_stream_start(gx_batch_stream* st, void* stream, gx_status_info* status);
+/* Appends one batch (num_columns views); *batch_index: its position. */
+int gx_batch_stream_push(gx_batch_stream* st, const gx_column_view* columns, int num_columns, int* batch_index,
+                         gx_status_info* status);
+/* Closes the session: out receives num_outputs columns per pushed batch,
+ * batch-major (library-owned views of one allocation, each released by
+ * gx_free_columns), out_rows[b] batch b's surviving rows; max_batches: the
+ * batches `out` / `out_rows` have room for. */
+int gx_batch_stream_finish(gx_batch_stream* st, gx_column* out, int64_t* out_rows, int max_batches,
+                           gx_status_info* status);
+void gx_batch_stream_destroy(gx_batch_stream* st);
+/* Test hook: the polls (about 2 us apart) the kernel waits for a batch before
+ * it gives up (default 2^22). */
+int gx_debug_batch_stream_wait_polls(gx_batch_stream* st, uint32_t polls);
+
 /* ---- learned conjunct ordering (no counterpart in the reference) ---------
  *
  * A learner wraps a compiled filter plan (condition = AND of side-effect-free
@@ -470,7 +511,8 @@ const char* gx_version(void);
  * (conjunct order given at launch), 5 the learner's labelling count pass
  * (per-conjunct pass counts), 6 the batch runner's persistent kernel, 7 the
  * learner's staged fused pass (conjunct columns copied to shared memory by TMA), 8 the tile-staged
- * single-pass filter (every column's tile copied to shared memory by bulk copies).  Writes at most buf_len
+ * single-pass filter (every column's tile copied to shared memory by bulk copies), 9 the batch
+ * stream's persistent kernel.  Writes at most buf_len
  * bytes (NUL-terminated) and returns the full length, or -1 on error. */
 int64_t gx_debug_kernel_source(const gx_plan* plan, int kind, const uint8_t* column_has_mask, char* buf,
                                int64_t buf_len, gx_status_info* status);
