@@ -41,6 +41,7 @@ is the literal repeated (:825).  Only tests/ use this module.
 """
 from __future__ import annotations
 
+import math
 import re
 from typing import List, Optional, Sequence, Tuple
 
@@ -176,19 +177,35 @@ def rewrite(texts: Sequence[str], string_cols: Sequence[int], ncols: int) -> Tup
     return out, ops
 
 
-STRING_RESULTS = {"CASE", "SLICE", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE", "CONCAT", "TO_STRING"}
+STRING_RESULTS = {"CASE", "SLICE", "SLICE_COLS", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE", "CONCAT",
+                  "TO_STRING"}
 PARSE_TYPES = {"CAST_TINYINT": T.INT8, "CAST_SMALLINT": T.INT16, "CAST_INTEGER": T.INT32, "CAST_BIGINT": T.INT64,
                "CAST_DATE": T.TIMESTAMP_DAYS, "CAST_TIMESTAMP_SECONDS": T.TIMESTAMP_SECONDS,
                "CAST_TIMESTAMP_MILLISECONDS": T.TIMESTAMP_MILLISECONDS,
-               "CAST_TIMESTAMP_MICROSECONDS": T.TIMESTAMP_MICROSECONDS, "CAST_TIMESTAMP": T.TIMESTAMP_NANOSECONDS}
+               "CAST_TIMESTAMP_MICROSECONDS": T.TIMESTAMP_MICROSECONDS, "CAST_TIMESTAMP": T.TIMESTAMP_NANOSECONDS,
+               "CAST_FLOAT": T.FLOAT32, "CAST_DOUBLE": T.FLOAT64}
 
 
 def string_function(name, a, strcol, int_lit):
     """The operator tuple of one of evaluate_string_functions' functions, or None."""
     if name == "SUBSTRING" and len(a) in (2, 3) and strcol(a[0]):
-        start = max(int_lit(a[1]), 1) - 1
-        length = int_lit(a[2]) if len(a) == 3 else -1
-        return ("SLICE", int(a[0].value[1:]), start, start + length if length >= 0 else None, 1)
+        def lit(x):
+            try:
+                return int_lit(x)
+            except ValueError:
+                return None
+        if lit(a[1]) is not None and (len(a) == 2 or lit(a[2]) is not None):
+            start = max(int_lit(a[1]), 1) - 1
+            length = int_lit(a[2]) if len(a) == 3 else -1
+            return ("SLICE", int(a[0].value[1:]), start, start + length if length >= 0 else None, 1)
+        # positions from columns or expressions (LogicalProject.cpp:221-300): a
+        # literal start is max(start, 1), any start then 1 less (zero-based,
+        # transform_start_to_zero_based_indexing), the stop start + length
+        # (transform_length_to_end), no length: to the end
+        st = lit(a[1])
+        start = str(max(st, 1) - 1) if st is not None else "-(" + rebuild(a[1], typed=True) + ", 1)"
+        stop = "+(" + start + ", " + rebuild(a[2], typed=True) + ")" if len(a) == 3 else None
+        return ("SLICE_COLS", int(a[0].value[1:]), start, stop)
     if name == "LEFT" and len(a) == 2 and strcol(a[0]):
         return ("SLICE", int(a[0].value[1:]), 0, max(int_lit(a[1]), 0), 1)
     if name == "RIGHT" and len(a) == 2 and strcol(a[0]):
@@ -214,13 +231,142 @@ def string_function(name, a, strcol, int_lit):
         return ("TO_STRING", int(a[0].value[1:]) if a[0].var else rebuild(a[0], typed=True))
     if name in PARSE_TYPES and len(a) == 1 and strcol(a[0]):
         t = PARSE_TYPES[name]
-        fmt = None if t in (T.INT8, T.INT16, T.INT32, T.INT64) else \
+        fmt = None if t in (T.INT8, T.INT16, T.INT32, T.INT64, T.FLOAT32, T.FLOAT64) else \
             ("%Y-%m-%d" if t == T.TIMESTAMP_DAYS else "%Y-%m-%d %H:%M:%S")
         return ("PARSE", int(a[0].value[1:]), t, fmt)
     if name in ("TO_DATE", "TO_TIMESTAMP") and len(a) == 2 and strcol(a[0]) and _is_lit(a[1]):
         return ("PARSE", int(a[0].value[1:]), T.TIMESTAMP_DAYS if name == "TO_DATE" else T.TIMESTAMP_NANOSECONDS,
                 _unquote(a[1].value))
     return None
+
+
+def _slice_cols(v: str, start: int, stop: int) -> str:
+    """cudf::strings::slice_strings with a start and a stop per row: the start
+    clamped at 0, a stop below 0 or past the end meaning the end, empty when
+    the start is not before the stop."""
+    L = len(v)
+    b = max(start, 0)
+    if b >= L:
+        return ""
+    e = L if stop < 0 or stop > L else stop
+    return v[b:e] if b < e else ""
+
+
+# Powers of ten for scaling a double into [1, 10) by the binary decomposition
+# of its decimal exponent (cudf::strings::from_floats' normalisation).
+_SCALE = ((256, 1e256, 1e-255), (128, 1e128, 1e-127), (64, 1e64, 1e-63), (32, 1e32, 1e-31), (16, 1e16, 1e-15),
+          (8, 1e8, 1e-7), (4, 1e4, 1e-3), (2, 1e2, 1e-1), (1, 1e1, 1e0))
+
+
+def format_float(x: float) -> str:
+    """CAST of a FLOAT64 (FLOAT32 widened) to VARCHAR as cudf::strings::from_floats
+    writes it: values in [1e-4, 1e9) in fixed notation, others as d.ddd with a
+    signed exponent of at least two digits; 9 significant digits at most (the
+    integer part's digits take from the 9 decimal places), the last one rounded
+    half up from the scaled remainder, trailing zeros dropped, at least one
+    decimal place; NaN, Inf, -Inf.  Pinned by process_project.cpp:389-412."""
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "-Inf" if x < 0 else "Inf"
+    neg = math.copysign(1.0, x) < 0
+    v = abs(float(x))
+    if v == 0.0:
+        return "-0.0" if neg else "0.0"
+    exp10 = 0
+    if v >= 1e9:
+        for fx, p, _ in _SCALE:
+            if v >= p:
+                v = v / p
+                exp10 += fx
+    elif v < 1e-4:
+        for fx, p, lo in _SCALE:
+            if v < lo:
+                v = v * p
+                exp10 -= fx
+    whole = int(v)
+    places, width = 9, 10 ** 9
+    i = whole
+    while i >= 10:
+        places -= 1
+        width //= 10
+        i //= 10
+    frac = (v - float(whole)) * float(width)
+    dec = int(frac)
+    dec += int(2.0 * (frac - float(dec)))
+    if dec >= width:
+        dec = 0
+        whole += 1
+        if exp10 and whole >= 10:
+            exp10 += 1
+            whole = 1
+    while dec % 10 == 0 and places > 0:
+        dec //= 10
+        places -= 1
+    out = ("-" if neg else "") + str(whole) + "." + (str(dec).zfill(places) if places > 0 else "0")
+    if exp10:
+        out += "e" + ("-" if exp10 < 0 else "+") + str(abs(exp10)).zfill(2)
+    return out
+
+
+def parse_float(v: str) -> float:
+    """CAST of a string to FLOAT64 as cudf::strings::to_floats reads it: an
+    optional sign, NaN / Inf / Infinity, else digits with one optional decimal
+    point and an optional e / E exponent; up to 19 significant digits are
+    accumulated into an integer (later ones only move the exponent), which is
+    then scaled by exact powers of ten (divided for a negative exponent, in
+    steps of 1e22), so that up to 15 digits and |exponent| <= 22 convert
+    exactly rounded.  Anything else reads as the digits before it (0 for
+    none).  Pinned by process_project.cpp:414-445."""
+    i, n = 0, len(v)
+    neg = False
+    if i < n and v[i] in "+-":
+        neg = v[i] == "-"
+        i += 1
+    rest = v[i:]
+    if rest.startswith("NaN"):
+        return math.nan
+    if rest.startswith("Inf"):
+        return -math.inf if neg else math.inf
+    mant, digits, exp10, dot = 0, 0, 0, False
+    while i < n:
+        c = v[i]
+        if c == "." and not dot:
+            dot = True
+        elif "0" <= c <= "9":
+            if digits < 19:
+                mant = mant * 10 + (ord(c) - 48)
+                if mant:
+                    digits += 1
+                if dot:
+                    exp10 -= 1
+            elif not dot:
+                exp10 += 1
+        else:
+            break
+        i += 1
+    if i < n and v[i] in "eE":
+        j, eneg, e = i + 1, False, 0
+        if j < n and v[j] in "+-":
+            eneg = v[j] == "-"
+            j += 1
+        while j < n and "0" <= v[j] <= "9":
+            e = min(e * 10 + (ord(v[j]) - 48), 100000)
+            j += 1
+        exp10 += -e if eneg else e
+    x = float(mant)
+    if exp10 >= 0:
+        while exp10 > 22:
+            x = x * 1e22
+            exp10 -= 22
+        x = x * float(10 ** exp10)
+    else:
+        e = -exp10
+        while e > 22:
+            x = x / 1e22
+            e -= 22
+        x = x / float(10 ** e)
+    return -x if neg else x
 
 
 def _slice(v: str, start, stop, step):
@@ -265,6 +411,8 @@ def format_value(t: int, x) -> str:
     """cast_to_str_functor for one valid value."""
     if t == T.BOOL8:
         return "true" if x else "false"
+    if t in (T.FLOAT32, T.FLOAT64):
+        return format_float(float(x))
     if t in (T.INT8, T.INT16, T.INT32, T.INT64, T.UINT8, T.UINT16, T.UINT32, T.UINT64):
         return str(int(x))
     if t == T.TIMESTAMP_DAYS:
@@ -312,6 +460,8 @@ def _format_items(fmt: str):
 
 def parse_value(t: int, v: str, fmt: Optional[str] = None) -> int:
     """to_integers / to_timestamps of one valid string."""
+    if t in (T.FLOAT32, T.FLOAT64):
+        return parse_float(v)
     b = v.encode("utf-8")
     if t in (T.INT8, T.INT16, T.INT32, T.INT64):
         neg = b[:1] == b"-"
@@ -398,6 +548,17 @@ def prepass(cols: Sequence, strings: dict, texts: Sequence[str], nthreads: int =
                  "LOWER": lambda v: v.lower(), "INITCAP": _initcap,
                  "TRIM": lambda v: _trim(v, op[2], op[3]), "REPLACE": lambda v: v.replace(op[2], op[3])}[op[0]]
             strings[k] = [None if v is None else f(v) for v in src]
+            table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] == "SLICE_COLS":
+            def positions(text, default):
+                if text is None:
+                    return [default] * n
+                c = pyoracle.evaluate_expressions(table, [text], nthreads)[0]
+                valid = unpack_validity(c.mask, n) if c.mask is not None else np.ones(n, dtype=bool)
+                return [int(c.data[i]) if valid[i] else 0 for i in range(n)]  # NULL positions read 0
+            b0, e0 = positions(op[2], 0), positions(op[3], 2 ** 31 - 1)
+            src = strings[op[1]]
+            strings[k] = [None if v is None else _slice_cols(v, b0[i], e0[i]) for i, v in enumerate(src)]
             table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
         elif op[0] == "CONCAT":
             def side(o):

@@ -177,7 +177,9 @@ def extract(root):
                            "test_string_case"),
         _string_table_test(root, "engine/tests/new-tests/process_project.cpp", "ProjectTestString",
                            "test_string_nested_case"),
-    ]
+    ] + [_string_table_test(root, "engine/tests/new-tests/process_project.cpp", "ProjectTestString", t)
+         for t in ("test_string_like", "test_string_substring", "test_string_substring_null", "test_char_length",
+                   "test_string_concat", "test_cast_to_string", "test_cast_from_string")]
     return out
 
 
@@ -201,15 +203,18 @@ def _brace_groups(text):
 
 def _wrapper_columns(block):
     cols = []
-    pat = r'(strings_column_wrapper|fixed_width_column_wrapper<(\w+)>)\s+(\w+)\s*[\({](.*?)[\)}];'
+    pat = r'(strings_column_wrapper|fixed_width_column_wrapper<([^>]*)>)\s+(\w+)\s*[\({](.*?)[\)}];'
     for m in re.finditer(pat, block, re.S):
-        kind = "string" if m.group(1).startswith("strings") else m.group(2)
+        # element type: bool, int32_t, double, ...; timestamp wrappers
+        # (cudf::timestamp_s, cudf::timestamp_s::rep) by their unit
+        kind = "string" if m.group(1).startswith("strings") else m.group(2).split(",")[0].strip().replace("cudf::", "")
         body = m.group(4)
         groups = _brace_groups(body)
         if kind == "string":
             values = [bytes(v, "utf-8").decode("unicode_escape") for v in re.findall(r'"((?:[^"\\]|\\.)*)"', groups[0])]
         elif kind == "bool":
-            values = [1 if w == "true" else 0 for w in re.findall(r"true|false", groups[0])]
+            words = re.findall(r"true|false", groups[0])
+            values = [1 if w == "true" else 0 for w in words] if words else _numbers(groups[0])
         else:
             values = _numbers(groups[0])
         valid = _numbers(groups[1]) if len(groups) > 1 else None

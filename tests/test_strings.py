@@ -137,18 +137,23 @@ def _gold_table(t):
             strings[i] = [v if valid is None or valid[k] else None for k, v in enumerate(c["values"])]
             cols.append(None)
         else:
-            assert c["kind"] == "int32_t"
-            cols.append(HostColumn(T.INT32, np.array(c["values"], dtype=np.int32),
+            t, dt = GOLD_KINDS[c["kind"]]
+            cols.append(HostColumn(t, np.array(c["values"], dtype=dt),
                                    pack_validity(valid) if valid is not None else None))
     return cols, strings
+
+
+# element kinds of the reference's column wrappers
+GOLD_KINDS = {"int32_t": (T.INT32, np.int32), "int": (T.INT32, np.int32), "bool": (T.BOOL8, np.uint8),
+              "double": (T.FLOAT64, np.float64), "timestamp_s": (T.TIMESTAMP_SECONDS, np.int64),
+              "timestamp_ns": (T.TIMESTAMP_NANOSECONDS, np.int64)}
 
 
 def _gold_expected(c):
     valid = c["valid"]
     if c["kind"] == "string":
         return [v if valid is None or valid[k] else None for k, v in enumerate(c["values"])]
-    t = {"int32_t": T.INT32, "bool": T.BOOL8}[c["kind"]]
-    dt = np.int32 if t == T.INT32 else np.uint8
+    t, dt = GOLD_KINDS[c["kind"]]
     return HostColumn(t, np.array(c["values"], dtype=dt),
                       pack_validity(np.array(valid, dtype=bool)) if valid is not None else None)
 
@@ -168,14 +173,26 @@ def _compare(got, exp, what):
             assert_columns_equal(g, e, 0, f"{what} col {i}")
 
 
-def _project_expr(query):
-    return re.fullmatch(r"LogicalProject\(EXPR\$0=\[(.*)\]\)", query).group(1)
+def _project_exprs(query):
+    """The expressions of a LogicalProject(EXPR$0=[...], EXPR$1=[...]) query part."""
+    body = re.fullmatch(r"LogicalProject\((.*)\)", query).group(1)
+    out, depth, start = [], 0, None
+    for i, ch in enumerate(body):
+        if ch == "[":
+            if depth == 0:
+                start = i + 1
+            depth += 1
+        elif ch == "]":
+            depth -= 1
+            if depth == 0:
+                out.append(body[start:i])
+    return out
 
 
 @pytest.mark.parametrize("name", sorted(STRING_TABLES))
 def test_reference_string_tables_oracle(name):
     """The oracle reproduces the reference's string-table tests (filter_tests.cpp:174-215,
-    process_project.cpp:447-485)."""
+    process_project.cpp:286-485)."""
     t = STRING_TABLES[name]
     cols, strings = _gold_table(t)
     exp = [_gold_expected(c) for c in t["expected"]]
@@ -184,7 +201,7 @@ def test_reference_string_tables_oracle(name):
         got, rows = strings_ref.process_filter(cols, strings, cond)
         assert rows == len(t["expected"][0]["values"])
     else:
-        got = strings_ref.evaluate_expressions(cols, strings, [_project_expr(t["query"])])
+        got = strings_ref.evaluate_expressions(cols, strings, _project_exprs(t["query"]))
     _compare(got, exp, name)
 
 
