@@ -19,7 +19,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgxeval.so")
 
 SOURCES = ["frontend.cpp", "plan.cpp", "jit.cpp", "driver.cpp", "capi.cpp", "runtime.cu", "noalloc.cu", "learned.cu",
-           "batch.cu", "aggregate.cu", "str_prepass.cu"]
+           "batch.cu", "aggregate.cu", "str_prepass.cu", "regex.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,5 +1,6 @@
 // frontend.cpp -- RexNode text -> typed expression tree (see frontend.h).
 #include "frontend.h"
+#include "regex.h"
 
 #include <functional>
 
@@ -1105,7 +1106,8 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
                         std::vector<StringOp>& ops) {
   bool any = false;
   for (int t : schema) any |= t == STRING;
-  for (const auto& t : texts) any |= t.find('\'') != std::string::npos;
+  // a CAST to VARCHAR / CHAR makes a string column from typed ones
+  for (const auto& t : texts) any |= t.find('\'') != std::string::npos || t.find("CHAR") != std::string::npos;
   if (!any) return;
   // the schema grows by one column per operator
   std::vector<int> types = schema;
@@ -1149,10 +1151,18 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
       // :212-220: start = max(start, 1) - 1; stop = start + length when a length >= 0 is given
       int st = 0, len = -1;
       need_strcol(a[0], "SUBSTRING");
-      if (!int_literal(a[1], &st) || (a.size() == 3 && !int_literal(a[2], &len)))
-        fail(GX_ERR_UNSUPPORTED, "SUBSTRING with non-literal positions");
       op.kind = StringOp::SLICE;
       op.col = a[0]->col;
+      const bool lit_start = int_literal(a[1], &st);
+      if (!lit_start || (a.size() == 3 && !int_literal(a[2], &len))) {
+        // :221-300, positions from columns or expressions: a literal start is
+        // max(start, 1), any start then one less (transform_start_to_zero_based_indexing,
+        // utilities/transform.cu:44-68); the stop is start + length
+        // (transform_length_to_end, transform.cu:15-42); no length: to the end
+        op.pos0 = lit_start ? std::to_string(std::max(st, 1) - 1) : "-(" + rebuild_typed(a[1]) + ", 1)";
+        if (a.size() == 3) op.pos1 = "+(" + op.pos0 + ", " + rebuild_typed(a[2]) + ")";
+        return true;
+      }
       op.i0 = std::max(st, 1) - 1;
       op.i0_valid = true;
       op.i1 = len >= 0 ? op.i0 + len : 0;
@@ -1200,6 +1210,28 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
       op.literal = unquote(a[1]->token);
       return true;
     }
+    if (t == "REGEXP_REPLACE" && a.size() >= 3 && a.size() <= 6) {
+      // :149-183: a string column, a pattern, a replacement and an optional position
+      if (a.size() > 4) fail(GX_ERR_UNSUPPORTED, "Optional parameters occurrence and match_type are not yet supported.");
+      if (a[0]->kind == Expr::LIT) fail(GX_ERR_UNSUPPORTED, "REGEXP_REPLACE function not supported for string literals");
+      need_strcol(a[0], "REGEXP_REPLACE");
+      if (!is_string_literal(a[1]) || !is_string_literal(a[2]))
+        fail(GX_ERR_UNSUPPORTED, "REGEXP_REPLACE with a non-literal pattern or replacement");
+      op.kind = StringOp::REGEXP_REPLACE;
+      op.col = a[0]->col;
+      op.literal = unquote(a[1]->token);
+      op.literal2 = unquote(a[2]->token);
+      if (a.size() == 4) {
+        int st = 0;
+        if (!int_literal(a[3], &st)) fail(GX_ERR_UNSUPPORTED, "REGEXP_REPLACE with a non-literal position");
+        if (st - 1 < 0) fail(GX_ERR_INVALID, "Position must be greater than zero.");  // :164
+        op.i0 = st - 1;
+        op.i0_valid = true;
+      }
+      std::string program, tmpl;
+      compile_regex_replace(op.literal, op.literal2, &program, &tmpl);  // rejects what is not supported now
+      return true;
+    }
     if (t == "REPLACE" && a.size() == 3) {
       need_strcol(a[0], "REPLACE");
       if (!is_string_literal(a[1]) || !is_string_literal(a[2]))
@@ -1226,14 +1258,13 @@ void rewrite_string_ops(std::vector<std::string>& texts, const std::vector<int>&
         {"CAST_FLOAT", FLOAT32}, {"CAST_DOUBLE", FLOAT64}};
     auto pt = parse_types.find(t);
     if (pt != parse_types.end() && a.size() == 1 && strcol(a[0])) {
-      if (pt->second == FLOAT32 || pt->second == FLOAT64)
-        fail(GX_ERR_UNSUPPORTED, "CAST of a string column to a floating-point type");
       op.kind = StringOp::PARSE;
       op.col = a[0]->col;
       op.type = pt->second;
       // to_timestamps' formats for the CASTs (LogicalProject.cpp:468-528)
       if (pt->second == TIMESTAMP_DAYS) op.literal = "%Y-%m-%d";
-      else if (pt->second != INT8 && pt->second != INT16 && pt->second != INT32 && pt->second != INT64)
+      else if (pt->second != INT8 && pt->second != INT16 && pt->second != INT32 && pt->second != INT64 &&
+               pt->second != FLOAT32 && pt->second != FLOAT64)
         op.literal = "%Y-%m-%d %H:%M:%S";
       return true;
     }

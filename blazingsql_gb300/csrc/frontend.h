@@ -81,13 +81,16 @@ struct StringOp {
   enum Kind {
     LIKE = 0, EQ, NE, LT, LE, GT, GE, CHAR_LENGTH,
     CASE,       // THEN (col / literal / null) where cond is true, else ELSE (col2 / literal2 / null)
-    SLICE,      // cudf::strings::slice_strings by characters: [i0, i1) with validity flags, step (+1 / -1)
+    SLICE,      // cudf::strings::slice_strings by characters: [i0, i1) with validity flags, step (+1 / -1),
+                // or [pos0, pos1) per row
     UPPER, LOWER, INITCAP,
     TRIM,       // side i0 (0 both, 1 leading, 2 trailing), characters to strip in `literal`
     REPLACE,    // every `literal` by `literal2`
     CONCAT,     // (col | literal) followed by (col2 | literal2)
     TO_STRING,  // CAST to VARCHAR of column `col` (or of the expression `cond`), formatted by its type
-    PARSE       // CAST of string column `col` to `type` (integers, DATE, TIMESTAMPs)
+    PARSE,      // CAST of string column `col` to `type` (integers, floating point, DATE, TIMESTAMPs)
+    REGEXP_REPLACE  // matches of pattern `literal` replaced by template `literal2`, after the first i0
+                    // characters when i0_valid
   };
   Kind kind = LIKE;
   int col = -1;         // the (first) string column; CASE: the THEN column, or -1
@@ -103,6 +106,10 @@ struct StringOp {
   bool then_null = false, else_null = false;
   int i0 = 0, i1 = 0, step = 1;
   bool i0_valid = false, i1_valid = false;
+  // SLICE with positions per row (SUBSTRING whose start or length is not a
+  // literal): the texts of the zero-based start and of the stop (empty: to
+  // the end), over the columns before this operator; i0 / i1 are then unused
+  std::string pos0, pos1;
   int type = 0;  // PARSE: the result type
   // CONCAT of more than two parts: parts 3, 4, ... (a column, or -1 and the literal)
   std::vector<int> more_cols;
@@ -111,7 +118,7 @@ struct StringOp {
     return kind == o.kind && col == o.col && literal == o.literal && col2 == o.col2 && cond == o.cond &&
            literal2 == o.literal2 && then_null == o.then_null && else_null == o.else_null && i0 == o.i0 &&
            i1 == o.i1 && step == o.step && i0_valid == o.i0_valid && i1_valid == o.i1_valid && type == o.type &&
-           more_cols == o.more_cols && more_lits == o.more_lits;
+           more_cols == o.more_cols && more_lits == o.more_lits && pos0 == o.pos0 && pos1 == o.pos1;
   }
   int result_type() const {
     switch (kind) {

@@ -18,6 +18,8 @@
 // (cudf::strings::count_characters).  A NULL string gives NULL.
 #include "str_prepass.h"
 
+#include "regex_vm.h"
+
 #include <algorithm>
 #include <array>
 #include <cstring>
@@ -379,6 +381,13 @@ struct XformArgs {
   int64_t num_off;
   int num_type;
   int i0, i1, step, i0v, i1v;
+  // SLICE with positions per row: the start and stop columns (integer types,
+  // offset 0; no stop column: to the end), a NULL position read as 0
+  const void* p0;
+  const void* p1;
+  const uint32_t* p0m;
+  const uint32_t* p1m;
+  int p0t, p1t;
   const unsigned char* s1;  // TRIM: characters to strip; REPLACE: target
   int l1;
   const unsigned char* s2;  // REPLACE: replacement
@@ -467,6 +476,77 @@ __device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {
   return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
 }
 
+// A double as cudf::strings::from_floats writes it (the CAST to VARCHAR of
+// FLOAT and DOUBLE columns, LogicalProject.cpp:62-92): NaN, Inf, -Inf; values
+// in [1e-4, 1e9) in fixed notation, others scaled into [1, 10) by the binary
+// decomposition of their decimal exponent and followed by e, its sign and at
+// least two digits; at most 9 significant digits (the integer part's digits
+// taken from 9 decimal places), the last rounded half up from the scaled
+// remainder, trailing zeros dropped but one decimal place kept.  Every
+// product, quotient and difference is a single correctly rounded operation
+// (no contraction into fused multiply-adds), so the digits are those of the
+// same steps in any IEEE binary64 arithmetic.
+__device__ int format_double(double x, unsigned char* d) {
+  const unsigned char* nan_t = (const unsigned char*)"NaN";
+  const unsigned char* inf_t = (const unsigned char*)"-Inf";
+  if (isnan(x)) return put(d, 0, nan_t, 3);
+  const bool neg = signbit(x);
+  if (isinf(x)) return neg ? put(d, 0, inf_t, 4) : put(d, 0, inf_t + 1, 3);
+  int at = 0;
+  if (neg) at = put(d, 0, inf_t, 1);
+  double v = fabs(x);
+  if (v == 0.0) return put(d, at, (const unsigned char*)"0.0", 3);
+  const int fx[9] = {256, 128, 64, 32, 16, 8, 4, 2, 1};
+  const double up[9] = {1e256, 1e128, 1e64, 1e32, 1e16, 1e8, 1e4, 1e2, 1e1};
+  const double lo[9] = {1e-255, 1e-127, 1e-63, 1e-31, 1e-15, 1e-7, 1e-3, 1e-1, 1e0};
+  int exp10 = 0;
+  if (v >= 1e9) {
+    for (int k = 0; k < 9; k++)
+      if (v >= up[k]) {
+        v = __ddiv_rn(v, up[k]);
+        exp10 += fx[k];
+      }
+  } else if (v < 1e-4) {
+    for (int k = 0; k < 9; k++)
+      if (v < lo[k]) {
+        v = __dmul_rn(v, up[k]);
+        exp10 -= fx[k];
+      }
+  }
+  uint64_t whole = (uint64_t)v;  // below 1e9 here
+  int places = 9;
+  uint64_t width = 1000000000ull;
+  for (uint64_t i = whole; i >= 10; i /= 10) {
+    places--;
+    width /= 10;
+  }
+  const double frac = __dmul_rn(__dsub_rn(v, (double)whole), (double)width);
+  uint64_t dec = (uint64_t)frac;
+  dec += (uint64_t)__dmul_rn(2.0, __dsub_rn(frac, (double)dec));
+  if (dec >= width) {
+    dec = 0;
+    whole++;
+    if (exp10 != 0 && whole >= 10) {
+      exp10++;
+      whole = 1;
+    }
+  }
+  while (places > 0 && dec % 10 == 0) {
+    dec /= 10;
+    places--;
+  }
+  const unsigned char dot = '.', e = 'e', plus = '+', minus = '-', zero = '0';
+  at = civil_digits(d, at, (int64_t)whole, 1);
+  at = put(d, at, &dot, 1);
+  at = places > 0 ? civil_digits(d, at, (int64_t)dec, places) : put(d, at, &zero, 1);
+  if (exp10 != 0) {
+    at = put(d, at, &e, 1);
+    at = put(d, at, exp10 < 0 ? &minus : &plus, 1);
+    at = civil_digits(d, at, exp10 < 0 ? -exp10 : exp10, 2);
+  }
+  return at;
+}
+
 // formats row o of the typed column (cast_to_str_functor, LogicalProject.cpp:62-92)
 __device__ int format_typed(const void* num, const uint32_t* mask, int64_t off, int type, int64_t o,
                              unsigned char* d, bool& valid) {
@@ -497,6 +577,8 @@ __device__ int format_typed(const void* num, const uint32_t* mask, int64_t off, 
                        : ((const uint64_t*)num)[q];
       return civil_digits(d, 0, (int64_t)u, 1);
     }
+    case FLOAT32: return format_double((double)((const float*)num)[q], d);
+    case FLOAT64: return format_double(((const double*)num)[q], d);
     default: break;
   }
   // timestamps: "%Y-%m-%d" for days, "%Y-%m-%d %H:%M:%S" otherwise
@@ -544,6 +626,20 @@ __device__ __forceinline__ bool is_segment_kind(const XformArgs& a) {
           a.b.kind != StrSource::FORMAT);
 }
 
+// row o of an integer position column, 0 where it is NULL
+__device__ __forceinline__ int64_t row_position(const void* p, const uint32_t* m, int t, int64_t o) {
+  if (!bit_of(m, o)) return 0;
+  switch (t) {
+    case INT8: return ((const int8_t*)p)[o];
+    case INT16: return ((const int16_t*)p)[o];
+    case INT32: return ((const int32_t*)p)[o];
+    case UINT8: return ((const uint8_t*)p)[o];
+    case UINT16: return ((const uint16_t*)p)[o];
+    case UINT32: return ((const uint32_t*)p)[o];
+    default: return ((const int64_t*)p)[o];  // INT64, UINT64
+  }
+}
+
 __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char*& p1, int& n1,
                               const unsigned char*& p2, bool& valid) {
   const unsigned char* p;
@@ -564,6 +660,26 @@ __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char
     return n + m;
   }
   if (!valid) return 0;
+  if (a.kind == StringOp::SLICE && a.p0) {
+    // cudf::strings::slice_strings with a start and a stop per row: the start
+    // clamped at 0, a stop below 0 or past the end meaning the end, empty when
+    // the start is not before the stop
+    const int64_t s0 = row_position(a.p0, a.p0m, a.p0t, o);
+    const int64_t s1 = a.p1 ? row_position(a.p1, a.p1m, a.p1t, o) : -1;
+    int L = 0;
+    for (int i = 0; i < n; i++) L += (p[i] & 0xC0) != 0x80;
+    const int64_t b = s0 > 0 ? s0 : 0;
+    if (b >= L) return 0;
+    const int64_t e = (s1 < 0 || s1 > L) ? L : s1;
+    if (b >= e) return 0;
+    int bb = 0, c = 0;
+    while (c < b) { bb += utf8_len(p[bb]); c++; }
+    int eb = bb;
+    while (c < e) { eb += utf8_len(p[eb]); c++; }
+    p1 = p + bb;
+    n1 = eb - bb;
+    return n1;
+  }
   if (a.kind == StringOp::SLICE && a.i0v && a.i1v && a.i0 >= 0 && a.i1 >= 0) {
     // [i0, i1) from the front (SUBSTRING with a length, LEFT): walk at most i1
     // characters; the same clipping as below, without counting the rest
@@ -612,6 +728,16 @@ __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char
   p1 = p + b;
   n1 = e - b;
   return n1;
+}
+
+// REGEXP_REPLACE of row o (cudf::strings::replace_with_backrefs,
+// LogicalProject.cpp:149-183), by the Pike VM of regex_vm.h
+__device__ int regex_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
+  const unsigned char* p;
+  int n;
+  source_row(a.a, o, p, n, valid);
+  if (!valid) return 0;
+  return regex_replace_row(a.s1, a.s2, a.l2, p, n, a.i0v ? a.i0 : 0, d);
 }
 
 __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
@@ -702,6 +828,9 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
   }
 }
 
+// kRegex: REGEXP_REPLACE rows (a separate instantiation keeps the Pike VM's
+// thread lists out of the other transforms' local memory)
+template <bool kRegex>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -712,7 +841,10 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
     if ((w0 + k) * 32 >= a.m) break;
     bool valid = false;
     int len = 0;
-    if (o < a.m) len = xform_row(a, o, nullptr, valid);
+    if (o < a.m) {
+      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
+      else len = xform_row(a, o, nullptr, valid);
+    }
     const uint32_t word = __ballot_sync(0xffffffffu, valid);
     if (lane == 0) a.out_mask[w0 + k] = word;
     total += (uint64_t)warp_sum(len);
@@ -726,6 +858,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
   }
 }
 
+template <bool kRegex>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -736,7 +869,10 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
     if ((w0 + k) * 32 >= a.m) break;
     bool valid = false;
     int len = 0;
-    if (o < a.m) len = xform_row(a, o, nullptr, valid);
+    if (o < a.m) {
+      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
+      else len = xform_row(a, o, nullptr, valid);
+    }
     total += (uint64_t)warp_sum(len);
   }
   if (lane == 0) s_sum[warp] = total;
@@ -746,11 +882,14 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
-    const bool seg = is_segment_kind(a);  // warp-uniform
+    const bool seg = !kRegex && is_segment_kind(a);  // warp-uniform
     const unsigned char *p1 = nullptr, *p2 = nullptr;
     int n1 = 0, len = 0;
     bool valid = false;
-    if (o < a.m) len = seg ? xform_segments(a, o, p1, n1, p2, valid) : xform_row(a, o, nullptr, valid);
+    if (o < a.m) {
+      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
+      else len = seg ? xform_segments(a, o, p1, n1, p2, valid) : xform_row(a, o, nullptr, valid);
+    }
     int incl = len;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -769,13 +908,14 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
       for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
       for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
     } else if (o < a.m && len > 0) {
-      xform_row(a, o, a.out_chars + dst, valid);
+      if constexpr (kRegex) regex_row(a, o, a.out_chars + dst, valid);
+      else xform_row(a, o, a.out_chars + dst, valid);
     }
     pos += (uint64_t)wtot;
   }
 }
 
-// string -> integer / DATE / TIMESTAMP (cudf::strings::to_integers and
+// string -> integer / floating point / DATE / TIMESTAMP (cudf::strings::to_integers, to_floats and
 // to_timestamps with "%Y-%m-%d" / "%Y-%m-%d %H:%M:%S", LogicalProject.cpp:379-528)
 constexpr int kMaxFormatItems = 32;
 struct ParseArgs {
@@ -811,6 +951,68 @@ __device__ int64_t days_from_civil(int64_t y, int64_t m, int64_t d) {
   return era * 146097 + doe - 719468;
 }
 
+// A string as cudf::strings::to_floats reads it: an optional sign, then NaN,
+// Inf, or digits with one optional decimal point and an optional e / E
+// exponent.  Up to 19 significant digits are accumulated into an integer
+// (later ones only move the decimal exponent), which is then scaled by exact
+// powers of ten -- multiplied for a positive exponent, divided for a negative
+// one, in steps of 1e22 -- each step one correctly rounded operation, so
+// values of up to 15 digits with |exponent| <= 22 convert exactly rounded.
+// Reading stops at the first other character (no digits: 0).
+__device__ double parse_double(const unsigned char* p, int n) {
+  int i = 0;
+  bool neg = false;
+  if (i < n && (p[i] == '+' || p[i] == '-')) {
+    neg = p[i] == '-';
+    i++;
+  }
+  if (i + 3 <= n && p[i] == 'N' && p[i + 1] == 'a' && p[i + 2] == 'N') return __longlong_as_double(0x7ff8000000000000ll);
+  if (i + 3 <= n && p[i] == 'I' && p[i + 1] == 'n' && p[i + 2] == 'f')
+    return __longlong_as_double(neg ? (long long)0xfff0000000000000ull : 0x7ff0000000000000ll);
+  uint64_t mant = 0;
+  int digits = 0, exp10 = 0;
+  bool dot = false;
+  for (; i < n; i++) {
+    const unsigned char c = p[i];
+    if (c == '.' && !dot) {
+      dot = true;
+    } else if (c >= '0' && c <= '9') {
+      if (digits < 19) {
+        mant = mant * 10 + (c - '0');
+        if (mant) digits++;
+        if (dot) exp10--;
+      } else if (!dot) {
+        exp10++;
+      }
+    } else {
+      break;
+    }
+  }
+  if (i < n && (p[i] == 'e' || p[i] == 'E')) {
+    int j = i + 1, e = 0;
+    bool eneg = false;
+    if (j < n && (p[j] == '+' || p[j] == '-')) {
+      eneg = p[j] == '-';
+      j++;
+    }
+    for (; j < n && p[j] >= '0' && p[j] <= '9'; j++) e = min(e * 10 + (p[j] - '0'), 100000);
+    exp10 += eneg ? -e : e;
+  }
+  // 1e0 .. 1e22: every one exact in binary64
+  const double pow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                            1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+  double x = __ull2double_rn(mant);
+  if (exp10 >= 0) {
+    for (; exp10 > 22; exp10 -= 22) x = __dmul_rn(x, 1e22);
+    x = __dmul_rn(x, pow10[exp10]);
+  } else {
+    int e = -exp10;
+    for (; e > 22; e -= 22) x = __ddiv_rn(x, 1e22);
+    x = __ddiv_rn(x, pow10[e]);
+  }
+  return neg ? -x : x;
+}
+
 __global__ void k_parse(ParseArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t nwords = (a.m + 31) / 32;
@@ -823,7 +1025,10 @@ __global__ void k_parse(ParseArgs a) {
       int n;
       source_row(a.a, r, p, n, valid);
       int64_t v = 0;
-      if (valid && (a.type == TIMESTAMP_DAYS || a.type == TIMESTAMP_SECONDS || a.type == TIMESTAMP_MILLISECONDS ||
+      double fv = 0.0;
+      if (valid && (a.type == FLOAT32 || a.type == FLOAT64)) {
+        fv = parse_double(p, n);
+      } else if (valid && (a.type == TIMESTAMP_DAYS || a.type == TIMESTAMP_SECONDS || a.type == TIMESTAMP_MILLISECONDS ||
                     a.type == TIMESTAMP_MICROSECONDS || a.type == TIMESTAMP_NANOSECONDS)) {
         // the format's items in order, each taking its width (less at the end of
         // the string); a field reads its digits up to the first non-digit
@@ -857,6 +1062,8 @@ __global__ void k_parse(ParseArgs a) {
         case INT8: ((int8_t*)a.out)[r] = (int8_t)v; break;
         case INT16: ((int16_t*)a.out)[r] = (int16_t)v; break;
         case INT32: case TIMESTAMP_DAYS: ((int32_t*)a.out)[r] = (int32_t)v; break;
+        case FLOAT32: ((float*)a.out)[r] = __double2float_rn(fv); break;
+        case FLOAT64: ((double*)a.out)[r] = fv; break;
         default: ((int64_t*)a.out)[r] = v; break;
       }
     }
@@ -879,8 +1086,6 @@ BuildSrc device_source(const StrSource& s, const unsigned char* lit_dev) {
     b.lit = lit_dev;
     b.lit_len = (int32_t)s.literal.size();
   } else if (s.kind == StrSource::FORMAT) {
-    if (s.col.type == FLOAT32 || s.col.type == FLOAT64)
-      fail(GX_ERR_UNSUPPORTED, "CAST of a floating-point value to VARCHAR");
     if (s.col.type == STRING || type_size(s.col.type) == 0 || s.col.type >= DURATION_DAYS)
       fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(s.col.type));
     b.num = s.col.data;
@@ -964,7 +1169,8 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
 }
 
 gx_column build_transform(const StringOp& op, const StrSource& a, const StrSource& b, const ColumnView* num,
-                          int64_t rows, cudaStream_t s, const std::vector<StrSource>& more) {
+                          int64_t rows, cudaStream_t s, const std::vector<StrSource>& more,
+                          const ColumnView* pos0 = nullptr, const ColumnView* pos1 = nullptr) {
   if (more.size() > (size_t)(kMaxConcatParts - 2)) fail(GX_ERR_INVALID, "too many CONCAT parts");
   if (rows < 0 || rows > INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string columns hold at most 2^31 - 1 rows");
   const int64_t nblocks = (rows + kBuildRows - 1) / kBuildRows;
@@ -1011,6 +1217,16 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
       x.num_off = num->offset;
       x.num_type = num->type;
     }
+    if (pos0) {
+      x.p0 = pos0->data;
+      x.p0m = pos0->mask;
+      x.p0t = pos0->type;
+    }
+    if (pos1) {
+      x.p1 = pos1->data;
+      x.p1m = pos1->mask;
+      x.p1t = pos1->type;
+    }
     x.i0 = op.i0;
     x.i1 = op.i1;
     x.step = op.step;
@@ -1027,7 +1243,8 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     x.flags = (int*)(sums + nblocks + 1);
     uint64_t host[2] = {0, 0};
     if (rows > 0) {
-      k_xf_sizes<<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      if (op.kind == StringOp::REGEXP_REPLACE) k_xf_sizes<true><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      else k_xf_sizes<false><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
       check_cuda(cudaGetLastError(), "k_xf_sizes");
       launch_scan_tiles(sums, nblocks, (unsigned long long*)(sums + nblocks), s);
       check_cuda(cudaMemcpyAsync(host, sums + nblocks, 16, cudaMemcpyDeviceToHost, s), "string size");
@@ -1041,7 +1258,8 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     out.string_bytes = (int64_t)total;
     if (rows > 0) {
       x.out_chars = (unsigned char*)out.data;
-      k_xf_write<<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      if (op.kind == StringOp::REGEXP_REPLACE) k_xf_write<true><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
+      else k_xf_write<false><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
       check_cuda(cudaGetLastError(), "k_xf_write");
       add_launches(1);
     }
@@ -1320,8 +1538,6 @@ std::vector<gx_column> run_string_prepass(
             a.col = v;
             out = build_strings(a, none, nullptr, nullptr, n, s);
           } else {
-            if (v.type == FLOAT32 || v.type == FLOAT64)
-              fail(GX_ERR_UNSUPPORTED, "CAST of a floating-point value to VARCHAR");
             if (type_size(v.type) == 0 || v.type >= DURATION_DAYS)
               fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(v.type));
             out = build_transform(op, StrSource{}, StrSource{}, &v, n, s, {});
@@ -1333,7 +1549,7 @@ std::vector<gx_column> run_string_prepass(
         if (tmp.data || tmp.null_mask) free_column(tmp, s);
       } else if (op.kind == StringOp::SLICE || op.kind == StringOp::UPPER || op.kind == StringOp::LOWER ||
                  op.kind == StringOp::INITCAP || op.kind == StringOp::TRIM || op.kind == StringOp::REPLACE ||
-                 op.kind == StringOp::CONCAT) {
+                 op.kind == StringOp::CONCAT || op.kind == StringOp::REGEXP_REPLACE) {
         // a part: a string column, a literal, or (CONCAT) a typed column to format
         auto part = [&](int c, const std::string& lit) {
           StrSource x;
@@ -1355,7 +1571,36 @@ std::vector<gx_column> run_string_prepass(
         for (size_t k = 0; k < op.more_cols.size(); k++) more.push_back(part(op.more_cols[k], op.more_lits[k]));
         StringOp xo = op;
         if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
-        out = build_transform(xo, a, b, nullptr, n, s, more);
+        if (op.kind == StringOp::REGEXP_REPLACE) compile_regex_replace(op.literal, op.literal2, &xo.literal, &xo.literal2);
+        if (op.kind == StringOp::SLICE && !op.pos0.empty()) {
+          // the start and stop columns (LogicalProject.cpp:241-300), made by
+          // the same evaluator as a CASE condition
+          gx_column pc[2] = {};
+          auto release = [&] {
+            for (auto& c : pc)
+              if (c.data || c.null_mask) free_column(c, s);
+          };
+          try {
+            ColumnView pv[2];
+            for (int k = 0; k < 2; k++) {
+              const std::string& text = k == 0 ? op.pos0 : op.pos1;
+              if (text.empty()) continue;
+              pc[k] = eval_bool(cols, text);
+              const int t = pc[k].type_id;
+              if (t != INT8 && t != INT16 && t != INT32 && t != INT64 && t != UINT8 && t != UINT16 &&
+                  t != UINT32 && t != UINT64)
+                fail(GX_ERR_TYPE, "Expression does not evaluate to an integer column");  // :252
+              pv[k] = ColumnView{t, pc[k].data, pc[k].null_mask, 0, n};
+            }
+            out = build_transform(xo, a, b, nullptr, n, s, more, &pv[0], op.pos1.empty() ? nullptr : &pv[1]);
+          } catch (...) {
+            release();
+            throw;
+          }
+          release();
+        } else {
+          out = build_transform(xo, a, b, nullptr, n, s, more);
+        }
       } else if (op.kind == StringOp::PARSE) {
         const ColumnView c = string_col(op.col);
         out = alloc_column(op.type, n, s);

@@ -51,8 +51,9 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
                         int64_t rows, cudaStream_t s);
 
 // Evaluates `ops` over `cols` and appends their columns to `cols` (column
-// ncols + i is op i).  eval_bool evaluates a CASE condition's text over the
-// columns so far into a BOOL8 column.  The returned columns are the caller's
+// ncols + i is op i).  eval_bool evaluates an expression's text over the
+// columns so far into a column: a CASE condition (BOOL8), the operand of a
+// CAST to VARCHAR, a SUBSTRING's start or stop (integers).  The returned columns are the caller's
 // to free once the work that reads them has been enqueued.
 std::vector<gx_column> run_string_prepass(
     std::vector<ColumnView>& cols, const std::vector<StringOp>& ops, cudaStream_t s,

@@ -178,7 +178,7 @@ def rewrite(texts: Sequence[str], string_cols: Sequence[int], ncols: int) -> Tup
 
 
 STRING_RESULTS = {"CASE", "SLICE", "SLICE_COLS", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE", "CONCAT",
-                  "TO_STRING"}
+                  "TO_STRING", "REGEX"}
 PARSE_TYPES = {"CAST_TINYINT": T.INT8, "CAST_SMALLINT": T.INT16, "CAST_INTEGER": T.INT32, "CAST_BIGINT": T.INT64,
                "CAST_DATE": T.TIMESTAMP_DAYS, "CAST_TIMESTAMP_SECONDS": T.TIMESTAMP_SECONDS,
                "CAST_TIMESTAMP_MILLISECONDS": T.TIMESTAMP_MILLISECONDS,
@@ -219,6 +219,12 @@ def string_function(name, a, strcol, int_lit):
         return ("TRIM", int(a[2].value[1:]), _unquote(a[0].value), _unquote(a[1].value))
     if name == "REPLACE" and len(a) == 3 and strcol(a[0]):
         return ("REPLACE", int(a[0].value[1:]), _unquote(a[1].value), _unquote(a[2].value))
+    if name == "REGEXP_REPLACE" and len(a) in (3, 4) and strcol(a[0]) and _is_lit(a[1]) and _is_lit(a[2]):
+        # LogicalProject.cpp:149-183: a position (1-based) keeps the characters before it
+        start = int_lit(a[3]) - 1 if len(a) == 4 else 0
+        if start < 0:
+            raise ValueError("Position must be greater than zero.")
+        return ("REGEX", int(a[0].value[1:]), _unquote(a[1].value), _unquote(a[2].value), start)
     if name in ("CONCAT", "||") and len(a) == 2:
         def operand(x):
             if strcol(x):
@@ -238,6 +244,60 @@ def string_function(name, a, strcol, int_lit):
         return ("PARSE", int(a[0].value[1:]), T.TIMESTAMP_DAYS if name == "TO_DATE" else T.TIMESTAMP_NANOSECONDS,
                 _unquote(a[1].value))
     return None
+
+
+def _regex(pattern: str):
+    """REGEXP_REPLACE's pattern as a Python regular expression with the same
+    leftmost-first semantics: ASCII classes and word boundaries (re.ASCII),
+    `$` only at the end of the subject (Python's `$` also matches before a
+    final newline, so it becomes `\\Z`).  Python's own backtracking matcher
+    tries alternatives and repeats in the same order as the device's Pike VM."""
+    out, i, n = [], 0, len(pattern)
+    while i < n:
+        c = pattern[i]
+        if c == "\\" and i + 1 < n:
+            out.append(pattern[i:i + 2])
+            i += 2
+        elif c == "[":  # copied up to its closing bracket (a ']' first is literal)
+            j = i + 1
+            if j < n and pattern[j] == "^":
+                j += 1
+            if j < n and pattern[j] == "]":
+                j += 1
+            while j < n and pattern[j] != "]":
+                j += 2 if pattern[j] == "\\" else 1
+            out.append(pattern[i:j + 1])
+            i = j + 1
+        else:
+            out.append("\\Z" if c == "$" else c)
+            i += 1
+    return re.compile("".join(out), re.ASCII)
+
+
+def _template(repl: str):
+    """The replacement as parts: text, or a group number (\\N or ${N})."""
+    parts, i = [], 0
+    while i < len(repl):
+        m = re.match(r"\\([0-9])|\$\{([0-9]+)\}", repl[i:])
+        if m:
+            parts.append(int(m.group(1) or m.group(2)))
+            i += m.end()
+        else:
+            parts.append(repl[i])
+            i += 1
+    return parts
+
+
+def _regex_replace(rx, tmpl, v: str) -> str:
+    """Every (non-empty, non-overlapping) match, left to right, replaced by the
+    template; a group that did not take part gives the empty string."""
+    out, pos = [], 0
+    for m in rx.finditer(v):
+        out.append(v[pos:m.start()])
+        out.extend(p if isinstance(p, str) else (m.group(p) or "") for p in tmpl)
+        pos = m.end()
+    out.append(v[pos:])
+    return "".join(out)
 
 
 def _slice_cols(v: str, start: int, stop: int) -> str:
@@ -548,6 +608,10 @@ def prepass(cols: Sequence, strings: dict, texts: Sequence[str], nthreads: int =
                  "LOWER": lambda v: v.lower(), "INITCAP": _initcap,
                  "TRIM": lambda v: _trim(v, op[2], op[3]), "REPLACE": lambda v: v.replace(op[2], op[3])}[op[0]]
             strings[k] = [None if v is None else f(v) for v in src]
+            table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
+        elif op[0] == "REGEX":
+            rx, tmpl = _regex(op[2]), _template(op[3])
+            strings[k] = [None if v is None else v[:op[4]] + _regex_replace(rx, tmpl, v[op[4]:]) for v in strings[op[1]]]
             table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
         elif op[0] == "SLICE_COLS":
             def positions(text, default):

@@ -359,7 +359,25 @@ def _function_table(rng, n):
             HostColumn(T.TIMESTAMP_MILLISECONDS, rng.integers(-10**12, 4 * 10**12, n).astype(np.int64)),
             None, None, None, None, None]
     s13 = [None if v is None else f"{v[8:10]}/{v[5:7]}/{v[:4]}" for v in s10]  # day/month/year
-    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12, 13: s13}
+    # floating-point texts: exact short decimals, full round-trip reprs, exponents,
+    # specials and malformed ones
+    texts = ["1.5", "-2e3", "1e400", ".5", "  1", "abc", "1.2.3", "12345678901234567890123", "NaN", "-Inf",
+             "0.1", "3.24e-05", "+7.", "1E+2", "-0", "", "999999.001", "0.45435436", "1e-320", "5e-324x"]
+    s14 = [None if rng.random() < 0.1 else
+           (texts[int(rng.integers(0, len(texts)))] if rng.random() < 0.4 else
+            repr(float(rng.normal(0, 10) * 10.0 ** int(rng.integers(-30, 30)))) if rng.random() < 0.5 else
+            f"{rng.uniform(-1000, 1000):.{int(rng.integers(0, 7))}f}") for _ in range(n)]
+    # doubles over the whole exponent range, with the rounding edges of the format
+    wide = np.sign(rng.normal(size=n)) * 10.0 ** rng.uniform(-325, 308.2, n)
+    edges = [0.0, -0.0, np.inf, -np.inf, np.nan, 1e9, 1e-4, 9.9999e-5, 999999999.9999999, 0.99999999995,
+             9.9999999999e20, 123456789.0, 1234567891.0, 5e-324, 1.7976931348623157e308, 0.1 + 0.2]
+    k = min(len(edges), n)
+    wide[:k] = edges[:k]
+    cols += [None,
+             HostColumn(T.FLOAT32, rng.normal(0, 1000, n).astype(np.float32), pack_validity(rng.random(n) > 0.1)),
+             HostColumn(T.FLOAT64, wide),
+             HostColumn(T.INT32, rng.integers(-3, 10, n).astype(np.int32), pack_validity(rng.random(n) > 0.15))]
+    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12, 13: s13, 14: s14}
 
 
 FUNCTION_EXPRS = [
@@ -378,6 +396,10 @@ FUNCTION_EXPRS = [
     "UPPER($12)", "LOWER($12)", "INITCAP($12)", "CASE(>($5, 0), UPPER($12), REVERSE($0))",
     "TO_DATE($10, '%Y-%m-%d')", "TO_TIMESTAMP($11, '%Y-%m-%d %H:%M:%S')", "TO_DATE($13, '%d/%m/%Y')",
     "TO_TIMESTAMP($13, '%d/%m/%Y')", "TO_DATE($11, '%Y%%%m%d')",
+    "CAST($2):VARCHAR", "CAST($15):VARCHAR", "CAST($16):VARCHAR", "CONCAT($0, '=', CAST($16):VARCHAR)",
+    "CAST($14):DOUBLE", "CAST($14):FLOAT", "CAST(CAST($16):VARCHAR):DOUBLE",
+    "SUBSTRING($0, $17)", "SUBSTRING($0, $17, 2)", "SUBSTRING($0, 2, $17)", "SUBSTRING($0, $17, CHAR_LENGTH($3))",
+    "SUBSTRING($0, 2, -(CHAR_LENGTH($0), 2))", "SUBSTRING($3, +($17, 1), $17)",
 ]
 
 
@@ -394,6 +416,16 @@ def test_string_functions_oracle_rules():
     assert strings_ref.format_value(T.TIMESTAMP_MILLISECONDS, -1) == "1969-12-31 23:59:59"
     assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "31/12/1996", "%d/%m/%Y") == 9861
     assert strings_ref.parse_value(T.TIMESTAMP_DAYS, "1996-12", "%Y-%m-%d") == strings_ref._days_from_civil(1996, 12, 0)
+    assert strings_ref.format_value(T.FLOAT64, 1e9) == "1.0e+09"              # from 1e9: scientific
+    assert strings_ref.format_value(T.FLOAT64, 1234567891.0) == "1.234567891e+09"
+    assert strings_ref.format_value(T.FLOAT64, 0.1 + 0.2) == "0.3"            # 9 significant digits
+    assert strings_ref.format_value(T.FLOAT64, -0.0) == "-0.0"
+    assert strings_ref.format_value(T.FLOAT64, float("inf")) == "Inf"
+    assert strings_ref.parse_value(T.FLOAT64, "-2e3") == -2000.0
+    assert strings_ref.parse_value(T.FLOAT64, "1.2.3") == 1.2                 # up to the second point
+    assert strings_ref._slice_cols("abcdef", -2, 3) == "abc"                   # start clamped at 0
+    assert strings_ref._slice_cols("abcdef", 2, -1) == "cdef"                  # a negative stop: the end
+    assert strings_ref._slice_cols("abc", 2, 1) == ""
     texts, ops = strings_ref.rewrite(["CONCAT($0, '-', $1)"], [0, 1], 2)
     assert texts == ["$3"] and [o[0] for o in ops] == ["CONCAT", "CONCAT"]
 
@@ -434,12 +466,8 @@ def test_string_function_errors():
     dev = [DeviceColumn.from_strings(["é", "b"]), DeviceColumn.from_host(HostColumn(T.FLOAT64, np.arange(2.0)))]
     with pytest.raises(N.GxError, match="non-ASCII"):
         g.evaluate_expressions(dev, ["UPPER($0)"])
-    with pytest.raises(N.GxError, match="floating-point"):
-        g.evaluate_expressions(dev, ["CAST($1):VARCHAR"])
-    with pytest.raises(N.GxError, match="floating-point"):
-        g.evaluate_expressions(dev, ["CAST($0):DOUBLE"])
-    with pytest.raises(N.GxError, match="non-literal"):
-        g.evaluate_expressions(dev, ["SUBSTRING($0, CAST($1):INTEGER)"])
+    with pytest.raises(N.GxError, match="integer column"):
+        g.evaluate_expressions(dev, ["SUBSTRING($0, $1)"])  # LogicalProject.cpp:252
     with pytest.raises(N.GxError, match="between literals"):
         g.evaluate_expressions(dev, ["CONCAT('a', 'b')"])
     with pytest.raises(N.GxError, match="between literals"):
