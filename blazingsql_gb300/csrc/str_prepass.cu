@@ -397,7 +397,6 @@ struct XformArgs {
   uint32_t* out_mask;
   unsigned char* out_chars;
   uint64_t* block_sums;
-  int* flags;  // bit 0: UPPER / LOWER / INITCAP met a non-ASCII byte
 };
 
 __device__ __forceinline__ void source_row(const BuildSrc& s, int64_t o, const unsigned char*& p, int& len,
@@ -740,6 +739,66 @@ __device__ int regex_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
   return regex_replace_row(a.s1, a.s2, a.l2, p, n, a.i0v ? a.i0 : 0, d);
 }
 
+// ------------------------------------------------------ case mapping
+// Unicode case mappings and alphabetic ranges, sorted by code point
+#include "case_tables.inc"
+
+__device__ __forceinline__ int find_cp(const uint32_t* keys, int count, uint32_t c) {
+  int lo = 0, hi = count - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const uint32_t k = keys[mid];
+    if (k == c) return mid;
+    if (k < c) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+// c's upper- or lowercase mapping into m (1 to 3 code points); returns the count
+__device__ int case_map(uint32_t c, bool upper, uint32_t* m) {
+  int k = upper ? find_cp(kUpperFrom, kUpperCount, c) : find_cp(kLowerFrom, kLowerCount, c);
+  if (k >= 0) {
+    m[0] = upper ? kUpperTo[k] : kLowerTo[k];
+    return 1;
+  }
+  k = upper ? find_cp(kUpperMultiFrom, kUpperMultiCount, c) : find_cp(kLowerMultiFrom, kLowerMultiCount, c);
+  if (k < 0) {
+    m[0] = c;
+    return 1;
+  }
+  const uint32_t* t = (upper ? kUpperMultiTo : kLowerMultiTo) + 3 * k;
+  int n = 0;
+  for (int j = 0; j < 3 && t[j]; j++) m[n++] = t[j];
+  return n;
+}
+
+__device__ bool is_alpha_cp(uint32_t c) {
+  int lo = 0, hi = kAlphaCount - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    if (c < kAlphaLo[mid]) hi = mid - 1;
+    else if (c > kAlphaHi[mid]) lo = mid + 1;
+    else return true;
+  }
+  return false;
+}
+
+// c as UTF-8 at d + at (counted only when d is null)
+__device__ __forceinline__ int put_utf8(unsigned char* d, int at, uint32_t c) {
+  const int n = c < 0x80 ? 1 : c < 0x800 ? 2 : c < 0x10000 ? 3 : 4;
+  if (d) {
+    if (n == 1) {
+      d[at] = (unsigned char)c;
+    } else {
+      const unsigned char lead = n == 2 ? 0xC0 : n == 3 ? 0xE0 : 0xF0;
+      d[at] = (unsigned char)(lead | (c >> (6 * (n - 1))));
+      for (int j = 1; j < n; j++) d[at + j] = (unsigned char)(0x80 | ((c >> (6 * (n - 1 - j))) & 0x3F));
+    }
+  }
+  return at + n;
+}
+
 __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& valid) {
   if (a.kind == StringOp::TO_STRING) return format_value(a, o, d, valid);
   if (is_segment_kind(a)) {
@@ -789,24 +848,52 @@ __device__ int xform_row(const XformArgs& a, int64_t o, unsigned char* d, bool& 
       return at;
     }
     case StringOp::UPPER: case StringOp::LOWER: case StringOp::INITCAP: {
-      bool word = false;  // INITCAP: inside a run of letters (cudf::strings::title)
-      for (int i = 0; i < n; i++) {
-        unsigned char c = p[i];
-        if (c >= 0x80) {
-          if (!d) atomicOr(a.flags, 1);
-        } else {
+      // per code point (cudf::strings::to_upper / to_lower / title): INITCAP
+      // maps the first alphabetic character of each run of them to upper
+      // case and the rest to lower case
+      bool word = false;
+      int at = 0;
+      for (int i = 0; i < n;) {
+        const unsigned char b = p[i];
+        if (b < 0x80) {  // ASCII
+          unsigned char c = b;
           const bool up = c >= 'A' && c <= 'Z', lo = c >= 'a' && c <= 'z';
-          bool to_up = a.kind == StringOp::UPPER;
-          if (a.kind == StringOp::INITCAP) to_up = !word;
-          if (up || lo) {
-            if (to_up && lo) c = (unsigned char)(c - 32);
-            if (!to_up && up) c = (unsigned char)(c + 32);
-          }
+          const bool to_up = a.kind == StringOp::INITCAP ? !word : a.kind == StringOp::UPPER;
+          if (to_up && lo) c = (unsigned char)(c - 32);
+          if (!to_up && up) c = (unsigned char)(c + 32);
           word = up || lo;
+          if (d) d[at] = c;
+          at++;
+          i++;
+          continue;
         }
-        if (d) d[i] = c;
+        int len = utf8_len(b);
+        bool ok = len > 1 && i + len <= n;
+        uint32_t c = len == 2 ? (b & 0x1Fu) : len == 3 ? (b & 0x0Fu) : (b & 0x07u);
+        for (int k = 1; ok && k < len; k++) {
+          ok = (p[i + k] & 0xC0) == 0x80;
+          c = (c << 6) | (p[i + k] & 0x3Fu);
+        }
+        if (!ok) {  // not a UTF-8 sequence: the byte as it is
+          if (d) d[at] = b;
+          at++;
+          i++;
+          word = false;
+          continue;
+        }
+        bool to_up = a.kind == StringOp::UPPER, map = true;
+        if (a.kind == StringOp::INITCAP) {
+          const bool alpha = is_alpha_cp(c);
+          to_up = !word;
+          map = alpha;
+          word = alpha;
+        }
+        uint32_t m[3] = {c, 0, 0};
+        const int k = map ? case_map(c, to_up, m) : 1;
+        for (int j = 0; j < k; j++) at = put_utf8(d, at, m[j]);
+        i += len;
       }
-      return n;
+      return at;
     }
     case StringOp::REPLACE: {  // cudf::strings::replace, every occurrence, left to right
       int at = 0, i = 0;
@@ -1176,9 +1263,9 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
   const int64_t nblocks = (rows + kBuildRows - 1) / kBuildRows;
   const int64_t words = mask_words_for(rows);
   auto al = [](size_t v) { return (v + 255) / 256 * 256; };
-  // [mask | offsets | block sums + total + flags | a, b, literal, literal2]
+  // [mask | offsets | block sums + total | a, b, literal, literal2]
   const size_t mask_b = al((size_t)words * 4), offs_b = al((size_t)(rows + 1) * 4);
-  const size_t sums_b = al((size_t)(nblocks + 2) * 8);
+  const size_t sums_b = al((size_t)(nblocks + 1) * 8);
   std::vector<std::string> lits = {a.kind == StrSource::LITERAL ? a.literal : std::string(),
                                    b.kind == StrSource::LITERAL ? b.literal : std::string(), op.literal,
                                    op.literal2};
@@ -1240,18 +1327,16 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     x.out_offs = out.string_offsets;
     x.out_mask = out.null_mask;
     x.block_sums = sums;
-    x.flags = (int*)(sums + nblocks + 1);
-    uint64_t host[2] = {0, 0};
+    uint64_t host[1] = {0};
     if (rows > 0) {
       if (op.kind == StringOp::REGEXP_REPLACE) k_xf_sizes<true><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
       else k_xf_sizes<false><<<(unsigned)nblocks, kBuildWarps * 32, 0, s>>>(x);
       check_cuda(cudaGetLastError(), "k_xf_sizes");
       launch_scan_tiles(sums, nblocks, (unsigned long long*)(sums + nblocks), s);
-      check_cuda(cudaMemcpyAsync(host, sums + nblocks, 16, cudaMemcpyDeviceToHost, s), "string size");
+      check_cuda(cudaMemcpyAsync(host, sums + nblocks, 8, cudaMemcpyDeviceToHost, s), "string size");
       add_launches(1);
     }
     check_cuda(cudaStreamSynchronize(s), "string size sync");
-    if (host[1] & 1) fail(GX_ERR_UNSUPPORTED, "UPPER / LOWER / INITCAP of non-ASCII text");
     const uint64_t total = host[0];
     if (total > (uint64_t)INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string column over 2^31 - 1 characters");
     out.data = dev_alloc(al(total ? total : 1), s);

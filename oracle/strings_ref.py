@@ -439,10 +439,23 @@ def _slice(v: str, start, stop, step):
     return v[b:e] if b < e else ""
 
 
+def _upper(v: str) -> str:
+    """UPPER per code point: its full uppercase mapping (SpecialCasing's
+    unconditional entries included, e.g. U+00DF -> "SS"); no context rules."""
+    return "".join(ch.upper() for ch in v)
+
+
+def _lower(v: str) -> str:
+    """LOWER per code point (so no final-sigma rule)."""
+    return "".join(ch.lower() for ch in v)
+
+
 def _initcap(v: str) -> str:
+    """INITCAP (cudf::strings::title): in each run of alphabetic characters
+    (general category L*), the first upper-cased, the rest lower-cased."""
     out, word = [], False
     for ch in v:
-        letter = ch.isascii() and ch.isalpha()
+        letter = ch.isalpha()
         out.append((ch.lower() if word else ch.upper()) if letter else ch)
         word = letter
     return "".join(out)
@@ -604,8 +617,8 @@ def prepass(cols: Sequence, strings: dict, texts: Sequence[str], nthreads: int =
             table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))
         elif op[0] in ("SLICE", "UPPER", "LOWER", "INITCAP", "TRIM", "REPLACE"):
             src = strings[op[1]]
-            f = {"SLICE": lambda v: _slice(v, op[2], op[3], op[4]), "UPPER": lambda v: v.upper(),
-                 "LOWER": lambda v: v.lower(), "INITCAP": _initcap,
+            f = {"SLICE": lambda v: _slice(v, op[2], op[3], op[4]), "UPPER": _upper,
+                 "LOWER": _lower, "INITCAP": _initcap,
                  "TRIM": lambda v: _trim(v, op[2], op[3]), "REPLACE": lambda v: v.replace(op[2], op[3])}[op[0]]
             strings[k] = [None if v is None else f(v) for v in src]
             table.append(HostColumn(T.INT8, np.zeros(n, dtype=np.int8)))

@@ -377,7 +377,12 @@ def _function_table(rng, n):
              HostColumn(T.FLOAT32, rng.normal(0, 1000, n).astype(np.float32), pack_validity(rng.random(n) > 0.1)),
              HostColumn(T.FLOAT64, wide),
              HostColumn(T.INT32, rng.integers(-3, 10, n).astype(np.int32), pack_validity(rng.random(n) > 0.15))]
-    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12, 13: s13, 14: s14}
+    # non-ASCII text for the case mappings: one-to-many (ß, ŉ, ﬀ, ΐ), İ, title-case
+    # digraphs, final sigma, Cyrillic, Deseret (4-byte), combining marks, digits
+    uni = list("aßŉﬀΐİǅǆǄΣσςЖжẞ𐐨𐐀ÀàÉé ́-1٣_xZ") + ["😀", "ǰ"]
+    s18 = [None if rng.random() < 0.1 else "".join(rng.choice(uni, int(rng.integers(0, 9)))) for _ in range(n)]
+    cols.append(None)
+    return cols, {0: s0, 3: s3, 9: s9, 10: s10, 11: s11, 12: s12, 13: s13, 14: s14, 18: s18}
 
 
 FUNCTION_EXPRS = [
@@ -400,6 +405,7 @@ FUNCTION_EXPRS = [
     "CAST($14):DOUBLE", "CAST($14):FLOAT", "CAST(CAST($16):VARCHAR):DOUBLE",
     "SUBSTRING($0, $17)", "SUBSTRING($0, $17, 2)", "SUBSTRING($0, 2, $17)", "SUBSTRING($0, $17, CHAR_LENGTH($3))",
     "SUBSTRING($0, 2, -(CHAR_LENGTH($0), 2))", "SUBSTRING($3, +($17, 1), $17)",
+    "UPPER($18)", "LOWER($18)", "INITCAP($18)", "CHAR_LENGTH(UPPER($18))", "UPPER($0)", "INITCAP($3)",
 ]
 
 
@@ -464,8 +470,6 @@ def test_string_function_errors():
     from blazingsql_gb300 import _native as N
     from blazingsql_gb300.api import DeviceColumn
     dev = [DeviceColumn.from_strings(["é", "b"]), DeviceColumn.from_host(HostColumn(T.FLOAT64, np.arange(2.0)))]
-    with pytest.raises(N.GxError, match="non-ASCII"):
-        g.evaluate_expressions(dev, ["UPPER($0)"])
     with pytest.raises(N.GxError, match="integer column"):
         g.evaluate_expressions(dev, ["SUBSTRING($0, $1)"])  # LogicalProject.cpp:252
     with pytest.raises(N.GxError, match="between literals"):
@@ -476,6 +480,21 @@ def test_string_function_errors():
         g.evaluate_expressions(dev, ["TO_DATE($0, '%Y-%m')"])
     with pytest.raises(N.GxError, match="specifier"):
         g.evaluate_expressions(dev, ["TO_TIMESTAMP($0, '%Y-%m-%d %I')"])
+
+
+def test_case_tables_match_the_oracles_unicode():
+    """The device's case tables come from the same Unicode version as the
+    oracle's str.upper / str.lower / str.isalpha."""
+    import unicodedata
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "blazingsql_gb300", "csrc",
+                        "case_tables.inc")
+    head = open(path).read(400)
+    m = re.search(r'GX_CASE_UNICODE_VERSION "([0-9.]+)"', head)
+    if m.group(1) != unicodedata.unidata_version:
+        pytest.skip(f"this Python's Unicode {unicodedata.unidata_version} is not the tables' {m.group(1)}")
+    assert strings_ref._upper("straße ŉ") == "STRASSE ʼN"
+    assert strings_ref._lower("ΣΑΣ") == "σασ"                  # per code point: no final sigma
+    assert strings_ref._initcap("ǆemal élan-x1y") == "Ǆemal Élan-X1Y"
 
 
 def test_string_rewrite_oracle_rules():
