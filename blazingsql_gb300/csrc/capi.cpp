@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -244,11 +245,17 @@ struct StringPrepass {
 };
 
 // A CASE condition of the pre-pass evaluated into a BOOL8 column.
+static void compact_plan_columns(std::vector<ColumnView>& cols, std::string& cond, std::vector<std::string>& texts);
+
 static gx_column eval_condition(const std::vector<ColumnView>& cols, const std::string& text, cudaStream_t s) {
-  auto ps = plan_for("eval", cols, "", {text}, false);
+  std::vector<ColumnView> pcols = cols;
+  std::string none;
+  std::vector<std::string> texts = {text};
+  compact_plan_columns(pcols, none, texts);
+  auto ps = plan_for("eval", pcols, "", texts, false);
   gx_column out{};
   int64_t rows = 0;
-  ps->execute(cols, &out, &rows, s);
+  ps->execute(pcols, &out, &rows, s);
   return out;
 }
 
@@ -270,6 +277,57 @@ static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std
   pp.made = run_string_prepass(cols, ops, s, [s](const std::vector<ColumnView>& c, const std::string& t) {
     return eval_condition(c, t, s);
   });
+}
+
+// The columns a text reads ($k outside quoted literals) appended to *used,
+// or, with map, the text with each $k renumbered to $map[k].
+static std::string map_columns(const std::string& t, std::vector<int>* used, const std::vector<int>* map) {
+  std::string r;
+  bool quoted = false;
+  for (size_t i = 0; i < t.size();) {
+    const char c = t[i];
+    if (c == '\'') {
+      if (quoted && i + 1 < t.size() && t[i + 1] == '\'') {  // '' inside a literal
+        r += "''";
+        i += 2;
+        continue;
+      }
+      quoted = !quoted;
+    } else if (!quoted && c == '$' && i + 1 < t.size() && std::isdigit((unsigned char)t[i + 1])) {
+      size_t j = i + 1;
+      long k = 0;
+      while (j < t.size() && std::isdigit((unsigned char)t[j]) && k < (1L << 30)) k = k * 10 + (t[j++] - '0');
+      if (used) used->push_back((int)k);
+      r += "$" + std::to_string(map && k < (long)map->size() && (*map)[k] >= 0 ? (*map)[k] : k);
+      i = j;
+      continue;
+    }
+    r += c;
+    i++;
+  }
+  return r;
+}
+
+// A plan binds at most GX_MAX_COLS columns.  When a table (with the string
+// pre-pass's columns) holds more, the plan gets only the columns its texts
+// read, renumbered in order.
+static void compact_plan_columns(std::vector<ColumnView>& cols, std::string& cond, std::vector<std::string>& texts) {
+  if (cols.size() <= (size_t)GX_MAX_COLS) return;
+  std::vector<int> used = {0};  // column 0 carries the row count of a plan that reads no column
+  map_columns(cond, &used, nullptr);
+  for (const auto& t : texts) map_columns(t, &used, nullptr);
+  std::sort(used.begin(), used.end());
+  used.erase(std::unique(used.begin(), used.end()), used.end());
+  std::vector<int> map(cols.size(), -1);
+  std::vector<ColumnView> kept;
+  for (int k : used) {
+    if (k < 0 || k >= (int)cols.size()) fail(GX_ERR_PARSE, "column index out of range: $" + std::to_string(k));
+    map[k] = (int)kept.size();
+    kept.push_back(cols[k]);
+  }
+  cond = map_columns(cond, nullptr, &map);
+  for (auto& t : texts) t = map_columns(t, nullptr, &map);
+  cols = std::move(kept);
 }
 
 // evaluate_expressions / process_filter / filter + project over a table that
@@ -321,8 +379,12 @@ static void evaluate_with_strings(std::vector<ColumnView> cols, std::string cond
   int64_t rows = n;
   try {
     if (!num.empty()) {
-      auto ps = plan_for(kind, cols, filtering ? cond : std::string(), num, rand_by_out);
-      ps->execute(cols, tmp.data(), &rows, s);
+      std::vector<ColumnView> pcols = cols;
+      std::string pcond = filtering ? cond : std::string();
+      std::vector<std::string> pnum = num;
+      compact_plan_columns(pcols, pcond, pnum);
+      auto ps = plan_for(kind, pcols, pcond, pnum, rand_by_out);
+      ps->execute(pcols, tmp.data(), &rows, s);
       for (size_t j = 0; j < num_pos.size(); j++) {
         out[num_pos[j]] = tmp[j];
         tmp[j] = gx_column{};

@@ -115,6 +115,27 @@ def test_column_offsets(gpu, ora):
         assert_tables_equal(got, exp, what=f"project offset {off}")
 
 
+def test_wide_table(gpu, ora):
+    """A table of more columns than one plan binds (64): the plan gets the
+    columns its expressions read, renumbered."""
+    n, width = 5000, 100
+    rng = np.random.default_rng(21)
+    cols = []
+    for k in range(width):
+        if k % 3 == 0:
+            cols.append(HostColumn(T.FLOAT64, rng.normal(0, 10, n), pack_validity(rng.random(n) > 0.1)))
+        else:
+            cols.append(HostColumn(T.INT64, rng.integers(-1000, 1000, n).astype(np.int64)))
+    exprs = ["+($0, $57)", "*($99, 2)", "$64", "CASE(>($80, 0), $98, $1)", "7"]
+    got = gpu.evaluate_expressions(cols, exprs)
+    exp = ora.evaluate_expressions(cols, exprs)
+    assert_tables_equal(got, exp, what="wide evaluate")
+    cond = "AND(>($80, -500), <($3, 10.0))"
+    got = gpu.filter_project(cols, cond, exprs)
+    exp = ora.filter_project(cols, cond, exprs)
+    assert_tables_equal(got, exp, what="wide filter")
+
+
 @pytest.mark.parametrize("mode", [N.GX_FILTER_TWO_PASS, N.GX_FILTER_SINGLE_PASS])
 @pytest.mark.parametrize("words,warps", [(1, 4), (2, 8), (4, 8), (8, 4), (8, 2), (16, 1)])
 def test_filter_modes_and_tiles(ora, mode, words, warps):
