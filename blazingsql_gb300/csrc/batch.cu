@@ -682,7 +682,8 @@ gx_batch_runner* gx_batch_runner_create(const gx_plan* plan, int max_batches, in
   gx_batch_runner* out = nullptr;
   guarded_call(status, [&] {
     const gx::CompiledPlan* cp = gx::single_chunk(plan);
-    if (!cp) gx::fail(GX_ERR_INVALID, "a batch runner needs a compiled plan with at most 32 outputs");
+    if (!cp) gx::fail(GX_ERR_INVALID, "a batch runner needs a compiled plan with at most 32 outputs "
+                                      "over at most 64 columns");
     out = new gx_batch_runner{std::make_unique<gx::BatchRunner>(*cp, max_batches, max_total_rows, autotune != 0)};
   });
   return out;
@@ -715,7 +716,8 @@ gx_batch_stream* gx_batch_stream_create(const gx_plan* plan, int max_batches, in
   gx_batch_stream* out = nullptr;
   guarded_call(status, [&] {
     const gx::CompiledPlan* cp = gx::single_chunk(plan);
-    if (!cp) gx::fail(GX_ERR_INVALID, "a batch stream needs a compiled plan with at most 32 outputs");
+    if (!cp) gx::fail(GX_ERR_INVALID, "a batch stream needs a compiled plan with at most 32 outputs "
+                                      "over at most 64 columns");
     if (block_threads % 32 != 0) gx::fail(GX_ERR_INVALID, "block_threads must be a multiple of 32");
     out = new gx_batch_stream{std::make_unique<gx::BatchStream>(*cp, max_batches, max_total_rows, block_threads / 32,
                                                                  words_per_warp)};

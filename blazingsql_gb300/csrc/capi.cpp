@@ -67,23 +67,75 @@ KernelConfig default_config() {
   return c;
 }
 
+// The columns a text reads ($k outside quoted literals) appended to *used,
+// or, with map, the text with each $k renumbered to $map[k].
+static std::string map_columns(const std::string& t, std::vector<int>* used, const std::vector<int>* map) {
+  std::string r;
+  bool quoted = false;
+  for (size_t i = 0; i < t.size();) {
+    const char c = t[i];
+    if (c == '\'') {
+      if (quoted && i + 1 < t.size() && t[i + 1] == '\'') {  // '' inside a literal
+        r += "''";
+        i += 2;
+        continue;
+      }
+      quoted = !quoted;
+    } else if (!quoted && c == '$' && i + 1 < t.size() && std::isdigit((unsigned char)t[i + 1])) {
+      size_t j = i + 1;
+      long k = 0;
+      while (j < t.size() && std::isdigit((unsigned char)t[j]) && k < (1L << 30)) k = k * 10 + (t[j++] - '0');
+      if (used) used->push_back((int)k);
+      r += "$" + std::to_string(map && k < (long)map->size() && (*map)[k] >= 0 ? (*map)[k] : k);
+      i = j;
+      continue;
+    }
+    r += c;
+    i++;
+  }
+  return r;
+}
+
 // One call's plans: expression lists longer than GX_OUTPUTS_PER_KERNEL run as
-// several kernels (chunks), each writing its slice of the outputs.
+// several kernels (chunks), each writing its slice of the outputs.  A kernel
+// binds at most GX_MAX_COLS columns: over a wider table each chunk binds only
+// the columns its texts read (col_maps[c], renumbered in order), and chunks
+// also end where one more output would pass that limit -- the reference
+// splits its plans at 64 slots the same way (LogicalProject.cpp:906-922).
 struct PlanSet {
   std::vector<std::shared_ptr<CompiledPlan>> chunks;
   std::vector<int> first_output;
+  std::vector<std::vector<int>> col_maps;  // per chunk: the table columns it binds (empty: all)
   int num_outputs = 0;
   int num_conjuncts = 0;
   std::vector<int> output_types;
+
+  bool binds_all() const {
+    for (const auto& m : col_maps)
+      if (!m.empty()) return false;
+    return true;
+  }
+  // the views chunk c binds
+  const std::vector<ColumnView>& chunk_cols(size_t c, const std::vector<ColumnView>& cols,
+                                            std::vector<ColumnView>& sub) const {
+    if (col_maps[c].empty()) return cols;
+    sub.clear();
+    for (int k : col_maps[c]) {
+      if (k >= (int)cols.size()) fail(GX_ERR_INVALID, "column count does not match the plan");
+      sub.push_back(cols[k]);
+    }
+    return sub;
+  }
 
   void execute(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, cudaStream_t s) const {
     const bool caller_bufs = num_outputs > 0 && out[0].data != nullptr;
     int64_t rows = -1;
     size_t done = 0;
+    std::vector<ColumnView> sub;
     try {
       for (size_t c = 0; c < chunks.size(); c++) {
         int64_t r = 0;
-        chunks[c]->execute(cols, out + first_output[c], &r, s);
+        chunks[c]->execute(chunk_cols(c, cols, sub), out + first_output[c], &r, s);
         done = c + 1;
         if (rows >= 0 && r != rows) fail(GX_ERR_CUDA, "chunks of one plan disagree on the row count");
         rows = r;
@@ -103,11 +155,49 @@ std::shared_ptr<PlanSet> make_plan_set(const std::vector<int>& schema, const std
                                        bool rand_by_out, const KernelConfig& cfg, int mode, uint64_t seed) {
   auto ps = std::make_shared<PlanSet>();
   int rand_base = 0;
-  for (size_t i = 0; i < exprs.size() || (i == 0 && exprs.empty()); i += GX_OUTPUTS_PER_KERNEL) {
-    std::vector<std::string> part(exprs.begin() + i,
-                                  exprs.begin() + std::min(exprs.size(), i + (size_t)GX_OUTPUTS_PER_KERNEL));
+  const bool wide = schema.size() > (size_t)GX_MAX_COLS;
+  std::vector<int> cond_cols;
+  map_columns(cond, &cond_cols, nullptr);
+  for (size_t i = 0; i < exprs.size() || (i == 0 && exprs.empty());) {
+    // this chunk's outputs: at most GX_OUTPUTS_PER_KERNEL, and over a wide
+    // table no more than keep its columns within GX_MAX_COLS
+    std::vector<int> bound = cond_cols;
+    size_t j = i;
+    while (j < exprs.size() && j - i < (size_t)GX_OUTPUTS_PER_KERNEL) {
+      std::vector<int> t = bound;
+      map_columns(exprs[j], &t, nullptr);
+      std::sort(t.begin(), t.end());
+      t.erase(std::unique(t.begin(), t.end()), t.end());
+      if (wide && j > i && t.size() > (size_t)GX_MAX_COLS) break;
+      bound = std::move(t);
+      j++;
+    }
+    std::vector<std::string> part(exprs.begin() + i, exprs.begin() + j);
+    std::vector<int> col_map;
+    std::vector<int> sub_schema = schema;
+    std::vector<bool> sub_nullable = nullable;
+    std::string sub_cond = cond;
+    if (wide) {
+      std::sort(bound.begin(), bound.end());
+      bound.erase(std::unique(bound.begin(), bound.end()), bound.end());
+      if (bound.empty()) bound.push_back(0);  // a column to carry the row count
+      std::vector<int> renum(schema.size(), -1);
+      sub_schema.clear();
+      sub_nullable.clear();
+      for (int k : bound) {
+        if (k < 0 || k >= (int)schema.size()) fail(GX_ERR_PARSE, "column index out of range: $" + std::to_string(k));
+        renum[k] = (int)sub_schema.size();
+        sub_schema.push_back(schema[k]);
+        sub_nullable.push_back(nullable[k]);
+      }
+      sub_cond = map_columns(cond, nullptr, &renum);
+      for (auto& e : part) e = map_columns(e, nullptr, &renum);
+      col_map = bound;
+    }
     int used = 0;
-    Plan p = build_plan(schema, nullable, cond, part, false, rand_by_out, rand_base, &used);
+    Plan p = build_plan(sub_schema, sub_nullable, sub_cond, part, false, rand_by_out, rand_base, &used);
+    ps->col_maps.push_back(col_map);
+    i = j;
     rand_base += used;
     p.rand_seed = seed;
     if (ps->chunks.empty()) ps->num_conjuncts = (int)p.conjuncts.size();
@@ -212,7 +302,7 @@ namespace gx {
 // The compiled plan of a gx_plan with one kernel (at most GX_OUTPUTS_PER_KERNEL
 // outputs), or null.
 const CompiledPlan* single_chunk(const gx_plan* plan) {
-  if (!plan || plan->ps->chunks.size() != 1) return nullptr;
+  if (!plan || plan->ps->chunks.size() != 1 || !plan->ps->binds_all()) return nullptr;
   return plan->ps->chunks[0].get();
 }
 }  // namespace gx
@@ -245,17 +335,11 @@ struct StringPrepass {
 };
 
 // A CASE condition of the pre-pass evaluated into a BOOL8 column.
-static void compact_plan_columns(std::vector<ColumnView>& cols, std::string& cond, std::vector<std::string>& texts);
-
 static gx_column eval_condition(const std::vector<ColumnView>& cols, const std::string& text, cudaStream_t s) {
-  std::vector<ColumnView> pcols = cols;
-  std::string none;
-  std::vector<std::string> texts = {text};
-  compact_plan_columns(pcols, none, texts);
-  auto ps = plan_for("eval", pcols, "", texts, false);
+  auto ps = plan_for("eval", cols, "", {text}, false);
   gx_column out{};
   int64_t rows = 0;
-  ps->execute(pcols, &out, &rows, s);
+  ps->execute(cols, &out, &rows, s);
   return out;
 }
 
@@ -277,57 +361,6 @@ static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std
   pp.made = run_string_prepass(cols, ops, s, [s](const std::vector<ColumnView>& c, const std::string& t) {
     return eval_condition(c, t, s);
   });
-}
-
-// The columns a text reads ($k outside quoted literals) appended to *used,
-// or, with map, the text with each $k renumbered to $map[k].
-static std::string map_columns(const std::string& t, std::vector<int>* used, const std::vector<int>* map) {
-  std::string r;
-  bool quoted = false;
-  for (size_t i = 0; i < t.size();) {
-    const char c = t[i];
-    if (c == '\'') {
-      if (quoted && i + 1 < t.size() && t[i + 1] == '\'') {  // '' inside a literal
-        r += "''";
-        i += 2;
-        continue;
-      }
-      quoted = !quoted;
-    } else if (!quoted && c == '$' && i + 1 < t.size() && std::isdigit((unsigned char)t[i + 1])) {
-      size_t j = i + 1;
-      long k = 0;
-      while (j < t.size() && std::isdigit((unsigned char)t[j]) && k < (1L << 30)) k = k * 10 + (t[j++] - '0');
-      if (used) used->push_back((int)k);
-      r += "$" + std::to_string(map && k < (long)map->size() && (*map)[k] >= 0 ? (*map)[k] : k);
-      i = j;
-      continue;
-    }
-    r += c;
-    i++;
-  }
-  return r;
-}
-
-// A plan binds at most GX_MAX_COLS columns.  When a table (with the string
-// pre-pass's columns) holds more, the plan gets only the columns its texts
-// read, renumbered in order.
-static void compact_plan_columns(std::vector<ColumnView>& cols, std::string& cond, std::vector<std::string>& texts) {
-  if (cols.size() <= (size_t)GX_MAX_COLS) return;
-  std::vector<int> used = {0};  // column 0 carries the row count of a plan that reads no column
-  map_columns(cond, &used, nullptr);
-  for (const auto& t : texts) map_columns(t, &used, nullptr);
-  std::sort(used.begin(), used.end());
-  used.erase(std::unique(used.begin(), used.end()), used.end());
-  std::vector<int> map(cols.size(), -1);
-  std::vector<ColumnView> kept;
-  for (int k : used) {
-    if (k < 0 || k >= (int)cols.size()) fail(GX_ERR_PARSE, "column index out of range: $" + std::to_string(k));
-    map[k] = (int)kept.size();
-    kept.push_back(cols[k]);
-  }
-  cond = map_columns(cond, nullptr, &map);
-  for (auto& t : texts) t = map_columns(t, nullptr, &map);
-  cols = std::move(kept);
 }
 
 // evaluate_expressions / process_filter / filter + project over a table that
@@ -379,12 +412,8 @@ static void evaluate_with_strings(std::vector<ColumnView> cols, std::string cond
   int64_t rows = n;
   try {
     if (!num.empty()) {
-      std::vector<ColumnView> pcols = cols;
-      std::string pcond = filtering ? cond : std::string();
-      std::vector<std::string> pnum = num;
-      compact_plan_columns(pcols, pcond, pnum);
-      auto ps = plan_for(kind, pcols, pcond, pnum, rand_by_out);
-      ps->execute(pcols, tmp.data(), &rows, s);
+      auto ps = plan_for(kind, cols, filtering ? cond : std::string(), num, rand_by_out);
+      ps->execute(cols, tmp.data(), &rows, s);
       for (size_t j = 0; j < num_pos.size(); j++) {
         out[num_pos[j]] = tmp[j];
         tmp[j] = gx_column{};
@@ -778,10 +807,12 @@ int gx_plan_execute_host(const gx_plan* plan, const gx_column_view* host_columns
     // a plan of more than one kernel (over 32 outputs) runs each one in turn
     const PlanSet& ps = *plan->ps;
     int64_t rows = -1;
+    std::vector<ColumnView> sub;
     for (size_t c = 0; c < ps.chunks.size(); c++) {
       int64_t r = 0;
       try {
-        ps.chunks[c]->execute_host(cols, host_out + ps.first_output[c], &r, (cudaStream_t)stream);
+        ps.chunks[c]->execute_host(ps.chunk_cols(c, cols, sub), host_out + ps.first_output[c], &r,
+                                   (cudaStream_t)stream);
       } catch (const Error& e) {
         if (out_rows && e.code == GX_ERR_CAPACITY) *out_rows = r;  // the count the buffers need
         throw;
@@ -813,6 +844,7 @@ static KernelKind kind_of(int k) {
 // order taken at launch, and the count pass with per-conjunct pass counts
 static std::string debug_source(const gx_plan* plan, int kind, const uint8_t* has_mask) {
   if (!plan) fail(GX_ERR_INVALID, "null plan");
+  if (!plan->ps->binds_all()) fail(GX_ERR_UNSUPPORTED, "diagnostics of a plan over more than 64 columns");
   Plan p = plan->ps->chunks.at(0)->plan();
   for (size_t i = 0; i < p.nullable.size(); i++) p.nullable[i] = has_mask ? has_mask[i] != 0 : true;
   KernelConfig cfg = plan->ps->chunks.at(0)->config();
@@ -865,7 +897,7 @@ void gx_debug_fail_allocation(int n) { debug_fail_allocation(n); }
 int gx_debug_filter_timeout(const gx_plan* plan, const gx_column_view* columns, int num_columns, int64_t first_tile,
                             uint32_t spin_limit, gx_status_info* status) {
   return guarded(status, [&] {
-    if (!plan) fail(GX_ERR_INVALID, "null plan");
+    if (!plan || !plan->ps->binds_all()) fail(GX_ERR_INVALID, "null plan or a plan over more than 64 columns");
     const CompiledPlan& cp = *plan->ps->chunks.at(0);
     if (!cp.plan().has_filter()) fail(GX_ERR_INVALID, "the wait test runs a filter plan");
     auto cols = to_views(columns, num_columns);

@@ -1642,7 +1642,8 @@ gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* opt
   gx_learner* out = nullptr;
   guarded_call(status, [&] {
     const gx::CompiledPlan* cp = gx::single_chunk(plan);
-    if (!cp) gx::fail(GX_ERR_INVALID, "a learner needs a compiled plan with at most 32 outputs");
+    if (!cp) gx::fail(GX_ERR_INVALID, "a learner needs a compiled plan with at most 32 outputs "
+                                      "over at most 64 columns");
     gx_learner_options o;
     gx_learner_options_init(&o);
     if (options) o = *options;

@@ -70,7 +70,8 @@ extern "C" int gx_plan_execute_noalloc(const gx_plan* plan, const gx_column_view
   };
   try {
     const gx::CompiledPlan* cp = gx::single_chunk(plan);
-    if (!cp) return set(GX_ERR_INVALID, "gx_plan_execute_noalloc needs a plan with at most 32 outputs");
+    if (!cp) return set(GX_ERR_INVALID, "gx_plan_execute_noalloc needs a plan with at most 32 outputs "
+                                          "over at most 64 columns");
     if (!out && cp->plan().outputs.size() > 0) return set(GX_ERR_INVALID, "null output array");
     gx::run_filter_noalloc(*cp, gx::to_views(columns, num_columns), out, out_rows, (cudaStream_t)stream);
     return set(GX_OK, "");

@@ -134,6 +134,15 @@ def test_wide_table(gpu, ora):
     got = gpu.filter_project(cols, cond, exprs)
     exp = ora.filter_project(cols, cond, exprs)
     assert_tables_equal(got, exp, what="wide filter")
+    # every column an output (a SELECT * of the table): several kernels, each
+    # binding its own columns
+    every = [f"${k}" for k in range(width)] + ["+($0, $99)"]
+    got = gpu.filter_project(cols, cond, every)
+    exp = ora.filter_project(cols, cond, every)
+    assert_tables_equal(got, exp, what="wide filter, every column")
+    got = gpu.evaluate_expressions(cols, every)
+    exp = ora.evaluate_expressions(cols, every)
+    assert_tables_equal(got, exp, what="wide evaluate, every column")
 
 
 @pytest.mark.parametrize("mode", [N.GX_FILTER_TWO_PASS, N.GX_FILTER_SINGLE_PASS])
