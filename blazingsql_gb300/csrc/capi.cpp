@@ -57,7 +57,6 @@ KernelConfig default_config() {
   c.tune_shape = !std::getenv("GX_WARPS") && !std::getenv("GX_WORDS");
   c.emulate_fp64 = env_int("GX_NATIVE_FP64", 0) == 0;
   c.native_f64_ops = env_int("GX_NATIVE_F64_OPS", -1);
-  c.small_int_convert = env_int("GX_SMALL_I2D", 1) != 0;
   c.dense = env_int("GX_DENSE", 1) != 0;
   c.lazy_case = env_int("GX_LAZY_CASE", 1) != 0;
   c.max_regs = env_int("GX_MAX_REGS", 0);
@@ -264,8 +263,7 @@ std::string cache_key(const char* kind, const std::vector<ColumnView>& cols, con
   }
   k += '|' + std::to_string(cfg.warps) + ':' + std::to_string(cfg.words) + ':' + std::to_string(mode) + ':' +
        std::to_string(cfg.emulate_fp64) + std::to_string(cfg.dense) + std::to_string(cfg.lazy_case) + ':' +
-       std::to_string(cfg.native_f64_ops) + ':' + std::to_string(cfg.small_int_convert) + ':' +
-       std::to_string(cfg.max_regs) + ':' + std::to_string(cfg.use_tma) +
+       std::to_string(cfg.native_f64_ops) + ':' + std::to_string(cfg.max_regs) + ':' + std::to_string(cfg.use_tma) +
        ':' + std::to_string(cfg.tma_warps) + 'x' + std::to_string(cfg.tma_words) + 'x' + std::to_string(cfg.stages);
   return k;
 }

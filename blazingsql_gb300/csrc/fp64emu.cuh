@@ -315,20 +315,6 @@ GXE_FN gxe_u64 gxe_i2d(gxe_i64 v) {
   return sign | ((gxe_u64)eb << 52) | (m & GXE_FRAC);
 }
 
-// (double)(int64) for |v| < 2^32 (always exact), as bits: the magnitude's
-// leading one gives the exponent, the bits below it the fraction, built in
-// two 32-bit words.  Fewer integer instructions than gxe_i2d, and none on
-// the FP64 pipe.
-GXE_FN gxe_u64 gxe_i2d_small(gxe_i64 v) {
-  const unsigned s = v < 0 ? 0x80000000u : 0u;
-  const unsigned u = (unsigned)(v < 0 ? 0ull - (gxe_u64)v : (gxe_u64)v);
-  const int p = 31 - (gxe_clz((gxe_u64)u) - 32);  // leading one; -1 for 0
-  const unsigned hi_m = p <= 20 ? (u << (20 - p)) : (u >> (p - 20));
-  const unsigned lo = p <= 20 ? 0u : (u << (52 - p));
-  const unsigned hi = s | ((unsigned)(p + 1023) << 20) | (hi_m & 0xFFFFFu);
-  return u == 0u ? 0ull : (((gxe_u64)hi << 32) | lo);
-}
-
 // (double)(float) (exact), as bits.
 GXE_FN gxe_u64 gxe_f2d(unsigned f) {
   const gxe_u64 sign = (gxe_u64)(f >> 31) << 63;

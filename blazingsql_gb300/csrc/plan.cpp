@@ -256,35 +256,12 @@ class Gen {
   // operand as a double value (native FP64 arithmetic follows)
   std::string asD(int id) const {
     if (kind_f(id)) return "gx_D(" + B(id) + ")";
-    if (small_int(id)) return "gx_D(gxe_i2d_small((i64)(" + B(id) + ")))";
     return emu_op(kNativeConvert) ? "gx_D(gxe_i2d((i64)(" + B(id) + ")))" : "gx_I2D(" + B(id) + ")";
   }
   // operand as the bits of its double value (integer-pipe binary64 routines follow)
   std::string asDB(int id) const {
     if (kind_f(id)) return B(id);
-    if (small_int(id)) return "gxe_i2d_small((i64)(" + B(id) + "))";
     return emu_op(kNativeConvert) ? "gxe_i2d((i64)(" + B(id) + "))" : "gx_B(gx_I2D(" + B(id) + "))";
-  }
-  // an integer-kind value whose magnitude is below 2^32 on every row: narrow
-  // integer columns, such literals, MOD by such a literal, ABS of such a value
-  // (its exact double then takes a short integer-pipe construction)
-  bool small_int(int id) const {
-    if (!cfg_.small_int_convert || kind_f(id)) return false;
-    const Node& n = p_.nodes[id];
-    const auto fits = [](int64_t v) { return v > -(int64_t(1) << 32) && v < (int64_t(1) << 32); };
-    if (n.kind == Node::LIT) return n.lit_valid && fits((int64_t)n.lit_bits);
-    if (n.kind == Node::COL) {
-      const int t = p_.schema[n.col];
-      return t == INT8 || t == INT16 || t == INT32 || t == UINT8 || t == UINT16 || t == UINT32 || t == BOOL8 ||
-             t == TIMESTAMP_DAYS;
-    }
-    if (n.op == OP_MOD) {
-      const Node& d = p_.nodes[n.b];
-      return !kind_f(n.a) && d.kind == Node::LIT && d.lit_valid && !kind_f(n.b) && d.lit_bits != 0 &&
-             fits((int64_t)d.lit_bits);
-    }
-    if (n.op == OP_ABS) return small_int(n.a);
-    return false;
   }
   std::string asI(int id) const {
     if (!kind_f(id)) return "(i64)(" + B(id) + ")";

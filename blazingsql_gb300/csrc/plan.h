@@ -56,9 +56,6 @@ struct KernelConfig {
   // forms are exact IEEE binary64): kNativeAddSub, kNativeMul, kNativeConvert,
   // kNativeCompare, kNativeRound, kNativeDiv; -1: chosen per plan
   int native_f64_ops = -1;
-  // integer-to-double conversions of values known to have a magnitude below
-  // 2^32 (narrow integer columns, MOD by a literal) built on the integer pipes
-  bool small_int_convert = true;
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
   bool lazy_case = true;     // dense phase: expensive CASE branches only for the rows that select them
   bool runtime_order = false;  // short-circuit AND conjuncts in the order given at launch (KernelArgs::order)

@@ -85,12 +85,6 @@ int main(int argc, char** argv) {
     if (gxe_i2d(iv) != bits((double)iv)) {
       if (bad++ < 10) printf("i2d %lld\n", (long long)iv);
     }
-    const int64_t sv = (int64_t)(int32_t)g.u64() >> (g.u64() % 32);  // |sv| <= 2^31
-    const int64_t uv = (int64_t)(g.u64() >> (32 + g.u64() % 32));    // 0 .. 2^32 - 1
-    if (gxe_i2d_small(sv) != bits((double)sv) || gxe_i2d_small(-uv) != bits((double)-uv) ||
-        gxe_i2d_small(uv) != bits((double)uv)) {
-      if (bad++ < 10) printf("i2d_small %lld %lld\n", (long long)sv, (long long)uv);
-    }
     const uint32_t fb = (uint32_t)g.u64();
     float fv;
     std::memcpy(&fv, &fb, 4);
