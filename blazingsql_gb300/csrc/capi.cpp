@@ -327,6 +327,8 @@ void gx_plan_options_init(gx_plan_options* o) {
 // ordered) when the call's work has been enqueued, unless an output took one.
 struct StringPrepass {
   std::vector<gx_column> made;
+  std::vector<StringOp> ops;
+  std::vector<bool> defer;  // per op: made after the filter, for the kept rows only
   cudaStream_t s = nullptr;
   ~StringPrepass() {
     for (auto& c : made)
@@ -345,8 +347,12 @@ static gx_column eval_condition(const std::vector<ColumnView>& cols, const std::
 
 // String operators over string columns in `cond` / `exprs` become columns
 // appended to `cols` (function_evaluator_transformer, LogicalProject.cpp:671-742).
+// Under a filter, an operator whose column is read only as a whole output
+// (and by nothing else: not the condition, another expression or another
+// operator) is deferred: it is made after the filter for the kept rows alone,
+// instead of for every row and then gathered.  The outputs are the same.
 static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std::vector<std::string>& exprs,
-                           StringPrepass& pp) {
+                           StringPrepass& pp, bool filtering) {
   const std::vector<int> schema = schema_of(cols);
   std::vector<std::string> texts;
   if (cond) texts.push_back(*cond);
@@ -357,10 +363,29 @@ static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std
   size_t i = 0;
   if (cond) *cond = texts[i++];
   for (auto& e : exprs) e = texts[i++];
+  pp.ops = ops;
+  pp.defer.assign(ops.size(), false);
+  if (filtering && !std::getenv("GX_NO_DEFER")) {
+    std::vector<int> read;  // columns read other than as a whole output
+    if (cond) map_columns(*cond, &read, nullptr);
+    for (const auto& e : exprs)
+      if (passthrough_column(e) < 0) map_columns(e, &read, nullptr);
+    for (const auto& op : ops) {
+      read.push_back(op.col);
+      read.push_back(op.col2);
+      read.insert(read.end(), op.more_cols.begin(), op.more_cols.end());
+      map_columns(op.cond, &read, nullptr);
+      map_columns(op.pos0, &read, nullptr);
+      map_columns(op.pos1, &read, nullptr);
+    }
+    for (size_t k = 0; k < ops.size(); k++)
+      pp.defer[k] = is_deferrable(ops[k]) &&
+                    std::find(read.begin(), read.end(), (int)(schema.size() + k)) == read.end();
+  }
   const cudaStream_t s = pp.s;
-  pp.made = run_string_prepass(cols, ops, s, [s](const std::vector<ColumnView>& c, const std::string& t) {
-    return eval_condition(c, t, s);
-  });
+  pp.made = run_string_prepass(
+      cols, ops, s, [s](const std::vector<ColumnView>& c, const std::string& t) { return eval_condition(c, t, s); },
+      &pp.defer);
 }
 
 // evaluate_expressions / process_filter / filter + project over a table that
@@ -379,7 +404,7 @@ static void evaluate_with_strings(std::vector<ColumnView> cols, std::string cond
   const size_t ncols0 = cols.size();
   StringPrepass pp;
   pp.s = s;
-  string_prepass(cols, filtering ? &cond : nullptr, ex, pp);
+  string_prepass(cols, filtering ? &cond : nullptr, ex, pp, filtering);
   if (filtering) {
     const int c = passthrough_column(cond);
     if ((c >= 0 && c < (int)cols.size() && cols[c].type == STRING) || string_literal_value(cond, nullptr))
@@ -430,6 +455,13 @@ static void evaluate_with_strings(std::vector<ColumnView> cols, std::string cond
         continue;
       }
       const size_t k = (size_t)src[i] - ncols0;
+      if (src[i] >= (int)ncols0 && k < pp.defer.size() && pp.defer[k]) {  // made now, for the kept rows
+        out[i] = transform_column(pp.ops[k], cols, filtering ? map : nullptr, rows, s,
+                                  [s](const std::vector<ColumnView>& c, const std::string& t) {
+                                    return eval_condition(c, t, s);
+                                  });
+        continue;
+      }
       if (!filtering && src[i] >= (int)ncols0 && k < pp.made.size() && pp.made[k].data) {
         out[i] = pp.made[k];  // a computed string column moves to the output
         pp.made[k] = gx_column{};

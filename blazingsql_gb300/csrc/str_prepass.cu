@@ -393,6 +393,7 @@ struct XformArgs {
   const unsigned char* s2;  // REPLACE: replacement
   int l2;
   int64_t m;
+  const int32_t* map;  // set: output row o is built from input row map[o] (a gather)
   int32_t* out_offs;
   uint32_t* out_mask;
   unsigned char* out_chars;
@@ -926,11 +927,12 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
+    const int64_t src = (o < a.m && a.map) ? (int64_t)a.map[o] : o;  // the input row
     bool valid = false;
     int len = 0;
     if (o < a.m) {
-      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
-      else len = xform_row(a, o, nullptr, valid);
+      if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
+      else len = xform_row(a, src, nullptr, valid);
     }
     const uint32_t word = __ballot_sync(0xffffffffu, valid);
     if (lane == 0) a.out_mask[w0 + k] = word;
@@ -954,11 +956,12 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
+    const int64_t src = (o < a.m && a.map) ? (int64_t)a.map[o] : o;  // the input row
     bool valid = false;
     int len = 0;
     if (o < a.m) {
-      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
-      else len = xform_row(a, o, nullptr, valid);
+      if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
+      else len = xform_row(a, src, nullptr, valid);
     }
     total += (uint64_t)warp_sum(len);
   }
@@ -969,13 +972,14 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
+    const int64_t src = (o < a.m && a.map) ? (int64_t)a.map[o] : o;  // the input row
     const bool seg = !kRegex && is_segment_kind(a);  // warp-uniform
     const unsigned char *p1 = nullptr, *p2 = nullptr;
     int n1 = 0, len = 0;
     bool valid = false;
     if (o < a.m) {
-      if constexpr (kRegex) len = regex_row(a, o, nullptr, valid);
-      else len = seg ? xform_segments(a, o, p1, n1, p2, valid) : xform_row(a, o, nullptr, valid);
+      if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
+      else len = seg ? xform_segments(a, src, p1, n1, p2, valid) : xform_row(a, src, nullptr, valid);
     }
     int incl = len;
 #pragma unroll
@@ -995,8 +999,8 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
       for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
       for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
     } else if (o < a.m && len > 0) {
-      if constexpr (kRegex) regex_row(a, o, a.out_chars + dst, valid);
-      else xform_row(a, o, a.out_chars + dst, valid);
+      if constexpr (kRegex) regex_row(a, src, a.out_chars + dst, valid);
+      else xform_row(a, src, a.out_chars + dst, valid);
     }
     pos += (uint64_t)wtot;
   }
@@ -1257,7 +1261,8 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
 
 gx_column build_transform(const StringOp& op, const StrSource& a, const StrSource& b, const ColumnView* num,
                           int64_t rows, cudaStream_t s, const std::vector<StrSource>& more,
-                          const ColumnView* pos0 = nullptr, const ColumnView* pos1 = nullptr) {
+                          const ColumnView* pos0 = nullptr, const ColumnView* pos1 = nullptr,
+                          const int32_t* map = nullptr) {
   if (more.size() > (size_t)(kMaxConcatParts - 2)) fail(GX_ERR_INVALID, "too many CONCAT parts");
   if (rows < 0 || rows > INT32_MAX) fail(GX_ERR_UNSUPPORTED, "string columns hold at most 2^31 - 1 rows");
   const int64_t nblocks = (rows + kBuildRows - 1) / kBuildRows;
@@ -1324,6 +1329,7 @@ gx_column build_transform(const StringOp& op, const StrSource& a, const StrSourc
     x.s2 = ldev + loff[3];
     x.l2 = (int)op.literal2.size();
     x.m = rows;
+    x.map = map;
     x.out_offs = out.string_offsets;
     x.out_mask = out.null_mask;
     x.block_sums = sums;
@@ -1547,9 +1553,107 @@ void launch_string_op(const ColumnView& col, const ColumnView* col2, const Strin
   add_launches(1);
 }
 
-std::vector<gx_column> run_string_prepass(
-    std::vector<ColumnView>& cols, const std::vector<StringOp>& ops, cudaStream_t s,
-    const std::function<gx_column(const std::vector<ColumnView>&, const std::string&)>& eval_bool) {
+bool is_deferrable(const StringOp& op) {
+  switch (op.kind) {
+    case StringOp::TO_STRING: case StringOp::SLICE: case StringOp::UPPER: case StringOp::LOWER:
+    case StringOp::INITCAP: case StringOp::TRIM: case StringOp::REPLACE: case StringOp::CONCAT:
+    case StringOp::REGEXP_REPLACE:
+      return true;
+    default:
+      return false;
+  }
+}
+
+gx_column transform_column(const StringOp& op, const std::vector<ColumnView>& cols, const int32_t* map,
+                           int64_t rows, cudaStream_t s, const EvalText& eval_bool) {
+  const int64_t n = cols.empty() ? 0 : cols[0].size;
+  auto string_col = [&](int c) {
+    const ColumnView v = cols.at(c);
+    if (v.type != STRING) fail(GX_ERR_TYPE, "string operator over a non-string column");
+    return v;
+  };
+  gx_column out{};
+  if (op.kind == StringOp::TO_STRING) {
+    gx_column tmp{};
+    ColumnView v = op.col >= 0 ? cols.at(op.col) : ColumnView{};
+    if (op.col < 0) {
+      tmp = eval_bool(cols, op.cond);
+      v = ColumnView{tmp.type_id, tmp.data, tmp.null_mask, 0, n, tmp.string_offsets};
+    }
+    try {
+      if (v.type == STRING) {
+        StrSource a, none;
+        a.kind = StrSource::COLUMN;
+        a.col = v;
+        out = build_strings(a, none, map, nullptr, rows, s);
+      } else {
+        if (type_size(v.type) == 0 || v.type >= DURATION_DAYS)
+          fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(v.type));
+        out = build_transform(op, StrSource{}, StrSource{}, &v, rows, s, {}, nullptr, nullptr, map);
+      }
+    } catch (...) {
+      if (tmp.data || tmp.null_mask) free_column(tmp, s);
+      throw;
+    }
+    if (tmp.data || tmp.null_mask) free_column(tmp, s);
+    return out;
+  }
+  // a part: a string column, a literal, or (CONCAT) a typed column to format
+  auto part = [&](int c, const std::string& lit) {
+    StrSource x;
+    if (c < 0) {
+      x.kind = StrSource::LITERAL;
+      x.literal = lit;
+    } else if (op.kind == StringOp::CONCAT && cols.at(c).type != STRING) {
+      x.kind = StrSource::FORMAT;
+      x.col = cols.at(c);
+    } else {
+      x.kind = StrSource::COLUMN;
+      x.col = string_col(c);
+    }
+    return x;
+  };
+  StrSource a = part(op.col, op.literal), b;
+  if (op.kind == StringOp::CONCAT) b = part(op.col2, op.literal2);
+  std::vector<StrSource> more;
+  for (size_t k = 0; k < op.more_cols.size(); k++) more.push_back(part(op.more_cols[k], op.more_lits[k]));
+  StringOp xo = op;
+  if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
+  if (op.kind == StringOp::REGEXP_REPLACE) compile_regex_replace(op.literal, op.literal2, &xo.literal, &xo.literal2);
+  if (op.kind == StringOp::SLICE && !op.pos0.empty()) {
+    // the start and stop columns (LogicalProject.cpp:241-300), made by
+    // the same evaluator as a CASE condition over every input row
+    gx_column pc[2] = {};
+    auto release = [&] {
+      for (auto& c : pc)
+        if (c.data || c.null_mask) free_column(c, s);
+    };
+    try {
+      ColumnView pv[2];
+      for (int k = 0; k < 2; k++) {
+        const std::string& text = k == 0 ? op.pos0 : op.pos1;
+        if (text.empty()) continue;
+        pc[k] = eval_bool(cols, text);
+        const int t = pc[k].type_id;
+        if (t != INT8 && t != INT16 && t != INT32 && t != INT64 && t != UINT8 && t != UINT16 && t != UINT32 &&
+            t != UINT64)
+          fail(GX_ERR_TYPE, "Expression does not evaluate to an integer column");  // :252
+        pv[k] = ColumnView{t, pc[k].data, pc[k].null_mask, 0, n};
+      }
+      out = build_transform(xo, a, b, nullptr, rows, s, more, &pv[0], op.pos1.empty() ? nullptr : &pv[1], map);
+    } catch (...) {
+      release();
+      throw;
+    }
+    release();
+    return out;
+  }
+  return build_transform(xo, a, b, nullptr, rows, s, more, nullptr, nullptr, map);
+}
+
+std::vector<gx_column> run_string_prepass(std::vector<ColumnView>& cols, const std::vector<StringOp>& ops,
+                                          cudaStream_t s, const EvalText& eval_bool,
+                                          const std::vector<bool>* defer) {
   std::vector<gx_column> made;
   if (ops.empty()) return made;
   const int64_t n = cols.empty() ? 0 : cols[0].size;
@@ -1584,6 +1688,13 @@ std::vector<gx_column> run_string_prepass(
     for (size_t i = 0; i < ops.size(); i++) {
       const StringOp& op = ops[i];
       gx_column out{};
+      if (defer && i < defer->size() && (*defer)[i]) {
+        // made later over the kept rows only (transform_column with a row
+        // map); nothing before the plan reads it
+        made.push_back(out);
+        cols.push_back(ColumnView{STRING, nullptr, nullptr, 0, n, nullptr});
+        continue;
+      }
       if (op.kind == StringOp::CASE) {
         StrSource a, b;
         if (op.col >= 0) {
@@ -1609,83 +1720,8 @@ std::vector<gx_column> run_string_prepass(
           throw;
         }
         free_column(mask, s);
-      } else if (op.kind == StringOp::TO_STRING) {
-        gx_column tmp{};
-        ColumnView v = op.col >= 0 ? cols.at(op.col) : ColumnView{};
-        if (op.col < 0) {
-          tmp = eval_bool(cols, op.cond);
-          v = ColumnView{tmp.type_id, tmp.data, tmp.null_mask, 0, n, tmp.string_offsets};
-        }
-        try {
-          if (v.type == STRING) {
-            StrSource a, none;
-            a.kind = StrSource::COLUMN;
-            a.col = v;
-            out = build_strings(a, none, nullptr, nullptr, n, s);
-          } else {
-            if (type_size(v.type) == 0 || v.type >= DURATION_DAYS)
-              fail(GX_ERR_UNSUPPORTED, "CAST to VARCHAR of type " + std::to_string(v.type));
-            out = build_transform(op, StrSource{}, StrSource{}, &v, n, s, {});
-          }
-        } catch (...) {
-          if (tmp.data || tmp.null_mask) free_column(tmp, s);
-          throw;
-        }
-        if (tmp.data || tmp.null_mask) free_column(tmp, s);
-      } else if (op.kind == StringOp::SLICE || op.kind == StringOp::UPPER || op.kind == StringOp::LOWER ||
-                 op.kind == StringOp::INITCAP || op.kind == StringOp::TRIM || op.kind == StringOp::REPLACE ||
-                 op.kind == StringOp::CONCAT || op.kind == StringOp::REGEXP_REPLACE) {
-        // a part: a string column, a literal, or (CONCAT) a typed column to format
-        auto part = [&](int c, const std::string& lit) {
-          StrSource x;
-          if (c < 0) {
-            x.kind = StrSource::LITERAL;
-            x.literal = lit;
-          } else if (op.kind == StringOp::CONCAT && cols.at(c).type != STRING) {
-            x.kind = StrSource::FORMAT;
-            x.col = cols.at(c);
-          } else {
-            x.kind = StrSource::COLUMN;
-            x.col = string_col(c);
-          }
-          return x;
-        };
-        StrSource a = part(op.col, op.literal), b;
-        if (op.kind == StringOp::CONCAT) b = part(op.col2, op.literal2);
-        std::vector<StrSource> more;
-        for (size_t k = 0; k < op.more_cols.size(); k++) more.push_back(part(op.more_cols[k], op.more_lits[k]));
-        StringOp xo = op;
-        if (op.kind == StringOp::CONCAT) xo.literal.clear(), xo.literal2.clear();
-        if (op.kind == StringOp::REGEXP_REPLACE) compile_regex_replace(op.literal, op.literal2, &xo.literal, &xo.literal2);
-        if (op.kind == StringOp::SLICE && !op.pos0.empty()) {
-          // the start and stop columns (LogicalProject.cpp:241-300), made by
-          // the same evaluator as a CASE condition
-          gx_column pc[2] = {};
-          auto release = [&] {
-            for (auto& c : pc)
-              if (c.data || c.null_mask) free_column(c, s);
-          };
-          try {
-            ColumnView pv[2];
-            for (int k = 0; k < 2; k++) {
-              const std::string& text = k == 0 ? op.pos0 : op.pos1;
-              if (text.empty()) continue;
-              pc[k] = eval_bool(cols, text);
-              const int t = pc[k].type_id;
-              if (t != INT8 && t != INT16 && t != INT32 && t != INT64 && t != UINT8 && t != UINT16 &&
-                  t != UINT32 && t != UINT64)
-                fail(GX_ERR_TYPE, "Expression does not evaluate to an integer column");  // :252
-              pv[k] = ColumnView{t, pc[k].data, pc[k].null_mask, 0, n};
-            }
-            out = build_transform(xo, a, b, nullptr, n, s, more, &pv[0], op.pos1.empty() ? nullptr : &pv[1]);
-          } catch (...) {
-            release();
-            throw;
-          }
-          release();
-        } else {
-          out = build_transform(xo, a, b, nullptr, n, s, more);
-        }
+      } else if (is_deferrable(op)) {
+        out = transform_column(op, cols, nullptr, n, s, eval_bool);
       } else if (op.kind == StringOp::PARSE) {
         const ColumnView c = string_col(op.col);
         out = alloc_column(op.type, n, s);

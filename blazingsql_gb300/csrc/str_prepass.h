@@ -55,8 +55,22 @@ gx_column build_strings(const StrSource& a, const StrSource& b, const int32_t* m
 // columns so far into a column: a CASE condition (BOOL8), the operand of a
 // CAST to VARCHAR, a SUBSTRING's start or stop (integers).  The returned columns are the caller's
 // to free once the work that reads them has been enqueued.
-std::vector<gx_column> run_string_prepass(
-    std::vector<ColumnView>& cols, const std::vector<StringOp>& ops, cudaStream_t s,
-    const std::function<gx_column(const std::vector<ColumnView>&, const std::string&)>& eval_bool);
+using EvalText = std::function<gx_column(const std::vector<ColumnView>&, const std::string&)>;
+// defer (optional, per op): ops to skip here, for transform_column to make
+// later over the kept rows; their columns are appended as empty placeholders.
+std::vector<gx_column> run_string_prepass(std::vector<ColumnView>& cols, const std::vector<StringOp>& ops,
+                                          cudaStream_t s, const EvalText& eval_bool,
+                                          const std::vector<bool>* defer = nullptr);
+
+// The operators whose result is built row by row from the rows of their
+// inputs (casts to VARCHAR, slices, case mappings, TRIM, REPLACE, CONCAT,
+// REGEXP_REPLACE): these can be made after a filter, for its kept rows only.
+bool is_deferrable(const StringOp& op);
+
+// Such an operator over `cols` (every input row) into a string column of
+// `rows` rows; with map, output row o is made from input row map[o] (the
+// kept rows of a filter, LogicalFilter.cpp:22-29, gathered while building).
+gx_column transform_column(const StringOp& op, const std::vector<ColumnView>& cols, const int32_t* map,
+                           int64_t rows, cudaStream_t s, const EvalText& eval_bool);
 
 }  // namespace gx

@@ -457,7 +457,13 @@ def test_string_functions_in_filters():
     cols, strings = _function_table(rng, n)
     dev = _device(cols, strings)
     cond = "AND(=(LEFT($12, 1), 'a'), >(CAST($9):INTEGER, 0))"
-    exprs = ["CONCAT($0, '/', CAST($5):VARCHAR)", "$12", "CAST($10):DATE", "REVERSE($3)"]
+    # string functions read only as outputs are made after the filter, for
+    # the kept rows alone (through the row map); LEFT($12, 1) is read by the
+    # condition and made before it
+    exprs = ["CONCAT($0, '/', CAST($5):VARCHAR)", "$12", "CAST($10):DATE", "REVERSE($3)",
+             "SUBSTRING($0, $17, CHAR_LENGTH($3))", "REGEXP_REPLACE($0, '[ab]+', '<\\0>')", "UPPER($18)",
+             "CAST($16):VARCHAR", "CAST(+($1, 7)):VARCHAR", "LEFT($12, 1)", "INITCAP($12)", "INITCAP($12)",
+             "CHAR_LENGTH(TRIM(FLAG(BOTH), ' ', $3))"]
     got = g.filter_project(dev, cond, exprs)
     exp, rows = strings_ref.filter_project(cols, strings, cond, exprs)
     assert got[0].size == rows
