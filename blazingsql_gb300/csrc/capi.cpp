@@ -365,7 +365,7 @@ static void string_prepass(std::vector<ColumnView>& cols, std::string* cond, std
   for (auto& e : exprs) e = texts[i++];
   pp.ops = ops;
   pp.defer.assign(ops.size(), false);
-  if (filtering && !std::getenv("GX_NO_DEFER")) {
+  if (filtering) {
     std::vector<int> read;  // columns read other than as a whole output
     if (cond) map_columns(*cond, &read, nullptr);
     for (const auto& e : exprs)
