@@ -295,6 +295,25 @@ __device__ __forceinline__ void warp_copy(unsigned char* out, int ex, int n1, co
   }
 }
 
+// Rows of one 32-row word whose bytes total at most kStageBytes are written
+// by their lanes into a per-warp shared-memory stage, then copied out by the
+// whole warp with coalesced 4-byte stores (byte stores only at the two
+// ends); the stage starts at pos % 4 so stage and output words line up.
+constexpr int kStageBytes = 32 * kWarpCopyBytes;
+
+__device__ __forceinline__ void stage_flush(unsigned char* out, uint64_t pos, const unsigned char* st, int wtot,
+                                            int lane) {
+  const int sh = (int)(pos & 3u);
+  const int head = min(wtot, (4 - sh) & 3);
+  if (lane < head) out[pos + lane] = st[sh + lane];
+  const int nw = (wtot - head) >> 2;
+  uint32_t* gw = (uint32_t*)(out + pos + head);
+  const uint32_t* sw = (const uint32_t*)(st + sh + head);
+  for (int w = lane; w < nw; w += 32) gw[w] = sw[w];
+  const int t0 = head + nw * 4;
+  if (lane < wtot - t0) out[pos + t0 + lane] = st[sh + t0 + lane];
+}
+
 __global__ void __launch_bounds__(kBuildWarps * 32) k_str_sizes(BuildArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -323,6 +342,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_str_sizes(BuildArgs a) {
 // block_sums hold each block's first character position (exclusive scan)
 __global__ void __launch_bounds__(kBuildWarps * 32) k_str_write(BuildArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
+  __shared__ __align__(16) unsigned char s_stage[kBuildWarps][kStageBytes + 8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
   uint64_t total = 0;
@@ -358,10 +378,15 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_str_write(BuildArgs a) {
       if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
     }
     const int wtot = __shfl_sync(0xffffffffu, incl, 31);
-    if (wtot > 32 * kWarpCopyBytes)  // long rows: the warp copies them together
+    if (wtot > kStageBytes) {  // long rows: the warp copies them together
       warp_copy(a.out_chars + pos, incl - len, len, p, nullptr, wtot, lane);
-    else  // short rows: a lane copies its own
-      for (int i = 0; i < len; i++) a.out_chars[dst + i] = p[i];
+    } else {  // short rows: each lane stages its own, the warp writes them out
+      unsigned char* st = s_stage[warp] + (pos & 3u) + (incl - len);
+      for (int i = 0; i < len; i++) st[i] = p[i];
+      __syncwarp();
+      stage_flush(a.out_chars, pos, s_stage[warp], wtot, lane);
+      __syncwarp();
+    }
     pos += (uint64_t)wtot;
   }
 }
@@ -950,6 +975,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
 template <bool kRegex>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
+  __shared__ __align__(16) unsigned char s_stage[kBuildWarps][kStageBytes + 8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
   uint64_t total = 0;
@@ -993,11 +1019,20 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
       if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
     }
     const int wtot = __shfl_sync(0xffffffffu, incl, 31);
-    if (seg && wtot > 32 * kWarpCopyBytes) {  // long rows: the warp copies them together
+    if (seg && wtot > kStageBytes) {  // long rows: the warp copies them together
       warp_copy(a.out_chars + pos, incl - len, n1, p1, p2, wtot, lane);
-    } else if (seg) {
-      for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
-      for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
+    } else if (wtot <= kStageBytes) {  // short rows: staged by their lanes, written out by the warp
+      unsigned char* st = s_stage[warp] + (pos & 3u) + (incl - len);
+      if (seg) {
+        for (int i = 0; i < n1; i++) st[i] = p1[i];
+        for (int i = n1; i < len; i++) st[i] = p2[i - n1];
+      } else if (o < a.m && len > 0) {
+        if constexpr (kRegex) regex_row(a, src, st, valid);
+        else xform_row(a, src, st, valid);
+      }
+      __syncwarp();
+      stage_flush(a.out_chars, pos, s_stage[warp], wtot, lane);
+      __syncwarp();
     } else if (o < a.m && len > 0) {
       if constexpr (kRegex) regex_row(a, src, a.out_chars + dst, valid);
       else xform_row(a, src, a.out_chars + dst, valid);
