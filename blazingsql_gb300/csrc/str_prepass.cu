@@ -156,20 +156,50 @@ __global__ void k_string_op(StrArgs a) {
         plen = a.offs2[q2 + 1] - a.offs2[q2];
       }
       if (a.op == StringOp::CHAR_LENGTH) {
-        int c = 0;
-        for (int i = 0; i < len; i++) c += (s[i] & 0xC0) != 0x80;
+        // characters = bytes that are not UTF-8 continuation bytes (10xxxxxx),
+        // counted four at a time over the aligned words of the row
+        int c = 0, i = 0;
+        for (; i < len && ((uintptr_t)(s + i) & 3u); i++) c += (s[i] & 0xC0) != 0x80;
+        for (; i + 4 <= len; i += 4) {
+          const uint32_t w = *(const uint32_t*)(s + i);
+          c += 4 - __popc((w >> 7) & ~(w >> 6) & 0x01010101u);
+        }
+        for (; i < len; i++) c += (s[i] & 0xC0) != 0x80;
         ((int32_t*)a.out)[r] = valid ? c : 0;
       } else {
         bool v = false;
         if (valid) {
           if (a.op == StringOp::LIKE && a.dfa) {
-            // a table step per byte, the same instructions in every lane
+            // a table step per byte, the same instructions in every lane; the
+            // row's aligned middle is read a 4-byte word at a time
             const unsigned char* flags = s_dfa + 256;
             const unsigned char* tr = flags + a.dfa_states;
-            int st = a.dfa_start;
-            for (int i = 0; i < len; i++) {
-              st = tr[st * a.dfa_classes + s_dfa[s[i]]];
-              if (flags[st] & 2) break;  // absorbing: decided
+            const int nc = a.dfa_classes;
+            int st = a.dfa_start, i = 0;
+            bool done = false;
+            for (; i < len && ((uintptr_t)(s + i) & 3u); i++) {
+              st = tr[st * nc + s_dfa[s[i]]];
+              if (flags[st] & 2) {  // absorbing: decided
+                done = true;
+                break;
+              }
+            }
+            for (; !done && i + 4 <= len; i += 4) {
+              const uint32_t w = *(const uint32_t*)(s + i);
+              const int c0 = s_dfa[w & 0xFFu], c1 = s_dfa[(w >> 8) & 0xFFu], c2 = s_dfa[(w >> 16) & 0xFFu],
+                        c3 = s_dfa[w >> 24];
+              st = tr[st * nc + c0];
+              if (flags[st] & 2) { done = true; break; }
+              st = tr[st * nc + c1];
+              if (flags[st] & 2) { done = true; break; }
+              st = tr[st * nc + c2];
+              if (flags[st] & 2) { done = true; break; }
+              st = tr[st * nc + c3];
+              if (flags[st] & 2) { done = true; break; }
+            }
+            for (; !done && i < len; i++) {
+              st = tr[st * nc + s_dfa[s[i]]];
+              if (flags[st] & 2) break;
             }
             v = flags[st] & 1;
           } else if (a.op == StringOp::LIKE) {
@@ -958,6 +988,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
     if (o < a.m) {
       if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
       else len = xform_row(a, src, nullptr, valid);
+      a.out_offs[o] = len;  // the row's length, read back by k_xf_write (which then writes offsets)
     }
     const uint32_t word = __ballot_sync(0xffffffffu, valid);
     if (lane == 0) a.out_mask[w0 + k] = word;
@@ -975,20 +1006,13 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
 template <bool kRegex>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
-  __shared__ __align__(16) unsigned char s_stage[kBuildWarps][kStageBytes + 8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
   uint64_t total = 0;
   for (int k = 0; k < kBuildWords; k++) {
     const int64_t o = (w0 + k) * 32 + lane;
     if ((w0 + k) * 32 >= a.m) break;
-    const int64_t src = (o < a.m && a.map) ? (int64_t)a.map[o] : o;  // the input row
-    bool valid = false;
-    int len = 0;
-    if (o < a.m) {
-      if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
-      else len = xform_row(a, src, nullptr, valid);
-    }
+    const int len = o < a.m ? a.out_offs[o] : 0;  // k_xf_sizes' row lengths
     total += (uint64_t)warp_sum(len);
   }
   if (lane == 0) s_sum[warp] = total;
@@ -1004,8 +1028,8 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
     int n1 = 0, len = 0;
     bool valid = false;
     if (o < a.m) {
-      if constexpr (kRegex) len = regex_row(a, src, nullptr, valid);
-      else len = seg ? xform_segments(a, src, p1, n1, p2, valid) : xform_row(a, src, nullptr, valid);
+      if (seg) len = xform_segments(a, src, p1, n1, p2, valid);
+      else len = a.out_offs[o];  // k_xf_sizes' row length
     }
     int incl = len;
 #pragma unroll
@@ -1019,20 +1043,11 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
       if (o == a.m - 1) a.out_offs[a.m] = (int32_t)(dst + (uint64_t)len);
     }
     const int wtot = __shfl_sync(0xffffffffu, incl, 31);
-    if (seg && wtot > kStageBytes) {  // long rows: the warp copies them together
+    if (seg && wtot > 32 * kWarpCopyBytes) {  // long rows: the warp copies them together
       warp_copy(a.out_chars + pos, incl - len, n1, p1, p2, wtot, lane);
-    } else if (wtot <= kStageBytes) {  // short rows: staged by their lanes, written out by the warp
-      unsigned char* st = s_stage[warp] + (pos & 3u) + (incl - len);
-      if (seg) {
-        for (int i = 0; i < n1; i++) st[i] = p1[i];
-        for (int i = n1; i < len; i++) st[i] = p2[i - n1];
-      } else if (o < a.m && len > 0) {
-        if constexpr (kRegex) regex_row(a, src, st, valid);
-        else xform_row(a, src, st, valid);
-      }
-      __syncwarp();
-      stage_flush(a.out_chars, pos, s_stage[warp], wtot, lane);
-      __syncwarp();
+    } else if (seg) {
+      for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
+      for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
     } else if (o < a.m && len > 0) {
       if constexpr (kRegex) regex_row(a, src, a.out_chars + dst, valid);
       else xform_row(a, src, a.out_chars + dst, valid);
