@@ -330,6 +330,15 @@ def test_string_empty_inputs():
     assert out[1].to_strings() == ["", None, ""]
     out = g.process_filter(dev, "LogicalFilter(condition=[<($1, 0)])")
     assert out[0].to_strings() == [] and out[1].size == 0
+    # string functions made after a filter that keeps no row, and over an empty table
+    exprs = ["UPPER($0)", "CONCAT($0, '-', CAST($1):VARCHAR)", "SUBSTRING($0, $1)", "REGEXP_REPLACE($0, 'a', 'b')"]
+    out = g.filter_project(dev, "<($1, 0)", exprs)
+    assert [c.to_strings() for c in out] == [[]] * 4
+    empty = [DeviceColumn.from_strings([]), DeviceColumn.from_host(HostColumn(T.INT32, np.zeros(0, np.int32)))]
+    out = g.filter_project(empty, ">($1, 0)", exprs)
+    assert [c.to_strings() for c in out] == [[]] * 4
+    out = g.filter_project(dev, ">=($1, 1)", exprs)
+    assert [c.to_strings() for c in out] == [[None, ""], [None, "-2"], [None, ""], [None, ""]]
 
 
 def _function_table(rng, n):
