@@ -50,6 +50,7 @@ struct AggFinal {
   AggTable t;
   unsigned long long* counter;
   int empty_group;  // no group keys and no row: one row of empty aggregates
+  unsigned long long cnt_rows;  // accumulators whose valid count is the group's row count (input never NULL)
 };
 
 __device__ __forceinline__ void store_w(void* d, uint64_t p, int w, uint64_t v) {
@@ -78,7 +79,7 @@ __device__ void write_row(const AggFinal& f, long long i, uint64_t p) {
   for (int j = 0; j < f.na; j++) {
     const int o = f.nk + j;
     const int q = f.acc_of[j];
-    const uint64_t c = i < 0 ? 0ull : (q < 0 ? f.t.rows[i] : f.t.cnt[q * cap + i]);
+    const uint64_t c = i < 0 ? 0ull : (q < 0 || ((f.cnt_rows >> q) & 1ull)) ? f.t.rows[i] : f.t.cnt[q * cap + i];
     const uint64_t a = (i < 0 || q < 0) ? 0ull : f.t.acc[q * cap + i];
     const int kind = f.kind[j];
     if (kind == 4 || kind == 5) {  // COUNT_VALID, COUNT_ALL
@@ -354,6 +355,11 @@ void AggPlan::execute(const std::vector<ColumnView>& cols, gx_column* out, int64
     f.t = t;
     f.counter = (unsigned long long*)(base + (size_t)cap * (4 + 4 + 8 + 8 * nk + 16 * na)) + 4;
     f.empty_group = empty_group ? 1 : 0;
+    {
+      Plan p = plan_;
+      p.nullable = nb;
+      f.cnt_rows = agg_counts_are_rows(p, layout_);
+    }
     const unsigned grid = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)device_sm_count() * 8);
     k_agg_finalize<<<grid, 256, 0, s>>>(f);
     check_cuda(cudaGetLastError(), "k_agg_finalize");

@@ -2308,6 +2308,16 @@ static std::string agg_identity(int kind, bool flt) {
   return "0ull";                                                 // sums (0 and +0.0 share bits)
 }
 
+uint64_t agg_counts_are_rows(const Plan& p, const AggLayout& L) {
+  KernelConfig cfg;
+  cfg.native_f64_ops = 0;
+  Gen g(p, cfg);
+  uint64_t m = 0;
+  for (size_t j = 0; j < L.in_nodes.size() && j < 64; j++)
+    if (L.in_nodes[j] >= 0 && g.never_null(L.in_nodes[j])) m |= 1ull << j;
+  return m;
+}
+
 std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelConfig& cfg_in,
                                 const std::string& name) {
   KernelConfig cfg = cfg_in;
@@ -2319,6 +2329,7 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   std::ostringstream o;
   emit_prelude(o, cfg);
   const int nk = (int)L.key_nodes.size(), na = (int)L.kinds.size(), S = L.smem_slots;
+  const uint64_t rows_cnt = agg_counts_are_rows(p, L);
   if (S < 16 || (S & (S - 1)) != 0) fail(GX_ERR_INVALID, "aggregation table slots must be a power of two >= 16");
   o << "#define GXA_S " << S << "\n#define GXA_NK " << std::max(nk, 1) << "\n#define GXA_NA " << std::max(na, 1)
     << "\n#define GXA_PROBES 32\n";
@@ -2505,7 +2516,8 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
     for (int j = 0; j < na; j++) {
       const int in = L.in_nodes[j];
       o << in2 << "  if (" << (in >= 0 ? g.V(in) : std::string("true")) << ") {\n";
-      o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], 1ull);\n";
+      if (!((rows_cnt >> j) & 1ull))
+        o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], 1ull);\n";
       if (!ac[j].ty.empty())
         o << in2 << "    " << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", ac[j].val) << "\n";
       o << in2 << "  }\n";
@@ -2518,7 +2530,10 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
       const int in = L.in_nodes[j];
       const std::string vj = in >= 0 ? "(sm_ && " + g.V(in) + ")" : "sm_";
       o << in2 << "const bool vl" << j << "_ = " << vj << ";\n";
-      o << in2 << "const u64 c" << j << "_ = (u64)__popc(__ballot_sync(GX_FULL, vl" << j << "_) & peers_);\n";
+      if ((rows_cnt >> j) & 1ull)  // never NULL: the count is the group's rows
+        o << in2 << "const u64 c" << j << "_ = (u64)__popc(peers_);\n";
+      else
+        o << in2 << "const u64 c" << j << "_ = (u64)__popc(__ballot_sync(GX_FULL, vl" << j << "_) & peers_);\n";
       if (!ac[j].ty.empty())
         o << in2 << ac[j].ty << " x" << j << "_ = vl" << j << "_ ? " << ac[j].val << " : " << ac[j].id << ";\n";
     }
@@ -2535,8 +2550,9 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
     o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
     for (int j = 0; j < na; j++) {
       o << in2 << "  if (c" << j << "_ != 0ull) {\n";
-      o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
-        << "_);\n";
+      if (!((rows_cnt >> j) & 1ull))
+        o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
+          << "_);\n";
       if (!ac[j].ty.empty())
         o << in2 << "    "
           << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", "x" + std::to_string(j) + "_") << "\n";
@@ -2553,7 +2569,8 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
     const int in = L.in_nodes[j];
     const std::string vj = in >= 0 ? g.V(in) : "true";
     o << in2 << "    if (" << vj << ") {\n";
-    o << in2 << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), 1ull);\n";
+    if (!((rows_cnt >> j) & 1ull))
+      o << in2 << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), 1ull);\n";
     if (!ac[j].ty.empty())
       o << in2 << "      " << atom(j, "ga.acc + " + std::to_string(j) + "ull * ga.cap + gs_", ac[j].val) << "\n";
     o << in2 << "    }\n";
@@ -2573,9 +2590,12 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   o << "    if (gs_ < 0) continue;\n";
   o << "    atomicAdd((unsigned long long*)(ga.rows + gs_), (unsigned long long)s_rows_[i]);\n";
   for (int j = 0; j < na; j++) {
-    o << "    if (s_cnt_[" << j << " * GXA_S + i] != 0ull) {\n";
-    o << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), (unsigned long long)s_cnt_["
-      << j << " * GXA_S + i]);\n";
+    const bool rc = (rows_cnt >> j) & 1ull;  // no valid count kept: every row of the group is valid
+    o << "    if (" << (rc ? std::string("s_rows_[i]") : "s_cnt_[" + std::to_string(j) + " * GXA_S + i]")
+      << " != 0ull) {\n";
+    if (!rc)
+      o << "      atomicAdd((unsigned long long*)(ga.cnt + " << j << "ull * ga.cap + gs_), (unsigned long long)s_cnt_["
+        << j << " * GXA_S + i]);\n";
     if (!ac[j].ty.empty()) {
       std::string x;
       if (ac[j].ty == "double") x = "__longlong_as_double((long long)s_acc_[" + std::to_string(j) + " * GXA_S + i])";

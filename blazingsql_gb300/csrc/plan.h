@@ -121,6 +121,10 @@ struct AggLayout {
   bool warp_combine = true;
 };
 std::string generate_agg_kernel(const Plan& plan, const AggLayout& L, const KernelConfig& cfg, const std::string& name);
+// Accumulators (bit j of L's accumulator j) whose input is never NULL under
+// plan.nullable: the aggregation kernel keeps no valid count for them, and
+// the group's row count stands for it.
+uint64_t agg_counts_are_rows(const Plan& plan, const AggLayout& L);
 
 // Outputs per plan kernel; longer expression lists are split into several
 // plans (the reference splits at 64 interpreter slots, LogicalProject.cpp:906-922).
