@@ -2537,7 +2537,10 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
       if (!ac[j].ty.empty())
         o << in2 << ac[j].ty << " x" << j << "_ = vl" << j << "_ ? " << ac[j].val << " : " << ac[j].id << ";\n";
     }
+    // a tree over each group's lanes: log2 of the largest group's lanes steps
+    o << in2 << "const int mx_ = (int)__reduce_max_sync(GX_FULL, (u32)__popc(peers_));\n";
     o << in2 << "#pragma unroll\n" << in2 << "for (int s_ = 1; s_ < 32; s_ <<= 1) {\n";
+    o << in2 << "  if (s_ >= mx_) break;\n";
     o << in2 << "  const int src_ = pr_.partner(); const bool rcv_ = pr_.receives(s_);\n";
     for (int j = 0; j < na; j++) {
       if (ac[j].ty.empty()) continue;
