@@ -2334,10 +2334,12 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   o << "#define GXA_S " << S << "\n#define GXA_NK " << std::max(nk, 1) << "\n#define GXA_NA " << std::max(na, 1)
     << "\n#define GXA_PROBES 32\n";
   // key hash (null keys hash as zero with their null bit set)
+  // (multiply by odd constants per key, then the high half folded onto the
+  // low one, which the table index takes)
   o << "__device__ __forceinline__ u64 gxa_hash(const u64* kv, u32 kn) {\n"
-       "  u64 h = 0x9E3779B97F4A7C15ull ^ (u64)kn;\n";
-  for (int j = 0; j < nk; j++) o << "  h = gx_mix64(h ^ (kv[" << j << "] + " << (j + 1) << "ull * 0x632BE59BD9B4E019ull));\n";
-  o << "  return gx_mix64(h);\n}\n";
+       "  u64 h = (0x9E3779B97F4A7C15ull ^ (u64)kn) * 0xBF58476D1CE4E5B9ull;\n";
+  for (int j = 0; j < nk; j++) o << "  h = (h ^ kv[" << j << "]) * 0x94D049BB133111EBull;\n";
+  o << "  return h ^ (h >> 32) ^ (h >> 47);\n}\n";
   auto same_keys = [&](const std::string& ks, const std::string& stride, const std::string& pos) {
     std::string r = "true";
     for (int j = 0; j < nk; j++)
