@@ -184,18 +184,17 @@ __global__ void k_string_op(StrArgs a) {
                 break;
               }
             }
+            // (an absorbing state keeps itself on every byte, so one check
+            // per word decides as early as a check per byte would)
             for (; !done && i + 4 <= len; i += 4) {
               const uint32_t w = *(const uint32_t*)(s + i);
               const int c0 = s_dfa[w & 0xFFu], c1 = s_dfa[(w >> 8) & 0xFFu], c2 = s_dfa[(w >> 16) & 0xFFu],
                         c3 = s_dfa[w >> 24];
               st = tr[st * nc + c0];
-              if (flags[st] & 2) { done = true; break; }
               st = tr[st * nc + c1];
-              if (flags[st] & 2) { done = true; break; }
               st = tr[st * nc + c2];
-              if (flags[st] & 2) { done = true; break; }
               st = tr[st * nc + c3];
-              if (flags[st] & 2) { done = true; break; }
+              done = (flags[st] & 2) != 0;
             }
             for (; !done && i < len; i++) {
               st = tr[st * nc + s_dfa[s[i]]];
