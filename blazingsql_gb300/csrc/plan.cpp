@@ -2551,19 +2551,34 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
     }
     o << in2 << "  pr_.step(s_);\n";
     o << in2 << "}\n";
+    // With one warp per block the table is the warp's own, and the leaders
+    // of one round hold distinct slots: plain read-modify-writes replace the
+    // shared-memory atomics (a __syncwarp orders them before the next round).
+    const bool own = cfg.warps == 1;
+    auto plain = [&](int j, const std::string& slot, const std::string& x) {
+      if (ac[j].ty == "double")
+        return "{ double* q_ = (double*)&" + slot + "; *q_ = *q_ + " + x + "; }";
+      if (ac[j].ty == "long long")
+        return "{ long long* q_ = (long long*)&" + slot + "; *q_ = " + ac[j].comb + "(*q_, " + x + "); }";
+      return slot + " += (u64)(" + x + ");";
+    };
     o << in2 << "if (sm_ && pr_.rank == 0) {\n";
-    o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
+    if (own) o << in2 << "  s_rows_[sl_] += (u64)__popc(peers_);\n";
+    else o << in2 << "  atomicAdd((unsigned long long*)&s_rows_[sl_], (unsigned long long)__popc(peers_));\n";
     for (int j = 0; j < na; j++) {
+      const std::string cs = "s_cnt_[" + std::to_string(j) + " * GXA_S + sl_]";
+      const std::string as = "s_acc_[" + std::to_string(j) + " * GXA_S + sl_]";
+      const std::string xj = "x" + std::to_string(j) + "_";
       o << in2 << "  if (c" << j << "_ != 0ull) {\n";
-      if (!((rows_cnt >> j) & 1ull))
-        o << in2 << "    atomicAdd((unsigned long long*)&s_cnt_[" << j << " * GXA_S + sl_], (unsigned long long)c" << j
-          << "_);\n";
-      if (!ac[j].ty.empty())
-        o << in2 << "    "
-          << atom(j, "&s_acc_[" + std::to_string(j) + " * GXA_S + sl_]", "x" + std::to_string(j) + "_") << "\n";
+      if (!((rows_cnt >> j) & 1ull)) {
+        if (own) o << in2 << "    " << cs << " += c" << j << "_;\n";
+        else o << in2 << "    atomicAdd((unsigned long long*)&" << cs << ", (unsigned long long)c" << j << "_);\n";
+      }
+      if (!ac[j].ty.empty()) o << in2 << "    " << (own ? plain(j, as, xj) : atom(j, "&" + as, xj)) << "\n";
       o << in2 << "  }\n";
     }
     o << in2 << "}\n";
+    if (own) o << in2 << "__syncwarp();\n";
   }
   // rows whose group found no room in the block's table go to the global one
   o << in2 << "if (act && sl_ == -1) {\n";
