@@ -202,6 +202,62 @@ GXE_FN gxe_u64 gxe_div_r(gxe_u64 a, gxe_u64 b, gxe_u64 r) {
   return gxe_div_finish(sign, ea - eb, fa | GXE_HIDDEN, (b & GXE_FRAC) | GXE_HIDDEN, r);
 }
 
+// x / b for a constant b (normal, finite) on the FMA unit, with y = RN(1/b)
+// and bd = b: Markstein's correction step (Muller et al., "Handbook of
+// Floating-Point Arithmetic", the theorem on the final correction of a
+// quotient): q = RN(x * y) is within an ulp of x / b, so r = x - q * b is
+// exact (one FMA), and RN(q + r * y) (one FMA) is the correctly rounded
+// quotient, provided nothing underflows or overflows.  So the step is taken
+// for x whose exponent field lies in [lo, hi] (chosen with b's exponent so
+// that x, the quotient and r stay normal); a zero gives the signed zero;
+// every other x (tiny, huge, subnormal, infinite, NaN) goes to gxe_div_r
+// with rr = gxe_recip_fixed(b's significand).  Same bits as gxe_div(x, b).
+GXE_FN double gxe_fma_(double a, double b, double c) {
+#if GXE_ON_DEVICE
+  return __fma_rn(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
+}
+GXE_FN double gxe_mul_rn_(double a, double b) {
+#if GXE_ON_DEVICE
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+GXE_FN gxe_u64 gxe_div_c(gxe_u64 a, gxe_u64 b, gxe_u64 rr, gxe_u64 ybits, int lo, int hi) {
+  if ((a & ~GXE_SIGN) == 0) return (a ^ b) & GXE_SIGN;
+  const int ea = (int)((a >> 52) & 0x7FF);
+  if (ea < lo || ea > hi) return gxe_div_r(a, b, rr);
+  double x, bd, y;
+#if GXE_ON_DEVICE
+  x = __longlong_as_double((long long)a);
+  bd = __longlong_as_double((long long)b);
+  y = __longlong_as_double((long long)ybits);
+#else
+  std::memcpy(&x, &a, 8);
+  std::memcpy(&bd, &b, 8);
+  std::memcpy(&y, &ybits, 8);
+#endif
+  const double q = gxe_mul_rn_(x, y);
+  const double r = gxe_fma_(-q, bd, x);
+  const double z = gxe_fma_(r, y, q);
+  gxe_u64 zb;
+#if GXE_ON_DEVICE
+  zb = (gxe_u64)__double_as_longlong(z);
+#else
+  std::memcpy(&zb, &z, 8);
+#endif
+  return zb;
+}
+// the exponent-field window of gxe_div_c for a divisor whose exponent field is eb
+GXE_FN void gxe_div_c_window(int eb, int* lo, int* hi) {
+  // x, x / b and the remainder (about 2^-106 |x|) all normal and far from overflow
+  *lo = 300 + (eb > 1023 ? eb - 1023 : 0);
+  *hi = 1700 + (eb < 1023 ? eb - 1023 : 0);
+}
+
 // x + y, correctly rounded, as bits (guard / round / sticky alignment).
 GXE_FN gxe_u64 gxe_add(gxe_u64 a, gxe_u64 b) {
   int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);

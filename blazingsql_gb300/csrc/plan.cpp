@@ -484,7 +484,20 @@ class Gen {
             : emu_op(kNativeMul) ? "gxe_mul(" + asDB(x) + ", " + asDB(y) + ")" : "gx_B(" + asD(x) + " * " + asD(y) + ")";
         break;
       case OP_DIV:
-        if (anyf && emu_op(kNativeDiv) && const_divisor(y)) {
+        if (anyf && emu_op(kNativeDiv) && const_divisor(y) && !emu_op(kNativeConstDiv)) {
+          // the FMA unit's correctly rounded constant division, the integer
+          // pipes' form outside its exponent window
+          const uint64_t db = literal_double_bits(y);
+          double bd, yd;
+          std::memcpy(&bd, &db, 8);
+          yd = 1.0 / bd;
+          uint64_t yb;
+          std::memcpy(&yb, &yd, 8);
+          int lo = 0, hi = 0;
+          gxe_div_c_window((int)((db >> 52) & 0x7FF), &lo, &hi);
+          r = "gxe_div_c(" + asDB(x) + ", " + hex64(db) + ", " + hex64(gxe_recip_fixed((db & GXE_FRAC) | GXE_HIDDEN)) +
+              ", " + hex64(yb) + ", " + std::to_string(lo) + ", " + std::to_string(hi) + ")";
+        } else if (anyf && emu_op(kNativeDiv) && const_divisor(y)) {
           // constant divisor: its fixed-point reciprocal is computed here
           const uint64_t db = literal_double_bits(y);
           r = "gxe_div_r(" + asDB(x) + ", " + hex64(db) + ", " +
@@ -2119,8 +2132,10 @@ std::vector<int> conjunct_columns(const Plan& p, int c) {
 // integer pipes.  Integer-to-double conversions go there too.  Compares go
 // there only when the plan has no transcendental (LN / EXP / trigonometric /
 // POWER / ROUND, which already load the FP64 pipe): with one they cost more
-// time there than they free.  Division stays emulated: natively it is a
-// reciprocal and Newton steps, several FP64-pipe instructions.  Measured on
+// time there than they free.  So does division by a literal (a multiply and
+// two FMAs instead of about 100 integer instructions).  Other division stays
+// emulated: natively it is a reciprocal and Newton steps, several FP64-pipe
+// instructions.  Measured on
 // GB300 against all-emulated: 25 % on the deep plan (with LN / EXP; the
 // conversions are 6.5 % of it), 10 % on the plain filter + divide.
 int auto_native_f64_ops(const Plan& p) {
@@ -2134,7 +2149,7 @@ int auto_native_f64_ops(const Plan& p) {
         default: break;
       }
   return transcendental ? (kNativeAddSub | kNativeMul | kNativeConvert)
-                        : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare);
+                        : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare | kNativeConstDiv);
 }
 
 std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg_in, const std::string& name) {

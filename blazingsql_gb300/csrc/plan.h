@@ -46,7 +46,7 @@ struct OutSpec {
 };
 
 constexpr int kNativeAddSub = 1, kNativeMul = 2, kNativeConvert = 4, kNativeCompare = 8, kNativeRound = 16,
-              kNativeDiv = 32;
+              kNativeDiv = 32, kNativeConstDiv = 64;
 
 struct KernelConfig {
   int warps = 8;           // warps per CTA
@@ -54,6 +54,7 @@ struct KernelConfig {
   bool emulate_fp64 = true;  // binary64 compares / divides / conversions on the integer pipes
   // with emulate_fp64, operation classes that still use the FP64 pipe (both
   // forms are exact IEEE binary64): kNativeAddSub, kNativeMul, kNativeConvert,
+  // kNativeConstDiv (division by a literal: two FMAs and a multiply),
   // kNativeCompare, kNativeRound, kNativeDiv; -1: chosen per plan
   int native_f64_ops = -1;
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows

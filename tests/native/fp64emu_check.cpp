@@ -64,6 +64,14 @@ int main(int argc, char** argv) {
     if (eb >= 1 && eb <= 2046) {
       const uint64_t r = gxe_recip_fixed((bits(b) & GXE_FRAC) | GXE_HIDDEN);
       const uint64_t q2 = gxe_div_r(bits(a), bits(b), r);
+      // the FMA-unit form (Markstein's correction step inside its window)
+      int lo = 0, hi = 0;
+      gxe_div_c_window(eb, &lo, &hi);
+      const uint64_t q3 = gxe_div_c(bits(a), bits(b), r, bits(1.0 / b), lo, hi);
+      if (!same(q3, a / b)) {
+        if (bad++ < 10) printf("div_c %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q3,
+                               (unsigned long long)bits(a / b));
+      }
       if (!same(q2, a / b)) {
         if (bad++ < 10) printf("div_r %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q2,
                                (unsigned long long)bits(a / b));
@@ -100,6 +108,35 @@ int main(int argc, char** argv) {
     }
     if (gxe_d2ll(bits(a)) != ref_d2ll(a)) {
       if (bad++ < 10) printf("d2ll %.17g\n", a);
+    }
+  }
+  // the FMA-unit constant division against literal divisors of the kind plans
+  // use, with dividends spread over the whole exponent window and its edges
+  {
+    static const double D[] = {100.0, 10.0, 1000.0, 3.0, 7.0, 0.1, 1e-3, 1.5, 86400.0, 1e9, 1e-300, 1e300,
+                               0.3333333333333333, 1.0000000000000002, 1.9999999999999998, 255.0, -100.0, 6.0};
+    for (double b : D) {
+      const uint64_t bb = bits(b);
+      const int eb = (int)((bb >> 52) & 0x7FF);
+      const uint64_t r = gxe_recip_fixed((bb & GXE_FRAC) | GXE_HIDDEN);
+      const uint64_t y = bits(1.0 / b);
+      int lo = 0, hi = 0;
+      gxe_div_c_window(eb, &lo, &hi);
+      for (long long i = 0; i < cases; i++) {
+        uint64_t ab;
+        switch (g.u64() % 4) {
+          case 0: ab = bits(g.any()); break;
+          case 1: ab = (g.u64() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(lo + (int)(g.u64() % (hi - lo + 1))) << 52); break;
+          case 2: ab = (g.u64() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 + (int)(g.u64() % 80) - 40) << 52); break;
+          default: ab = bits((double)(int64_t)(g.u64() >> (g.u64() % 64)) / (double)(1 + g.u64() % 1000)); break;
+        }
+        const double a = dbl(ab);
+        const uint64_t q = gxe_div_c(ab, bb, r, y, lo, hi);
+        if (!same(q, a / b)) {
+          if (bad++ < 10) printf("div_c %.17g / %.17g: got %016llx want %016llx\n", a, b, (unsigned long long)q,
+                                 (unsigned long long)bits(a / b));
+        }
+      }
     }
   }
   printf("cases=%lld mismatches=%lld\n", cases, bad);
