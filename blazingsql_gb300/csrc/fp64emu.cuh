@@ -384,6 +384,43 @@ GXE_FN gxe_u64 gxe_f2d(unsigned f) {
   return sign | ((gxe_u64)(ef - 127 + 1023) << 52) | ((gxe_u64)mf << 29);
 }
 
+// x / k for an integer divisor k: when 1 <= |k| <= n, Markstein's
+// correction step (as gxe_div_c) on the FMA unit with y = RN(1/|k|) read from
+// the table rcp (rcp[i] = RN(1 / (i + 1)) as bits) and the quotient's sign
+// flipped for a negative k (x / -k = -(x / k) exactly); a zero x gives the
+// signed zero.  Other k, and x outside the exponent window, take gxe_div.
+// Same bits as gxe_div(x, (double)k).
+GXE_FN gxe_u64 gxe_div_small(gxe_u64 a, gxe_i64 k, const gxe_u64* rcp, int n) {
+  const gxe_u64 ak = k < 0 ? 0ull - (gxe_u64)k : (gxe_u64)k;
+  const int ea = (int)((a >> 52) & 0x7FF);
+  const bool zero = (a & ~GXE_SIGN) == 0;
+  if (ak - 1ull >= (gxe_u64)n || (!zero && (ea < 310 || ea > 1700))) return gxe_div(a, gxe_i2d(k));
+  gxe_u64 q;
+  if (zero) {
+    q = a & GXE_SIGN;
+  } else {
+#if GXE_ON_DEVICE
+    const double y = __longlong_as_double((long long)__ldg(rcp + (ak - 1ull)));
+    const double x = __longlong_as_double((long long)a);
+    const double b = (double)(long long)ak;  // exact: |k| <= n
+#else
+    double y, x;
+    std::memcpy(&y, rcp + (ak - 1ull), 8);
+    std::memcpy(&x, &a, 8);
+    const double b = (double)(long long)ak;
+#endif
+    const double q0 = gxe_mul_rn_(x, y);
+    const double r = gxe_fma_(-q0, b, x);
+    const double z = gxe_fma_(r, y, q0);
+#if GXE_ON_DEVICE
+    q = (gxe_u64)__double_as_longlong(z);
+#else
+    std::memcpy(&q, &z, 8);
+#endif
+  }
+  return k < 0 ? q ^ GXE_SIGN : q;
+}
+
 GXE_FN bool gxe_isnan(gxe_u64 a) { return (a & ~GXE_SIGN) > GXE_INF; }
 
 // total order key for non-NaN values with -0 == +0

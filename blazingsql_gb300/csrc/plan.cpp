@@ -281,6 +281,39 @@ class Gen {
     const Node& n = p_.nodes[id];
     return kind_f(id) ? n.lit_bits : gxe_i2d((gxe_i64)n.lit_bits);
   }
+  // A divisor whose value is an integer (an integer-kind node, or its CAST
+  // to DOUBLE / FLOAT, which keeps the exact value inside a plan): the node
+  // holding that integer, or -1.  Divisions by it may take the reciprocal
+  // table (gxe_div_small) when the plan puts literal divisions on the FMA unit.
+  int int_divisor(int y) const {
+    const Node& n = p_.nodes[y];
+    if (n.kind == Node::LIT) return -1;
+    if (!kind_f(y)) return y;
+    if (n.kind == Node::OP && (n.op == OP_CAST_DOUBLE || n.op == OP_CAST_FLOAT) && !kind_f(n.a) &&
+        p_.nodes[n.a].kind != Node::LIT)
+      return n.a;
+    return -1;
+  }
+  bool small_div(int id) const {
+    const Node& n = p_.nodes[id];
+    return n.kind == Node::OP && n.op == OP_DIV && (kind_f(n.a) || kind_f(n.b)) && emu_op(kNativeDiv) &&
+           !emu_op(kNativeConstDiv) && !const_divisor(n.b) && int_divisor(n.b) >= 0;
+  }
+  // the reciprocal table gxe_div_small reads, when some division of the plan uses it
+  void emit_rcp_table(std::ostringstream& o) const {
+    bool any = false;
+    for (size_t i = 0; i < p_.nodes.size() && !any; i++) any = small_div((int)i);
+    if (!any) return;
+    o << "#define GX_RCP_N " << kRcpTable << "\n__device__ const unsigned long long gx_rcp_[GX_RCP_N] = {";
+    for (int k = 1; k <= kRcpTable; k++) {
+      const double y = 1.0 / (double)k;
+      uint64_t b;
+      std::memcpy(&b, &y, 8);
+      o << (k > 1 ? "," : "") << (k % 8 == 1 ? "\n  " : "") << hex64(b);
+    }
+    o << "};\n";
+  }
+  static constexpr int kRcpTable = 1024;
   // a literal divisor that is a normal finite nonzero double
   bool const_divisor(int id) const {
     const Node& n = p_.nodes[id];
@@ -497,6 +530,8 @@ class Gen {
           gxe_div_c_window((int)((db >> 52) & 0x7FF), &lo, &hi);
           r = "gxe_div_c(" + asDB(x) + ", " + hex64(db) + ", " + hex64(gxe_recip_fixed((db & GXE_FRAC) | GXE_HIDDEN)) +
               ", " + hex64(yb) + ", " + std::to_string(lo) + ", " + std::to_string(hi) + ")";
+        } else if (small_div(id)) {  // an integer divisor: RN(1/|k|) from the table for small |k|
+          r = "gxe_div_small(" + asDB(x) + ", (i64)(" + B(int_divisor(y)) + "), gx_rcp_, GX_RCP_N)";
         } else if (anyf && emu_op(kNativeDiv) && const_divisor(y)) {
           // constant divisor: its fixed-point reciprocal is computed here
           const uint64_t db = literal_double_bits(y);
@@ -2176,6 +2211,7 @@ std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& 
   }
   std::ostringstream o;
   emit_prelude(o, cfg);
+  g.emit_rcp_table(o);
   if (kind == KernelKind::FUSED_STAGED) {
     if (!p.has_filter() || p.conjuncts.size() > 16) fail(GX_ERR_INVALID, "the staged kernel runs filters of at most 16 conjuncts");
     KernelConfig c = cfg;

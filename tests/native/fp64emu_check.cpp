@@ -139,6 +139,27 @@ int main(int argc, char** argv) {
       }
     }
   }
+  // integer divisors through the reciprocal table (and past its end)
+  {
+    const int n = 256;
+    static gxe_u64 rcp[256];
+    for (int i = 0; i < n; i++) rcp[i] = bits(1.0 / (double)(i + 1));
+    for (long long i = 0; i < cases * 4; i++) {
+      const int64_t k = (int64_t)(g.u64() % 600) - 300;  // -300 .. 299, zero and beyond the table included
+      uint64_t ab;
+      switch (g.u64() % 3) {
+        case 0: ab = bits(g.any()); break;
+        case 1: ab = (g.u64() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(300 + (int)(g.u64() % 1420)) << 52); break;
+        default: ab = bits((double)(int64_t)(g.u64() >> (g.u64() % 64)) * (double)(1 + g.u64() % 1000)); break;
+      }
+      const double a = dbl(ab), b = (double)k;
+      const uint64_t q = gxe_div_small(ab, k, rcp, n);
+      if (!same(q, a / b)) {
+        if (bad++ < 10) printf("div_small %.17g / %lld: got %016llx want %016llx\n", a, (long long)k,
+                               (unsigned long long)q, (unsigned long long)bits(a / b));
+      }
+    }
+  }
   printf("cases=%lld mismatches=%lld\n", cases, bad);
   return bad ? 1 : 0;
 }
