@@ -297,7 +297,7 @@ class Gen {
   bool small_div(int id) const {
     const Node& n = p_.nodes[id];
     return n.kind == Node::OP && n.op == OP_DIV && (kind_f(n.a) || kind_f(n.b)) && emu_op(kNativeDiv) &&
-           !emu_op(kNativeConstDiv) && !const_divisor(n.b) && int_divisor(n.b) >= 0;
+           !emu_op(kNativeIntDiv) && !const_divisor(n.b) && int_divisor(n.b) >= 0;
   }
   // the reciprocal table gxe_div_small reads, when some division of the plan uses it
   void emit_rcp_table(std::ostringstream& o) const {
@@ -2184,7 +2184,8 @@ int auto_native_f64_ops(const Plan& p) {
         default: break;
       }
   return transcendental ? (kNativeAddSub | kNativeMul | kNativeConvert)
-                        : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare | kNativeConstDiv);
+                        : (kNativeAddSub | kNativeMul | kNativeConvert | kNativeCompare | kNativeConstDiv |
+                           kNativeIntDiv);
 }
 
 std::string generate_kernel(const Plan& p, KernelKind kind, const KernelConfig& cfg_in, const std::string& name) {
@@ -2382,6 +2383,7 @@ std::string generate_agg_kernel(const Plan& p, const AggLayout& L, const KernelC
   Gen g(p, cfg);
   std::ostringstream o;
   emit_prelude(o, cfg);
+  g.emit_rcp_table(o);
   const int nk = (int)L.key_nodes.size(), na = (int)L.kinds.size(), S = L.smem_slots;
   const uint64_t rows_cnt = agg_counts_are_rows(p, L);
   if (S < 16 || (S & (S - 1)) != 0) fail(GX_ERR_INVALID, "aggregation table slots must be a power of two >= 16");

@@ -46,7 +46,7 @@ struct OutSpec {
 };
 
 constexpr int kNativeAddSub = 1, kNativeMul = 2, kNativeConvert = 4, kNativeCompare = 8, kNativeRound = 16,
-              kNativeDiv = 32, kNativeConstDiv = 64;
+              kNativeDiv = 32, kNativeConstDiv = 64, kNativeIntDiv = 128;
 
 struct KernelConfig {
   int warps = 8;           // warps per CTA
@@ -55,6 +55,7 @@ struct KernelConfig {
   // with emulate_fp64, operation classes that still use the FP64 pipe (both
   // forms are exact IEEE binary64): kNativeAddSub, kNativeMul, kNativeConvert,
   // kNativeConstDiv (division by a literal: two FMAs and a multiply),
+  // kNativeIntDiv (division by an integer value: the same with a table reciprocal),
   // kNativeCompare, kNativeRound, kNativeDiv; -1: chosen per plan
   int native_f64_ops = -1;
   bool dense = true;         // filter kernels: projections on warp-compacted kept rows
