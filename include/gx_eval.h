@@ -179,7 +179,10 @@ void gx_plan_options_init(gx_plan_options* options);
 
 /* Compiles condition + expressions for a column schema.  Nullability is a
  * per-column hint (1 = may have nulls); a NULL null_mask at run time is always
- * accepted. */
+ * accepted.  Any number of columns and expressions: the plan runs as kernels
+ * of at most 32 outputs, each binding at most 64 of the columns (the ones its
+ * expressions read, over tables wider than that), as the reference splits its
+ * interpreter plans at 64 slots (LogicalProject.cpp:906-922). */
 gx_plan* gx_plan_compile(const int32_t* column_types, const uint8_t* column_nullable, int num_columns,
                          const char* condition, const char* const* expressions, int num_expressions,
                          const gx_plan_options* options, gx_status_info* status);
@@ -197,7 +200,8 @@ int gx_plan_num_conjuncts(const gx_plan* plan);
 int gx_plan_execute(const gx_plan* plan, const gx_column_view* columns, int num_columns,
                     gx_column* out, int64_t* out_rows, void* stream, gx_status_info* status);
 
-/* Runs a filter plan (condition required, at most 32 outputs) into the
+/* Runs a filter plan (condition required, at most 32 outputs over a table of
+ * at most 64 columns) into the
  * caller's buffers without allocating any device memory.  No counterpart in
  * the reference.
  *
@@ -350,7 +354,8 @@ int gx_skip_data_rewrite(const char* condition, const int* dropped_columns, int 
  * at a time. */
 typedef struct gx_batch_runner gx_batch_runner;
 
-/* plan: a compiled filter plan (condition + at most 32 outputs); a run takes at
+/* plan: a compiled filter plan (condition + at most 32 outputs, at most 64
+ * columns); a run takes at
  * most max_batches batches of max_total_rows rows in all. */
 gx_batch_runner* gx_batch_runner_create(const gx_plan* plan, int max_batches, int64_t max_total_rows, int autotune,
                                         gx_status_info* status);
@@ -385,7 +390,8 @@ void gx_batch_runner_destroy(gx_batch_runner* runner);
  * object.  No counterpart in the reference. */
 typedef struct gx_batch_stream gx_batch_stream;
 
-/* plan: a compiled filter plan (condition, at most 32 outputs, no literal
+/* plan: a compiled filter plan (condition, at most 32 outputs, at most 64
+ * columns, no literal
  * outputs); a session takes at most max_batches batches of max_total_rows rows
  * in all; block_threads / words_per_warp: the kernel's block shape (0: the
  * plan's). */
@@ -464,8 +470,8 @@ typedef struct gx_learned_batch_info {
 
 void gx_learner_options_init(gx_learner_options* options);
 
-/* Creates a learner for a plan made by gx_plan_compile (with a condition and at
- * most 32 outputs).  The plan may be destroyed afterwards. */
+/* Creates a learner for a plan made by gx_plan_compile (with a condition, at
+ * most 32 outputs and at most 64 columns).  The plan may be destroyed afterwards. */
 gx_learner* gx_learner_create(const gx_plan* plan, const gx_learner_options* options, gx_status_info* status);
 
 /* Filters one batch; same arguments and output contract as gx_plan_execute
