@@ -385,7 +385,7 @@ def single_config(name: str, rows: int, reps: int = 10):
         g.api.free_columns(out, stream)
         return r
 
-    for _ in range(4):  # warm-up: JIT and the plan's block-shape trials
+    for _ in range(6):  # warm-up: JIT and the plan's block-shape trials (a warm-up and four candidates)
         out_rows = step()
     torch.cuda.synchronize()
     L.gx_debug_kernel_ms(1)
@@ -439,7 +439,7 @@ def c5_batches(rows: int = 600_000_000, batch_rows: int = 1 << 22, reps: int = 3
     torch.cuda.synchronize()
     ms_runner = e0.elapsed_time(e1) / reps
     out_rows = sum(r)
-    for b in batches[:4]:  # warm the per-call path: its block-shape tuning compiles three candidates
+    for b in batches[:6]:  # warm the per-call path: its block-shape tuning tries four candidates
         o, _ = plan.execute(b, stream=stream)
         g.api.free_columns(o, stream)
     torch.cuda.synchronize()
@@ -846,7 +846,10 @@ def main():
     ap.add_argument("--agg-rows", type=int, default=1 << 27,
                     help="rows of the fused filter + aggregation measurement (0 skips it)")
     args = ap.parse_args()
-    args.warmup = max(3, args.warmup)
+    # at least 3 warm-up steps, and enough for the block-shape tuner of the
+    # library's single-pass filter to have measured its four candidates (its
+    # first large call is a warm-up, the next four try one candidate each)
+    args.warmup = max(3 if args.impl == "reference" else 6, args.warmup)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -432,18 +432,20 @@ static const char* kind_name(KernelKind k) {
   }
 }
 
-// Candidate block shapes (warps x words) of a tuned single-pass filter: the
-// first is used until the others have been measured.  Measured on GB300: the
-// deep C2 plan is fastest at 4 x 8, the light C1 / C5 plans at 1 x 16 (no
-// block barrier between warps, more blocks per SM) or 2 x 8.
-static const CompiledPlan::Shape kShapes[] = {{4, 8}, {1, 16}, {2, 8}};
-static constexpr int kNumShapes = 3;
+// Candidate block shapes (warps x words, register cap) of a tuned single-pass
+// filter: the first is used until the others have been measured.  Measured on
+// GB300: the deep C2 plan is fastest at 4 x 8, the order-line C5 plan at 1 x 16
+// (no block barrier between warps), the light C1 plan at 4 x 8 held to 40
+// registers (more resident warps for a latency-bound pass: 0.179 ms against
+// 0.191 at 1 x 16 and 0.220 at 4 x 8 uncapped, 2^24 rows).
+static const CompiledPlan::Shape kShapes[] = {{4, 8, 0}, {1, 16, 0}, {2, 8, 0}, {4, 8, 40}};
+static constexpr int kNumShapes = 4;
 
 // The first large call runs the first candidate unmeasured (it pays the
 // first touches of fresh output memory), the next ones measure each candidate.
 CompiledPlan::Shape CompiledPlan::filter_shape(int64_t n, int* explore) const {
   *explore = -1;
-  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words};
+  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words, 0};
   std::lock_guard<std::mutex> g(tmu_);
   if (chosen_ >= 0) return kShapes[chosen_];
   if (cand_ms_.empty()) cand_ms_.assign(kNumShapes, -1.f);
@@ -457,7 +459,7 @@ CompiledPlan::Shape CompiledPlan::filter_shape(int64_t n, int* explore) const {
 }
 
 CompiledPlan::Shape CompiledPlan::current_shape() const {
-  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words};
+  if (!cfg_.tune_shape) return {cfg_.warps, cfg_.words, 0};
   std::lock_guard<std::mutex> g(tmu_);
   return chosen_ >= 0 ? kShapes[chosen_] : kShapes[0];
 }
@@ -474,13 +476,15 @@ void CompiledPlan::shape_measured(int idx, float ms) const {
   chosen_ = best;
 }
 
-JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable, int warps, int words) const {
+JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullable, int warps, int words,
+                               int regs) const {
   if (warps <= 0) warps = cfg_.warps;
   if (words <= 0) words = cfg_.words;
+  if (regs <= 0) regs = cfg_.max_regs;
   int dev = 0;
   check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   std::string key = std::to_string((int)kind) + ":" + std::to_string(dev) + ":" + std::to_string(warps) + "x" +
-                    std::to_string(words) + "x" + std::to_string(cfg_.stages) + ":";
+                    std::to_string(words) + "x" + std::to_string(cfg_.stages) + "r" + std::to_string(regs) + ":";
   for (bool b : nullable) key += b ? '1' : '0';
   {
     std::lock_guard<std::mutex> g(kmu_);
@@ -492,6 +496,7 @@ JitKernel CompiledPlan::kernel(KernelKind kind, const std::vector<bool>& nullabl
   KernelConfig c = cfg_;
   c.warps = warps;
   c.words = words;
+  c.max_regs = regs;
   // the single pass in a conjunct order given at launch (learned ordering) is
   // named apart, so that profiles can tell it from the fixed-order pass
   const std::string name =
@@ -867,7 +872,7 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     a.capacity = capacity;
     KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : tma ? KernelKind::FUSED_TMA : KernelKind::FUSED_FILTER;
     if (!two_pass && cfg_.staged && cfg_.runtime_order && staging_aligned(plan_, cols)) kind = KernelKind::FUSED_STAGED;
-    const JitKernel k = two_pass ? kernel(kind, nb) : kernel(kind, nb, sh.warps, sh.words);
+    const JitKernel k = two_pass ? kernel(kind, nb) : kernel(kind, nb, sh.warps, sh.words, sh.regs);
     int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
     if (grid > ntiles) grid = ntiles;
     last.grid = (int)grid;
@@ -1157,7 +1162,7 @@ void CompiledPlan::execute_host(const std::vector<ColumnView>& hcols, gx_column*
     }
     std::vector<bool> nb(hcols.size());
     for (size_t i = 0; i < hcols.size(); i++) nb[i] = hcols[i].mask != nullptr;
-    const JitKernel kern = kernel(KernelKind::FUSED_FILTER, nb, sh.warps, sh.words);
+    const JitKernel kern = kernel(KernelKind::FUSED_FILTER, nb, sh.warps, sh.words, sh.regs);
     for (int k = 0; k < nchunks; k++) {
       const int64_t r1 = std::min<int64_t>(n, (k + 1) * chunk_rows);
       check_cuda(cudaStreamWaitEvent(s, R.ev[2 * k], 0), "event wait");

@@ -90,6 +90,7 @@ class CompiledPlan {
  public:
   struct Shape {
     int warps, words;  // block shape of a filter kernel: warps x 32-row words per warp
+    int regs = 0;      // registers per thread the kernel is held to (0: the configured cap, if any)
   };
   // the single-pass filter's block shape now: the tuned one once chosen
   Shape current_shape() const;
@@ -142,8 +143,9 @@ class CompiledPlan {
   mutable ExecStats last;
 
  private:
-  // warps / words: a block shape other than the configured one (0: configured)
-  JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable, int warps = 0, int words = 0) const;
+  // warps / words / regs: a block shape and register cap other than the configured ones (0: configured)
+  JitKernel kernel(KernelKind kind, const std::vector<bool>& nullable, int warps = 0, int words = 0,
+                   int regs = 0) const;
   // Block shape of a single-pass filter call over n rows.  With tune_shape,
   // calls of at least kShapeTuneRows rows first run the first candidate once
   // unmeasured (a warm-up), then each candidate once (*explore = its index;
