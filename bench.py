@@ -486,7 +486,7 @@ def aggregate_compare(rows: int, seed: int = 5, reps: int = 5):
     torch.cuda.synchronize()
 
     def timed(fn):
-        for _ in range(4):  # warm-up: JIT and the plan's block-shape trials
+        for _ in range(6):  # warm-up: JIT and the plan's block-shape trials (a warm-up and four candidates)
             fn()
         torch.cuda.synchronize()
         L.gx_debug_kernel_ms(1)
@@ -636,7 +636,7 @@ def strings_compare(rows: int, seed: int = 6, reps: int = 5):
     def fp():
         return g.filter_project(cols, STRING_CONDITION, STRING_PROJECTIONS, stream=stream)
 
-    for _ in range(4):
+    for _ in range(6):  # warm-up: JIT and the plan's block-shape trials (a warm-up and four candidates)
         g.api.free_columns(fp(), stream)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

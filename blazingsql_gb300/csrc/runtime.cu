@@ -451,7 +451,10 @@ CompiledPlan::Shape CompiledPlan::filter_shape(int64_t n, int* explore) const {
   if (cand_ms_.empty()) cand_ms_.assign(kNumShapes, -1.f);
   if (n >= kShapeTuneRows && next_cand_ <= kNumShapes) {
     const int k = next_cand_++;
-    if (k == 0) return kShapes[0];  // warm-up
+    if (k == 0) {  // warm-up; every candidate is compiled now, so no trial pays a compile
+      tune_compile_ = true;
+      return kShapes[0];
+    }
     *explore = k - 1;
     return kShapes[*explore];
   }
@@ -872,6 +875,8 @@ void CompiledPlan::run_filter(const std::vector<ColumnView>& cols, gx_column* ou
     a.capacity = capacity;
     KernelKind kind = two_pass ? KernelKind::WRITE_FILTER : tma ? KernelKind::FUSED_TMA : KernelKind::FUSED_FILTER;
     if (!two_pass && cfg_.staged && cfg_.runtime_order && staging_aligned(plan_, cols)) kind = KernelKind::FUSED_STAGED;
+    if (kind == KernelKind::FUSED_FILTER && tune_compile_.exchange(false))
+      for (const Shape& c : kShapes) kernel(kind, nb, c.warps, c.words, c.regs);
     const JitKernel k = two_pass ? kernel(kind, nb) : kernel(kind, nb, sh.warps, sh.words, sh.regs);
     int64_t grid = (int64_t)device_sm_count() * k.max_blocks_per_sm;
     if (grid > ntiles) grid = ntiles;

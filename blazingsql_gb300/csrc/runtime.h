@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -158,6 +159,7 @@ class CompiledPlan {
   mutable std::vector<float> cand_ms_;  // per candidate, < 0 until measured
   mutable int next_cand_ = 0;
   mutable int chosen_ = -1;
+  mutable std::atomic<bool> tune_compile_{false};  // compile every candidate on the next call
   void run_project(const std::vector<ColumnView>& cols, gx_column* out, bool caller_bufs, cudaStream_t s) const;
   void run_filter(const std::vector<ColumnView>& cols, gx_column* out, int64_t* out_rows, bool caller_bufs,
                   const ExecExtras* extras,
