@@ -61,7 +61,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     nvcc = _nvcc()
     root = _cuda_root(nvcc)
     _embed_prelude()
-    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "gx_eval.h"))
     headers.append(os.path.join(BUILD, "device_rt.inc"))
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", *ARCH, "-I", CSRC, "-I", BUILD,
