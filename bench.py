@@ -836,7 +836,7 @@ def main():
     ap.add_argument("--c1-rows", type=int, default=1 << 24, help="C1 rows (0 skips the C1 key)")
     ap.add_argument("--c5-rows", type=int, default=600_000_000, help="C5 rows (0 skips the C5 key)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--mode", type=int, default=-1, help="filter mode override (0 auto, 1 two-pass, 2 single)")
     ap.add_argument("--learned-batches", type=int, default=64, help="C4 batches (0 skips the learned comparison)")
     ap.add_argument("--learned-rows", type=int, default=1 << 22, help="C4 rows per batch")
