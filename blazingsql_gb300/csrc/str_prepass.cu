@@ -694,6 +694,17 @@ __device__ __forceinline__ int64_t row_position(const void* p, const uint32_t* m
   }
 }
 
+// the first lim bytes at p are all ASCII (read a 4-byte word at a time where
+// aligned, so the loads do not wait on one another)
+__device__ __forceinline__ bool ascii_prefix(const unsigned char* p, int lim) {
+  uint32_t acc = 0;
+  int i = 0;
+  for (; i < lim && ((uintptr_t)(p + i) & 3u); i++) acc |= p[i];
+  for (; i + 4 <= lim; i += 4) acc |= *(const uint32_t*)(p + i);
+  for (; i < lim; i++) acc |= p[i];
+  return (acc & 0x80808080u) == 0;
+}
+
 __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char*& p1, int& n1,
                               const unsigned char*& p2, bool& valid) {
   const unsigned char* p;
@@ -735,8 +746,18 @@ __device__ int xform_segments(const XformArgs& a, int64_t o, const unsigned char
     return n1;
   }
   if (a.kind == StringOp::SLICE && a.i0v && a.i1v && a.i0 >= 0 && a.i1 >= 0) {
-    // [i0, i1) from the front (SUBSTRING with a length, LEFT): walk at most i1
-    // characters; the same clipping as below, without counting the rest
+    // [i0, i1) from the front (SUBSTRING with a length, LEFT).  When the
+    // first min(n, i1) bytes are ASCII, characters are bytes: the slice is
+    // [i0, min(n, i1)), found without a dependent walk
+    const int lim = min(n, a.i1);
+    if (ascii_prefix(p, lim)) {
+      if (a.i0 >= lim) return 0;
+      p1 = p + a.i0;
+      n1 = lim - a.i0;
+      return n1;
+    }
+    // otherwise walk at most i1 characters; the same clipping as below,
+    // without counting the rest
     int i = 0, c = 0, bb = 0;
     while (i < n && c < a.i1) {
       if (c == a.i0) bb = i;
