@@ -131,7 +131,7 @@ struct StrArgs {
 __global__ void k_string_op(StrArgs a) {
   extern __shared__ unsigned char s_dfa[];
   if (a.dfa) {  // uniform over the block
-    const int bytes = 256 + a.dfa_states * (1 + a.dfa_classes);
+    const int bytes = a.dfa_classes ? 256 + a.dfa_states * (1 + a.dfa_classes) : a.dfa_states * 257;
     for (int i = threadIdx.x; i < bytes; i += blockDim.x) s_dfa[i] = a.dfa[i];
     __syncthreads();
   }
@@ -169,7 +169,24 @@ __global__ void k_string_op(StrArgs a) {
       } else {
         bool v = false;
         if (valid) {
-          if (a.op == StringOp::LIKE && a.dfa) {
+          if (a.op == StringOp::LIKE && a.dfa && a.dfa_classes == 0) {
+            // byte-indexed automaton: one shared-memory read per byte; bit 7
+            // of a state marks an absorbing one (the answer is decided)
+            const unsigned char* tr = s_dfa;
+            const unsigned char* flags = s_dfa + a.dfa_states * 256;
+            unsigned st = (unsigned)a.dfa_start | ((flags[a.dfa_start] & 2) ? 0x80u : 0u);
+            int i = 0;
+            for (; i < len && !(st & 0x80u) && ((uintptr_t)(s + i) & 3u); i++) st = tr[((st & 0x7Fu) << 8) | s[i]];
+            for (; !(st & 0x80u) && i + 4 <= len; i += 4) {
+              const uint32_t w = *(const uint32_t*)(s + i);
+              st = tr[((st & 0x7Fu) << 8) | (w & 0xFFu)];
+              st = tr[((st & 0x7Fu) << 8) | ((w >> 8) & 0xFFu)];
+              st = tr[((st & 0x7Fu) << 8) | ((w >> 16) & 0xFFu)];
+              st = tr[((st & 0x7Fu) << 8) | (w >> 24)];
+            }
+            for (; i < len && !(st & 0x80u); i++) st = tr[((st & 0x7Fu) << 8) | s[i]];
+            v = flags[st & 0x7Fu] & 1;
+          } else if (a.op == StringOp::LIKE && a.dfa) {
             // a table step per byte, the same instructions in every lane; the
             // row's aligned middle is read a 4-byte word at a time
             const unsigned char* flags = s_dfa + 256;
@@ -1479,8 +1496,13 @@ void launch_parse(const ColumnView& col, int type, const std::string& format, gx
 // False (the matcher is used) for a middle over 15 bytes or over 128 states.
 struct LikeDfa {
   int states = 0, classes = 0, start = 0;
-  std::string blob;  // [class of each byte 256 | flags per state | transitions states x classes]
+  // classes > 0: [class of each byte 256 | flags per state | transitions states x classes];
+  // direct (classes == 0, at most kDirectStates states): [transitions states x 256
+  // bytes, each the next state with bit 7 set when that state is absorbing |
+  // flags per state] -- one table read per byte, no class lookup
+  std::string blob;
 };
+constexpr int kDirectStates = 64;
 
 static int host_utf8_len(unsigned char c) {
   return c < 0x80 ? 1 : (c >> 5) == 0x6 ? 2 : (c >> 4) == 0xE ? 3 : (c >> 3) == 0x1E ? 4 : 1;
@@ -1570,6 +1592,19 @@ static bool build_like_dfa(const std::string& pat, LikeDfa& d) {
   }
   for (int b = 0; b < 256; b++)
     for (int i = 0; i < d.states; i++) d.blob[256 + d.states + i * d.classes + cls[b]] = (char)tr[i][b];
+  if (d.states <= kDirectStates) {  // byte-indexed form
+    std::string direct((size_t)d.states * 256 + d.states, '\0');
+    for (int i = 0; i < d.states; i++) {
+      for (int b = 0; b < 256; b++) {
+        const int nx = tr[i][b];
+        const bool absorbing = (d.blob[256 + nx] & 2) != 0;
+        direct[(size_t)i * 256 + b] = (char)(nx | (absorbing ? 0x80 : 0));
+      }
+      direct[(size_t)d.states * 256 + i] = d.blob[256 + i];
+    }
+    d.blob = direct;
+    d.classes = 0;
+  }
   return true;
 }
 
@@ -1577,6 +1612,13 @@ int like_dfa_host_match(const std::string& pattern, const unsigned char* text, i
   LikeDfa d;
   if (!build_like_dfa(pattern, d)) return -1;
   // the same walk as k_string_op's
+  if (d.classes == 0) {  // byte-indexed
+    const unsigned char* tr = (const unsigned char*)d.blob.data();
+    const unsigned char* flags = tr + (size_t)d.states * 256;
+    unsigned st = (unsigned)d.start | ((flags[d.start] & 2) ? 0x80u : 0u);
+    for (int64_t i = 0; i < n && !(st & 0x80u); i++) st = tr[((st & 0x7Fu) << 8) | text[i]];
+    return flags[st & 0x7Fu] & 1;
+  }
   const unsigned char* cls = (const unsigned char*)d.blob.data();
   const unsigned char* flags = cls + 256;
   const unsigned char* tr = flags + d.states;
