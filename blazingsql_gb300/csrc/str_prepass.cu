@@ -1043,6 +1043,7 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_sizes(XformArgs a) {
 template <bool kRegex>
 __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
   __shared__ uint64_t s_sum[kBuildWarps];
+  __shared__ __align__(16) unsigned char s_stage[kBuildWarps][kStageBytes + 8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w0 = ((int64_t)blockIdx.x * kBuildWarps + warp) * kBuildWords;
   uint64_t total = 0;
@@ -1082,9 +1083,13 @@ __global__ void __launch_bounds__(kBuildWarps * 32) k_xf_write(XformArgs a) {
     const int wtot = __shfl_sync(0xffffffffu, incl, 31);
     if (seg && wtot > 32 * kWarpCopyBytes) {  // long rows: the warp copies them together
       warp_copy(a.out_chars + pos, incl - len, n1, p1, p2, wtot, lane);
-    } else if (seg) {
-      for (int i = 0; i < n1; i++) a.out_chars[dst + i] = p1[i];
-      for (int i = n1; i < len; i++) a.out_chars[dst + i] = p2[i - n1];
+    } else if (seg) {  // short rows: staged by their lanes, written out by the warp
+      unsigned char* st = s_stage[warp] + (pos & 3u) + (incl - len);
+      for (int i = 0; i < n1; i++) st[i] = p1[i];
+      for (int i = n1; i < len; i++) st[i] = p2[i - n1];
+      __syncwarp();
+      stage_flush(a.out_chars, pos, s_stage[warp], wtot, lane);
+      __syncwarp();
     } else if (o < a.m && len > 0) {
       if constexpr (kRegex) regex_row(a, src, a.out_chars + dst, valid);
       else xform_row(a, src, a.out_chars + dst, valid);
