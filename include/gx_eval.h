@@ -73,7 +73,8 @@ typedef struct gx_column_view {
    * int32 offsets, row r spanning data[string_offsets[offset + r]] up to
    * data[string_offsets[offset + r + 1]]; NULL for every other type.  String
    * columns are read by the string pre-pass (LIKE, CHAR_LENGTH, comparisons,
-   * CASE with string results), passed through as outputs ($i) and compacted
+   * CASE with string results, the string functions and CASTs of
+   * evaluate_string_functions), passed through as outputs ($i) and compacted
    * by gx_process_filter / gx_filter_project. */
   const int32_t* string_offsets;
 } gx_column_view;
