@@ -5,8 +5,9 @@ Vectors come from the reference's gtest sources (see tests/golden/
 reference_vectors.json, produced by extract_reference_vectors.py, each entry
 citing file:lines).  Where a reference test hand-encodes an interpreter plan
 (interops_tests.cpp) the same plan is written as the RexNode expression it
-encodes.  String columns of the reference fixtures are replaced by an unused
-INT32 column (string operators are outside this evaluator).
+encodes.  In the numeric tables here, string columns of the reference fixtures
+are replaced by an unused INT32 column; the reference's string-table tests run
+in test_strings.py.
 """
 import json
 import os
