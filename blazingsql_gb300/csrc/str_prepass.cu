@@ -1670,6 +1670,13 @@ void launch_string_op(const ColumnView& col, const ColumnView* col2, const Strin
   add_launches(1);
 }
 
+// column c of cols, which a string operator reads as a string column
+static ColumnView string_column(const std::vector<ColumnView>& cols, int c) {
+  const ColumnView v = cols.at(c);
+  if (v.type != STRING) fail(GX_ERR_TYPE, "string operator over a non-string column");
+  return v;
+}
+
 bool is_deferrable(const StringOp& op) {
   switch (op.kind) {
     case StringOp::TO_STRING: case StringOp::SLICE: case StringOp::UPPER: case StringOp::LOWER:
@@ -1684,11 +1691,7 @@ bool is_deferrable(const StringOp& op) {
 gx_column transform_column(const StringOp& op, const std::vector<ColumnView>& cols, const int32_t* map,
                            int64_t rows, cudaStream_t s, const EvalText& eval_bool) {
   const int64_t n = cols.empty() ? 0 : cols[0].size;
-  auto string_col = [&](int c) {
-    const ColumnView v = cols.at(c);
-    if (v.type != STRING) fail(GX_ERR_TYPE, "string operator over a non-string column");
-    return v;
-  };
+  auto string_col = [&](int c) { return string_column(cols, c); };
   gx_column out{};
   if (op.kind == StringOp::TO_STRING) {
     gx_column tmp{};
@@ -1795,11 +1798,7 @@ std::vector<gx_column> run_string_prepass(std::vector<ColumnView>& cols, const s
     at += slot(b->size());
   }
   char* pdev = (char*)dev_alloc(host.size(), s);
-  auto string_col = [&](int c) {
-    const ColumnView v = cols.at(c);
-    if (v.type != STRING) fail(GX_ERR_TYPE, "string operator over a non-string column");
-    return v;
-  };
+  auto string_col = [&](int c) { return string_column(cols, c); };
   try {
     check_cuda(cudaMemcpyAsync(pdev, host.data(), host.size(), cudaMemcpyHostToDevice, s), "string patterns");
     for (size_t i = 0; i < ops.size(); i++) {
